@@ -1,0 +1,185 @@
+/*
+ * pymoto_gb300 -- C ABI of the GB300 (sm_103a) kernels for pyMOTO's structured-grid compliance path.
+ *
+ * Conventions
+ *  - Grids are given by their element counts (nelx, nely, nelz); nelz == 0 selects the 2D (Q4, 2 dofs
+ *    per node) path, nelz > 0 the 3D (hex8, 3 dofs per node) path.  Numbering is pyMOTO's:
+ *    element (i,j,k) -> (k*nely + j)*nelx + i, node (i,j,k) -> (k*(nely+1) + j)*(nelx+1) + i,
+ *    dof -> node*dim + d (pymoto/common/domain.py:200-251).
+ *  - All array arguments are DEVICE pointers unless the name ends in _host.  `dtype` selects the
+ *    storage type of the floating-point arrays: PMG_F64 or PMG_F32.  Reductions always accumulate in
+ *    FP64 and write FP64 results.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are asynchronous and stream-
+ *    ordered; none of them synchronises the device or allocates device memory.  Scratch buffers are
+ *    passed in by the caller and their minimum sizes are given by the *_scratch_bytes queries.
+ *  - Every call returns a pmg_status.  Invalid arguments are rejected before any launch.
+ *  - `bcmask` is one byte per node; bit d set means dof (node, d) is a Dirichlet dof whose row and column
+ *    are replaced by `bcdiag` on the diagonal (pymoto/modules/assembly.py:94-98, :210-230, :272).
+ *  - Element matrices `K0_host` are row-major (2^dim*dim)^2 FP64 arrays in pyMOTO's local dof order.
+ */
+#ifndef PYMOTO_GB300_H
+#define PYMOTO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PMG_OK = 0,
+  PMG_BAD_ARG = 1,
+  PMG_NOT_CONVERGED = 2,
+  PMG_TIMEOUT = 3,
+  PMG_CUDA_ERR = 4,
+  PMG_NOT_SPD = 5
+} pmg_status;
+
+enum { PMG_F64 = 0, PMG_F32 = 1 };
+
+/* Operator application modes for pmg_ebe_apply / pmg_stencil_apply. */
+enum {
+  PMG_APPLY_MATVEC = 0,   /* y = A u                                   */
+  PMG_APPLY_RESIDUAL = 1, /* y = b - A u                               */
+  PMG_APPLY_JACOBI = 2    /* y = u + omega * ((b - A u) / diag)        */
+};
+
+/* Library identification. */
+int pmg_version(void);
+const char* pmg_status_string(int status);
+/* Last CUDA error string seen by the library in this thread (for PMG_CUDA_ERR). */
+const char* pmg_last_error(void);
+
+/* Element stiffness matrix (2^dim*dim)^2, row-major, of pyMOTO's AssembleStiffness (2x2(x2) Gauss
+ * quadrature, replaces pymoto/modules/assembly.py:427-463).  dim 2 uses plane stress when
+ * plane_stress != 0, else plane strain (pyMOTO's default); unitz is the 2D thickness.  Host-only. */
+int pmg_element_stiffness(int dim, double E, double nu, int plane_stress, double unitx, double unity, double unitz,
+                          double* K0_host);
+
+/* ---- index maps ------------------------------------------------------------------------------
+ * Dof connectivity (nel, 2^dim*dim) int64, bit-exact with VoxelDomain.get_dofconnectivity
+ * (replaces pymoto/common/domain.py:338-362). */
+int pmg_dof_connectivity(int nelx, int nely, int nelz, int64_t* dofconn, void* stream);
+
+/* ---- matrix-free stiffness operator K(x) = sum_e x_e K0 (Dirichlet rows/cols -> bcdiag) --------
+ * Replaces AssembleGeneral.__call__ (pymoto/modules/assembly.py:245-296) followed by the CSR products
+ * of CG and GeometricMultigrid (pymoto/solvers/iterative.py:236-255, :375) and the damped-Jacobi
+ * smoother (pymoto/solvers/iterative.py:41-47).  u, b, diag, y: ndof; xe: nel. */
+int pmg_ebe_apply(int mode, int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
+                  const uint8_t* bcmask, double bcdiag, const void* u, const void* b, const void* diag,
+                  double omega, void* y, void* stream);
+/* diag(K(x)), replaces A.diagonal() of DampedJacobi.update (pymoto/solvers/iterative.py:38-39). */
+int pmg_ebe_diagonal(int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
+                     const uint8_t* bcmask, double bcdiag, void* diag, void* stream);
+
+/* ---- assembled node-stencil operator of the coarse multigrid levels ---------------------------
+ * S holds, per node, the (3^dim) x dim x dim coupling blocks in structure-of-arrays order
+ * S[(o*dim + d)*dim + c][node], o = (dz+1)*9 + (dy+1)*3 + (dx+1) (3D) or (dy+1)*3 + (dx+1) (2D).
+ * Replaces the CSR products with the Galerkin operators R^T A R (pymoto/solvers/iterative.py:173,
+ * :233-255). */
+int pmg_stencil_apply(int mode, int dtype, int nelx, int nely, int nelz, const void* S, const void* u,
+                      const void* b, const void* diag, double omega, void* y, void* stream);
+int pmg_stencil_diagonal(int dtype, int nelx, int nely, int nelz, const void* S, void* diag, void* stream);
+
+/* ---- grid transfers (trilinear / bilinear prolongation R of pymoto/solvers/iterative.py:178-220) --
+ * Grid arguments are the FINE grid.  rc = R^T rf (iterative.py:244);  uf += R uc (iterative.py:250). */
+int pmg_restrict(int dtype, int nelx, int nely, int nelz, const void* rf, void* rc, void* stream);
+int pmg_prolong_add(int dtype, int nelx, int nely, int nelz, const void* uc, void* uf, void* stream);
+
+/* ---- Galerkin coarse operators Ac = R^T A R (pymoto/solvers/iterative.py:173) -------------------
+ * Computed per coarse element: E_C = sum_children M_c^T E_child M_c.  The coarse element matrices are
+ * stored element-major, E[e][(2^dim*dim)^2].
+ * pmg_galerkin_table fills the 2^dim host matrices M_c^T K0 M_c (the unconstrained children).
+ * pmg_galerkin_from_ebe builds level-1 element matrices from the matrix-free fine operator; `table`
+ * is the device copy of pmg_galerkin_table's output in the same dtype.
+ * pmg_galerkin_from_elements builds the next level from element matrices (grid = the fine grid whose
+ * elements Ef belongs to). */
+int pmg_galerkin_table(int dim, const double* K0_host, double* table_host);
+int pmg_galerkin_from_ebe(int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
+                          const uint8_t* bcmask, double bcdiag, const void* table, void* Ec, void* stream);
+int pmg_galerkin_from_elements(int dtype, int nelx, int nely, int nelz, const void* Ef, void* Ec, void* stream);
+/* Node stencils of a grid from its element matrices (assembly of sum_e P_e^T E_e P_e). */
+int pmg_stencil_from_elements(int dtype, int nelx, int nely, int nelz, const void* E, void* S, void* stream);
+/* Dense FP64 matrix (ndof x ndof, row-major) of a stencil operator: the coarsest-level system. */
+int pmg_stencil_to_dense(int dtype, int nelx, int nely, int nelz, const void* S, double* A, void* stream);
+/* Half bandwidth of the dense coarsest matrix of a grid. */
+int pmg_stencil_bandwidth(int nelx, int nely, int nelz);
+
+/* ---- coarsest-level direct solve (replaces SolverSparseLU, pymoto/solvers/sparse.py:515-555, as
+ * chosen by auto_determine_solver, pymoto/solvers/auto_determine.py:109-122) -----------------------
+ * In-place FP64 Cholesky A = L L^T of a dense SPD matrix with half bandwidth `bw` (lower triangle
+ * used).  `info` (device int) is set to 0, or to k+1 if the k-th pivot is not positive (that pivot is
+ * replaced by 1 so the call always completes); the caller reads `info` once the stream has finished. */
+int pmg_cholesky_factor(int n, double* A, int bw, int* info, void* stream);
+/* x = (L L^T)^{-1} b.  L is FP64 or FP32 (dtype); b and x have the same dtype as L. */
+int pmg_cholesky_solve(int dtype, int n, const void* L, int bw, const void* b, void* x, void* stream);
+
+/* ---- reductions and vector updates of CG (pymoto/solvers/iterative.py:340-403) -----------------
+ * Deterministic single-launch reductions with FP64 accumulation (CTA partials summed in CTA order by the
+ * last CTA).  scratch >= pmg_reduce_scratch_bytes() bytes, zero-filled once before its first use; every
+ * call leaves it ready for the next one.  Calls sharing one scratch buffer must be stream-ordered. */
+size_t pmg_reduce_scratch_bytes(void);
+/* out[0] = a.b */
+int pmg_dot(int dtype, int64_t n, const void* a, const void* b, double* out, void* scratch, void* stream);
+/* out[0] = a.b, out[1] = c.d in one pass */
+int pmg_dot2(int dtype, int64_t n, const void* a, const void* b, const void* c, const void* d, double* out,
+             void* scratch, void* stream);
+/* alpha = num[0]/den[0];  x += alpha p;  r -= alpha q;  rr_out[0] = r.r   (FP64 CG step). */
+int pmg_cg_update(int dtype, int64_t n, void* x, void* r, const void* p, const void* q, const double* num,
+                  const double* den, double* rr_out, void* scratch, void* stream);
+/* alpha = num[0]/den[0]; x += alpha p only (the explicit-residual iterations). */
+int pmg_axpy_ratio(int dtype, int64_t n, void* x, const void* p, const double* num, const double* den,
+                   void* stream);
+/* beta = -num[0]/den[0];  p = z + beta p. */
+int pmg_xpby_ratio(int dtype, int64_t n, void* p, const void* z, const double* num, const double* den,
+                   void* stream);
+/* y = x * (1/sqrt(nrm2[0]))  (orth of a single vector, pymoto/solvers/iterative.py:259-292). */
+int pmg_scale_rsqrt(int dtype, int64_t n, void* y, const void* x, const double* nrm2, void* stream);
+/* y = a * x   (y, x of dtype), scalar a on the host. */
+int pmg_scale(int dtype, int64_t n, void* y, const void* x, double a, void* stream);
+/* y = x with the Dirichlet dofs zeroed (or only the Dirichlet dofs kept when keep_bc != 0). */
+int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int keep_bc, const void* x, void* y,
+                void* stream);
+/* Precision conversion y(dst_dtype) = x(src_dtype); and x64 += a * d32 (mixed-precision correction). */
+int pmg_convert(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, void* stream);
+int pmg_add_f32_to_f64(int64_t n, double* x, const float* d, double a, void* stream);
+/* y = w * (b / diag): the first damped-Jacobi sweep from a zero guess (pymoto/solvers/iterative.py:233-234). */
+int pmg_diag_scale(int dtype, int64_t n, const void* b, const void* diag, double w, void* y, void* stream);
+
+/* ---- density filters (pymoto/modules/filter.py) --------------------------------------------------
+ * DensityFilter (filter.py:223-378): y = H x / s, H_ij = max(0, r - |i-j|) over the window int(r).
+ * `transpose` != 0 computes H (x / s).  s (nel) is written by pmg_density_filter_rowsum. */
+int pmg_density_filter_rowsum(int nelx, int nely, int nelz, double radius, double* s, void* stream);
+int pmg_density_filter(int transpose, int nelx, int nely, int nelz, double radius, const double* s,
+                       const double* x, double* y, void* stream);
+/* FilterConv (filter.py:8-220) with per-axis padded index maps pad{x,y,z} (int32, length n+2p, device)
+ * and kernel weights w (kx*ky*kz, C order, device).  Forward: y = W * x_pad ('valid').  Transpose:
+ * full correlation accumulated through the pad maps. */
+int pmg_conv_filter(int transpose, int nelx, int nely, int nelz, const double* w, int kx, int ky, int kz,
+                    const int32_t* padx, const int32_t* pady, const int32_t* padz, const double* x, double* y,
+                    void* stream);
+
+/* ---- SIMP interpolation (MathExpression "xmin + (1-xmin) x^p", pymoto/modules/generic.py:94-140) -- */
+int pmg_simp(int64_t n, double xmin, double penal, const double* x, double* y, void* y32, void* stream);
+/* dx = dy * p (1-xmin) x^(p-1) */
+int pmg_simp_backward(int64_t n, double xmin, double penal, const double* x, const double* dy, double* dx,
+                      void* stream);
+
+/* ---- adjoint sensitivity contraction (pymoto/modules/assembly.py:298-315 with
+ * DyadicMatrix.contract, pymoto/common/dyadcarrier.py:366-414) ------------------------------------
+ * dx_e (+)= alpha * u_e^T K0 v_e with Dirichlet entries of u and v zeroed (dyadcarrier.py:179-189). */
+int pmg_sens_contract(int nelx, int nely, int nelz, const double* K0_host, const uint8_t* bcmask,
+                      const double* u, const double* v, double alpha, int accumulate, double* dx, void* stream);
+
+/* ---- optimality-criteria update (OC.step, pymoto/common/optimizers.py:402-437) -----------------
+ * Bisection on the Lagrange multiplier fully on the device; xnew is the design of the last bisection
+ * step.  scratch >= pmg_oc_scratch_bytes(). */
+size_t pmg_oc_scratch_bytes(void);
+int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, double volfrac, double move,
+                  double xmin, double xmax, double l1, double l2, double l1l2tol, void* scratch, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYMOTO_GB300_H */

@@ -1,0 +1,24 @@
+"""pymoto_gb300 -- pyMOTO's structured-grid topology-optimisation hot path on GB300 (sm_103a).
+
+Drop-in GPU Modules and LinearSolvers with pyMOTO's API:
+  DensityFilter, FilterConv, SIMP / MathExpression (SIMP form), AssembleStiffness, LinSolve, EinSum,
+  CG, GeometricMultigrid, DampedJacobi, DenseCholesky, MixedPrecisionCG, OC.
+The arithmetic runs in hand-written CUDA kernels of libpymoto_gb300.so through its C ABI
+(include/pymoto_gb300.h); there is no CPU fallback.
+"""
+from . import _lib
+from .core import HOST_RUNTIME, Module, Network, Signal
+from .domain import VoxelDomain
+from .modules import (AssembleStiffness, DensityFilter, DeviceDyad, EinSum, FilterConv, LinSolve, MathExpression,
+                      SIMP)
+from .operators import Grid, StencilOperator, StiffnessOperator, element_stiffness
+from .optimizers import OC
+from .solvers import (CG, DampedJacobi, DenseCholesky, GeometricMultigrid, LinearSolver, MixedPrecisionCG,
+                      Preconditioner)
+
+__version__ = "0.1.0"
+
+__all__ = ["AssembleStiffness", "DensityFilter", "DeviceDyad", "EinSum", "FilterConv", "LinSolve", "MathExpression",
+           "SIMP", "Grid", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "DampedJacobi",
+           "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
+           "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME"]

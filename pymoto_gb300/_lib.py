@@ -1,0 +1,146 @@
+"""ctypes binding of libpymoto_gb300.so (the C ABI of include/pymoto_gb300.h).
+
+There is no CPU fallback: if the library cannot be loaded, every operation raises.
+"""
+import ctypes
+import os
+import threading
+from ctypes import c_char_p, c_double, c_int, c_int64, c_size_t, c_void_p
+
+import numpy as np
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpymoto_gb300.so")
+
+P = c_void_p
+I = c_int
+D = c_double
+L = c_int64
+
+# name -> (restype, argtypes); mirrors include/pymoto_gb300.h
+SIGNATURES = {
+    "pmg_version": (I, []),
+    "pmg_status_string": (c_char_p, [I]),
+    "pmg_last_error": (c_char_p, []),
+    "pmg_element_stiffness": (I, [I, D, D, I, D, D, D, P]),
+    "pmg_dof_connectivity": (I, [I, I, I, P, P]),
+    "pmg_ebe_apply": (I, [I, I, I, I, I, P, P, P, D, P, P, P, D, P, P]),
+    "pmg_ebe_diagonal": (I, [I, I, I, I, P, P, P, D, P, P]),
+    "pmg_stencil_apply": (I, [I, I, I, I, I, P, P, P, P, D, P, P]),
+    "pmg_stencil_diagonal": (I, [I, I, I, I, P, P, P]),
+    "pmg_restrict": (I, [I, I, I, I, P, P, P]),
+    "pmg_prolong_add": (I, [I, I, I, I, P, P, P]),
+    "pmg_galerkin_table": (I, [I, P, P]),
+    "pmg_galerkin_from_ebe": (I, [I, I, I, I, P, P, P, D, P, P, P]),
+    "pmg_galerkin_from_elements": (I, [I, I, I, I, P, P, P]),
+    "pmg_stencil_from_elements": (I, [I, I, I, I, P, P, P]),
+    "pmg_stencil_to_dense": (I, [I, I, I, I, P, P, P]),
+    "pmg_stencil_bandwidth": (I, [I, I, I]),
+    "pmg_cholesky_factor": (I, [I, P, I, P, P]),
+    "pmg_cholesky_solve": (I, [I, I, P, I, P, P, P]),
+    "pmg_reduce_scratch_bytes": (c_size_t, []),
+    "pmg_dot": (I, [I, L, P, P, P, P, P]),
+    "pmg_dot2": (I, [I, L, P, P, P, P, P, P, P]),
+    "pmg_cg_update": (I, [I, L, P, P, P, P, P, P, P, P, P]),
+    "pmg_axpy_ratio": (I, [I, L, P, P, P, P, P]),
+    "pmg_xpby_ratio": (I, [I, L, P, P, P, P, P]),
+    "pmg_scale_rsqrt": (I, [I, L, P, P, P, P]),
+    "pmg_scale": (I, [I, L, P, P, D, P]),
+    "pmg_mask_bc": (I, [I, I, L, P, I, P, P, P]),
+    "pmg_convert": (I, [I, I, L, P, P, P]),
+    "pmg_add_f32_to_f64": (I, [L, P, P, D, P]),
+    "pmg_diag_scale": (I, [I, L, P, P, D, P, P]),
+    "pmg_density_filter_rowsum": (I, [I, I, I, D, P, P]),
+    "pmg_density_filter": (I, [I, I, I, I, D, P, P, P, P]),
+    "pmg_conv_filter": (I, [I, I, I, I, P, I, I, I, P, P, P, P, P, P]),
+    "pmg_simp": (I, [L, D, D, P, P, P, P]),
+    "pmg_simp_backward": (I, [L, D, D, P, P, P, P]),
+    "pmg_sens_contract": (I, [I, I, I, P, P, P, P, D, I, P, P]),
+    "pmg_oc_scratch_bytes": (c_size_t, []),
+    "pmg_oc_update": (I, [L, P, P, P, D, D, D, D, D, D, D, P, P]),
+}
+
+# Returns that are values, not statuses
+_VALUE_RETURNING = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_reduce_scratch_bytes",
+                    "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth"}
+
+F64, F32 = 0, 1
+MATVEC, RESIDUAL, JACOBI = 0, 1, 2
+
+
+class PMGError(RuntimeError):
+    """A pymoto_gb300 C-ABI call returned a non-zero status."""
+
+    def __init__(self, name, status, detail=""):
+        self.status = status
+        super().__init__(f"{name} failed with status {status}{': ' + detail if detail else ''}")
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load():
+    """Load the CUDA library, building it first when it is absent (nvcc required)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            from .build import build
+            build()
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def _arg(a):
+    if a is None:
+        return None
+    if isinstance(a, torch.Tensor):
+        return a.data_ptr()
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if isinstance(a, bool):
+        return int(a)
+    return a
+
+
+def call(name, *args):
+    """Call a C-ABI function; raise PMGError on a non-zero status."""
+    lib = load()
+    fn = getattr(lib, name)
+    rc = fn(*[_arg(a) for a in args])
+    if name in _VALUE_RETURNING:
+        return rc
+    if rc != 0:
+        msg = lib.pmg_status_string(rc).decode()
+        err = lib.pmg_last_error().decode()
+        raise PMGError(name, rc, msg + (f" ({err})" if err else ""))
+    return rc
+
+
+def stream():
+    """Handle of the current torch CUDA stream (all library calls are ordered on it)."""
+    return torch.cuda.current_stream().cuda_stream
+
+
+def dtype_code(t):
+    if t.dtype == torch.float64:
+        return F64
+    if t.dtype == torch.float32:
+        return F32
+    raise TypeError(f"unsupported dtype {t.dtype}")
+
+
+def require_cuda(t, name="tensor"):
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.is_contiguous()):
+        raise TypeError(f"{name} must be a contiguous CUDA tensor")
+    return t

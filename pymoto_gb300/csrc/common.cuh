@@ -1,0 +1,85 @@
+// Shared definitions of the pymoto_gb300 CUDA library (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstring>
+
+#include "../../include/pymoto_gb300.h"
+
+namespace pmg {
+
+// Structured voxel grid given by its element counts; nz == 0 is the 2D grid.
+struct Grid {
+  int nx, ny, nz;
+  __host__ __device__ int dim() const { return nz == 0 ? 2 : 3; }
+  __host__ __device__ int nnx() const { return nx + 1; }
+  __host__ __device__ int nny() const { return ny + 1; }
+  __host__ __device__ int nnz() const { return nz + 1; }
+  __host__ __device__ int ez() const { return nz == 0 ? 1 : nz; }  // element layers
+  __host__ __device__ int64_t nel() const { return (int64_t)nx * ny * ez(); }
+  __host__ __device__ int64_t nnodes() const { return (int64_t)(nx + 1) * (ny + 1) * (nz + 1); }
+  __host__ __device__ Grid coarse() const { return Grid{nx / 2, ny / 2, nz / 2}; }
+};
+
+template <int DIM>
+struct Traits {
+  static constexpr int NN = 1 << DIM;         // nodes per element
+  static constexpr int NDE = NN * DIM;        // dofs per element
+  static constexpr int NOFF = DIM == 3 ? 27 : 9;  // node-stencil offsets
+  static constexpr int NSB = NOFF * DIM * DIM;     // stencil values per node
+};
+
+// Element matrix passed by value in the kernel parameter space (constant bank): all threads of a warp
+// read the same entry at the same time, so the FMAs take it as a uniform operand.
+template <typename T, int NDE>
+struct ElemMat {
+  T v[NDE * NDE];
+};
+
+// Thread-local error of the last failing call.
+void set_error(const char* msg);
+const char* last_error();
+
+inline int check_launch() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(cudaGetErrorString(e));
+    return PMG_CUDA_ERR;
+  }
+  return PMG_OK;
+}
+
+inline bool grid_ok(int nx, int ny, int nz) {
+  return nx > 0 && ny > 0 && nz >= 0 && (int64_t)(nx + 1) * (ny + 1) * (nz + 1) < (int64_t(1) << 31);
+}
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+template <typename T, int NDE>
+inline ElemMat<T, NDE> make_elem_mat(const double* K0) {
+  ElemMat<T, NDE> m;
+  for (int i = 0; i < NDE * NDE; ++i) m.v[i] = (T)K0[i];
+  return m;
+}
+
+// Node coordinates from a linear node index.
+__device__ __forceinline__ void node_ijk(const Grid& g, int64_t n, int& i, int& j, int& k) {
+  const int nnx = g.nx + 1, nny = g.ny + 1;
+  i = (int)(n % nnx);
+  int64_t t = n / nnx;
+  j = (int)(t % nny);
+  k = (int)(t / nny);
+}
+
+__device__ __forceinline__ int64_t node_id(const Grid& g, int i, int j, int k) {
+  return ((int64_t)k * (g.ny + 1) + j) * (g.nx + 1) + i;
+}
+
+__device__ __forceinline__ int64_t elem_id(const Grid& g, int i, int j, int k) {
+  return ((int64_t)k * g.ny + j) * g.nx + i;
+}
+
+}  // namespace pmg

@@ -1,0 +1,365 @@
+// Design-variable kernels: density filters and their adjoints, SIMP, the adjoint sensitivity contraction
+// and the optimality-criteria update.  All FP64 (these streams are small next to the solve).
+#include "common.cuh"
+
+namespace pmg {
+
+// ------------------------------------------------------------------------------------------ DensityFilter
+// Cone weights max(0, r - |d|) over the window int(r) (element-index distances).
+__device__ __forceinline__ double cone(double r, int dx, int dy, int dz) {
+  const double d = sqrt((double)(dx * dx + dy * dy + dz * dz));
+  return r - d > 0.0 ? r - d : 0.0;
+}
+
+__device__ __forceinline__ void elem_ijk(const Grid& g, int64_t e, int& i, int& j, int& k) {
+  i = (int)(e % g.nx);
+  j = (int)((e / g.nx) % g.ny);
+  k = (int)(e / ((int64_t)g.nx * g.ny));
+}
+
+__global__ void density_rowsum_kernel(Grid g, double r, double* __restrict__ s) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.nel()) return;
+  int i, j, k;
+  elem_ijk(g, e, i, j, k);
+  const int d = (int)r;
+  const int dzr = g.nz == 0 ? 0 : d;
+  double acc = 0.0;
+  for (int dz = -dzr; dz <= dzr; ++dz) {
+    const int kk = k + dz;
+    if (kk < 0 || kk >= g.ez()) continue;
+    for (int dy = -d; dy <= d; ++dy) {
+      const int jj = j + dy;
+      if (jj < 0 || jj >= g.ny) continue;
+      for (int dx = -d; dx <= d; ++dx) {
+        const int ii = i + dx;
+        if (ii < 0 || ii >= g.nx) continue;
+        acc += cone(r, dx, dy, dz);
+      }
+    }
+  }
+  s[e] = acc;
+}
+
+// forward: y_i = sum_j H_ij x_j / s_i ;  transpose: y_j = sum_i H_ij (x_i / s_i)  (H symmetric)
+template <bool TRANSPOSE>
+__global__ void density_filter_kernel(Grid g, double r, const double* __restrict__ s, const double* __restrict__ x,
+                                      double* __restrict__ y) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.nel()) return;
+  int i, j, k;
+  elem_ijk(g, e, i, j, k);
+  const int d = (int)r;
+  const int dzr = g.nz == 0 ? 0 : d;
+  double acc = 0.0;
+  for (int dz = -dzr; dz <= dzr; ++dz) {
+    const int kk = k + dz;
+    if (kk < 0 || kk >= g.ez()) continue;
+    for (int dy = -d; dy <= d; ++dy) {
+      const int jj = j + dy;
+      if (jj < 0 || jj >= g.ny) continue;
+      for (int dx = -d; dx <= d; ++dx) {
+        const int ii = i + dx;
+        if (ii < 0 || ii >= g.nx) continue;
+        const int64_t m = elem_id(g, ii, jj, kk);
+        const double v = TRANSPOSE ? x[m] / s[m] : x[m];
+        acc = fma(cone(r, dx, dy, dz), v, acc);
+      }
+    }
+  }
+  y[e] = TRANSPOSE ? acc : acc / s[e];
+}
+
+// ------------------------------------------------------------------------------------------ FilterConv
+// Forward: y[o] = sum_m w[m] x[pad(o + (K-1) - m)]  (kernel flipped: 'valid' convolution).
+__global__ void conv_filter_kernel(Grid g, const double* __restrict__ w, int kx, int ky, int kz,
+                                   const int32_t* __restrict__ px, const int32_t* __restrict__ py,
+                                   const int32_t* __restrict__ pz, const double* __restrict__ x, double* __restrict__ y) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.nel()) return;
+  int i, j, k;
+  elem_ijk(g, e, i, j, k);
+  double acc = 0.0;
+  for (int c = 0; c < kz; ++c) {
+    const int kk = pz[k + (kz - 1) - c];
+    for (int b = 0; b < ky; ++b) {
+      const int jj = py[j + (ky - 1) - b];
+      const double* wr = w + ((int64_t)0 * ky + b) * kz + c;
+      for (int a = 0; a < kx; ++a) {
+        const int ii = px[i + (kx - 1) - a];
+        acc = fma(wr[(int64_t)a * ky * kz], x[elem_id(g, ii, jj, kk)], acc);
+      }
+    }
+  }
+  y[e] = acc;
+}
+
+// Transpose, gather form: dx[j] = sum over padded positions P with pad(P) = j of sum_m w[m] d[P - (K-1) + m]
+// (output o = P - (K-1) + m must lie inside the grid).  The padded positions of j along an axis are all
+// P in [0, n+K-1) with map[P] == j; they are found by scanning the (short) pad map.
+__global__ void conv_filter_T_kernel(Grid g, const double* __restrict__ w, int kx, int ky, int kz,
+                                     const int32_t* __restrict__ px, const int32_t* __restrict__ py,
+                                     const int32_t* __restrict__ pz, const double* __restrict__ d, double* __restrict__ y) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.nel()) return;
+  int i, j, k;
+  elem_ijk(g, e, i, j, k);
+  const int ez = g.ez();
+  const int lx = g.nx + kx - 1, ly = g.ny + ky - 1, lz = ez + kz - 1;
+  double acc = 0.0;
+  for (int Pz = 0; Pz < lz; ++Pz) {
+    if (pz[Pz] != k) continue;
+    for (int Py = 0; Py < ly; ++Py) {
+      if (py[Py] != j) continue;
+      for (int Px = 0; Px < lx; ++Px) {
+        if (px[Px] != i) continue;
+        // outputs o = P - (K-1) + m for taps m
+        for (int c = 0; c < kz; ++c) {
+          const int oz = Pz - (kz - 1) + c;
+          if (oz < 0 || oz >= ez) continue;
+          for (int b = 0; b < ky; ++b) {
+            const int oy = Py - (ky - 1) + b;
+            if (oy < 0 || oy >= g.ny) continue;
+            for (int a = 0; a < kx; ++a) {
+              const int ox = Px - (kx - 1) + a;
+              if (ox < 0 || ox >= g.nx) continue;
+              acc = fma(w[((int64_t)a * ky + b) * kz + c], d[elem_id(g, ox, oy, oz)], acc);
+            }
+          }
+        }
+      }
+    }
+  }
+  y[e] = acc;
+}
+
+// ------------------------------------------------------------------------------------------ SIMP
+__global__ void simp_kernel(int64_t n, double xmin, double p, const double* __restrict__ x, double* __restrict__ y,
+                            float* __restrict__ y32) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double xi = x[i];
+  const double xp = p == 3.0 ? xi * xi * xi : pow(xi, p);
+  const double v = xmin + (1.0 - xmin) * xp;
+  if (y) y[i] = v;
+  if (y32) y32[i] = (float)v;
+}
+
+__global__ void simp_backward_kernel(int64_t n, double xmin, double p, const double* __restrict__ x,
+                                     const double* __restrict__ dy, double* __restrict__ dx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double xi = x[i];
+  const double xp = p == 3.0 ? xi * xi : pow(xi, p - 1.0);
+  dx[i] = dy[i] * (p * (1.0 - xmin) * xp);
+}
+
+// ------------------------------------------------------------------------------------------ sensitivity
+// dx_e (+)= alpha * u_e^T K0 v_e with Dirichlet entries zeroed; one thread per element.
+template <int DIM>
+__global__ void sens_kernel(Grid g, ElemMat<double, Traits<DIM>::NDE> K0, const uint8_t* __restrict__ bcmask,
+                            const double* __restrict__ u, const double* __restrict__ v, double alpha, int accumulate,
+                            double* __restrict__ dx) {
+  constexpr int NN = Traits<DIM>::NN;
+  constexpr int NDE = Traits<DIM>::NDE;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.nel()) return;
+  int i, j, k;
+  elem_ijk(g, e, i, j, k);
+  double ue[NDE], ve[NDE];
+#pragma unroll
+  for (int a = 0; a < NN; ++a) {
+    const int64_t nd = node_id(g, i + (a & 1), j + ((a >> 1) & 1), k + ((a >> 2) & 1));
+    const uint8_t m = bcmask ? bcmask[nd] : 0;
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      const bool bc = (m >> c) & 1;
+      ue[a * DIM + c] = bc ? 0.0 : u[nd * DIM + c];
+      ve[a * DIM + c] = bc ? 0.0 : v[nd * DIM + c];
+    }
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int r = 0; r < NDE; ++r) {
+    double t = 0.0;
+#pragma unroll
+    for (int c = 0; c < NDE; ++c) t = fma(K0.v[r * NDE + c], ve[c], t);
+    s = fma(ue[r], t, s);
+  }
+  const double val = alpha * s;
+  dx[e] = accumulate ? dx[e] + val : val;
+}
+
+// ------------------------------------------------------------------------------------------ OC update
+// State in scratch: sum partials and the bisection interval, all on the device.
+constexpr int OC_THREADS = 256;
+constexpr int OC_MAX_BLOCKS = 1024;
+struct OCScratch {
+  double partial[OC_MAX_BLOCKS];
+  double l1, l2, lmid;
+  unsigned int ticket;
+};
+
+__device__ __forceinline__ double oc_warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ double oc_block_sum(double v) {
+  __shared__ double sh[OC_THREADS / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = oc_warp_sum(v);
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (wid == 0) {
+    t = lane < OC_THREADS / 32 ? sh[lane] : 0.0;
+    t = oc_warp_sum(t);
+  }
+  __syncthreads();
+  return t;
+}
+
+__global__ void oc_init_kernel(OCScratch* s, double l1, double l2) {
+  s->l1 = l1;
+  s->l2 = l2;
+  s->lmid = 0.5 * (l1 + l2);
+  s->ticket = 0u;
+}
+
+// One bisection step: xnew = clip(x sqrt(-dg/lmid), lb, ub); the last CTA compares the volume with the
+// target and moves l1 or l2, exactly as OC.step does.
+__global__ void __launch_bounds__(OC_THREADS) oc_step_kernel(int64_t n, const double* __restrict__ x,
+                                                             const double* __restrict__ dg, double* __restrict__ xnew,
+                                                             double target, double move, double xmin, double xmax,
+                                                             OCScratch* s) {
+  const double lmid = s->lmid;
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double xi = x[i];
+    const double g = dg[i] < 0.0 ? dg[i] : 0.0;
+    const double lb = fmax(xmin, xi - move), ub = fmin(xmax, xi + move);
+    double v = xi * sqrt(-g / lmid);
+    v = fmin(fmax(v, lb), ub);
+    xnew[i] = v;
+    acc += v;
+  }
+  acc = oc_block_sum(acc);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    s->partial[blockIdx.x] = acc;
+    __threadfence();
+    last = atomicAdd(&s->ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double t = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) t += ((volatile double*)s->partial)[b];
+  t = oc_block_sum(t);
+  if (threadIdx.x == 0) {
+    if (t - target > 0.0)
+      s->l1 = lmid;
+    else
+      s->l2 = lmid;
+    s->lmid = 0.5 * (s->l1 + s->l2);
+    s->ticket = 0u;
+  }
+}
+
+}  // namespace pmg
+
+using namespace pmg;
+
+extern "C" {
+
+int pmg_density_filter_rowsum(int nelx, int nely, int nelz, double radius, double* s, void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || !s || !(radius > 0.0)) return PMG_BAD_ARG;
+  Grid g{nelx, nely, nelz};
+  density_rowsum_kernel<<<blocks_for(g.nel(), 128), 128, 0, as_stream(stream)>>>(g, radius, s);
+  return check_launch();
+}
+
+int pmg_density_filter(int transpose, int nelx, int nely, int nelz, double radius, const double* s, const double* x,
+                       double* y, void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || !s || !x || !y || x == y || !(radius > 0.0)) return PMG_BAD_ARG;
+  Grid g{nelx, nely, nelz};
+  const unsigned b = blocks_for(g.nel(), 128);
+  if (transpose)
+    density_filter_kernel<true><<<b, 128, 0, as_stream(stream)>>>(g, radius, s, x, y);
+  else
+    density_filter_kernel<false><<<b, 128, 0, as_stream(stream)>>>(g, radius, s, x, y);
+  return check_launch();
+}
+
+int pmg_conv_filter(int transpose, int nelx, int nely, int nelz, const double* w, int kx, int ky, int kz,
+                    const int32_t* padx, const int32_t* pady, const int32_t* padz, const double* x, double* y,
+                    void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || !w || !padx || !pady || !padz || !x || !y || x == y) return PMG_BAD_ARG;
+  if (kx < 1 || ky < 1 || kz < 1 || !(kx & 1) || !(ky & 1) || !(kz & 1)) return PMG_BAD_ARG;
+  if (nelz == 0 && kz != 1) return PMG_BAD_ARG;
+  Grid g{nelx, nely, nelz};
+  const unsigned b = blocks_for(g.nel(), 128);
+  if (transpose)
+    conv_filter_T_kernel<<<b, 128, 0, as_stream(stream)>>>(g, w, kx, ky, kz, padx, pady, padz, x, y);
+  else
+    conv_filter_kernel<<<b, 128, 0, as_stream(stream)>>>(g, w, kx, ky, kz, padx, pady, padz, x, y);
+  return check_launch();
+}
+
+int pmg_simp(int64_t n, double xmin, double penal, const double* x, double* y, void* y32, void* stream) {
+  if (n < 0 || !x || (!y && !y32)) return PMG_BAD_ARG;
+  if (n == 0) return PMG_OK;
+  simp_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(n, xmin, penal, x, y, (float*)y32);
+  return check_launch();
+}
+
+int pmg_simp_backward(int64_t n, double xmin, double penal, const double* x, const double* dy, double* dx,
+                      void* stream) {
+  if (n < 0 || !x || !dy || !dx) return PMG_BAD_ARG;
+  if (n == 0) return PMG_OK;
+  simp_backward_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(n, xmin, penal, x, dy, dx);
+  return check_launch();
+}
+
+int pmg_sens_contract(int nelx, int nely, int nelz, const double* K0_host, const uint8_t* bcmask, const double* u,
+                      const double* v, double alpha, int accumulate, double* dx, void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || !K0_host || !u || !v || !dx) return PMG_BAD_ARG;
+  Grid g{nelx, nely, nelz};
+  const unsigned b = blocks_for(g.nel(), 128);
+  if (g.dim() == 3)
+    sens_kernel<3><<<b, 128, 0, as_stream(stream)>>>(g, make_elem_mat<double, 24>(K0_host), bcmask, u, v, alpha,
+                                                     accumulate, dx);
+  else
+    sens_kernel<2><<<b, 128, 0, as_stream(stream)>>>(g, make_elem_mat<double, 8>(K0_host), bcmask, u, v, alpha,
+                                                     accumulate, dx);
+  return check_launch();
+}
+
+size_t pmg_oc_scratch_bytes(void) { return sizeof(OCScratch); }
+
+int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, double volfrac, double move, double xmin,
+                  double xmax, double l1, double l2, double l1l2tol, void* scratch, void* stream) {
+  if (n <= 0 || !x || !dg || !xnew || !scratch || !(l1l2tol > 0.0) || !(l2 >= l1)) return PMG_BAD_ARG;
+  cudaStream_t st = as_stream(stream);
+  OCScratch* s = (OCScratch*)scratch;
+  int64_t nb = (n + OC_THREADS * 4 - 1) / (OC_THREADS * 4);
+  if (nb > OC_MAX_BLOCKS) nb = OC_MAX_BLOCKS;
+  if (nb < 1) nb = 1;
+  oc_init_kernel<<<1, 1, 0, st>>>(s, l1, l2);
+  // the interval halves every step, so the step count is known on the host: same loop as OC.step
+  double a = l1, b = l2;
+  const double target = volfrac * (double)n;
+  int steps = 0;
+  while (b - a > l1l2tol) {
+    oc_step_kernel<<<(unsigned)nb, OC_THREADS, 0, st>>>(n, x, dg, xnew, target, move, xmin, xmax, s);
+    const double mid = 0.5 * (a + b);
+    a = mid;  // only the interval width matters for the count
+    ++steps;
+    if (steps > 200) return PMG_BAD_ARG;
+  }
+  return check_launch();
+}
+
+}  // extern "C"

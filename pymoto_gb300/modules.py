@@ -1,0 +1,424 @@
+"""Drop-in GPU Modules of pyMOTO's compliance path.
+
+Each class keeps the constructor keywords and the response / sensitivity contract of its pyMOTO
+counterpart and runs on the device through libpymoto_gb300.  Signal states may be numpy arrays (the
+answer is then numpy, so the modules mix with pyMOTO's own modules and optimizers) or CUDA tensors
+(everything stays on the device).
+"""
+import copy
+import re
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import F64, RESIDUAL, call, stream
+from .core import Module
+from .domain import grid_of
+from .operators import Grid, StiffnessOperator, Workspace, bc_node_mask, element_stiffness
+from .solvers import _from_device, _to_device, default_solver
+
+
+def _kind_of(v):
+    if isinstance(v, torch.Tensor):
+        return "torch" if v.is_cuda else "torch-cpu"
+    return "numpy"
+
+
+# --------------------------------------------------------------------------------------------- filters
+class DensityFilter(Module):
+    """y = H x / s with H_ij = max(0, r - |c_i - c_j|) (pymoto/modules/filter.py:273-378, Filter :223-270)."""
+
+    def __init__(self, domain, radius=2.0, nonpadding=None):
+        if nonpadding is not None:
+            raise NotImplementedError("DensityFilter(nonpadding=...) is not supported on the GPU path")
+        self.domain = domain
+        self.grid = Grid(*grid_of(domain))
+        self.radius = float(radius)
+        self._s = None
+
+    def _rowsum(self, device):
+        if self._s is None or self._s.device != device:
+            g = self.grid
+            self._s = torch.empty(g.nel, dtype=torch.float64, device=device)
+            call("pmg_density_filter_rowsum", g.nelx, g.nely, g.nelz, self.radius, self._s, stream())
+        return self._s
+
+    def _apply(self, v, transpose):
+        vd, kind = _to_device(v)
+        g = self.grid
+        y = torch.empty_like(vd)
+        call("pmg_density_filter", int(transpose), g.nelx, g.nely, g.nelz, self.radius, self._rowsum(vd.device), vd,
+             y, stream())
+        return _from_device(y, kind)
+
+    def __call__(self, x):
+        return self._apply(x, False)
+
+    def _sensitivity(self, dfdy):
+        return self._apply(dfdy, True)
+
+
+def _pad_map(n, p, low, high):
+    """Padded index map of one axis as FilterConv composes it (pymoto/modules/filter.py:98-160): wrapped
+    sides first, then the high side, then the low side; numeric sides pad with index 0 and are
+    overridden by their constant value."""
+    idx = np.arange(n)
+    wl = p if low == "wrap" else 0
+    wh = p if high == "wrap" else 0
+    if wl or wh:
+        idx = np.pad(idx, (wl, wh), mode="wrap")
+    for side, mode in (("high", high), ("low", low)):
+        if mode == "wrap":
+            continue
+        width = (0, p) if side == "high" else (p, 0)
+        if mode in ("edge", "symmetric"):
+            idx = np.pad(idx, width, mode=mode)
+        elif isinstance(mode, (int, float)):
+            idx = np.pad(idx, width, mode="constant", constant_values=0)
+        else:
+            raise ValueError(f"unknown padding mode {mode!r}")
+    return idx.astype(np.int32)
+
+
+class FilterConv(Module):
+    """Density filter as a padded convolution (pymoto/modules/filter.py:8-220).
+
+    Padding modes 'symmetric' (default), 'edge' and 'wrap' per side; constant-value padding is not
+    supported on the GPU path.
+    """
+
+    def __init__(self, domain, radius=None, relative_units=True, weights=None, xmin_bc="symmetric",
+                 xmax_bc="symmetric", ymin_bc="symmetric", ymax_bc="symmetric", zmin_bc="symmetric",
+                 zmax_bc="symmetric"):
+        self.domain = domain
+        self.grid = Grid(*grid_of(domain))
+        if (weights is None) == (radius is None):
+            raise ValueError("Only one of arguments 'filter_radius' or 'weights' must be provided.")
+        if weights is not None:
+            w = np.array(weights, dtype=np.float64)
+            while w.ndim < 3:
+                w = w[..., None]
+            if any(s % 2 == 0 for s in w.shape):
+                raise ValueError("Size of weights must be uneven")
+            self.weights = w
+        else:
+            self.set_filter_radius(radius, relative_units)
+        bcs = [xmin_bc, xmax_bc, ymin_bc, ymax_bc, zmin_bc, zmax_bc]
+        if any(isinstance(b, (int, float)) and not isinstance(b, bool) for b in bcs):
+            raise NotImplementedError("constant-value padding is not supported on the GPU path")
+        g = self.grid
+        sizes = [g.nelx, g.nely, max(g.nelz, 1)]
+        self.pad_sizes = [s // 2 for s in self.weights.shape]
+        self._maps_host = [_pad_map(n, p, bcs[2 * a], bcs[2 * a + 1]) for a, (n, p) in
+                           enumerate(zip(sizes, self.pad_sizes))]
+        self._dev = None
+
+    def set_filter_radius(self, radius, relative_units=True):
+        """Cone kernel max(0, r - |d|) normalised to unit sum (pymoto/modules/filter.py:189-205)."""
+        d = self.domain
+        dx, dy, dz = (1.0, 1.0, 1.0) if relative_units else (d.unitx, d.unity, d.unitz)
+        nx, ny, nz = grid_of(d)
+        ex = min(nx, int((radius - 1e-10 * dx) / dx))
+        ey = min(ny, int((radius - 1e-10 * dy) / dy))
+        ez = min(nz, int((radius - 1e-10 * dz) / dz))
+        X, Y, Z = np.meshgrid(np.arange(-ex, ex + 1) * dx, np.arange(-ey, ey + 1) * dy, np.arange(-ez, ez + 1) * dz,
+                              indexing="ij")
+        w = np.maximum(0.0, radius - np.sqrt(X * X + Y * Y + Z * Z))
+        self.weights = w / np.sum(w)
+
+    def _device_data(self, device):
+        if self._dev is None or self._dev[0].device != device:
+            w = torch.from_numpy(np.ascontiguousarray(self.weights)).to(device)
+            maps = [torch.from_numpy(m).to(device) for m in self._maps_host]
+            self._dev = (w, *maps)
+        return self._dev
+
+    def _apply(self, v, transpose):
+        vd, kind = _to_device(v)
+        g = self.grid
+        w, px, py, pz = self._device_data(vd.device)
+        kx, ky, kz = self.weights.shape
+        y = torch.empty_like(vd)
+        call("pmg_conv_filter", int(transpose), g.nelx, g.nely, g.nelz, w, kx, ky, kz, px, py, pz, vd, y, stream())
+        return _from_device(y, kind)
+
+    def __call__(self, x):
+        return self._apply(x, False)
+
+    def _sensitivity(self, dfdv):
+        return self._apply(dfdv, True)
+
+
+# --------------------------------------------------------------------------------------------- SIMP
+class SIMP(Module):
+    """y = xmin + (1 - xmin) x^penal, the interpolation pyMOTO's examples write as
+    MathExpression("xmin + (1-xmin)*inp0^3") (pymoto/modules/generic.py:14-140)."""
+
+    def __init__(self, xmin=1e-9, penal=3.0):
+        self.xmin = float(xmin)
+        self.penal = float(penal)
+        self.x = None
+
+    def __call__(self, x):
+        xd, kind = _to_device(x)
+        self.x = xd
+        y = torch.empty_like(xd)
+        call("pmg_simp", xd.numel(), self.xmin, self.penal, xd, y, None, stream())
+        return _from_device(y, kind)
+
+    def _sensitivity(self, dy):
+        dd, kind = _to_device(dy)
+        dx = torch.empty_like(dd)
+        call("pmg_simp_backward", dd.numel(), self.xmin, self.penal, self.x, dd, dx, stream())
+        return _from_device(dx, kind)
+
+
+_SIMP_EXPR = re.compile(r"^\s*([0-9.eE+-]+)\s*\+\s*\(\s*1\s*-\s*([0-9.eE+-]+)\s*\)\s*\*\s*(\w+)\s*(?:\^|\*\*)\s*"
+                        r"([0-9.]+)\s*$")
+
+
+class MathExpression(SIMP):
+    """The SIMP subset of pyMOTO's MathExpression: expressions "a + (1-a)*inp0^p" (any input name)."""
+
+    def __init__(self, expression):
+        m = _SIMP_EXPR.match(expression)
+        if m is None or float(m.group(1)) != float(m.group(2)):
+            raise NotImplementedError(f"only 'xmin + (1-xmin)*inp0^p' runs on the GPU path, got {expression!r}")
+        super().__init__(xmin=float(m.group(1)), penal=float(m.group(4)))
+        self.expression = expression
+
+
+# --------------------------------------------------------------------------------------------- dyad
+class DeviceDyad:
+    """Sum of outer products sum_k u_k v_k^T on the device: the dK that LinSolve passes to the assembly
+    (the role of pyMOTO's DyadicMatrix, pymoto/common/dyadcarrier.py)."""
+
+    def __init__(self, u=None, v=None, shape=None):
+        self.u = list(u or [])
+        self.v = list(v or [])
+        n = self.u[0].numel() if self.u else 0
+        self.shape = shape if shape is not None else (n, n)
+
+    @property
+    def size(self):
+        return self.shape[0] * self.shape[1]
+
+    def add_sensitivity(self, other):
+        self += other
+        return self
+
+    def __iadd__(self, other):
+        if isinstance(other, DeviceDyad):
+            self.u += other.u
+            self.v += other.v
+            return self
+        raise TypeError(f"cannot add {type(other).__name__} to a DeviceDyad")
+
+    def __imul__(self, s):
+        self.u = [ui * s for ui in self.u]
+        return self
+
+    def __deepcopy__(self, memo):
+        return DeviceDyad([x.clone() for x in self.u], [x.clone() for x in self.v], self.shape)
+
+    def todense(self):
+        return sum(torch.outer(a, b) for a, b in zip(self.u, self.v))
+
+
+# --------------------------------------------------------------------------------------------- assembly
+class AssembleStiffness(Module):
+    """K(x) = sum_e x_e K0 with Dirichlet rows/columns (pymoto/modules/assembly.py:407-463 over
+    AssembleGeneral :18-315).  The output is a matrix-free StiffnessOperator on the device, not a CSR
+    matrix; its sensitivity contracts the incoming dyad with K0 per element."""
+
+    def __init__(self, domain, bc=None, bcdiagval=None, matrix_type=None, add_constant=None, reuse_sparsity=True,
+                 e_modulus=1.0, poisson_ratio=0.3, plane="strain"):
+        if add_constant is not None:
+            raise NotImplementedError("add_constant is not supported by the matrix-free operator")
+        self.domain = domain
+        self.grid = Grid(*grid_of(domain))
+        g = self.grid
+        self.E, self.nu, self.plane = e_modulus, poisson_ratio, plane
+        unit = (domain.unitx, domain.unity, domain.unitz)
+        self.stiffness_element = element_stiffness(g.dim, e_modulus, poisson_ratio, plane, unit)
+        self.bc = None if bc is None else np.asarray(bc, dtype=np.int64).ravel()
+        self.bcdiagval = float(np.max(self.stiffness_element)) if bcdiagval is None else float(bcdiagval)
+        self._mask_host = bc_node_mask(g.nnodes, g.dim, self.bc)
+        self._mask = None
+
+    def bcmask(self, device):
+        if self._mask is None or self._mask.device != device:
+            self._mask = torch.from_numpy(self._mask_host).to(device)
+        return self._mask
+
+    def __call__(self, x):
+        xd, kind = _to_device(x)
+        if xd.numel() != self.grid.nel:
+            raise ValueError(f"Input vector wrong size ({xd.numel()}), must be equal to #nel ({self.grid.nel})")
+        self._kind = kind
+        return StiffnessOperator(self.grid, xd, self.stiffness_element, self.bcmask(xd.device), self.bcdiagval)
+
+    def _sensitivity(self, dgdmat):
+        if dgdmat is None or getattr(dgdmat, "size", 1) <= 0:
+            return [None]
+        g = self.grid
+        device = self._mask.device
+        dx = torch.zeros(g.nel, dtype=torch.float64, device=device)
+        if isinstance(dgdmat, DeviceDyad) or (hasattr(dgdmat, "u") and hasattr(dgdmat, "v")):
+            pairs = list(zip(dgdmat.u, dgdmat.v))
+        else:
+            raise TypeError(f"unsupported sensitivity type {type(dgdmat).__name__} (a dyad is expected)")
+        for k, (u, v) in enumerate(pairs):
+            ud = _to_device(u, device=device)[0]
+            vd = _to_device(v, device=device)[0]
+            call("pmg_sens_contract", g.nelx, g.nely, g.nelz, self.stiffness_element, self._mask, ud, vd, 1.0,
+                 int(k > 0), dx, stream())
+        return _from_device(dx, self._kind)
+
+
+# --------------------------------------------------------------------------------------------- LinSolve
+class LinSolve(Module):
+    """Solve K u = f (pymoto/modules/linalg.py:121-219) with the bookkeeping of the linear-dependency-aware
+    wrapper that pyMOTO puts around every solver (pymoto/solvers/solvers.py:99-306):
+      * Dirichlet rows (diagonal-only) are solved directly as f / bcdiag;
+      * the solve starts from the previous solution with those rows zeroed (warm start);
+      * each solution is stored as a normalised (u, K u) pair; later right-hand sides (the adjoint) are
+        first projected on the stored pairs and only solved for when the projection residual exceeds
+        5 x the solver tolerance -- so the compliance adjoint costs one FP64 residual, not a solve.
+    """
+
+    use_lda_solver = True
+
+    def __init__(self, dep_tol=1e-5, hermitian=None, symmetric=None, positive_definite=None, solver=None):
+        self.dep_tol = dep_tol
+        self.ishermitian = hermitian
+        self.issymmetric = symmetric
+        self.ispositivedefinite = positive_definite
+        self.solver = solver
+        self.u = None
+        self._pairs = []
+
+    @property
+    def lda_tol(self):
+        return 5.0 * self.solver.tol if hasattr(self.solver, "tol") else 1e-7
+
+    def _split(self, A, rhs):
+        """(direct part on Dirichlet dofs, rhs with those dofs zeroed)."""
+        n = A.grid.nnodes
+        direct = torch.empty_like(rhs)
+        call("pmg_mask_bc", F64, A.grid.dim, n, A.bcmask, 1, rhs, direct, stream())
+        call("pmg_scale", F64, rhs.numel(), direct, direct, 1.0 / A.bcdiag, stream())
+        rl = torch.empty_like(rhs)
+        call("pmg_mask_bc", F64, A.grid.dim, n, A.bcmask, 0, rhs, rl, stream())
+        return direct, rl
+
+    def _mask(self, A, v):
+        out = torch.empty_like(v)
+        call("pmg_mask_bc", F64, A.grid.dim, A.grid.nnodes, A.bcmask, 0, v, out, stream())
+        return out
+
+    def _lda_solve(self, rhs, x0=None):
+        A = self.A
+        ws = Workspace.get(rhs.device)
+        st = stream()
+        n = rhs.numel()
+        sol, rl = self._split(A, rhs)
+        sc = torch.zeros(4, dtype=torch.float64, device=rhs.device)
+        for xs, bs in self._pairs:   # modified Gram-Schmidt projection on the stored pairs
+            call("pmg_dot2", F64, n, rl, bs, bs, bs, sc[0:1], ws.reduce, st)
+            alpha = (sc[0] / sc[1])
+            rl.sub_(alpha * bs)
+            sol.add_(alpha * xs)
+        if self._pairs:
+            r = A.apply(RESIDUAL, sol, rhs)
+            call("pmg_dot2", F64, n, r, r, rhs, rhs, sc[2:3], ws.reduce, st)
+            rn, bn = sc[2:4].sqrt().tolist()
+            rtol = rn / (bn if bn != 0 else 1.0)
+        else:
+            call("pmg_dot2", F64, n, rl, rl, rhs, rhs, sc[2:3], ws.reduce, st)
+            rn, bn = sc[2:4].sqrt().tolist()
+            rtol = rn / (bn if bn != 0 else 1.0)
+        self.last_rtol = rtol
+        if rtol <= self.lda_tol:
+            return sol
+        x0l = None
+        if x0 is not None:
+            x0l = self._mask(A, x0)
+            for xs, _ in self._pairs:
+                call("pmg_dot2", F64, n, x0l, xs, xs, xs, sc[0:1], ws.reduce, st)
+                x0l.sub_((sc[0] / sc[1]) * xs)
+        xnew = self.solver.solve(rl, x0=x0l)
+        xnew = self._mask(A, xnew)
+        sol.add_(xnew)
+        # store the new (x, A x) pair, orthogonalised against the stored ones and normalised
+        ba = self._mask(A, A.matvec(xnew))
+        xa = xnew
+        for xs, bs in self._pairs:
+            call("pmg_dot2", F64, n, ba, bs, bs, bs, sc[0:1], ws.reduce, st)
+            beta = sc[0] / sc[1]
+            ba = ba - beta * bs
+            xa = xa - beta * xs
+        call("pmg_dot", F64, n, ba, ba, sc[2:3], ws.reduce, st)
+        bnrm = float(sc[2].sqrt().item())
+        if np.isfinite(bnrm) and bnrm != 0.0:
+            self._pairs.append((xa / bnrm, ba / bnrm))
+        return sol
+
+    def __call__(self, mat, rhs):
+        if not isinstance(mat, StiffnessOperator):
+            raise TypeError("LinSolve on the GPU path expects the StiffnessOperator of AssembleStiffness")
+        fd, kind = _to_device(rhs, device=mat.device)
+        self._kind = kind
+        if self.solver is None:
+            self.solver = default_solver(mat)
+        self.A = mat.astype(F64)
+        self.solver.update(mat)
+        self._pairs = []
+        x0 = None if self.u is None else _to_device(self.u, device=mat.device)[0]
+        u = self._lda_solve(fd, x0)
+        self._u_dev = u
+        self.u = _from_device(u, kind)
+        return self.u
+
+    def _sensitivity(self, dfdv):
+        dd, kind = _to_device(dfdv, device=self._u_dev.device)
+        lam = self._lda_solve(dd)
+        dmat = DeviceDyad([-lam], [self._u_dev])
+        return dmat, _from_device(lam, kind)
+
+
+# --------------------------------------------------------------------------------------------- EinSum
+class EinSum(Module):
+    """The contractions of pyMOTO's EinSum (pymoto/modules/generic.py:143-226) used on the compliance path:
+    'i,i->' (c = f.u) and 'i->' (sum, e.g. the volume), FP64 on the device."""
+
+    _SUPPORTED = {"i,i->", "i->"}
+
+    def __init__(self, expression):
+        expr = expression.replace(" ", "")
+        if expr not in self._SUPPORTED:
+            raise NotImplementedError(f"EinSum({expression!r}) is not supported on the GPU path")
+        self.expr = expr
+
+    def __call__(self, *args):
+        devs = [_to_device(a) for a in args]
+        self._in = devs
+        ws = Workspace.get(devs[0][0].device)
+        out = torch.empty(1, dtype=torch.float64, device=devs[0][0].device)
+        a = devs[0][0]
+        b = devs[1][0] if self.expr == "i,i->" else torch.ones_like(a)
+        call("pmg_dot", F64, a.numel(), a, b, out, ws.reduce, stream())
+        return np.float64(out.item())
+
+    def _sensitivity(self, df):
+        df = float(df)
+        if self.expr == "i->":
+            (a, kind), = self._in
+            return _from_device(torch.full_like(a, df), kind)
+        (a, ka), (b, kb) = self._in
+        da = torch.empty_like(a)
+        db = torch.empty_like(b)
+        call("pmg_scale", F64, b.numel(), da, b, df, stream())
+        call("pmg_scale", F64, a.numel(), db, a, df, stream())
+        return [_from_device(da, ka), _from_device(db, kb)]

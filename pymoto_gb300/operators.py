@@ -1,0 +1,274 @@
+"""Device-resident stiffness operators of the multigrid hierarchy.
+
+StiffnessOperator is what AssembleStiffness outputs in place of pyMOTO's CSR matrix
+(pymoto/modules/assembly.py:245-296): the matrix-free K(x) = sum_e x_e K0 with Dirichlet rows/columns
+replaced by `bcdiag` on the diagonal.  StencilOperator holds a Galerkin coarse operator R^T A R
+(pymoto/solvers/iterative.py:173) as element matrices plus assembled node stencils.  Both provide the
+matrix protocol the solvers use: shape, dtype, `@`, diagonal(), T, apply().
+"""
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import F32, F64, JACOBI, MATVEC, RESIDUAL, call, stream
+
+TORCH_DTYPE = {F64: torch.float64, F32: torch.float32}
+
+
+class Grid:
+    """Element counts of a structured grid; nelz == 0 is 2D."""
+
+    def __init__(self, nelx, nely, nelz=0):
+        self.nelx, self.nely, self.nelz = int(nelx), int(nely), int(nelz or 0)
+        self.dim = 2 if self.nelz == 0 else 3
+        self.nel = self.nelx * self.nely * max(self.nelz, 1)
+        self.nnodes = (self.nelx + 1) * (self.nely + 1) * (self.nelz + 1)
+        self.ndof = self.nnodes * self.dim
+
+    @property
+    def dims(self):
+        return self.nelx, self.nely, self.nelz
+
+    def can_coarsen(self):
+        return self.nelx % 2 == 0 and self.nely % 2 == 0 and self.nelz % 2 == 0 and self.nelx >= 2 and self.nely >= 2
+
+    def coarse(self):
+        if not self.can_coarsen():
+            raise ValueError(f"grid {self.dims} must be divisible by 2")
+        return Grid(self.nelx // 2, self.nely // 2, self.nelz // 2)
+
+    def __repr__(self):
+        return f"Grid{self.dims}"
+
+
+class Workspace:
+    """Per-device scratch for the reductions and the OC bisection (zero-filled once)."""
+
+    _by_device = {}
+
+    def __init__(self, device):
+        self.device = device
+        nred = call("pmg_reduce_scratch_bytes")
+        noc = call("pmg_oc_scratch_bytes")
+        self.reduce = torch.zeros(nred, dtype=torch.uint8, device=device)
+        self.oc = torch.zeros(noc, dtype=torch.uint8, device=device)
+
+    @classmethod
+    def get(cls, device=None):
+        device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        key = device.index if device.index is not None else torch.cuda.current_device()
+        ws = cls._by_device.get(key)
+        if ws is None:
+            ws = cls._by_device[key] = cls(torch.device("cuda", key))
+        return ws
+
+
+def element_stiffness(dim, e_modulus=1.0, poisson_ratio=0.3, plane="strain", unit=(1.0, 1.0, 1.0)):
+    """Element stiffness matrix of pyMOTO's AssembleStiffness, computed by the library (host)."""
+    nde = (2 ** dim) * dim
+    K0 = np.zeros((nde, nde))
+    call("pmg_element_stiffness", dim, float(e_modulus), float(poisson_ratio), int("stress" in plane.lower()),
+         float(unit[0]), float(unit[1]), float(unit[2]), K0)
+    return K0
+
+
+def bc_node_mask(nnodes, dim, bc):
+    """One byte per node, bit d set for Dirichlet dof node*dim + d (host array)."""
+    m = np.zeros(nnodes, dtype=np.uint8)
+    if bc is not None:
+        bc = np.asarray(bc, dtype=np.int64).ravel()
+        if bc.size and (bc.min() < 0 or bc.max() >= nnodes * dim):
+            raise IndexError("Dirichlet dof index out of range")
+        np.bitwise_or.at(m, bc // dim, (1 << (bc % dim)).astype(np.uint8))
+    return m
+
+
+def dot(a, b, out=None, ws=None):
+    """FP64 device scalar a.b (accumulated in FP64)."""
+    ws = ws or Workspace.get(a.device)
+    out = torch.empty(1, dtype=torch.float64, device=a.device) if out is None else out
+    call("pmg_dot", _lib.dtype_code(a), a.numel(), a, b, out, ws.reduce, stream())
+    return out
+
+
+class _GalerkinTables:
+    _cache = {}
+
+    @classmethod
+    def get(cls, K0, dim, dtype, device):
+        key = (K0.tobytes(), dim, dtype, str(device))
+        t = cls._cache.get(key)
+        if t is None:
+            nde = (2 ** dim) * dim
+            host = np.zeros((2 ** dim, nde, nde))
+            call("pmg_galerkin_table", dim, np.ascontiguousarray(K0, dtype=np.float64), host)
+            t = cls._cache[key] = torch.from_numpy(host).to(device=device, dtype=TORCH_DTYPE[dtype])
+        return t
+
+
+class StiffnessOperator:
+    """Matrix-free K(x) = sum_e x_e K0 with Dirichlet rows/columns (level 0 of the hierarchy)."""
+
+    def __init__(self, grid, xe, K0, bcmask, bcdiag, dtype=F64, _xe64=None):
+        self.grid = grid
+        self.xe = xe                      # element scaling in the operator dtype
+        self.K0 = np.ascontiguousarray(K0, dtype=np.float64)
+        self.bcmask = bcmask              # uint8 per node (device)
+        self.bcdiag = float(bcdiag)
+        self.code = dtype
+        self._xe64 = xe if _xe64 is None and dtype == F64 else _xe64
+        self._diag = None
+        self._variants = {dtype: self}
+
+    # matrix protocol -------------------------------------------------------------------------
+    @property
+    def shape(self):
+        return (self.grid.ndof, self.grid.ndof)
+
+    @property
+    def ndim(self):
+        return 2
+
+    @property
+    def dtype(self):
+        return np.dtype(np.float64 if self.code == F64 else np.float32)
+
+    @property
+    def torch_dtype(self):
+        return TORCH_DTYPE[self.code]
+
+    @property
+    def device(self):
+        return self.xe.device
+
+    @property
+    def T(self):
+        return self
+
+    def astype(self, code):
+        """Operator with the element scaling stored in `code` precision (cached)."""
+        if code in self._variants:
+            return self._variants[code]
+        xe = torch.empty(self.xe.shape, dtype=TORCH_DTYPE[code], device=self.xe.device)
+        call("pmg_convert", self.code, code, self.xe.numel(), self.xe, xe, stream())
+        op = StiffnessOperator(self.grid, xe, self.K0, self.bcmask, self.bcdiag, code, _xe64=self._xe64)
+        op._variants = self._variants
+        self._variants[code] = op
+        return op
+
+    def apply(self, mode, u, b=None, diag=None, w=0.0, out=None):
+        out = torch.empty_like(u) if out is None else out
+        g = self.grid
+        call("pmg_ebe_apply", mode, self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag,
+             u, b, diag, float(w), out, stream())
+        return out
+
+    def matvec(self, u, out=None):
+        return self.apply(MATVEC, u, out=out)
+
+    def __matmul__(self, u):
+        if isinstance(u, np.ndarray):
+            ud = torch.from_numpy(np.ascontiguousarray(u, dtype=self.dtype)).to(self.device)
+            return self.matvec(ud).cpu().numpy()
+        return self.matvec(u.contiguous())
+
+    def diagonal(self):
+        if self._diag is None:
+            g = self.grid
+            d = torch.empty(g.ndof, dtype=self.torch_dtype, device=self.device)
+            call("pmg_ebe_diagonal", self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag,
+                 d, stream())
+            self._diag = d
+        return self._diag
+
+    def galerkin(self):
+        """Coarse operator R^T K R as a StencilOperator (same precision)."""
+        g = self.grid
+        gc = g.coarse()
+        nde = (2 ** g.dim) * g.dim
+        table = _GalerkinTables.get(self.K0, g.dim, self.code, self.device)
+        E = torch.empty((gc.nel, nde * nde), dtype=self.torch_dtype, device=self.device)
+        call("pmg_galerkin_from_ebe", self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag,
+             table, E, stream())
+        return StencilOperator(gc, E, self.code)
+
+    def __repr__(self):
+        return f"StiffnessOperator({self.grid}, {self.dtype})"
+
+
+class StencilOperator:
+    """Galerkin operator of a coarse grid: element matrices E and node stencils S (same dtype)."""
+
+    def __init__(self, grid, E, code):
+        self.grid = grid
+        self.E = E
+        self.code = code
+        g = grid
+        nsb = (27 if g.dim == 3 else 9) * g.dim * g.dim
+        self.S = torch.empty((nsb, g.nnodes), dtype=TORCH_DTYPE[code], device=E.device)
+        call("pmg_stencil_from_elements", code, g.nelx, g.nely, g.nelz, E, self.S, stream())
+        self._diag = None
+
+    @property
+    def shape(self):
+        return (self.grid.ndof, self.grid.ndof)
+
+    @property
+    def dtype(self):
+        return np.dtype(np.float64 if self.code == F64 else np.float32)
+
+    @property
+    def torch_dtype(self):
+        return TORCH_DTYPE[self.code]
+
+    @property
+    def device(self):
+        return self.E.device
+
+    @property
+    def T(self):
+        return self
+
+    def apply(self, mode, u, b=None, diag=None, w=0.0, out=None):
+        out = torch.empty_like(u) if out is None else out
+        g = self.grid
+        call("pmg_stencil_apply", mode, self.code, g.nelx, g.nely, g.nelz, self.S, u, b, diag, float(w), out, stream())
+        return out
+
+    def matvec(self, u, out=None):
+        return self.apply(MATVEC, u, out=out)
+
+    def __matmul__(self, u):
+        if isinstance(u, np.ndarray):
+            ud = torch.from_numpy(np.ascontiguousarray(u, dtype=self.dtype)).to(self.device)
+            return self.matvec(ud).cpu().numpy()
+        return self.matvec(u.contiguous())
+
+    def diagonal(self):
+        if self._diag is None:
+            g = self.grid
+            d = torch.empty(g.ndof, dtype=self.torch_dtype, device=self.device)
+            call("pmg_stencil_diagonal", self.code, g.nelx, g.nely, g.nelz, self.S, d, stream())
+            self._diag = d
+        return self._diag
+
+    def galerkin(self):
+        g = self.grid
+        gc = g.coarse()
+        nde = (2 ** g.dim) * g.dim
+        E = torch.empty((gc.nel, nde * nde), dtype=self.torch_dtype, device=self.device)
+        call("pmg_galerkin_from_elements", self.code, g.nelx, g.nely, g.nelz, self.E, E, stream())
+        return StencilOperator(gc, E, self.code)
+
+    def to_dense(self):
+        g = self.grid
+        A = torch.empty((g.ndof, g.ndof), dtype=torch.float64, device=self.device)
+        call("pmg_stencil_to_dense", self.code, g.nelx, g.nely, g.nelz, self.S, A, stream())
+        return A
+
+    def bandwidth(self):
+        g = self.grid
+        return call("pmg_stencil_bandwidth", g.nelx, g.nely, g.nelz)
+
+    def __repr__(self):
+        return f"StencilOperator({self.grid}, {self.dtype})"

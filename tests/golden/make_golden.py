@@ -1,0 +1,197 @@
+"""Write the golden fixtures of tests/golden/ by running pyMOTO itself (v2.0.1).
+
+Run in a container where the pyMOTO sources are available (default: /root/reference, or the path in
+$PYMOTO_REFERENCE).  matplotlib is not needed: a module stub stands in for it, because pyMOTO imports it
+at module level for plotting only.  The fixtures are small .npz files; the tests never import pyMOTO.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+import types
+import warnings
+
+import numpy as np
+
+REF = os.environ.get("PYMOTO_REFERENCE", "/root/reference")
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def import_reference():
+    mpl = types.ModuleType("matplotlib")
+    mpl.use = lambda *a, **k: None
+    sys.modules["matplotlib"] = mpl
+    for sub in ["patches", "path", "pyplot", "colors", "cm", "figure", "axes"]:
+        m = types.ModuleType("matplotlib." + sub)
+        sys.modules["matplotlib." + sub] = m
+        setattr(mpl, sub, m)
+    sys.modules["matplotlib.patches"].PathPatch = object
+    sys.modules["matplotlib.path"].Path = object
+    sys.path.insert(0, REF)
+    import pymoto
+    return pymoto
+
+
+def clamp_face_dofs(d, dim):
+    nodes = d.nodes[0, ...].flatten()
+    return (nodes[:, None] * dim + np.arange(dim)).ravel()
+
+
+def save(name, **arrs):
+    np.savez_compressed(os.path.join(OUT, name), **arrs)
+    print("wrote", name, sorted(arrs))
+
+
+def maps_and_k0(pym):
+    out = {}
+    for tag, shp, units in [("q4", (6, 4), (1.0, 1.0, 1.0)), ("q4s", (5, 3), (0.5, 2.0, 0.3)),
+                            ("h8", (4, 3, 2), (1.0, 1.0, 1.0)), ("h8s", (3, 2, 2), (0.1, 0.2, 0.3))]:
+        d = pym.VoxelDomain(*shp, unitx=units[0], unity=units[1], unitz=units[2])
+        out[f"{tag}_shape"] = np.array(shp)
+        out[f"{tag}_units"] = np.array(units)
+        out[f"{tag}_conn"] = d.conn
+        out[f"{tag}_dofconn"] = d.get_dofconnectivity(d.dim)
+        out[f"{tag}_K0"] = pym.AssembleStiffness(d).stiffness_element
+        if d.dim == 2:
+            out[f"{tag}_K0stress"] = pym.AssembleStiffness(d, plane="stress").stiffness_element
+    save("maps_k0.npz", **out)
+
+
+def assembly(pym):
+    out = {}
+    for tag, shp in [("q4", (6, 4)), ("h8", (4, 3, 2))]:
+        d = pym.VoxelDomain(*shp)
+        rng = np.random.default_rng(7)
+        x = rng.uniform(0.05, 1.0, d.nel)
+        bc = clamp_face_dofs(d, d.dim)
+        K = pym.AssembleStiffness(d, bc=bc)(x).tocsr()
+        K.eliminate_zeros()
+        u = rng.standard_normal(K.shape[0])
+        out.update({f"{tag}_shape": np.array(shp), f"{tag}_x": x, f"{tag}_bc": bc, f"{tag}_data": K.data,
+                    f"{tag}_indices": K.indices, f"{tag}_indptr": K.indptr, f"{tag}_u": u,
+                    f"{tag}_Ku": K @ u})
+    save("assembly.npz", **out)
+
+
+def filters(pym):
+    out = {}
+    for tag, shp, r in [("q4", (10, 6), 1.5), ("q4r3", (9, 7), 3.0), ("h8", (8, 6, 4), 2.5), ("h8r15", (5, 4, 3), 1.5)]:
+        d = pym.VoxelDomain(*shp)
+        rng = np.random.default_rng(3)
+        x = rng.uniform(0.0, 1.0, d.nel)
+        dy = rng.standard_normal(d.nel)
+        df = pym.DensityFilter(d, radius=r)
+        fc = pym.FilterConv(d, radius=r)
+        sx = pym.Signal("x", x)
+        sy = fc(sx)
+        out.update({f"{tag}_shape": np.array(shp), f"{tag}_r": np.array(r), f"{tag}_x": x, f"{tag}_dy": dy,
+                    f"{tag}_density_y": df(x), f"{tag}_density_dx": df._sensitivity(dy),
+                    f"{tag}_conv_y": sy.state, f"{tag}_conv_dx": fc._sensitivity(dy),
+                    f"{tag}_conv_w": fc.weights})
+    save("filters.npz", **out)
+
+
+def multigrid(pym):
+    out = {}
+    for tag, shp in [("q4", (8, 4)), ("h8", (4, 4, 4)), ("h8b", (8, 4, 4))]:
+        d = pym.VoxelDomain(*shp)
+        rng = np.random.default_rng(11)
+        x = rng.uniform(1e-3, 1.0, d.nel) ** 3
+        bc = clamp_face_dofs(d, d.dim)
+        K = pym.AssembleStiffness(d, bc=bc)(x)
+        mg1 = pym.solvers.GeometricMultigrid(d, smoother=pym.solvers.DampedJacobi(w=0.6), smooth_steps=2)
+        mg2 = pym.solvers.GeometricMultigrid(mg1.sub_domain, smoother=pym.solvers.DampedJacobi(w=0.6), smooth_steps=2)
+        mg1.inner_level = mg2
+        mg1.update(K)
+        R = mg1.R.tocoo()
+        Ac = mg1.inner_level.A.tocsr()
+        Ac.eliminate_zeros()
+        r = rng.standard_normal(K.shape[0])
+        r[bc] = 0.0
+        z = mg1.solve(r)
+        out.update({f"{tag}_shape": np.array(shp), f"{tag}_x": x, f"{tag}_bc": bc,
+                    f"{tag}_R_row": R.row, f"{tag}_R_col": R.col, f"{tag}_R_val": R.data,
+                    f"{tag}_Ac_data": Ac.data, f"{tag}_Ac_indices": Ac.indices, f"{tag}_Ac_indptr": Ac.indptr,
+                    f"{tag}_r": r, f"{tag}_z": z})
+    save("multigrid.npz", **out)
+
+
+def pipeline(pym, tag, shp, filt, radius, levels, tol, plane="strain"):
+    d = pym.VoxelDomain(*shp)
+    dim = d.dim
+    bc = clamp_face_dofs(d, dim)
+    f = np.zeros(d.nnodes * dim)
+    if dim == 2:
+        f[dim * d.get_nodenumber(shp[0], shp[1] // 2) + 1] = -1.0
+    else:
+        f[dim * d.get_nodenumber(shp[0], shp[1] // 2, shp[2] // 2) + 1] = -1.0
+    rng = np.random.default_rng(5)
+    x1 = rng.uniform(1e-3, 1.0, d.nel)
+    x2 = np.clip(x1 + 0.05 * (rng.uniform(size=d.nel) - 0.5), 1e-3, 1.0)
+    sx = pym.Signal("x", x1)
+    with pym.Network() as fn:
+        xf = (pym.DensityFilter(d, radius=radius) if filt == "density" else pym.FilterConv(d, radius=radius))(sx)
+        xs = pym.MathExpression("1e-9 + (1-1e-9)*inp0^3")(xf)
+        sK = pym.AssembleStiffness(d, bc=bc, plane=plane)(xs)
+        if levels > 0:
+            mgs = [pym.solvers.GeometricMultigrid(d, smoother=pym.solvers.DampedJacobi(w=0.6), smooth_steps=2)]
+            while len(mgs) < levels - 1:
+                mgs.append(pym.solvers.GeometricMultigrid(mgs[-1].sub_domain,
+                                                          smoother=pym.solvers.DampedJacobi(w=0.6), smooth_steps=2))
+                mgs[-2].inner_level = mgs[-1]
+            solver = pym.solvers.CG(preconditioner=mgs[0], tol=tol)
+        else:
+            solver = None
+        su = pym.LinSolve(hermitian=True, symmetric=True, solver=solver)(sK, f)
+        sc = pym.EinSum("i,i->")(su, f)
+    res = {"shape": np.array(shp), "bc": bc, "f": f, "radius": np.array(radius), "levels": np.array(levels),
+           "tol": np.array(tol)}
+    for it, x in enumerate([x1, x2]):
+        sx.state = x
+        fn.response()
+        fn.reset()
+        sc.sensitivity = 1.0
+        fn.sensitivity()
+        res.update({f"x{it}": x, f"u{it}": su.state.copy(), f"c{it}": np.array(sc.state),
+                    f"dx{it}": sx.sensitivity.copy()})
+    save(f"pipeline_{tag}.npz", **{k: v for k, v in res.items()})
+
+
+def oc_mbb(pym):
+    """60x20 half-MBB beam, DensityFilter r=1.5, plane stress, direct solve, OC move 0.2, 50 iterations."""
+    d = pym.VoxelDomain(60, 20)
+    left_x = 2 * d.nodes[0, :].flatten()
+    br_y = 2 * d.get_nodenumber(60, 0) + 1
+    bc = np.concatenate([left_x, [br_y]])
+    f = np.zeros(d.nnodes * 2)
+    f[2 * d.get_nodenumber(0, 20) + 1] = -1.0
+    sx = pym.Signal("x", np.full(d.nel, 0.5))
+    with pym.Network() as fn:
+        xf = pym.DensityFilter(d, radius=1.5)(sx)
+        xs = pym.MathExpression("1e-9 + (1-1e-9)*inp0^3")(xf)
+        K = pym.AssembleStiffness(d, bc=bc, plane="stress")(xs)
+        u = pym.LinSolve(hermitian=True, symmetric=True)(K, f)
+        c = pym.EinSum("i,i->")(u, f)
+    hist = [float(c.state)]  # the first response ran when the network was built
+    orig = fn.response
+
+    def resp():
+        orig()
+        hist.append(float(c.state))
+    fn.response = resp
+    oc = pym.OC(sx, c, fn, move=0.2, verbosity=0)
+    oc.optimize(maxiter=50, tolx=0, tolf=0)
+    save("oc_mbb.npz", bc=bc, f=f, c_hist=np.array(hist), x_final=sx.state.copy())
+
+
+if __name__ == "__main__":
+    warnings.filterwarnings("ignore")
+    pym = import_reference()
+    maps_and_k0(pym)
+    assembly(pym)
+    filters(pym)
+    multigrid(pym)
+    pipeline(pym, "h8_mg", (8, 4, 4), "conv", 1.5, 3, 1e-8)
+    pipeline(pym, "q4_mg", (16, 8), "density", 2.0, 3, 1e-8, plane="stress")
+    pipeline(pym, "h8_direct", (6, 4, 2), "density", 1.5, 0, 1e-8)
+    oc_mbb(pym)

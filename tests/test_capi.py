@@ -1,0 +1,94 @@
+"""The C-ABI library: loads without a GPU, exports every declared symbol, host-only entry points (no GPU)."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import ROOT
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\b(pmg_\w+)\s*\(", text))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from pymoto_gb300 import _lib
+    return _lib.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_symbols()
+    assert len(names) > 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_the_header():
+    from pymoto_gb300 import _lib
+    assert set(declared_symbols()) == set(_lib.SIGNATURES)
+
+
+def test_version_and_status_strings(lib):
+    from pymoto_gb300 import _lib
+    assert _lib.call("pmg_version") >= 100
+    assert lib.pmg_status_string(1) == b"invalid argument"
+    assert lib.pmg_status_string(5) == b"matrix not positive definite"
+
+
+@pytest.mark.parametrize("dim,plane,units", [(2, "strain", (1, 1, 1)), (2, "stress", (0.5, 2.0, 0.3)),
+                                             (3, "strain", (1, 1, 1)), (3, "strain", (0.1, 0.2, 0.3))])
+def test_element_stiffness_matches_oracle(dim, plane, units):
+    from pymoto_gb300 import element_stiffness
+    g = O.Grid(2, 2, 2 if dim == 3 else 0, *units)
+    ref = O.element_stiffness(g, plane=plane)
+    np.testing.assert_allclose(element_stiffness(dim, plane=plane, unit=units), ref, rtol=0,
+                               atol=1e-15 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_galerkin_table_is_child_transfer_product(dim):
+    """table[s] = M_s^T K0 M_s with M_s the restriction of R to child s of one coarse cell."""
+    from pymoto_gb300._lib import call
+    g = O.Grid(2, 2, 2 if dim == 3 else 0)
+    K0 = O.element_stiffness(g)
+    nde = K0.shape[0]
+    table = np.zeros((2 ** dim, nde, nde))
+    call("pmg_galerkin_table", dim, K0, table)
+    R = O.prolongation(g).toarray()          # fine 2x2(x2) grid -> coarse 1x1(x1) grid
+    fine_dc = g.dofconn()
+    cg = g.coarse()
+    coarse_dc = cg.dofconn()[0]
+    for s in range(2 ** dim):
+        M = R[np.ix_(fine_dc[g.elem_number(s & 1, (s >> 1) & 1, (s >> 2) & 1 if dim == 3 else 0)], coarse_dc)]
+        np.testing.assert_allclose(table[s], M.T @ K0 @ M, rtol=0, atol=1e-14 * np.abs(K0).max())
+
+
+def test_invalid_arguments_fail_before_any_launch():
+    from pymoto_gb300._lib import PMGError, call
+    with pytest.raises(PMGError) as e:
+        call("pmg_ebe_apply", 0, 0, 0, 4, 4, None, None, None, 1.0, None, None, None, 0.0, None, None)
+    assert e.value.status == 1
+    with pytest.raises(PMGError):
+        call("pmg_restrict", 0, 5, 4, 0, None, None, None)      # odd grid
+    with pytest.raises(PMGError):
+        call("pmg_conv_filter", 0, 4, 4, 0, None, 2, 1, 1, None, None, None, None, None, None)
+    with pytest.raises(PMGError):
+        call("pmg_element_stiffness", 4, 1.0, 0.3, 0, 1.0, 1.0, 1.0, np.zeros(4))
+    assert call("pmg_stencil_bandwidth", 2, 1, 1) == (1 + 3 + 3 * 2) * 3 + 2
+
+
+def test_product_package_never_imports_the_oracle():
+    pkg = os.path.join(ROOT, "pymoto_gb300")
+    for path in glob.glob(os.path.join(pkg, "**", "*.py"), recursive=True):
+        src = open(path).read()
+        assert not re.search(r"^\s*(import|from)\s+oracle\b", src, flags=re.M), path

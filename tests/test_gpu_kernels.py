@@ -1,0 +1,293 @@
+"""Kernel-by-kernel parity of libpymoto_gb300 against the oracle and the golden vectors (GPU)."""
+import numpy as np
+import pytest
+import scipy.sparse as sps
+import torch
+
+import oracle as O
+from conftest import clamp_face_dofs
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(6, 4, 0), (4, 3, 2), (8, 6, 4), (7, 5, 3)]
+
+
+def dev(a, dtype=torch.float64):
+    return torch.from_numpy(np.ascontiguousarray(a)).to("cuda", dtype)
+
+
+def host(t):
+    return t.double().cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import pymoto_gb300 as pg
+    from pymoto_gb300 import _lib
+    _lib.load()
+    return pg
+
+
+def _setup(pg, shape, seed=0, bc=True):
+    from pymoto_gb300.operators import bc_node_mask
+    g = O.Grid(*shape)
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(1e-3, 1.0, g.nel) ** 3
+    bcd = clamp_face_dofs(g) if bc else np.zeros(0, dtype=np.int64)
+    K0 = O.element_stiffness(g)
+    K = O.assemble(g, K0, x, bcd)
+    mask = dev(bc_node_mask(g.nnodes, g.dim, bcd), torch.uint8)
+    op = pg.StiffnessOperator(pg.Grid(*shape), dev(x), K0, mask, O.default_bcdiagval(K0))
+    return g, K, op, rng
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_dof_connectivity_bit_exact(pg, shape):
+    from pymoto_gb300._lib import call, stream
+    g = O.Grid(*shape)
+    dc = torch.empty((g.nel, g.elemnodes * g.dim), dtype=torch.int64, device="cuda")
+    call("pmg_dof_connectivity", *shape, dc, stream())
+    assert np.array_equal(dc.cpu().numpy(), g.dofconn())
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("bc", [True, False])
+def test_matvec_fp64_matches_csr(pg, shape, bc):
+    g, K, op, rng = _setup(pg, shape, bc=bc)
+    u = rng.standard_normal(g.ndof)
+    y = host(op.matvec(dev(u)))
+    ref = K @ u
+    np.testing.assert_allclose(y, ref, rtol=0, atol=1e-13 * np.abs(ref).max())
+    np.testing.assert_allclose(host(op.diagonal()), K.diagonal(), rtol=1e-14)
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_matvec_fp32_and_modes(pg, shape):
+    from pymoto_gb300._lib import F32, JACOBI, RESIDUAL
+    g, K, op, rng = _setup(pg, shape, seed=1)
+    u, b = rng.standard_normal(g.ndof), rng.standard_normal(g.ndof)
+    D = K.diagonal()
+    r = host(op.apply(RESIDUAL, dev(u), dev(b)))
+    np.testing.assert_allclose(r, b - K @ u, atol=1e-12 * np.abs(b - K @ u).max())
+    jac = host(op.apply(JACOBI, dev(u), dev(b), op.diagonal(), 0.6))
+    np.testing.assert_allclose(jac, u + 0.6 * ((b - K @ u) / D), rtol=1e-12, atol=1e-12)
+    op32 = op.astype(F32)
+    y32 = host(op32.matvec(dev(u, torch.float32)))
+    ref = K @ u.astype(np.float32).astype(np.float64)
+    assert np.abs(y32 - ref).max() <= 2e-6 * np.abs(ref).max()
+
+
+def test_matvec_golden(pg, golden):
+    g = golden("assembly.npz")
+    from pymoto_gb300.operators import bc_node_mask
+    for tag in ["q4", "h8"]:
+        shape = tuple(int(v) for v in g[f"{tag}_shape"]) + ((0,) if len(g[f"{tag}_shape"]) == 2 else ())
+        grid = O.Grid(*shape)
+        K0 = pg.element_stiffness(grid.dim)
+        mask = dev(bc_node_mask(grid.nnodes, grid.dim, g[f"{tag}_bc"]), torch.uint8)
+        op = pg.StiffnessOperator(pg.Grid(*shape), dev(g[f"{tag}_x"]), K0, mask, float(np.max(K0)))
+        y = host(op.matvec(dev(g[f"{tag}_u"])))
+        np.testing.assert_allclose(y, g[f"{tag}_Ku"], rtol=0, atol=1e-13 * np.abs(g[f"{tag}_Ku"]).max())
+
+
+@pytest.mark.parametrize("shape", [(8, 4, 0), (6, 4, 2), (8, 6, 4)])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_transfers_match_R(pg, shape, dtype):
+    from pymoto_gb300._lib import call, dtype_code, stream
+    g = O.Grid(*shape)
+    R = O.prolongation(g)
+    rng = np.random.default_rng(2)
+    rf = rng.standard_normal(g.ndof)
+    uc = rng.standard_normal(R.shape[1])
+    uf0 = rng.standard_normal(g.ndof)
+    rc = torch.empty(R.shape[1], dtype=dtype, device="cuda")
+    call("pmg_restrict", dtype_code(rc), *shape, dev(rf, dtype), rc, stream())
+    tol = 1e-14 if dtype == torch.float64 else 1e-6
+    np.testing.assert_allclose(host(rc), R.T @ rf, rtol=0, atol=tol * np.abs(R.T @ rf).max())
+    uf = dev(uf0, dtype)
+    call("pmg_prolong_add", dtype_code(uf), *shape, dev(uc, dtype), uf, stream())
+    np.testing.assert_allclose(host(uf), uf0 + R @ uc, rtol=0, atol=tol * np.abs(uf0 + R @ uc).max())
+
+
+def _stencil_csr(op):
+    """Assemble a StencilOperator into CSR via its dense matrix (test helper)."""
+    return sps.csr_matrix(host(op.to_dense()))
+
+
+@pytest.mark.parametrize("shape", [(8, 4, 0), (4, 4, 4), (8, 4, 4), (6, 4, 2)])
+def test_galerkin_matches_RtKR(pg, shape):
+    g, K, op, rng = _setup(pg, shape, seed=3)
+    R = O.prolongation(g)
+    Ac = (R.T @ K @ R).tocsr()
+    A1 = op.galerkin()
+    D1 = _stencil_csr(A1)
+    scale = abs(Ac).max()
+    assert abs(D1 - Ac).max() <= 1e-13 * scale
+    # stencil apply and diagonal against the CSR product
+    u = rng.standard_normal(Ac.shape[0])
+    np.testing.assert_allclose(host(A1.matvec(dev(u))), Ac @ u, rtol=0, atol=1e-12 * np.abs(Ac @ u).max())
+    np.testing.assert_allclose(host(A1.diagonal()), Ac.diagonal(), rtol=1e-13)
+    # second level from element matrices
+    gc = g.coarse()
+    if gc.nelx % 2 == 0 and gc.nely % 2 == 0 and gc.nelz % 2 == 0 and gc.nelx >= 2 and gc.nely >= 2:
+        R2 = O.prolongation(gc)
+        Ac2 = (R2.T @ Ac @ R2).tocsr()
+        D2 = _stencil_csr(A1.galerkin())
+        assert abs(D2 - Ac2).max() <= 1e-12 * abs(Ac2).max()
+
+
+def test_galerkin_golden(pg, golden):
+    g = golden("multigrid.npz")
+    from pymoto_gb300.operators import bc_node_mask
+    for tag in ["q4", "h8", "h8b"]:
+        s = [int(v) for v in g[f"{tag}_shape"]]
+        shape = tuple(s + [0] * (3 - len(s)))
+        grid = O.Grid(*shape)
+        K0 = pg.element_stiffness(grid.dim)
+        mask = dev(bc_node_mask(grid.nnodes, grid.dim, g[f"{tag}_bc"]), torch.uint8)
+        op = pg.StiffnessOperator(pg.Grid(*shape), dev(g[f"{tag}_x"]), K0, mask, float(np.max(K0)))
+        Ac = sps.csr_matrix((g[f"{tag}_Ac_data"], g[f"{tag}_Ac_indices"], g[f"{tag}_Ac_indptr"]))
+        D1 = _stencil_csr(op.galerkin())
+        Ac = sps.csr_matrix(Ac, shape=D1.shape)
+        assert abs(D1 - Ac).max() <= 1e-13 * abs(Ac).max()
+
+
+@pytest.mark.parametrize("n_shape", [(4, 2, 2), (8, 4, 4), (16, 8, 0), (50, 26, 0)])
+def test_cholesky_banded(pg, n_shape):
+    from pymoto_gb300._lib import call, stream
+    g, K, op, rng = _setup(pg, n_shape, seed=4)
+    A1 = op  # use a coarse Galerkin operator as the SPD test matrix where possible
+    if O.Grid(*n_shape).nelx % 2 == 0 and n_shape[1] % 2 == 0 and n_shape[2] % 2 == 0:
+        A1 = op.galerkin()
+    Ad = A1.to_dense() if hasattr(A1, "to_dense") else None
+    if Ad is None:
+        pytest.skip("no stencil form")
+    n = Ad.shape[0]
+    bw = A1.bandwidth()
+    An = host(Ad)
+    Lf = Ad.clone()
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    call("pmg_cholesky_factor", n, Lf, bw, info, stream())
+    assert int(info.item()) == 0
+    Lh = np.tril(host(Lf))
+    # backward-stable factorisation: L L^T reproduces A to rounding
+    assert np.abs(Lh @ Lh.T - An).max() <= 1e-13 * np.abs(An).max()
+    b = rng.standard_normal(n)
+    x = torch.empty(n, dtype=torch.float64, device="cuda")
+    call("pmg_cholesky_solve", 0, n, Lf, bw, dev(b), x, stream())
+    xh = host(x)
+    assert np.linalg.norm(An @ xh - b) <= 1e-12 * np.linalg.norm(An, 2) * np.linalg.norm(xh)
+    ref = np.linalg.solve(An, b)
+    assert np.linalg.norm(xh - ref) <= 1e-4 * np.linalg.norm(ref)
+
+
+def test_cholesky_reports_not_spd(pg):
+    from pymoto_gb300._lib import call, stream
+    A = torch.eye(40, dtype=torch.float64, device="cuda")
+    A[17, 17] = -1.0
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    call("pmg_cholesky_factor", 40, A, 39, info, stream())
+    assert int(info.item()) == 18
+
+
+@pytest.mark.parametrize("n", [1, 1000, 1 << 20, 3_000_017])
+def test_dot_reductions_deterministic(pg, n):
+    from pymoto_gb300._lib import call, stream
+    from pymoto_gb300.operators import Workspace
+    rng = np.random.default_rng(n)
+    a, b = rng.standard_normal(n), rng.standard_normal(n)
+    ws = Workspace.get()
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    call("pmg_dot2", 0, n, dev(a), dev(b), dev(a), dev(a), out, ws.reduce, stream())
+    o1 = out.cpu().numpy().copy()
+    call("pmg_dot2", 0, n, dev(a), dev(b), dev(a), dev(a), out, ws.reduce, stream())
+    assert np.array_equal(o1, out.cpu().numpy())  # run-to-run bitwise reproducible
+    assert abs(o1[0] - a @ b) <= 1e-12 * np.sqrt(n) * max(1.0, abs(a @ b))
+    assert abs(o1[1] - a @ a) <= 1e-12 * (a @ a)
+    out32 = torch.zeros(1, dtype=torch.float64, device="cuda")
+    call("pmg_dot", 1, n, dev(a, torch.float32), dev(b, torch.float32), out32, ws.reduce, stream())
+    ref32 = a.astype(np.float32).astype(np.float64) @ b.astype(np.float32).astype(np.float64)
+    assert abs(out32.item() - ref32) <= 1e-10 * np.sqrt(n)
+
+
+def test_filters_golden(pg, golden):
+    g = golden("filters.npz")
+    for tag in ["q4", "q4r3", "h8", "h8r15"]:
+        s = [int(v) for v in g[f"{tag}_shape"]]
+        shape = tuple(s + [0] * (3 - len(s)))
+        d = pg.VoxelDomain(*shape)
+        r = float(g[f"{tag}_r"])
+        x, dy = dev(g[f"{tag}_x"]), dev(g[f"{tag}_dy"])
+        df = pg.DensityFilter(d, radius=r)
+        np.testing.assert_allclose(host(df(x)), g[f"{tag}_density_y"], rtol=1e-13, atol=1e-15)
+        np.testing.assert_allclose(host(df._sensitivity(dy)), g[f"{tag}_density_dx"], rtol=1e-12, atol=1e-14)
+        fc = pg.FilterConv(d, radius=r)
+        np.testing.assert_allclose(host(fc(x)), g[f"{tag}_conv_y"], rtol=1e-13, atol=1e-15)
+        np.testing.assert_allclose(host(fc._sensitivity(dy)), g[f"{tag}_conv_dx"], rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("mode", ["edge", "wrap"])
+def test_conv_filter_other_paddings_are_adjoint(pg, mode):
+    d = pg.VoxelDomain(9, 6, 5)
+    fc = pg.FilterConv(d, radius=2.5, xmin_bc=mode, ymax_bc=mode)
+    rng = np.random.default_rng(5)
+    x, y = rng.standard_normal(d.nel), rng.standard_normal(d.nel)
+    fx = host(fc(dev(x)))
+    fty = host(fc._sensitivity(dev(y)))
+    assert abs(fx @ y - x @ fty) <= 1e-12 * np.abs(fx @ y)
+    # forward equals the padded convolution of the oracle's index-map definition
+    from pymoto_gb300.modules import _pad_map
+    maps = fc._maps_host
+    I, J, K = np.meshgrid(*maps, indexing="ij")
+    g = O.Grid(9, 6, 5)
+    xp = x[g.elem_number(I, J, K)]
+    W = fc.weights
+    ref = np.zeros((9, 6, 5))
+    for a in range(W.shape[0]):
+        for b in range(W.shape[1]):
+            for c in range(W.shape[2]):
+                ref += W[-1 - a, -1 - b, -1 - c] * xp[a:a + 9, b:b + 6, c:c + 5]
+    I, J, K = np.meshgrid(np.arange(9), np.arange(6), np.arange(5), indexing="ij")
+    yref = np.zeros(g.nel)
+    yref[g.elem_number(I, J, K).ravel()] = ref.ravel()
+    np.testing.assert_allclose(fx, yref, rtol=1e-13, atol=1e-14)
+
+
+def test_simp_and_sensitivity(pg):
+    rng = np.random.default_rng(6)
+    for shape in [(6, 4, 0), (5, 4, 3)]:
+        g, K, op, _ = _setup(pg, shape, seed=7)
+        x = rng.uniform(0, 1, g.nel)
+        simp = pg.SIMP(xmin=1e-9, penal=3.0)
+        np.testing.assert_allclose(host(simp(dev(x))), O.simp(x), rtol=1e-15)
+        dy = rng.standard_normal(g.nel)
+        np.testing.assert_allclose(host(simp._sensitivity(dev(dy))), dy * O.simp_derivative(x), rtol=1e-14)
+        u, v = rng.standard_normal(g.ndof), rng.standard_normal(g.ndof)
+        bc = clamp_face_dofs(g)
+        K0 = O.element_stiffness(g)
+        ref = O.sensitivity_contract(g, K0, [u], [v], bc)
+        from pymoto_gb300._lib import call, stream
+        dx = torch.empty(g.nel, dtype=torch.float64, device="cuda")
+        call("pmg_sens_contract", *shape, K0, op.bcmask, dev(u), dev(v), 1.0, 0, dx, stream())
+        np.testing.assert_allclose(host(dx), ref, rtol=1e-12, atol=1e-13 * np.abs(ref).max())
+
+
+def test_oc_update_matches_oracle(pg):
+    from pymoto_gb300._lib import call, stream
+    from pymoto_gb300.operators import Workspace
+    rng = np.random.default_rng(8)
+    for n in [1200, 200_000]:
+        x = rng.uniform(0.01, 1.0, n)
+        dg = -rng.uniform(0, 10, n)
+        dg[::17] = 1e-3  # positive entries are clipped to zero
+        xn = torch.empty(n, dtype=torch.float64, device="cuda")
+        call("pmg_oc_update", n, dev(x), dev(dg), xn, 0.4, 0.2, 0.0, 1.0, 0.0, 1e5, 1e-4, Workspace.get().oc, stream())
+        np.testing.assert_allclose(host(xn), O.oc_step(x, dg, 0.4, move=0.2), rtol=1e-13, atol=1e-15)
+
+
+def test_bad_arguments_are_rejected(pg):
+    from pymoto_gb300._lib import PMGError, call, stream
+    with pytest.raises(PMGError):
+        call("pmg_restrict", 0, 5, 4, 0, None, None, stream())
+    with pytest.raises(PMGError):
+        call("pmg_ebe_apply", 7, 0, 4, 4, 0, None, None, None, 1.0, None, None, None, 0.0, None, stream())

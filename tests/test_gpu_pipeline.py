@@ -1,0 +1,194 @@
+"""End-to-end parity of the GPU path against pyMOTO's golden vectors and the oracle (GPU)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from conftest import clamp_face_dofs
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(a, dtype=torch.float64):
+    return torch.from_numpy(np.ascontiguousarray(a)).to("cuda", dtype)
+
+
+def host(t):
+    return t.double().cpu().numpy() if isinstance(t, torch.Tensor) else np.asarray(t)
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import pymoto_gb300 as pg
+    pg._lib.load()
+    return pg
+
+
+def _shape3(s):
+    s = [int(v) for v in s]
+    return tuple(s + [0] * (3 - len(s)))
+
+
+def build_network(pg, shape, bc, f, filt, radius, levels, tol, plane="strain", mixed=False, w=0.6, steps=2,
+                  state_kind="numpy"):
+    d = pg.VoxelDomain(*shape)
+    x0 = np.full(d.nel, 0.5)
+    sx = pg.Signal("x", x0 if state_kind == "numpy" else dev(x0))
+    with pg.Network() as fn:
+        xf = (pg.DensityFilter(d, radius=radius) if filt == "density" else pg.FilterConv(d, radius=radius))(sx)
+        xs = pg.MathExpression("1e-9 + (1-1e-9)*inp0^3")(xf)
+        sK = pg.AssembleStiffness(d, bc=bc, plane=plane)(xs)
+        if levels > 0:
+            mgs = pg.GeometricMultigrid.hierarchy(d, levels=levels, smoother_w=w, smooth_steps=steps,
+                                                  precision="fp32" if mixed else None)
+            if mixed:
+                solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=tol)
+            else:
+                solver = pg.CG(preconditioner=mgs[0], tol=tol)
+        else:
+            solver = None
+        su = pg.LinSolve(hermitian=True, symmetric=True, solver=solver)(sK, f if state_kind == "numpy" else dev(f))
+        sc = pg.EinSum("i,i->")(su, f if state_kind == "numpy" else dev(f))
+    return d, sx, su, sc, fn
+
+
+def run_design(fn, sx, sc, x, kind="numpy"):
+    sx.state = x if kind == "numpy" else dev(x)
+    fn.response()
+    fn.reset()
+    sc.sensitivity = 1.0
+    fn.sensitivity()
+    return float(sc.state), host(sx.sensitivity)
+
+
+def test_vcycle_matches_reference(pg, golden):
+    g = golden("multigrid.npz")
+    for tag in ["q4", "h8", "h8b"]:
+        shape = _shape3(g[f"{tag}_shape"])
+        d = pg.VoxelDomain(*shape)
+        K = pg.AssembleStiffness(d, bc=g[f"{tag}_bc"])(dev(g[f"{tag}_x"]))
+        mgs = pg.GeometricMultigrid.hierarchy(d, levels=3, smoother_w=0.6, smooth_steps=2)
+        mgs[0].update(K)
+        z = host(mgs[0].solve(dev(g[f"{tag}_r"])))
+        np.testing.assert_allclose(z, g[f"{tag}_z"], rtol=0, atol=1e-11 * np.abs(g[f"{tag}_z"]).max())
+
+
+@pytest.mark.parametrize("name", ["h8_mg", "q4_mg", "h8_direct"])
+@pytest.mark.parametrize("state_kind", ["numpy", "torch"])
+def test_pipeline_fp64_matches_reference(pg, golden, name, state_kind):
+    """FP64 path vs pyMOTO's own FP64 results: compliance and sensitivities to 1e-8 relative."""
+    g = golden(f"pipeline_{name}.npz")
+    shape = _shape3(g["shape"])
+    levels = int(g["levels"])
+    filt = "conv" if name == "h8_mg" else "density"
+    plane = "stress" if name == "q4_mg" else "strain"
+    d, sx, su, sc, fn = build_network(pg, shape, g["bc"], g["f"], filt, float(g["radius"]), levels,
+                                      float(g["tol"]), plane=plane, state_kind=state_kind)
+    for it in range(2):
+        c, dx = run_design(fn, sx, sc, g[f"x{it}"], state_kind)
+        assert abs(c - float(g[f"c{it}"])) <= 1e-8 * abs(c), (c, float(g[f"c{it}"]))
+        u = host(su.state)
+        np.testing.assert_allclose(u, g[f"u{it}"], rtol=0, atol=1e-8 * np.abs(u).max())
+        np.testing.assert_allclose(dx, g[f"dx{it}"], rtol=0, atol=1e-8 * np.abs(dx).max())
+
+
+def test_cg_iterations_match_reference_algorithm(pg):
+    """Same algorithm, same iterates: the FP64 GPU CG needs the oracle's iteration count."""
+    shape = (16, 8, 8)
+    g = O.Grid(*shape)
+    bc = clamp_face_dofs(g)
+    f = np.zeros(g.ndof)
+    f[3 * g.node_number(16, 4, 4) + 1] = -1.0
+    rng = np.random.default_rng(0)
+    x = O.simp(rng.uniform(1e-3, 1.0, g.nel))
+    K = O.assemble(g, O.element_stiffness(g), x, bc)
+    hier = O.build_hierarchy(g, K, 3, w=0.6, smooth_steps=2)
+    fr = f.copy()
+    fr[bc] = 0
+    u_ref, its_ref, _ = O.cg_solve(K, fr, lambda r: O.vcycle(hier[0], r), tol=1e-8)
+    d = pg.VoxelDomain(*shape)
+    Kop = pg.AssembleStiffness(d, bc=bc)(dev(x))
+    mgs = pg.GeometricMultigrid.hierarchy(d, levels=3, smoother_w=0.6, smooth_steps=2)
+    cg = pg.CG(preconditioner=mgs[0], tol=1e-8)
+    cg.update(Kop)
+    u = host(cg.solve(dev(fr)))
+    assert cg.iterations - 1 == its_ref
+    np.testing.assert_allclose(u, u_ref, rtol=0, atol=1e-9 * np.abs(u_ref).max())
+
+
+@pytest.mark.parametrize("shape", [(32, 16, 16), (64, 32, 0)])
+def test_mixed_precision_reaches_fp64_residual(pg, shape):
+    """Mixed FP32/FP64 solve: true FP64 relative residual <= 1e-6 and compliance within 1e-6 of the
+    oracle's FP64 solution."""
+    g = O.Grid(*shape)
+    bc = clamp_face_dofs(g)
+    f = np.zeros(g.ndof)
+    tip = g.node_number(g.nelx, g.nely // 2, g.nelz // 2)
+    f[g.dim * tip + 1] = -1.0
+    rng = np.random.default_rng(1)
+    x = O.simp(rng.uniform(1e-3, 1.0, g.nel))
+    K = O.assemble(g, O.element_stiffness(g), x, bc)
+    fr = f.copy()
+    fr[bc] = 0
+    u_ref = O.direct_solve(K, fr) if g.ndof < 60000 else O.cg_solve(K, fr, tol=1e-12)[0]
+    c_ref = fr @ u_ref
+    d = pg.VoxelDomain(*shape)
+    Kop = pg.AssembleStiffness(d, bc=bc)(dev(x))
+    mgs = pg.GeometricMultigrid.hierarchy(d, smoother_w=0.6, smooth_steps=2, precision="fp32")
+    solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=1e-6)
+    solver.update(Kop)
+    u = solver.solve(dev(fr))
+    res = pg.LinearSolver.residual(Kop, u, dev(fr))
+    assert res <= 1e-6
+    c = float(fr @ host(u))
+    assert abs(c - c_ref) <= 1e-6 * abs(c_ref)
+
+
+def test_oc_trajectory_matches_reference(pg, golden):
+    """60x20 half-MBB, DensityFilter r=1.5, OC move 0.2: 50 design iterations on the device."""
+    g = golden("oc_mbb.npz")
+    d = pg.VoxelDomain(60, 20)
+    sx = pg.Signal("x", dev(np.full(d.nel, 0.5)))
+    with pg.Network() as fn:
+        xf = pg.DensityFilter(d, radius=1.5)(sx)
+        xs = pg.SIMP(xmin=1e-9, penal=3.0)(xf)
+        K = pg.AssembleStiffness(d, bc=g["bc"], plane="stress")(xs)
+        u = pg.LinSolve(hermitian=True, symmetric=True)(K, dev(g["f"]))
+        c = pg.EinSum("i,i->")(u, dev(g["f"]))
+    oc = pg.OC(sx, c, fn, move=0.2, verbosity=0)
+    x_eval = None
+    for _ in range(50):
+        x_eval = host(sx.state)
+        oc.step()
+    np.testing.assert_allclose(oc.history, g["c_hist"], rtol=1e-6)
+    np.testing.assert_allclose(x_eval, g["x_final"], atol=1e-5)
+
+
+def test_sensitivity_central_differences(pg):
+    """Adjoint sensitivities vs central finite differences on 64 seeded elements (h = 1e-6 x)."""
+    shape = (16, 8, 8)
+    d = pg.VoxelDomain(*shape)
+    g = O.Grid(*shape)
+    bc = clamp_face_dofs(g)
+    f = np.zeros(g.ndof)
+    f[3 * g.node_number(16, 4, 4) + 1] = -1.0
+    rng = np.random.default_rng(2)
+    x = rng.uniform(0.1, 1.0, g.nel)
+    d_, sx, su, sc, fn = build_network(pg, shape, bc, f, "conv", 2.5, 3, 1e-12)
+    c0, dx = run_design(fn, sx, sc, x)
+    els = rng.choice(g.nel, 64, replace=False)
+    fd = []
+    for e in els:
+        h = 1e-6 * x[e]
+        xp, xm = x.copy(), x.copy()
+        xp[e] += h
+        xm[e] -= h
+        sx.state = xp
+        fn.response()
+        cp = float(sc.state)
+        sx.state = xm
+        fn.response()
+        cm = float(sc.state)
+        fd.append((cp - cm) / (2 * h))
+    fd = np.array(fd)
+    np.testing.assert_allclose(dx[els], fd, rtol=1e-5, atol=1e-6 * np.abs(fd).max())

@@ -1,0 +1,69 @@
+"""Standalone graph runtime: pyMOTO's Signal / Module / Network protocol (no GPU)."""
+import numpy as np
+import pytest
+
+from pymoto_gb300 import _graph as G
+
+
+class Square(G.Module):
+    def __call__(self, x):
+        return x * x
+
+    def _sensitivity(self, dy):
+        return 2 * self.get_input_states() * dy
+
+
+class Mul(G.Module):
+    def __call__(self, a, b):
+        return a * b
+
+    def _sensitivity(self, dy):
+        a, b = self.get_input_states()
+        return dy * b, dy * a
+
+
+def test_network_response_and_reverse_sweep():
+    sx = G.Signal("x", np.array([1.0, 2.0, 3.0]))
+    with G.Network() as fn:
+        sy = Square()(sx)
+        sz = Mul()(sy, sx)      # z = x^3
+    assert len(fn) == 2
+    np.testing.assert_allclose(sz.state, [1, 8, 27])
+    sx.state = np.array([2.0, 3.0, 4.0])
+    fn.response()
+    np.testing.assert_allclose(sz.state, [8, 27, 64])
+    sz.sensitivity = np.ones(3)
+    fn.sensitivity()
+    np.testing.assert_allclose(sx.sensitivity, 3 * sx.state ** 2)   # two contributions accumulated
+    fn.reset()
+    assert sx.sensitivity is None
+
+
+def test_add_sensitivity_deep_copies_first_contribution():
+    s = G.Signal("a")
+    d = np.ones(2)
+    s.add_sensitivity(d)
+    s.add_sensitivity(d)
+    np.testing.assert_allclose(s.sensitivity, 2.0)
+    np.testing.assert_allclose(d, 1.0)
+
+
+def test_keyword_only_arguments_rejected():
+    with pytest.raises(SyntaxError):
+        class Bad(G.Module):
+            def __call__(self, x, *, y=1):
+                return x
+
+
+def test_module_added_to_active_networks_once():
+    sx = G.Signal("x", 1.0)
+    with G.Network() as fn:
+        m = Square()
+        m(sx)
+        with pytest.raises(RuntimeError):
+            m(sx)
+    assert fn.mods == [m]
+
+
+def test_constant_inputs_give_plain_values():
+    assert Square()(3.0) == 9.0
