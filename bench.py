@@ -1,0 +1,400 @@
+"""Design iterations per second of pyMOTO's 3D compliance path on GB300.
+
+Workload (one "step" = one design iteration): 3D cantilever, hex8 128x64x64 (1,635,075 dofs), E0=1,
+nu=0.3, SIMP p=3 (xmin=1e-9), FilterConv r=2.5, left face clamped, unit -y point load at node
+(128,32,32); FilterConv -> SIMP -> K(x) -> multigrid-PCG to relative residual 1e-6 (warm-started from
+the previous solution) -> compliance -> adjoint (LDA projection) -> sensitivity -> filter transpose ->
+OC update (move 0.2), all on the device.  Initial density: seeded U(1e-3, 1).
+
+Arms: "plain_fp64" (FP64 CG with an FP64 geometric-multigrid preconditioner, pyMOTO's algorithm) and the
+headline "mixed" arm (FP64 flexible CG around an FP32 multigrid preconditioner).  `value` is the headline
+arm.  `--impl reference` times the CPU restatement of pyMOTO's own path (oracle) on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "design iters/s, hex8 128×64×64 @1e-6 residual: learned+mixed vs plain FP64 PCG"
+SHAPE = (128, 64, 64)
+RADIUS, PENAL, XMIN, TOL, MOVE, OMEGA, SWEEPS = 2.5, 3.0, 1e-9, 1e-6, 0.2, 0.6, 2
+GPU_LEVELS = 6          # 128x64x64 -> 4x2x2 coarsest (135 dofs, dense FP64 Cholesky)
+REF_LEVELS = 4          # the reference example's hierarchy: coarsest 16x8x8 (SuperLU)
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--shape", default=None, help="override the grid, e.g. 64x32x32")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-breakdown", action="store_true", help="print a per-kernel time table")
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ------------------------------------------------------------------------------------------ problem
+def cantilever(shape):
+    nx, ny, nz = shape
+    nnx, nny = nx + 1, ny + 1
+    left = np.array([(k * nny + j) * nnx for k in range(nz + 1) for j in range(nny)], dtype=np.int64)
+    bc = (left[:, None] * 3 + np.arange(3)).ravel()
+    f = np.zeros((nx + 1) * (ny + 1) * (nz + 1) * 3)
+    tip = ((nz // 2) * nny + ny // 2) * nnx + nx
+    f[3 * tip + 1] = -1.0
+    return bc, f
+
+
+class DesignRun:
+    """The network of the workload on the device, for one solver arm."""
+
+    def __init__(self, arm, shape, seed, torch, pg):
+        self.arm = arm
+        d = pg.VoxelDomain(*shape)
+        bc, f = cantilever(shape)
+        self.nel = d.nel
+        rng = np.random.default_rng(seed)
+        x0 = rng.uniform(1e-3, 1.0, d.nel)
+        self.f = torch.from_numpy(f).cuda()
+        self.sx = pg.Signal("x", torch.from_numpy(x0).cuda())
+        mixed = arm != "plain_fp64"
+        with pg.Network() as fn:
+            xf = pg.FilterConv(d, radius=RADIUS)(self.sx)
+            xs = pg.SIMP(xmin=XMIN, penal=PENAL)(xf)
+            K = pg.AssembleStiffness(d, bc=bc)(xs)
+            mgs = pg.GeometricMultigrid.hierarchy(d, levels=GPU_LEVELS, smoother_w=OMEGA, smooth_steps=SWEEPS,
+                                                  precision="fp32" if mixed else None)
+            if mixed:
+                self.solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=4)
+            else:
+                self.solver = pg.CG(preconditioner=mgs[0], tol=TOL)
+            self.u = pg.LinSolve(hermitian=True, symmetric=True, solver=self.solver)(K, self.f)
+            self.c = pg.EinSum("i,i->")(self.u, self.f)
+        self.fn = fn
+        self.K = K
+        self.oc = pg.OC(self.sx, self.c, fn, move=MOVE, verbosity=0)
+        self.iters = []
+
+    def step(self):
+        self.oc.step()
+        self.iters.append(self.solver.iterations)
+
+
+class ClockSampler:
+    """nvidia-smi samples (SM clock, throttle reasons) while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [v.strip() for v in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_arm(run, steps, warmup, torch, flush, probe_targets=None, pg=None):
+    """Warm up, then time `steps` design iterations with CUDA events (L2 flushed before each step)."""
+    for _ in range(warmup):
+        run.step()
+    torch.cuda.synchronize()
+    run.iters.clear()
+    durs = []
+    probe = pg._lib.Probe(targets=probe_targets) if pg is not None else None
+    if probe is not None:
+        probe.__enter__()
+    try:
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            run.step()
+            e1.record()
+            torch.cuda.synchronize()
+            durs.append(e0.elapsed_time(e1))
+    finally:
+        if probe is not None:
+            probe.__exit__()
+    return durs, probe
+
+
+def kernel_bytes(key, shape):
+    """Algorithmic bytes of one launch of the entry points we report a roofline for."""
+    nx, ny, nz = shape
+    nel = nx * ny * nz
+    nn = (nx + 1) * (ny + 1) * (nz + 1)
+    ndof = 3 * nn
+    name = key[0]
+    if name == "pmg_ebe_apply":
+        mode, dtype = key[1], key[2]
+        s = 8 if dtype == 0 else 4
+        vec_reads = {0: 1, 1: 2, 2: 3}[mode]       # u (+ b) (+ diag)
+        return ndof * s * (vec_reads + 1) + nel * s + nn
+    if name == "pmg_sens_contract":
+        return 2 * ndof * 8 + nel * 8 + nn
+    return None
+
+
+def measure_gb300(args, rank, world, local_rank):
+    import torch
+    import pymoto_gb300 as pg
+
+    torch.cuda.set_device(local_rank)
+    shape = SHAPE if args.shape is None else tuple(int(v) for v in args.shape.split("x"))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    peaks = {}
+    pth = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pth):
+        with open(pth) as fh:
+            peaks = json.load(fh)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(v):
+        if world > 1:
+            t = torch.tensor([v], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            return float(t.item())
+        return v
+
+    results = {}
+    for arm in ["plain_fp64", "mixed"]:
+        run = DesignRun(arm, shape, seed=1234 + rank, torch=torch, pg=pg)
+        targets = {"pmg_ebe_apply", "pmg_sens_contract"} if arm == "mixed" else None
+        barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local_rank) as clk:
+            durs, probe = time_arm(run, args.steps, args.warmup, torch, flush, targets, pg)
+        barrier()
+        total = max_over_ranks(sum(durs))
+        results[arm] = {"durs": durs, "total_ms": total, "iters": list(run.iters), "probe": probe,
+                        "clocks": clk.summary(), "run": run}
+        # true FP64 residual of the last solve
+        A = run.K.state if hasattr(run.K, "state") else None
+        lin = run.fn.mods[3]
+        res = pg.LinearSolver.residual(lin.A, lin._u_dev, run.f)
+        results[arm]["true_residual"] = res
+        results[arm]["compliance"] = float(run.c.state)
+
+    # same-design parity: solve the plain arm's final design with both solvers
+    run_p = results["plain_fp64"]["run"]
+    lin_p = run_p.fn.mods[3]
+    A = lin_p.A
+    b = run_p.f.clone()
+    mask = torch.empty_like(b)
+    pg._lib.call("pmg_mask_bc", 0, 3, A.grid.nnodes, A.bcmask, 0, b, mask, pg._lib.stream())
+    mgs = pg.GeometricMultigrid.hierarchy(pg.VoxelDomain(*shape), levels=GPU_LEVELS, smoother_w=OMEGA,
+                                          smooth_steps=SWEEPS, precision="fp32")
+    ms = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=4)
+    ms.update(A)
+    u_m = ms.solve(mask)
+    mgs64 = pg.GeometricMultigrid.hierarchy(pg.VoxelDomain(*shape), levels=GPU_LEVELS, smoother_w=OMEGA,
+                                            smooth_steps=SWEEPS)
+    tight = pg.CG(preconditioner=mgs64[0], tol=1e-11)
+    tight.update(A)
+    u_t = tight.solve(mask)
+    c_m = float(torch.dot(mask, u_m).item())
+    c_t = float(torch.dot(mask, u_t).item())
+
+    # end-to-end through the public API with host buffers (mixed arm)
+    run = results["mixed"]["run"]
+    nel = run.nel
+    x_host = torch.empty(nel, dtype=torch.float64).pin_memory()
+    x_host.copy_(run.sx.state.cpu())
+    c_host = torch.empty(1, dtype=torch.float64).pin_memory()
+    barrier()
+    torch.cuda.synchronize()
+    e2e_durs = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run.sx.state = x_host.to("cuda", non_blocking=True)          # H2D of the step's design
+        run.oc.step()
+        c_host.copy_(torch.tensor([float(run.c.state)]))               # compliance (already read on the host)
+        x_host.copy_(run.sx.state, non_blocking=True)                  # D2H of the new design
+        torch.cuda.synchronize()
+        e2e_durs.append(time.perf_counter() - t0)
+    e2e_total = max_over_ranks(sum(e2e_durs))
+
+    out = {"results": results, "shape": shape, "hbm_peak": hbm_peak, "peak_src": peak_src, "c_mixed": c_m,
+           "c_tight": c_t, "e2e_total_s": e2e_total, "nel": nel, "res_mixed_same_design": ms.last_residual}
+    if args.profile_breakdown and rank == 0:
+        run = DesignRun("mixed", shape, seed=99, torch=torch, pg=pg)
+        for _ in range(2):
+            run.step()
+        torch.cuda.synchronize()
+        with pg._lib.Probe(targets=None) as pr:
+            for _ in range(3):
+                run.step()
+        torch.cuda.synchronize()
+        out["breakdown"] = pr.summary()
+    return out
+
+
+def cpu_reference_sample(shape, warm_steps=1, budget_s=None):
+    """Time warm design iterations of the CPU restatement (one cold iteration first, untimed)."""
+    import oracle
+    L = oracle.ReferenceDesignLoop(shape, radius=RADIUS, levels=REF_LEVELS, w=OMEGA, smooth_steps=SWEEPS, tol=TOL,
+                                   move=MOVE)
+    L.step()                       # cold solve, untimed
+    times = []
+    for _ in range(warm_steps):
+        t0 = time.perf_counter()
+        L.step()
+        times.append(time.perf_counter() - t0)
+        if budget_s is not None and sum(times) > budget_s:
+            break
+    return times, L
+
+
+def main():
+    args = parse()
+    rank, world, local_rank = dist_info()
+    threads = os.cpu_count() or 1
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        shape = SHAPE if args.shape is None else tuple(int(v) for v in args.shape.split("x"))
+        times, L = cpu_reference_sample(shape, warm_steps=max(1, args.steps), budget_s=150.0)
+        per = statistics.mean(times)
+        line = {"metric": METRIC, "value": 1.0 / per, "unit": "design it/s", "impl": "reference", "n_gpus": args.gpus,
+                "steps": len(times), "warmup": 1, "ms_per_step": per * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded U(1e-3,1) density)",
+                "config": {"workload": f"3D cantilever hex8 {shape[0]}x{shape[1]}x{shape[2]}, FilterConv r=2.5, "
+                                       f"SIMP p=3, CG+GMG {REF_LEVELS} levels (SuperLU coarsest), tol 1e-6, OC"},
+                "cpu_baseline": {"value": 1.0 / per, "unit": "design it/s", "cores": threads, "kind": "port",
+                                 "sample": f"{len(times)} warm design iteration(s) after 1 cold one; numpy/scipy "
+                                           f"restatement of pyMOTO's path (assembly by add.at, SpGEMM Galerkin, "
+                                           f"SuperLU coarsest, CG)"},
+                "e2e": {"value": 1.0 / per, "unit": "design it/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "cg_iterations": L.solver.cg_iterations}
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    m = measure_gb300(args, rank, world, local_rank)
+    if rank == 0:
+        shape = m["shape"]
+        R = m["results"]
+        steps = args.steps
+        val_mixed = world * steps / (R["mixed"]["total_ms"] / 1e3)
+        val_plain = world * steps / (R["plain_fp64"]["total_ms"] / 1e3)
+        # roofline of the dominant probed kernel of the headline arm
+        summ = R["mixed"]["probe"].summary()
+        top = max(summ.items(), key=lambda kv: kv[1]["total_ms"])
+        key, st = top
+        nbytes = kernel_bytes(key, shape)
+        achieved = nbytes / (st["avg_ms"] * 1e-3) / 1e9 if nbytes else None
+        roofline = {"bound": "hbm", "kernel": "%s(mode=%s,dtype=%s)" % (key[0], key[1] if len(key) > 1 else "-",
+                                                                      "f64" if len(key) > 2 and key[2] == 0 else "f32"),
+                    "achieved": achieved, "peak": m["hbm_peak"], "unit": "GB/s",
+                    "frac": achieved / m["hbm_peak"] if achieved else None, "traffic": None,
+                    "bytes_per_launch": nbytes, "avg_launch_ms": st["avg_ms"], "launches": st["launches"],
+                    "peak_source": m["peak_src"], "share_of_step": st["total_ms"] / R["mixed"]["total_ms"]}
+        cpu = None
+        if not args.no_cpu_baseline and world == 1:
+            times, L = cpu_reference_sample(shape, warm_steps=1)
+            cpu = {"value": 1.0 / statistics.mean(times), "unit": "design it/s", "cores": os.cpu_count(),
+                   "kind": "port", "sample": "1 warm design iteration of the same workload (after 1 cold one) with "
+                                             "the numpy/scipy restatement of pyMOTO's path, 4-level CG+GMG"}
+        e2e_val = world * steps / m["e2e_total_s"]
+        launches = R["mixed"]["probe"].launches
+        line = {"metric": METRIC, "value": val_mixed, "unit": "design it/s", "n_gpus": world, "steps": steps,
+                "warmup": args.warmup, "ms_per_step": R["mixed"]["total_ms"] / steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32",
+                "data": "synthetic (seeded U(1e-3,1) initial density, replicas seeded per rank)",
+                "config": {"workload": f"3D cantilever hex8 {shape[0]}x{shape[1]}x{shape[2]} "
+                                       f"({3 * (shape[0] + 1) * (shape[1] + 1) * (shape[2] + 1)} dofs), FilterConv "
+                                       f"r=2.5, SIMP p=3, OC move 0.2, rel. residual 1e-6",
+                           "solver": f"FP64 FCG(4) + FP32 GMG {GPU_LEVELS} levels (Jacobi w=0.6, 2 sweeps), "
+                                     f"FP64 Cholesky coarsest", "learned_warm_start": False,
+                           "parallelism": f"replicas x{world}", "l2": "flushed before every step (256 MB write)"},
+                "arms": {arm: {"design_it_per_s": world * steps / (R[arm]["total_ms"] / 1e3),
+                               "ms_per_step": R[arm]["total_ms"] / steps,
+                               "solver_iterations": R[arm]["iters"], "true_rel_residual_last": R[arm]["true_residual"],
+                               "compliance_last": R[arm]["compliance"]} for arm in R},
+                "speedup_mixed_vs_plain_fp64": val_mixed / val_plain,
+                "parity": {"same_design_compliance_mixed": m["c_mixed"], "same_design_compliance_fp64_tol1e-11":
+                           m["c_tight"], "rel_diff": abs(m["c_mixed"] - m["c_tight"]) / abs(m["c_tight"]),
+                           "mixed_true_rel_residual": m["res_mixed_same_design"]},
+                "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": {"value": e2e_val, "unit": "design it/s", "h2d_bytes_per_step": 8 * m["nel"],
+                        "d2h_bytes_per_step": 8 * m["nel"] + 8},
+                "gpu_launches": launches, "clocks": R["mixed"]["clocks"]}
+        if "breakdown" in m:
+            print(json.dumps({"breakdown": {"|".join(map(str, k)): v for k, v in sorted(
+                m["breakdown"].items(), key=lambda kv: -kv[1]["total_ms"])}}), file=sys.stderr)
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -128,8 +128,8 @@ int pmg_dot2(int dtype, int64_t n, const void* a, const void* b, const void* c, 
 /* alpha = num[0]/den[0];  x += alpha p;  r -= alpha q;  rr_out[0] = r.r   (FP64 CG step). */
 int pmg_cg_update(int dtype, int64_t n, void* x, void* r, const void* p, const void* q, const double* num,
                   const double* den, double* rr_out, void* scratch, void* stream);
-/* alpha = num[0]/den[0]; x += alpha p only (the explicit-residual iterations). */
-int pmg_axpy_ratio(int dtype, int64_t n, void* x, const void* p, const double* num, const double* den,
+/* x += scale * (num[0]/den[0]) p  (the explicit-residual iterations; scale -1 for projections). */
+int pmg_axpy_ratio(int dtype, int64_t n, void* x, const void* p, const double* num, const double* den, double scale,
                    void* stream);
 /* beta = -num[0]/den[0];  p = z + beta p. */
 int pmg_xpby_ratio(int dtype, int64_t n, void* p, const void* z, const double* num, const double* den,
@@ -141,8 +141,8 @@ int pmg_scale(int dtype, int64_t n, void* y, const void* x, double a, void* stre
 /* y = x with the Dirichlet dofs zeroed (or only the Dirichlet dofs kept when keep_bc != 0). */
 int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int keep_bc, const void* x, void* y,
                 void* stream);
-/* Precision conversion y(dst_dtype) = x(src_dtype); and x64 += a * d32 (mixed-precision correction). */
-int pmg_convert(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, void* stream);
+/* Precision conversion y(dst_dtype) = a * x(src_dtype) (product formed in FP64); and x64 += a * d32. */
+int pmg_convert(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, double a, void* stream);
 int pmg_add_f32_to_f64(int64_t n, double* x, const float* d, double a, void* stream);
 /* y = w * (b / diag): the first damped-Jacobi sweep from a zero guess (pymoto/solvers/iterative.py:233-234). */
 int pmg_diag_scale(int dtype, int64_t n, const void* b, const void* diag, double w, void* y, void* stream);

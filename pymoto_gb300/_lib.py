@@ -43,12 +43,12 @@ SIGNATURES = {
     "pmg_dot": (I, [I, L, P, P, P, P, P]),
     "pmg_dot2": (I, [I, L, P, P, P, P, P, P, P]),
     "pmg_cg_update": (I, [I, L, P, P, P, P, P, P, P, P, P]),
-    "pmg_axpy_ratio": (I, [I, L, P, P, P, P, P]),
+    "pmg_axpy_ratio": (I, [I, L, P, P, P, P, D, P]),
     "pmg_xpby_ratio": (I, [I, L, P, P, P, P, P]),
     "pmg_scale_rsqrt": (I, [I, L, P, P, P, P]),
     "pmg_scale": (I, [I, L, P, P, D, P]),
     "pmg_mask_bc": (I, [I, I, L, P, I, P, P, P]),
-    "pmg_convert": (I, [I, I, L, P, P, P]),
+    "pmg_convert": (I, [I, I, L, P, P, D, P]),
     "pmg_add_f32_to_f64": (I, [L, P, P, D, P]),
     "pmg_diag_scale": (I, [I, L, P, P, D, P, P]),
     "pmg_density_filter_rowsum": (I, [I, I, I, D, P, P]),
@@ -113,11 +113,76 @@ def _arg(a):
     return a
 
 
+# kernels launched per call where it is not exactly one (host-only entry points launch none)
+_HOST_ONLY = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_element_stiffness", "pmg_galerkin_table",
+              "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth"}
+
+
+def _launches(name, args):
+    if name in _HOST_ONLY:
+        return 0
+    if name == "pmg_cholesky_factor":
+        nblk = (int(args[0]) + 31) // 32
+        return 3 * nblk - 2
+    if name == "pmg_oc_update":
+        width, steps = float(args[9]) - float(args[8]), 1
+        while width > float(args[10]):
+            width *= 0.5
+            steps += 1
+        return steps
+    return 1
+
+
+class Probe:
+    """Counts kernel launches and, for the entry points in `targets` (None = all), brackets each call with
+    CUDA events on the launching stream.  Use as a context manager; `summary()` after synchronising."""
+
+    active = None
+
+    def __init__(self, targets=None, key_args=2):
+        self.targets = targets
+        self.key_args = key_args
+        self.launches = 0
+        self.records = []
+
+    def __enter__(self):
+        Probe.active = self
+        return self
+
+    def __exit__(self, *exc):
+        Probe.active = None
+
+    def summary(self):
+        out = {}
+        for key, e0, e1 in self.records:
+            d = out.setdefault(key, [0, 0.0])
+            d[0] += 1
+            d[1] += e0.elapsed_time(e1)
+        return {k: {"launches": v[0], "total_ms": v[1], "avg_ms": v[1] / v[0]} for k, v in out.items()}
+
+
 def call(name, *args):
     """Call a C-ABI function; raise PMGError on a non-zero status."""
     lib = load()
     fn = getattr(lib, name)
-    rc = fn(*[_arg(a) for a in args])
+    pr = Probe.active
+    if pr is not None:
+        pr.launches += _launches(name, args)
+        if pr.targets is None or name in pr.targets:
+            if name not in _HOST_ONLY:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                rc = fn(*[_arg(a) for a in args])
+                e1.record()
+                key = (name,) + tuple(a for a in args[:pr.key_args] if isinstance(a, int))
+                pr.records.append((key, e0, e1))
+            else:
+                rc = fn(*[_arg(a) for a in args])
+        else:
+            rc = fn(*[_arg(a) for a in args])
+    else:
+        rc = fn(*[_arg(a) for a in args])
     if name in _VALUE_RETURNING:
         return rc
     if rc != 0:

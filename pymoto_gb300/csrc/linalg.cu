@@ -119,8 +119,8 @@ __global__ void __launch_bounds__(RED_THREADS) cg_update_kernel(int64_t n, T* __
 
 template <typename T>
 __global__ void axpy_ratio_kernel(int64_t n, T* __restrict__ x, const T* __restrict__ p, const double* num,
-                                  const double* den) {
-  const T a = (T)(num[0] / den[0]);
+                                  const double* den, double scale) {
+  const T a = (T)(scale * (num[0] / den[0]));
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     x[i] = x[i] + p[i] * a;
 }
@@ -157,9 +157,14 @@ __global__ void mask_bc_kernel(int dim, int64_t nnodes, const uint8_t* __restric
 }
 
 template <typename S, typename D>
-__global__ void convert_kernel(int64_t n, const S* __restrict__ x, D* __restrict__ y) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = (D)x[i];
+__global__ void convert_kernel(int64_t n, const S* __restrict__ x, D* __restrict__ y, double a) {
+  if (a == 1.0) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+      y[i] = (D)x[i];
+  } else {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+      y[i] = (D)(a * (double)x[i]);
+  }
 }
 
 __global__ void add_f32_to_f64_kernel(int64_t n, double* __restrict__ x, const float* __restrict__ d, double a) {
@@ -398,13 +403,14 @@ int pmg_cg_update(int dtype, int64_t n, void* x, void* r, const void* p, const v
   return check_launch();
 }
 
-int pmg_axpy_ratio(int dtype, int64_t n, void* x, const void* p, const double* num, const double* den, void* stream) {
+int pmg_axpy_ratio(int dtype, int64_t n, void* x, const void* p, const double* num, const double* den, double scale,
+                   void* stream) {
   if (n < 0 || !x || !p || !num || !den) return PMG_BAD_ARG;
   cudaStream_t st = as_stream(stream);
   if (dtype == PMG_F64)
-    axpy_ratio_kernel<double><<<stream_blocks(n), 256, 0, st>>>(n, (double*)x, (const double*)p, num, den);
+    axpy_ratio_kernel<double><<<stream_blocks(n), 256, 0, st>>>(n, (double*)x, (const double*)p, num, den, scale);
   else if (dtype == PMG_F32)
-    axpy_ratio_kernel<float><<<stream_blocks(n), 256, 0, st>>>(n, (float*)x, (const float*)p, num, den);
+    axpy_ratio_kernel<float><<<stream_blocks(n), 256, 0, st>>>(n, (float*)x, (const float*)p, num, den, scale);
   else
     return PMG_BAD_ARG;
   return check_launch();
@@ -460,18 +466,18 @@ int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int k
   return check_launch();
 }
 
-int pmg_convert(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, void* stream) {
+int pmg_convert(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, double a, void* stream) {
   if (n < 0 || !x || !y) return PMG_BAD_ARG;
   cudaStream_t st = as_stream(stream);
   const unsigned g = stream_blocks(n);
   if (src_dtype == PMG_F64 && dst_dtype == PMG_F32)
-    convert_kernel<double, float><<<g, 256, 0, st>>>(n, (const double*)x, (float*)y);
+    convert_kernel<double, float><<<g, 256, 0, st>>>(n, (const double*)x, (float*)y, a);
   else if (src_dtype == PMG_F32 && dst_dtype == PMG_F64)
-    convert_kernel<float, double><<<g, 256, 0, st>>>(n, (const float*)x, (double*)y);
+    convert_kernel<float, double><<<g, 256, 0, st>>>(n, (const float*)x, (double*)y, a);
   else if (src_dtype == PMG_F64 && dst_dtype == PMG_F64)
-    convert_kernel<double, double><<<g, 256, 0, st>>>(n, (const double*)x, (double*)y);
+    convert_kernel<double, double><<<g, 256, 0, st>>>(n, (const double*)x, (double*)y, a);
   else if (src_dtype == PMG_F32 && dst_dtype == PMG_F32)
-    convert_kernel<float, float><<<g, 256, 0, st>>>(n, (const float*)x, (float*)y);
+    convert_kernel<float, float><<<g, 256, 0, st>>>(n, (const float*)x, (float*)y, a);
   else
     return PMG_BAD_ARG;
   return check_launch();

@@ -150,7 +150,7 @@ class StiffnessOperator:
         if code in self._variants:
             return self._variants[code]
         xe = torch.empty(self.xe.shape, dtype=TORCH_DTYPE[code], device=self.xe.device)
-        call("pmg_convert", self.code, code, self.xe.numel(), self.xe, xe, stream())
+        call("pmg_convert", self.code, code, self.xe.numel(), self.xe, xe, 1.0, stream())
         op = StiffnessOperator(self.grid, xe, self.K0, self.bcmask, self.bcdiag, code, _xe64=self._xe64)
         op._variants = self._variants
         self._variants[code] = op

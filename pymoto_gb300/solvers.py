@@ -6,8 +6,9 @@
                          smoothing, V-cycle; with precision="fp32" every level runs in FP32.
   DampedJacobi        -- pymoto/solvers/iterative.py:21-47.
   DenseCholesky       -- FP64 banded Cholesky of the coarsest level (in place of SuperLU).
-  MixedPrecisionCG    -- FP64 iterative refinement around an FP32 MG-PCG; the outer residual
-                         r = f - K(x) u, the alpha/beta dot products and the stopping test are FP64.
+  MixedPrecisionCG    -- flexible CG (FCG(m)) in FP64 around an FP32 multigrid preconditioner; the
+                         residual r = f - K(x) u, the operator products, the alpha/beta dot products and
+                         the stopping test are FP64.
 All vectors are CUDA tensors; numpy right-hand sides are accepted and answered with numpy.
 """
 import math
@@ -299,7 +300,7 @@ def pcg(A, b, M, x, tol, maxit, restart, bnorm=None, callback=None):
         A.apply(MATVEC, p, out=q)
         call("pmg_dot2", code, n, p, q, p, r, sc[0], ws.reduce, st)  # pq, pr
         if it % restart == 0:
-            call("pmg_axpy_ratio", code, n, x, p, sc[1], sc[0], st)
+            call("pmg_axpy_ratio", code, n, x, p, sc[1], sc[0], 1.0, st)
             A.apply(RESIDUAL, x, b, out=r)
             call("pmg_dot", code, n, r, r, sc[2], ws.reduce, st)
         else:
@@ -355,26 +356,33 @@ class CG(LinearSolver):
 
 
 class MixedPrecisionCG(LinearSolver):
-    """FP64 iterative refinement around an FP32 multigrid-preconditioned CG.
+    """Flexible CG in FP64 around an FP32 multigrid preconditioner.
 
-    Outer loop (FP64): r = f - K(x) u with the FP64 matrix-free operator, stop when ||r|| / ||f|| <= tol;
-    otherwise solve K d = r / ||r|| in FP32 (FP32 operator, FP32 MG preconditioner, FP64 alpha/beta dots) to
-    the relative tolerance `inner_tol` and update u += ||r|| d in FP64.  `warm_start` is an optional object
-    with `.predict(A, rhs)` (the learned initial guess) used when no x0 is given.
+    FP64: the solution, the residual, the operator products q = K(x) p, the alpha/beta dot products and the
+    stopping test ||f - K(x) u|| / ||f|| <= tol (the recursive residual, recomputed explicitly every
+    `restart` iterations and once more before returning).
+    FP32: the preconditioner -- one V-cycle of the FP32 hierarchy (inner_iters=0) or up to `inner_iters`
+    FP32 PCG iterations on the FP32 operator to the relative tolerance `inner_tol`.
+    Because the preconditioner is inexact (and may be nonlinear), directions are K-orthogonalised against
+    the last `m` directions (FCG(m)); the reference's beta = -(q.z)/(p.q) is the m = 1 case.
+    `warm_start` is an optional object with `.predict(A, rhs)` giving the initial guess when no x0 is
+    passed; `coarse_correction` an optional callable r64 -> z64 added to the preconditioned residual.
     """
 
-    def __init__(self, A=None, preconditioner=None, tol=1e-6, inner_tol=1e-2, maxit=200, max_outer=30, restart=50,
-                 verbosity=0, warm_start=None):
+    def __init__(self, A=None, preconditioner=None, tol=1e-6, m=4, inner_iters=0, inner_tol=0.1, maxit=500,
+                 restart=50, verbosity=0, warm_start=None, coarse_correction=None):
         self.preconditioner = preconditioner
         self.tol = tol
+        self.m = max(1, int(m))
+        self.inner_iters = inner_iters
         self.inner_tol = inner_tol
         self.maxit = maxit
-        self.max_outer = max_outer
         self.restart = restart
         self.verbosity = verbosity
         self.warm_start = warm_start
+        self.coarse_correction = coarse_correction
         self.iterations = 0
-        self.outer_iterations = 0
+        self.inner_iterations = 0
         self.last_residual = None
         super().__init__(A)
 
@@ -385,44 +393,81 @@ class MixedPrecisionCG(LinearSolver):
         if self.preconditioner is not None:
             self.preconditioner.update(self.A32)
 
+    def _precondition(self, r, rn, z):
+        """z (FP64) = ||r|| M32(r / ||r||)."""
+        n = r.numel()
+        st = stream()
+        call("pmg_convert", F64, F32, n, r, self._r32, 1.0 / rn, st)
+        if self.preconditioner is None:
+            z32 = self._r32
+        elif self.inner_iters > 0:
+            z32 = self._z32
+            z32.zero_()
+            its, _ = pcg(self.A32, self._r32, self.preconditioner.solve, z32, self.inner_tol, self.inner_iters,
+                         self.restart)
+            self.inner_iterations += its
+        else:
+            z32 = self.preconditioner.solve(self._r32)
+        call("pmg_convert", F32, F64, n, z32, z, rn, st)
+        if self.coarse_correction is not None:
+            z.add_(self.coarse_correction(r))
+        return z
+
     def solve(self, rhs, x0=None, trans="N"):
-        A64, A32 = self.A64, self.A32
+        A = self.A64
         b, kind = _to_device(rhs, torch.float64)
         n = b.numel()
+        dev = b.device
         if x0 is not None:
             x = _to_device(x0, torch.float64)[0].clone()
         elif self.warm_start is not None:
-            x = self.warm_start.predict(A64, b).to(torch.float64).contiguous()
+            x = self.warm_start.predict(A, b).to(torch.float64).contiguous()
         else:
             x = torch.zeros_like(b)
-        ws = Workspace.get(b.device)
+        ws = Workspace.get(dev)
         st = stream()
-        sc = torch.zeros(2, dtype=torch.float64, device=b.device)
-        call("pmg_dot", F64, n, b, b, sc[0:1], ws.reduce, st)
-        bn = math.sqrt(sc[0].item()) or 1.0
-        M = self.preconditioner.solve if self.preconditioner is not None else (lambda v: v.clone())
-        r32 = torch.empty(n, dtype=torch.float32, device=b.device)
-        total_inner = 0
-        res = float("inf")
-        outer = 0
-        for outer in range(self.max_outer + 1):
-            r = A64.apply(RESIDUAL, x, b)
-            call("pmg_dot", F64, n, r, r, sc[1:2], ws.reduce, st)
-            rn = math.sqrt(sc[1].item())
-            res = rn / bn
+        self._r32 = torch.empty(n, dtype=torch.float32, device=dev)
+        self._z32 = torch.empty(n, dtype=torch.float32, device=dev)
+        sc = torch.zeros(2 + self.m, dtype=torch.float64, device=dev)   # bb | rr, q_j.z ...
+        r = A.apply(RESIDUAL, x, b)
+        call("pmg_dot2", F64, n, b, b, r, r, sc[0:1], ws.reduce, st)
+        bb, rr = sc[0:2].tolist()
+        bn = math.sqrt(bb) or 1.0
+        res = math.sqrt(rr) / bn
+        self.inner_iterations = 0
+        it = 0
+        hist = []               # FIFO of the last m (p, K p, [p.Kp, p.r]) triples
+        z = torch.empty_like(b)
+        while res > self.tol and it < self.maxit:
+            self._precondition(r, res * bn, z)
+            # p = z - sum_j (q_j.z)/(p_j.q_j) p_j
+            p = z.clone()
+            for j, (pj, qj, sj) in enumerate(hist):
+                call("pmg_dot", F64, n, qj, z, sc[2 + j:3 + j], ws.reduce, st)
+                call("pmg_axpy_ratio", F64, n, p, pj, sc[2 + j:3 + j], sj[0:1], -1.0, st)
+            q = A.apply(MATVEC, p, out=hist[0][1] if len(hist) == self.m else None)
+            s2 = torch.empty(2, dtype=torch.float64, device=dev)
+            call("pmg_dot2", F64, n, p, q, p, r, s2, ws.reduce, st)           # p.q, p.r
+            it += 1
+            if it % self.restart == 0:
+                call("pmg_axpy_ratio", F64, n, x, p, s2[1:2], s2[0:1], 1.0, st)
+                A.apply(RESIDUAL, x, b, out=r)
+                call("pmg_dot", F64, n, r, r, sc[1:2], ws.reduce, st)
+            else:
+                call("pmg_cg_update", F64, n, x, r, p, q, s2[1:2], s2[0:1], sc[1:2], ws.reduce, st)
+            res = math.sqrt(max(sc[1].item(), 0.0)) / bn
             if self.verbosity >= 2:
-                print(f"MixedPrecisionCG outer {outer}: residual {res:.3e} ({total_inner} inner iterations)")
-            if res <= self.tol or outer == self.max_outer or not math.isfinite(res):
+                print(f"FCG it {it}: residual {res:.3e}")
+            if len(hist) == self.m:
+                hist.pop(0)
+            hist.append((p, q, s2))
+            if not math.isfinite(res):
                 break
-            call("pmg_convert", F64, F32, n, r, r32, st)
-            call("pmg_scale", F32, n, r32, r32, 1.0 / rn, st)
-            d = torch.zeros(n, dtype=torch.float32, device=b.device)
-            # inner tolerance relative to this refinement step, never tighter than FP32 can deliver
-            itol = max(self.inner_tol, 0.5 * self.tol / res, 1e-5)
-            its, _ = pcg(A32, r32, M, d, min(itol, 0.5), self.maxit, self.restart)
-            total_inner += its
-            call("pmg_add_f32_to_f64", n, x, d, rn, st)
-        self.iterations, self.outer_iterations, self.last_residual = total_inner, outer, res
+        # final true FP64 residual
+        A.apply(RESIDUAL, x, b, out=r)
+        call("pmg_dot", F64, n, r, r, sc[1:2], ws.reduce, st)
+        res = math.sqrt(max(sc[1].item(), 0.0)) / bn
+        self.iterations, self.last_residual = it, res
         if res > self.tol:
             warnings.warn(f"MixedPrecisionCG did not reach tol {self.tol}: residual {res}")
         return _from_device(x, kind)
