@@ -125,6 +125,13 @@ int pmg_dot(int dtype, int64_t n, const void* a, const void* b, double* out, voi
 /* out[0] = a.b, out[1] = c.d in one pass */
 int pmg_dot2(int dtype, int64_t n, const void* a, const void* b, const void* c, const void* d, double* out,
              void* scratch, void* stream);
+/* out[0] = a.b without a scratch argument, for callers that cannot allocate device memory (for example
+ * a plugin inside a host application that owns every device allocation).  This entry point has no
+ * counterpart in the reference.  Its scratch is a static device array of about 32 KB held by every GPU that
+ * loads the library; n is limited to 4,194,304 elements (larger n: PMG_BAD_ARG).  All calls on a device
+ * share that array, so calls that overlap on the GPU race; calls ordered on one stream are safe.  The first
+ * call on each device looks up the array's device address; make it before any stream capture. */
+int pmg_dot_noalloc(int dtype, int64_t n, const void* a, const void* b, double* out, void* stream);
 /* alpha = num[0]/den[0];  x += alpha p;  r -= alpha q;  rr_out[0] = r.r   (FP64 CG step). */
 int pmg_cg_update(int dtype, int64_t n, void* x, void* r, const void* p, const void* q, const double* num,
                   const double* den, double* rr_out, void* scratch, void* stream);

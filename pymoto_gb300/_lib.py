@@ -42,6 +42,7 @@ SIGNATURES = {
     "pmg_reduce_scratch_bytes": (c_size_t, []),
     "pmg_dot": (I, [I, L, P, P, P, P, P]),
     "pmg_dot2": (I, [I, L, P, P, P, P, P, P, P]),
+    "pmg_dot_noalloc": (I, [I, L, P, P, P, P]),
     "pmg_cg_update": (I, [I, L, P, P, P, P, P, P, P, P, P]),
     "pmg_axpy_ratio": (I, [I, L, P, P, P, P, D, P]),
     "pmg_xpby_ratio": (I, [I, L, P, P, P, P, P]),
