@@ -30,7 +30,7 @@ sys.path.insert(0, ROOT)
 METRIC = "design iters/s, hex8 128×64×64 @1e-6 residual: learned+mixed vs plain FP64 PCG"
 SHAPE = (128, 64, 64)
 RADIUS, PENAL, XMIN, TOL, MOVE, OMEGA, SWEEPS = 2.5, 3.0, 1e-9, 1e-6, 0.2, 0.6, 2
-GPU_LEVELS = 6          # 128x64x64 -> 4x2x2 coarsest (135 dofs, dense FP64 Cholesky)
+GPU_LEVELS = 5          # 128x64x64 -> 8x4x4 coarsest (675 dofs, dense FP64 Cholesky + explicit inverse)
 REF_LEVELS = 4          # the reference example's hierarchy: coarsest 16x8x8 (SuperLU)
 L2_FLUSH_BYTES = 256 << 20
 
@@ -44,6 +44,13 @@ def parse():
     ap.add_argument("--shape", default=None, help="override the grid, e.g. 64x32x32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-breakdown", action="store_true", help="print a per-kernel time table")
+    ap.add_argument("--inner-iters", type=int, default=0, help="FP32 PCG iterations per FCG preconditioning")
+    ap.add_argument("--inner-tol", type=float, default=0.1)
+    ap.add_argument("--fcg-m", type=int, default=1)
+    ap.add_argument("--levels", type=int, default=GPU_LEVELS)
+    ap.add_argument("--sweeps", type=int, default=SWEEPS)
+    ap.add_argument("--coarse-sweeps", type=int, default=None)
+    ap.add_argument("--arms", default="plain_fp64,mixed")
     return ap.parse_args()
 
 
@@ -66,7 +73,10 @@ def cantilever(shape):
 class DesignRun:
     """The network of the workload on the device, for one solver arm."""
 
+    opts = {"inner_iters": 0, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None}
+
     def __init__(self, arm, shape, seed, torch, pg):
+        o = DesignRun.opts
         self.arm = arm
         d = pg.VoxelDomain(*shape)
         bc, f = cantilever(shape)
@@ -80,10 +90,12 @@ class DesignRun:
             xf = pg.FilterConv(d, radius=RADIUS)(self.sx)
             xs = pg.SIMP(xmin=XMIN, penal=PENAL)(xf)
             K = pg.AssembleStiffness(d, bc=bc)(xs)
-            mgs = pg.GeometricMultigrid.hierarchy(d, levels=GPU_LEVELS, smoother_w=OMEGA, smooth_steps=SWEEPS,
-                                                  precision="fp32" if mixed else None)
+            mgs = pg.GeometricMultigrid.hierarchy(d, levels=o["levels"], smoother_w=OMEGA, smooth_steps=o["sweeps"],
+                                                  precision="fp32" if mixed else None,
+                                                  coarse_smooth_steps=o["coarse_sweeps"])
             if mixed:
-                self.solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=4)
+                self.solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=o["m"], inner_iters=o["inner_iters"],
+                                                  inner_tol=o["inner_tol"])
             else:
                 self.solver = pg.CG(preconditioner=mgs[0], tol=TOL)
             self.u = pg.LinSolve(hermitian=True, symmetric=True, solver=self.solver)(K, self.f)
@@ -190,8 +202,11 @@ def kernel_bytes(key, shape):
         s = 8 if dtype == 0 else 4
         vec_reads = {0: 1, 1: 2, 2: 3}[mode]       # u (+ b) (+ diag)
         return ndof * s * (vec_reads + 1) + nel * s + nn
-    if name == "pmg_sens_contract":
-        return 2 * ndof * 8 + nel * 8 + nn
+    if name == "pmg_stencil_apply" and len(key) > 3 and key[3] == nx:
+        mode, dtype = key[1], key[2]
+        s = 8 if dtype == 0 else 4
+        vec_reads = {0: 1, 1: 2, 2: 3}[mode]
+        return ndof * s * (vec_reads + 1) + 243 * nn * s      # u (+ b, diag), y, the 243-entry node stencils
     return None
 
 
@@ -221,10 +236,12 @@ def measure_gb300(args, rank, world, local_rank):
             return float(t.item())
         return v
 
+    DesignRun.opts = {"inner_iters": args.inner_iters, "inner_tol": args.inner_tol, "m": args.fcg_m,
+                      "levels": args.levels, "sweeps": args.sweeps, "coarse_sweeps": args.coarse_sweeps}
     results = {}
-    for arm in ["plain_fp64", "mixed"]:
+    for arm in args.arms.split(","):
         run = DesignRun(arm, shape, seed=1234 + rank, torch=torch, pg=pg)
-        targets = {"pmg_ebe_apply", "pmg_sens_contract"} if arm == "mixed" else None
+        targets = {"pmg_ebe_apply", "pmg_stencil_apply"} if arm == "mixed" else None
         barrier()
         torch.cuda.synchronize()
         with ClockSampler(local_rank) as clk:
@@ -241,18 +258,19 @@ def measure_gb300(args, rank, world, local_rank):
         results[arm]["compliance"] = float(run.c.state)
 
     # same-design parity: solve the plain arm's final design with both solvers
-    run_p = results["plain_fp64"]["run"]
+    run_p = results[next(iter(results))]["run"]
     lin_p = run_p.fn.mods[3]
     A = lin_p.A
     b = run_p.f.clone()
     mask = torch.empty_like(b)
     pg._lib.call("pmg_mask_bc", 0, 3, A.grid.nnodes, A.bcmask, 0, b, mask, pg._lib.stream())
-    mgs = pg.GeometricMultigrid.hierarchy(pg.VoxelDomain(*shape), levels=GPU_LEVELS, smoother_w=OMEGA,
-                                          smooth_steps=SWEEPS, precision="fp32")
-    ms = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=4)
+    mgs = pg.GeometricMultigrid.hierarchy(pg.VoxelDomain(*shape), levels=args.levels, smoother_w=OMEGA,
+                                          smooth_steps=args.sweeps, precision="fp32")
+    ms = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=args.fcg_m, inner_iters=args.inner_iters,
+                             inner_tol=args.inner_tol)
     ms.update(A)
     u_m = ms.solve(mask)
-    mgs64 = pg.GeometricMultigrid.hierarchy(pg.VoxelDomain(*shape), levels=GPU_LEVELS, smoother_w=OMEGA,
+    mgs64 = pg.GeometricMultigrid.hierarchy(pg.VoxelDomain(*shape), levels=args.levels, smoother_w=OMEGA,
                                             smooth_steps=SWEEPS)
     tight = pg.CG(preconditioner=mgs64[0], tol=1e-11)
     tight.update(A)
@@ -345,15 +363,15 @@ def main():
         R = m["results"]
         steps = args.steps
         val_mixed = world * steps / (R["mixed"]["total_ms"] / 1e3)
-        val_plain = world * steps / (R["plain_fp64"]["total_ms"] / 1e3)
+        val_plain = world * steps / (R["plain_fp64"]["total_ms"] / 1e3) if "plain_fp64" in R else None
         # roofline of the dominant probed kernel of the headline arm
-        summ = R["mixed"]["probe"].summary()
+        summ = {k: v for k, v in R["mixed"]["probe"].summary().items() if kernel_bytes(k, shape)}
         top = max(summ.items(), key=lambda kv: kv[1]["total_ms"])
         key, st = top
         nbytes = kernel_bytes(key, shape)
         achieved = nbytes / (st["avg_ms"] * 1e-3) / 1e9 if nbytes else None
-        roofline = {"bound": "hbm", "kernel": "%s(mode=%s,dtype=%s)" % (key[0], key[1] if len(key) > 1 else "-",
-                                                                      "f64" if len(key) > 2 and key[2] == 0 else "f32"),
+        roofline = {"bound": "hbm", "kernel": "%s(mode=%s,dtype=%s,grid=%s)" % (
+                        key[0], key[1], "f64" if key[2] == 0 else "f32", "x".join(map(str, shape))),
                     "achieved": achieved, "peak": m["hbm_peak"], "unit": "GB/s",
                     "frac": achieved / m["hbm_peak"] if achieved else None, "traffic": None,
                     "bytes_per_launch": nbytes, "avg_launch_ms": st["avg_ms"], "launches": st["launches"],
@@ -373,14 +391,15 @@ def main():
                 "config": {"workload": f"3D cantilever hex8 {shape[0]}x{shape[1]}x{shape[2]} "
                                        f"({3 * (shape[0] + 1) * (shape[1] + 1) * (shape[2] + 1)} dofs), FilterConv "
                                        f"r=2.5, SIMP p=3, OC move 0.2, rel. residual 1e-6",
-                           "solver": f"FP64 FCG(4) + FP32 GMG {GPU_LEVELS} levels (Jacobi w=0.6, 2 sweeps), "
+                           "solver": f"FP64 FCG({args.fcg_m}) + FP32 GMG {args.levels} levels (Jacobi w=0.6, "
+                                     f"{args.sweeps} sweeps, {args.inner_iters} inner FP32 PCG its), "
                                      f"FP64 Cholesky coarsest", "learned_warm_start": False,
                            "parallelism": f"replicas x{world}", "l2": "flushed before every step (256 MB write)"},
                 "arms": {arm: {"design_it_per_s": world * steps / (R[arm]["total_ms"] / 1e3),
                                "ms_per_step": R[arm]["total_ms"] / steps,
                                "solver_iterations": R[arm]["iters"], "true_rel_residual_last": R[arm]["true_residual"],
                                "compliance_last": R[arm]["compliance"]} for arm in R},
-                "speedup_mixed_vs_plain_fp64": val_mixed / val_plain,
+                "speedup_mixed_vs_plain_fp64": val_mixed / val_plain if val_plain else None,
                 "parity": {"same_design_compliance_mixed": m["c_mixed"], "same_design_compliance_fp64_tol1e-11":
                            m["c_tight"], "rel_diff": abs(m["c_mixed"] - m["c_tight"]) / abs(m["c_tight"]),
                            "mixed_true_rel_residual": m["res_mixed_same_design"]},

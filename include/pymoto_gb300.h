@@ -101,6 +101,12 @@ int pmg_galerkin_from_ebe(int dtype, int nelx, int nely, int nelz, const void* x
 int pmg_galerkin_from_elements(int dtype, int nelx, int nely, int nelz, const void* Ef, void* Ec, void* stream);
 /* Node stencils of a grid from its element matrices (assembly of sum_e P_e^T E_e P_e). */
 int pmg_stencil_from_elements(int dtype, int nelx, int nely, int nelz, const void* E, void* S, void* stream);
+/* Node stencils (same layout) of the level-0 operator K(x) with its Dirichlet rows/columns: K(x) assembled
+ * once per design so that repeated products cost 3^dim*dim^2 FMA per node instead of the matrix-free
+ * 2^dim*(2^dim*dim)*dim (the FP64 products of the solver; replaces the CSR data assembly of
+ * pymoto/modules/assembly.py:245-296). */
+int pmg_ebe_stencil(int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
+                    const uint8_t* bcmask, double bcdiag, void* S, void* stream);
 /* Dense FP64 matrix (ndof x ndof, row-major) of a stencil operator: the coarsest-level system. */
 int pmg_stencil_to_dense(int dtype, int nelx, int nely, int nelz, const void* S, double* A, void* stream);
 /* Half bandwidth of the dense coarsest matrix of a grid. */
@@ -114,6 +120,11 @@ int pmg_stencil_bandwidth(int nelx, int nely, int nelz);
 int pmg_cholesky_factor(int n, double* A, int bw, int* info, void* stream);
 /* x = (L L^T)^{-1} b.  L is FP64 or FP32 (dtype); b and x have the same dtype as L. */
 int pmg_cholesky_solve(int dtype, int n, const void* L, int bw, const void* b, void* x, void* stream);
+/* Ainv = (L L^T)^{-1} (dense, FP64, n x n): one CTA per row.  For the small coarsest level, whose solve is
+ * then one dense matrix-vector product per V-cycle instead of two sequential substitutions. */
+int pmg_cholesky_inverse(int n, const double* L, int bw, double* Ainv, void* stream);
+/* y = A x, dense row-major n x n, FP64 or FP32 storage with FP64 accumulation. */
+int pmg_dense_gemv(int dtype, int n, const void* A, const void* x, void* y, void* stream);
 
 /* ---- reductions and vector updates of CG (pymoto/solvers/iterative.py:340-403) -----------------
  * Deterministic single-launch reductions with FP64 accumulation (CTA partials summed in CTA order by the
@@ -132,6 +143,7 @@ int pmg_dot2(int dtype, int64_t n, const void* a, const void* b, const void* c, 
  * share that array, so calls that overlap on the GPU race; calls ordered on one stream are safe.  The first
  * call on each device looks up the array's device address; make it before any stream capture. */
 int pmg_dot_noalloc(int dtype, int64_t n, const void* a, const void* b, double* out, void* stream);
+/* In the *_ratio updates below a zero denominator gives a zero ratio (no update) instead of inf/nan. */
 /* alpha = num[0]/den[0];  x += alpha p;  r -= alpha q;  rr_out[0] = r.r   (FP64 CG step). */
 int pmg_cg_update(int dtype, int64_t n, void* x, void* r, const void* p, const void* q, const double* num,
                   const double* den, double* rr_out, void* scratch, void* stream);
@@ -151,6 +163,10 @@ int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int k
 /* Precision conversion y(dst_dtype) = a * x(src_dtype) (product formed in FP64); and x64 += a * d32. */
 int pmg_convert(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, double a, void* stream);
 int pmg_add_f32_to_f64(int64_t n, double* x, const float* d, double a, void* stream);
+/* y = x * sqrt(s[0]) (inverse == 0) or x / sqrt(s[0]) (inverse != 0) with s a device scalar, e.g. the
+ * squared residual norm: normalising a residual to the preconditioner's precision without a host read. */
+int pmg_convert_dscale(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, const double* s, int inverse,
+                       void* stream);
 /* y = w * (b / diag): the first damped-Jacobi sweep from a zero guess (pymoto/solvers/iterative.py:233-234). */
 int pmg_diag_scale(int dtype, int64_t n, const void* b, const void* diag, double w, void* y, void* stream);
 
@@ -161,11 +177,15 @@ int pmg_density_filter_rowsum(int nelx, int nely, int nelz, double radius, doubl
 int pmg_density_filter(int transpose, int nelx, int nely, int nelz, double radius, const double* s,
                        const double* x, double* y, void* stream);
 /* FilterConv (filter.py:8-220) with per-axis padded index maps pad{x,y,z} (int32, length n+2p, device)
- * and kernel weights w (kx*ky*kz, C order, device).  Forward: y = W * x_pad ('valid').  Transpose:
- * full correlation accumulated through the pad maps. */
-int pmg_conv_filter(int transpose, int nelx, int nely, int nelz, const double* w, int kx, int ky, int kz,
-                    const int32_t* padx, const int32_t* pady, const int32_t* padz, const double* x, double* y,
-                    void* stream);
+ * and kernel weights w (kx*ky*kz, C order, device).  Forward: y = W * x_pad ('valid', filter.py:207-212). */
+int pmg_conv_filter(int nelx, int nely, int nelz, const double* w, int kx, int ky, int kz, const int32_t* padx,
+                    const int32_t* pady, const int32_t* padz, const double* x, double* y, void* stream);
+/* Its adjoint (filter.py:214-220: full correlation accumulated through the pad maps), with the inverse pad
+ * maps: the padded positions of index j along an axis are inv_pos[inv_ptr[j] .. inv_ptr[j+1]). */
+int pmg_conv_filter_adjoint(int nelx, int nely, int nelz, const double* w, int kx, int ky, int kz,
+                            const int32_t* invx_ptr, const int32_t* invx_pos, const int32_t* invy_ptr,
+                            const int32_t* invy_pos, const int32_t* invz_ptr, const int32_t* invz_pos,
+                            const double* d, double* y, void* stream);
 
 /* ---- SIMP interpolation (MathExpression "xmin + (1-xmin) x^p", pymoto/modules/generic.py:94-140) -- */
 int pmg_simp(int64_t n, double xmin, double penal, const double* x, double* y, void* y32, void* stream);

@@ -36,9 +36,12 @@ SIGNATURES = {
     "pmg_galerkin_from_elements": (I, [I, I, I, I, P, P, P]),
     "pmg_stencil_from_elements": (I, [I, I, I, I, P, P, P]),
     "pmg_stencil_to_dense": (I, [I, I, I, I, P, P, P]),
+    "pmg_ebe_stencil": (I, [I, I, I, I, P, P, P, D, P, P]),
     "pmg_stencil_bandwidth": (I, [I, I, I]),
     "pmg_cholesky_factor": (I, [I, P, I, P, P]),
     "pmg_cholesky_solve": (I, [I, I, P, I, P, P, P]),
+    "pmg_cholesky_inverse": (I, [I, P, I, P, P]),
+    "pmg_dense_gemv": (I, [I, I, P, P, P, P]),
     "pmg_reduce_scratch_bytes": (c_size_t, []),
     "pmg_dot": (I, [I, L, P, P, P, P, P]),
     "pmg_dot2": (I, [I, L, P, P, P, P, P, P, P]),
@@ -51,10 +54,12 @@ SIGNATURES = {
     "pmg_mask_bc": (I, [I, I, L, P, I, P, P, P]),
     "pmg_convert": (I, [I, I, L, P, P, D, P]),
     "pmg_add_f32_to_f64": (I, [L, P, P, D, P]),
+    "pmg_convert_dscale": (I, [I, I, L, P, P, P, I, P]),
     "pmg_diag_scale": (I, [I, L, P, P, D, P, P]),
     "pmg_density_filter_rowsum": (I, [I, I, I, D, P, P]),
     "pmg_density_filter": (I, [I, I, I, I, D, P, P, P, P]),
-    "pmg_conv_filter": (I, [I, I, I, I, P, I, I, I, P, P, P, P, P, P]),
+    "pmg_conv_filter": (I, [I, I, I, P, I, I, I, P, P, P, P, P, P]),
+    "pmg_conv_filter_adjoint": (I, [I, I, I, P, I, I, I, P, P, P, P, P, P, P, P, P]),
     "pmg_simp": (I, [L, D, D, P, P, P, P]),
     "pmg_simp_backward": (I, [L, D, D, P, P, P, P]),
     "pmg_sens_contract": (I, [I, I, I, P, P, P, P, D, I, P, P]),
@@ -126,7 +131,7 @@ def _launches(name, args):
         nblk = (int(args[0]) + 31) // 32
         return 3 * nblk - 2
     if name == "pmg_oc_update":
-        width, steps = float(args[9]) - float(args[8]), 1
+        width, steps = float(args[9]) - float(args[8]), 3
         while width > float(args[10]):
             width *= 0.5
             steps += 1
@@ -140,7 +145,7 @@ class Probe:
 
     active = None
 
-    def __init__(self, targets=None, key_args=2):
+    def __init__(self, targets=None, key_args=3):
         self.targets = targets
         self.key_args = key_args
         self.launches = 0
@@ -153,6 +158,19 @@ class Probe:
     def __exit__(self, *exc):
         Probe.active = None
 
+    def replay(self, key, graph, launches):
+        """Replay a captured CUDA graph; counted and (when `targets` is None or contains "graph") timed."""
+        self.launches += launches
+        if self.targets is None or "graph" in self.targets:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            graph.replay()
+            e1.record()
+            self.records.append((("graph", key), e0, e1))
+        else:
+            graph.replay()
+
     def summary(self):
         out = {}
         for key, e0, e1 in self.records:
@@ -160,6 +178,14 @@ class Probe:
             d[0] += 1
             d[1] += e0.elapsed_time(e1)
         return {k: {"launches": v[0], "total_ms": v[1], "avg_ms": v[1] / v[0]} for k, v in out.items()}
+
+
+def replay(key, graph, launches):
+    """Replay a CUDA graph of library kernels (accounted to the active Probe, if any)."""
+    if Probe.active is not None:
+        Probe.active.replay(key, graph, launches)
+    else:
+        graph.replay()
 
 
 def call(name, *args):

@@ -65,21 +65,22 @@ inline ElemMat<T, NDE> make_elem_mat(const double* K0) {
   return m;
 }
 
-// Node coordinates from a linear node index.
-__device__ __forceinline__ void node_ijk(const Grid& g, int64_t n, int& i, int& j, int& k) {
-  const int nnx = g.nx + 1, nny = g.ny + 1;
-  i = (int)(n % nnx);
-  int64_t t = n / nnx;
-  j = (int)(t % nny);
+// Node coordinates from a linear node index.  Node and element counts are below 2^31 (checked by every
+// entry point), so the index arithmetic is 32-bit: 64-bit division costs hundreds of instructions.
+__device__ __forceinline__ void node_ijk(const Grid& g, int64_t n64, int& i, int& j, int& k) {
+  const unsigned n = (unsigned)n64, nnx = (unsigned)(g.nx + 1), nny = (unsigned)(g.ny + 1);
+  const unsigned t = n / nnx;
+  i = (int)(n - t * nnx);
   k = (int)(t / nny);
+  j = (int)(t - (unsigned)k * nny);
 }
 
 __device__ __forceinline__ int64_t node_id(const Grid& g, int i, int j, int k) {
-  return ((int64_t)k * (g.ny + 1) + j) * (g.nx + 1) + i;
+  return (int64_t)((k * (g.ny + 1) + j) * (g.nx + 1) + i);
 }
 
 __device__ __forceinline__ int64_t elem_id(const Grid& g, int i, int j, int k) {
-  return ((int64_t)k * g.ny + j) * g.nx + i;
+  return (int64_t)((k * g.ny + j) * g.nx + i);
 }
 
 }  // namespace pmg

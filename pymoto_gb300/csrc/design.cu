@@ -11,10 +11,12 @@ __device__ __forceinline__ double cone(double r, int dx, int dy, int dz) {
   return r - d > 0.0 ? r - d : 0.0;
 }
 
-__device__ __forceinline__ void elem_ijk(const Grid& g, int64_t e, int& i, int& j, int& k) {
-  i = (int)(e % g.nx);
-  j = (int)((e / g.nx) % g.ny);
-  k = (int)(e / ((int64_t)g.nx * g.ny));
+__device__ __forceinline__ void elem_ijk(const Grid& g, int64_t e64, int& i, int& j, int& k) {
+  const unsigned e = (unsigned)e64, nx = (unsigned)g.nx, ny = (unsigned)g.ny;
+  const unsigned t = e / nx;
+  i = (int)(e - t * nx);
+  k = (int)(t / ny);
+  j = (int)(t - (unsigned)k * ny);
 }
 
 __global__ void density_rowsum_kernel(Grid g, double r, double* __restrict__ s) {
@@ -94,26 +96,26 @@ __global__ void conv_filter_kernel(Grid g, const double* __restrict__ w, int kx,
   y[e] = acc;
 }
 
-// Transpose, gather form: dx[j] = sum over padded positions P with pad(P) = j of sum_m w[m] d[P - (K-1) + m]
-// (output o = P - (K-1) + m must lie inside the grid).  The padded positions of j along an axis are all
-// P in [0, n+K-1) with map[P] == j; they are found by scanning the (short) pad map.
-__global__ void conv_filter_T_kernel(Grid g, const double* __restrict__ w, int kx, int ky, int kz,
-                                     const int32_t* __restrict__ px, const int32_t* __restrict__ py,
-                                     const int32_t* __restrict__ pz, const double* __restrict__ d, double* __restrict__ y) {
+// Adjoint, gather form: dx[j] = sum over padded positions P with pad(P) = j of sum_m w[m] d[P - (K-1) + m]
+// (the output o = P - (K-1) + m must lie inside the grid).  The padded positions of index j along each
+// axis are inv_pos[inv_ptr[j] .. inv_ptr[j+1]) (inverse of the pad map, built on the host).
+__global__ void conv_filter_adjoint_kernel(Grid g, const double* __restrict__ w, int kx, int ky, int kz,
+                                           const int32_t* __restrict__ xp, const int32_t* __restrict__ xs,
+                                           const int32_t* __restrict__ yp, const int32_t* __restrict__ ys,
+                                           const int32_t* __restrict__ zp, const int32_t* __restrict__ zs,
+                                           const double* __restrict__ d, double* __restrict__ y) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= g.nel()) return;
   int i, j, k;
   elem_ijk(g, e, i, j, k);
   const int ez = g.ez();
-  const int lx = g.nx + kx - 1, ly = g.ny + ky - 1, lz = ez + kz - 1;
   double acc = 0.0;
-  for (int Pz = 0; Pz < lz; ++Pz) {
-    if (pz[Pz] != k) continue;
-    for (int Py = 0; Py < ly; ++Py) {
-      if (py[Py] != j) continue;
-      for (int Px = 0; Px < lx; ++Px) {
-        if (px[Px] != i) continue;
-        // outputs o = P - (K-1) + m for taps m
+  for (int qz = zp[k]; qz < zp[k + 1]; ++qz) {
+    const int Pz = zs[qz];
+    for (int qy = yp[j]; qy < yp[j + 1]; ++qy) {
+      const int Py = ys[qy];
+      for (int qx = xp[i]; qx < xp[i + 1]; ++qx) {
+        const int Px = xs[qx];
         for (int c = 0; c < kz; ++c) {
           const int oz = Pz - (kz - 1) + c;
           if (oz < 0 || oz >= ez) continue;
@@ -192,11 +194,13 @@ __global__ void sens_kernel(Grid g, ElemMat<double, Traits<DIM>::NDE> K0, const 
 
 // ------------------------------------------------------------------------------------------ OC update
 // State in scratch: sum partials and the bisection interval, all on the device.
+// x sqrt(-dg/lmid) is evaluated as (x sqrt(-dg)) / sqrt(lmid): the per-element square root is taken once and
+// each bisection step costs one multiply and a clip per element (the two forms differ in the last bits).
 constexpr int OC_THREADS = 256;
 constexpr int OC_MAX_BLOCKS = 1024;
 struct OCScratch {
   double partial[OC_MAX_BLOCKS];
-  double l1, l2, lmid;
+  double l1, l2, lmid, lmid_last;
   unsigned int ticket;
 };
 
@@ -225,26 +229,37 @@ __global__ void oc_init_kernel(OCScratch* s, double l1, double l2) {
   s->l1 = l1;
   s->l2 = l2;
   s->lmid = 0.5 * (l1 + l2);
+  s->lmid_last = s->lmid;
   s->ticket = 0u;
 }
 
-// One bisection step: xnew = clip(x sqrt(-dg/lmid), lb, ub); the last CTA compares the volume with the
-// target and moves l1 or l2, exactly as OC.step does.
-__global__ void __launch_bounds__(OC_THREADS) oc_step_kernel(int64_t n, const double* __restrict__ x,
-                                                             const double* __restrict__ dg, double* __restrict__ xnew,
-                                                             double target, double move, double xmin, double xmax,
-                                                             OCScratch* s) {
-  const double lmid = s->lmid;
-  double acc = 0.0;
+// t = x sqrt(-min(dg, 0)), stored in xnew until the final step overwrites it
+__global__ void oc_prepare_kernel(int64_t n, const double* __restrict__ x, const double* __restrict__ dg,
+                                  double* __restrict__ t) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double xi = x[i];
     const double g = dg[i] < 0.0 ? dg[i] : 0.0;
-    const double lb = fmax(xmin, xi - move), ub = fmin(xmax, xi + move);
-    double v = xi * sqrt(-g / lmid);
-    v = fmin(fmax(v, lb), ub);
-    xnew[i] = v;
-    acc += v;
+    t[i] = x[i] * sqrt(-g);
   }
+}
+
+__device__ __forceinline__ double oc_value(double xi, double ti, double s, double move, double xmin, double xmax) {
+  const double lb = fmax(xmin, xi - move), ub = fmin(xmax, xi + move);
+  return fmin(fmax(ti * s, lb), ub);
+}
+
+// One bisection step: volume of clip(t / sqrt(lmid), lb, ub); the last CTA compares it with the target and
+// moves l1 or l2, exactly as OC.step does.
+__global__ void __launch_bounds__(OC_THREADS) oc_step_kernel(int64_t n, const double* __restrict__ x,
+                                                             const double* __restrict__ t, double target, double move,
+                                                             double xmin, double xmax, OCScratch* s) {
+  __shared__ double s_scale;
+  const double lmid = s->lmid;
+  if (threadIdx.x == 0) s_scale = 1.0 / sqrt(lmid);
+  __syncthreads();
+  const double sc = s_scale;
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += oc_value(x[i], t[i], sc, move, xmin, xmax);
   acc = oc_block_sum(acc);
   __shared__ bool last;
   if (threadIdx.x == 0) {
@@ -255,17 +270,26 @@ __global__ void __launch_bounds__(OC_THREADS) oc_step_kernel(int64_t n, const do
   __syncthreads();
   if (!last) return;
   __threadfence();
-  double t = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) t += ((volatile double*)s->partial)[b];
-  t = oc_block_sum(t);
+  double tot = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) tot += ((volatile double*)s->partial)[b];
+  tot = oc_block_sum(tot);
   if (threadIdx.x == 0) {
-    if (t - target > 0.0)
+    if (tot - target > 0.0)
       s->l1 = lmid;
     else
       s->l2 = lmid;
+    s->lmid_last = lmid;
     s->lmid = 0.5 * (s->l1 + s->l2);
     s->ticket = 0u;
   }
+}
+
+// xnew = the design of the last bisection step (t is read from xnew and overwritten in place)
+__global__ void oc_final_kernel(int64_t n, const double* __restrict__ x, double* __restrict__ xnew, double move,
+                                double xmin, double xmax, const OCScratch* s) {
+  const double sc = 1.0 / sqrt(s->lmid_last);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    xnew[i] = oc_value(x[i], xnew[i], sc, move, xmin, xmax);
 }
 
 }  // namespace pmg
@@ -293,18 +317,28 @@ int pmg_density_filter(int transpose, int nelx, int nely, int nelz, double radiu
   return check_launch();
 }
 
-int pmg_conv_filter(int transpose, int nelx, int nely, int nelz, const double* w, int kx, int ky, int kz,
-                    const int32_t* padx, const int32_t* pady, const int32_t* padz, const double* x, double* y,
-                    void* stream) {
+int pmg_conv_filter(int nelx, int nely, int nelz, const double* w, int kx, int ky, int kz, const int32_t* padx,
+                    const int32_t* pady, const int32_t* padz, const double* x, double* y, void* stream) {
   if (!grid_ok(nelx, nely, nelz) || !w || !padx || !pady || !padz || !x || !y || x == y) return PMG_BAD_ARG;
   if (kx < 1 || ky < 1 || kz < 1 || !(kx & 1) || !(ky & 1) || !(kz & 1)) return PMG_BAD_ARG;
   if (nelz == 0 && kz != 1) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
-  const unsigned b = blocks_for(g.nel(), 128);
-  if (transpose)
-    conv_filter_T_kernel<<<b, 128, 0, as_stream(stream)>>>(g, w, kx, ky, kz, padx, pady, padz, x, y);
-  else
-    conv_filter_kernel<<<b, 128, 0, as_stream(stream)>>>(g, w, kx, ky, kz, padx, pady, padz, x, y);
+  conv_filter_kernel<<<blocks_for(g.nel(), 128), 128, 0, as_stream(stream)>>>(g, w, kx, ky, kz, padx, pady, padz, x, y);
+  return check_launch();
+}
+
+int pmg_conv_filter_adjoint(int nelx, int nely, int nelz, const double* w, int kx, int ky, int kz,
+                            const int32_t* invx_ptr, const int32_t* invx_pos, const int32_t* invy_ptr,
+                            const int32_t* invy_pos, const int32_t* invz_ptr, const int32_t* invz_pos,
+                            const double* d, double* y, void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || !w || !invx_ptr || !invx_pos || !invy_ptr || !invy_pos || !invz_ptr ||
+      !invz_pos || !d || !y || d == y)
+    return PMG_BAD_ARG;
+  if (kx < 1 || ky < 1 || kz < 1 || !(kx & 1) || !(ky & 1) || !(kz & 1)) return PMG_BAD_ARG;
+  if (nelz == 0 && kz != 1) return PMG_BAD_ARG;
+  Grid g{nelx, nely, nelz};
+  conv_filter_adjoint_kernel<<<blocks_for(g.nel(), 128), 128, 0, as_stream(stream)>>>(
+      g, w, kx, ky, kz, invx_ptr, invx_pos, invy_ptr, invy_pos, invz_ptr, invz_pos, d, y);
   return check_launch();
 }
 
@@ -344,21 +378,22 @@ int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, do
   if (n <= 0 || !x || !dg || !xnew || !scratch || !(l1l2tol > 0.0) || !(l2 >= l1)) return PMG_BAD_ARG;
   cudaStream_t st = as_stream(stream);
   OCScratch* s = (OCScratch*)scratch;
-  int64_t nb = (n + OC_THREADS * 4 - 1) / (OC_THREADS * 4);
-  if (nb > OC_MAX_BLOCKS) nb = OC_MAX_BLOCKS;
+  int64_t nb = (n + OC_THREADS * 8 - 1) / (OC_THREADS * 8);
+  if (nb > 2 * 152) nb = 2 * 152;
   if (nb < 1) nb = 1;
+  if (x == xnew || dg == xnew) return PMG_BAD_ARG;
   oc_init_kernel<<<1, 1, 0, st>>>(s, l1, l2);
+  oc_prepare_kernel<<<(unsigned)nb, OC_THREADS, 0, st>>>(n, x, dg, xnew);
   // the interval halves every step, so the step count is known on the host: same loop as OC.step
   double a = l1, b = l2;
   const double target = volfrac * (double)n;
   int steps = 0;
   while (b - a > l1l2tol) {
-    oc_step_kernel<<<(unsigned)nb, OC_THREADS, 0, st>>>(n, x, dg, xnew, target, move, xmin, xmax, s);
-    const double mid = 0.5 * (a + b);
-    a = mid;  // only the interval width matters for the count
-    ++steps;
-    if (steps > 200) return PMG_BAD_ARG;
+    oc_step_kernel<<<(unsigned)nb, OC_THREADS, 0, st>>>(n, x, xnew, target, move, xmin, xmax, s);
+    a = 0.5 * (a + b);  // only the interval width matters for the count
+    if (++steps > 200) return PMG_BAD_ARG;
   }
+  oc_final_kernel<<<(unsigned)nb, OC_THREADS, 0, st>>>(n, x, xnew, move, xmin, xmax, s);
   return check_launch();
 }
 

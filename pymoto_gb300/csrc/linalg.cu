@@ -7,8 +7,9 @@ namespace pmg {
 // Deterministic single-launch reduction: every CTA writes its partial sums, the last CTA to finish
 // (counted with an atomic ticket) adds the partials in CTA order and resets the ticket.
 constexpr int RED_THREADS = 256;
-constexpr int RED_MAX_BLOCKS = 1024;
+constexpr int RED_MAX_BLOCKS = 2048;
 constexpr int RED_MAX_OUT = 2;
+constexpr int ILP = 4;  // elements per thread and pass in the streaming kernels
 
 struct RedScratch {
   double partial[RED_MAX_OUT][RED_MAX_BLOCKS];
@@ -72,19 +73,40 @@ __device__ __forceinline__ void finish_reduction(double (&v)[NOUT], RedScratch* 
   }
 }
 
+// Two CTAs per SM at most: each thread then reduces ~20 elements of a 1.6M vector in registers and the last
+// CTA sums few partials.
 inline unsigned red_blocks(int64_t n) {
-  int64_t b = (n + RED_THREADS * 4 - 1) / (RED_THREADS * 4);
+  int64_t b = (n + RED_THREADS * ILP - 1) / (RED_THREADS * ILP);
   if (b < 1) b = 1;
   if (b > RED_MAX_BLOCKS) b = RED_MAX_BLOCKS;
   return (unsigned)b;
 }
 
+// Scalar num/den (times scale) computed once per CTA: an FP64 division per thread is expensive on GB300.
+// A zero denominator gives a zero ratio (no update) instead of inf/nan.
+__device__ __forceinline__ double cta_ratio(const double* num, const double* den, double scale) {
+  __shared__ double s_ratio;
+  if (threadIdx.x == 0) s_ratio = den[0] != 0.0 ? scale * (num[0] / den[0]) : 0.0;
+  __syncthreads();
+  return s_ratio;
+}
+
+// Element loops of the streaming kernels: each thread takes ILP elements per pass (strided by the CTA width,
+// so every load instruction of a warp is coalesced) and keeps their loads in flight together.
+#define PMG_ILP_LOOP(n, BODY)                                                                               \
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x * ILP + threadIdx.x; base < (n);                     \
+       base += (int64_t)gridDim.x * blockDim.x * ILP) {                                                     \
+    _Pragma("unroll") for (int k_ = 0; k_ < ILP; ++k_) {                                                    \
+      const int64_t i = base + (int64_t)k_ * blockDim.x;                                                    \
+      if (i < (n)) { BODY; }                                                                                \
+    }                                                                                                       \
+  }
+
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) dot_kernel(int64_t n, const T* __restrict__ a, const T* __restrict__ b,
                                                          double* out, RedScratch* scr) {
   double v[1] = {0.0};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    v[0] = fma((double)a[i], (double)b[i], v[0]);
+  PMG_ILP_LOOP(n, v[0] = fma((double)a[i], (double)b[i], v[0]))
   finish_reduction<1>(v, scr, out);
 }
 
@@ -93,10 +115,7 @@ __global__ void __launch_bounds__(RED_THREADS) dot2_kernel(int64_t n, const T* _
                                                           const T* __restrict__ c, const T* __restrict__ d, double* out,
                                                           RedScratch* scr) {
   double v[2] = {0.0, 0.0};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    v[0] = fma((double)a[i], (double)b[i], v[0]);
-    v[1] = fma((double)c[i], (double)d[i], v[1]);
-  }
+  PMG_ILP_LOOP(n, v[0] = fma((double)a[i], (double)b[i], v[0]); v[1] = fma((double)c[i], (double)d[i], v[1]))
   finish_reduction<2>(v, scr, out);
 }
 
@@ -105,39 +124,34 @@ __global__ void __launch_bounds__(RED_THREADS) cg_update_kernel(int64_t n, T* __
                                                                const T* __restrict__ p, const T* __restrict__ q,
                                                                const double* num, const double* den, double* rr,
                                                                RedScratch* scr) {
-  const double alpha = num[0] / den[0];
-  const T a = (T)alpha;
+  const T a = (T)cta_ratio(num, den, 1.0);
   double v[1] = {0.0};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] = x[i] + p[i] * a;
-    const T ri = r[i] - q[i] * a;
-    r[i] = ri;
-    v[0] = fma((double)ri, (double)ri, v[0]);
-  }
+  PMG_ILP_LOOP(n, x[i] = x[i] + p[i] * a; const T ri = r[i] - q[i] * a; r[i] = ri; v[0] = fma((double)ri, (double)ri, v[0]))
   finish_reduction<1>(v, scr, rr);
 }
 
 template <typename T>
 __global__ void axpy_ratio_kernel(int64_t n, T* __restrict__ x, const T* __restrict__ p, const double* num,
                                   const double* den, double scale) {
-  const T a = (T)(scale * (num[0] / den[0]));
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    x[i] = x[i] + p[i] * a;
+  const T a = (T)cta_ratio(num, den, scale);
+  PMG_ILP_LOOP(n, x[i] = x[i] + p[i] * a)
 }
 
 template <typename T>
 __global__ void xpby_ratio_kernel(int64_t n, T* __restrict__ p, const T* __restrict__ z, const double* num,
                                   const double* den) {
-  const T beta = (T)(-(num[0] / den[0]));
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = z[i] + p[i] * beta;
+  const T beta = (T)cta_ratio(num, den, -1.0);
+  PMG_ILP_LOOP(n, p[i] = z[i] + p[i] * beta)
 }
 
 template <typename T>
 __global__ void scale_rsqrt_kernel(int64_t n, T* __restrict__ y, const T* __restrict__ x, const double* nrm2) {
-  const double s = sqrt(nrm2[0]);
+  __shared__ double s_inv;
+  if (threadIdx.x == 0) s_inv = nrm2[0] > 0.0 ? 1.0 / sqrt(nrm2[0]) : 0.0;
+  __syncthreads();
+  const double s = s_inv;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = (T)((double)x[i] / s);
+    y[i] = (T)((double)x[i] * s);
 }
 
 template <typename T>
@@ -159,12 +173,24 @@ __global__ void mask_bc_kernel(int dim, int64_t nnodes, const uint8_t* __restric
 template <typename S, typename D>
 __global__ void convert_kernel(int64_t n, const S* __restrict__ x, D* __restrict__ y, double a) {
   if (a == 1.0) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-      y[i] = (D)x[i];
+    PMG_ILP_LOOP(n, y[i] = (D)x[i])
   } else {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-      y[i] = (D)(a * (double)x[i]);
+    PMG_ILP_LOOP(n, y[i] = (D)(a * (double)x[i]))
   }
+}
+
+// y = x * sqrt(s[0]) or x / sqrt(s[0]) (inverse != 0): the scale comes from device memory
+template <typename S, typename D>
+__global__ void convert_dscale_kernel(int64_t n, const S* __restrict__ x, D* __restrict__ y, const double* s,
+                                      int inverse) {
+  __shared__ double sc;
+  if (threadIdx.x == 0) {
+    const double v = s[0];
+    sc = inverse ? (v > 0.0 ? 1.0 / sqrt(v) : 0.0) : sqrt(v > 0.0 ? v : 0.0);
+  }
+  __syncthreads();
+  const double a = sc;
+  PMG_ILP_LOOP(n, y[i] = (D)(a * (double)x[i]))
 }
 
 __global__ void add_f32_to_f64_kernel(int64_t n, double* __restrict__ x, const float* __restrict__ d, double a) {
@@ -174,13 +200,12 @@ __global__ void add_f32_to_f64_kernel(int64_t n, double* __restrict__ x, const f
 
 template <typename T>
 __global__ void diag_scale_kernel(int64_t n, const T* __restrict__ b, const T* __restrict__ diag, T w, T* __restrict__ y) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = w * (b[i] / diag[i]);
+  PMG_ILP_LOOP(n, y[i] = w * (b[i] / diag[i]))
 }
 
 inline unsigned stream_blocks(int64_t n) {
-  int64_t b = (n + 255) / 256;
-  if (b > 152 * 16) b = 152 * 16;
+  int64_t b = (n + 256 * ILP - 1) / (256 * ILP);
+  if (b > 65535) b = 65535;
   if (b < 1) b = 1;
   return (unsigned)b;
 }
@@ -189,10 +214,17 @@ inline unsigned stream_blocks(int64_t n) {
 // Right-looking blocked Cholesky (lower, row-major, in place) with TB x TB tiles; tiles entirely outside
 // the band stay zero and are skipped.
 constexpr int TB = 32;
+constexpr int CHOL_SMEM_MAX_N = 20000;  // x of a solve lives in shared memory (<= 160 KB in FP64)
 
-// Factor the diagonal tile kb in shared memory (one CTA of TB*TB/4 threads).
-__global__ void chol_diag_kernel(int n, double* A, int kb, int* info) {
+// Diagonal tile kb and the panel below it, by one CTA.  The tile is factored in shared memory with one
+// barrier per column: A[r][c] -= A[r][k] A[c][k] / A[k][k] on the unscaled columns, each column scaled by
+// 1/sqrt of its final pivot at the end.  Then every panel row within the band is solved against the
+// tile (x L^T = a) by one thread.
+constexpr int CHOL_THREADS = 256;
+
+__global__ void __launch_bounds__(CHOL_THREADS) chol_diag_panel_kernel(int n, double* A, int kb, int bw, int* info) {
   __shared__ double T[TB][TB + 1];
+  __shared__ double rdiag[TB];   // 1 / L[c][c]
   const int k0 = kb * TB;
   const int nb = min(TB, n - k0);
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
@@ -201,59 +233,49 @@ __global__ void chol_diag_kernel(int n, double* A, int kb, int* info) {
   }
   __syncthreads();
   for (int k = 0; k < nb; ++k) {
-    __shared__ double piv;
-    if (threadIdx.x == 0) {
-      double d = T[k][k];
-      if (!(d > 0.0)) {
-        if (*info == 0) *info = k0 + k + 1;
-        d = 1.0;  // keep going with a unit pivot; the caller reports NOT_SPD
-      }
-      piv = sqrt(d);
-      T[k][k] = piv;
-    }
-    __syncthreads();
-    for (int r = k + 1 + threadIdx.x; r < nb; r += blockDim.x) T[r][k] /= piv;
-    __syncthreads();
+    double d = T[k][k];
+    if (!(d > 0.0)) d = 1.0;   // reported below; a unit pivot keeps the sweep finite
+    const double rd = 1.0 / d;
     for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
       const int r = e / TB, c = e % TB;
-      if (r > k && c > k && c <= r && r < nb) T[r][c] -= T[r][k] * T[c][k];
+      if (c > k && r >= c && r < nb) T[r][c] -= T[r][k] * T[c][k] * rd;
     }
     __syncthreads();
   }
-  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
-    const int r = e / TB, c = e % TB;
-    if (r < nb && c < nb) A[(int64_t)(k0 + r) * n + k0 + c] = c <= r ? T[r][c] : 0.0;
-  }
-}
-
-// Panel: L[ib,kb] = A[ib,kb] L[kb,kb]^{-T}, one CTA (TB threads) per tile row ib > kb within the band.
-__global__ void chol_panel_kernel(int n, double* A, int kb, int bw) {
-  __shared__ double L[TB][TB + 1];
-  const int k0 = kb * TB;
-  const int nb = min(TB, n - k0);
-  const int ib = kb + 1 + blockIdx.x;
-  const int i0 = ib * TB;
-  if (i0 >= n || i0 - (k0 + nb - 1) > bw) return;
-  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
-    const int r = e / TB, c = e % TB;
-    L[r][c] = (r < nb && c < nb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
+  if (threadIdx.x < nb) {
+    const int c = threadIdx.x;
+    double d = T[c][c];
+    if (!(d > 0.0)) {
+      atomicCAS(info, 0, k0 + c + 1);
+      d = 1.0;
+    }
+    rdiag[c] = 1.0 / sqrt(d);
   }
   __syncthreads();
-  const int r = threadIdx.x;  // one row of the panel per thread
-  const int row = i0 + r;
-  if (r < TB && row < n) {
+  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
+    const int r = e / TB, c = e % TB;
+    if (r < nb && c < nb) {
+      const double v = c <= r ? T[r][c] * rdiag[c] : 0.0;
+      T[r][c] = v;
+      A[(int64_t)(k0 + r) * n + k0 + c] = v;
+    }
+  }
+  if (threadIdx.x < nb) rdiag[threadIdx.x] = 1.0 / T[threadIdx.x][threadIdx.x];
+  __syncthreads();
+  // panel rows k0+nb .. k0+nb+bw (band)
+  const int rend = min(n, k0 + nb + bw);
+  for (int row = k0 + nb + threadIdx.x; row < rend; row += blockDim.x) {
     double x[TB];
 #pragma unroll
     for (int c = 0; c < TB; ++c) x[c] = c < nb ? A[(int64_t)row * n + k0 + c] : 0.0;
-    // solve x L^T = a  (forward substitution over columns)
 #pragma unroll
     for (int c = 0; c < TB; ++c) {
       if (c < nb) {
         double v = x[c];
 #pragma unroll
         for (int q = 0; q < TB; ++q)
-          if (q < c) v -= x[q] * L[c][q];
-        x[c] = v / L[c][c];
+          if (q < c) v -= x[q] * T[c][q];
+        x[c] = v * rdiag[c];
       }
     }
 #pragma unroll
@@ -292,66 +314,113 @@ __global__ void chol_update_kernel(int n, double* A, int kb, int bw, int ntiles_
   }
 }
 
-// x = (L L^T)^{-1} b for a banded lower factor, one CTA: forward then backward substitution, with the
-// band rows of each TB block updated in parallel.
+// x = (L L^T)^{-1} x in place (x in shared memory) for a banded lower factor, by one CTA: forward then
+// backward substitution in TB blocks; a warp solves each diagonal block, the CTA updates the band rows.
+// `first` skips the leading blocks of x known to be zero (the right-hand side e_j of the inverse).
 template <typename T>
-__global__ void __launch_bounds__(256) chol_solve_kernel(int n, const T* __restrict__ L, int bw, const T* __restrict__ b,
-                                                        T* __restrict__ x) {
-  // forward: y = L^{-1} b, stored in x
-  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = b[i];
-  __syncthreads();
-  for (int k0 = 0; k0 < n; k0 += TB) {
+__device__ void chol_solve_smem(int n, const T* __restrict__ L, int bw, T* x, int first) {
+  const int kstart = (first / TB) * TB;
+  for (int k0 = kstart; k0 < n; k0 += TB) {
     const int nb = min(TB, n - k0);
     if (threadIdx.x < 32) {
-      // one warp solves the diagonal block sequentially
-      for (int k = 0; k < nb; ++k) {
-        T v = x[k0 + k];
-        if (threadIdx.x == 0) {
-          v = v / L[(int64_t)(k0 + k) * n + k0 + k];
-          x[k0 + k] = v;
+      // lane r holds row r of the diagonal block in registers; the block is solved by shuffles
+      const int lane = threadIdx.x;
+      T xr = lane < nb ? x[k0 + lane] : T(0);
+      T Lrow[TB];
+#pragma unroll
+      for (int c = 0; c < TB; ++c)
+        Lrow[c] = (lane < nb && c <= lane) ? L[(int64_t)(k0 + lane) * n + k0 + c] : T(0);
+#pragma unroll
+      for (int k = 0; k < TB; ++k) {
+        if (k < nb) {
+          const T dk = __shfl_sync(0xffffffffu, Lrow[k], k);
+          const T xk = __shfl_sync(0xffffffffu, xr, k) / dk;
+          if (lane == k) xr = xk;
+          if (lane > k) xr -= Lrow[k] * xk;
         }
-        __syncwarp();
-        v = x[k0 + k];
-        const int r = k + 1 + threadIdx.x;
-        if (r < nb) x[k0 + r] -= L[(int64_t)(k0 + r) * n + k0 + k] * v;
-        __syncwarp();
       }
+      if (lane < nb) x[k0 + lane] = xr;
     }
     __syncthreads();
-    // rows below the block within the band
     const int rend = min(n, k0 + nb + bw);
     for (int r = k0 + nb + threadIdx.x; r < rend; r += blockDim.x) {
-      T s = T(0);
-      for (int c = 0; c < nb; ++c) s += L[(int64_t)r * n + k0 + c] * x[k0 + c];
-      x[r] -= s;
+      T acc = T(0);
+      const T* Lr = L + (int64_t)r * n + k0;
+      for (int c = 0; c < nb; ++c) acc += Lr[c] * x[k0 + c];
+      x[r] -= acc;
     }
     __syncthreads();
   }
-  // backward: x = L^{-T} y
   const int nblk = (n + TB - 1) / TB;
   for (int kb = nblk - 1; kb >= 0; --kb) {
     const int k0 = kb * TB;
     const int nb = min(TB, n - k0);
     if (threadIdx.x < 32) {
-      for (int k = nb - 1; k >= 0; --k) {
-        if (threadIdx.x == 0) x[k0 + k] = x[k0 + k] / L[(int64_t)(k0 + k) * n + k0 + k];
-        __syncwarp();
-        const T v = x[k0 + k];
-        const int r = threadIdx.x;
-        if (r < k) x[k0 + r] -= L[(int64_t)(k0 + k) * n + k0 + r] * v;
-        __syncwarp();
+      // lane c holds column c of the diagonal block (L^T is solved by columns)
+      const int lane = threadIdx.x;
+      T xr = lane < nb ? x[k0 + lane] : T(0);
+      T Lcol[TB];
+#pragma unroll
+      for (int r = 0; r < TB; ++r)
+        Lcol[r] = (lane < nb && r < nb && r >= lane) ? L[(int64_t)(k0 + r) * n + k0 + lane] : T(0);
+#pragma unroll
+      for (int k = TB - 1; k >= 0; --k) {
+        if (k < nb) {
+          const T dk = __shfl_sync(0xffffffffu, Lcol[k], k);
+          const T xk = __shfl_sync(0xffffffffu, xr, k) / dk;
+          if (lane == k) xr = xk;
+          if (lane < k) xr -= Lcol[k] * xk;
+        }
       }
+      if (lane < nb) x[k0 + lane] = xr;
     }
     __syncthreads();
-    // columns above the block within the band: x[c] -= sum_r L[r][c] x[r] for rows r in this block
     const int cbeg = max(0, k0 - bw);
     for (int c = cbeg + threadIdx.x; c < k0; c += blockDim.x) {
-      T s = T(0);
-      for (int r = 0; r < nb; ++r) s += L[(int64_t)(k0 + r) * n + c] * x[k0 + r];
-      x[c] -= s;
+      T acc = T(0);
+      for (int r = 0; r < nb; ++r) acc += L[(int64_t)(k0 + r) * n + c] * x[k0 + r];
+      x[c] -= acc;
     }
     __syncthreads();
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) chol_solve_kernel(int n, const T* __restrict__ L, int bw, const T* __restrict__ b,
+                                                        T* __restrict__ x) {
+  extern __shared__ __align__(16) unsigned char c_smem[];
+  T* xs = reinterpret_cast<T*>(c_smem);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = b[i];
+  __syncthreads();
+  chol_solve_smem<T>(n, L, bw, xs, 0);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xs[i];
+}
+
+// Row j of A^{-1} (= column j, A symmetric) by one CTA per row: solve A x = e_j with the factor.
+__global__ void __launch_bounds__(256) chol_inverse_kernel(int n, const double* __restrict__ L, int bw,
+                                                          double* __restrict__ Ainv) {
+  extern __shared__ __align__(16) unsigned char c_smem[];
+  double* xs = reinterpret_cast<double*>(c_smem);
+  const int j = blockIdx.x;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = i == j ? 1.0 : 0.0;
+  __syncthreads();
+  chol_solve_smem<double>(n, L, bw, xs, j);
+  double* row = Ainv + (int64_t)j * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) row[i] = xs[i];
+}
+
+// y = A x for a dense row-major n x n matrix, one warp per row (coalesced along the row).
+template <typename T>
+__global__ void dense_gemv_kernel(int n, const T* __restrict__ A, const T* __restrict__ x, T* __restrict__ y) {
+  const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const T* row = A + (int64_t)warp * n;
+  double acc = 0.0;
+  for (int c = lane; c < n; c += 32) acc = fma((double)row[c], (double)x[c], acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) y[warp] = (T)acc;
 }
 
 }  // namespace pmg
@@ -483,6 +552,24 @@ int pmg_convert(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y,
   return check_launch();
 }
 
+int pmg_convert_dscale(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, const double* s, int inverse,
+                       void* stream) {
+  if (n < 0 || !x || !y || !s) return PMG_BAD_ARG;
+  cudaStream_t st = as_stream(stream);
+  const unsigned g = stream_blocks(n);
+  if (src_dtype == PMG_F64 && dst_dtype == PMG_F32)
+    convert_dscale_kernel<double, float><<<g, 256, 0, st>>>(n, (const double*)x, (float*)y, s, inverse);
+  else if (src_dtype == PMG_F32 && dst_dtype == PMG_F64)
+    convert_dscale_kernel<float, double><<<g, 256, 0, st>>>(n, (const float*)x, (double*)y, s, inverse);
+  else if (src_dtype == PMG_F64 && dst_dtype == PMG_F64)
+    convert_dscale_kernel<double, double><<<g, 256, 0, st>>>(n, (const double*)x, (double*)y, s, inverse);
+  else if (src_dtype == PMG_F32 && dst_dtype == PMG_F32)
+    convert_dscale_kernel<float, float><<<g, 256, 0, st>>>(n, (const float*)x, (float*)y, s, inverse);
+  else
+    return PMG_BAD_ARG;
+  return check_launch();
+}
+
 int pmg_add_f32_to_f64(int64_t n, double* x, const float* d, double a, void* stream) {
   if (n < 0 || !x || !d) return PMG_BAD_ARG;
   add_f32_to_f64_kernel<<<stream_blocks(n), 256, 0, as_stream(stream)>>>(n, x, d, a);
@@ -512,11 +599,10 @@ int pmg_cholesky_factor(int n, double* A, int bw, int* info, void* stream) {
   const int nblk = (n + TB - 1) / TB;
   const int band_tiles = min(nblk, bw / TB + 2);
   for (int kb = 0; kb < nblk; ++kb) {
-    chol_diag_kernel<<<1, 256, 0, st>>>(n, A, kb, info);
+    chol_diag_panel_kernel<<<1, CHOL_THREADS, 0, st>>>(n, A, kb, bw, info);
     const int rem = nblk - kb - 1;
     if (rem <= 0) break;
     const int pt = min(rem, band_tiles);
-    chol_panel_kernel<<<pt, TB, 0, st>>>(n, A, kb, bw);
     chol_update_kernel<<<pt * pt, 256, 0, st>>>(n, A, kb, bw, pt);
     const int rc = check_launch();
     if (rc != PMG_OK) return rc;
@@ -524,15 +610,55 @@ int pmg_cholesky_factor(int n, double* A, int bw, int* info, void* stream) {
   return check_launch();
 }
 
-int pmg_cholesky_solve(int dtype, int n, const void* L, int bw, const void* b, void* x, void* stream) {
-  if (n <= 0 || !L || !b || !x || bw < 0 || b == x) return PMG_BAD_ARG;
+int pmg_cholesky_inverse(int n, const double* L, int bw, double* Ainv, void* stream) {
+  if (n <= 0 || n > CHOL_SMEM_MAX_N || !L || !Ainv || bw < 0 || (const void*)L == (const void*)Ainv) return PMG_BAD_ARG;
+  const size_t smem = sizeof(double) * (size_t)n;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(chol_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      set_error(cudaGetErrorString(e));
+      return PMG_CUDA_ERR;
+    }
+  }
+  chol_inverse_kernel<<<(unsigned)n, 256, smem, as_stream(stream)>>>(n, L, bw, Ainv);
+  return check_launch();
+}
+
+int pmg_dense_gemv(int dtype, int n, const void* A, const void* x, void* y, void* stream) {
+  if (n <= 0 || !A || !x || !y || x == y) return PMG_BAD_ARG;
+  const unsigned blocks = (unsigned)(((int64_t)n * 32 + 255) / 256);
   cudaStream_t st = as_stream(stream);
   if (dtype == PMG_F64)
-    chol_solve_kernel<double><<<1, 256, 0, st>>>(n, (const double*)L, bw, (const double*)b, (double*)x);
+    dense_gemv_kernel<double><<<blocks, 256, 0, st>>>(n, (const double*)A, (const double*)x, (double*)y);
   else if (dtype == PMG_F32)
-    chol_solve_kernel<float><<<1, 256, 0, st>>>(n, (const float*)L, bw, (const float*)b, (float*)x);
+    dense_gemv_kernel<float><<<blocks, 256, 0, st>>>(n, (const float*)A, (const float*)x, (float*)y);
   else
     return PMG_BAD_ARG;
+  return check_launch();
+}
+
+int pmg_cholesky_solve(int dtype, int n, const void* L, int bw, const void* b, void* x, void* stream) {
+  if (n <= 0 || n > CHOL_SMEM_MAX_N || !L || !b || !x || bw < 0 || b == x) return PMG_BAD_ARG;
+  cudaStream_t st = as_stream(stream);
+  const size_t smem = (dtype == PMG_F64 ? sizeof(double) : sizeof(float)) * (size_t)n;
+  cudaError_t e = cudaSuccess;
+  if (dtype == PMG_F64) {
+    if (smem > 48 * 1024)
+      e = cudaFuncSetAttribute(chol_solve_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      chol_solve_kernel<double><<<1, 256, smem, st>>>(n, (const double*)L, bw, (const double*)b, (double*)x);
+  } else if (dtype == PMG_F32) {
+    if (smem > 48 * 1024)
+      e = cudaFuncSetAttribute(chol_solve_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      chol_solve_kernel<float><<<1, 256, smem, st>>>(n, (const float*)L, bw, (const float*)b, (float*)x);
+  } else {
+    return PMG_BAD_ARG;
+  }
+  if (e != cudaSuccess) {
+    set_error(cudaGetErrorString(e));
+    return PMG_CUDA_ERR;
+  }
   return check_launch();
 }
 

@@ -98,6 +98,110 @@ __global__ void __launch_bounds__(128) ebe_apply_kernel(Grid g, const T* __restr
   }
 }
 
+// 3D tiled variant: a CTA owns a BX x BY x BZ brick of nodes.  It stages the u of the brick plus a one-node
+// halo in shared memory (Dirichlet components and nodes outside the grid stored as zero) and the x_e of
+// the (BX+1)(BY+1)(BZ+1) surrounding elements (zero outside the grid), so every thread reads its 27
+// neighbours and 8 elements at constant shared-memory offsets with no bounds or mask logic.
+constexpr int TBX = 32, TBY = 4, TBZ = 2;
+
+// Shared-memory loads the compiler may not re-issue at every use: the 81 neighbour values are read once
+// and stay in registers for the 600 FMAs (otherwise it rematerialises a shared load per FMA).
+__device__ __forceinline__ float lds_keep(const float* p) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"((unsigned)__cvta_generic_to_shared(p)));
+  return v;
+}
+__device__ __forceinline__ double lds_keep(const double* p) {
+  double v;
+  asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"((unsigned)__cvta_generic_to_shared(p)));
+  return v;
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(TBX * TBY * TBZ) ebe_apply_tiled_kernel(Grid g, const T* __restrict__ xe,
+                                                                         ElemMat<T, 24> K0,
+                                                                         const uint8_t* __restrict__ bcmask, T bcdiag,
+                                                                         const T* __restrict__ u, const T* __restrict__ b,
+                                                                         const T* __restrict__ diag, T w,
+                                                                         T* __restrict__ y) {
+  constexpr int UX = TBX + 2, UY = TBY + 2, UZ = TBZ + 2;   // node tile with halo
+  constexpr int EX = TBX + 1, EY = TBY + 1, EZ = TBZ + 1;   // element tile
+  constexpr int NT = TBX * TBY * TBZ;
+  __shared__ T su[UZ][UY][UX][3];
+  __shared__ T sx[EZ][EY][EX];
+  const int i0 = blockIdx.x * TBX, j0 = blockIdx.y * TBY, k0 = blockIdx.z * TBZ;
+  const int tid = threadIdx.x + TBX * (threadIdx.y + TBY * threadIdx.z);
+  // stage u (coalesced along x: consecutive q -> consecutive component, then node)
+  for (int q = tid; q < UX * UY * UZ * 3; q += NT) {
+    const int c = q % 3, t = q / 3;
+    const int lx = t % UX, ly = (t / UX) % UY, lz = t / (UX * UY);
+    const int gi = i0 - 1 + lx, gj = j0 - 1 + ly, gk = k0 - 1 + lz;
+    T v = T(0);
+    if (gi >= 0 && gi <= g.nx && gj >= 0 && gj <= g.ny && gk >= 0 && gk <= g.nz) {
+      const int64_t m = node_id(g, gi, gj, gk);
+      const uint8_t msk = bcmask ? bcmask[m] : 0;
+      if (!((msk >> c) & 1)) v = u[m * 3 + c];
+    }
+    (&su[0][0][0][0])[q] = v;
+  }
+  for (int q = tid; q < EX * EY * EZ; q += NT) {
+    const int lx = q % EX, ly = (q / EX) % EY, lz = q / (EX * EY);
+    const int gi = i0 - 1 + lx, gj = j0 - 1 + ly, gk = k0 - 1 + lz;
+    T v = T(0);
+    if (gi >= 0 && gi < g.nx && gj >= 0 && gj < g.ny && gk >= 0 && gk < g.nz) v = xe[elem_id(g, gi, gj, gk)];
+    (&sx[0][0][0])[q] = v;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
+  const int i = i0 + tx, j = j0 + ty, k = k0 + tz;
+  if (i > g.nx || j > g.ny || k > g.nz) return;
+  T un[27][3];
+#pragma unroll
+  for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) un[(dz * 3 + dy) * 3 + dx][c] = lds_keep(&su[tz + dz][ty + dy][tx + dx][c]);
+  T acc[3] = {T(0), T(0), T(0)};
+#pragma unroll
+  for (int oz = 0; oz < 2; ++oz)
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+      for (int ox = 0; ox < 2; ++ox) {
+        const T x = lds_keep(&sx[tz + oz][ty + oy][tx + ox]);
+        const int ln = (1 - ox) + 2 * (1 - oy) + 4 * (1 - oz);
+        T t[3] = {T(0), T(0), T(0)};
+#pragma unroll
+        for (int lb = 0; lb < 8; ++lb) {
+          const int o = ((oz + ((lb >> 2) & 1)) * 3 + (oy + ((lb >> 1) & 1))) * 3 + (ox + (lb & 1));
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) t[d] = fma(K0.v[(ln * 3 + d) * 24 + lb * 3 + c], un[o][c], t[d]);
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) acc[d] = fma(x, t[d], acc[d]);
+      }
+  const int64_t n = node_id(g, i, j, k);
+  const uint8_t mymask = bcmask ? bcmask[n] : 0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int64_t q = n * 3 + d;
+    const T uq = u[q];
+    const T Au = ((mymask >> d) & 1) ? bcdiag * uq : acc[d];
+    if (MODE == 0) {
+      y[q] = Au;
+    } else if (MODE == 1) {
+      y[q] = b[q] - Au;
+    } else {
+      y[q] = uq + w * ((b[q] - Au) / diag[q]);
+    }
+  }
+}
+
 template <typename T, int DIM>
 __global__ void ebe_diag_kernel(Grid g, const T* __restrict__ xe, ElemMat<T, Traits<DIM>::NDE> K0,
                                 const uint8_t* __restrict__ bcmask, T bcdiag, T* __restrict__ diag) {
@@ -128,43 +232,37 @@ __global__ void ebe_diag_kernel(Grid g, const T* __restrict__ xe, ElemMat<T, Tra
 }
 
 // ------------------------------------------------------------------------------------------ stencils
+// One thread per (component d, node n), d slowest so that the stencil loads of a warp are coalesced.
+// Neighbours outside the grid are read at a clamped (valid) index: their stencil entries are exactly zero,
+// so the loads need no branches and can all be in flight together.
 template <typename T, int DIM, int MODE>
-__global__ void __launch_bounds__(128) stencil_apply_kernel(Grid g, const T* __restrict__ S, const T* __restrict__ u,
+__global__ void __launch_bounds__(256) stencil_apply_kernel(Grid g, const T* __restrict__ S, const T* __restrict__ u,
                                                             const T* __restrict__ b, const T* __restrict__ diag, T w,
                                                             T* __restrict__ y) {
   constexpr int NOFF = Traits<DIM>::NOFF;
-  const int64_t nn = g.nnodes();
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= nn) return;
+  const int nn = (int)g.nnodes();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nn * DIM) return;
+  const int d = t / nn, n = t - d * nn;
   int i, j, k;
   node_ijk(g, n, i, j, k);
-  T acc[DIM];
-#pragma unroll
-  for (int d = 0; d < DIM; ++d) acc[d] = T(0);
+  T acc = T(0);
 #pragma unroll
   for (int o = 0; o < NOFF; ++o) {
     const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dz = DIM == 3 ? o / 9 - 1 : 0;
-    const int ii = i + dx, jj = j + dy, kk = k + dz;
-    if (ii < 0 || ii > g.nx || jj < 0 || jj > g.ny || kk < 0 || kk > g.nz) continue;
-    const int64_t m = node_id(g, ii, jj, kk);
-    T um[DIM];
+    const int ii = min(max(i + dx, 0), g.nx), jj = min(max(j + dy, 0), g.ny), kk = min(max(k + dz, 0), g.nz);
+    const int m = (kk * (g.ny + 1) + jj) * (g.nx + 1) + ii;
+    const T* Sd = S + (int64_t)((o * DIM + d) * DIM) * nn + n;
 #pragma unroll
-    for (int c = 0; c < DIM; ++c) um[c] = u[m * DIM + c];
-#pragma unroll
-    for (int d = 0; d < DIM; ++d)
-#pragma unroll
-      for (int c = 0; c < DIM; ++c) acc[d] = fma(S[((int64_t)(o * DIM + d) * DIM + c) * nn + n], um[c], acc[d]);
+    for (int c = 0; c < DIM; ++c) acc = fma(Sd[(int64_t)c * nn], u[(int64_t)m * DIM + c], acc);
   }
-#pragma unroll
-  for (int d = 0; d < DIM; ++d) {
-    const int64_t q = n * DIM + d;
-    if (MODE == 0) {
-      y[q] = acc[d];
-    } else if (MODE == 1) {
-      y[q] = b[q] - acc[d];
-    } else {
-      y[q] = u[q] + w * ((b[q] - acc[d]) / diag[q]);
-    }
+  const int64_t q = (int64_t)n * DIM + d;
+  if (MODE == 0) {
+    y[q] = acc;
+  } else if (MODE == 1) {
+    y[q] = b[q] - acc;
+  } else {
+    y[q] = u[q] + w * ((b[q] - acc) / diag[q]);
   }
 }
 
@@ -182,17 +280,18 @@ __global__ void stencil_diag_kernel(Grid g, const T* __restrict__ S, T* __restri
 // weight of a fine node at signed offset a (in fine units) from a coarse node: 1 at 0, 1/2 at +-1
 __device__ __forceinline__ double tw(int a) { return a == 0 ? 1.0 : 0.5; }
 
-// rc = R^T rf, one thread per coarse node (gather over the 3^dim fine neighbourhood)
+// rc = R^T rf: one thread per (component d, coarse node N), gathering the 3^dim fine neighbours of the
+// coarse node with branch-free clamped loads (weight zero outside the grid).
 template <typename T, int DIM>
-__global__ void restrict_kernel(Grid gf, const T* __restrict__ rf, T* __restrict__ rc) {
+__global__ void __launch_bounds__(256) restrict_kernel(Grid gf, const T* __restrict__ rf, T* __restrict__ rc) {
   const Grid gc = gf.coarse();
-  const int64_t N = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (N >= gc.nnodes()) return;
+  const int ncn = (int)gc.nnodes();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncn * DIM) return;
+  const int d = t / ncn, N = t - d * ncn;
   int I, J, K;
   node_ijk(gc, N, I, J, K);
-  T acc[DIM];
-#pragma unroll
-  for (int d = 0; d < DIM; ++d) acc[d] = T(0);
+  T acc = T(0);
 #pragma unroll
   for (int c = (DIM == 3 ? -1 : 0); c <= (DIM == 3 ? 1 : 0); ++c)
 #pragma unroll
@@ -200,39 +299,43 @@ __global__ void restrict_kernel(Grid gf, const T* __restrict__ rf, T* __restrict
 #pragma unroll
       for (int a = -1; a <= 1; ++a) {
         const int i = 2 * I + a, j = 2 * J + bb, k = 2 * K + c;
-        if (i < 0 || i > gf.nx || j < 0 || j > gf.ny || k < 0 || k > gf.nz) continue;
-        const T wgt = (T)(tw(a) * tw(bb) * tw(c));
-        const int64_t m = node_id(gf, i, j, k);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) acc[d] = fma(wgt, rf[m * DIM + d], acc[d]);
+        const bool in = i >= 0 && i <= gf.nx && j >= 0 && j <= gf.ny && k >= 0 && k <= gf.nz;
+        const T wgt = in ? (T)(tw(a) * tw(bb) * tw(c)) : T(0);
+        const int m = (min(max(k, 0), gf.nz) * (gf.ny + 1) + min(max(j, 0), gf.ny)) * (gf.nx + 1) + min(max(i, 0), gf.nx);
+        acc = fma(wgt, rf[(int64_t)m * DIM + d], acc);
       }
-#pragma unroll
-  for (int d = 0; d < DIM; ++d) rc[N * DIM + d] = acc[d];
+  rc[(int64_t)N * DIM + d] = acc;
 }
 
-// uf += R uc, one thread per fine node (gather over the <= 2^dim coarse parents)
+// uf += R uc: one thread per (component d, fine node n); the 2^dim candidate parents are read at clamped
+// indices with weight zero where a parent does not exist (even coordinate).
 template <typename T, int DIM>
-__global__ void prolong_add_kernel(Grid gf, const T* __restrict__ uc, T* __restrict__ uf) {
+__global__ void __launch_bounds__(256) prolong_add_kernel(Grid gf, const T* __restrict__ uc, T* __restrict__ uf) {
   const Grid gc = gf.coarse();
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= gf.nnodes()) return;
+  const int nfn = (int)gf.nnodes();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nfn * DIM) return;
+  const int d = t / nfn, n = t - d * nfn;
   int i, j, k;
   node_ijk(gf, n, i, j, k);
-  T acc[DIM];
-#pragma unroll
-  for (int d = 0; d < DIM; ++d) acc[d] = T(0);
   const int i0 = i >> 1, j0 = j >> 1, k0 = k >> 1;
-  const int ni = (i & 1) + 1, nj = (j & 1) + 1, nk = (DIM == 3) ? (k & 1) + 1 : 1;
-  for (int c = 0; c < nk; ++c)
-    for (int bb = 0; bb < nj; ++bb)
-      for (int a = 0; a < ni; ++a) {
-        const T wgt = (T)((ni == 2 ? 0.5 : 1.0) * (nj == 2 ? 0.5 : 1.0) * (nk == 2 ? 0.5 : 1.0));
-        const int64_t M = node_id(gc, i0 + a, j0 + bb, k0 + c);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) acc[d] = fma(wgt, uc[M * DIM + d], acc[d]);
-      }
-#pragma unroll
-  for (int d = 0; d < DIM; ++d) uf[n * DIM + d] += acc[d];
+  const int i1 = i0 + (i & 1), j1 = j0 + (j & 1), k1 = k0 + (k & 1);
+  const T wx0 = (i & 1) ? T(0.5) : T(1), wx1 = (i & 1) ? T(0.5) : T(0);
+  const T wy0 = (j & 1) ? T(0.5) : T(1), wy1 = (j & 1) ? T(0.5) : T(0);
+  const T wz0 = (DIM == 3 && (k & 1)) ? T(0.5) : T(1), wz1 = (DIM == 3 && (k & 1)) ? T(0.5) : T(0);
+  const int cx = gc.nx + 1, cxy = (gc.nx + 1) * (gc.ny + 1);
+  T acc = T(0);
+  acc = fma(wz0 * wy0 * wx0, uc[(int64_t)(k0 * cxy + j0 * cx + i0) * DIM + d], acc);
+  acc = fma(wz0 * wy0 * wx1, uc[(int64_t)(k0 * cxy + j0 * cx + i1) * DIM + d], acc);
+  acc = fma(wz0 * wy1 * wx0, uc[(int64_t)(k0 * cxy + j1 * cx + i0) * DIM + d], acc);
+  acc = fma(wz0 * wy1 * wx1, uc[(int64_t)(k0 * cxy + j1 * cx + i1) * DIM + d], acc);
+  if (DIM == 3) {
+    acc = fma(wz1 * wy0 * wx0, uc[(int64_t)(k1 * cxy + j0 * cx + i0) * DIM + d], acc);
+    acc = fma(wz1 * wy0 * wx1, uc[(int64_t)(k1 * cxy + j0 * cx + i1) * DIM + d], acc);
+    acc = fma(wz1 * wy1 * wx0, uc[(int64_t)(k1 * cxy + j1 * cx + i0) * DIM + d], acc);
+    acc = fma(wz1 * wy1 * wx1, uc[(int64_t)(k1 * cxy + j1 * cx + i1) * DIM + d], acc);
+  }
+  uf[(int64_t)n * DIM + d] += acc;
 }
 
 // ------------------------------------------------------------------------------------------ Galerkin
@@ -301,39 +404,57 @@ __global__ void galerkin_from_ebe_kernel(Grid gf, const T* __restrict__ xe, Elem
   __shared__ T E[NE];
   __shared__ T Kc[NE];
   __shared__ T buf[NE];
-  __shared__ uint8_t cmask[NN];
-  __shared__ int any_bc;
+  __shared__ T xs[NN];
+  __shared__ uint8_t cmask[NN][NN];
   const Grid gc = gf.coarse();
-  const int64_t ec = blockIdx.x;
-  const int CI = (int)(ec % gc.nx), CJ = (int)((ec / gc.nx) % gc.ny), CK = (int)(ec / ((int64_t)gc.nx * gc.ny));
+  const int ec = blockIdx.x;
+  const int CI = ec % gc.nx, CJ = (ec / gc.nx) % gc.ny, CK = ec / (gc.nx * gc.ny);
+  // masks of all children's nodes and the children's x in one pass, then one vote
+  int mine = 0;
+  if (threadIdx.x < NN * NN) {
+    const int sc = threadIdx.x / NN, a = threadIdx.x % NN;
+    const int ni = 2 * CI + (sc & 1) + (a & 1), nj = 2 * CJ + ((sc >> 1) & 1) + ((a >> 1) & 1);
+    const int nk = DIM == 3 ? 2 * CK + ((sc >> 2) & 1) + ((a >> 2) & 1) : 0;
+    const uint8_t m = bcmask ? bcmask[node_id(gf, ni, nj, nk)] : 0;
+    cmask[sc][a] = m;
+    mine = m != 0;
+  }
+  if (threadIdx.x < NN) {
+    const int sc = threadIdx.x;
+    xs[sc] = xe[elem_id(gf, 2 * CI + (sc & 1), 2 * CJ + ((sc >> 1) & 1), DIM == 3 ? 2 * CK + ((sc >> 2) & 1) : 0)];
+  }
+  const int any_bc = __syncthreads_or(mine);
+  if (!any_bc) {
+    // every child unconstrained: E = sum_c x_c (M_c^T K0 M_c), straight to global memory
+    for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+      T v = T(0);
+#pragma unroll
+      for (int sc = 0; sc < NN; ++sc) v = fma(xs[sc], table[sc * NE + e], v);
+      Ec[(int64_t)ec * NE + e] = v;
+    }
+    return;
+  }
   for (int e = threadIdx.x; e < NE; e += blockDim.x) E[e] = T(0);
   __syncthreads();
   for (int s = 0; s < NN; ++s) {
     const int fi = 2 * CI + (s & 1), fj = 2 * CJ + ((s >> 1) & 1), fk = DIM == 3 ? 2 * CK + ((s >> 2) & 1) : 0;
-    const T x = xe[elem_id(gf, fi, fj, fk)];
-    if (threadIdx.x == 0) any_bc = 0;
-    __syncthreads();
-    if (threadIdx.x < NN) {
-      const int a = threadIdx.x;
-      const int ni = fi + (a & 1), nj = fj + ((a >> 1) & 1), nk = DIM == 3 ? fk + ((a >> 2) & 1) : 0;
-      const uint8_t m = bcmask ? bcmask[node_id(gf, ni, nj, nk)] : 0;
-      cmask[a] = m;
-      if (m) atomicOr(&any_bc, 1);
-    }
-    __syncthreads();
-    if (!any_bc) {
+    const T x = xs[s];
+    bool child_bc = false;
+#pragma unroll
+    for (int a = 0; a < NN; ++a) child_bc |= cmask[s][a] != 0;
+    if (!child_bc) {
       for (int e = threadIdx.x; e < NE; e += blockDim.x) E[e] = fma(x, table[s * NE + e], E[e]);
       __syncthreads();
       continue;
     }
-    // masked child matrix x Z K0 Z + bcdiag on assigned Dirichlet dofs
+    // masked child matrix x Z K0 Z + bcdiag on the Dirichlet dofs assigned to this fine element (each fine
+    // node is assigned to element (min(i, nx-1), min(j, ny-1), min(k, nz-1)))
     for (int e = threadIdx.x; e < NE; e += blockDim.x) {
       const int r = e / NDE, c = e % NDE;
       const int rn = r / DIM, rd = r % DIM, cn = c / DIM, cd = c % DIM;
-      const bool rb = (cmask[rn] >> rd) & 1, cb = (cmask[cn] >> cd) & 1;
+      const bool rb = (cmask[s][rn] >> rd) & 1, cb = (cmask[s][cn] >> cd) & 1;
       T v = (rb || cb) ? T(0) : x * K0.v[e];
       if (r == c && rb) {
-        // assigned to this fine element?
         const int ni = fi + (rn & 1), nj = fj + ((rn >> 1) & 1), nk = DIM == 3 ? fk + ((rn >> 2) & 1) : 0;
         const int ai = min(ni, gf.nx - 1), aj = min(nj, gf.ny - 1), ak = DIM == 3 ? min(nk, gf.nz - 1) : 0;
         if (ai == fi && aj == fj && ak == fk) v = bcdiag;
@@ -343,31 +464,66 @@ __global__ void galerkin_from_ebe_kernel(Grid gf, const T* __restrict__ xe, Elem
     __syncthreads();
     galerkin_child_accumulate<T, DIM>(E, Kc, buf, s);
   }
-  for (int e = threadIdx.x; e < NE; e += blockDim.x) Ec[ec * NE + e] = E[e];
+  for (int e = threadIdx.x; e < NE; e += blockDim.x) Ec[(int64_t)ec * NE + e] = E[e];
 }
 
-// Next-level coarse element matrices from element matrices Ef of grid gf.
+// Next-level coarse element matrices from element matrices Ef of grid gf.  The CTA stages all 2^dim child
+// matrices in shared memory and transforms them together (M_c^T E_c M_c by sum factorisation, one axis per
+// pass, 2*dim passes), then sums the children: 2*dim + 2 barriers per coarse element.
 template <typename T, int DIM>
 __global__ void galerkin_from_elements_kernel(Grid gf, const T* __restrict__ Ef, T* __restrict__ Ec) {
   constexpr int NN = Traits<DIM>::NN;
   constexpr int NDE = Traits<DIM>::NDE;
   constexpr int NE = NDE * NDE;
-  __shared__ T E[NE];
-  __shared__ T Kc[NE];
-  __shared__ T buf[NE];
+  extern __shared__ __align__(16) unsigned char g_smem[];
+  T* A = reinterpret_cast<T*>(g_smem);
+  T* B = A + NN * NE;
   const Grid gc = gf.coarse();
-  const int64_t ec = blockIdx.x;
-  const int CI = (int)(ec % gc.nx), CJ = (int)((ec / gc.nx) % gc.ny), CK = (int)(ec / ((int64_t)gc.nx * gc.ny));
-  for (int e = threadIdx.x; e < NE; e += blockDim.x) E[e] = T(0);
-  __syncthreads();
-  for (int s = 0; s < NN; ++s) {
-    const int fi = 2 * CI + (s & 1), fj = 2 * CJ + ((s >> 1) & 1), fk = DIM == 3 ? 2 * CK + ((s >> 2) & 1) : 0;
-    const T* src = Ef + elem_id(gf, fi, fj, fk) * NE;
-    for (int e = threadIdx.x; e < NE; e += blockDim.x) Kc[e] = src[e];
-    __syncthreads();
-    galerkin_child_accumulate<T, DIM>(E, Kc, buf, s);
+  const int ec = blockIdx.x;
+  const int CI = ec % gc.nx, CJ = (ec / gc.nx) % gc.ny, CK = ec / (gc.nx * gc.ny);
+  for (int idx = threadIdx.x; idx < NN * NE; idx += blockDim.x) {
+    const int sc = idx / NE, e = idx - sc * NE;
+    const int64_t child = elem_id(gf, 2 * CI + (sc & 1), 2 * CJ + ((sc >> 1) & 1), DIM == 3 ? 2 * CK + ((sc >> 2) & 1) : 0);
+    A[idx] = Ef[child * NE + e];
   }
-  for (int e = threadIdx.x; e < NE; e += blockDim.x) Ec[ec * NE + e] = E[e];
+  __syncthreads();
+  T* src = A;
+  T* dst = B;
+#pragma unroll 1
+  for (int side = 0; side < 2; ++side) {
+#pragma unroll 1
+    for (int axis = 0; axis < DIM; ++axis) {
+      for (int idx = threadIdx.x; idx < NN * NE; idx += blockDim.x) {
+        const int sc = idx / NE, e = idx - sc * NE;
+        const int sa = (sc >> axis) & 1;
+        const int r = e / NDE, c = e - r * NDE;
+        const int q = side == 0 ? r : c;
+        const int node = q / DIM, d = q - node * DIM;
+        const int Ab = (node >> axis) & 1;
+        const T* S = src + sc * NE;
+        T v = T(0);
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+          const double wgt = p1(sa, a, Ab);
+          if (wgt != 0.0) {
+            const int qa = ((node & ~(1 << axis)) | (a << axis)) * DIM + d;
+            v = fma((T)wgt, S[side == 0 ? qa * NDE + c : r * NDE + qa], v);
+          }
+        }
+        dst[idx] = v;
+      }
+      __syncthreads();
+      T* t = src;
+      src = dst;
+      dst = t;
+    }
+  }
+  for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+    T v = T(0);
+#pragma unroll
+    for (int sc = 0; sc < NN; ++sc) v += src[sc * NE + e];
+    Ec[(int64_t)ec * NE + e] = v;
+  }
 }
 
 // Node stencils from element matrices: thread per (offset o, node n).
@@ -412,6 +568,60 @@ __global__ void stencil_from_elements_kernel(Grid g, const T* __restrict__ E, T*
     for (int c = 0; c < DIM; ++c) S[((int64_t)(o * DIM + d) * DIM + c) * nn + n] = acc[d * DIM + c];
 }
 
+// Level-0 node stencils of K(x) (Dirichlet rows: bcdiag on the diagonal only; Dirichlet columns: zero).
+// Thread per (offset o, node n): sums x_e K0[ln, lm] over the elements containing n and m = n + o.
+template <typename T, int DIM>
+__global__ void ebe_stencil_kernel(Grid g, const T* __restrict__ xe, ElemMat<T, Traits<DIM>::NDE> K0,
+                                   const uint8_t* __restrict__ bcmask, T bcdiag, T* __restrict__ S) {
+  constexpr int NDE = Traits<DIM>::NDE;
+  constexpr int NOFF = Traits<DIM>::NOFF;
+  constexpr int CENTER = DIM == 3 ? 13 : 4;
+  const int64_t nn = g.nnodes();
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nn * NOFF) return;
+  const int o = (int)(t / nn);
+  const int64_t n = t % nn;
+  int i, j, k;
+  node_ijk(g, n, i, j, k);
+  const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dz = DIM == 3 ? o / 9 - 1 : 0;
+  const int ii = i + dx, jj = j + dy, kk = k + dz;
+  const bool nbr_in = ii >= 0 && ii <= g.nx && jj >= 0 && jj <= g.ny && kk >= 0 && kk <= g.nz;
+  const uint8_t mrow = bcmask ? bcmask[n] : 0;
+  const uint8_t mcol = (bcmask && nbr_in) ? bcmask[node_id(g, ii, jj, kk)] : 0;
+  T acc[DIM * DIM];
+#pragma unroll
+  for (int q = 0; q < DIM * DIM; ++q) acc[q] = T(0);
+  if (nbr_in) {
+#pragma unroll
+    for (int oz = 0; oz < (DIM == 3 ? 2 : 1); ++oz)
+#pragma unroll
+      for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+        for (int ox = 0; ox < 2; ++ox) {
+          const int ei = i - 1 + ox, ej = j - 1 + oy, ek = DIM == 3 ? k - 1 + oz : 0;
+          if (ei < 0 || ei >= g.nx || ej < 0 || ej >= g.ny || ek < 0 || ek >= g.ez()) continue;
+          const int lx = 1 - ox, ly = 1 - oy, lz = DIM == 3 ? 1 - oz : 0;
+          const int mx = lx + dx, my = ly + dy, mz = lz + dz;
+          if (mx < 0 || mx > 1 || my < 0 || my > 1 || mz < 0 || mz > 1) continue;
+          const int ln = lx + 2 * ly + 4 * lz, lm = mx + 2 * my + 4 * mz;
+          const T x = xe[elem_id(g, ei, ej, ek)];
+#pragma unroll
+          for (int d = 0; d < DIM; ++d)
+#pragma unroll
+            for (int c = 0; c < DIM; ++c) acc[d * DIM + c] = fma(x, K0.v[(ln * DIM + d) * NDE + lm * DIM + c], acc[d * DIM + c]);
+        }
+  }
+#pragma unroll
+  for (int d = 0; d < DIM; ++d)
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      T v = acc[d * DIM + c];
+      if (((mrow >> d) & 1) || ((mcol >> c) & 1)) v = T(0);
+      if (((mrow >> d) & 1) && o == CENTER && c == d) v = bcdiag;
+      S[((int64_t)(o * DIM + d) * DIM + c) * nn + n] = v;
+    }
+}
+
 template <typename T, int DIM>
 __global__ void stencil_to_dense_kernel(Grid g, const T* __restrict__ S, double* __restrict__ A) {
   constexpr int NOFF = Traits<DIM>::NOFF;
@@ -450,6 +660,22 @@ template <typename T, int DIM>
 int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
                 const void* u, const void* b, const void* diag, double w, void* y, cudaStream_t st) {
   auto K = make_elem_mat<T, Traits<DIM>::NDE>(K0);
+  if constexpr (DIM == 3) {
+    const dim3 block(TBX, TBY, TBZ);
+    const dim3 grid((g.nx + 1 + TBX - 1) / TBX, (g.ny + 1 + TBY - 1) / TBY, (g.nz + 1 + TBZ - 1) / TBZ);
+    const T* xe_ = (const T*)xe;
+    const T* u_ = (const T*)u;
+    const T* b_ = (const T*)b;
+    const T* d_ = (const T*)diag;
+    T* y_ = (T*)y;
+    if (mode == PMG_APPLY_MATVEC)
+      ebe_apply_tiled_kernel<T, 0><<<grid, block, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_);
+    else if (mode == PMG_APPLY_RESIDUAL)
+      ebe_apply_tiled_kernel<T, 1><<<grid, block, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_);
+    else
+      ebe_apply_tiled_kernel<T, 2><<<grid, block, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_);
+    return check_launch();
+  }
   const int threads = 128;
   const unsigned blocks = blocks_for(g.nnodes(), threads);
   const T* xe_ = (const T*)xe;
@@ -469,8 +695,8 @@ int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_
 template <typename T, int DIM>
 int stencil_apply_t(int mode, Grid g, const void* S, const void* u, const void* b, const void* diag, double w,
                     void* y, cudaStream_t st) {
-  const int threads = 128;
-  const unsigned blocks = blocks_for(g.nnodes(), threads);
+  const int threads = 256;
+  const unsigned blocks = blocks_for(g.nnodes() * DIM, threads);
   const T* S_ = (const T*)S;
   const T* u_ = (const T*)u;
   const T* b_ = (const T*)b;
@@ -575,7 +801,7 @@ int pmg_restrict(int dtype, int nelx, int nely, int nelz, const void* rf, void* 
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !even_grid(nelx, nely, nelz) || !rf || !rc) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
   PMG_DISPATCH(dtype, g.dim(),
-               (launch_simple<T, DIM>(restrict_kernel<T, DIM>, g.coarse().nnodes(), as_stream(stream), g,
+               (launch_simple<T, DIM>(restrict_kernel<T, DIM>, g.coarse().nnodes() * DIM, as_stream(stream), g,
                                       (const T*)rf, (T*)rc)));
 }
 
@@ -583,8 +809,8 @@ int pmg_prolong_add(int dtype, int nelx, int nely, int nelz, const void* uc, voi
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !even_grid(nelx, nely, nelz) || !uc || !uf) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
   PMG_DISPATCH(dtype, g.dim(),
-               (launch_simple<T, DIM>(prolong_add_kernel<T, DIM>, g.nnodes(), as_stream(stream), g, (const T*)uc,
-                                      (T*)uf)));
+               (launch_simple<T, DIM>(prolong_add_kernel<T, DIM>, g.nnodes() * DIM, as_stream(stream), g,
+                                      (const T*)uc, (T*)uf)));
 }
 
 int pmg_galerkin_table(int dim, const double* K0, double* table) {
@@ -623,7 +849,7 @@ int pmg_galerkin_from_ebe(int dtype, int nelx, int nely, int nelz, const void* x
     return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
   const unsigned nblk = (unsigned)g.coarse().nel();
-  const int threads = g.dim() == 3 ? 288 : 64;
+  const int threads = g.dim() == 3 ? 576 : 64;
   cudaStream_t st = as_stream(stream);
   PMG_DISPATCH(dtype, g.dim(), ([&]() -> int {
                  galerkin_from_ebe_kernel<T, DIM><<<nblk, threads, 0, st>>>(
@@ -637,10 +863,17 @@ int pmg_galerkin_from_elements(int dtype, int nelx, int nely, int nelz, const vo
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !even_grid(nelx, nely, nelz) || !Ef || !Ec) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
   const unsigned nblk = (unsigned)g.coarse().nel();
-  const int threads = g.dim() == 3 ? 288 : 64;
+  const int threads = g.dim() == 3 ? 576 : 128;
   cudaStream_t st = as_stream(stream);
   PMG_DISPATCH(dtype, g.dim(), ([&]() -> int {
-                 galerkin_from_elements_kernel<T, DIM><<<nblk, threads, 0, st>>>(g, (const T*)Ef, (T*)Ec);
+                 const size_t smem = 2 * sizeof(T) * Traits<DIM>::NN * Traits<DIM>::NDE * Traits<DIM>::NDE;
+                 cudaError_t e = cudaFuncSetAttribute(galerkin_from_elements_kernel<T, DIM>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                 if (e != cudaSuccess) {
+                   set_error(cudaGetErrorString(e));
+                   return PMG_CUDA_ERR;
+                 }
+                 galerkin_from_elements_kernel<T, DIM><<<nblk, threads, smem, st>>>(g, (const T*)Ef, (T*)Ec);
                  return check_launch();
                }()));
 }
@@ -652,6 +885,16 @@ int pmg_stencil_from_elements(int dtype, int nelx, int nely, int nelz, const voi
   PMG_DISPATCH(dtype, g.dim(),
                (launch_simple<T, DIM>(stencil_from_elements_kernel<T, DIM>, work, as_stream(stream), g, (const T*)E,
                                       (T*)S)));
+}
+
+int pmg_ebe_stencil(int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
+                    const uint8_t* bcmask, double bcdiag, void* S, void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !xe || !K0_host || !S) return PMG_BAD_ARG;
+  Grid g{nelx, nely, nelz};
+  const int64_t work = g.nnodes() * (g.dim() == 3 ? 27 : 9);
+  PMG_DISPATCH(dtype, g.dim(),
+               (launch_simple<T, DIM>(ebe_stencil_kernel<T, DIM>, work, as_stream(stream), g, (const T*)xe,
+                                      make_elem_mat<T, Traits<DIM>::NDE>(K0_host), bcmask, (T)bcdiag, (T*)S)));
 }
 
 int pmg_stencil_to_dense(int dtype, int nelx, int nely, int nelz, const void* S, double* A, void* stream) {

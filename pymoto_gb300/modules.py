@@ -127,20 +127,37 @@ class FilterConv(Module):
         w = np.maximum(0.0, radius - np.sqrt(X * X + Y * Y + Z * Z))
         self.weights = w / np.sum(w)
 
+    @staticmethod
+    def _inverse_map(m, n):
+        """(ptr, pos): the padded positions P with m[P] == j are pos[ptr[j]:ptr[j+1]]."""
+        order = np.argsort(m, kind="stable").astype(np.int32)
+        ptr = np.searchsorted(m[order], np.arange(n + 1)).astype(np.int32)
+        return ptr, order
+
     def _device_data(self, device):
         if self._dev is None or self._dev[0].device != device:
             w = torch.from_numpy(np.ascontiguousarray(self.weights)).to(device)
             maps = [torch.from_numpy(m).to(device) for m in self._maps_host]
-            self._dev = (w, *maps)
+            g = self.grid
+            sizes = [g.nelx, g.nely, max(g.nelz, 1)]
+            inv = []
+            for m, n in zip(self._maps_host, sizes):
+                ptr, pos = self._inverse_map(m, n)
+                inv += [torch.from_numpy(ptr).to(device), torch.from_numpy(pos).to(device)]
+            self._dev = (w, *maps, *inv)
         return self._dev
 
     def _apply(self, v, transpose):
         vd, kind = _to_device(v)
         g = self.grid
-        w, px, py, pz = self._device_data(vd.device)
+        w, px, py, pz, ixp, ixs, iyp, iys, izp, izs = self._device_data(vd.device)
         kx, ky, kz = self.weights.shape
         y = torch.empty_like(vd)
-        call("pmg_conv_filter", int(transpose), g.nelx, g.nely, g.nelz, w, kx, ky, kz, px, py, pz, vd, y, stream())
+        if transpose:
+            call("pmg_conv_filter_adjoint", g.nelx, g.nely, g.nelz, w, kx, ky, kz, ixp, ixs, iyp, iys, izp, izs, vd, y,
+                 stream())
+        else:
+            call("pmg_conv_filter", g.nelx, g.nely, g.nelz, w, kx, ky, kz, px, py, pz, vd, y, stream())
         return _from_device(y, kind)
 
     def __call__(self, x):
@@ -372,8 +389,10 @@ class LinSolve(Module):
         self._kind = kind
         if self.solver is None:
             self.solver = default_solver(mat)
-        self.A = mat.astype(F64)
         self.solver.update(mat)
+        # FP64 products of the LDA bookkeeping use the solver's (persistent, already assembled) operator
+        sa = getattr(self.solver, "A64", None) or getattr(self.solver, "A", None)
+        self.A = sa if isinstance(sa, StiffnessOperator) and sa.code == F64 else mat.astype(F64)
         self._pairs = []
         x0 = None if self.u is None else _to_device(self.u, device=mat.device)[0]
         u = self._lda_solve(fd, x0)

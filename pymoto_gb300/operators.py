@@ -107,7 +107,13 @@ class _GalerkinTables:
 
 
 class StiffnessOperator:
-    """Matrix-free K(x) = sum_e x_e K0 with Dirichlet rows/columns (level 0 of the hierarchy)."""
+    """K(x) = sum_e x_e K0 with Dirichlet rows/columns (level 0 of the hierarchy).
+
+    FP32 products are matrix-free (600 FMA per node, memory-light).  FP64 products use node stencils
+    assembled once on the first FP64 product (243 FMA per node in 3D; FP64 throughput is 1/58 of FP32 on
+    GB300, so fewer FMAs win over the extra 1 GB of stencil traffic) unless `fp64_stencil` is False."""
+
+    fp64_stencil = True
 
     def __init__(self, grid, xe, K0, bcmask, bcdiag, dtype=F64, _xe64=None):
         self.grid = grid
@@ -119,6 +125,34 @@ class StiffnessOperator:
         self._xe64 = xe if _xe64 is None and dtype == F64 else _xe64
         self._diag = None
         self._variants = {dtype: self}
+        self._S = None
+        self.persistent = False
+
+    @classmethod
+    def like(cls, other, code):
+        """An operator with its own device buffers (precision `code`) for the grid / K0 / BCs of `other`,
+        meant to be refreshed in place with assign() every design iteration (stable device addresses, so
+        CUDA graphs that read it stay valid)."""
+        xe = torch.empty(other.xe.shape, dtype=TORCH_DTYPE[code], device=other.device)
+        op = cls(other.grid, xe, other.K0, other.bcmask, other.bcdiag, code)
+        op.persistent = True
+        return op
+
+    def assign(self, other):
+        """Copy the element scaling of `other` (any precision) into this operator's buffer and refresh the
+        derived stencil and diagonal in place."""
+        if other is self:
+            return self
+        if other.grid.dims != self.grid.dims:
+            raise ValueError("assign: grid mismatch")
+        src = other._xe64 if other._xe64 is not None else other.xe
+        call("pmg_convert", _lib.dtype_code(src), self.code, src.numel(), src, self.xe, 1.0, stream())
+        self.bcmask, self.bcdiag = other.bcmask, other.bcdiag
+        if self._S is not None:
+            self._assemble_stencil(self._S)
+        if self._diag is not None:
+            self._diagonal_into(self._diag)
+        return self
 
     # matrix protocol -------------------------------------------------------------------------
     @property
@@ -156,11 +190,29 @@ class StiffnessOperator:
         self._variants[code] = op
         return op
 
+    def _assemble_stencil(self, S):
+        g = self.grid
+        call("pmg_ebe_stencil", self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag, S,
+             stream())
+
+    def stencil(self):
+        """Node stencils of this operator (assembled on first use, same precision)."""
+        if self._S is None:
+            g = self.grid
+            nsb = (27 if g.dim == 3 else 9) * g.dim * g.dim
+            self._S = torch.empty((nsb, g.nnodes), dtype=self.torch_dtype, device=self.device)
+            self._assemble_stencil(self._S)
+        return self._S
+
     def apply(self, mode, u, b=None, diag=None, w=0.0, out=None):
         out = torch.empty_like(u) if out is None else out
         g = self.grid
-        call("pmg_ebe_apply", mode, self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag,
-             u, b, diag, float(w), out, stream())
+        if self.code == F64 and self.fp64_stencil:
+            call("pmg_stencil_apply", mode, self.code, g.nelx, g.nely, g.nelz, self.stencil(), u, b, diag, float(w),
+                 out, stream())
+        else:
+            call("pmg_ebe_apply", mode, self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask,
+                 self.bcdiag, u, b, diag, float(w), out, stream())
         return out
 
     def matvec(self, u, out=None):
@@ -172,24 +224,28 @@ class StiffnessOperator:
             return self.matvec(ud).cpu().numpy()
         return self.matvec(u.contiguous())
 
+    def _diagonal_into(self, d):
+        g = self.grid
+        call("pmg_ebe_diagonal", self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag, d,
+             stream())
+
     def diagonal(self):
         if self._diag is None:
-            g = self.grid
-            d = torch.empty(g.ndof, dtype=self.torch_dtype, device=self.device)
-            call("pmg_ebe_diagonal", self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag,
-                 d, stream())
-            self._diag = d
+            self._diag = torch.empty(self.grid.ndof, dtype=self.torch_dtype, device=self.device)
+            self._diagonal_into(self._diag)
         return self._diag
 
-    def galerkin(self):
-        """Coarse operator R^T K R as a StencilOperator (same precision)."""
+    def galerkin(self, out=None):
+        """Coarse operator R^T K R as a StencilOperator (same precision); recomputed in place into `out`."""
         g = self.grid
         gc = g.coarse()
         nde = (2 ** g.dim) * g.dim
         table = _GalerkinTables.get(self.K0, g.dim, self.code, self.device)
-        E = torch.empty((gc.nel, nde * nde), dtype=self.torch_dtype, device=self.device)
-        call("pmg_galerkin_from_ebe", self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag,
-             table, E, stream())
+        E = out.E if out is not None else torch.empty((gc.nel, nde * nde), dtype=self.torch_dtype, device=self.device)
+        call("pmg_galerkin_from_ebe", self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0,
+             self.bcmask, self.bcdiag, table, E, stream())
+        if out is not None:
+            return out.recompute()
         return StencilOperator(gc, E, self.code)
 
     def __repr__(self):
@@ -206,8 +262,16 @@ class StencilOperator:
         g = grid
         nsb = (27 if g.dim == 3 else 9) * g.dim * g.dim
         self.S = torch.empty((nsb, g.nnodes), dtype=TORCH_DTYPE[code], device=E.device)
-        call("pmg_stencil_from_elements", code, g.nelx, g.nely, g.nelz, E, self.S, stream())
         self._diag = None
+        self.recompute()
+
+    def recompute(self):
+        """Refresh the node stencils (and the diagonal, if it was requested) from E in place."""
+        g = self.grid
+        call("pmg_stencil_from_elements", self.code, g.nelx, g.nely, g.nelz, self.E, self.S, stream())
+        if self._diag is not None:
+            call("pmg_stencil_diagonal", self.code, g.nelx, g.nely, g.nelz, self.S, self._diag, stream())
+        return self
 
     @property
     def shape(self):
@@ -252,17 +316,19 @@ class StencilOperator:
             self._diag = d
         return self._diag
 
-    def galerkin(self):
+    def galerkin(self, out=None):
         g = self.grid
         gc = g.coarse()
         nde = (2 ** g.dim) * g.dim
-        E = torch.empty((gc.nel, nde * nde), dtype=self.torch_dtype, device=self.device)
+        E = out.E if out is not None else torch.empty((gc.nel, nde * nde), dtype=self.torch_dtype, device=self.device)
         call("pmg_galerkin_from_elements", self.code, g.nelx, g.nely, g.nelz, self.E, E, stream())
+        if out is not None:
+            return out.recompute()
         return StencilOperator(gc, E, self.code)
 
-    def to_dense(self):
+    def to_dense(self, out=None):
         g = self.grid
-        A = torch.empty((g.ndof, g.ndof), dtype=torch.float64, device=self.device)
+        A = torch.empty((g.ndof, g.ndof), dtype=torch.float64, device=self.device) if out is None else out
         call("pmg_stencil_to_dense", self.code, g.nelx, g.nely, g.nelz, self.S, A, stream())
         return A
 

@@ -110,10 +110,13 @@ class DenseCholesky(LinearSolver):
     """
 
     MAX_DOFS = 20000
+    INVERSE_MAX_DOFS = 4096   # up to this size the solve is one dense product with the explicit inverse
 
     def __init__(self, A=None):
         self.L = None
         self.L32 = None
+        self.Ainv = None
+        self.Ainv32 = None
         super().__init__(A)
 
     def update(self, A):
@@ -124,21 +127,39 @@ class DenseCholesky(LinearSolver):
             raise ValueError(f"coarsest level has {n} dofs (> {self.MAX_DOFS}); add multigrid levels")
         self.n = n
         self.bw = A.bandwidth()
-        L = A.to_dense()
-        info = torch.zeros(1, dtype=torch.int32, device=L.device)
-        call("pmg_cholesky_factor", n, L, self.bw, info, stream())
-        bad = int(info.item())
+        dev = A.device
+        if self.L is None or self.L.shape[0] != n or self.L.device != dev:
+            # device buffers kept across updates (stable addresses for captured CUDA graphs)
+            self.L = torch.empty((n, n), dtype=torch.float64, device=dev)
+            self._info = torch.zeros(1, dtype=torch.int32, device=dev)
+            self.Ainv = torch.empty_like(self.L) if n <= self.INVERSE_MAX_DOFS else None
+            self.Ainv32 = torch.empty((n, n), dtype=torch.float32, device=dev) if self.Ainv is not None else None
+            self.L32 = None
+        L = A.to_dense(out=self.L)
+        call("pmg_cholesky_factor", n, L, self.bw, self._info, stream())
+        bad = int(self._info.item())
         if bad != 0:
             raise np.linalg.LinAlgError(f"coarsest-level matrix not positive definite (pivot {bad - 1})")
-        self.L = L
-        self.L32 = L.to(torch.float32) if A.code == F32 else None
+        if self.Ainv is not None:
+            call("pmg_cholesky_inverse", n, L, self.bw, self.Ainv, stream())
+            call("pmg_convert", F64, F32, n * n, self.Ainv, self.Ainv32, 1.0, stream())
+        elif A.code == F32:
+            if self.L32 is None:
+                self.L32 = torch.empty((n, n), dtype=torch.float32, device=dev)
+            call("pmg_convert", F64, F32, n * n, self.L, self.L32, 1.0, stream())
 
     def solve(self, rhs, x0=None, trans="N"):
         code = _lib.dtype_code(rhs)
+        out = getattr(self, "_out", None)
+        if out is None or out.dtype != rhs.dtype or out.numel() != rhs.numel() or out.device != rhs.device:
+            out = self._out = torch.empty_like(rhs)
+        if self.Ainv is not None:
+            Ai = self.Ainv if code == F64 else self.Ainv32
+            call("pmg_dense_gemv", code, self.n, Ai, rhs.contiguous(), out, stream())
+            return out
         L = self.L if code == F64 else self.L32
         if L is None:
             L = self.L32 = self.L.to(torch.float32)
-        out = torch.empty_like(rhs)
         call("pmg_cholesky_solve", code, self.n, L, self.bw, rhs.contiguous(), out, stream())
         return out
 
@@ -173,16 +194,36 @@ class GeometricMultigrid(Preconditioner):
                                        domain.unitz * 2)
         self.A = None
         self._buf = None
+        self.use_graph = True
+        self._graph = None
         super().__init__(A)
 
     def update(self, A):
+        """Refresh the level for a new operator.  Device buffers (level-0 copy of the operator, Galerkin
+        operators, diagonals, coarsest factor) are reused in place, so a captured V-cycle stays valid."""
         code = self.precision if self.precision is not None else A.code
-        op = A.astype(code) if isinstance(A, StiffnessOperator) else A
+        if isinstance(A, StiffnessOperator):
+            if A.persistent and A.code == code:
+                op = A
+            else:
+                if getattr(self, "_A0", None) is None or self._A0.code != code or self._A0.grid.dims != A.grid.dims:
+                    self._A0 = StiffnessOperator.like(A, code)
+                    self._graph = None
+                op = self._A0.assign(A)
+        else:
+            op = A
         if op.code != code:
             raise TypeError("coarse operators keep the precision of their parent level")
+        if self.A is not op:
+            self._graph = None
         self.A = op
         self.smoother.update(op)
-        Ac = op.galerkin()
+        if getattr(self, "_Ac", None) is None or self._Ac.code != code:
+            self._Ac = op.galerkin()
+            self._graph = None
+        else:
+            op.galerkin(out=self._Ac)
+        Ac = self._Ac
         if self.inner_level is None:
             self.inner_level = DenseCholesky()
         if isinstance(self.inner_level, GeometricMultigrid) and self.inner_level.precision is None:
@@ -191,16 +232,33 @@ class GeometricMultigrid(Preconditioner):
         n = self.grid.ndof
         if self._buf is None or self._buf[0].dtype != op.torch_dtype or self._buf[0].device != op.device:
             self._buf = [torch.empty(n, dtype=op.torch_dtype, device=op.device) for _ in range(3)]
+            self._rc = torch.empty(self.grid.coarse().ndof, dtype=op.torch_dtype, device=op.device)
 
     @property
     def code(self):
         return self.A.code
 
     def solve(self, rhs, x0=None, trans="N"):
+        """One V-cycle.  The result is a buffer of this object, valid until the next solve."""
         in_code = _lib.dtype_code(rhs)
         b = rhs if in_code == self.A.code else rhs.to(self.A.torch_dtype)
-        u = self._vcycle(b, x0 if x0 is None or x0.dtype == b.dtype else x0.to(b.dtype))
+        if x0 is None and self.use_graph and not torch.cuda.is_current_stream_capturing():
+            u = self._replay(b)
+        else:
+            u = self._vcycle(b, x0 if x0 is None or x0.dtype == b.dtype else x0.to(b.dtype))
         return u if in_code == self.A.code else u.to(rhs.dtype)
+
+    def _replay(self, b):
+        """V-cycle from a zero guess through a CUDA graph captured once per update()."""
+        if self._graph is None:
+            self._g_in = torch.zeros_like(b)
+            self._vcycle(self._g_in)                 # eager run: loads every kernel before the capture
+            graph, counter = capture_graph(lambda: self._vcycle(self._g_in))
+            self._graph, self._g_out = graph, counter.result
+            self._g_launches = counter.launches
+        self._g_in.copy_(b)
+        _lib.replay(f"vcycle{self.grid.dims}|{self.A.code}", self._graph, self._g_launches)
+        return self._g_out
 
     def _vcycle(self, b, x0=None):
         A, w, steps = self.A, None, self.smooth_steps
@@ -226,7 +284,7 @@ class GeometricMultigrid(Preconditioner):
         A.apply(RESIDUAL, u, b, out=r)
         g = self.grid
         inner = self.inner_level
-        rc = torch.empty(g.coarse().ndof, dtype=b.dtype, device=b.device)
+        rc = self._rc
         call("pmg_restrict", A.code, g.nelx, g.nely, g.nelz, r, rc, stream())
         uc = inner._vcycle(rc) if isinstance(inner, GeometricMultigrid) else inner.solve(rc)
         call("pmg_prolong_add", A.code, g.nelx, g.nely, g.nelz, uc, u, stream())
@@ -242,9 +300,12 @@ class GeometricMultigrid(Preconditioner):
         return u
 
     @classmethod
-    def hierarchy(cls, domain, levels=None, smoother_w=0.5, smooth_steps=5, precision=None, max_coarse_dofs=3000):
+    def hierarchy(cls, domain, levels=None, smoother_w=0.5, smooth_steps=5, precision=None, max_coarse_dofs=3000,
+                  coarse_smooth_steps=None):
         """Chain of GeometricMultigrid levels as ex_compliance_multigrid.py:108-121 builds it.  With
-        levels=None, coarsen while the grid halves evenly and the coarse level has > max_coarse_dofs."""
+        levels=None, coarsen while the grid halves evenly and the coarse level has > max_coarse_dofs.
+        `coarse_smooth_steps` (default: smooth_steps) applies to every level below the finest."""
+        css = smooth_steps if coarse_smooth_steps is None else coarse_smooth_steps
         mgs = [cls(domain, smoother=DampedJacobi(w=smoother_w), smooth_steps=smooth_steps, precision=precision)]
         while True:
             if levels is not None and len(mgs) >= levels - 1:
@@ -255,9 +316,35 @@ class GeometricMultigrid(Preconditioner):
                 break
             if not g.can_coarsen():
                 raise ValueError(f"cannot build {levels} levels: grid {g.dims} does not halve evenly")
-            mgs.append(cls(sub, smoother=DampedJacobi(w=smoother_w), smooth_steps=smooth_steps, precision=precision))
+            mgs.append(cls(sub, smoother=DampedJacobi(w=smoother_w), smooth_steps=css, precision=precision))
             mgs[-2].inner_level = mgs[-1]
         return mgs
+
+
+class _CaptureResult:
+    def __init__(self):
+        self.result = None
+        self.launches = 0
+
+
+def capture_graph(fn):
+    """Capture fn() (device work on the current torch stream only, no host synchronisation) into a CUDA
+    graph.  Returns (graph, info) with info.result = fn's return value and info.launches = kernels
+    launched.  Every tensor fn allocates comes from the graph's private pool and is kept alive by the
+    returned objects."""
+    info = _CaptureResult()
+    probe = _lib.Probe(targets=set())       # counts launches, records no events
+    prev = _lib.Probe.active
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    try:
+        _lib.Probe.active = probe
+        with torch.cuda.graph(graph):
+            info.result = fn()
+    finally:
+        _lib.Probe.active = prev
+    info.launches = probe.launches
+    return graph, info
 
 
 class _Scalars:
@@ -316,6 +403,30 @@ def pcg(A, b, M, x, tol, maxit, restart, bnorm=None, callback=None):
     return it + 1, res
 
 
+def pcg_fixed(A, b, M, x, k, bufs):
+    """Exactly k PCG iterations from x = 0 with the update formulas of pcg(), without any host
+    synchronisation (so it can be captured in a CUDA graph).  bufs = (r, p, q, scalars[8])."""
+    code = _lib.dtype_code(b)
+    n = b.numel()
+    ws = Workspace.get(b.device)
+    st = stream()
+    r, p, q, sc = bufs
+    x.zero_()
+    r.copy_(b)
+    z = M(r)
+    call("pmg_dot", code, n, z, z, sc[5:6], ws.reduce, st)
+    call("pmg_scale_rsqrt", code, n, p, z, sc[5:6], st)
+    for i in range(k):
+        A.apply(MATVEC, p, out=q)
+        call("pmg_dot2", code, n, p, q, p, r, sc[0:1], ws.reduce, st)   # pq, pr
+        call("pmg_cg_update", code, n, x, r, p, q, sc[1:2], sc[0:1], sc[2:3], ws.reduce, st)
+        if i < k - 1:
+            z = M(r)
+            call("pmg_dot", code, n, q, z, sc[3:4], ws.reduce, st)
+            call("pmg_xpby_ratio", code, n, p, z, sc[3:4], sc[0:1], st)
+    return x
+
+
 class CG(LinearSolver):
     """Preconditioned conjugate gradient (pymoto/solvers/iterative.py:295-403), on the device."""
 
@@ -332,6 +443,10 @@ class CG(LinearSolver):
 
     def update(self, A):
         t0 = time.perf_counter()
+        if isinstance(A, StiffnessOperator):
+            if getattr(self, "_Ap", None) is None or self._Ap.code != A.code or self._Ap.grid.dims != A.grid.dims:
+                self._Ap = StiffnessOperator.like(A, A.code)
+            A = self._Ap.assign(A)
         self.A = A
         self.preconditioner.update(A)
         if self.verbosity >= 1:
@@ -361,17 +476,22 @@ class MixedPrecisionCG(LinearSolver):
     FP64: the solution, the residual, the operator products q = K(x) p, the alpha/beta dot products and the
     stopping test ||f - K(x) u|| / ||f|| <= tol (the recursive residual, recomputed explicitly every
     `restart` iterations and once more before returning).
-    FP32: the preconditioner -- one V-cycle of the FP32 hierarchy (inner_iters=0) or up to `inner_iters`
-    FP32 PCG iterations on the FP32 operator to the relative tolerance `inner_tol`.
+    FP32: the preconditioner -- one V-cycle of the FP32 hierarchy (inner_iters=0) or exactly `inner_iters`
+    FP32 PCG iterations on the FP32 operator (no host synchronisation: the whole preconditioner is one
+    CUDA-graph replay, captured once per update()).
     Because the preconditioner is inexact (and may be nonlinear), directions are K-orthogonalised against
     the last `m` directions (FCG(m)); the reference's beta = -(q.z)/(p.q) is the m = 1 case.
     `warm_start` is an optional object with `.predict(A, rhs)` giving the initial guess when no x0 is
     passed; `coarse_correction` an optional callable r64 -> z64 added to the preconditioned residual.
     """
 
-    def __init__(self, A=None, preconditioner=None, tol=1e-6, m=4, inner_iters=0, inner_tol=0.1, maxit=500,
-                 restart=50, verbosity=0, warm_start=None, coarse_correction=None):
+    def __init__(self, A=None, preconditioner=None, tol=1e-6, m=2, inner_iters=0, inner_tol=0.1, maxit=500,
+                 restart=50, verbosity=0, warm_start=None, coarse_correction=None, fallback=True, stall_window=30):
         self.preconditioner = preconditioner
+        self.fallback = fallback
+        self.stall_window = stall_window
+        self.fell_back = False
+        self._fallback_pc = None
         self.tol = tol
         self.m = max(1, int(m))
         self.inner_iters = inner_iters
@@ -387,25 +507,67 @@ class MixedPrecisionCG(LinearSolver):
         super().__init__(A)
 
     def update(self, A):
-        self.A64 = A.astype(F64)
-        self.A32 = A.astype(F32)
+        if getattr(self, "_A64", None) is None or self._A64.grid.dims != A.grid.dims:
+            self._A64 = StiffnessOperator.like(A, F64)
+        self.A64 = self._A64.assign(A)
         self.A = self.A64
         if self.preconditioner is not None:
-            self.preconditioner.update(self.A32)
+            self.preconditioner.update(A)
+            lv0 = getattr(self.preconditioner, "A", None)
+            self.A32 = lv0 if isinstance(lv0, StiffnessOperator) and lv0.code == F32 else A.astype(F32)
+        else:
+            self.A32 = A.astype(F32)
+        self._fallback_ready = False
+        n, dev = self.A64.grid.ndof, self.A64.device
+        if getattr(self, "_r32", None) is None or self._r32.numel() != n or self._r32.device != dev:
+            f32 = dict(dtype=torch.float32, device=dev)
+            self._r32 = torch.empty(n, **f32)
+            self._z32 = torch.empty(n, **f32)
+            self._inner_bufs = (torch.empty(n, **f32), torch.empty(n, **f32), torch.empty(n, **f32),
+                                torch.zeros(8, dtype=torch.float64, device=dev))
+            self._inner_graph = None
+
+    def _inner(self):
+        """k fixed FP32 PCG iterations on self._r32 -> self._z32, as a CUDA graph captured per update."""
+        run = lambda: pcg_fixed(self.A32, self._r32, self.preconditioner.solve, self._z32, self.inner_iters,
+                                self._inner_bufs)
+        if self._inner_graph is None:
+            run()                                     # eager run: loads every kernel before the capture
+            self._inner_graph, info = capture_graph(run)
+            self._inner_launches = info.launches
+        _lib.replay(f"inner_pcg{self.inner_iters}", self._inner_graph, self._inner_launches)
+        self.inner_iterations += self.inner_iters
+        return self._z32
+
+    def _fp64_preconditioner(self):
+        """The same multigrid hierarchy in FP64: the fallback when the FP32 preconditioner stalls."""
+        if self._fallback_pc is None:
+            chain, lv = [], self.preconditioner
+            while isinstance(lv, GeometricMultigrid):
+                sm = lv.smoother
+                chain.append(GeometricMultigrid(lv.domain, smoother=DampedJacobi(w=getattr(sm, "w", 0.5)),
+                                                smooth_steps=lv.smooth_steps, precision="fp64"))
+                if len(chain) > 1:
+                    chain[-2].inner_level = chain[-1]
+                lv = lv.inner_level
+            self._fallback_pc = chain[0] if chain else DampedJacobi(w=1.0)
+        if not self._fallback_ready:
+            self._fallback_pc.update(self.A64)   # shares the persistent FP64 operator
+            self._fallback_ready = True
+        return self._fallback_pc
 
     def _precondition(self, r, rn, z):
-        """z (FP64) = ||r|| M32(r / ||r||)."""
+        """z (FP64) = ||r|| M32(r / ||r||), or the FP64 fallback preconditioner once switched."""
         n = r.numel()
         st = stream()
+        if self.fell_back:
+            z.copy_(self._fp64_preconditioner().solve(r))
+            return z
         call("pmg_convert", F64, F32, n, r, self._r32, 1.0 / rn, st)
         if self.preconditioner is None:
             z32 = self._r32
         elif self.inner_iters > 0:
-            z32 = self._z32
-            z32.zero_()
-            its, _ = pcg(self.A32, self._r32, self.preconditioner.solve, z32, self.inner_tol, self.inner_iters,
-                         self.restart)
-            self.inner_iterations += its
+            z32 = self._inner()
         else:
             z32 = self.preconditioner.solve(self._r32)
         call("pmg_convert", F32, F64, n, z32, z, rn, st)
@@ -413,64 +575,149 @@ class MixedPrecisionCG(LinearSolver):
             z.add_(self.coarse_correction(r))
         return z
 
+    # ---------------------------------------------------------------------------------- FCG iteration
+    def _ensure_fcg_buffers(self, n, dev):
+        k = self.m + 1
+        bufs = getattr(self, "_fcg", None)
+        if bufs is not None and bufs["n"] == n and bufs["dev"] == dev and bufs["k"] == k:
+            return bufs
+        f64 = dict(dtype=torch.float64, device=dev)
+        bufs = {"n": n, "dev": dev, "k": k, "x": torch.empty(n, **f64), "b": torch.empty(n, **f64),
+                "r": torch.empty(n, **f64), "z": torch.empty(n, **f64),
+                "P": [torch.zeros(n, **f64) for _ in range(k)], "Q": [torch.zeros(n, **f64) for _ in range(k)],
+                # scalars: 0 bb, 1 rr, 2 pr, 3.. 3+k q_j.z, 3+k.. 3+2k p_j.q_j
+                "s": torch.zeros(3 + 2 * k, **f64), "graphs": [None] * k, "seen": [False] * k}
+        self._fcg = bufs
+        return bufs
+
+    def _fcg_step(self, slot):
+        """One FCG(m) iteration writing its direction into history slot `slot` (device work only)."""
+        B = self._fcg
+        A, n, k = self.A64, B["n"], B["k"]
+        s, P, Q = B["s"], B["P"], B["Q"]
+        ws = Workspace.get(B["dev"])
+        st = stream()
+        r, z, x = B["r"], B["z"], B["x"]
+        if self.fell_back:
+            z.copy_(self._fp64_preconditioner().solve(r))
+        else:
+            call("pmg_convert_dscale", F64, F32, n, r, self._r32, s[1:2], 1, st)
+            if self.preconditioner is None:
+                z32 = self._r32
+            elif self.inner_iters > 0:
+                z32 = pcg_fixed(self.A32, self._r32, self.preconditioner.solve, self._z32, self.inner_iters,
+                                self._inner_bufs)
+            else:
+                z32 = self.preconditioner.solve(self._r32)
+            call("pmg_convert_dscale", F32, F64, n, z32, z, s[1:2], 0, st)
+        if self.coarse_correction is not None:
+            z.add_(self.coarse_correction(r))
+        p, q = P[slot], Q[slot]
+        p.copy_(z)
+        for j in range(k):           # K-orthogonalise against the other (older) directions
+            if j == slot:
+                continue
+            call("pmg_dot", F64, n, Q[j], z, s[3 + j:4 + j], ws.reduce, st)
+            call("pmg_axpy_ratio", F64, n, p, P[j], s[3 + j:4 + j], s[3 + k + j:4 + k + j], -1.0, st)
+        A.apply(MATVEC, p, out=q)
+        pq = s[3 + k + slot:4 + k + slot]
+        call("pmg_dot2", F64, n, p, q, p, r, self._pqpr, ws.reduce, st)
+        pq.copy_(self._pqpr[0:1])
+        s[2:3].copy_(self._pqpr[1:2])
+        call("pmg_cg_update", F64, n, x, r, p, q, s[2:3], pq, s[1:2], ws.reduce, st)
+
+    def _run_step(self, slot):
+        B = self._fcg
+        if self.fell_back or not self.use_graph:
+            self._fcg_step(slot)
+            return
+        g = B["graphs"][slot]
+        if g is None:
+            if not B["seen"][slot]:            # first use of this slot: eager (loads every kernel)
+                B["seen"][slot] = True
+                self._fcg_step(slot)
+                return
+            B["graphs"][slot], info = capture_graph(lambda: self._fcg_step(slot))
+            B.setdefault("launches", {})[slot] = info.launches
+            self._fcg_step_replay(slot)
+            return
+        self._fcg_step_replay(slot)
+
+    def _fcg_step_replay(self, slot):
+        B = self._fcg
+        _lib.replay(f"fcg_step|m={self.m}|inner={self.inner_iters}", B["graphs"][slot], B["launches"][slot])
+        if self.inner_iters > 0:
+            self.inner_iterations += self.inner_iters
+
+    use_graph = True
+
     def solve(self, rhs, x0=None, trans="N"):
         A = self.A64
-        b, kind = _to_device(rhs, torch.float64)
-        n = b.numel()
-        dev = b.device
+        b_in, kind = _to_device(rhs, torch.float64)
+        n = b_in.numel()
+        dev = b_in.device
+        B = self._ensure_fcg_buffers(n, dev)
+        if getattr(self, "_pqpr", None) is None or self._pqpr.device != dev:
+            self._pqpr = torch.zeros(2, dtype=torch.float64, device=dev)
+        x, b, r = B["x"], B["b"], B["r"]
+        b.copy_(b_in)
         if x0 is not None:
-            x = _to_device(x0, torch.float64)[0].clone()
+            x.copy_(_to_device(x0, torch.float64)[0])
         elif self.warm_start is not None:
-            x = self.warm_start.predict(A, b).to(torch.float64).contiguous()
+            x.copy_(self.warm_start.predict(A, b).to(torch.float64))
         else:
-            x = torch.zeros_like(b)
+            x.zero_()
         ws = Workspace.get(dev)
         st = stream()
-        self._r32 = torch.empty(n, dtype=torch.float32, device=dev)
-        self._z32 = torch.empty(n, dtype=torch.float32, device=dev)
-        sc = torch.zeros(2 + self.m, dtype=torch.float64, device=dev)   # bb | rr, q_j.z ...
-        r = A.apply(RESIDUAL, x, b)
-        call("pmg_dot2", F64, n, b, b, r, r, sc[0:1], ws.reduce, st)
-        bb, rr = sc[0:2].tolist()
-        bn = math.sqrt(bb) or 1.0
-        res = math.sqrt(rr) / bn
-        self.inner_iterations = 0
-        it = 0
-        hist = []               # FIFO of the last m (p, K p, [p.Kp, p.r]) triples
-        z = torch.empty_like(b)
-        while res > self.tol and it < self.maxit:
-            self._precondition(r, res * bn, z)
-            # p = z - sum_j (q_j.z)/(p_j.q_j) p_j
-            p = z.clone()
-            for j, (pj, qj, sj) in enumerate(hist):
-                call("pmg_dot", F64, n, qj, z, sc[2 + j:3 + j], ws.reduce, st)
-                call("pmg_axpy_ratio", F64, n, p, pj, sc[2 + j:3 + j], sj[0:1], -1.0, st)
-            q = A.apply(MATVEC, p, out=hist[0][1] if len(hist) == self.m else None)
-            s2 = torch.empty(2, dtype=torch.float64, device=dev)
-            call("pmg_dot2", F64, n, p, q, p, r, s2, ws.reduce, st)           # p.q, p.r
-            it += 1
-            if it % self.restart == 0:
-                call("pmg_axpy_ratio", F64, n, x, p, s2[1:2], s2[0:1], 1.0, st)
-                A.apply(RESIDUAL, x, b, out=r)
-                call("pmg_dot", F64, n, r, r, sc[1:2], ws.reduce, st)
-            else:
-                call("pmg_cg_update", F64, n, x, r, p, q, s2[1:2], s2[0:1], sc[1:2], ws.reduce, st)
-            res = math.sqrt(max(sc[1].item(), 0.0)) / bn
-            if self.verbosity >= 2:
-                print(f"FCG it {it}: residual {res:.3e}")
-            if len(hist) == self.m:
-                hist.pop(0)
-            hist.append((p, q, s2))
-            if not math.isfinite(res):
-                break
-        # final true FP64 residual
+        s = B["s"]
         A.apply(RESIDUAL, x, b, out=r)
-        call("pmg_dot", F64, n, r, r, sc[1:2], ws.reduce, st)
-        res = math.sqrt(max(sc[1].item(), 0.0)) / bn
+        call("pmg_dot2", F64, n, b, b, r, r, s[0:1], ws.reduce, st)
+        bb, rr = s[0:2].tolist()
+        bn = math.sqrt(bb) or 1.0
+        res = math.sqrt(max(rr, 0.0)) / bn
+        self.inner_iterations = 0
+        self.fell_back = False
+        can_fall_back = self.fallback and self.preconditioner is not None
+        it, it_fb, best, best_it = 0, 0, res, 0
+        while res > self.tol:
+            # fresh direction history (slots zeroed: zero products give zero projections)
+            for t in B["P"] + B["Q"]:
+                t.zero_()
+            s[3:].zero_()
+            slot = 0
+            while res > self.tol:
+                if can_fall_back and not self.fell_back and (it >= self.maxit or it - best_it >= self.stall_window):
+                    self.fell_back = True          # FP32 preconditioning stalled: FP64 hierarchy from here on
+                    it_fb = it
+                    for t in B["P"] + B["Q"]:
+                        t.zero_()
+                    s[3:].zero_()
+                    slot = 0
+                    if self.verbosity >= 1:
+                        print(f"MixedPrecisionCG: FP32 preconditioner stalled at {res:.3e}; FP64 fallback")
+                if (self.fell_back or not can_fall_back) and it - it_fb >= self.maxit:
+                    break
+                self._run_step(slot)
+                slot = (slot + 1) % B["k"]
+                it += 1
+                res = math.sqrt(max(s[1].item(), 0.0)) / bn
+                if self.verbosity >= 2:
+                    print(f"FCG it {it}: residual {res:.3e}")
+                if res < 0.5 * best:
+                    best, best_it = res, it
+                if not math.isfinite(res):
+                    break
+            # true FP64 residual; continue from it if the recursive residual drifted
+            A.apply(RESIDUAL, x, b, out=r)
+            call("pmg_dot", F64, n, r, r, s[1:2], ws.reduce, st)
+            res = math.sqrt(max(s[1].item(), 0.0)) / bn
+            if not math.isfinite(res) or ((self.fell_back or not can_fall_back) and it - it_fb >= self.maxit):
+                break
         self.iterations, self.last_residual = it, res
         if res > self.tol:
             warnings.warn(f"MixedPrecisionCG did not reach tol {self.tol}: residual {res}")
-        return _from_device(x, kind)
+        out = x.clone()
+        return _from_device(out, kind)
 
 
 def default_solver(A, tol=1e-10):

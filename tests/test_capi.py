@@ -81,7 +81,7 @@ def test_invalid_arguments_fail_before_any_launch():
     with pytest.raises(PMGError):
         call("pmg_restrict", 0, 5, 4, 0, None, None, None)      # odd grid
     with pytest.raises(PMGError):
-        call("pmg_conv_filter", 0, 4, 4, 0, None, 2, 1, 1, None, None, None, None, None, None)
+        call("pmg_conv_filter", 4, 4, 0, None, 2, 1, 1, None, None, None, None, None, None)
     with pytest.raises(PMGError):
         call("pmg_element_stiffness", 4, 1.0, 0.3, 0, 1.0, 1.0, 1.0, np.zeros(4))
     assert call("pmg_stencil_bandwidth", 2, 1, 1) == (1 + 3 + 3 * 2) * 3 + 2

@@ -62,6 +62,21 @@ def test_matvec_fp64_matches_csr(pg, shape, bc):
 
 
 @pytest.mark.parametrize("shape", SHAPES)
+def test_fp64_stencil_and_matrix_free_agree(pg, shape):
+    """The two FP64 product paths (assembled level-0 stencil, matrix-free gather) give the same K u."""
+    from pymoto_gb300._lib import JACOBI
+    g, K, op, rng = _setup(pg, shape, seed=5)
+    u, b = rng.standard_normal(g.ndof), rng.standard_normal(g.ndof)
+    ys = host(op.matvec(dev(u)))
+    js = host(op.apply(JACOBI, dev(u), dev(b), op.diagonal(), 0.6))
+    op.fp64_stencil = False
+    ym = host(op.matvec(dev(u)))
+    jm = host(op.apply(JACOBI, dev(u), dev(b), op.diagonal(), 0.6))
+    np.testing.assert_allclose(ys, ym, rtol=0, atol=1e-13 * np.abs(ym).max())
+    np.testing.assert_allclose(js, jm, rtol=1e-12, atol=1e-12 * np.abs(jm).max())
+
+
+@pytest.mark.parametrize("shape", SHAPES)
 def test_matvec_fp32_and_modes(pg, shape):
     from pymoto_gb300._lib import F32, JACOBI, RESIDUAL
     g, K, op, rng = _setup(pg, shape, seed=1)
@@ -179,6 +194,31 @@ def test_cholesky_banded(pg, n_shape):
     assert np.linalg.norm(An @ xh - b) <= 1e-12 * np.linalg.norm(An, 2) * np.linalg.norm(xh)
     ref = np.linalg.solve(An, b)
     assert np.linalg.norm(xh - ref) <= 1e-4 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("n_shape", [(8, 4, 4), (16, 8, 0)])
+def test_cholesky_inverse_and_gemv(pg, n_shape):
+    from pymoto_gb300._lib import call, stream
+    g, K, op, rng = _setup(pg, n_shape, seed=9)
+    A1 = op.galerkin()
+    Ad = A1.to_dense()
+    n, bw = Ad.shape[0], A1.bandwidth()
+    An = host(Ad)
+    L = Ad.clone()
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    call("pmg_cholesky_factor", n, L, bw, info, stream())
+    Ainv = torch.empty_like(L)
+    call("pmg_cholesky_inverse", n, L, bw, Ainv, stream())
+    Ai = host(Ainv)
+    assert np.abs(Ai - Ai.T).max() <= 1e-10 * np.abs(Ai).max()
+    assert np.abs(An @ Ai - np.eye(n)).max() <= 1e-8
+    b = rng.standard_normal(n)
+    for dt, tol in [(torch.float64, 1e-12), (torch.float32, 1e-5)]:
+        A = Ainv.to(dt)
+        y = torch.empty(n, dtype=dt, device="cuda")
+        call("pmg_dense_gemv", 0 if dt == torch.float64 else 1, n, A, dev(b, dt), y, stream())
+        ref = host(A) @ host(dev(b, dt))
+        np.testing.assert_allclose(host(y), ref, rtol=0, atol=tol * np.abs(ref).max())
 
 
 def test_cholesky_reports_not_spd(pg):

@@ -117,17 +117,22 @@ def test_cg_iterations_match_reference_algorithm(pg):
     np.testing.assert_allclose(u, u_ref, rtol=0, atol=1e-9 * np.abs(u_ref).max())
 
 
-@pytest.mark.parametrize("shape", [(32, 16, 16), (64, 32, 0)])
-def test_mixed_precision_reaches_fp64_residual(pg, shape):
-    """Mixed FP32/FP64 solve: true FP64 relative residual <= 1e-6 and compliance within 1e-6 of the
-    oracle's FP64 solution."""
-    g = O.Grid(*shape)
-    bc = clamp_face_dofs(g)
+def _cantilever_rhs(g):
     f = np.zeros(g.ndof)
     tip = g.node_number(g.nelx, g.nely // 2, g.nelz // 2)
     f[g.dim * tip + 1] = -1.0
+    return f
+
+
+@pytest.mark.parametrize("shape", [(32, 16, 16), (64, 32, 0)])
+def test_mixed_precision_reaches_fp64_residual(pg, shape):
+    """Mixed FP32/FP64 solve of the pipeline's stiffness (filtered random densities, r = 2.5, SIMP p = 3):
+    true FP64 relative residual <= 1e-6 and compliance within 1e-6 of the oracle's FP64 solution."""
+    g = O.Grid(*shape)
+    bc = clamp_face_dofs(g)
+    f = _cantilever_rhs(g)
     rng = np.random.default_rng(1)
-    x = O.simp(rng.uniform(1e-3, 1.0, g.nel))
+    x = O.simp(O.conv_filter(g, O.conv_filter_weights(g, 2.5), rng.uniform(1e-3, 1.0, g.nel)))
     K = O.assemble(g, O.element_stiffness(g), x, bc)
     fr = f.copy()
     fr[bc] = 0
@@ -143,6 +148,25 @@ def test_mixed_precision_reaches_fp64_residual(pg, shape):
     assert res <= 1e-6
     c = float(fr @ host(u))
     assert abs(c - c_ref) <= 1e-6 * abs(c_ref)
+    assert not solver.fell_back
+
+
+def test_mixed_precision_falls_back_on_extreme_contrast(pg):
+    """Unfiltered SIMP noise (element-to-element contrast up to 1e9): the FP32 preconditioner stalls, the
+    solver switches to the FP64 hierarchy and still reaches the FP64 residual tolerance."""
+    shape = (16, 8, 8)
+    g = O.Grid(*shape)
+    bc = clamp_face_dofs(g)
+    f = _cantilever_rhs(g)
+    f[bc] = 0
+    x = O.simp(np.random.default_rng(1).uniform(1e-3, 1.0, g.nel))
+    d = pg.VoxelDomain(*shape)
+    Kop = pg.AssembleStiffness(d, bc=bc)(dev(x))
+    mgs = pg.GeometricMultigrid.hierarchy(d, smoother_w=0.6, smooth_steps=2, precision="fp32")
+    solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=1e-6, maxit=400, stall_window=20)
+    solver.update(Kop)
+    u = solver.solve(dev(f))
+    assert pg.LinearSolver.residual(Kop, u, dev(f)) <= 1e-6
 
 
 def test_oc_trajectory_matches_reference(pg, golden):
@@ -166,7 +190,8 @@ def test_oc_trajectory_matches_reference(pg, golden):
 
 
 def test_sensitivity_central_differences(pg):
-    """Adjoint sensitivities vs central finite differences on 64 seeded elements (h = 1e-6 x)."""
+    """Adjoint sensitivities vs central finite differences on 64 seeded elements.  h = 1e-4 x keeps the
+    solver's rounding (~1e-14 c) / h below the rtol while the O(h^2) truncation stays ~1e-8."""
     shape = (16, 8, 8)
     d = pg.VoxelDomain(*shape)
     g = O.Grid(*shape)
@@ -180,7 +205,7 @@ def test_sensitivity_central_differences(pg):
     els = rng.choice(g.nel, 64, replace=False)
     fd = []
     for e in els:
-        h = 1e-6 * x[e]
+        h = 1e-4 * x[e]
         xp, xm = x.copy(), x.copy()
         xp[e] += h
         xm[e] -= h
