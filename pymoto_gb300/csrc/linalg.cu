@@ -216,15 +216,14 @@ inline unsigned stream_blocks(int64_t n) {
 constexpr int TB = 32;
 constexpr int CHOL_SMEM_MAX_N = 20000;  // x of a solve lives in shared memory (<= 160 KB in FP64)
 
-// Diagonal tile kb and the panel below it, by one CTA.  The tile is factored in shared memory with one
-// barrier per column: A[r][c] -= A[r][k] A[c][k] / A[k][k] on the unscaled columns, each column scaled by
-// 1/sqrt of its final pivot at the end.  Then every panel row within the band is solved against the
-// tile (x L^T = a) by one thread.
+// Diagonal tile kb, factored in shared memory by one CTA with one barrier per column:
+// A[r][c] -= A[r][k] A[c][k] / A[k][k] on the unscaled columns, each column scaled by 1/sqrt of its final
+// pivot at the end (a non-positive pivot is recorded in *info and replaced by 1 so the sweep stays finite).
 constexpr int CHOL_THREADS = 256;
 
-__global__ void __launch_bounds__(CHOL_THREADS) chol_diag_panel_kernel(int n, double* A, int kb, int bw, int* info) {
+__global__ void __launch_bounds__(CHOL_THREADS) chol_diag_kernel(int n, double* A, int kb, int* info) {
   __shared__ double T[TB][TB + 1];
-  __shared__ double rdiag[TB];   // 1 / L[c][c]
+  __shared__ double rdiag[TB];
   const int k0 = kb * TB;
   const int nb = min(TB, n - k0);
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
@@ -234,7 +233,7 @@ __global__ void __launch_bounds__(CHOL_THREADS) chol_diag_panel_kernel(int n, do
   __syncthreads();
   for (int k = 0; k < nb; ++k) {
     double d = T[k][k];
-    if (!(d > 0.0)) d = 1.0;   // reported below; a unit pivot keeps the sweep finite
+    if (!(d > 0.0)) d = 1.0;
     const double rd = 1.0 / d;
     for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
       const int r = e / TB, c = e % TB;
@@ -254,17 +253,29 @@ __global__ void __launch_bounds__(CHOL_THREADS) chol_diag_panel_kernel(int n, do
   __syncthreads();
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
     const int r = e / TB, c = e % TB;
-    if (r < nb && c < nb) {
-      const double v = c <= r ? T[r][c] * rdiag[c] : 0.0;
-      T[r][c] = v;
-      A[(int64_t)(k0 + r) * n + k0 + c] = v;
-    }
+    if (r < nb && c < nb) A[(int64_t)(k0 + r) * n + k0 + c] = c <= r ? T[r][c] * rdiag[c] : 0.0;
   }
-  if (threadIdx.x < nb) rdiag[threadIdx.x] = 1.0 / T[threadIdx.x][threadIdx.x];
+}
+
+// Panel: L[ib,kb] = A[ib,kb] L[kb,kb]^{-T}, one CTA of TB threads per tile row ib > kb within the band, one
+// row per thread (x L^T = a by forward substitution with the reciprocal pivots).
+__global__ void __launch_bounds__(TB) chol_panel_kernel(int n, double* A, int kb, int bw) {
+  __shared__ double L[TB][TB + 1];
+  __shared__ double rinv[TB];
+  const int k0 = kb * TB;
+  const int nb = min(TB, n - k0);
+  const int ib = kb + 1 + blockIdx.x;
+  const int i0 = ib * TB;
+  if (i0 >= n || i0 - (k0 + nb - 1) > bw) return;
+  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
+    const int r = e / TB, c = e % TB;
+    L[r][c] = (r < nb && c < nb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
+  }
   __syncthreads();
-  // panel rows k0+nb .. k0+nb+bw (band)
-  const int rend = min(n, k0 + nb + bw);
-  for (int row = k0 + nb + threadIdx.x; row < rend; row += blockDim.x) {
+  if (threadIdx.x < nb) rinv[threadIdx.x] = 1.0 / L[threadIdx.x][threadIdx.x];
+  __syncthreads();
+  const int row = i0 + threadIdx.x;
+  if (row < n) {
     double x[TB];
 #pragma unroll
     for (int c = 0; c < TB; ++c) x[c] = c < nb ? A[(int64_t)row * n + k0 + c] : 0.0;
@@ -274,8 +285,8 @@ __global__ void __launch_bounds__(CHOL_THREADS) chol_diag_panel_kernel(int n, do
         double v = x[c];
 #pragma unroll
         for (int q = 0; q < TB; ++q)
-          if (q < c) v -= x[q] * T[c][q];
-        x[c] = v * rdiag[c];
+          if (q < c) v -= x[q] * L[c][q];
+        x[c] = v * rinv[c];
       }
     }
 #pragma unroll
@@ -330,11 +341,11 @@ __device__ void chol_solve_smem(int n, const T* __restrict__ L, int bw, T* x, in
 #pragma unroll
       for (int c = 0; c < TB; ++c)
         Lrow[c] = (lane < nb && c <= lane) ? L[(int64_t)(k0 + lane) * n + k0 + c] : T(0);
+      const T rinv = lane < nb ? T(1) / L[(int64_t)(k0 + lane) * n + k0 + lane] : T(0);
 #pragma unroll
       for (int k = 0; k < TB; ++k) {
         if (k < nb) {
-          const T dk = __shfl_sync(0xffffffffu, Lrow[k], k);
-          const T xk = __shfl_sync(0xffffffffu, xr, k) / dk;
+          const T xk = __shfl_sync(0xffffffffu, xr, k) * __shfl_sync(0xffffffffu, rinv, k);
           if (lane == k) xr = xk;
           if (lane > k) xr -= Lrow[k] * xk;
         }
@@ -363,11 +374,11 @@ __device__ void chol_solve_smem(int n, const T* __restrict__ L, int bw, T* x, in
 #pragma unroll
       for (int r = 0; r < TB; ++r)
         Lcol[r] = (lane < nb && r < nb && r >= lane) ? L[(int64_t)(k0 + r) * n + k0 + lane] : T(0);
+      const T rinv = lane < nb ? T(1) / L[(int64_t)(k0 + lane) * n + k0 + lane] : T(0);
 #pragma unroll
       for (int k = TB - 1; k >= 0; --k) {
         if (k < nb) {
-          const T dk = __shfl_sync(0xffffffffu, Lcol[k], k);
-          const T xk = __shfl_sync(0xffffffffu, xr, k) / dk;
+          const T xk = __shfl_sync(0xffffffffu, xr, k) * __shfl_sync(0xffffffffu, rinv, k);
           if (lane == k) xr = xk;
           if (lane < k) xr -= Lcol[k] * xk;
         }
@@ -599,10 +610,11 @@ int pmg_cholesky_factor(int n, double* A, int bw, int* info, void* stream) {
   const int nblk = (n + TB - 1) / TB;
   const int band_tiles = min(nblk, bw / TB + 2);
   for (int kb = 0; kb < nblk; ++kb) {
-    chol_diag_panel_kernel<<<1, CHOL_THREADS, 0, st>>>(n, A, kb, bw, info);
+    chol_diag_kernel<<<1, CHOL_THREADS, 0, st>>>(n, A, kb, info);
     const int rem = nblk - kb - 1;
     if (rem <= 0) break;
     const int pt = min(rem, band_tiles);
+    chol_panel_kernel<<<pt, TB, 0, st>>>(n, A, kb, bw);
     chol_update_kernel<<<pt * pt, 256, 0, st>>>(n, A, kb, bw, pt);
     const int rc = check_launch();
     if (rc != PMG_OK) return rc;
