@@ -83,4 +83,8 @@ __device__ __forceinline__ int64_t elem_id(const Grid& g, int i, int j, int k) {
   return (int64_t)((k * g.ny + j) * g.nx + i);
 }
 
+// 3D FP32 operator apply on the tensor cores (ebe_mma.cu).
+int ebe_apply_mma_f32(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
+                      const float* u, const float* b, const float* diag, double w, float* y, cudaStream_t st);
+
 }  // namespace pmg

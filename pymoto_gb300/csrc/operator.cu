@@ -659,6 +659,9 @@ __global__ void dofconn_kernel(Grid g, int64_t* __restrict__ dc) {
 template <typename T, int DIM>
 int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
                 const void* u, const void* b, const void* diag, double w, void* y, cudaStream_t st) {
+  if constexpr (DIM == 3 && sizeof(T) == 4)
+    return ebe_apply_mma_f32(mode, g, (const float*)xe, K0, bcmask, bcdiag, (const float*)u, (const float*)b,
+                             (const float*)diag, w, (float*)y, st);
   auto K = make_elem_mat<T, Traits<DIM>::NDE>(K0);
   if constexpr (DIM == 3) {
     const dim3 block(TBX, TBY, TBZ);

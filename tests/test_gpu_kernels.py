@@ -92,6 +92,37 @@ def test_matvec_fp32_and_modes(pg, shape):
     assert np.abs(y32 - ref).max() <= 2e-6 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("shape", [(40, 12, 10), (33, 9, 17), (64, 16, 8), (2, 2, 2)])
+@pytest.mark.parametrize("field", ["random", "smooth"])
+def test_matvec_fp32_tensor_core_tiles(pg, shape, field):
+    """FP32 3D operator (tensor-core tiles): several CTA tiles in x, y and z, ragged edges, all three modes.
+    The smooth field sits on a large constant offset: K annihilates the offset, and the result must keep
+    its accuracy relative to |K u|, not to |K| |u|."""
+    from pymoto_gb300._lib import F32, JACOBI, RESIDUAL
+    g, K, op, rng = _setup(pg, shape, seed=3)
+    if field == "random":
+        u = rng.standard_normal(g.ndof)
+    else:
+        nx, ny, nz = shape
+        kk, jj, ii = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+        base = np.stack([np.sin(0.3 * ii + 0.2 * jj), np.cos(0.25 * jj - 0.1 * kk), np.sin(0.2 * kk + 0.15 * ii)], -1)
+        u = (1000.0 + base).reshape(-1)
+    u = u.astype(np.float32).astype(np.float64)
+    b = rng.standard_normal(g.ndof).astype(np.float32).astype(np.float64)
+    op32 = op.astype(F32)
+    D = op32.diagonal()
+    ref = K @ u
+    tol = (1e-5 if field == "random" else 1e-4) * np.abs(ref).max()
+    y = host(op32.matvec(dev(u, torch.float32)))
+    assert np.abs(y - ref).max() <= tol
+    r = host(op32.apply(RESIDUAL, dev(u, torch.float32), dev(b, torch.float32)))
+    assert np.abs(r - (b - ref)).max() <= tol + 1e-6 * np.abs(b).max()
+    Dh = host(D)
+    jac = host(op32.apply(JACOBI, dev(u, torch.float32), dev(b, torch.float32), D, 0.6))
+    jref = u + 0.6 * (b - ref) / Dh
+    assert np.abs(jac - jref).max() <= 0.6 * (tol + 1e-6 * np.abs(b).max()) / np.abs(Dh).min() + 1e-6 * np.abs(u).max()
+
+
 def test_matvec_golden(pg, golden):
     g = golden("assembly.npz")
     from pymoto_gb300.operators import bc_node_mask
