@@ -73,7 +73,8 @@ def cantilever(shape):
 class DesignRun:
     """The network of the workload on the device, for one solver arm."""
 
-    opts = {"inner_iters": 0, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None}
+    opts = {"inner_iters": 0, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None,
+            "smoother": "chebyshev", "cheb_degree": 2, "cheb_coarse_degree": None, "cheb_ratio": 10.0}
 
     def __init__(self, arm, shape, seed, torch, pg):
         o = DesignRun.opts
@@ -85,14 +86,25 @@ class DesignRun:
         x0 = rng.uniform(1e-3, 1.0, d.nel)
         self.f = torch.from_numpy(f).cuda()
         self.sx = pg.Signal("x", torch.from_numpy(x0).cuda())
-        mixed = arm != "plain_fp64"
+        # arms: plain_fp64 = the reference's method (FP64 CG + FP64 GMG, damped Jacobi w=0.6, 2 sweeps) on the
+        # GPU; mixed = FP64 FCG + FP32 GMG with the Chebyshev smoother; the *_cheb / *_jacobi variants are
+        # the ablations (smoother swapped)
+        mixed = arm.startswith("mixed")
+        cheb = (mixed and arm != "mixed_jacobi" and o["smoother"] == "chebyshev") or arm == "plain_fp64_cheb"
+        self.smoother = "chebyshev" if cheb else "jacobi"
         with pg.Network() as fn:
             xf = pg.FilterConv(d, radius=RADIUS)(self.sx)
             xs = pg.SIMP(xmin=XMIN, penal=PENAL)(xf)
             K = pg.AssembleStiffness(d, bc=bc)(xs)
-            mgs = pg.GeometricMultigrid.hierarchy(d, levels=o["levels"], smoother_w=OMEGA, smooth_steps=o["sweeps"],
-                                                  precision="fp32" if mixed else None,
-                                                  coarse_smooth_steps=o["coarse_sweeps"])
+            if cheb:
+                mgs = pg.GeometricMultigrid.hierarchy(d, levels=o["levels"], smooth_steps=o["cheb_degree"],
+                                                      precision="fp32" if mixed else None,
+                                                      coarse_smooth_steps=o["cheb_coarse_degree"],
+                                                      smoother="chebyshev", cheb_ratio=o["cheb_ratio"])
+            else:
+                mgs = pg.GeometricMultigrid.hierarchy(d, levels=o["levels"], smoother_w=OMEGA,
+                                                      smooth_steps=o["sweeps"], precision="fp32" if mixed else None,
+                                                      coarse_smooth_steps=o["coarse_sweeps"])
             if mixed:
                 self.solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=o["m"], inner_iters=o["inner_iters"],
                                                   inner_tol=o["inner_tol"])

@@ -112,6 +112,19 @@ int pmg_stencil_to_dense(int dtype, int nelx, int nely, int nelz, const void* S,
 /* Half bandwidth of the dense coarsest matrix of a grid. */
 int pmg_stencil_bandwidth(int nelx, int nely, int nelz);
 
+/* ---- Chebyshev smoother (extends DampedJacobi, pymoto/solvers/iterative.py:21-47, with a polynomial
+ * smoother on [lmax/ratio, lmax] of D^-1 A; Saad, Iterative Methods for Sparse Linear Systems, Alg. 12.1)
+ * out (dof vector, operator dtype) = sum_j |A_ij| of a stencil operator: the l1-Jacobi diagonal, with
+ * which lmax(D^-1 A) <= 1 by Gershgorin's theorem.  The matrix-free finest operator gets the same bound
+ * from pmg_ebe_diagonal with K0 replaced by diag(sum_j |K0_aj|). */
+int pmg_stencil_rowabs(int dtype, int nelx, int nely, int nelz, const void* S, void* out, void* stream);
+/* coef[2j], coef[2j+1] (device, j < degree) = the step coefficients a_j, c_j for lmax = *lmax_dev (device
+ * double) or lmax_host when lmax_dev is NULL. */
+int pmg_cheb_coeffs(const double* lmax_dev, double lmax_host, double ratio, int degree, double* coef, void* stream);
+/* Step `step`: d = a d + c r / diag, x = x + d; init != 0 starts from x = 0 (d = x = c r / diag). */
+int pmg_cheb_step(int dtype, int64_t n, const void* r, const void* diag, void* d, void* x, const double* coef, int step,
+                  int init, void* stream);
+
 /* ---- coarsest-level direct solve (replaces SolverSparseLU, pymoto/solvers/sparse.py:515-555, as
  * chosen by auto_determine_solver, pymoto/solvers/auto_determine.py:109-122) -----------------------
  * In-place FP64 Cholesky A = L L^T of a dense SPD matrix with half bandwidth `bw` (lower triangle
@@ -123,6 +136,19 @@ int pmg_cholesky_solve(int dtype, int n, const void* L, int bw, const void* b, v
 /* Ainv = (L L^T)^{-1} (dense, FP64, n x n): one CTA per row.  For the small coarsest level, whose solve is
  * then one dense matrix-vector product per V-cycle instead of two sequential substitutions. */
 int pmg_cholesky_inverse(int n, const double* L, int bw, double* Ainv, void* stream);
+/* Inverses of the TB x TB (TB = 32) diagonal tiles of the FP64 factor L, stored row-major one tile after
+ * the other ((n+31)/32 tiles, zero-padded) in dtype FP64 or FP32: the operands of the blocked solve. */
+int pmg_cholesky_block_inverses(int dtype, int n, const double* L, void* Dinv, void* stream);
+/* x = (L L^T)^{-1} b by tiles: each tile of the forward and backward substitutions is one dense product
+ * with its tile inverse, so the solve has no scalar recurrence (one CTA, x in shared memory).  L, Dinv, b
+ * and x share the dtype; L is the banded factor (FP32 copy for FP32 right-hand sides). */
+int pmg_cholesky_solve_blocked(int dtype, int n, const void* L, int bw, const void* Dinv, const void* b, void* x,
+                               void* stream);
+/* FP32 inverse Ainv = (L L^T)^{-1} (n x n, row-major) of the FP64 factor, for FP32 coarse solves by one
+ * dense product: L^{-1} is formed in FP32 by tiles (tile inverses from the FP64 factor), then
+ * Ainv = L^{-T} L^{-1}.  scratch >= pmg_cholesky_inverse_f32_scratch_bytes(n) bytes. */
+size_t pmg_cholesky_inverse_f32_scratch_bytes(int n);
+int pmg_cholesky_inverse_f32(int n, const double* L, int bw, void* scratch, float* Ainv, void* stream);
 /* y = A x, dense row-major n x n, FP64 or FP32 storage with FP64 accumulation. */
 int pmg_dense_gemv(int dtype, int n, const void* A, const void* x, void* y, void* stream);
 

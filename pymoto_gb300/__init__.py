@@ -13,12 +13,12 @@ from .modules import (AssembleStiffness, DensityFilter, DeviceDyad, EinSum, Filt
                       SIMP)
 from .operators import Grid, StencilOperator, StiffnessOperator, element_stiffness
 from .optimizers import OC
-from .solvers import (CG, DampedJacobi, DenseCholesky, GeometricMultigrid, LinearSolver, MixedPrecisionCG,
-                      Preconditioner)
+from .solvers import (CG, Chebyshev, DampedJacobi, DenseCholesky, GeometricMultigrid, LinearSolver,
+                      MixedPrecisionCG, Preconditioner)
 
 __version__ = "0.1.0"
 
 __all__ = ["AssembleStiffness", "DensityFilter", "DeviceDyad", "EinSum", "FilterConv", "LinSolve", "MathExpression",
-           "SIMP", "Grid", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "DampedJacobi",
+           "SIMP", "Grid", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "Chebyshev", "DampedJacobi",
            "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
            "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME"]

@@ -38,9 +38,16 @@ SIGNATURES = {
     "pmg_stencil_to_dense": (I, [I, I, I, I, P, P, P]),
     "pmg_ebe_stencil": (I, [I, I, I, I, P, P, P, D, P, P]),
     "pmg_stencil_bandwidth": (I, [I, I, I]),
+    "pmg_stencil_rowabs": (I, [I, I, I, I, P, P, P]),
+    "pmg_cheb_coeffs": (I, [P, D, D, I, P, P]),
+    "pmg_cheb_step": (I, [I, L, P, P, P, P, P, I, I, P]),
     "pmg_cholesky_factor": (I, [I, P, I, P, P]),
     "pmg_cholesky_solve": (I, [I, I, P, I, P, P, P]),
     "pmg_cholesky_inverse": (I, [I, P, I, P, P]),
+    "pmg_cholesky_block_inverses": (I, [I, I, P, P, P]),
+    "pmg_cholesky_solve_blocked": (I, [I, I, P, I, P, P, P, P]),
+    "pmg_cholesky_inverse_f32_scratch_bytes": (c_size_t, [I]),
+    "pmg_cholesky_inverse_f32": (I, [I, P, I, P, P, P]),
     "pmg_dense_gemv": (I, [I, I, P, P, P, P]),
     "pmg_reduce_scratch_bytes": (c_size_t, []),
     "pmg_dot": (I, [I, L, P, P, P, P, P]),
@@ -121,7 +128,8 @@ def _arg(a):
 
 # kernels launched per call where it is not exactly one (host-only entry points launch none)
 _HOST_ONLY = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_element_stiffness", "pmg_galerkin_table",
-              "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth"}
+              "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth",
+              "pmg_cholesky_inverse_f32_scratch_bytes"}
 
 
 def _launches(name, args):
@@ -129,7 +137,9 @@ def _launches(name, args):
         return 0
     if name == "pmg_cholesky_factor":
         nblk = (int(args[0]) + 31) // 32
-        return 3 * nblk - 2
+        return 3 * nblk - 2 if int(args[2]) > 0 else nblk
+    if name == "pmg_cholesky_inverse_f32":
+        return 4
     if name == "pmg_oc_update":
         width, steps = float(args[9]) - float(args[8]), 3
         while width > float(args[10]):

@@ -1,0 +1,457 @@
+// Kernels of the learned warm start: a small 3D convolutional network on a voxel grid.
+//
+// Layout: channels-last, act[v][c] with v = (k*ny + j)*nx + i.  Activations and weights are stored as
+// BF16, gradients and accumulators are FP32, master weights FP32 (Adam).  3x3x3 convolutions with zero
+// padding; weights w[tap][cin][cout], tap = (dz+1)*9 + (dy+1)*3 + (dx+1).
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace pmg {
+namespace nn {
+
+struct VGrid {
+  int nx, ny, nz;
+  __host__ __device__ __forceinline__ int64_t nvox() const { return (int64_t)nx * ny * nz; }
+};
+
+__device__ __forceinline__ void vox_ijk(const VGrid& g, int v, int& i, int& j, int& k) {
+  const unsigned t = (unsigned)v / (unsigned)g.nx;
+  i = v - (int)t * g.nx;
+  k = (int)(t / (unsigned)g.ny);
+  j = (int)t - k * g.ny;
+}
+
+__device__ __forceinline__ float ld(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+__device__ __forceinline__ float ld(const float* p) { return *p; }
+
+// out[v][co] = bias[co] + sum_{tap, ci} w[tap][ci][co] in[v + tap][ci]  (+ ReLU).  One thread per (v, co),
+// co fastest: the input values of a voxel are broadcast across the warp, the weights coalesced.
+template <typename TIN>
+__global__ void conv3d_fwd_kernel(VGrid g, int cin, int cout, const TIN* __restrict__ in,
+                                  const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias, int relu,
+                                  __nv_bfloat16* __restrict__ out_bf, float* __restrict__ out_f) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.nvox() * cout) return;
+  const int co = (int)(t % cout);
+  const int v = (int)(t / cout);
+  int i, j, k;
+  vox_ijk(g, v, i, j, k);
+  float acc = bias ? bias[co] : 0.f;
+  for (int tap = 0; tap < 27; ++tap) {
+    const int ii = i + tap % 3 - 1, jj = j + (tap / 3) % 3 - 1, kk = k + tap / 9 - 1;
+    if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || kk < 0 || kk >= g.nz) continue;
+    const TIN* src = in + ((int64_t)(kk * g.ny + jj) * g.nx + ii) * cin;
+    const __nv_bfloat16* wt = w + (int64_t)tap * cin * cout + co;
+    for (int ci = 0; ci < cin; ++ci) acc = fmaf(ld(src + ci), __bfloat162float(wt[(int64_t)ci * cout]), acc);
+  }
+  if (relu) acc = fmaxf(acc, 0.f);
+  if (out_bf) out_bf[t] = __float2bfloat16(acc);
+  if (out_f) out_f[t] = acc;
+}
+
+// din[v][ci] = sum_{tap, co} w[tap][ci][co] dout[v - tap][co]  (dout already masked by the ReLU).
+__global__ void conv3d_dgrad_kernel(VGrid g, int cin, int cout, const float* __restrict__ dout,
+                                    const __nv_bfloat16* __restrict__ w, float* __restrict__ din) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.nvox() * cin) return;
+  const int ci = (int)(t % cin);
+  const int v = (int)(t / cin);
+  int i, j, k;
+  vox_ijk(g, v, i, j, k);
+  float acc = 0.f;
+  for (int tap = 0; tap < 27; ++tap) {
+    const int ii = i - (tap % 3 - 1), jj = j - ((tap / 3) % 3 - 1), kk = k - (tap / 9 - 1);
+    if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || kk < 0 || kk >= g.nz) continue;
+    const float* src = dout + ((int64_t)(kk * g.ny + jj) * g.nx + ii) * cout;
+    const __nv_bfloat16* wt = w + ((int64_t)tap * cin + ci) * cout;
+    for (int co = 0; co < cout; ++co) acc = fmaf(src[co], __bfloat162float(wt[co]), acc);
+  }
+  din[t] = acc;
+}
+
+// Partial weight gradients over a chunk of voxels: part[chunk][tap*cin*cout + ci*cout + co] (and the
+// bias gradient in the last cout entries).  Deterministic: the chunks are summed in order afterwards.
+constexpr int WG_CHUNK = 2048;
+
+template <typename TIN>
+__global__ void conv3d_wgrad_partial_kernel(VGrid g, int cin, int cout, const TIN* __restrict__ in,
+                                            const float* __restrict__ dout, float* __restrict__ part) {
+  const int nw = 27 * cin * cout + cout;
+  const int widx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (widx >= nw) return;
+  const int chunk = blockIdx.y;
+  const int64_t v0 = (int64_t)chunk * WG_CHUNK;
+  const int64_t v1 = min((int64_t)g.nvox(), v0 + WG_CHUNK);
+  float acc = 0.f;
+  if (widx < 27 * cin * cout) {
+    const int co = widx % cout, ci = (widx / cout) % cin, tap = widx / (cin * cout);
+    const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
+    for (int64_t v = v0; v < v1; ++v) {
+      int i, j, k;
+      vox_ijk(g, (int)v, i, j, k);
+      const int ii = i + dx, jj = j + dy, kk = k + dz;
+      if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || kk < 0 || kk >= g.nz) continue;
+      acc = fmaf(ld(in + ((int64_t)(kk * g.ny + jj) * g.nx + ii) * cin + ci), dout[v * cout + co], acc);
+    }
+  } else {
+    const int co = widx - 27 * cin * cout;
+    for (int64_t v = v0; v < v1; ++v) acc += dout[v * cout + co];
+  }
+  part[(int64_t)chunk * nw + widx] = acc;
+}
+
+__global__ void sum_chunks_kernel(int nw, int nchunk, const float* __restrict__ part, float* __restrict__ out,
+                                  int accumulate) {
+  const int widx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (widx >= nw) return;
+  float acc = accumulate ? out[widx] : 0.f;
+  for (int c = 0; c < nchunk; ++c) acc += part[(int64_t)c * nw + widx];
+  out[widx] = acc;
+}
+
+// dout *= (act > 0)  (ReLU backward on the stored BF16 output)
+__global__ void relu_bwd_kernel(int64_t n, const __nv_bfloat16* __restrict__ act, float* __restrict__ d) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n && !(__bfloat162float(act[t]) > 0.f)) d[t] = 0.f;
+}
+
+// 2x average pooling (fine grid 2nx x 2ny x 2nz -> coarse nx x ny x nz), forward and adjoint.
+__global__ void pool2_fwd_kernel(VGrid gc, int c, const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= gc.nvox() * c) return;
+  const int ch = (int)(t % c);
+  const int v = (int)(t / c);
+  int i, j, k;
+  vox_ijk(gc, v, i, j, k);
+  const int fx = 2 * gc.nx, fy = 2 * gc.ny;
+  float acc = 0.f;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int ii = 2 * i + (q & 1), jj = 2 * j + ((q >> 1) & 1), kk = 2 * k + ((q >> 2) & 1);
+    acc += __bfloat162float(in[((int64_t)(kk * fy + jj) * fx + ii) * c + ch]);
+  }
+  out[t] = __float2bfloat16(0.125f * acc);
+}
+
+__global__ void pool2_bwd_kernel(VGrid gf, int c, const float* __restrict__ dout, float* __restrict__ din) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= gf.nvox() * c) return;
+  const int ch = (int)(t % c);
+  const int v = (int)(t / c);
+  int i, j, k;
+  vox_ijk(gf, v, i, j, k);
+  const int cx = gf.nx / 2, cy = gf.ny / 2;
+  din[t] = 0.125f * dout[((int64_t)((k / 2) * cy + j / 2) * cx + i / 2) * c + ch];
+}
+
+// 2x nearest upsampling written into channels [coff, coff+c) of a ctot-channel output (the decoder concat).
+__global__ void up2_fwd_kernel(VGrid gf, int c, int ctot, int coff, const __nv_bfloat16* __restrict__ in,
+                               __nv_bfloat16* __restrict__ out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= gf.nvox() * c) return;
+  const int ch = (int)(t % c);
+  const int v = (int)(t / c);
+  int i, j, k;
+  vox_ijk(gf, v, i, j, k);
+  const int cx = gf.nx / 2, cy = gf.ny / 2;
+  out[(int64_t)v * ctot + coff + ch] = in[((int64_t)((k / 2) * cy + j / 2) * cx + i / 2) * c + ch];
+}
+
+// adjoint of up2: dcoarse[vc][ch] = sum over the 8 children of dfine[vf][coff + ch]
+__global__ void up2_bwd_kernel(VGrid gc, int c, int ctot, int coff, const float* __restrict__ dfine,
+                               float* __restrict__ dcoarse) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= gc.nvox() * c) return;
+  const int ch = (int)(t % c);
+  const int v = (int)(t / c);
+  int i, j, k;
+  vox_ijk(gc, v, i, j, k);
+  const int fx = 2 * gc.nx, fy = 2 * gc.ny;
+  float acc = 0.f;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int ii = 2 * i + (q & 1), jj = 2 * j + ((q >> 1) & 1), kk = 2 * k + ((q >> 2) & 1);
+    acc += dfine[((int64_t)(kk * fy + jj) * fx + ii) * ctot + coff + ch];
+  }
+  dcoarse[t] = acc;
+}
+
+// copy channels: out[v][coff + ch] = in[v][ch]  (skip connection into the concat buffer)
+__global__ void copy_channels_kernel(int64_t nvox, int c, int ctot, int coff, const __nv_bfloat16* __restrict__ in,
+                                     __nv_bfloat16* __restrict__ out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nvox * c) return;
+  const int ch = (int)(t % c);
+  const int64_t v = t / c;
+  out[v * ctot + coff + ch] = in[t];
+}
+
+// dskip[v][ch] += dcat[v][coff + ch]
+__global__ void split_channels_kernel(int64_t nvox, int c, int ctot, int coff, const float* __restrict__ dcat,
+                                      float* __restrict__ dskip) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nvox * c) return;
+  const int ch = (int)(t % c);
+  const int64_t v = t / c;
+  dskip[t] += dcat[v * ctot + coff + ch];
+}
+
+// Network input on a voxel grid of stride s over the element grid: channel 0 = mean of x over the s^3
+// elements of the voxel (x in [0,1] is mapped to 2x-1), channels 1..3 = voxel-centre coordinates in [-1,1].
+__global__ void input_features_kernel(Grid ge, int s, VGrid gv, const double* __restrict__ xe,
+                                      __nv_bfloat16* __restrict__ feat) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= gv.nvox()) return;
+  int i, j, k;
+  vox_ijk(gv, (int)v, i, j, k);
+  double acc = 0.0;
+  int cnt = 0;
+  const int ez = ge.nz == 0 ? 1 : ge.nz;
+  for (int c = 0; c < s; ++c)
+    for (int b = 0; b < s; ++b)
+      for (int a = 0; a < s; ++a) {
+        const int ei = i * s + a, ej = j * s + b, ek = k * s + c;
+        if (ei < ge.nx && ej < ge.ny && ek < ez) {
+          acc += xe[((int64_t)ek * ge.ny + ej) * ge.nx + ei];
+          ++cnt;
+        }
+      }
+  const float m = cnt ? (float)(acc / cnt) : 0.f;
+  feat[v * 4 + 0] = __float2bfloat16(2.f * m - 1.f);
+  feat[v * 4 + 1] = __float2bfloat16(2.f * (i + 0.5f) / gv.nx - 1.f);
+  feat[v * 4 + 2] = __float2bfloat16(2.f * (j + 0.5f) / gv.ny - 1.f);
+  feat[v * 4 + 3] = __float2bfloat16(2.f * (k + 0.5f) / gv.nz - 1.f);
+}
+
+// Nodal field (3 components, node grid (nx+1)(ny+1)(nz+1)) from voxel values [v][3]: each node averages
+// the voxels that touch it.  Adjoint: voxel gradient = sum over its 8 nodes of dnode / count(node).
+__global__ void vox_to_node_kernel(VGrid gv, const float* __restrict__ vox, double* __restrict__ node) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nnx = gv.nx + 1, nny = gv.ny + 1;
+  if (n >= (int64_t)nnx * nny * (gv.nz + 1)) return;
+  const int i = (int)(n % nnx), j = (int)((n / nnx) % nny), k = (int)(n / ((int64_t)nnx * nny));
+  float acc[3] = {0.f, 0.f, 0.f};
+  int cnt = 0;
+  for (int q = 0; q < 8; ++q) {
+    const int vi = i - 1 + (q & 1), vj = j - 1 + ((q >> 1) & 1), vk = k - 1 + ((q >> 2) & 1);
+    if (vi < 0 || vi >= gv.nx || vj < 0 || vj >= gv.ny || vk < 0 || vk >= gv.nz) continue;
+    const float* p = vox + ((int64_t)(vk * gv.ny + vj) * gv.nx + vi) * 3;
+    acc[0] += p[0];
+    acc[1] += p[1];
+    acc[2] += p[2];
+    ++cnt;
+  }
+  const float r = cnt ? 1.f / cnt : 0.f;
+  for (int d = 0; d < 3; ++d) node[n * 3 + d] = (double)(acc[d] * r);
+}
+
+__global__ void node_to_vox_adjoint_kernel(VGrid gv, const float* __restrict__ dnode, float* __restrict__ dvox) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= gv.nvox()) return;
+  int i, j, k;
+  vox_ijk(gv, (int)v, i, j, k);
+  const int nnx = gv.nx + 1, nny = gv.ny + 1;
+  float acc[3] = {0.f, 0.f, 0.f};
+  for (int q = 0; q < 8; ++q) {
+    const int ni = i + (q & 1), nj = j + ((q >> 1) & 1), nk = k + ((q >> 2) & 1);
+    const int cx = (ni == 0 || ni == gv.nx) ? 1 : 2, cy = (nj == 0 || nj == gv.ny) ? 1 : 2,
+              cz = (nk == 0 || nk == gv.nz) ? 1 : 2;
+    const float r = 1.f / (cx * cy * cz);
+    const float* p = dnode + ((int64_t)(nk * nny + nj) * nnx + ni) * 3;
+    acc[0] += r * p[0];
+    acc[1] += r * p[1];
+    acc[2] += r * p[2];
+  }
+  for (int d = 0; d < 3; ++d) dvox[v * 3 + d] = acc[d];
+}
+
+// Adam on FP32 master weights; the BF16 copy used by the kernels is refreshed in the same pass.
+__global__ void adam_kernel(int n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ vv, __nv_bfloat16* __restrict__ wb, float lr, float b1, float b2,
+                            float eps, float c1, float c2, float wd) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const float gt = g[t] + wd * w[t];
+  const float mt = b1 * m[t] + (1.f - b1) * gt;
+  const float vt = b2 * vv[t] + (1.f - b2) * gt * gt;
+  m[t] = mt;
+  vv[t] = vt;
+  const float wn = w[t] - lr * (mt / c1) / (sqrtf(vt / c2) + eps);
+  w[t] = wn;
+  if (wb) wb[t] = __float2bfloat16(wn);
+}
+
+// Masked mean-squared error on nodal values (FP64 prediction vs target) and its gradient (FP32).
+__global__ void mse_kernel(int64_t n, const double* __restrict__ pred, const double* __restrict__ target,
+                           const uint8_t* __restrict__ keep, double inv_n, float* __restrict__ grad,
+                           double* __restrict__ loss_partial) {
+  __shared__ double sh[256];
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double l = 0.0;
+  if (t < n) {
+    const bool k = keep ? (keep[t / 3] >> (t % 3)) & 1 ? false : true : true;
+    const double e = k ? pred[t] - target[t] : 0.0;
+    l = e * e;
+    grad[t] = (float)(2.0 * e * inv_n);
+  }
+  sh[threadIdx.x] = l;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) loss_partial[blockIdx.x] = sh[0] * inv_n;
+}
+
+}  // namespace nn
+}  // namespace pmg
+
+using namespace pmg;
+using namespace pmg::nn;
+
+static bool vgrid_ok(int nx, int ny, int nz) {
+  return nx > 0 && ny > 0 && nz > 0 && (int64_t)nx * ny * nz < (int64_t(1) << 30);
+}
+
+extern "C" {
+
+int pmg_nn_conv3d_forward(int nx, int ny, int nz, int cin, int cout, int in_is_f32, const void* in, const void* w,
+                          const float* bias, int relu, void* out_bf16, float* out_f32, void* stream) {
+  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || !in || !w || (!out_bf16 && !out_f32)) return PMG_BAD_ARG;
+  VGrid g{nx, ny, nz};
+  const int64_t work = g.nvox() * cout;
+  const unsigned blocks = blocks_for(work, 256);
+  cudaStream_t st = as_stream(stream);
+  if (in_is_f32)
+    conv3d_fwd_kernel<float><<<blocks, 256, 0, st>>>(g, cin, cout, (const float*)in, (const __nv_bfloat16*)w, bias, relu,
+                                                     (__nv_bfloat16*)out_bf16, out_f32);
+  else
+    conv3d_fwd_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(g, cin, cout, (const __nv_bfloat16*)in,
+                                                             (const __nv_bfloat16*)w, bias, relu,
+                                                             (__nv_bfloat16*)out_bf16, out_f32);
+  return check_launch();
+}
+
+int pmg_nn_conv3d_backward_data(int nx, int ny, int nz, int cin, int cout, const float* dout, const void* w, float* din,
+                                void* stream) {
+  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || !dout || !w || !din) return PMG_BAD_ARG;
+  VGrid g{nx, ny, nz};
+  conv3d_dgrad_kernel<<<blocks_for(g.nvox() * cin, 256), 256, 0, as_stream(stream)>>>(g, cin, cout, dout,
+                                                                                    (const __nv_bfloat16*)w, din);
+  return check_launch();
+}
+
+size_t pmg_nn_wgrad_scratch_bytes(int nx, int ny, int nz, int cin, int cout) {
+  const int64_t nv = (int64_t)nx * ny * nz;
+  const int64_t nchunk = (nv + WG_CHUNK - 1) / WG_CHUNK;
+  return sizeof(float) * (size_t)nchunk * (size_t)(27 * cin * cout + cout);
+}
+
+int pmg_nn_conv3d_backward_weights(int nx, int ny, int nz, int cin, int cout, int in_is_f32, const void* in,
+                                   const float* dout, float* dw_db, int accumulate, void* scratch, void* stream) {
+  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || !in || !dout || !dw_db || !scratch) return PMG_BAD_ARG;
+  VGrid g{nx, ny, nz};
+  const int nw = 27 * cin * cout + cout;
+  const int nchunk = (int)((g.nvox() + WG_CHUNK - 1) / WG_CHUNK);
+  cudaStream_t st = as_stream(stream);
+  dim3 grid((nw + 127) / 128, nchunk);
+  if (in_is_f32)
+    conv3d_wgrad_partial_kernel<float><<<grid, 128, 0, st>>>(g, cin, cout, (const float*)in, dout, (float*)scratch);
+  else
+    conv3d_wgrad_partial_kernel<__nv_bfloat16><<<grid, 128, 0, st>>>(g, cin, cout, (const __nv_bfloat16*)in, dout,
+                                                                     (float*)scratch);
+  sum_chunks_kernel<<<(nw + 255) / 256, 256, 0, st>>>(nw, nchunk, (const float*)scratch, dw_db, accumulate);
+  return check_launch();
+}
+
+int pmg_nn_relu_backward(int64_t n, const void* act_bf16, float* d, void* stream) {
+  if (n < 0 || !act_bf16 || !d) return PMG_BAD_ARG;
+  if (n == 0) return PMG_OK;
+  relu_bwd_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(n, (const __nv_bfloat16*)act_bf16, d);
+  return check_launch();
+}
+
+int pmg_nn_pool2(int direction, int cnx, int cny, int cnz, int c, const void* in, void* out, void* stream) {
+  if (!vgrid_ok(cnx, cny, cnz) || c <= 0 || !in || !out) return PMG_BAD_ARG;
+  cudaStream_t st = as_stream(stream);
+  VGrid gc{cnx, cny, cnz};
+  if (direction == 0) {
+    pool2_fwd_kernel<<<blocks_for(gc.nvox() * c, 256), 256, 0, st>>>(gc, c, (const __nv_bfloat16*)in,
+                                                                   (__nv_bfloat16*)out);
+  } else {
+    VGrid gf{2 * cnx, 2 * cny, 2 * cnz};
+    pool2_bwd_kernel<<<blocks_for(gf.nvox() * c, 256), 256, 0, st>>>(gf, c, (const float*)in, (float*)out);
+  }
+  return check_launch();
+}
+
+int pmg_nn_up2(int direction, int cnx, int cny, int cnz, int c, int ctot, int coff, const void* in, void* out,
+               void* stream) {
+  if (!vgrid_ok(cnx, cny, cnz) || c <= 0 || ctot < c + coff || coff < 0 || !in || !out) return PMG_BAD_ARG;
+  cudaStream_t st = as_stream(stream);
+  VGrid gc{cnx, cny, cnz};
+  VGrid gf{2 * cnx, 2 * cny, 2 * cnz};
+  if (direction == 0)
+    up2_fwd_kernel<<<blocks_for(gf.nvox() * c, 256), 256, 0, st>>>(gf, c, ctot, coff, (const __nv_bfloat16*)in,
+                                                                  (__nv_bfloat16*)out);
+  else
+    up2_bwd_kernel<<<blocks_for(gc.nvox() * c, 256), 256, 0, st>>>(gc, c, ctot, coff, (const float*)in, (float*)out);
+  return check_launch();
+}
+
+int pmg_nn_copy_channels(int64_t nvox, int c, int ctot, int coff, const void* in, void* out, void* stream) {
+  if (nvox <= 0 || c <= 0 || ctot < c + coff || coff < 0 || !in || !out) return PMG_BAD_ARG;
+  copy_channels_kernel<<<blocks_for(nvox * c, 256), 256, 0, as_stream(stream)>>>(nvox, c, ctot, coff,
+                                                                               (const __nv_bfloat16*)in,
+                                                                               (__nv_bfloat16*)out);
+  return check_launch();
+}
+
+int pmg_nn_split_channels(int64_t nvox, int c, int ctot, int coff, const float* dcat, float* dskip, void* stream) {
+  if (nvox <= 0 || c <= 0 || ctot < c + coff || coff < 0 || !dcat || !dskip) return PMG_BAD_ARG;
+  split_channels_kernel<<<blocks_for(nvox * c, 256), 256, 0, as_stream(stream)>>>(nvox, c, ctot, coff, dcat, dskip);
+  return check_launch();
+}
+
+int pmg_nn_input_features(int nelx, int nely, int nelz, int stride, int vnx, int vny, int vnz, const double* xe,
+                          void* feat, void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || nelz == 0 || stride < 1 || !vgrid_ok(vnx, vny, vnz) || !xe || !feat)
+    return PMG_BAD_ARG;
+  VGrid gv{vnx, vny, vnz};
+  input_features_kernel<<<blocks_for(gv.nvox(), 256), 256, 0, as_stream(stream)>>>(Grid{nelx, nely, nelz}, stride, gv,
+                                                                                 xe, (__nv_bfloat16*)feat);
+  return check_launch();
+}
+
+int pmg_nn_vox_to_node(int direction, int vnx, int vny, int vnz, const void* in, void* out, void* stream) {
+  if (!vgrid_ok(vnx, vny, vnz) || !in || !out) return PMG_BAD_ARG;
+  VGrid gv{vnx, vny, vnz};
+  cudaStream_t st = as_stream(stream);
+  if (direction == 0) {
+    const int64_t nn = (int64_t)(vnx + 1) * (vny + 1) * (vnz + 1);
+    vox_to_node_kernel<<<blocks_for(nn, 256), 256, 0, st>>>(gv, (const float*)in, (double*)out);
+  } else {
+    node_to_vox_adjoint_kernel<<<blocks_for(gv.nvox(), 256), 256, 0, st>>>(gv, (const float*)in, (float*)out);
+  }
+  return check_launch();
+}
+
+int pmg_nn_adam(int n, float* w, const float* g, float* m, float* v, void* w_bf16, float lr, float beta1, float beta2,
+                float eps, int step, float weight_decay, void* stream) {
+  if (n <= 0 || !w || !g || !m || !v || step < 1) return PMG_BAD_ARG;
+  const float c1 = 1.f - powf(beta1, (float)step), c2 = 1.f - powf(beta2, (float)step);
+  adam_kernel<<<(n + 255) / 256, 256, 0, as_stream(stream)>>>(n, w, g, m, v, (__nv_bfloat16*)w_bf16, lr, beta1, beta2,
+                                                             eps, c1, c2, weight_decay);
+  return check_launch();
+}
+
+int pmg_nn_mse(int64_t n, const double* pred, const double* target, const uint8_t* dof_mask, float* grad,
+               double* loss_partial, void* stream) {
+  if (n <= 0 || !pred || !target || !grad || !loss_partial) return PMG_BAD_ARG;
+  mse_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(n, pred, target, dof_mask, 1.0 / (double)n, grad,
+                                                               loss_partial);
+  return check_launch();
+}
+
+}  // extern "C"

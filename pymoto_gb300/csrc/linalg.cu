@@ -203,6 +203,42 @@ __global__ void diag_scale_kernel(int64_t n, const T* __restrict__ b, const T* _
   PMG_ILP_LOOP(n, y[i] = w * (b[i] / diag[i]))
 }
 
+// Chebyshev smoothing (polynomial in D^-1 A on [lmax/ratio, lmax]; Saad, Iterative Methods for Sparse
+// Linear Systems, 2nd ed., Alg. 12.1): step j updates d <- a_j d + c_j D^-1 r, x <- x + d, with
+// a_0 = 0, c_0 = 1/theta, a_j = rho_j rho_{j-1}, c_j = 2 rho_j / delta, rho_0 = 1/sigma,
+// rho_j = 1/(2 sigma - rho_{j-1}), theta = (lmax + lmin)/2, delta = (lmax - lmin)/2, sigma = theta/delta.
+__global__ void cheb_coeffs_kernel(const double* __restrict__ lmax_dev, double lmax_host, double ratio, int degree,
+                                   double* __restrict__ coef) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double hi = lmax_dev ? *lmax_dev : lmax_host;
+  if (!(hi > 0.0)) hi = 1.0;
+  const double lo = hi / ratio;
+  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+  double rho = 1.0 / sigma;
+  coef[0] = 0.0;
+  coef[1] = 1.0 / theta;
+  for (int j = 1; j < degree; ++j) {
+    const double rn = 1.0 / (2.0 * sigma - rho);
+    coef[2 * j] = rn * rho;
+    coef[2 * j + 1] = 2.0 * rn / delta;
+    rho = rn;
+  }
+}
+
+// d = a_j d + c_j r / diag; x = x + d (init != 0: the first step from x = 0, d = c_0 r / diag, x = d)
+template <typename T>
+__global__ void cheb_step_kernel(int64_t n, const T* __restrict__ r, const T* __restrict__ diag, T* __restrict__ d,
+                                 T* __restrict__ x, const double* __restrict__ coef, int step, int init) {
+  const T a = (T)coef[2 * step], c = (T)coef[2 * step + 1];
+  if (init) {
+    PMG_ILP_LOOP(n, { const T v = c * (r[i] / diag[i]); d[i] = v; x[i] = v; })
+  } else if (step == 0) {   // a_0 = 0: d is not read
+    PMG_ILP_LOOP(n, { const T v = c * (r[i] / diag[i]); d[i] = v; x[i] += v; })
+  } else {
+    PMG_ILP_LOOP(n, { const T v = a * d[i] + c * (r[i] / diag[i]); d[i] = v; x[i] += v; })
+  }
+}
+
 inline unsigned stream_blocks(int64_t n) {
   int64_t b = (n + 256 * ILP - 1) / (256 * ILP);
   if (b > 65535) b = 65535;
@@ -216,28 +252,69 @@ inline unsigned stream_blocks(int64_t n) {
 constexpr int TB = 32;
 constexpr int CHOL_SMEM_MAX_N = 20000;  // x of a solve lives in shared memory (<= 160 KB in FP64)
 
-// Diagonal tile kb, factored in shared memory by one CTA with one barrier per column:
-// A[r][c] -= A[r][k] A[c][k] / A[k][k] on the unscaled columns, each column scaled by 1/sqrt of its final
-// pivot at the end (a non-positive pivot is recorded in *info and replaced by 1 so the sweep stays finite).
+// Diagonal tile kb, factored in shared memory by one CTA with one barrier per column (right-looking, on the
+// unscaled columns: T[r][c] -= T[r][k] T[c][k] / T[k][k]; column c is scaled by 1/sqrt(T[c][c]) at the end).
+// FP64 throughput is the limit here, so every thread owns fixed elements of the lower triangle, numbered
+// column by column: at step k only the elements of columns > k are live, and whole warps drop out as k
+// grows.  The reciprocal pivot of step k+1 is computed once, by the owner of (k+1, k+1), right after its
+// step-k update.  A non-positive pivot is recorded in *info and replaced by 1 so the sweep stays finite.
+// 1/d in FP64 from the FP32 reciprocal by two Newton-Raphson steps r <- r + r (1 - d r) (quadratic
+// convergence: 2^-23 -> 2^-46 -> below FP64 rounding).  Used for the pivots of the factorisation, which
+// lie well inside the FP32 range for stiffness matrices.
+__device__ __forceinline__ double recip_newton(double d) {
+  double r = (double)__frcp_rn((float)d);
+  r = fma(r, fma(-d, r, 1.0), r);
+  r = fma(r, fma(-d, r, 1.0), r);
+  return r;
+}
+
 constexpr int CHOL_THREADS = 256;
+constexpr int TRI_ELEMS = TB * (TB + 1) / 2;                              // 528
+constexpr int TRI_PER_THREAD = (TRI_ELEMS + CHOL_THREADS - 1) / CHOL_THREADS;   // 3
 
 __global__ void __launch_bounds__(CHOL_THREADS) chol_diag_kernel(int n, double* A, int kb, int* info) {
   __shared__ double T[TB][TB + 1];
-  __shared__ double rdiag[TB];
+  __shared__ double rinv[TB];
+  __shared__ double rsq[TB];
   const int k0 = kb * TB;
   const int nb = min(TB, n - k0);
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
     const int r = e / TB, c = e % TB;
     T[r][c] = (r < nb && c < nb) ? A[(int64_t)(k0 + r) * n + k0 + c] : (r == c ? 1.0 : 0.0);
   }
+  // owned elements: packed column-major index q -> (r, c), r >= c
+  int er[TRI_PER_THREAD], ec[TRI_PER_THREAD];
+#pragma unroll
+  for (int m = 0; m < TRI_PER_THREAD; ++m) {
+    const int q = threadIdx.x + m * CHOL_THREADS;
+    int c = 0, off = 0;
+    while (c < TB && off + (TB - c) <= q) {   // at most 32 steps, once per kernel
+      off += TB - c;
+      ++c;
+    }
+    ec[m] = q < TRI_ELEMS ? c : -1;
+    er[m] = q < TRI_ELEMS ? c + (q - off) : -1;
+  }
   __syncthreads();
-  for (int k = 0; k < nb; ++k) {
-    double d = T[k][k];
+  if (threadIdx.x == 0) {
+    double d = T[0][0];
     if (!(d > 0.0)) d = 1.0;
-    const double rd = 1.0 / d;
-    for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
-      const int r = e / TB, c = e % TB;
-      if (c > k && r >= c && r < nb) T[r][c] -= T[r][k] * T[c][k] * rd;
+    rinv[0] = recip_newton(d);
+  }
+  __syncthreads();
+  for (int k = 0; k < nb - 1; ++k) {
+    const double rk = rinv[k];
+#pragma unroll
+    for (int m = 0; m < TRI_PER_THREAD; ++m) {
+      const int r = er[m], c = ec[m];
+      if (c > k) {
+        T[r][c] = fma(-T[r][k] * rk, T[c][k], T[r][c]);
+        if (r == k + 1 && c == k + 1) {
+          double d = T[r][c];
+          if (!(d > 0.0)) d = 1.0;
+          rinv[k + 1] = recip_newton(d);
+        }
+      }
     }
     __syncthreads();
   }
@@ -248,81 +325,243 @@ __global__ void __launch_bounds__(CHOL_THREADS) chol_diag_kernel(int n, double* 
       atomicCAS(info, 0, k0 + c + 1);
       d = 1.0;
     }
-    rdiag[c] = 1.0 / sqrt(d);
+    rsq[c] = rsqrt(d);
   }
   __syncthreads();
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
     const int r = e / TB, c = e % TB;
-    if (r < nb && c < nb) A[(int64_t)(k0 + r) * n + k0 + c] = c <= r ? T[r][c] * rdiag[c] : 0.0;
+    if (r < nb && c < nb) A[(int64_t)(k0 + r) * n + k0 + c] = c <= r ? T[r][c] * rsq[c] : 0.0;
   }
 }
 
-// Panel: L[ib,kb] = A[ib,kb] L[kb,kb]^{-T}, one CTA of TB threads per tile row ib > kb within the band, one
-// row per thread (x L^T = a by forward substitution with the reciprocal pivots).
-__global__ void __launch_bounds__(TB) chol_panel_kernel(int n, double* A, int kb, int bw) {
+// Panel: L[i, kb] = A[i, kb] L[kb,kb]^{-T} for the rows i below the diagonal tile within the band, one warp
+// per row (lane c holds entry c; forward substitution with the reciprocal pivots, broadcast by shuffles).
+constexpr int PANEL_WARPS = 8;
+__global__ void __launch_bounds__(PANEL_WARPS * 32) chol_panel_kernel(int n, double* A, int kb, int bw) {
   __shared__ double L[TB][TB + 1];
-  __shared__ double rinv[TB];
+  __shared__ double rp[TB];
   const int k0 = kb * TB;
   const int nb = min(TB, n - k0);
-  const int ib = kb + 1 + blockIdx.x;
-  const int i0 = ib * TB;
-  if (i0 >= n || i0 - (k0 + nb - 1) > bw) return;
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
     const int r = e / TB, c = e % TB;
-    L[r][c] = (r < nb && c < nb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
+    L[r][c] = (r < nb && c < nb && c <= r) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
   }
   __syncthreads();
-  if (threadIdx.x < nb) rinv[threadIdx.x] = 1.0 / L[threadIdx.x][threadIdx.x];
+  if (threadIdx.x < TB) rp[threadIdx.x] = threadIdx.x < nb ? recip_newton(L[threadIdx.x][threadIdx.x]) : 0.0;
   __syncthreads();
-  const int row = i0 + threadIdx.x;
-  if (row < n) {
-    double x[TB];
-#pragma unroll
-    for (int c = 0; c < TB; ++c) x[c] = c < nb ? A[(int64_t)row * n + k0 + c] : 0.0;
-#pragma unroll
-    for (int c = 0; c < TB; ++c) {
-      if (c < nb) {
-        double v = x[c];
-#pragma unroll
-        for (int q = 0; q < TB; ++q)
-          if (q < c) v -= x[q] * L[c][q];
-        x[c] = v * rinv[c];
-      }
+  const int lane = threadIdx.x & 31;
+  const int row = k0 + nb + blockIdx.x * PANEL_WARPS + (threadIdx.x >> 5);
+  if (row >= n || row - (k0 + nb - 1) > bw) return;   // whole warps exit together
+  double x = lane < nb ? A[(int64_t)row * n + k0 + lane] : 0.0;
+  for (int c = 0; c < nb; ++c) {
+    if (lane == c) x *= rp[c];
+    const double xc = __shfl_sync(0xffffffffu, x, c);
+    if (lane > c) x = fma(-L[lane][c], xc, x);
+  }
+  if (lane < nb) A[(int64_t)row * n + k0 + lane] = x;
+}
+
+// Trailing update A[i][j] -= sum_q L[i][k0+q] L[j][k0+q] over the rows/columns below the diagonal tile within
+// the band (j <= i), one 16 x 16 output tile per CTA (one element per thread).
+constexpr int UT = 16;
+__global__ void __launch_bounds__(UT * UT) chol_update_kernel(int n, double* A, int kb, int bw, int nt) {
+  __shared__ double Li[UT][TB + 1];
+  __shared__ double Lj[UT][TB + 1];
+  const int k0 = kb * TB;
+  const int nb = min(TB, n - k0);
+  const int base = k0 + nb;
+  const int last = min(n - 1, k0 + nb - 1 + bw);   // last row with a nonzero in this block column
+  // lower-triangular tile enumeration: t -> (ti, tj), tj <= ti
+  const int t = blockIdx.x;
+  int ti = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+  while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+  while (ti * (ti + 1) / 2 > t) --ti;
+  const int tj = t - ti * (ti + 1) / 2;
+  if (ti >= nt) return;
+  const int i0 = base + ti * UT, j0 = base + tj * UT;
+  if (i0 > last || j0 > last) return;
+  if (i0 - (j0 + UT - 1) > bw) return;            // tile entirely outside the band
+  for (int e = threadIdx.x; e < UT * TB; e += blockDim.x) {
+    const int r = e / TB, c = e % TB;
+    Li[r][c] = (i0 + r <= last && c < nb) ? A[(int64_t)(i0 + r) * n + k0 + c] : 0.0;
+    Lj[r][c] = (j0 + r <= last && c < nb) ? A[(int64_t)(j0 + r) * n + k0 + c] : 0.0;
+  }
+  __syncthreads();
+  const int r = threadIdx.x / UT, c = threadIdx.x % UT;
+  const int row = i0 + r, col = j0 + c;
+  if (row > last || col > row || row - col > bw) return;
+  double s = 0.0;
+#pragma unroll 8
+  for (int q = 0; q < TB; ++q) s = fma(Li[r][q], Lj[c][q], s);
+  A[(int64_t)row * n + col] -= s;
+}
+
+// Inverses of the diagonal tiles of the factor, for the blocked triangular solves: Dinv[b] = L[b,b]^{-1}
+// (lower triangular, row-major TB x TB, zero-padded for a ragged last tile).  One CTA per tile; warp w
+// computes columns w, w+8, ... by forward substitution with lanes as rows.
+template <typename T>
+__global__ void __launch_bounds__(256) chol_block_inverse_kernel(int n, const double* __restrict__ L,
+                                                                 T* __restrict__ Dinv) {
+  __shared__ double Ls[TB][TB + 1];
+  __shared__ double rp[TB];
+  const int k0 = blockIdx.x * TB;
+  const int nb = min(TB, n - k0);
+  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
+    const int r = e / TB, c = e % TB;
+    Ls[r][c] = (r < nb && c < nb && c <= r) ? L[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x < TB) rp[threadIdx.x] = threadIdx.x < nb ? recip_newton(Ls[threadIdx.x][threadIdx.x]) : 0.0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* D = Dinv + (int64_t)blockIdx.x * TB * TB;
+  for (int j = warp; j < TB; j += 8) {
+    double x = (lane == j) ? 1.0 : 0.0;
+    for (int c = j; c < nb; ++c) {
+      if (lane == c) x *= rp[c];
+      const double xc = __shfl_sync(0xffffffffu, x, c);
+      if (lane > c) x = fma(-Ls[lane][c], xc, x);
     }
-#pragma unroll
-    for (int c = 0; c < TB; ++c)
-      if (c < nb) A[(int64_t)row * n + k0 + c] = x[c];
+    D[lane * TB + j] = (lane < nb && j < nb && lane >= j) ? (T)x : T(0);
   }
 }
 
-// Trailing update A[ib,jb] -= L[ib,kb] L[jb,kb]^T for kb < jb <= ib within the band; one CTA per tile.
-__global__ void chol_update_kernel(int n, double* A, int kb, int bw, int ntiles_band) {
-  __shared__ double Li[TB][TB + 1];
-  __shared__ double Lj[TB][TB + 1];
-  const int k0 = kb * TB;
-  const int nb = min(TB, n - k0);
-  // tile enumeration: jb = kb+1+tj, ib = jb + ti, with ti, tj < ntiles_band
-  const int tj = blockIdx.x % ntiles_band, ti = blockIdx.x / ntiles_band;
-  const int jb = kb + 1 + tj, ib = jb + ti;
-  const int i0 = ib * TB, j0 = jb * TB;
-  if (i0 >= n || j0 >= n) return;
-  if (i0 - (k0 + nb - 1) > bw || j0 - (k0 + nb - 1) > bw) return;  // L tiles are zero
-  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
-    const int r = e / TB, c = e % TB;
-    Li[r][c] = (i0 + r < n && c < nb) ? A[(int64_t)(i0 + r) * n + k0 + c] : 0.0;
-    Lj[r][c] = (j0 + r < n && c < nb) ? A[(int64_t)(j0 + r) * n + k0 + c] : 0.0;
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
-    const int r = e / TB, c = e % TB;
-    const int row = i0 + r, col = j0 + c;
-    if (row < n && col < n && col <= row) {
-      double s = 0.0;
-#pragma unroll 8
-      for (int q = 0; q < TB; ++q) s = fma(Li[r][q], Lj[c][q], s);
-      A[(int64_t)row * n + col] -= s;
+// FP32 inverse of a banded FP64 factor for the FP32 coarse solve: XT = (L^{-1})^T row by row, one warp
+// per column c of L^{-1} (x = L^{-1} e_c by tiles: x_B = Dinv[b] (e_c - L[B, <B] x_<B), lanes as the rows of
+// the tile), then Ainv = XT XT^T (= L^{-T} L^{-1}) by a tiled product.  L32 is the FP32 copy of the factor.
+constexpr int TRINV_WARPS = 8;
+__global__ void __launch_bounds__(TRINV_WARPS * 32) chol_trinv_f32_kernel(int n, const float* __restrict__ L32, int bw,
+                                                                         const float* __restrict__ Dinv,
+                                                                         float* __restrict__ XT) {
+  extern __shared__ __align__(16) unsigned char c_smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int c = blockIdx.x * TRINV_WARPS + warp;
+  if (c >= n) return;   // whole warps
+  float* x = reinterpret_cast<float*>(c_smem) + (size_t)warp * n;
+  const int nblk = (n + TB - 1) / TB;
+  const int bc = c / TB;
+  float* out = XT + (int64_t)c * n;
+  for (int i = lane; i < bc * TB; i += 32) out[i] = 0.f;
+  for (int kb = bc; kb < nblk; ++kb) {
+    const int k0 = kb * TB;
+    const int nb = min(TB, n - k0);
+    const int i = k0 + lane;
+    float t = 0.f;
+    if (kb == bc) {
+      t = (i == c) ? 1.f : 0.f;
+    } else if (lane < nb) {
+      const float* Lr = L32 + (int64_t)i * n;
+      float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;   // four independent chains
+      int j = max(c, k0 - bw);
+      for (; j + 4 <= k0; j += 4) {
+        p0 = fmaf(Lr[j], x[j], p0);
+        p1 = fmaf(Lr[j + 1], x[j + 1], p1);
+        p2 = fmaf(Lr[j + 2], x[j + 2], p2);
+        p3 = fmaf(Lr[j + 3], x[j + 3], p3);
+      }
+      for (; j < k0; ++j) p0 = fmaf(Lr[j], x[j], p0);
+      t = -((p0 + p1) + (p2 + p3));
     }
+    const float* D = Dinv + (int64_t)kb * TB * TB + lane * TB;
+    float acc = 0.f;
+#pragma unroll 8
+    for (int q = 0; q < TB; ++q) acc = fmaf(D[q], __shfl_sync(0xffffffffu, t, q), acc);
+    if (lane < nb) {
+      x[i] = acc;
+      out[i] = acc;
+    }
+    __syncwarp();
   }
+}
+
+// C = XT XT^T for an n x n row-major XT (upper triangular: XT[i][k] = 0 for k < i), 32 x 32 output tiles.
+__global__ void __launch_bounds__(256) syrk_f32_kernel(int n, const float* __restrict__ XT, float* __restrict__ C) {
+  __shared__ float As[32][33];
+  __shared__ float Bs[32][33];
+  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 8 rows of 4 outputs each
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int k0 = max(i0, j0) & ~31; k0 < n; k0 += 32) {
+    for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+      const int r = e >> 5, q = e & 31;
+      As[r][q] = (i0 + r < n && k0 + q < n) ? XT[(int64_t)(i0 + r) * n + k0 + q] : 0.f;
+      Bs[r][q] = (j0 + r < n && k0 + q < n) ? XT[(int64_t)(j0 + r) * n + k0 + q] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int q = 0; q < 32; ++q) {
+      const float bv = Bs[tx][q];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) acc[m] = fmaf(As[ty * 4 + m][q], bv, acc[m]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int i = i0 + ty * 4 + m, j = j0 + tx;
+    if (i < n && j < n) C[(int64_t)i * n + j] = acc[m];
+  }
+}
+
+// x = (L L^T)^{-1} b by one CTA with the tile inverses: forward, per tile b: t = x_B - L[B, <B] x_<B (warps
+// over rows, lanes over the band columns), x_B = Dinv[b] t; backward, per tile (descending):
+// x_B = Dinv[b]^T x_B, then x_j -= sum_{i in B} L[i][j] x_i for the band columns j before the tile.
+template <typename T>
+__global__ void __launch_bounds__(256) chol_solve_blocked_kernel(int n, const T* __restrict__ L, int bw,
+                                                                 const T* __restrict__ Dinv,
+                                                                 const T* __restrict__ b, T* __restrict__ x) {
+  extern __shared__ __align__(16) unsigned char c_smem[];
+  T* xs = reinterpret_cast<T*>(c_smem);
+  __shared__ T Ds[TB][TB + 1];
+  __shared__ T tv[TB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = b[i];
+  const int nblk = (n + TB - 1) / TB;
+  for (int kb = 0; kb < nblk; ++kb) {
+    const int k0 = kb * TB;
+    const int nb = min(TB, n - k0);
+    const T* Dg = Dinv + (int64_t)kb * TB * TB;
+    for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) Ds[e / TB][e % TB] = Dg[e];
+    __syncthreads();
+    const int jbeg = max(0, k0 - bw);
+    for (int rr = warp; rr < nb; rr += 8) {
+      const T* Lr = L + (int64_t)(k0 + rr) * n;
+      T acc = T(0);
+      for (int j = jbeg + lane; j < k0; j += 32) acc += Lr[j] * xs[j];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) tv[rr] = xs[k0 + rr] - acc;
+    }
+    __syncthreads();
+    if (warp == 0 && lane < nb) {
+      T acc = T(0);
+      for (int c = 0; c <= lane; ++c) acc += Ds[lane][c] * tv[c];
+      xs[k0 + lane] = acc;
+    }
+    __syncthreads();
+  }
+  for (int kb = nblk - 1; kb >= 0; --kb) {
+    const int k0 = kb * TB;
+    const int nb = min(TB, n - k0);
+    const T* Dg = Dinv + (int64_t)kb * TB * TB;
+    for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) Ds[e / TB][e % TB] = Dg[e];
+    if (threadIdx.x < TB) tv[threadIdx.x] = threadIdx.x < nb ? xs[k0 + threadIdx.x] : T(0);
+    __syncthreads();
+    if (warp == 0 && lane < nb) {
+      T acc = T(0);
+      for (int r = lane; r < nb; ++r) acc += Ds[r][lane] * tv[r];
+      xs[k0 + lane] = acc;
+    }
+    __syncthreads();
+    const int jbeg = max(0, k0 - bw);
+    for (int j = jbeg + threadIdx.x; j < k0; j += blockDim.x) {
+      T acc = T(0);
+      for (int r = 0; r < nb; ++r) acc += L[(int64_t)(k0 + r) * n + j] * xs[k0 + r];
+      xs[j] -= acc;
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xs[i];
 }
 
 // x = (L L^T)^{-1} x in place (x in shared memory) for a banded lower factor, by one CTA: forward then
@@ -599,6 +838,28 @@ int pmg_diag_scale(int dtype, int64_t n, const void* b, const void* diag, double
   return check_launch();
 }
 
+int pmg_cheb_coeffs(const double* lmax_dev, double lmax_host, double ratio, int degree, double* coef, void* stream) {
+  if (degree < 1 || degree > 64 || !(ratio > 1.0) || !coef) return PMG_BAD_ARG;
+  cheb_coeffs_kernel<<<1, 32, 0, as_stream(stream)>>>(lmax_dev, lmax_host, ratio, degree, coef);
+  return check_launch();
+}
+
+int pmg_cheb_step(int dtype, int64_t n, const void* r, const void* diag, void* d, void* x, const double* coef, int step,
+                  int init, void* stream) {
+  if (n < 0 || !r || !diag || !d || !x || !coef || step < 0 || step >= 64) return PMG_BAD_ARG;
+  if (n == 0) return PMG_OK;
+  cudaStream_t st = as_stream(stream);
+  if (dtype == PMG_F64)
+    cheb_step_kernel<double><<<stream_blocks(n), 256, 0, st>>>(n, (const double*)r, (const double*)diag, (double*)d,
+                                                              (double*)x, coef, step, init);
+  else if (dtype == PMG_F32)
+    cheb_step_kernel<float><<<stream_blocks(n), 256, 0, st>>>(n, (const float*)r, (const float*)diag, (float*)d,
+                                                             (float*)x, coef, step, init);
+  else
+    return PMG_BAD_ARG;
+  return check_launch();
+}
+
 int pmg_cholesky_factor(int n, double* A, int bw, int* info, void* stream) {
   if (n <= 0 || !A || !info || bw < 0) return PMG_BAD_ARG;
   cudaStream_t st = as_stream(stream);
@@ -608,16 +869,103 @@ int pmg_cholesky_factor(int n, double* A, int bw, int* info, void* stream) {
     return PMG_CUDA_ERR;
   }
   const int nblk = (n + TB - 1) / TB;
-  const int band_tiles = min(nblk, bw / TB + 2);
   for (int kb = 0; kb < nblk; ++kb) {
     chol_diag_kernel<<<1, CHOL_THREADS, 0, st>>>(n, A, kb, info);
-    const int rem = nblk - kb - 1;
-    if (rem <= 0) break;
-    const int pt = min(rem, band_tiles);
-    chol_panel_kernel<<<pt, TB, 0, st>>>(n, A, kb, bw);
-    chol_update_kernel<<<pt * pt, 256, 0, st>>>(n, A, kb, bw, pt);
+    const int k0 = kb * TB, nb = min(TB, n - k0);
+    const int rows = min(n - (k0 + nb), bw);      // band rows below the tile
+    if (rows <= 0) continue;
+    chol_panel_kernel<<<(rows + PANEL_WARPS - 1) / PANEL_WARPS, PANEL_WARPS * 32, 0, st>>>(n, A, kb, bw);
+    const int nt = (rows + UT - 1) / UT;
+    chol_update_kernel<<<nt * (nt + 1) / 2, UT * UT, 0, st>>>(n, A, kb, bw, nt);
     const int rc = check_launch();
     if (rc != PMG_OK) return rc;
+  }
+  return check_launch();
+}
+
+int pmg_cholesky_block_inverses(int dtype, int n, const double* L, void* Dinv, void* stream) {
+  if (n <= 0 || !L || !Dinv || (const void*)L == Dinv) return PMG_BAD_ARG;
+  const int nblk = (n + TB - 1) / TB;
+  cudaStream_t st = as_stream(stream);
+  if (dtype == PMG_F64)
+    chol_block_inverse_kernel<double><<<nblk, 256, 0, st>>>(n, L, (double*)Dinv);
+  else if (dtype == PMG_F32)
+    chol_block_inverse_kernel<float><<<nblk, 256, 0, st>>>(n, L, (float*)Dinv);
+  else
+    return PMG_BAD_ARG;
+  return check_launch();
+}
+
+size_t pmg_cholesky_inverse_f32_scratch_bytes(int n) {
+  if (n <= 0) return 0;
+  const size_t nblk = (size_t)(n + TB - 1) / TB;
+  return sizeof(float) * ((size_t)n * n * 2 + nblk * TB * TB);
+}
+
+int pmg_cholesky_inverse_f32(int n, const double* L, int bw, void* scratch, float* Ainv, void* stream) {
+  if (n <= 0 || n > CHOL_SMEM_MAX_N || !L || !scratch || !Ainv || bw < 0) return PMG_BAD_ARG;
+  cudaStream_t st = as_stream(stream);
+  const int nblk = (n + TB - 1) / TB;
+  float* L32 = reinterpret_cast<float*>(scratch);
+  float* XT = L32 + (size_t)n * n;
+  float* Dinv = XT + (size_t)n * n;
+  chol_block_inverse_kernel<float><<<nblk, 256, 0, st>>>(n, L, Dinv);
+  convert_kernel<double, float><<<stream_blocks((int64_t)n * n), 256, 0, st>>>((int64_t)n * n, L, L32, 1.0);
+  // warps per CTA bounded by the shared memory for their columns (n floats each)
+  const size_t smem = sizeof(float) * (size_t)n * TRINV_WARPS;
+  static size_t smem_set[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return check_launch();
+  if (smem > 200 * 1024) return PMG_BAD_ARG;
+  if (smem > smem_set[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(chol_trinv_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      set_error(cudaGetErrorString(e));
+      return PMG_CUDA_ERR;
+    }
+    smem_set[dev] = smem;
+  }
+  chol_trinv_f32_kernel<<<(n + TRINV_WARPS - 1) / TRINV_WARPS, TRINV_WARPS * 32, smem, st>>>(n, L32, bw, Dinv, XT);
+  const dim3 grid(nblk, nblk);
+  syrk_f32_kernel<<<grid, 256, 0, st>>>(n, XT, Ainv);
+  return check_launch();
+}
+
+int pmg_cholesky_solve_blocked(int dtype, int n, const void* L, int bw, const void* Dinv, const void* b, void* x,
+                               void* stream) {
+  if (n <= 0 || n > CHOL_SMEM_MAX_N || !L || !Dinv || !b || !x || bw < 0 || b == x) return PMG_BAD_ARG;
+  cudaStream_t st = as_stream(stream);
+  const size_t smem = (dtype == PMG_F64 ? sizeof(double) : sizeof(float)) * (size_t)n;
+  cudaError_t e = cudaSuccess;
+  // the opt-in above the default dynamic shared memory limit, raised once per size (x lives in smem)
+  static size_t smem_set[2][64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return check_launch();
+  const int ti = dtype == PMG_F64 ? 0 : 1;
+  if (dtype == PMG_F64) {
+    if (smem > smem_set[ti][dev]) {
+      e = cudaFuncSetAttribute(chol_solve_blocked_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e == cudaSuccess) smem_set[ti][dev] = smem;
+    }
+    if (e == cudaSuccess)
+      chol_solve_blocked_kernel<double><<<1, 256, smem, st>>>(n, (const double*)L, bw, (const double*)Dinv,
+                                                              (const double*)b, (double*)x);
+  } else if (dtype == PMG_F32) {
+    if (smem > smem_set[ti][dev]) {
+      e = cudaFuncSetAttribute(chol_solve_blocked_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e == cudaSuccess) smem_set[ti][dev] = smem;
+    }
+    if (e == cudaSuccess)
+      chol_solve_blocked_kernel<float><<<1, 256, smem, st>>>(n, (const float*)L, bw, (const float*)Dinv,
+                                                             (const float*)b, (float*)x);
+  } else {
+    return PMG_BAD_ARG;
+  }
+  if (e != cudaSuccess) {
+    set_error(cudaGetErrorString(e));
+    return PMG_CUDA_ERR;
   }
   return check_launch();
 }

@@ -276,6 +276,24 @@ __global__ void stencil_diag_kernel(Grid g, const T* __restrict__ S, T* __restri
   for (int d = 0; d < DIM; ++d) diag[n * DIM + d] = S[((int64_t)(C * DIM + d) * DIM + d) * nn + n];
 }
 
+// Row sums of |A| of a stencil operator, per dof (the l1-Jacobi diagonal: with it the spectrum of
+// D_l1^-1 A lies in (0, 1] by Gershgorin's theorem, whatever the contrast of the element scaling).
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) stencil_rowabs_kernel(Grid g, const T* __restrict__ S, T* __restrict__ out) {
+  constexpr int NOFF = Traits<DIM>::NOFF;
+  const int64_t nn = g.nnodes();
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nn * DIM) return;
+  const int d = (int)(t / nn);
+  const int64_t n = t - (int64_t)d * nn;
+  T sum = T(0);
+#pragma unroll
+  for (int o = 0; o < NOFF; ++o)
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) sum += fabs(S[((int64_t)(o * DIM + d) * DIM + c) * nn + n]);
+  out[n * DIM + d] = sum;
+}
+
 // ------------------------------------------------------------------------------------------ transfers
 // weight of a fine node at signed offset a (in fine units) from a coarse node: 1 at 0, 1/2 at +-1
 __device__ __forceinline__ double tw(int a) { return a == 0 ? 1.0 : 0.5; }
@@ -796,6 +814,14 @@ int pmg_stencil_diagonal(int dtype, int nelx, int nely, int nelz, const void* S,
   PMG_DISPATCH(dtype, g.dim(),
                (launch_simple<T, DIM>(stencil_diag_kernel<T, DIM>, g.nnodes(), as_stream(stream), g, (const T*)S,
                                       (T*)diag)));
+}
+
+int pmg_stencil_rowabs(int dtype, int nelx, int nely, int nelz, const void* S, void* out, void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !S || !out) return PMG_BAD_ARG;
+  Grid g{nelx, nely, nelz};
+  PMG_DISPATCH(dtype, g.dim(),
+               (launch_simple<T, DIM>(stencil_rowabs_kernel<T, DIM>, g.nnodes() * DIM, as_stream(stream), g,
+                                      (const T*)S, (T*)out)));
 }
 
 static bool even_grid(int nx, int ny, int nz) { return nx % 2 == 0 && ny % 2 == 0 && nz % 2 == 0 && nx >= 2 && ny >= 2; }

@@ -138,9 +138,9 @@ class StiffnessOperator:
         op.persistent = True
         return op
 
-    def assign(self, other):
-        """Copy the element scaling of `other` (any precision) into this operator's buffer and refresh the
-        derived stencil and diagonal in place."""
+    def assign(self, other, derived=True):
+        """Copy the element scaling of `other` (any precision) into this operator's buffer and (derived=True)
+        refresh the derived stencil and diagonal in place; derived=False leaves that to refresh_derived()."""
         if other is self:
             return self
         if other.grid.dims != self.grid.dims:
@@ -148,6 +148,12 @@ class StiffnessOperator:
         src = other._xe64 if other._xe64 is not None else other.xe
         call("pmg_convert", _lib.dtype_code(src), self.code, src.numel(), src, self.xe, 1.0, stream())
         self.bcmask, self.bcdiag = other.bcmask, other.bcdiag
+        if derived:
+            self.refresh_derived()
+        return self
+
+    def refresh_derived(self):
+        """Reassemble the stencil and the diagonal (when they exist) from the current element scaling."""
         if self._S is not None:
             self._assemble_stencil(self._S)
         if self._diag is not None:

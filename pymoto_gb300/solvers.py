@@ -101,20 +101,82 @@ class DampedJacobi(Preconditioner):
         return out
 
 
+class Chebyshev(Preconditioner):
+    """Chebyshev polynomial smoother on the l1-Jacobi scaled operator (Saad, Iterative Methods for Sparse
+    Linear Systems, Alg. 12.1; l1 smoothers: Baker, Falgout, Kolev, Yang, SIAM J. Sci. Comput. 33 (2011)).
+
+    An extension of the reference's DampedJacobi smoother (pymoto/solvers/iterative.py:21-47): `degree`
+    steps preconditioned by D_l1 = diag(sum_j |A_ij|) with the weights of the Chebyshev polynomial on
+    [1/ratio, 1].  By Gershgorin's theorem the spectrum of D_l1^-1 A lies in (0, 1] for any element scaling,
+    so no eigenvalue estimate is needed and no mode is amplified, however high the density contrast.  The
+    l1 diagonal of a stencil operator is its row sums of |A|; for the matrix-free finest operator the
+    element bound sum_e x_e sum_j |K0_aj| (>= the assembled row sum) is used.  The step coefficients live in
+    device memory, so a captured V-cycle stays valid across updates.
+    """
+
+    def __init__(self, A=None, degree=2, ratio=10.0):
+        if degree < 1:
+            raise ValueError("degree must be >= 1")
+        if not ratio > 1.0:
+            raise ValueError("ratio must be > 1")
+        self.degree = int(degree)
+        self.ratio = float(ratio)
+        self.D = None
+        self.coef = None
+        super().__init__(A)
+
+    @staticmethod
+    def l1_element_matrix(K0):
+        """diag(sum_j |K0_aj|): fed to the diagonal kernel it yields the matrix-free l1 diagonal."""
+        K0 = np.asarray(K0, dtype=np.float64)
+        return np.diag(np.abs(K0).sum(axis=1))
+
+    def update(self, A):
+        n = A.grid.ndof
+        if self.D is None or self.D.numel() != n or self.D.dtype != A.torch_dtype or self.D.device != A.device:
+            self.D = torch.empty(n, dtype=A.torch_dtype, device=A.device)
+            self.coef = torch.zeros(2 * self.degree, dtype=torch.float64, device=A.device)
+            call("pmg_cheb_coeffs", None, 1.0, self.ratio, self.degree, self.coef, stream())
+        g = A.grid
+        if isinstance(A, StencilOperator):
+            call("pmg_stencil_rowabs", A.code, g.nelx, g.nely, g.nelz, A.S, self.D, stream())
+        else:
+            call("pmg_ebe_diagonal", A.code, g.nelx, g.nely, g.nelz, A.xe, self.l1_element_matrix(A.K0), A.bcmask,
+                 A.bcdiag, self.D, stream())
+
+    def smooth(self, A, b, x, d, r, zero_start):
+        """`degree` steps on x (in place); d and r are work vectors of the size of b."""
+        code, n, st = A.code, b.numel(), stream()
+        j0 = 0
+        if zero_start:
+            call("pmg_cheb_step", code, n, b, self.D, d, x, self.coef, 0, 1, st)
+            j0 = 1
+        for j in range(j0, self.degree):
+            A.apply(RESIDUAL, x, b, out=r)
+            call("pmg_cheb_step", code, n, r, self.D, d, x, self.coef, j, 0, st)
+        return x
+
+    def solve(self, rhs, x0=None, trans="N"):
+        raise NotImplementedError("Chebyshev is a multigrid smoother (GeometricMultigrid calls smooth())")
+
+
 class DenseCholesky(LinearSolver):
     """Direct solve of the coarsest Galerkin operator: dense FP64 banded Cholesky on the device.
 
     Stands in for SolverSparseLU (pymoto/solvers/sparse.py:515-555), which auto_determine_solver picks for
-    the coarse sparse matrix (pymoto/solvers/auto_determine.py:109-122).  The factorisation is FP64; an
-    FP32 copy of the factor serves FP32 right-hand sides.
+    the coarse sparse matrix (pymoto/solvers/auto_determine.py:109-122).  The factorisation is always FP64.
+    FP64 operators (small enough) get the explicit FP64 inverse, so that each solve is one dense product;
+    FP32 operators (the mixed-precision hierarchy) get an FP32 copy of the factor and of its diagonal-tile
+    inverses, and each solve is a blocked forward/backward substitution without any scalar recurrence.
     """
 
     MAX_DOFS = 20000
-    INVERSE_MAX_DOFS = 4096   # up to this size the solve is one dense product with the explicit inverse
+    INVERSE_MAX_DOFS = 4096   # FP64: up to this size the solve is one dense product with the explicit inverse
 
     def __init__(self, A=None):
         self.L = None
         self.L32 = None
+        self.Dinv32 = None
         self.Ainv = None
         self.Ainv32 = None
         super().__init__(A)
@@ -127,40 +189,59 @@ class DenseCholesky(LinearSolver):
             raise ValueError(f"coarsest level has {n} dofs (> {self.MAX_DOFS}); add multigrid levels")
         self.n = n
         self.bw = A.bandwidth()
+        self.code = A.code
         dev = A.device
         if self.L is None or self.L.shape[0] != n or self.L.device != dev:
             # device buffers kept across updates (stable addresses for captured CUDA graphs)
             self.L = torch.empty((n, n), dtype=torch.float64, device=dev)
             self._info = torch.zeros(1, dtype=torch.int32, device=dev)
-            self.Ainv = torch.empty_like(self.L) if n <= self.INVERSE_MAX_DOFS else None
-            self.Ainv32 = torch.empty((n, n), dtype=torch.float32, device=dev) if self.Ainv is not None else None
-            self.L32 = None
+            self.Ainv = self.L32 = self.Dinv32 = self.Ainv32 = None
         L = A.to_dense(out=self.L)
         call("pmg_cholesky_factor", n, L, self.bw, self._info, stream())
         bad = int(self._info.item())
         if bad != 0:
             raise np.linalg.LinAlgError(f"coarsest-level matrix not positive definite (pivot {bad - 1})")
-        if self.Ainv is not None:
+        if A.code == F64 and n <= self.INVERSE_MAX_DOFS:
+            if self.Ainv is None:
+                self.Ainv = torch.empty_like(self.L)
             call("pmg_cholesky_inverse", n, L, self.bw, self.Ainv, stream())
-            call("pmg_convert", F64, F32, n * n, self.Ainv, self.Ainv32, 1.0, stream())
         elif A.code == F32:
-            if self.L32 is None:
-                self.L32 = torch.empty((n, n), dtype=torch.float32, device=dev)
-            call("pmg_convert", F64, F32, n * n, self.L, self.L32, 1.0, stream())
+            self._prepare_f32()
+
+    def _prepare_f32(self):
+        n, dev = self.n, self.L.device
+        if n <= self.INVERSE_MAX_DOFS:
+            # explicit FP32 inverse from the FP64 factor: each solve is one dense product
+            if getattr(self, "Ainv32", None) is None:
+                nbytes = _lib.load().pmg_cholesky_inverse_f32_scratch_bytes(n)
+                self._inv_scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+                self.Ainv32 = torch.empty((n, n), dtype=torch.float32, device=dev)
+            call("pmg_cholesky_inverse_f32", n, self.L, self.bw, self._inv_scratch, self.Ainv32, stream())
+            return
+        if self.L32 is None:
+            self.L32 = torch.empty((n, n), dtype=torch.float32, device=dev)
+            self.Dinv32 = torch.empty(((n + 31) // 32) * 32 * 32, dtype=torch.float32, device=dev)
+        call("pmg_convert", F64, F32, n * n, self.L, self.L32, 1.0, stream())
+        call("pmg_cholesky_block_inverses", F32, n, self.L, self.Dinv32, stream())
 
     def solve(self, rhs, x0=None, trans="N"):
         code = _lib.dtype_code(rhs)
         out = getattr(self, "_out", None)
         if out is None or out.dtype != rhs.dtype or out.numel() != rhs.numel() or out.device != rhs.device:
             out = self._out = torch.empty_like(rhs)
-        if self.Ainv is not None:
-            Ai = self.Ainv if code == F64 else self.Ainv32
-            call("pmg_dense_gemv", code, self.n, Ai, rhs.contiguous(), out, stream())
+        if code == F64 and self.Ainv is not None:
+            call("pmg_dense_gemv", code, self.n, self.Ainv, rhs.contiguous(), out, stream())
             return out
-        L = self.L if code == F64 else self.L32
-        if L is None:
-            L = self.L32 = self.L.to(torch.float32)
-        call("pmg_cholesky_solve", code, self.n, L, self.bw, rhs.contiguous(), out, stream())
+        if code == F32:
+            if getattr(self, "Ainv32", None) is None and self.L32 is None:
+                self._prepare_f32()
+            if getattr(self, "Ainv32", None) is not None:
+                call("pmg_dense_gemv", F32, self.n, self.Ainv32, rhs.contiguous(), out, stream())
+            else:
+                call("pmg_cholesky_solve_blocked", F32, self.n, self.L32, self.bw, self.Dinv32, rhs.contiguous(),
+                     out, stream())
+            return out
+        call("pmg_cholesky_solve", code, self.n, self.L, self.bw, rhs.contiguous(), out, stream())
         return out
 
 
@@ -262,7 +343,9 @@ class GeometricMultigrid(Preconditioner):
 
     def _vcycle(self, b, x0=None):
         A, w, steps = self.A, None, self.smooth_steps
-        u, t, r = self._buf
+        u, t, r = self._buf[0], self._buf[1], self._buf[2]
+        if isinstance(self.smoother, Chebyshev):
+            return self._vcycle_chebyshev(b, x0)
         fused = type(self.smoother) is DampedJacobi
         if fused:
             w, D = self.smoother.w, self.smoother.D
@@ -299,14 +382,42 @@ class GeometricMultigrid(Preconditioner):
             self._buf[0], self._buf[1] = u, self._buf[0]
         return u
 
+    def _vcycle_chebyshev(self, b, x0=None):
+        A, sm = self.A, self.smoother
+        u, d, r = self._buf[0], self._buf[1], self._buf[2]
+        if x0 is None:
+            sm.smooth(A, b, u, d, r, zero_start=True)
+        else:
+            u.copy_(x0)
+            sm.smooth(A, b, u, d, r, zero_start=False)
+        A.apply(RESIDUAL, u, b, out=r)
+        g = self.grid
+        inner = self.inner_level
+        rc = self._rc
+        call("pmg_restrict", A.code, g.nelx, g.nely, g.nelz, r, rc, stream())
+        uc = inner._vcycle(rc) if isinstance(inner, GeometricMultigrid) else inner.solve(rc)
+        call("pmg_prolong_add", A.code, g.nelx, g.nely, g.nelz, uc, u, stream())
+        sm.smooth(A, b, u, d, r, zero_start=False)
+        return u
+
     @classmethod
     def hierarchy(cls, domain, levels=None, smoother_w=0.5, smooth_steps=5, precision=None, max_coarse_dofs=3000,
-                  coarse_smooth_steps=None):
+                  coarse_smooth_steps=None, smoother="jacobi", cheb_ratio=10.0):
         """Chain of GeometricMultigrid levels as ex_compliance_multigrid.py:108-121 builds it.  With
         levels=None, coarsen while the grid halves evenly and the coarse level has > max_coarse_dofs.
-        `coarse_smooth_steps` (default: smooth_steps) applies to every level below the finest."""
+        `coarse_smooth_steps` (default: smooth_steps) applies to every level below the finest.
+        smoother="chebyshev" replaces the damped-Jacobi sweeps by a Chebyshev smoother of degree
+        smooth_steps (coarse_smooth_steps below the finest level) on [lmax/cheb_ratio, lmax]."""
         css = smooth_steps if coarse_smooth_steps is None else coarse_smooth_steps
-        mgs = [cls(domain, smoother=DampedJacobi(w=smoother_w), smooth_steps=smooth_steps, precision=precision)]
+        if smoother not in ("jacobi", "chebyshev"):
+            raise ValueError("smoother must be 'jacobi' or 'chebyshev'")
+
+        def make(steps):
+            if smoother == "chebyshev":
+                return Chebyshev(degree=steps, ratio=cheb_ratio)
+            return DampedJacobi(w=smoother_w)
+
+        mgs = [cls(domain, smoother=make(smooth_steps), smooth_steps=smooth_steps, precision=precision)]
         while True:
             if levels is not None and len(mgs) >= levels - 1:
                 break
@@ -316,7 +427,7 @@ class GeometricMultigrid(Preconditioner):
                 break
             if not g.can_coarsen():
                 raise ValueError(f"cannot build {levels} levels: grid {g.dims} does not halve evenly")
-            mgs.append(cls(sub, smoother=DampedJacobi(w=smoother_w), smooth_steps=css, precision=precision))
+            mgs.append(cls(sub, smoother=make(css), smooth_steps=css, precision=precision))
             mgs[-2].inner_level = mgs[-1]
         return mgs
 
@@ -345,6 +456,15 @@ def capture_graph(fn):
         _lib.Probe.active = prev
     info.launches = probe.launches
     return graph, info
+
+
+def _side_stream(owner):
+    """A second CUDA stream of `owner` (created once per device), for setup work that overlaps the main one."""
+    dev = torch.cuda.current_device()
+    s = getattr(owner, "_side", None)
+    if s is None or s.device.index != dev:
+        s = owner._side = torch.cuda.Stream(device=dev)
+    return s
 
 
 class _Scalars:
@@ -446,9 +566,18 @@ class CG(LinearSolver):
         if isinstance(A, StiffnessOperator):
             if getattr(self, "_Ap", None) is None or self._Ap.code != A.code or self._Ap.grid.dims != A.grid.dims:
                 self._Ap = StiffnessOperator.like(A, A.code)
-            A = self._Ap.assign(A)
+            A = self._Ap.assign(A, derived=False)
+            # the preconditioner setup (Galerkin chain, coarsest factorisation) needs only the element scaling:
+            # it runs on a side stream while the main stream reassembles the operator's stencil and diagonal
+            main, side = torch.cuda.current_stream(), _side_stream(self)
+            side.wait_stream(main)
+            A.refresh_derived()
+            with torch.cuda.stream(side):
+                self.preconditioner.update(A)
+            main.wait_stream(side)
+        else:
+            self.preconditioner.update(A)
         self.A = A
-        self.preconditioner.update(A)
         if self.verbosity >= 1:
             torch.cuda.synchronize()
             print(f"CG Preconditioner set up in {np.round(time.perf_counter() - t0, 3)}s")
@@ -509,14 +638,20 @@ class MixedPrecisionCG(LinearSolver):
     def update(self, A):
         if getattr(self, "_A64", None) is None or self._A64.grid.dims != A.grid.dims:
             self._A64 = StiffnessOperator.like(A, F64)
+        # the FP32 hierarchy is built from the element scaling of A alone: on a side stream, overlapping the
+        # FP64 stencil assembly of the outer operator on the main stream
+        main, side = torch.cuda.current_stream(), _side_stream(self)
+        side.wait_stream(main)
         self.A64 = self._A64.assign(A)
         self.A = self.A64
-        if self.preconditioner is not None:
-            self.preconditioner.update(A)
-            lv0 = getattr(self.preconditioner, "A", None)
-            self.A32 = lv0 if isinstance(lv0, StiffnessOperator) and lv0.code == F32 else A.astype(F32)
-        else:
-            self.A32 = A.astype(F32)
+        with torch.cuda.stream(side):
+            if self.preconditioner is not None:
+                self.preconditioner.update(A)
+                lv0 = getattr(self.preconditioner, "A", None)
+                self.A32 = lv0 if isinstance(lv0, StiffnessOperator) and lv0.code == F32 else A.astype(F32)
+            else:
+                self.A32 = A.astype(F32)
+        main.wait_stream(side)
         self._fallback_ready = False
         n, dev = self.A64.grid.ndof, self.A64.device
         if getattr(self, "_r32", None) is None or self._r32.numel() != n or self._r32.device != dev:
@@ -714,6 +849,8 @@ class MixedPrecisionCG(LinearSolver):
             if not math.isfinite(res) or ((self.fell_back or not can_fall_back) and it - it_fb >= self.maxit):
                 break
         self.iterations, self.last_residual = it, res
+        # the explicit FP64 residual b - A x of the returned solution (LinSolve derives A x from it)
+        self.final_residual = r if trans == "N" else None
         if res > self.tol:
             warnings.warn(f"MixedPrecisionCG did not reach tol {self.tol}: residual {res}")
         out = x.clone()

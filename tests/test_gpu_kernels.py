@@ -225,6 +225,29 @@ def test_cholesky_banded(pg, n_shape):
     assert np.linalg.norm(An @ xh - b) <= 1e-12 * np.linalg.norm(An, 2) * np.linalg.norm(xh)
     ref = np.linalg.solve(An, b)
     assert np.linalg.norm(xh - ref) <= 1e-4 * np.linalg.norm(ref)
+    # blocked substitution with the diagonal-tile inverses, FP64 and FP32
+    nblk = (n + 31) // 32
+    Lh_full = np.tril(Lh)
+    for code, dt in [(0, torch.float64), (1, torch.float32)]:
+        Dinv = torch.empty(nblk * 32 * 32, dtype=dt, device="cuda")
+        call("pmg_cholesky_block_inverses", code, n, Lf, Dinv, stream())
+        D = host(Dinv).reshape(nblk, 32, 32)
+        for kb in range(nblk):
+            k0, nb = 32 * kb, min(32, n - 32 * kb)
+            blk = Lh_full[k0:k0 + nb, k0:k0 + nb]
+            tol = 1e-12 if code == 0 else 1e-6
+            assert np.abs(D[kb, :nb, :nb] @ blk - np.eye(nb)).max() <= tol * max(1.0, np.abs(D[kb]).max() * np.abs(blk).max())
+            assert np.abs(D[kb, nb:, :]).max(initial=0.0) == 0.0 and np.abs(D[kb, :, nb:]).max(initial=0.0) == 0.0
+        Ld = Lf.to(dt)
+        xb = torch.empty(n, dtype=dt, device="cuda")
+        call("pmg_cholesky_solve_blocked", code, n, Ld, bw, Dinv, dev(b, dt), xb, stream())
+        xbh = host(xb)
+        if code == 0:
+            assert np.linalg.norm(An @ xbh - b) <= 1e-12 * np.linalg.norm(An, 2) * np.linalg.norm(xbh)
+        else:
+            # FP32 substitution with the rounded factor: backward error at FP32 level
+            Lr = np.tril(host(Ld))
+            assert np.linalg.norm(Lr @ (Lr.T @ xbh) - host(dev(b, dt))) <= 1e-4 * np.linalg.norm(Lr, 2) ** 2 * np.linalg.norm(xbh)
 
 
 @pytest.mark.parametrize("n_shape", [(8, 4, 4), (16, 8, 0)])
@@ -243,6 +266,16 @@ def test_cholesky_inverse_and_gemv(pg, n_shape):
     Ai = host(Ainv)
     assert np.abs(Ai - Ai.T).max() <= 1e-10 * np.abs(Ai).max()
     assert np.abs(An @ Ai - np.eye(n)).max() <= 1e-8
+    # FP32 inverse from the FP64 factor (tiles of L^{-1} in FP32, then L^{-T} L^{-1})
+    from pymoto_gb300 import _lib
+    scratch = torch.empty(_lib.load().pmg_cholesky_inverse_f32_scratch_bytes(n), dtype=torch.uint8, device="cuda")
+    Ai32 = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    call("pmg_cholesky_inverse_f32", n, L, bw, scratch, Ai32, stream())
+    A32 = host(Ai32)
+    rel = np.linalg.norm(A32 - Ai, 2) / np.linalg.norm(Ai, 2)
+    kappa = np.linalg.cond(An)
+    print(f"FP32 inverse: relative error {rel:.2e}, condition number {kappa:.2e}")
+    assert rel <= max(1e-5, 1e-6 * np.sqrt(kappa))
     b = rng.standard_normal(n)
     for dt, tol in [(torch.float64, 1e-12), (torch.float32, 1e-5)]:
         A = Ainv.to(dt)
@@ -250,6 +283,59 @@ def test_cholesky_inverse_and_gemv(pg, n_shape):
         call("pmg_dense_gemv", 0 if dt == torch.float64 else 1, n, A, dev(b, dt), y, stream())
         ref = host(A) @ host(dev(b, dt))
         np.testing.assert_allclose(host(y), ref, rtol=0, atol=tol * np.abs(ref).max())
+
+
+def test_chebyshev_smoother(pg):
+    """l1 diagonals (stencil and matrix-free), step coefficients and smoothing steps against the same
+    recurrence in numpy; the spectrum of D_l1^-1 A lies in (0, 1] and the smoother contracts."""
+    from pymoto_gb300._lib import call, stream
+    g, K, op, rng = _setup(pg, (8, 6, 4), seed=11)
+    A1 = op.galerkin()
+    Ad = host(A1.to_dense())
+    n = Ad.shape[0]
+    l1 = np.abs(Ad).sum(axis=1)
+    deg, ratio = 3, 10.0
+    sm = pg.Chebyshev(degree=deg, ratio=ratio)
+    sm.update(A1)
+    np.testing.assert_allclose(host(sm.D), l1, rtol=1e-13)
+    assert np.linalg.eigvals(Ad / l1[:, None]).real.max() <= 1 + 1e-12
+    # matrix-free finest operator: element bound >= assembled row sums of |K|
+    sm0 = pg.Chebyshev(degree=2)
+    sm0.update(op)
+    Kd = K.toarray()
+    D0 = host(sm0.D)
+    assert np.all(D0 >= np.abs(Kd).sum(axis=1) * (1 - 1e-12))
+    assert np.linalg.eigvals(Kd / D0[:, None]).real.max() <= 1 + 1e-12
+    hi, lo = 1.0, 1.0 / ratio
+    theta, delta = (hi + lo) / 2, (hi - lo) / 2
+    sigma = theta / delta
+    rho = 1 / sigma
+    coef = [0.0, 1 / theta]
+    for _ in range(1, deg):
+        rn = 1 / (2 * sigma - rho)
+        coef += [rn * rho, 2 * rn / delta]
+        rho = rn
+    np.testing.assert_allclose(host(sm.coef), coef, rtol=1e-13)
+    b = rng.standard_normal(n)
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    dv, r = torch.empty_like(x), torch.empty_like(x)
+    sm.smooth(A1, dev(b), x, dv, r, zero_start=True)
+    xr = np.zeros(n)
+    dr = coef[1] * b / l1
+    xr = xr + dr
+    for j in range(1, deg):
+        dr = coef[2 * j] * dr + coef[2 * j + 1] * (b - Ad @ xr) / l1
+        xr = xr + dr
+    np.testing.assert_allclose(host(x), xr, rtol=1e-11, atol=1e-12 * np.abs(xr).max())
+    # error propagator I - X A of the smoother: spectral radius < 1
+    Mi = np.diag(1 / l1)
+    E = np.eye(n)
+    Dk = coef[1] * Mi
+    Xk = Dk.copy()
+    for j in range(1, deg):
+        Dk = coef[2 * j] * Dk + coef[2 * j + 1] * Mi @ (E - Ad @ Xk)
+        Xk = Xk + Dk
+    assert np.abs(np.linalg.eigvals(E - Xk @ Ad)).max() < 1.0
 
 
 def test_cholesky_reports_not_spd(pg):
