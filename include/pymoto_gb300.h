@@ -232,6 +232,50 @@ size_t pmg_oc_scratch_bytes(void);
 int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, double volfrac, double move,
                   double xmin, double xmax, double l1, double l2, double l1l2tol, void* scratch, void* stream);
 
+/* ---- learned warm start (no counterpart in the reference: the reference solves every design from the
+ * previous solution only).  A 3-level convolutional encoder-decoder on the voxel grid of a coarse
+ * multigrid level, trained on the device on (density, displacement) pairs of the solver.  Layout
+ * channels-last act[v][c], v = (k*ny + j)*nx + i; activations and weights BF16, accumulation and gradients
+ * FP32, weights w[tap][cin][cout] with tap = (dz+1)*9 + (dy+1)*3 + (dx+1), zero padding. -------------- */
+/* out[v][co] = bias[co] + sum w in (+ ReLU); `in` BF16 (or FP32 if in_is_f32); out_bf16 and/or out_f32. */
+int pmg_nn_conv3d_forward(int nx, int ny, int nz, int cin, int cout, int in_is_f32, const void* in, const void* w,
+                          const float* bias, int relu, void* out_bf16, float* out_f32, void* stream);
+/* din = conv^T(dout) (FP32). */
+int pmg_nn_conv3d_backward_data(int nx, int ny, int nz, int cin, int cout, const float* dout, const void* w, float* din,
+                                void* stream);
+/* dw_db[27*cin*cout + cout] (+)= weight and bias gradients; scratch >= pmg_nn_wgrad_scratch_bytes(). */
+size_t pmg_nn_wgrad_scratch_bytes(int nx, int ny, int nz, int cin, int cout);
+int pmg_nn_conv3d_backward_weights(int nx, int ny, int nz, int cin, int cout, int in_is_f32, const void* in,
+                                   const float* dout, float* dw_db, int accumulate, void* scratch, void* stream);
+/* d *= (act > 0) for the stored BF16 ReLU output act. */
+int pmg_nn_relu_backward(int64_t n, const void* act_bf16, float* d, void* stream);
+/* 2x average pooling onto the coarse grid cnx x cny x cnz (direction 0, BF16), or its adjoint (direction 1,
+ * FP32, adding into the fine gradient). */
+int pmg_nn_pool2(int direction, int cnx, int cny, int cnz, int c, const void* in, void* out, void* stream);
+/* 2x nearest upsampling of c channels into channels [coff, coff+c) of a ctot-channel fine tensor
+ * (direction 0, BF16), or its adjoint (direction 1, FP32). */
+int pmg_nn_up2(int direction, int cnx, int cny, int cnz, int c, int ctot, int coff, const void* in, void* out,
+               void* stream);
+/* out[v][coff + ch] = in[v][ch] (BF16) and the adjoint dskip[v][ch] += dcat[v][coff + ch] (FP32). */
+int pmg_nn_copy_channels(int64_t nvox, int c, int ctot, int coff, const void* in, void* out, void* stream);
+int pmg_nn_split_channels(int64_t nvox, int c, int ctot, int coff, const float* dcat, float* dskip, void* stream);
+/* Input features on the voxel grid of stride `stride`: mean cube root of the element stiffness scaling xe
+ * (mapped to [-1,1]) and voxel coordinates. */
+int pmg_nn_input_features(int nelx, int nely, int nelz, int stride, int vnx, int vny, int vnz, const double* xe,
+                          void* feat, void* stream);
+/* Nodal field (FP64, 3 components) averaged from voxel values (direction 0), or the adjoint from FP32 nodal
+ * gradients to FP32 voxel gradients (direction 1). */
+int pmg_nn_vox_to_node(int direction, int vnx, int vny, int vnz, const void* in, void* out, void* stream);
+/* Adam step (step >= 1) on FP32 master weights, refreshing their BF16 copy (if not NULL). */
+int pmg_nn_adam(int n, float* w, const float* g, float* m, float* v, void* w_bf16, float lr, float beta1, float beta2,
+                float eps, int step, float weight_decay, void* stream);
+/* loss_partial[block] = weight * sum (pred - target)^2 over the block; grad = 2 weight (pred - target). */
+int pmg_nn_mse(int64_t n, const double* pred, const double* target, double weight, float* grad, double* loss_partial,
+               void* stream);
+/* uc = scale * u_f at every stride-th node of the fine grid (3 components). */
+int pmg_nn_inject(int nelx, int nely, int nelz, int stride, const double* uf, double scale, double* uc,
+                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif

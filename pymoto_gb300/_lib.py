@@ -5,7 +5,7 @@ There is no CPU fallback: if the library cannot be loaded, every operation raise
 import ctypes
 import os
 import threading
-from ctypes import c_char_p, c_double, c_int, c_int64, c_size_t, c_void_p
+from ctypes import c_char_p, c_double, c_float, c_int, c_int64, c_size_t, c_void_p
 
 import numpy as np
 import torch
@@ -17,6 +17,7 @@ P = c_void_p
 I = c_int
 D = c_double
 L = c_int64
+F = c_float
 
 # name -> (restype, argtypes); mirrors include/pymoto_gb300.h
 SIGNATURES = {
@@ -72,6 +73,20 @@ SIGNATURES = {
     "pmg_sens_contract": (I, [I, I, I, P, P, P, P, D, I, P, P]),
     "pmg_oc_scratch_bytes": (c_size_t, []),
     "pmg_oc_update": (I, [L, P, P, P, D, D, D, D, D, D, D, P, P]),
+    "pmg_nn_conv3d_forward": (I, [I, I, I, I, I, I, P, P, P, I, P, P, P]),
+    "pmg_nn_conv3d_backward_data": (I, [I, I, I, I, I, P, P, P, P]),
+    "pmg_nn_wgrad_scratch_bytes": (c_size_t, [I, I, I, I, I]),
+    "pmg_nn_conv3d_backward_weights": (I, [I, I, I, I, I, I, P, P, P, I, P, P]),
+    "pmg_nn_relu_backward": (I, [L, P, P, P]),
+    "pmg_nn_pool2": (I, [I, I, I, I, I, P, P, P]),
+    "pmg_nn_up2": (I, [I, I, I, I, I, I, I, P, P, P]),
+    "pmg_nn_copy_channels": (I, [L, I, I, I, P, P, P]),
+    "pmg_nn_split_channels": (I, [L, I, I, I, P, P, P]),
+    "pmg_nn_input_features": (I, [I, I, I, I, I, I, I, P, P, P]),
+    "pmg_nn_vox_to_node": (I, [I, I, I, I, P, P, P]),
+    "pmg_nn_adam": (I, [I, P, P, P, P, P, F, F, F, F, I, F, P]),
+    "pmg_nn_mse": (I, [L, P, P, D, P, P, P]),
+    "pmg_nn_inject": (I, [I, I, I, I, P, D, P, P]),
 }
 
 # Returns that are values, not statuses
@@ -129,7 +144,7 @@ def _arg(a):
 # kernels launched per call where it is not exactly one (host-only entry points launch none)
 _HOST_ONLY = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_element_stiffness", "pmg_galerkin_table",
               "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth",
-              "pmg_cholesky_inverse_f32_scratch_bytes"}
+              "pmg_cholesky_inverse_f32_scratch_bytes", "pmg_nn_wgrad_scratch_bytes"}
 
 
 def _launches(name, args):
@@ -140,6 +155,8 @@ def _launches(name, args):
         return 3 * nblk - 2 if int(args[2]) > 0 else nblk
     if name == "pmg_cholesky_inverse_f32":
         return 4
+    if name == "pmg_nn_conv3d_backward_weights":
+        return 2
     if name == "pmg_oc_update":
         width, steps = float(args[9]) - float(args[8]), 3
         while width > float(args[10]):

@@ -1,8 +1,10 @@
-// Kernels of the learned warm start: a small 3D convolutional network on a voxel grid.
+// Kernels of the learned warm start: a small 3D convolutional network on a voxel grid (the coarse grid of
+// the multigrid hierarchy), trained on the device on (density, displacement) pairs of the solver.
 //
 // Layout: channels-last, act[v][c] with v = (k*ny + j)*nx + i.  Activations and weights are stored as
 // BF16, gradients and accumulators are FP32, master weights FP32 (Adam).  3x3x3 convolutions with zero
-// padding; weights w[tap][cin][cout], tap = (dz+1)*9 + (dy+1)*3 + (dx+1).
+// padding; weights w[tap][cin][cout], tap = (dz+1)*9 + (dy+1)*3 + (dx+1).  Weight gradients are summed
+// over fixed voxel chunks and then over the chunks in order, so every result is deterministic.
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -116,7 +118,8 @@ __global__ void relu_bwd_kernel(int64_t n, const __nv_bfloat16* __restrict__ act
   if (t < n && !(__bfloat162float(act[t]) > 0.f)) d[t] = 0.f;
 }
 
-// 2x average pooling (fine grid 2nx x 2ny x 2nz -> coarse nx x ny x nz), forward and adjoint.
+// 2x average pooling (fine grid 2nx x 2ny x 2nz -> coarse nx x ny x nz), forward and adjoint (the adjoint
+// adds into its output, which also holds the gradient of the skip connection).
 __global__ void pool2_fwd_kernel(VGrid gc, int c, const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= gc.nvox() * c) return;
@@ -142,7 +145,7 @@ __global__ void pool2_bwd_kernel(VGrid gf, int c, const float* __restrict__ dout
   int i, j, k;
   vox_ijk(gf, v, i, j, k);
   const int cx = gf.nx / 2, cy = gf.ny / 2;
-  din[t] = 0.125f * dout[((int64_t)((k / 2) * cy + j / 2) * cx + i / 2) * c + ch];
+  din[t] += 0.125f * dout[((int64_t)((k / 2) * cy + j / 2) * cx + i / 2) * c + ch];   // accumulates
 }
 
 // 2x nearest upsampling written into channels [coff, coff+c) of a ctot-channel output (the decoder concat).
@@ -197,8 +200,9 @@ __global__ void split_channels_kernel(int64_t nvox, int c, int ctot, int coff, c
   dskip[t] += dcat[v * ctot + coff + ch];
 }
 
-// Network input on a voxel grid of stride s over the element grid: channel 0 = mean of x over the s^3
-// elements of the voxel (x in [0,1] is mapped to 2x-1), channels 1..3 = voxel-centre coordinates in [-1,1].
+// Network input on a voxel grid of stride s over the element grid: channel 0 = mean of the cube root of the
+// element stiffness scaling over the s^3 elements of the voxel (a density in [0,1] under SIMP p = 3, mapped
+// to 2x-1), channels 1..3 = voxel-centre coordinates in [-1,1].
 __global__ void input_features_kernel(Grid ge, int s, VGrid gv, const double* __restrict__ xe,
                                       __nv_bfloat16* __restrict__ feat) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -213,7 +217,7 @@ __global__ void input_features_kernel(Grid ge, int s, VGrid gv, const double* __
       for (int a = 0; a < s; ++a) {
         const int ei = i * s + a, ej = j * s + b, ek = k * s + c;
         if (ei < ge.nx && ej < ge.ny && ek < ez) {
-          acc += xe[((int64_t)ek * ge.ny + ej) * ge.nx + ei];
+          acc += cbrt(xe[((int64_t)ek * ge.ny + ej) * ge.nx + ei]);
           ++cnt;
         }
       }
@@ -282,18 +286,17 @@ __global__ void adam_kernel(int n, float* __restrict__ w, const float* __restric
   if (wb) wb[t] = __float2bfloat16(wn);
 }
 
-// Masked mean-squared error on nodal values (FP64 prediction vs target) and its gradient (FP32).
+// Weighted squared error weight * sum (pred - target)^2 on nodal values (FP64 prediction vs target) and its
+// gradient (FP32); per-block partial losses (summed in block order by the caller).
 __global__ void mse_kernel(int64_t n, const double* __restrict__ pred, const double* __restrict__ target,
-                           const uint8_t* __restrict__ keep, double inv_n, float* __restrict__ grad,
-                           double* __restrict__ loss_partial) {
+                           double weight, float* __restrict__ grad, double* __restrict__ loss_partial) {
   __shared__ double sh[256];
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double l = 0.0;
   if (t < n) {
-    const bool k = keep ? (keep[t / 3] >> (t % 3)) & 1 ? false : true : true;
-    const double e = k ? pred[t] - target[t] : 0.0;
+    const double e = pred[t] - target[t];
     l = e * e;
-    grad[t] = (float)(2.0 * e * inv_n);
+    grad[t] = (float)(2.0 * e * weight);
   }
   sh[threadIdx.x] = l;
   __syncthreads();
@@ -301,7 +304,21 @@ __global__ void mse_kernel(int64_t n, const double* __restrict__ pred, const dou
     if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) loss_partial[blockIdx.x] = sh[0] * inv_n;
+  if (threadIdx.x == 0) loss_partial[blockIdx.x] = sh[0] * weight;
+}
+
+// Injection of a nodal field of a fine grid onto the nodes of the grid coarser by `stride` (every
+// stride-th node in each direction), scaled by `scale`.
+__global__ void inject_kernel(Grid gf, int stride, const double* __restrict__ uf, double scale,
+                              double* __restrict__ uc) {
+  const int cnx = gf.nx / stride + 1, cny = gf.ny / stride + 1, cnz = gf.nz / stride + 1;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)cnx * cny * cnz * 3) return;
+  const int d = (int)(t % 3);
+  const int64_t n = t / 3;
+  const int i = (int)(n % cnx), j = (int)((n / cnx) % cny), k = (int)(n / ((int64_t)cnx * cny));
+  const int64_t m = ((int64_t)(k * stride) * (gf.ny + 1) + j * stride) * (gf.nx + 1) + i * stride;
+  uc[t] = scale * uf[m * 3 + d];
 }
 
 }  // namespace nn
@@ -446,11 +463,21 @@ int pmg_nn_adam(int n, float* w, const float* g, float* m, float* v, void* w_bf1
   return check_launch();
 }
 
-int pmg_nn_mse(int64_t n, const double* pred, const double* target, const uint8_t* dof_mask, float* grad,
-               double* loss_partial, void* stream) {
+int pmg_nn_mse(int64_t n, const double* pred, const double* target, double weight, float* grad, double* loss_partial,
+               void* stream) {
   if (n <= 0 || !pred || !target || !grad || !loss_partial) return PMG_BAD_ARG;
-  mse_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(n, pred, target, dof_mask, 1.0 / (double)n, grad,
-                                                               loss_partial);
+  mse_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(n, pred, target, weight, grad, loss_partial);
+  return check_launch();
+}
+
+int pmg_nn_inject(int nelx, int nely, int nelz, int stride, const double* uf, double scale, double* uc,
+                  void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || nelz == 0 || stride < 1 || nelx % stride || nely % stride || nelz % stride ||
+      !uf || !uc)
+    return PMG_BAD_ARG;
+  Grid gf{nelx, nely, nelz};
+  const int64_t n = (int64_t)(nelx / stride + 1) * (nely / stride + 1) * (nelz / stride + 1) * 3;
+  inject_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(gf, stride, uf, scale, uc);
   return check_launch();
 }
 

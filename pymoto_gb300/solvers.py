@@ -610,8 +610,10 @@ class MixedPrecisionCG(LinearSolver):
     CUDA-graph replay, captured once per update()).
     Because the preconditioner is inexact (and may be nonlinear), directions are K-orthogonalised against
     the last `m` directions (FCG(m)); the reference's beta = -(q.z)/(p.q) is the m = 1 case.
-    `warm_start` is an optional object with `.predict(A, rhs)` giving the initial guess when no x0 is
-    passed; `coarse_correction` an optional callable r64 -> z64 added to the preconditioned residual.
+    `warm_start` is an optional learned predictor (pymoto_gb300.learned.LearnedWarmStart): its prediction and
+    the given x0 span the space in which the initial guess is the energy-optimal (Rayleigh-Ritz)
+    combination, and every converged solution is passed back to it for training; `coarse_correction` an
+    optional callable r64 -> z64 added to the preconditioned residual.
     """
 
     def __init__(self, A=None, preconditioner=None, tol=1e-6, m=2, inner_iters=0, inner_tol=0.1, maxit=500,
@@ -796,16 +798,26 @@ class MixedPrecisionCG(LinearSolver):
             self._pqpr = torch.zeros(2, dtype=torch.float64, device=dev)
         x, b, r = B["x"], B["b"], B["r"]
         b.copy_(b_in)
-        if x0 is not None:
-            x.copy_(_to_device(x0, torch.float64)[0])
-        elif self.warm_start is not None:
-            x.copy_(self.warm_start.predict(A, b).to(torch.float64))
-        else:
-            x.zero_()
         ws = Workspace.get(dev)
         st = stream()
         s = B["s"]
-        A.apply(RESIDUAL, x, b, out=r)
+        learned = self.warm_start is not None and getattr(self.warm_start, "ready", True) and trans == "N"
+        if learned:
+            # initial guess: energy-optimal combination of the given guess and the network's prediction
+            from .learned import rayleigh_ritz
+            if "wsv" not in B:
+                B["wsv"] = torch.empty(n, dtype=torch.float64, device=dev)
+                B["wsq"] = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(2)]
+            un = B["wsv"]
+            call("pmg_mask_bc", F64, A.grid.dim, A.grid.nnodes, A.bcmask, 0, self.warm_start.predict(A), un, st)
+            vecs = [un] if x0 is None else [_to_device(x0, torch.float64)[0].contiguous(), un]
+            self.warm_start_coefficients = rayleigh_ritz(A, b, vecs, x, r, B["wsq"])
+        else:
+            if x0 is not None:
+                x.copy_(_to_device(x0, torch.float64)[0])
+            else:
+                x.zero_()
+            A.apply(RESIDUAL, x, b, out=r)
         call("pmg_dot2", F64, n, b, b, r, r, s[0:1], ws.reduce, st)
         bb, rr = s[0:2].tolist()
         bn = math.sqrt(bb) or 1.0
@@ -851,6 +863,8 @@ class MixedPrecisionCG(LinearSolver):
         self.iterations, self.last_residual = it, res
         # the explicit FP64 residual b - A x of the returned solution (LinSolve derives A x from it)
         self.final_residual = r if trans == "N" else None
+        if self.warm_start is not None and trans == "N" and math.isfinite(res):
+            self.warm_start.observe(A, x)
         if res > self.tol:
             warnings.warn(f"MixedPrecisionCG did not reach tol {self.tol}: residual {res}")
         out = x.clone()
