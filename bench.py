@@ -50,7 +50,11 @@ def parse():
     ap.add_argument("--levels", type=int, default=GPU_LEVELS)
     ap.add_argument("--sweeps", type=int, default=SWEEPS)
     ap.add_argument("--coarse-sweeps", type=int, default=None)
-    ap.add_argument("--arms", default="plain_fp64,mixed")
+    ap.add_argument("--case", default=None, choices=["operator"],
+                    help="instead of the bench: time the level-0 operator kernels alone (a small case for ncu)")
+    ap.add_argument("--arms", default="plain_fp64,mixed,mixed_learned",
+                    help="plain_fp64 (the reference's method), mixed (headline), mixed_learned (with the learned "
+                         "warm start), ablations: mixed_jacobi, plain_fp64_cheb")
     return ap.parse_args()
 
 
@@ -74,7 +78,9 @@ class DesignRun:
     """The network of the workload on the device, for one solver arm."""
 
     opts = {"inner_iters": 0, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None,
-            "smoother": "chebyshev", "cheb_degree": 2, "cheb_coarse_degree": None, "cheb_ratio": 10.0}
+            "smoother": "chebyshev", "cheb_degree": 2, "cheb_coarse_degree": 3, "cheb_ratio": 10.0,
+            "learned_train_steps": 1, "learned_stride": 4, "learned_lr": 2e-3, "learned_net": True,
+            "learned_history": 1}
 
     def __init__(self, arm, shape, seed, torch, pg):
         o = DesignRun.opts
@@ -106,8 +112,15 @@ class DesignRun:
                                                       smooth_steps=o["sweeps"], precision="fp32" if mixed else None,
                                                       coarse_smooth_steps=o["coarse_sweeps"])
             if mixed:
+                self.warm_start = None
+                if arm == "mixed_learned":
+                    from pymoto_gb300.learned import LearnedWarmStart
+                    self.warm_start = LearnedWarmStart(shape, stride=o["learned_stride"], capacity=8,
+                                                       train_steps=o["learned_train_steps"], lr=o["learned_lr"],
+                                                       seed=seed, use_net=o["learned_net"],
+                                                       history=o["learned_history"])
                 self.solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=o["m"], inner_iters=o["inner_iters"],
-                                                  inner_tol=o["inner_tol"])
+                                                  inner_tol=o["inner_tol"], warm_start=self.warm_start)
             else:
                 self.solver = pg.CG(preconditioner=mgs[0], tol=TOL)
             self.u = pg.LinSolve(hermitian=True, symmetric=True, solver=self.solver)(K, self.f)
@@ -248,8 +261,8 @@ def measure_gb300(args, rank, world, local_rank):
             return float(t.item())
         return v
 
-    DesignRun.opts = {"inner_iters": args.inner_iters, "inner_tol": args.inner_tol, "m": args.fcg_m,
-                      "levels": args.levels, "sweeps": args.sweeps, "coarse_sweeps": args.coarse_sweeps}
+    DesignRun.opts.update({"inner_iters": args.inner_iters, "inner_tol": args.inner_tol, "m": args.fcg_m,
+                           "levels": args.levels, "sweeps": args.sweeps, "coarse_sweeps": args.coarse_sweeps})
     results = {}
     for arm in args.arms.split(","):
         run = DesignRun(arm, shape, seed=1234 + rank, torch=torch, pg=pg)
@@ -276,8 +289,10 @@ def measure_gb300(args, rank, world, local_rank):
     b = run_p.f.clone()
     mask = torch.empty_like(b)
     pg._lib.call("pmg_mask_bc", 0, 3, A.grid.nnodes, A.bcmask, 0, b, mask, pg._lib.stream())
-    mgs = pg.GeometricMultigrid.hierarchy(pg.VoxelDomain(*shape), levels=args.levels, smoother_w=OMEGA,
-                                          smooth_steps=args.sweeps, precision="fp32")
+    o = DesignRun.opts
+    mgs = pg.GeometricMultigrid.hierarchy(pg.VoxelDomain(*shape), levels=args.levels, smooth_steps=o["cheb_degree"],
+                                          precision="fp32", coarse_smooth_steps=o["cheb_coarse_degree"],
+                                          smoother="chebyshev", cheb_ratio=o["cheb_ratio"])
     ms = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=args.fcg_m, inner_iters=args.inner_iters,
                              inner_tol=args.inner_tol)
     ms.update(A)
@@ -342,8 +357,41 @@ def cpu_reference_sample(shape, warm_steps=1, budget_s=None):
     return times, L
 
 
+def operator_case(args):
+    """Level-0 products of the workload alone: FP32 tensor-core operator (residual mode), FP64 stencil
+    product; 3 launches each after 2 warm-up launches, CUDA-event times printed as JSON."""
+    import torch
+    import pymoto_gb300 as pg
+    from pymoto_gb300._lib import F32, F64, RESIDUAL, MATVEC
+    shape = SHAPE if args.shape is None else tuple(int(v) for v in args.shape.split("x"))
+    d = pg.VoxelDomain(*shape)
+    bc, f = cantilever(shape)
+    x = torch.from_numpy(np.random.default_rng(0).uniform(1e-3, 1.0, d.nel) ** 3).cuda()
+    K = pg.AssembleStiffness(d, bc=bc)(x)
+    K32 = K.astype(F32)
+    u = torch.randn(K.grid.ndof, dtype=torch.float64, device="cuda")
+    u32, b32 = u.float(), torch.randn_like(u.float())
+    out = {}
+    for name, fn in [("ebe_apply_mma_f32_residual", lambda: K32.apply(RESIDUAL, u32, b32)),
+                     ("stencil_apply_f64_matvec", lambda: K.apply(MATVEC, u))]:
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        out[name + "_us"] = e0.elapsed_time(e1) / 3 * 1e3
+    print(json.dumps({"case": "operator", "shape": list(shape), **out}))
+
+
 def main():
     args = parse()
+    if args.case == "operator":
+        operator_case(args)
+        return
     rank, world, local_rank = dist_info()
     threads = os.cpu_count() or 1
     if args.impl == "reference":
@@ -403,9 +451,13 @@ def main():
                 "config": {"workload": f"3D cantilever hex8 {shape[0]}x{shape[1]}x{shape[2]} "
                                        f"({3 * (shape[0] + 1) * (shape[1] + 1) * (shape[2] + 1)} dofs), FilterConv "
                                        f"r=2.5, SIMP p=3, OC move 0.2, rel. residual 1e-6",
-                           "solver": f"FP64 FCG({args.fcg_m}) + FP32 GMG {args.levels} levels (Jacobi w=0.6, "
-                                     f"{args.sweeps} sweeps, {args.inner_iters} inner FP32 PCG its), "
-                                     f"FP64 Cholesky coarsest", "learned_warm_start": False,
+                           "solver": f"FP64 FCG({args.fcg_m}) + FP32 GMG {args.levels} levels (l1-Jacobi "
+                                     f"Chebyshev degree {DesignRun.opts['cheb_degree']}/"
+                                     f"{DesignRun.opts['cheb_coarse_degree']} fine/coarse), FP64 Cholesky coarsest "
+                                     f"with FP32 inverse; plain arm: FP64 CG + FP64 GMG, damped Jacobi w=0.6, "
+                                     f"2 sweeps, FP64 inverse", "learned_warm_start": False,
+                           "learned_warm_start_note": "measured as arms.mixed_learned (network + previous solution "
+                                                      "in a Rayleigh-Ritz initial guess); not in the headline",
                            "parallelism": f"replicas x{world}", "l2": "flushed before every step (256 MB write)"},
                 "arms": {arm: {"design_it_per_s": world * steps / (R[arm]["total_ms"] / 1e3),
                                "ms_per_step": R[arm]["total_ms"] / steps,

@@ -201,8 +201,12 @@ class LearnedWarmStart:
     first `min_samples` pairs were seen.
     """
 
-    def __init__(self, grid, stride=4, capacity=8, train_steps=2, lr=1e-3, min_samples=1, seed=0, device="cuda"):
+    def __init__(self, grid, stride=4, capacity=8, train_steps=2, lr=1e-3, min_samples=1, seed=0, device="cuda",
+                 use_net=True, history=1):
         nx, ny, nz = grid
+        self.use_net = use_net
+        self.history = int(history)
+        self._hist = []             # older solutions (FP64, fine grid), most recent first
         if nz == 0:
             raise ValueError("the learned warm start is 3D")
         if nx % stride or ny % stride or nz % stride or stride & (stride - 1):
@@ -251,8 +255,25 @@ class LearnedWarmStart:
             src = buf
         return src
 
+    def basis(self, A, x0):
+        """Directions of the Rayleigh-Ritz initial guess besides x0: the `history` solutions before the
+        latest one (x0 is the latest, as LinSolve passes it; linear extrapolation in the design sequence)
+        and the network's prediction."""
+        hist = [h for h in self._hist if h.numel() == A.grid.ndof]
+        vecs = hist[1:1 + self.history] if x0 is not None else hist[:self.history]
+        if self.use_net and self.ready:
+            vecs.append(self.predict(A))
+        return vecs
+
     def observe(self, A, u):
         """Store the pair (stiffness field of A, solution u) and train on the stored pairs."""
+        if self.history > 0:
+            keep = self._hist[:self.history + 1]
+            buf = keep.pop() if len(keep) == self.history + 1 else torch.empty_like(u)
+            buf.copy_(u)
+            self._hist = [buf] + keep
+        if not self.use_net:
+            return
         slot = self.count % self.capacity
         self._features(A._xe64 if A._xe64 is not None else A.xe, self.feats[slot])
         t = self.targets[slot]

@@ -801,16 +801,20 @@ class MixedPrecisionCG(LinearSolver):
         ws = Workspace.get(dev)
         st = stream()
         s = B["s"]
-        learned = self.warm_start is not None and getattr(self.warm_start, "ready", True) and trans == "N"
-        if learned:
-            # initial guess: energy-optimal combination of the given guess and the network's prediction
+        extra = self.warm_start.basis(A, x0) if self.warm_start is not None and trans == "N" else []
+        if extra:
+            # initial guess: energy-optimal combination of the given guess, older solutions and the network's
+            # prediction (all with their constrained dofs zeroed)
             from .learned import rayleigh_ritz
-            if "wsv" not in B:
-                B["wsv"] = torch.empty(n, dtype=torch.float64, device=dev)
-                B["wsq"] = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(2)]
-            un = B["wsv"]
-            call("pmg_mask_bc", F64, A.grid.dim, A.grid.nnodes, A.bcmask, 0, self.warm_start.predict(A), un, st)
-            vecs = [un] if x0 is None else [_to_device(x0, torch.float64)[0].contiguous(), un]
+            k = len(extra) + (x0 is not None)
+            if len(B.get("wsv", [])) < len(extra):
+                B["wsv"] = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(len(extra))]
+            if len(B.get("wsq", [])) < k:
+                B["wsq"] = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(k)]
+            vecs = [] if x0 is None else [_to_device(x0, torch.float64)[0].contiguous()]
+            for v, buf in zip(extra, B["wsv"]):
+                call("pmg_mask_bc", F64, A.grid.dim, A.grid.nnodes, A.bcmask, 0, v, buf, st)
+                vecs.append(buf)
             self.warm_start_coefficients = rayleigh_ritz(A, b, vecs, x, r, B["wsq"])
         else:
             if x0 is not None:
