@@ -121,6 +121,14 @@ int pmg_stencil_rowabs(int dtype, int nelx, int nely, int nelz, const void* S, v
 /* coef[2j], coef[2j+1] (device, j < degree) = the step coefficients a_j, c_j for lmax = *lmax_dev (device
  * double) or lmax_host when lmax_dev is NULL. */
 int pmg_cheb_coeffs(const double* lmax_dev, double lmax_host, double ratio, int degree, double* coef, void* stream);
+/* Fused smoothing step on a stencil operator: r = b - A u computed in the product, d = a_j d + c_j r / dl1
+ * (d not read at step 0), y = u + d (y != u). */
+int pmg_stencil_cheb_step(int dtype, int nelx, int nely, int nelz, const void* S, const void* u, const void* b,
+                          const void* dl1, void* d, const double* coef, int step, void* y, void* stream);
+/* The same on the matrix-free FP32 3D level-0 operator (tensor-core kernel of pmg_ebe_apply). */
+int pmg_ebe_cheb_step(int nelx, int nely, int nelz, const float* xe, const double* K0_host, const uint8_t* bcmask,
+                      double bcdiag, const float* u, const float* b, const float* dl1, float* d, const double* coef,
+                      int step, float* y, void* stream);
 /* Step `step`: d = a d + c r / diag, x = x + d; init != 0 starts from x = 0 (d = x = c r / diag). */
 int pmg_cheb_step(int dtype, int64_t n, const void* r, const void* diag, void* d, void* x, const double* coef, int step,
                   int init, void* stream);

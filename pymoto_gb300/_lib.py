@@ -42,6 +42,8 @@ SIGNATURES = {
     "pmg_stencil_rowabs": (I, [I, I, I, I, P, P, P]),
     "pmg_cheb_coeffs": (I, [P, D, D, I, P, P]),
     "pmg_cheb_step": (I, [I, L, P, P, P, P, P, I, I, P]),
+    "pmg_stencil_cheb_step": (I, [I, I, I, I, P, P, P, P, P, P, I, P, P]),
+    "pmg_ebe_cheb_step": (I, [I, I, I, P, P, P, D, P, P, P, P, P, I, P, P]),
     "pmg_cholesky_factor": (I, [I, P, I, P, P]),
     "pmg_cholesky_solve": (I, [I, I, P, I, P, P, P]),
     "pmg_cholesky_inverse": (I, [I, P, I, P, P]),

@@ -83,8 +83,19 @@ __device__ __forceinline__ int64_t elem_id(const Grid& g, int i, int j, int k) {
   return (int64_t)((k * g.ny + j) * g.nx + i);
 }
 
+// Operands of the fused Chebyshev smoothing step (operator apply mode 3): with r = b - A u,
+// d <- a_j d + c_j r / diag (a_0 = 0: d not read at step 0), y = u + d; coef[2j], coef[2j+1] = a_j, c_j.
+template <typename T>
+struct ChebArgs {
+  T* d;
+  const double* coef;
+  int step;
+};
+constexpr int PMG_APPLY_CHEB = 3;
+
 // 3D FP32 operator apply on the tensor cores (ebe_mma.cu).
 int ebe_apply_mma_f32(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
-                      const float* u, const float* b, const float* diag, double w, float* y, cudaStream_t st);
+                      const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
+                      cudaStream_t st);
 
 }  // namespace pmg

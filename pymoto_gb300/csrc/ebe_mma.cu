@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     ebe_apply_mma_kernel(Grid g, const float* __restrict__ xe, ElemMat<float, 24> K0,
                          const uint8_t* __restrict__ bcmask, float bcdiag, const float* __restrict__ u,
                          const float* __restrict__ b, const float* __restrict__ diag, float w,
-                         float* __restrict__ y) {
+                         float* __restrict__ y, ChebArgs<float> ch) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MmaSmem& S = *reinterpret_cast<MmaSmem*>(smem_raw);
   float* const Su = &S.u[0][0][0];
@@ -79,6 +79,11 @@ __global__ void __launch_bounds__(NTHREADS, 2)
   const int NE = EP * (nyw + 1);
   const int nmt = (NE + 15) >> 4;
   const int64_t nlayer = (int64_t)nnx * nny;
+  float ca = 0.f, cc = 0.f;   // Chebyshev step coefficients (mode 3)
+  if (MODE == 3) {
+    ca = (float)ch.coef[2 * ch.step];
+    cc = (float)ch.coef[2 * ch.step + 1];
+  }
 
   for (int q = tid; q < 576; q += NTHREADS) S.k0[q] = K0.v[q];
   for (int e = tid; e < 16 * NMT; e += NTHREADS) {
@@ -243,7 +248,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       if (MODE >= 1) ob[d] = b[n * 3 + d];
-      if (MODE == 2) {
+      if (MODE >= 2) {
         od[d] = diag[n * 3 + d];
         ou[d] = u[n * 3 + d];
       }
@@ -275,9 +280,14 @@ __global__ void __launch_bounds__(NTHREADS, 2)
         y[q] = fixed ? bcdiag * u[q] : acc[d];
       } else if (MODE == 1) {
         y[q] = ob[d] - (fixed ? bcdiag * u[q] : acc[d]);
-      } else {
+      } else if (MODE == 2) {
         const float Au = fixed ? bcdiag * ou[d] : acc[d];
         y[q] = ou[d] + w * __fdividef(ob[d] - Au, od[d]);
+      } else {
+        const float Au = fixed ? bcdiag * ou[d] : acc[d];
+        const float dn = (ch.step == 0 ? 0.f : ca * ch.d[q]) + cc * __fdividef(ob[d] - Au, od[d]);
+        ch.d[q] = dn;
+        y[q] = ou[d] + dn;
       }
     }
   };
@@ -308,9 +318,10 @@ __global__ void __launch_bounds__(NTHREADS, 2)
 
 // 3D FP32 operator apply on the tensor cores (modes as pmg_ebe_apply).
 int ebe_apply_mma_f32(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
-                      const float* u, const float* b, const float* diag, double w, float* y, cudaStream_t st) {
+                      const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
+                      cudaStream_t st) {
   static int sm_count[64] = {0};
-  static bool attr_set[64][3] = {};
+  static bool attr_set[64][4] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return check_launch();
   if (!sm_count[dev]) {
@@ -334,11 +345,13 @@ int ebe_apply_mma_f32(int mode, Grid g, const float* xe, const double* K0, const
   }
   const dim3 grid(tx, ty, nzc);
   auto K = make_elem_mat<float, 24>(K0);
-  const int m = mode == PMG_APPLY_MATVEC ? 0 : (mode == PMG_APPLY_RESIDUAL ? 1 : 2);
+  const int m = mode == PMG_APPLY_MATVEC ? 0 : (mode == PMG_APPLY_RESIDUAL ? 1 : (mode == PMG_APPLY_JACOBI ? 2 : 3));
   cudaError_t e = cudaSuccess;
   if (!attr_set[dev][m]) {
-    const void* fn = m == 0 ? (const void*)ebe_apply_mma_kernel<0>
-                            : (m == 1 ? (const void*)ebe_apply_mma_kernel<1> : (const void*)ebe_apply_mma_kernel<2>);
+    const void* fn = m == 0   ? (const void*)ebe_apply_mma_kernel<0>
+                     : m == 1 ? (const void*)ebe_apply_mma_kernel<1>
+                     : m == 2 ? (const void*)ebe_apply_mma_kernel<2>
+                              : (const void*)ebe_apply_mma_kernel<3>;
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) {
       set_error(cudaGetErrorString(e));
@@ -348,11 +361,13 @@ int ebe_apply_mma_f32(int mode, Grid g, const float* xe, const double* K0, const
   }
   const float bd = (float)bcdiag, wf = (float)w;
   if (m == 0)
-    ebe_apply_mma_kernel<0><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y);
+    ebe_apply_mma_kernel<0><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
   else if (m == 1)
-    ebe_apply_mma_kernel<1><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y);
+    ebe_apply_mma_kernel<1><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
+  else if (m == 2)
+    ebe_apply_mma_kernel<2><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
   else
-    ebe_apply_mma_kernel<2><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y);
+    ebe_apply_mma_kernel<3><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
   return check_launch();
 }
 

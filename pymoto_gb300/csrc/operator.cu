@@ -238,7 +238,7 @@ __global__ void ebe_diag_kernel(Grid g, const T* __restrict__ xe, ElemMat<T, Tra
 template <typename T, int DIM, int MODE>
 __global__ void __launch_bounds__(256) stencil_apply_kernel(Grid g, const T* __restrict__ S, const T* __restrict__ u,
                                                             const T* __restrict__ b, const T* __restrict__ diag, T w,
-                                                            T* __restrict__ y) {
+                                                            T* __restrict__ y, ChebArgs<T> ch) {
   constexpr int NOFF = Traits<DIM>::NOFF;
   const int nn = (int)g.nnodes();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -261,8 +261,13 @@ __global__ void __launch_bounds__(256) stencil_apply_kernel(Grid g, const T* __r
     y[q] = acc;
   } else if (MODE == 1) {
     y[q] = b[q] - acc;
-  } else {
+  } else if (MODE == 2) {
     y[q] = u[q] + w * ((b[q] - acc) / diag[q]);
+  } else {
+    const T a = (T)ch.coef[2 * ch.step], c = (T)ch.coef[2 * ch.step + 1];
+    const T dn = (ch.step == 0 ? T(0) : a * ch.d[q]) + c * ((b[q] - acc) / diag[q]);
+    ch.d[q] = dn;
+    y[q] = u[q] + dn;
   }
 }
 
@@ -679,7 +684,7 @@ int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_
                 const void* u, const void* b, const void* diag, double w, void* y, cudaStream_t st) {
   if constexpr (DIM == 3 && sizeof(T) == 4)
     return ebe_apply_mma_f32(mode, g, (const float*)xe, K0, bcmask, bcdiag, (const float*)u, (const float*)b,
-                             (const float*)diag, w, (float*)y, st);
+                             (const float*)diag, w, (float*)y, ChebArgs<float>{nullptr, nullptr, 0}, st);
   auto K = make_elem_mat<T, Traits<DIM>::NDE>(K0);
   if constexpr (DIM == 3) {
     const dim3 block(TBX, TBY, TBZ);
@@ -715,7 +720,7 @@ int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_
 
 template <typename T, int DIM>
 int stencil_apply_t(int mode, Grid g, const void* S, const void* u, const void* b, const void* diag, double w,
-                    void* y, cudaStream_t st) {
+                    void* y, cudaStream_t st, ChebArgs<T> ch = ChebArgs<T>{nullptr, nullptr, 0}) {
   const int threads = 256;
   const unsigned blocks = blocks_for(g.nnodes() * DIM, threads);
   const T* S_ = (const T*)S;
@@ -724,11 +729,13 @@ int stencil_apply_t(int mode, Grid g, const void* S, const void* u, const void* 
   const T* d_ = (const T*)diag;
   T* y_ = (T*)y;
   if (mode == PMG_APPLY_MATVEC)
-    stencil_apply_kernel<T, DIM, 0><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_);
+    stencil_apply_kernel<T, DIM, 0><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
   else if (mode == PMG_APPLY_RESIDUAL)
-    stencil_apply_kernel<T, DIM, 1><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_);
+    stencil_apply_kernel<T, DIM, 1><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+  else if (mode == PMG_APPLY_JACOBI)
+    stencil_apply_kernel<T, DIM, 2><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
   else
-    stencil_apply_kernel<T, DIM, 2><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_);
+    stencil_apply_kernel<T, DIM, 3><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
   return check_launch();
 }
 
@@ -806,6 +813,27 @@ int pmg_stencil_apply(int mode, int dtype, int nelx, int nely, int nelz, const v
   if (mode == PMG_APPLY_JACOBI && !diag) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
   PMG_DISPATCH(dtype, g.dim(), (stencil_apply_t<T, DIM>(mode, g, S, u, b, diag, omega, y, as_stream(stream))));
+}
+
+int pmg_stencil_cheb_step(int dtype, int nelx, int nely, int nelz, const void* S, const void* u, const void* b,
+                          const void* dl1, void* d, const double* coef, int step, void* y, void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !S || !u || !b || !dl1 || !d || !coef || !y || y == u ||
+      step < 0 || step >= 64)
+    return PMG_BAD_ARG;
+  Grid g{nelx, nely, nelz};
+  PMG_DISPATCH(dtype, g.dim(),
+               (stencil_apply_t<T, DIM>(PMG_APPLY_CHEB, g, S, u, b, dl1, 0.0, y, as_stream(stream),
+                                        ChebArgs<T>{(T*)d, coef, step})));
+}
+
+int pmg_ebe_cheb_step(int nelx, int nely, int nelz, const float* xe, const double* K0_host, const uint8_t* bcmask,
+                      double bcdiag, const float* u, const float* b, const float* dl1, float* d, const double* coef,
+                      int step, float* y, void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || nelz == 0 || !xe || !K0_host || !u || !b || !dl1 || !d || !coef || !y || y == u ||
+      step < 0 || step >= 64)
+    return PMG_BAD_ARG;
+  return ebe_apply_mma_f32(PMG_APPLY_CHEB, Grid{nelx, nely, nelz}, xe, K0_host, bcmask, bcdiag, u, b, dl1, 0.0, y,
+                           ChebArgs<float>{d, coef, step}, as_stream(stream));
 }
 
 int pmg_stencil_diagonal(int dtype, int nelx, int nely, int nelz, const void* S, void* diag, void* stream) {

@@ -210,6 +210,19 @@ class StiffnessOperator:
             self._assemble_stencil(self._S)
         return self._S
 
+    def cheb_step(self, u, b, dl1, d, coef, step, out):
+        """Fused Chebyshev smoothing step (see Chebyshev): out = u + d with d updated from r = b - K u."""
+        g = self.grid
+        if self.code == F32 and g.dim == 3:
+            call("pmg_ebe_cheb_step", g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag, u, b, dl1, d,
+                 coef, step, out, stream())
+            return out
+        if self.code == F64 and self.fp64_stencil:
+            call("pmg_stencil_cheb_step", self.code, g.nelx, g.nely, g.nelz, self.stencil(), u, b, dl1, d, coef, step,
+                 out, stream())
+            return out
+        return None
+
     def apply(self, mode, u, b=None, diag=None, w=0.0, out=None):
         out = torch.empty_like(u) if out is None else out
         g = self.grid
@@ -303,6 +316,13 @@ class StencilOperator:
         out = torch.empty_like(u) if out is None else out
         g = self.grid
         call("pmg_stencil_apply", mode, self.code, g.nelx, g.nely, g.nelz, self.S, u, b, diag, float(w), out, stream())
+        return out
+
+    def cheb_step(self, u, b, dl1, d, coef, step, out):
+        """Fused Chebyshev smoothing step (see Chebyshev): out = u + d with d updated from r = b - S u."""
+        g = self.grid
+        call("pmg_stencil_cheb_step", self.code, g.nelx, g.nely, g.nelz, self.S, u, b, dl1, d, coef, step, out,
+             stream())
         return out
 
     def matvec(self, u, out=None):

@@ -145,16 +145,22 @@ class Chebyshev(Preconditioner):
                  A.bcdiag, self.D, stream())
 
     def smooth(self, A, b, x, d, r, zero_start):
-        """`degree` steps on x (in place); d and r are work vectors of the size of b."""
+        """`degree` steps from x; d and r are work vectors of the size of b.  Each step is one fused
+        operator product (residual, update of d and of the iterate) where the operator has it, writing the
+        new iterate into the other of (x, r); returns the buffer holding the result."""
         code, n, st = A.code, b.numel(), stream()
         j0 = 0
         if zero_start:
             call("pmg_cheb_step", code, n, b, self.D, d, x, self.coef, 0, 1, st)
             j0 = 1
+        cur, other = x, r
         for j in range(j0, self.degree):
-            A.apply(RESIDUAL, x, b, out=r)
-            call("pmg_cheb_step", code, n, r, self.D, d, x, self.coef, j, 0, st)
-        return x
+            if A.cheb_step(cur, b, self.D, d, self.coef, j, out=other) is not None:
+                cur, other = other, cur
+            else:
+                A.apply(RESIDUAL, cur, b, out=other)
+                call("pmg_cheb_step", code, n, other, self.D, d, cur, self.coef, j, 0, st)
+        return cur
 
     def solve(self, rhs, x0=None, trans="N"):
         raise NotImplementedError("Chebyshev is a multigrid smoother (GeometricMultigrid calls smooth())")
@@ -384,21 +390,21 @@ class GeometricMultigrid(Preconditioner):
 
     def _vcycle_chebyshev(self, b, x0=None):
         A, sm = self.A, self.smoother
-        u, d, r = self._buf[0], self._buf[1], self._buf[2]
+        u0, u1, d = self._buf[0], self._buf[1], self._buf[2]
         if x0 is None:
-            sm.smooth(A, b, u, d, r, zero_start=True)
+            u = sm.smooth(A, b, u0, d, u1, zero_start=True)
         else:
-            u.copy_(x0)
-            sm.smooth(A, b, u, d, r, zero_start=False)
-        A.apply(RESIDUAL, u, b, out=r)
+            u0.copy_(x0)
+            u = sm.smooth(A, b, u0, d, u1, zero_start=False)
+        other = u1 if u is u0 else u0
+        A.apply(RESIDUAL, u, b, out=other)
         g = self.grid
         inner = self.inner_level
         rc = self._rc
-        call("pmg_restrict", A.code, g.nelx, g.nely, g.nelz, r, rc, stream())
+        call("pmg_restrict", A.code, g.nelx, g.nely, g.nelz, other, rc, stream())
         uc = inner._vcycle(rc) if isinstance(inner, GeometricMultigrid) else inner.solve(rc)
         call("pmg_prolong_add", A.code, g.nelx, g.nely, g.nelz, uc, u, stream())
-        sm.smooth(A, b, u, d, r, zero_start=False)
-        return u
+        return sm.smooth(A, b, u, d, other, zero_start=False)
 
     @classmethod
     def hierarchy(cls, domain, levels=None, smoother_w=0.5, smooth_steps=5, precision=None, max_coarse_dofs=3000,

@@ -319,14 +319,31 @@ def test_chebyshev_smoother(pg):
     b = rng.standard_normal(n)
     x = torch.zeros(n, dtype=torch.float64, device="cuda")
     dv, r = torch.empty_like(x), torch.empty_like(x)
-    sm.smooth(A1, dev(b), x, dv, r, zero_start=True)
+    res = sm.smooth(A1, dev(b), x, dv, r, zero_start=True)     # fused stencil steps
     xr = np.zeros(n)
     dr = coef[1] * b / l1
     xr = xr + dr
     for j in range(1, deg):
         dr = coef[2 * j] * dr + coef[2 * j + 1] * (b - Ad @ xr) / l1
         xr = xr + dr
-    np.testing.assert_allclose(host(x), xr, rtol=1e-11, atol=1e-12 * np.abs(xr).max())
+    np.testing.assert_allclose(host(res), xr, rtol=1e-11, atol=1e-12 * np.abs(xr).max())
+    # fused steps of the FP32 tensor-core level-0 operator from a nonzero start, against FP64 numpy
+    from pymoto_gb300._lib import F32
+    op32 = op.astype(F32)
+    sm32 = pg.Chebyshev(degree=3, ratio=ratio)
+    sm32.update(op32)
+    D32 = host(sm32.D)
+    x0 = rng.standard_normal(K.shape[0]).astype(np.float32)
+    b0 = rng.standard_normal(K.shape[0]).astype(np.float32)
+    xs = dev(x0, torch.float32)
+    res32 = sm32.smooth(op32, dev(b0, torch.float32), xs, torch.empty_like(xs), torch.empty_like(xs), zero_start=False)
+    xr = x0.astype(np.float64)
+    dr = np.zeros_like(xr)
+    for j in range(3):
+        rr = b0 - Kd @ xr
+        dr = (coef[2 * j] * dr if j else 0.0) + coef[2 * j + 1] * rr / D32
+        xr = xr + dr
+    assert np.abs(host(res32) - xr).max() <= 1e-4 * np.abs(xr).max()
     # error propagator I - X A of the smoother: spectral radius < 1
     Mi = np.diag(1 / l1)
     E = np.eye(n)
