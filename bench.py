@@ -101,7 +101,7 @@ class DesignRun:
         with pg.Network() as fn:
             xf = pg.FilterConv(d, radius=RADIUS)(self.sx)
             xs = pg.SIMP(xmin=XMIN, penal=PENAL)(xf)
-            K = pg.AssembleStiffness(d, bc=bc)(xs)
+            K = pg.AssembleStiffness(d, bc=bc, sensitivity_precision="mixed" if mixed else "fp64")(xs)
             if cheb:
                 mgs = pg.GeometricMultigrid.hierarchy(d, levels=o["levels"], smooth_steps=o["cheb_degree"],
                                                       precision="fp32" if mixed else None,

@@ -232,6 +232,11 @@ int pmg_simp_backward(int64_t n, double xmin, double penal, const double* x, con
  * dx_e (+)= alpha * u_e^T K0 v_e with Dirichlet entries of u and v zeroed (dyadcarrier.py:179-189). */
 int pmg_sens_contract(int nelx, int nely, int nelz, const double* K0_host, const uint8_t* bcmask,
                       const double* u, const double* v, double alpha, int accumulate, double* dx, void* stream);
+/* The same contraction for the mixed-precision path: element vectors shifted in FP64 by their first-node
+ * value (exact: K0 annihilates translations), the quadratic form in FP32, the result in FP64. */
+int pmg_sens_contract_mixed(int nelx, int nely, int nelz, const double* K0_host, const uint8_t* bcmask,
+                            const double* u, const double* v, double alpha, int accumulate, double* dx,
+                            void* stream);
 
 /* ---- optimality-criteria update (OC.step, pymoto/common/optimizers.py:402-437) -----------------
  * Bisection on the Lagrange multiplier fully on the device; xnew is the design of the last bisection
@@ -239,6 +244,9 @@ int pmg_sens_contract(int nelx, int nely, int nelz, const double* K0_host, const
 size_t pmg_oc_scratch_bytes(void);
 int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, double volfrac, double move,
                   double xmin, double xmax, double l1, double l2, double l1l2tol, void* scratch, void* stream);
+/* Status of the last pmg_oc_update on `scratch` (host-synchronous read): PMG_OK, or PMG_TIMEOUT if a
+ * bounded wait of the single-launch bisection expired (its CTAs were not all resident). */
+int pmg_oc_status(const void* scratch);
 
 /* ---- learned warm start (no counterpart in the reference: the reference solves every design from the
  * previous solution only).  A 3-level convolutional encoder-decoder on the voxel grid of a coarse

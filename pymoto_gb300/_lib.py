@@ -73,7 +73,9 @@ SIGNATURES = {
     "pmg_simp": (I, [L, D, D, P, P, P, P]),
     "pmg_simp_backward": (I, [L, D, D, P, P, P, P]),
     "pmg_sens_contract": (I, [I, I, I, P, P, P, P, D, I, P, P]),
+    "pmg_sens_contract_mixed": (I, [I, I, I, P, P, P, P, D, I, P, P]),
     "pmg_oc_scratch_bytes": (c_size_t, []),
+    "pmg_oc_status": (I, [P]),
     "pmg_oc_update": (I, [L, P, P, P, D, D, D, D, D, D, D, P, P]),
     "pmg_nn_conv3d_forward": (I, [I, I, I, I, I, I, P, P, P, I, P, P, P]),
     "pmg_nn_conv3d_backward_data": (I, [I, I, I, I, I, P, P, P, P]),
@@ -146,7 +148,7 @@ def _arg(a):
 # kernels launched per call where it is not exactly one (host-only entry points launch none)
 _HOST_ONLY = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_element_stiffness", "pmg_galerkin_table",
               "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth",
-              "pmg_cholesky_inverse_f32_scratch_bytes", "pmg_nn_wgrad_scratch_bytes"}
+              "pmg_cholesky_inverse_f32_scratch_bytes", "pmg_nn_wgrad_scratch_bytes", "pmg_oc_status"}
 
 
 def _launches(name, args):
@@ -160,6 +162,10 @@ def _launches(name, args):
     if name == "pmg_nn_conv3d_backward_weights":
         return 2
     if name == "pmg_oc_update":
+        # init + one cooperative launch while the design fits the registers of the resident CTAs (2 CTAs of
+        # 256 threads x 8 elements per SM); above that init + prepare + one launch per step + final
+        if int(args[0]) <= 152 * 2 * 256 * 8:
+            return 2
         width, steps = float(args[9]) - float(args[8]), 3
         while width > float(args[10]):
             width *= 0.5

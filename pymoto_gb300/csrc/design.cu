@@ -1,5 +1,7 @@
 // Design-variable kernels: density filters and their adjoints, SIMP, the adjoint sensitivity contraction
 // and the optimality-criteria update.  All FP64 (these streams are small next to the solve).
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace pmg {
@@ -192,6 +194,51 @@ __global__ void sens_kernel(Grid g, ElemMat<double, Traits<DIM>::NDE> K0, const 
   dx[e] = accumulate ? dx[e] + val : val;
 }
 
+// Mixed-precision contraction for the mixed solver path: the element vectors are shifted (in FP64) by the
+// value at their first node per component (K0 annihilates rigid translations, so the shift is exact), the
+// differences are rounded to FP32 and the 24 x 24 quadratic form runs in FP32 (FP32 K0 as a uniform
+// operand); only the result returns to FP64.  The error is that of FP32 arithmetic on the deformation of the
+// element, not on its displacement.
+template <int DIM>
+__global__ void sens_mixed_kernel(Grid g, ElemMat<float, Traits<DIM>::NDE> K0, const uint8_t* __restrict__ bcmask,
+                                  const double* __restrict__ u, const double* __restrict__ v, double alpha,
+                                  int accumulate, double* __restrict__ dx) {
+  constexpr int NN = Traits<DIM>::NN;
+  constexpr int NDE = Traits<DIM>::NDE;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.nel()) return;
+  int i, j, k;
+  elem_ijk(g, e, i, j, k);
+  double ud[NDE], vd[NDE];
+#pragma unroll
+  for (int a = 0; a < NN; ++a) {
+    const int64_t nd = node_id(g, i + (a & 1), j + ((a >> 1) & 1), k + ((a >> 2) & 1));
+    const uint8_t m = bcmask ? bcmask[nd] : 0;
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      const bool bc = (m >> c) & 1;
+      ud[a * DIM + c] = bc ? 0.0 : u[nd * DIM + c];
+      vd[a * DIM + c] = bc ? 0.0 : v[nd * DIM + c];
+    }
+  }
+  float uf[NDE], vf[NDE];
+#pragma unroll
+  for (int q = 0; q < NDE; ++q) {
+    uf[q] = (float)(ud[q] - ud[q % DIM]);
+    vf[q] = (float)(vd[q] - vd[q % DIM]);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int r = 0; r < NDE; ++r) {
+    float t = 0.f;
+#pragma unroll
+    for (int c = 0; c < NDE; ++c) t = fmaf(K0.v[r * NDE + c], vf[c], t);
+    s = fmaf(uf[r], t, s);
+  }
+  const double val = alpha * (double)s;
+  dx[e] = accumulate ? dx[e] + val : val;
+}
+
 // ------------------------------------------------------------------------------------------ OC update
 // State in scratch: sum partials and the bisection interval, all on the device.
 // x sqrt(-dg/lmid) is evaluated as (x sqrt(-dg)) / sqrt(lmid): the per-element square root is taken once and
@@ -202,6 +249,8 @@ struct OCScratch {
   double partial[OC_MAX_BLOCKS];
   double l1, l2, lmid, lmid_last;
   unsigned int ticket;
+  unsigned int generation, error;           // release counter and error flag of the single-launch bisection
+  unsigned int arrived[OC_MAX_BLOCKS];      // per-CTA step counters (arrival flags, no shared atomics)
 };
 
 __device__ __forceinline__ double oc_warp_sum(double v) {
@@ -226,11 +275,16 @@ __device__ double oc_block_sum(double v) {
 }
 
 __global__ void oc_init_kernel(OCScratch* s, double l1, double l2) {
-  s->l1 = l1;
-  s->l2 = l2;
-  s->lmid = 0.5 * (l1 + l2);
-  s->lmid_last = s->lmid;
-  s->ticket = 0u;
+  for (int b = threadIdx.x; b < OC_MAX_BLOCKS; b += blockDim.x) s->arrived[b] = 0u;
+  if (threadIdx.x == 0) {
+    s->l1 = l1;
+    s->l2 = l2;
+    s->lmid = 0.5 * (l1 + l2);
+    s->lmid_last = s->lmid;
+    s->ticket = 0u;
+    s->generation = 0u;
+    s->error = 0u;
+  }
 }
 
 // t = x sqrt(-min(dg, 0)), stored in xnew until the final step overwrites it
@@ -281,6 +335,105 @@ __global__ void __launch_bounds__(OC_THREADS) oc_step_kernel(int64_t n, const do
     s->lmid_last = lmid;
     s->lmid = 0.5 * (s->l1 + s->l2);
     s->ticket = 0u;
+  }
+}
+
+// All bisection steps in one cooperative launch (every CTA resident): each thread keeps its elements in
+// registers (x, x sqrt(-dg), lower and upper bound).  Per step every CTA writes its partial volume and then
+// its step counter; CTA 0 waits for all counters (one thread per CTA), sums the partials in CTA order,
+// updates the interval exactly as oc_step_kernel and publishes the step through a generation counter that
+// the other CTAs wait for.  No shared-address atomics; every wait is bounded: after OC_SPIN_LIMIT polls the
+// kernel sets s->error and returns.  Finally xnew = the design of the last step.
+constexpr int OCP_PER_THREAD = 8;
+constexpr unsigned OC_SPIN_LIMIT = 1u << 24;   // polls of about 0.1-0.5 us each: a few seconds at most
+
+__global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, const double* __restrict__ x,
+                                                                   const double* __restrict__ dg,
+                                                                   double* __restrict__ xnew, double target,
+                                                                   double move, double xmin, double xmax, int steps,
+                                                                   OCScratch* s) {
+  __shared__ double s_lmid;
+  __shared__ int s_abort;
+  volatile OCScratch* vs = (volatile OCScratch*)s;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double tv[OCP_PER_THREAD], lo[OCP_PER_THREAD], hi[OCP_PER_THREAD];
+#pragma unroll
+  for (int k = 0; k < OCP_PER_THREAD; ++k) {
+    const int64_t i = i0 + k * stride;
+    if (i < n) {
+      const double g = dg[i] < 0.0 ? dg[i] : 0.0;
+      const double xv = x[i];
+      tv[k] = xv * sqrt(-g);
+      lo[k] = fmax(xmin, xv - move);
+      hi[k] = fmin(xmax, xv + move);
+    } else {
+      tv[k] = lo[k] = hi[k] = 0.0;
+    }
+  }
+  if (threadIdx.x == 0) s_abort = 0;
+  for (int step = 0; step < steps; ++step) {
+    if (threadIdx.x == 0) s_lmid = vs->lmid;
+    __syncthreads();
+    const double sc = 1.0 / sqrt(s_lmid);
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < OCP_PER_THREAD; ++k)
+      if (i0 + k * stride < n) acc += fmin(fmax(tv[k] * sc, lo[k]), hi[k]);
+    acc = oc_block_sum(acc);
+    const unsigned gen = (unsigned)(step + 1);
+    if (threadIdx.x == 0) {
+      vs->partial[blockIdx.x] = acc;
+      __threadfence();
+      vs->arrived[blockIdx.x] = gen;
+    }
+    if (blockIdx.x == 0) {
+      // wait for every CTA (one polling thread per CTA), then decide
+      for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        unsigned polls = 0;
+        while (vs->arrived[b] < gen) {
+          if (++polls > OC_SPIN_LIMIT) {
+            atomicExch(&s->error, 1u);
+            s_abort = 1;
+            break;
+          }
+        }
+      }
+      __syncthreads();
+      __threadfence();
+      double tot = 0.0;
+      for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) tot += vs->partial[b];
+      tot = oc_block_sum(tot);
+      if (threadIdx.x == 0) {
+        const double lmid = vs->lmid;
+        if (tot - target > 0.0)
+          vs->l1 = lmid;
+        else
+          vs->l2 = lmid;
+        vs->lmid_last = lmid;
+        vs->lmid = 0.5 * (vs->l1 + vs->l2);
+        __threadfence();
+        vs->generation = gen;
+      }
+    } else if (threadIdx.x == 0) {
+      unsigned polls = 0;
+      while (vs->generation < gen) {
+        if (++polls > OC_SPIN_LIMIT) {
+          atomicExch(&s->error, 1u);
+          s_abort = 1;
+          break;
+        }
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    if (s_abort) return;
+  }
+  const double sc = 1.0 / sqrt(vs->lmid_last);
+#pragma unroll
+  for (int k = 0; k < OCP_PER_THREAD; ++k) {
+    const int64_t i = i0 + k * stride;
+    if (i < n) xnew[i] = fmin(fmax(tv[k] * sc, lo[k]), hi[k]);
   }
 }
 
@@ -371,7 +524,33 @@ int pmg_sens_contract(int nelx, int nely, int nelz, const double* K0_host, const
   return check_launch();
 }
 
+int pmg_sens_contract_mixed(int nelx, int nely, int nelz, const double* K0_host, const uint8_t* bcmask,
+                            const double* u, const double* v, double alpha, int accumulate, double* dx,
+                            void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || !K0_host || !u || !v || !dx) return PMG_BAD_ARG;
+  Grid g{nelx, nely, nelz};
+  const unsigned b = blocks_for(g.nel(), 128);
+  if (g.dim() == 3)
+    sens_mixed_kernel<3><<<b, 128, 0, as_stream(stream)>>>(g, make_elem_mat<float, 24>(K0_host), bcmask, u, v, alpha,
+                                                           accumulate, dx);
+  else
+    sens_mixed_kernel<2><<<b, 128, 0, as_stream(stream)>>>(g, make_elem_mat<float, 8>(K0_host), bcmask, u, v, alpha,
+                                                           accumulate, dx);
+  return check_launch();
+}
+
 size_t pmg_oc_scratch_bytes(void) { return sizeof(OCScratch); }
+
+int pmg_oc_status(const void* scratch) {
+  if (!scratch) return PMG_BAD_ARG;
+  unsigned err = 0;
+  cudaError_t e = cudaMemcpy(&err, &((const OCScratch*)scratch)->error, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    set_error(cudaGetErrorString(e));
+    return PMG_CUDA_ERR;
+  }
+  return err ? PMG_TIMEOUT : PMG_OK;
+}
 
 int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, double volfrac, double move, double xmin,
                   double xmax, double l1, double l2, double l1l2tol, void* scratch, void* stream) {
@@ -382,17 +561,43 @@ int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, do
   if (nb > 2 * 152) nb = 2 * 152;
   if (nb < 1) nb = 1;
   if (x == xnew || dg == xnew) return PMG_BAD_ARG;
-  oc_init_kernel<<<1, 1, 0, st>>>(s, l1, l2);
-  oc_prepare_kernel<<<(unsigned)nb, OC_THREADS, 0, st>>>(n, x, dg, xnew);
   // the interval halves every step, so the step count is known on the host: same loop as OC.step
   double a = l1, b = l2;
   const double target = volfrac * (double)n;
   int steps = 0;
   while (b - a > l1l2tol) {
-    oc_step_kernel<<<(unsigned)nb, OC_THREADS, 0, st>>>(n, x, xnew, target, move, xmin, xmax, s);
     a = 0.5 * (a + b);  // only the interval width matters for the count
     if (++steps > 200) return PMG_BAD_ARG;
   }
+  oc_init_kernel<<<1, 256, 0, st>>>(s, l1, l2);
+  // single cooperative launch when every element fits in the registers of co-resident CTAs
+  static int coop_blocks[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) {
+    if (coop_blocks[dev] == 0) {
+      int sms = 0, per_sm = 0, coop = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, oc_persistent_kernel, OC_THREADS, 0);
+      coop_blocks[dev] = coop ? std::min(sms * per_sm, OC_MAX_BLOCKS) : -1;
+    }
+    const int cb = coop_blocks[dev];
+    if (cb > 0 && n <= (int64_t)cb * OC_THREADS * OCP_PER_THREAD) {
+      const int grid = cb;   // all co-resident slots: the fewest elements per thread
+      void* args[] = {(void*)&n, (void*)&x, (void*)&dg, (void*)&xnew, (void*)&target, (void*)&move,
+                      (void*)&xmin, (void*)&xmax, (void*)&steps, (void*)&s};
+      cudaError_t e = cudaLaunchCooperativeKernel((const void*)oc_persistent_kernel, dim3(grid), dim3(OC_THREADS),
+                                                  args, 0, st);
+      if (e != cudaSuccess) {
+        set_error(cudaGetErrorString(e));
+        return PMG_CUDA_ERR;
+      }
+      return check_launch();
+    }
+  }
+  oc_prepare_kernel<<<(unsigned)nb, OC_THREADS, 0, st>>>(n, x, dg, xnew);
+  for (int k = 0; k < steps; ++k)
+    oc_step_kernel<<<(unsigned)nb, OC_THREADS, 0, st>>>(n, x, xnew, target, move, xmin, xmax, s);
   oc_final_kernel<<<(unsigned)nb, OC_THREADS, 0, st>>>(n, x, xnew, move, xmin, xmax, s);
   return check_launch();
 }

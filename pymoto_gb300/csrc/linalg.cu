@@ -1,4 +1,6 @@
 // Reductions, CG vector updates, precision conversion and the FP64 banded Cholesky of the coarsest level.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace pmg {
@@ -160,13 +162,17 @@ __global__ void scale_kernel(int64_t n, T* __restrict__ y, const T* __restrict__
     y[i] = a * x[i];
 }
 
-template <typename T>
-__global__ void mask_bc_kernel(int dim, int64_t nnodes, const uint8_t* __restrict__ m, int keep, const T* __restrict__ x,
+// One thread per node (the mask byte is read once, no index division).
+template <typename T, int DIM>
+__global__ void mask_bc_kernel(int64_t nnodes, const uint8_t* __restrict__ m, int keep, const T* __restrict__ x,
                                T* __restrict__ y) {
-  const int64_t n = nnodes * dim;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const bool bc = (m[i / dim] >> (i % dim)) & 1;
-    y[i] = (bc == (keep != 0)) ? x[i] : T(0);
+  for (int64_t nd = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; nd < nnodes; nd += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned mm = m[nd];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const bool bc = (mm >> d) & 1u;
+      y[nd * DIM + d] = (bc == (keep != 0)) ? x[nd * DIM + d] : T(0);
+    }
   }
 }
 
@@ -429,30 +435,51 @@ __global__ void __launch_bounds__(256) chol_block_inverse_kernel(int n, const do
 // FP32 inverse of a banded FP64 factor for the FP32 coarse solve: XT = (L^{-1})^T row by row, one warp
 // per column c of L^{-1} (x = L^{-1} e_c by tiles: x_B = Dinv[b] (e_c - L[B, <B] x_<B), lanes as the rows of
 // the tile), then Ainv = XT XT^T (= L^{-T} L^{-1}) by a tiled product.  L32 is the FP32 copy of the factor.
+// The 8 warps of a CTA handle 8 consecutive columns, which share their first tile, so they walk the tiles
+// together: each tile row of L (32 rows x the band) is staged once per CTA in shared memory (coalesced)
+// and read from there by all 8 warps.
 constexpr int TRINV_WARPS = 8;
+constexpr int TRINV_PITCH_PAD = 1;   // odd row pitch: lanes (rows) hit distinct banks
 __global__ void __launch_bounds__(TRINV_WARPS * 32) chol_trinv_f32_kernel(int n, const float* __restrict__ L32, int bw,
                                                                          const float* __restrict__ Dinv,
                                                                          float* __restrict__ XT) {
   extern __shared__ __align__(16) unsigned char c_smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int c = blockIdx.x * TRINV_WARPS + warp;
-  if (c >= n) return;   // whole warps
-  float* x = reinterpret_cast<float*>(c_smem) + (size_t)warp * n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int c0 = blockIdx.x * nwarps;
+  const int c = c0 + warp;
+  const int span = bw + TB;                                  // band columns of a tile row, rounded up
+  const int pitch = (span | 1) + TRINV_PITCH_PAD - 1;        // odd
+  float* Ls = reinterpret_cast<float*>(c_smem);              // [TB][pitch]
+  float* Dsm = Ls + TB * pitch;                              // [TB][TB + 1]: the tile inverse
+  float* xall = Dsm + TB * (TB + 1);                         // [warps][n]
+  float* x = xall + (size_t)warp * n;
   const int nblk = (n + TB - 1) / TB;
-  const int bc = c / TB;
-  float* out = XT + (int64_t)c * n;
-  for (int i = lane; i < bc * TB; i += 32) out[i] = 0.f;
+  const int bc = c0 / TB;                                    // first tile of every column of this CTA
+  if (c < n) {
+    float* out = XT + (int64_t)c * n;
+    for (int i = lane; i < bc * TB; i += 32) out[i] = 0.f;
+  }
   for (int kb = bc; kb < nblk; ++kb) {
     const int k0 = kb * TB;
     const int nb = min(TB, n - k0);
+    const int jbeg = max(c0, k0 - bw);                       // leftmost column any warp of the CTA reads
+    const int width = k0 - jbeg;                             // <= bw
+    __syncthreads();                                          // previous tile row fully consumed
+    for (int e = threadIdx.x; e < TB * width; e += blockDim.x) {
+      const int r = e / width, j = e - r * width;
+      Ls[r * pitch + j] = r < nb ? L32[(int64_t)(k0 + r) * n + jbeg + j] : 0.f;
+    }
+    for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) Dsm[(e / TB) * (TB + 1) + e % TB] = Dinv[(int64_t)kb * TB * TB + e];
+    __syncthreads();
+    if (c >= n) continue;
     const int i = k0 + lane;
     float t = 0.f;
-    if (kb == bc) {
+    if (kb <= c / TB) {                                       // tiles up to the column's own: x = e_c there
       t = (i == c) ? 1.f : 0.f;
     } else if (lane < nb) {
-      const float* Lr = L32 + (int64_t)i * n;
+      const float* Lr = Ls + lane * pitch - jbeg;
       float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;   // four independent chains
-      int j = max(c, k0 - bw);
+      int j = max(c, jbeg);
       for (; j + 4 <= k0; j += 4) {
         p0 = fmaf(Lr[j], x[j], p0);
         p1 = fmaf(Lr[j + 1], x[j + 1], p1);
@@ -462,13 +489,13 @@ __global__ void __launch_bounds__(TRINV_WARPS * 32) chol_trinv_f32_kernel(int n,
       for (; j < k0; ++j) p0 = fmaf(Lr[j], x[j], p0);
       t = -((p0 + p1) + (p2 + p3));
     }
-    const float* D = Dinv + (int64_t)kb * TB * TB + lane * TB;
+    const float* D = Dsm + lane * (TB + 1);
     float acc = 0.f;
 #pragma unroll 8
     for (int q = 0; q < TB; ++q) acc = fmaf(D[q], __shfl_sync(0xffffffffu, t, q), acc);
     if (lane < nb) {
       x[i] = acc;
-      out[i] = acc;
+      XT[(int64_t)c * n + i] = acc;
     }
     __syncwarp();
   }
@@ -775,11 +802,16 @@ int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int k
                 void* stream) {
   if (nnodes < 0 || (dim != 2 && dim != 3) || !bcmask || !x || !y) return PMG_BAD_ARG;
   cudaStream_t st = as_stream(stream);
-  const int64_t n = nnodes * dim;
-  if (dtype == PMG_F64)
-    mask_bc_kernel<double><<<stream_blocks(n), 256, 0, st>>>(dim, nnodes, bcmask, keep_bc, (const double*)x, (double*)y);
+  if (nnodes == 0) return PMG_OK;
+  const unsigned g = blocks_for(nnodes, 256);
+  if (dtype == PMG_F64 && dim == 3)
+    mask_bc_kernel<double, 3><<<g, 256, 0, st>>>(nnodes, bcmask, keep_bc, (const double*)x, (double*)y);
+  else if (dtype == PMG_F64)
+    mask_bc_kernel<double, 2><<<g, 256, 0, st>>>(nnodes, bcmask, keep_bc, (const double*)x, (double*)y);
+  else if (dtype == PMG_F32 && dim == 3)
+    mask_bc_kernel<float, 3><<<g, 256, 0, st>>>(nnodes, bcmask, keep_bc, (const float*)x, (float*)y);
   else if (dtype == PMG_F32)
-    mask_bc_kernel<float><<<stream_blocks(n), 256, 0, st>>>(dim, nnodes, bcmask, keep_bc, (const float*)x, (float*)y);
+    mask_bc_kernel<float, 2><<<g, 256, 0, st>>>(nnodes, bcmask, keep_bc, (const float*)x, (float*)y);
   else
     return PMG_BAD_ARG;
   return check_launch();
@@ -911,12 +943,17 @@ int pmg_cholesky_inverse_f32(int n, const double* L, int bw, void* scratch, floa
   float* Dinv = XT + (size_t)n * n;
   chol_block_inverse_kernel<float><<<nblk, 256, 0, st>>>(n, L, Dinv);
   convert_kernel<double, float><<<stream_blocks((int64_t)n * n), 256, 0, st>>>((int64_t)n * n, L, L32, 1.0);
-  // warps per CTA bounded by the shared memory for their columns (n floats each)
-  const size_t smem = sizeof(float) * (size_t)n * TRINV_WARPS;
+  // shared memory: one staged tile row of L (TB x odd pitch >= bw + TB) and one column per warp (up to 8
+  // warps, fewer when the columns do not fit)
+  const int pitch = ((bw + TB) | 1) + TRINV_PITCH_PAD - 1;
+  const size_t tile_bytes = sizeof(float) * ((size_t)TB * pitch + TB * (TB + 1)), col_bytes = sizeof(float) * (size_t)n;
+  const size_t budget = 200 * 1024;
+  if (tile_bytes + col_bytes > budget) return PMG_BAD_ARG;
+  const int warps = (int)std::min<size_t>(TRINV_WARPS, (budget - tile_bytes) / col_bytes);
+  const size_t smem = tile_bytes + col_bytes * warps;
   static size_t smem_set[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return check_launch();
-  if (smem > 200 * 1024) return PMG_BAD_ARG;
   if (smem > smem_set[dev]) {
     cudaError_t e = cudaFuncSetAttribute(chol_trinv_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) {
@@ -925,7 +962,7 @@ int pmg_cholesky_inverse_f32(int n, const double* L, int bw, void* scratch, floa
     }
     smem_set[dev] = smem;
   }
-  chol_trinv_f32_kernel<<<(n + TRINV_WARPS - 1) / TRINV_WARPS, TRINV_WARPS * 32, smem, st>>>(n, L32, bw, Dinv, XT);
+  chol_trinv_f32_kernel<<<(n + warps - 1) / warps, warps * 32, smem, st>>>(n, L32, bw, Dinv, XT);
   const dim3 grid(nblk, nblk);
   syrk_f32_kernel<<<grid, 256, 0, st>>>(n, XT, Ainv);
   return check_launch();

@@ -8,6 +8,8 @@
 //  Galerkin: coarse element matrices E_C = sum_c M_c^T E_c M_c by sum factorisation.
 #include <cstdio>
 
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace pmg {
@@ -414,138 +416,208 @@ __device__ void galerkin_child_accumulate(T* E, T* K, T* buf, int s) {
 }
 
 // Level-1 coarse element matrices from the matrix-free fine operator.
-// One CTA per coarse element.  Unconstrained children use the precomputed table; children touching a
-// Dirichlet dof are transformed explicitly with their masked matrix plus the bcdiag terms of the fine
-// Dirichlet dofs assigned to them (each fine node is assigned to the element min(i, nx-1), ...).
+// Persistent CTAs of 8 warps walk the coarse elements 8 at a time, one warp per coarse element: if no node
+// of its children is constrained (the common case) the warp writes E = sum_c x_c (M_c^T K0 M_c) from the
+// precomputed table (staged in shared memory), 18 entries per lane in 3D.  Coarse elements touching a
+// Dirichlet dof are queued and then transformed by the whole CTA: unconstrained children from the table,
+// the others with their masked matrix plus the bcdiag terms of the fine Dirichlet dofs assigned to them
+// (each fine node is assigned to the element min(i, nx-1), ...), by sum factorisation.
+constexpr int GAL_THREADS = 256;
+constexpr int GAL_WARPS = GAL_THREADS / 32;
+
 template <typename T, int DIM>
-__global__ void galerkin_from_ebe_kernel(Grid gf, const T* __restrict__ xe, ElemMat<T, Traits<DIM>::NDE> K0,
-                                         const uint8_t* __restrict__ bcmask, T bcdiag, const T* __restrict__ table,
-                                         T* __restrict__ Ec) {
+__global__ void __launch_bounds__(GAL_THREADS) galerkin_from_ebe_kernel(Grid gf, const T* __restrict__ xe,
+                                                                        ElemMat<T, Traits<DIM>::NDE> K0,
+                                                                        const uint8_t* __restrict__ bcmask, T bcdiag,
+                                                                        const T* __restrict__ table,
+                                                                        T* __restrict__ Ec, unsigned perm) {
   constexpr int NN = Traits<DIM>::NN;
   constexpr int NDE = Traits<DIM>::NDE;
   constexpr int NE = NDE * NDE;
-  __shared__ T E[NE];
-  __shared__ T Kc[NE];
-  __shared__ T buf[NE];
+  constexpr int PER_LANE = (NE + 31) / 32;
+  extern __shared__ __align__(16) unsigned char gal_smem[];
+  T* tab = reinterpret_cast<T*>(gal_smem);   // [NN][NE]
+  T* E = tab + NN * NE;
+  T* Kc = E + NE;
+  T* buf = Kc + NE;
   __shared__ T xs[NN];
   __shared__ uint8_t cmask[NN][NN];
+  __shared__ int queue[GAL_WARPS];
+  __shared__ int nqueue;
   const Grid gc = gf.coarse();
-  const int ec = blockIdx.x;
-  const int CI = ec % gc.nx, CJ = (ec / gc.nx) % gc.ny, CK = ec / (gc.nx * gc.ny);
-  // masks of all children's nodes and the children's x in one pass, then one vote
-  int mine = 0;
-  if (threadIdx.x < NN * NN) {
-    const int sc = threadIdx.x / NN, a = threadIdx.x % NN;
-    const int ni = 2 * CI + (sc & 1) + (a & 1), nj = 2 * CJ + ((sc >> 1) & 1) + ((a >> 1) & 1);
-    const int nk = DIM == 3 ? 2 * CK + ((sc >> 2) & 1) + ((a >> 2) & 1) : 0;
-    const uint8_t m = bcmask ? bcmask[node_id(gf, ni, nj, nk)] : 0;
-    cmask[sc][a] = m;
-    mine = m != 0;
-  }
-  if (threadIdx.x < NN) {
-    const int sc = threadIdx.x;
-    xs[sc] = xe[elem_id(gf, 2 * CI + (sc & 1), 2 * CJ + ((sc >> 1) & 1), DIM == 3 ? 2 * CK + ((sc >> 2) & 1) : 0)];
-  }
-  const int any_bc = __syncthreads_or(mine);
-  if (!any_bc) {
-    // every child unconstrained: E = sum_c x_c (M_c^T K0 M_c), straight to global memory
-    for (int e = threadIdx.x; e < NE; e += blockDim.x) {
-      T v = T(0);
-#pragma unroll
-      for (int sc = 0; sc < NN; ++sc) v = fma(xs[sc], table[sc * NE + e], v);
-      Ec[(int64_t)ec * NE + e] = v;
-    }
-    return;
-  }
-  for (int e = threadIdx.x; e < NE; e += blockDim.x) E[e] = T(0);
+  const int nelc = (int)gc.nel();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int e = threadIdx.x; e < NN * NE; e += blockDim.x) tab[e] = table[e];
+  if (threadIdx.x == 0) nqueue = 0;
   __syncthreads();
-  for (int s = 0; s < NN; ++s) {
-    const int fi = 2 * CI + (s & 1), fj = 2 * CJ + ((s >> 1) & 1), fk = DIM == 3 ? 2 * CK + ((s >> 2) & 1) : 0;
-    const T x = xs[s];
-    bool child_bc = false;
-#pragma unroll
-    for (int a = 0; a < NN; ++a) child_bc |= cmask[s][a] != 0;
-    if (!child_bc) {
-      for (int e = threadIdx.x; e < NE; e += blockDim.x) E[e] = fma(x, table[s * NE + e], E[e]);
-      __syncthreads();
-      continue;
-    }
-    // masked child matrix x Z K0 Z + bcdiag on the Dirichlet dofs assigned to this fine element (each fine
-    // node is assigned to element (min(i, nx-1), min(j, ny-1), min(k, nz-1)))
-    for (int e = threadIdx.x; e < NE; e += blockDim.x) {
-      const int r = e / NDE, c = e % NDE;
-      const int rn = r / DIM, rd = r % DIM, cn = c / DIM, cd = c % DIM;
-      const bool rb = (cmask[s][rn] >> rd) & 1, cb = (cmask[s][cn] >> cd) & 1;
-      T v = (rb || cb) ? T(0) : x * K0.v[e];
-      if (r == c && rb) {
-        const int ni = fi + (rn & 1), nj = fj + ((rn >> 1) & 1), nk = DIM == 3 ? fk + ((rn >> 2) & 1) : 0;
-        const int ai = min(ni, gf.nx - 1), aj = min(nj, gf.ny - 1), ak = DIM == 3 ? min(nk, gf.nz - 1) : 0;
-        if (ai == fi && aj == fj && ak == fk) v = bcdiag;
+  for (int base = blockIdx.x * GAL_WARPS; base < nelc; base += gridDim.x * GAL_WARPS) {
+    // elements visited in a permuted order (perm coprime to the count): constrained elements, which take
+    // the slow path, spread over all CTAs instead of following the period of the grid
+    const int lin = base + warp;
+    const int ec = lin < nelc ? (int)(((uint64_t)lin * perm) % (uint64_t)nelc) : nelc;
+    if (lin < nelc) {
+      const int CI = ec % gc.nx, CJ = (ec / gc.nx) % gc.ny, CK = ec / (gc.nx * gc.ny);
+      // children's x (lanes 0..NN-1) and any constrained node of the children (NN*NN pairs over the lanes)
+      T xv = T(0);
+      if (lane < NN)
+        xv = xe[elem_id(gf, 2 * CI + (lane & 1), 2 * CJ + ((lane >> 1) & 1), DIM == 3 ? 2 * CK + ((lane >> 2) & 1) : 0)];
+      int mine = 0;
+      for (int q = lane; q < NN * NN; q += 32) {
+        const int sc = q / NN, a = q % NN;
+        const int ni = 2 * CI + (sc & 1) + (a & 1), nj = 2 * CJ + ((sc >> 1) & 1) + ((a >> 1) & 1);
+        const int nk = DIM == 3 ? 2 * CK + ((sc >> 2) & 1) + ((a >> 2) & 1) : 0;
+        mine |= (bcmask ? bcmask[node_id(gf, ni, nj, nk)] : 0) != 0;
       }
-      Kc[e] = v;
+      if (__any_sync(0xffffffffu, mine)) {
+        if (lane == 0) queue[atomicAdd(&nqueue, 1)] = ec;
+      } else {
+        T xc[NN];
+#pragma unroll
+        for (int sc = 0; sc < NN; ++sc) xc[sc] = __shfl_sync(0xffffffffu, xv, sc);
+        T* out = Ec + (int64_t)ec * NE;
+#pragma unroll
+        for (int k = 0; k < PER_LANE; ++k) {
+          const int e = lane + 32 * k;
+          if (e < NE) {
+            T v = T(0);
+#pragma unroll
+            for (int sc = 0; sc < NN; ++sc) v = fma(xc[sc], tab[sc * NE + e], v);
+            out[e] = v;
+          }
+        }
+      }
     }
     __syncthreads();
-    galerkin_child_accumulate<T, DIM>(E, Kc, buf, s);
+    const int nq = nqueue;
+    for (int qi = 0; qi < nq; ++qi) {
+      const int ecq = queue[qi];
+      const int CI = ecq % gc.nx, CJ = (ecq / gc.nx) % gc.ny, CK = ecq / (gc.nx * gc.ny);
+      for (int q = threadIdx.x; q < NN * NN; q += blockDim.x) {
+        const int sc = q / NN, a = q % NN;
+        const int ni = 2 * CI + (sc & 1) + (a & 1), nj = 2 * CJ + ((sc >> 1) & 1) + ((a >> 1) & 1);
+        const int nk = DIM == 3 ? 2 * CK + ((sc >> 2) & 1) + ((a >> 2) & 1) : 0;
+        cmask[sc][a] = bcmask ? bcmask[node_id(gf, ni, nj, nk)] : 0;
+      }
+      if (threadIdx.x < NN) {
+        const int sc = threadIdx.x;
+        xs[sc] = xe[elem_id(gf, 2 * CI + (sc & 1), 2 * CJ + ((sc >> 1) & 1), DIM == 3 ? 2 * CK + ((sc >> 2) & 1) : 0)];
+      }
+      for (int e = threadIdx.x; e < NE; e += blockDim.x) E[e] = T(0);
+      __syncthreads();
+      for (int sidx = 0; sidx < NN; ++sidx) {
+        const int fi = 2 * CI + (sidx & 1), fj = 2 * CJ + ((sidx >> 1) & 1), fk = DIM == 3 ? 2 * CK + ((sidx >> 2) & 1) : 0;
+        const T x = xs[sidx];
+        bool child_bc = false;
+#pragma unroll
+        for (int a = 0; a < NN; ++a) child_bc |= cmask[sidx][a] != 0;
+        if (!child_bc) {
+          for (int e = threadIdx.x; e < NE; e += blockDim.x) E[e] = fma(x, tab[sidx * NE + e], E[e]);
+          __syncthreads();
+          continue;
+        }
+        for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+          const int r = e / NDE, c = e % NDE;
+          const int rn = r / DIM, rd = r % DIM, cn = c / DIM, cd = c % DIM;
+          const bool rb = (cmask[sidx][rn] >> rd) & 1, cb = (cmask[sidx][cn] >> cd) & 1;
+          T v = (rb || cb) ? T(0) : x * K0.v[e];
+          if (r == c && rb) {
+            const int ni = fi + (rn & 1), nj = fj + ((rn >> 1) & 1), nk = DIM == 3 ? fk + ((rn >> 2) & 1) : 0;
+            const int ai = min(ni, gf.nx - 1), aj = min(nj, gf.ny - 1), ak = DIM == 3 ? min(nk, gf.nz - 1) : 0;
+            if (ai == fi && aj == fj && ak == fk) v = bcdiag;
+          }
+          Kc[e] = v;
+        }
+        __syncthreads();
+        galerkin_child_accumulate<T, DIM>(E, Kc, buf, sidx);
+      }
+      for (int e = threadIdx.x; e < NE; e += blockDim.x) Ec[(int64_t)ecq * NE + e] = E[e];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) nqueue = 0;
+    __syncthreads();
   }
-  for (int e = threadIdx.x; e < NE; e += blockDim.x) Ec[(int64_t)ec * NE + e] = E[e];
 }
 
-// Next-level coarse element matrices from element matrices Ef of grid gf.  The CTA stages all 2^dim child
-// matrices in shared memory and transforms them together (M_c^T E_c M_c by sum factorisation, one axis per
-// pass, 2*dim passes), then sums the children: 2*dim + 2 barriers per coarse element.
+// Next-level coarse element matrices from element matrices Ef of grid gf: E_C = sum_c M_c^T E_c M_c, where
+// M_c maps the coarse element's dofs to those of child c (trilinear weights).  One warp per coarse element,
+// children one after the other, no CTA barriers: lane a forms row a of T = E_c M_c (one column J at a time,
+// so the trip count over the nonzeros of column J of M_c is uniform across the warp), then lane J adds
+// column J of M_c^T T (one row I at a time) to its column of E_C, kept in registers.  The nonzeros of M_c
+// (child c, coarse node N -> fine nodes with nonzero weight) come from a table in shared memory.
 template <typename T, int DIM>
-__global__ void galerkin_from_elements_kernel(Grid gf, const T* __restrict__ Ef, T* __restrict__ Ec) {
+__global__ void __launch_bounds__(GAL_THREADS) galerkin_from_elements_kernel(Grid gf, const T* __restrict__ Ef,
+                                                                             T* __restrict__ Ec) {
   constexpr int NN = Traits<DIM>::NN;
   constexpr int NDE = Traits<DIM>::NDE;
   constexpr int NE = NDE * NDE;
+  constexpr int PITCH = NDE + 1;   // odd row pitch: lanes reading one column hit distinct banks
   extern __shared__ __align__(16) unsigned char g_smem[];
-  T* A = reinterpret_cast<T*>(g_smem);
-  T* B = A + NN * NE;
-  const Grid gc = gf.coarse();
-  const int ec = blockIdx.x;
-  const int CI = ec % gc.nx, CJ = (ec / gc.nx) % gc.ny, CK = ec / (gc.nx * gc.ny);
-  for (int idx = threadIdx.x; idx < NN * NE; idx += blockDim.x) {
-    const int sc = idx / NE, e = idx - sc * NE;
-    const int64_t child = elem_id(gf, 2 * CI + (sc & 1), 2 * CJ + ((sc >> 1) & 1), DIM == 3 ? 2 * CK + ((sc >> 2) & 1) : 0);
-    A[idx] = Ef[child * NE + e];
+  __shared__ int8_t sup_cnt[NN][NN];
+  __shared__ int8_t sup_node[NN][NN][NN];
+  __shared__ T sup_w[NN][NN][NN];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* Es = reinterpret_cast<T*>(g_smem) + (size_t)warp * (NDE * PITCH + NE);   // child matrix, padded rows
+  T* Ts = Es + NDE * PITCH;                                                     // T = E_c M_c, [a][J]
+  if (threadIdx.x < NN * NN) {
+    const int c = threadIdx.x / NN, N = threadIdx.x % NN;
+    int cnt = 0;
+    for (int a = 0; a < NN; ++a) {
+      double w = 1.0;
+#pragma unroll
+      for (int ax = 0; ax < DIM; ++ax) w *= p1((c >> ax) & 1, (a >> ax) & 1, (N >> ax) & 1);
+      if (w != 0.0) {
+        sup_node[c][N][cnt] = (int8_t)a;
+        sup_w[c][N][cnt] = (T)w;
+        ++cnt;
+      }
+    }
+    sup_cnt[c][N] = (int8_t)cnt;
   }
   __syncthreads();
-  T* src = A;
-  T* dst = B;
-#pragma unroll 1
-  for (int side = 0; side < 2; ++side) {
-#pragma unroll 1
-    for (int axis = 0; axis < DIM; ++axis) {
-      for (int idx = threadIdx.x; idx < NN * NE; idx += blockDim.x) {
-        const int sc = idx / NE, e = idx - sc * NE;
-        const int sa = (sc >> axis) & 1;
-        const int r = e / NDE, c = e - r * NDE;
-        const int q = side == 0 ? r : c;
-        const int node = q / DIM, d = q - node * DIM;
-        const int Ab = (node >> axis) & 1;
-        const T* S = src + sc * NE;
-        T v = T(0);
+  const Grid gc = gf.coarse();
+  const int nelc = (int)gc.nel();
+  const int nwarps = gridDim.x * GAL_WARPS;
+  for (int ec = blockIdx.x * GAL_WARPS + warp; ec < nelc; ec += nwarps) {
+    const int CI = ec % gc.nx, CJ = (ec / gc.nx) % gc.ny, CK = ec / (gc.nx * gc.ny);
+    T acc[NDE];
 #pragma unroll
-        for (int a = 0; a < 2; ++a) {
-          const double wgt = p1(sa, a, Ab);
-          if (wgt != 0.0) {
-            const int qa = ((node & ~(1 << axis)) | (a << axis)) * DIM + d;
-            v = fma((T)wgt, S[side == 0 ? qa * NDE + c : r * NDE + qa], v);
-          }
-        }
-        dst[idx] = v;
+    for (int I = 0; I < NDE; ++I) acc[I] = T(0);
+    for (int c = 0; c < NN; ++c) {
+      const int64_t child = elem_id(gf, 2 * CI + (c & 1), 2 * CJ + ((c >> 1) & 1), DIM == 3 ? 2 * CK + ((c >> 2) & 1) : 0);
+      const T* src = Ef + child * NE;
+      for (int e = lane; e < NE; e += 32) {
+        const int r = e / NDE;
+        Es[r * PITCH + (e - r * NDE)] = src[e];
       }
-      __syncthreads();
-      T* t = src;
-      src = dst;
-      dst = t;
-    }
-  }
-  for (int e = threadIdx.x; e < NE; e += blockDim.x) {
-    T v = T(0);
+      __syncwarp();
+      if (lane < NDE) {
+#pragma unroll 1
+        for (int J = 0; J < NDE; ++J) {
+          const int NJ = J / DIM, dJ = J - NJ * DIM;
+          const int cnt = sup_cnt[c][NJ];
+          T v = T(0);
+          for (int k = 0; k < cnt; ++k) v = fma(sup_w[c][NJ][k], Es[lane * PITCH + sup_node[c][NJ][k] * DIM + dJ], v);
+          Ts[lane * NDE + J] = v;
+        }
+      }
+      __syncwarp();
+      if (lane < NDE) {
 #pragma unroll
-    for (int sc = 0; sc < NN; ++sc) v += src[sc * NE + e];
-    Ec[(int64_t)ec * NE + e] = v;
+        for (int I = 0; I < NDE; ++I) {
+          const int NI = I / DIM, dI = I - NI * DIM;
+          const int cnt = sup_cnt[c][NI];
+          T v = acc[I];
+          for (int k = 0; k < cnt; ++k) v = fma(sup_w[c][NI][k], Ts[(sup_node[c][NI][k] * DIM + dI) * NDE + lane], v);
+          acc[I] = v;
+        }
+      }
+      __syncwarp();
+    }
+    if (lane < NDE) {
+      T* out = Ec + (int64_t)ec * NE;
+#pragma unroll
+      for (int I = 0; I < NDE; ++I) out[I * NDE + lane] = acc[I];
+    }
   }
 }
 
@@ -774,6 +846,21 @@ using namespace pmg;
 
 static bool dtype_ok(int dtype) { return dtype == PMG_F64 || dtype == PMG_F32; }
 
+// A multiplier coprime to n (visiting i -> i * m mod n is then a permutation of 0..n-1).
+static unsigned coprime_stride(int64_t n) {
+  const unsigned cands[] = {10007u, 10009u, 10037u, 1009u, 101u, 7u};
+  for (unsigned m : cands) {
+    int64_t a = n, b = m;
+    while (b) {
+      const int64_t t = a % b;
+      a = b;
+      b = t;
+    }
+    if (a == 1) return m;
+  }
+  return 1u;
+}
+
 extern "C" {
 
 int pmg_dof_connectivity(int nelx, int nely, int nelz, int64_t* dofconn, void* stream) {
@@ -905,13 +992,23 @@ int pmg_galerkin_from_ebe(int dtype, int nelx, int nely, int nelz, const void* x
       !Ec)
     return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
-  const unsigned nblk = (unsigned)g.coarse().nel();
-  const int threads = g.dim() == 3 ? 576 : 64;
+  const int64_t nelc = g.coarse().nel();
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned nblk = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nelc + GAL_WARPS - 1) / GAL_WARPS, 4 * sms));
   cudaStream_t st = as_stream(stream);
   PMG_DISPATCH(dtype, g.dim(), ([&]() -> int {
-                 galerkin_from_ebe_kernel<T, DIM><<<nblk, threads, 0, st>>>(
+                 constexpr int NE = Traits<DIM>::NDE * Traits<DIM>::NDE;
+                 const size_t smem = sizeof(T) * (size_t)(Traits<DIM>::NN + 3) * NE;
+                 cudaError_t e = cudaFuncSetAttribute(galerkin_from_ebe_kernel<T, DIM>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                 if (e != cudaSuccess) {
+                   set_error(cudaGetErrorString(e));
+                   return PMG_CUDA_ERR;
+                 }
+                 galerkin_from_ebe_kernel<T, DIM><<<nblk, GAL_THREADS, smem, st>>>(
                      g, (const T*)xe, make_elem_mat<T, Traits<DIM>::NDE>(K0_host), bcmask, (T)bcdiag, (const T*)table,
-                     (T*)Ec);
+                     (T*)Ec, coprime_stride(nelc));
                  return check_launch();
                }()));
 }
@@ -919,18 +1016,21 @@ int pmg_galerkin_from_ebe(int dtype, int nelx, int nely, int nelz, const void* x
 int pmg_galerkin_from_elements(int dtype, int nelx, int nely, int nelz, const void* Ef, void* Ec, void* stream) {
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !even_grid(nelx, nely, nelz) || !Ef || !Ec) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
-  const unsigned nblk = (unsigned)g.coarse().nel();
-  const int threads = g.dim() == 3 ? 576 : 128;
+  const int64_t nelc = g.coarse().nel();
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned nblk = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nelc + GAL_WARPS - 1) / GAL_WARPS, 8 * sms));
   cudaStream_t st = as_stream(stream);
   PMG_DISPATCH(dtype, g.dim(), ([&]() -> int {
-                 const size_t smem = 2 * sizeof(T) * Traits<DIM>::NN * Traits<DIM>::NDE * Traits<DIM>::NDE;
+                 constexpr int NDE = Traits<DIM>::NDE;
+                 const size_t smem = sizeof(T) * GAL_WARPS * (size_t)(NDE * (NDE + 1) + NDE * NDE);
                  cudaError_t e = cudaFuncSetAttribute(galerkin_from_elements_kernel<T, DIM>,
                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
                  if (e != cudaSuccess) {
                    set_error(cudaGetErrorString(e));
                    return PMG_CUDA_ERR;
                  }
-                 galerkin_from_elements_kernel<T, DIM><<<nblk, threads, smem, st>>>(g, (const T*)Ef, (T*)Ec);
+                 galerkin_from_elements_kernel<T, DIM><<<nblk, GAL_THREADS, smem, st>>>(g, (const T*)Ef, (T*)Ec);
                  return check_launch();
                }()));
 }

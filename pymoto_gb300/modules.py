@@ -250,9 +250,14 @@ class AssembleStiffness(Module):
     matrix; its sensitivity contracts the incoming dyad with K0 per element."""
 
     def __init__(self, domain, bc=None, bcdiagval=None, matrix_type=None, add_constant=None, reuse_sparsity=True,
-                 e_modulus=1.0, poisson_ratio=0.3, plane="strain"):
+                 e_modulus=1.0, poisson_ratio=0.3, plane="strain", sensitivity_precision="fp64"):
+        """sensitivity_precision: "fp64" (the reference's contraction) or "mixed" (element vectors shifted
+        in FP64 by their first-node value, quadratic form in FP32: for the mixed-precision solver path)."""
         if add_constant is not None:
             raise NotImplementedError("add_constant is not supported by the matrix-free operator")
+        if sensitivity_precision not in ("fp64", "mixed"):
+            raise ValueError("sensitivity_precision must be 'fp64' or 'mixed'")
+        self.sensitivity_precision = sensitivity_precision
         self.domain = domain
         self.grid = Grid(*grid_of(domain))
         g = self.grid
@@ -289,7 +294,8 @@ class AssembleStiffness(Module):
         for k, (u, v) in enumerate(pairs):
             ud = _to_device(u, device=device)[0]
             vd = _to_device(v, device=device)[0]
-            call("pmg_sens_contract", g.nelx, g.nely, g.nelz, self.stiffness_element, self._mask, ud, vd, 1.0,
+            fn = "pmg_sens_contract" if self.sensitivity_precision == "fp64" else "pmg_sens_contract_mixed"
+            call(fn, g.nelx, g.nely, g.nelz, self.stiffness_element, self._mask, ud, vd, 1.0,
                  int(k > 0), dx, stream())
         return _from_device(dx, self._kind)
 

@@ -50,8 +50,13 @@ class OC:
         dg = _to_device(self.calculate_dg(), device=x.device)[0]
         xnew = torch.empty_like(x)
         ws = Workspace.get(x.device)
+        if getattr(self, "_issued", False):
+            # status of the previous update's bisection (a bounded wait that expired), read after the host has
+            # synchronised on the response anyway
+            call("pmg_oc_status", ws.oc)
         call("pmg_oc_update", x.numel(), x, dg, xnew, self.maxvol, self.move, self.xmin, self.xmax, self.l1init,
              self.l2init, self.l1l2tol, ws.oc, stream())
+        self._issued = True
         self.variable.state = _from_device(xnew, kind)
         self.history.append(g)
         return xnew, g, dg

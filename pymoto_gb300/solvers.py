@@ -204,15 +204,30 @@ class DenseCholesky(LinearSolver):
             self.Ainv = self.L32 = self.Dinv32 = self.Ainv32 = None
         L = A.to_dense(out=self.L)
         call("pmg_cholesky_factor", n, L, self.bw, self._info, stream())
-        bad = int(self._info.item())
-        if bad != 0:
-            raise np.linalg.LinAlgError(f"coarsest-level matrix not positive definite (pivot {bad - 1})")
+        # the pivot check is read back without blocking the host (check() raises once it has arrived), so
+        # that the host can queue the next work while the factorisation runs
+        if getattr(self, "_info_host", None) is None:
+            self._info_host = torch.zeros(1, dtype=torch.int32).pin_memory()
+            self._info_event = torch.cuda.Event()
+        self._info_host.copy_(self._info, non_blocking=True)
+        self._info_event.record()
+        self._checked = False
         if A.code == F64 and n <= self.INVERSE_MAX_DOFS:
             if self.Ainv is None:
                 self.Ainv = torch.empty_like(self.L)
             call("pmg_cholesky_inverse", n, L, self.bw, self.Ainv, stream())
         elif A.code == F32:
             self._prepare_f32()
+
+    def check(self):
+        """Raise LinAlgError if the last factorisation met a non-positive pivot (waits for the factorisation)."""
+        if getattr(self, "_checked", True):
+            return
+        self._info_event.synchronize()
+        self._checked = True
+        bad = int(self._info_host.item())
+        if bad != 0:
+            raise np.linalg.LinAlgError(f"coarsest-level matrix not positive definite (pivot {bad - 1})")
 
     def _prepare_f32(self):
         n, dev = self.n, self.L.device
@@ -464,6 +479,15 @@ def capture_graph(fn):
     return graph, info
 
 
+def _check_coarsest(pc):
+    """check() the coarsest direct solver below a multigrid chain (after its factorisation was queued)."""
+    lv = pc
+    while isinstance(lv, GeometricMultigrid):
+        lv = lv.inner_level
+    if isinstance(lv, DenseCholesky):
+        lv.check()
+
+
 def _side_stream(owner):
     """A second CUDA stream of `owner` (created once per device), for setup work that overlaps the main one."""
     dev = torch.cuda.current_device()
@@ -596,6 +620,7 @@ class CG(LinearSolver):
         x = torch.zeros_like(b) if x0 is None else _to_device(x0, A.torch_dtype)[0].clone()
         t0 = time.perf_counter()
         it, res = pcg(A, b, self.preconditioner.solve, x, self.tol, self.maxit, self.restart)
+        _check_coarsest(self.preconditioner)
         self.iterations, self.last_residual = it, res
         if res > self.tol:
             warnings.warn(f"CG Maximum iterations ({self.maxit}) reached, with final residuals {res}")
@@ -659,7 +684,9 @@ class MixedPrecisionCG(LinearSolver):
                 self.A32 = lv0 if isinstance(lv0, StiffnessOperator) and lv0.code == F32 else A.astype(F32)
             else:
                 self.A32 = A.astype(F32)
-        main.wait_stream(side)
+        # joined just before the first preconditioner application of the next solve, so the FP64 work that
+        # precedes it (initial residual, warm-start products) also overlaps the hierarchy set-up
+        self._side_pending = side
         self._fallback_ready = False
         n, dev = self.A64.grid.ndof, self.A64.device
         if getattr(self, "_r32", None) is None or self._r32.numel() != n or self._r32.device != dev:
@@ -769,7 +796,14 @@ class MixedPrecisionCG(LinearSolver):
         s[2:3].copy_(self._pqpr[1:2])
         call("pmg_cg_update", F64, n, x, r, p, q, s[2:3], pq, s[1:2], ws.reduce, st)
 
+    def _join_setup(self):
+        side = getattr(self, "_side_pending", None)
+        if side is not None:
+            torch.cuda.current_stream().wait_stream(side)
+            self._side_pending = None
+
     def _run_step(self, slot):
+        self._join_setup()
         B = self._fcg
         if self.fell_back or not self.use_graph:
             self._fcg_step(slot)
@@ -870,6 +904,9 @@ class MixedPrecisionCG(LinearSolver):
             res = math.sqrt(max(s[1].item(), 0.0)) / bn
             if not math.isfinite(res) or ((self.fell_back or not can_fall_back) and it - it_fb >= self.maxit):
                 break
+        self._join_setup()
+        if self.preconditioner is not None:
+            _check_coarsest(self.preconditioner)
         self.iterations, self.last_residual = it, res
         # the explicit FP64 residual b - A x of the returned solution (LinSolve derives A x from it)
         self.final_residual = r if trans == "N" else None

@@ -444,6 +444,13 @@ def test_simp_and_sensitivity(pg):
         dx = torch.empty(g.nel, dtype=torch.float64, device="cuda")
         call("pmg_sens_contract", *shape, K0, op.bcmask, dev(u), dev(v), 1.0, 0, dx, stream())
         np.testing.assert_allclose(host(dx), ref, rtol=1e-12, atol=1e-13 * np.abs(ref).max())
+        # mixed contraction: FP32 quadratic form on FP64-shifted element vectors; displacements on a large
+        # offset (the shift removes it exactly), error relative to the largest sensitivity
+        off = 1e3 * np.tile([1.0, -2.0, 0.5][:g.dim], g.nnodes)
+        ref2 = O.sensitivity_contract(g, K0, [u + off], [v - off], bc)
+        dxm = torch.empty(g.nel, dtype=torch.float64, device="cuda")
+        call("pmg_sens_contract_mixed", *shape, K0, op.bcmask, dev(u + off), dev(v - off), 1.0, 0, dxm, stream())
+        assert np.abs(host(dxm) - ref2).max() <= 2e-6 * np.abs(ref2).max()
 
 
 def test_oc_update_matches_oracle(pg):
