@@ -80,7 +80,7 @@ class DesignRun:
     opts = {"inner_iters": 0, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None,
             "smoother": "chebyshev", "cheb_degree": 2, "cheb_coarse_degree": 3, "cheb_ratio": 10.0,
             "learned_train_steps": 1, "learned_stride": 4, "learned_lr": 2e-3, "learned_net": True,
-            "learned_history": 1}
+            "learned_history": 1, "coarse_lag": False}
 
     def __init__(self, arm, shape, seed, torch, pg):
         o = DesignRun.opts
@@ -106,7 +106,8 @@ class DesignRun:
                 mgs = pg.GeometricMultigrid.hierarchy(d, levels=o["levels"], smooth_steps=o["cheb_degree"],
                                                       precision="fp32" if mixed else None,
                                                       coarse_smooth_steps=o["cheb_coarse_degree"],
-                                                      smoother="chebyshev", cheb_ratio=o["cheb_ratio"])
+                                                      smoother="chebyshev", cheb_ratio=o["cheb_ratio"],
+                                                      coarse_lag=o["coarse_lag"] and mixed)
             else:
                 mgs = pg.GeometricMultigrid.hierarchy(d, levels=o["levels"], smoother_w=OMEGA,
                                                       smooth_steps=o["sweeps"], precision="fp32" if mixed else None,

@@ -97,7 +97,10 @@ int pmg_prolong_add(int dtype, int nelx, int nely, int nelz, const void* uc, voi
  * elements Ef belongs to). */
 int pmg_galerkin_table(int dim, const double* K0_host, double* table_host);
 int pmg_galerkin_from_ebe(int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
-                          const uint8_t* bcmask, double bcdiag, const void* table, void* Ec, void* stream);
+                          const uint8_t* bcmask, double bcdiag, const void* table, const int32_t* bc_elems, int n_bc,
+                          void* Ec, void* stream);
+/* bc_elems (device, n_bc entries, or NULL): the coarse elements with a constrained fine node, which a second
+ * launch handles one CTA each; with NULL they are found and handled inside the first launch. */
 int pmg_galerkin_from_elements(int dtype, int nelx, int nely, int nelz, const void* Ef, void* Ec, void* stream);
 /* Node stencils of a grid from its element matrices (assembly of sum_e P_e^T E_e P_e). */
 int pmg_stencil_from_elements(int dtype, int nelx, int nely, int nelz, const void* E, void* S, void* stream);

@@ -33,7 +33,7 @@ SIGNATURES = {
     "pmg_restrict": (I, [I, I, I, I, P, P, P]),
     "pmg_prolong_add": (I, [I, I, I, I, P, P, P]),
     "pmg_galerkin_table": (I, [I, P, P]),
-    "pmg_galerkin_from_ebe": (I, [I, I, I, I, P, P, P, D, P, P, P]),
+    "pmg_galerkin_from_ebe": (I, [I, I, I, I, P, P, P, D, P, P, I, P, P]),
     "pmg_galerkin_from_elements": (I, [I, I, I, I, P, P, P]),
     "pmg_stencil_from_elements": (I, [I, I, I, I, P, P, P]),
     "pmg_stencil_to_dense": (I, [I, I, I, I, P, P, P]),
@@ -159,6 +159,8 @@ def _launches(name, args):
         return 3 * nblk - 2 if int(args[2]) > 0 else nblk
     if name == "pmg_cholesky_inverse_f32":
         return 4
+    if name == "pmg_galerkin_from_ebe":
+        return 2 if args[9] is not None and int(args[10]) > 0 else 1
     if name == "pmg_nn_conv3d_backward_weights":
         return 2
     if name == "pmg_oc_update":

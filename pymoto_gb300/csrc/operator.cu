@@ -430,7 +430,8 @@ __global__ void __launch_bounds__(GAL_THREADS) galerkin_from_ebe_kernel(Grid gf,
                                                                         ElemMat<T, Traits<DIM>::NDE> K0,
                                                                         const uint8_t* __restrict__ bcmask, T bcdiag,
                                                                         const T* __restrict__ table,
-                                                                        T* __restrict__ Ec, unsigned perm) {
+                                                                        T* __restrict__ Ec, unsigned perm,
+                                                                        int listed) {
   constexpr int NN = Traits<DIM>::NN;
   constexpr int NDE = Traits<DIM>::NDE;
   constexpr int NE = NDE * NDE;
@@ -440,6 +441,7 @@ __global__ void __launch_bounds__(GAL_THREADS) galerkin_from_ebe_kernel(Grid gf,
   T* E = tab + NN * NE;
   T* Kc = E + NE;
   T* buf = Kc + NE;
+  T* K0s = buf + NE;                         // K0 in shared memory: the slow path reads it at per-thread indices
   __shared__ T xs[NN];
   __shared__ uint8_t cmask[NN][NN];
   __shared__ int queue[GAL_WARPS];
@@ -448,6 +450,7 @@ __global__ void __launch_bounds__(GAL_THREADS) galerkin_from_ebe_kernel(Grid gf,
   const int nelc = (int)gc.nel();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int e = threadIdx.x; e < NN * NE; e += blockDim.x) tab[e] = table[e];
+  for (int e = threadIdx.x; e < NE; e += blockDim.x) K0s[e] = K0.v[e];
   if (threadIdx.x == 0) nqueue = 0;
   __syncthreads();
   for (int base = blockIdx.x * GAL_WARPS; base < nelc; base += gridDim.x * GAL_WARPS) {
@@ -469,7 +472,8 @@ __global__ void __launch_bounds__(GAL_THREADS) galerkin_from_ebe_kernel(Grid gf,
         mine |= (bcmask ? bcmask[node_id(gf, ni, nj, nk)] : 0) != 0;
       }
       if (__any_sync(0xffffffffu, mine)) {
-        if (lane == 0) queue[atomicAdd(&nqueue, 1)] = ec;
+        // constrained element: left to galerkin_listed_kernel when the caller lists them, else queued here
+        if (lane == 0 && !listed) queue[atomicAdd(&nqueue, 1)] = ec;
       } else {
         T xc[NN];
 #pragma unroll
@@ -519,7 +523,7 @@ __global__ void __launch_bounds__(GAL_THREADS) galerkin_from_ebe_kernel(Grid gf,
           const int r = e / NDE, c = e % NDE;
           const int rn = r / DIM, rd = r % DIM, cn = c / DIM, cd = c % DIM;
           const bool rb = (cmask[sidx][rn] >> rd) & 1, cb = (cmask[sidx][cn] >> cd) & 1;
-          T v = (rb || cb) ? T(0) : x * K0.v[e];
+          T v = (rb || cb) ? T(0) : x * K0s[e];
           if (r == c && rb) {
             const int ni = fi + (rn & 1), nj = fj + ((rn >> 1) & 1), nk = DIM == 3 ? fk + ((rn >> 2) & 1) : 0;
             const int ai = min(ni, gf.nx - 1), aj = min(nj, gf.ny - 1), ak = DIM == 3 ? min(nk, gf.nz - 1) : 0;
@@ -536,6 +540,73 @@ __global__ void __launch_bounds__(GAL_THREADS) galerkin_from_ebe_kernel(Grid gf,
     if (threadIdx.x == 0) nqueue = 0;
     __syncthreads();
   }
+}
+
+// The coarse elements with a constrained node, listed by the caller (fixed for a problem): one CTA each,
+// spread over the whole GPU.  Unconstrained children from the table, constrained ones by their masked
+// matrix plus bcdiag on the fine Dirichlet dofs assigned to them, transformed by sum factorisation.
+template <typename T, int DIM>
+__global__ void __launch_bounds__(GAL_THREADS) galerkin_listed_kernel(Grid gf, const T* __restrict__ xe,
+                                                                      ElemMat<T, Traits<DIM>::NDE> K0,
+                                                                      const uint8_t* __restrict__ bcmask, T bcdiag,
+                                                                      const T* __restrict__ table,
+                                                                      const int32_t* __restrict__ list,
+                                                                      T* __restrict__ Ec) {
+  constexpr int NN = Traits<DIM>::NN;
+  constexpr int NDE = Traits<DIM>::NDE;
+  constexpr int NE = NDE * NDE;
+  extern __shared__ __align__(16) unsigned char gal_smem[];
+  T* E = reinterpret_cast<T*>(gal_smem);
+  T* Kc = E + NE;
+  T* buf = Kc + NE;
+  T* K0s = buf + NE;
+  __shared__ T xs[NN];
+  __shared__ uint8_t cmask[NN][NN];
+  const Grid gc = gf.coarse();
+  const int ecq = list[blockIdx.x];
+  const int CI = ecq % gc.nx, CJ = (ecq / gc.nx) % gc.ny, CK = ecq / (gc.nx * gc.ny);
+  for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+    K0s[e] = K0.v[e];
+    E[e] = T(0);
+  }
+  for (int q = threadIdx.x; q < NN * NN; q += blockDim.x) {
+    const int sc = q / NN, a = q % NN;
+    const int ni = 2 * CI + (sc & 1) + (a & 1), nj = 2 * CJ + ((sc >> 1) & 1) + ((a >> 1) & 1);
+    const int nk = DIM == 3 ? 2 * CK + ((sc >> 2) & 1) + ((a >> 2) & 1) : 0;
+    cmask[sc][a] = bcmask ? bcmask[node_id(gf, ni, nj, nk)] : 0;
+  }
+  if (threadIdx.x < NN) {
+    const int sc = threadIdx.x;
+    xs[sc] = xe[elem_id(gf, 2 * CI + (sc & 1), 2 * CJ + ((sc >> 1) & 1), DIM == 3 ? 2 * CK + ((sc >> 2) & 1) : 0)];
+  }
+  __syncthreads();
+  for (int sidx = 0; sidx < NN; ++sidx) {
+    const int fi = 2 * CI + (sidx & 1), fj = 2 * CJ + ((sidx >> 1) & 1), fk = DIM == 3 ? 2 * CK + ((sidx >> 2) & 1) : 0;
+    const T x = xs[sidx];
+    bool child_bc = false;
+#pragma unroll
+    for (int a = 0; a < NN; ++a) child_bc |= cmask[sidx][a] != 0;
+    if (!child_bc) {
+      for (int e = threadIdx.x; e < NE; e += blockDim.x) E[e] = fma(x, table[sidx * NE + e], E[e]);
+      __syncthreads();
+      continue;
+    }
+    for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+      const int r = e / NDE, c = e % NDE;
+      const int rn = r / DIM, rd = r % DIM, cn = c / DIM, cd = c % DIM;
+      const bool rb = (cmask[sidx][rn] >> rd) & 1, cb = (cmask[sidx][cn] >> cd) & 1;
+      T v = (rb || cb) ? T(0) : x * K0s[e];
+      if (r == c && rb) {
+        const int ni = fi + (rn & 1), nj = fj + ((rn >> 1) & 1), nk = DIM == 3 ? fk + ((rn >> 2) & 1) : 0;
+        const int ai = min(ni, gf.nx - 1), aj = min(nj, gf.ny - 1), ak = DIM == 3 ? min(nk, gf.nz - 1) : 0;
+        if (ai == fi && aj == fj && ak == fk) v = bcdiag;
+      }
+      Kc[e] = v;
+    }
+    __syncthreads();
+    galerkin_child_accumulate<T, DIM>(E, Kc, buf, sidx);
+  }
+  for (int e = threadIdx.x; e < NE; e += blockDim.x) Ec[(int64_t)ecq * NE + e] = E[e];
 }
 
 // Next-level coarse element matrices from element matrices Ef of grid gf: E_C = sum_c M_c^T E_c M_c, where
@@ -987,7 +1058,9 @@ int pmg_galerkin_table(int dim, const double* K0, double* table) {
 }
 
 int pmg_galerkin_from_ebe(int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
-                          const uint8_t* bcmask, double bcdiag, const void* table, void* Ec, void* stream) {
+                          const uint8_t* bcmask, double bcdiag, const void* table, const int32_t* bc_elems, int n_bc,
+                          void* Ec, void* stream) {
+  if (n_bc < 0 || (n_bc > 0 && !bc_elems)) return PMG_BAD_ARG;
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !even_grid(nelx, nely, nelz) || !xe || !K0_host || !table ||
       !Ec)
     return PMG_BAD_ARG;
@@ -999,16 +1072,28 @@ int pmg_galerkin_from_ebe(int dtype, int nelx, int nely, int nelz, const void* x
   cudaStream_t st = as_stream(stream);
   PMG_DISPATCH(dtype, g.dim(), ([&]() -> int {
                  constexpr int NE = Traits<DIM>::NDE * Traits<DIM>::NDE;
-                 const size_t smem = sizeof(T) * (size_t)(Traits<DIM>::NN + 3) * NE;
+                 const size_t smem = sizeof(T) * (size_t)(Traits<DIM>::NN + 4) * NE;
                  cudaError_t e = cudaFuncSetAttribute(galerkin_from_ebe_kernel<T, DIM>,
                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
                  if (e != cudaSuccess) {
                    set_error(cudaGetErrorString(e));
                    return PMG_CUDA_ERR;
                  }
+                 const auto K = make_elem_mat<T, Traits<DIM>::NDE>(K0_host);
                  galerkin_from_ebe_kernel<T, DIM><<<nblk, GAL_THREADS, smem, st>>>(
-                     g, (const T*)xe, make_elem_mat<T, Traits<DIM>::NDE>(K0_host), bcmask, (T)bcdiag, (const T*)table,
-                     (T*)Ec, coprime_stride(nelc));
+                     g, (const T*)xe, K, bcmask, (T)bcdiag, (const T*)table, (T*)Ec, coprime_stride(nelc),
+                     bc_elems != nullptr);
+                 if (bc_elems && n_bc > 0) {
+                   const size_t smem2 = sizeof(T) * 4 * (size_t)NE;
+                   e = cudaFuncSetAttribute(galerkin_listed_kernel<T, DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem2);
+                   if (e != cudaSuccess) {
+                     set_error(cudaGetErrorString(e));
+                     return PMG_CUDA_ERR;
+                   }
+                   galerkin_listed_kernel<T, DIM><<<n_bc, GAL_THREADS, smem2, st>>>(g, (const T*)xe, K, bcmask, (T)bcdiag,
+                                                                                    (const T*)table, bc_elems, (T*)Ec);
+                 }
                  return check_launch();
                }()));
 }

@@ -261,11 +261,35 @@ class StiffnessOperator:
         nde = (2 ** g.dim) * g.dim
         table = _GalerkinTables.get(self.K0, g.dim, self.code, self.device)
         E = out.E if out is not None else torch.empty((gc.nel, nde * nde), dtype=self.torch_dtype, device=self.device)
+        bl = self._constrained_coarse_elements()
         call("pmg_galerkin_from_ebe", self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0,
-             self.bcmask, self.bcdiag, table, E, stream())
+             self.bcmask, self.bcdiag, table, bl if bl.numel() else None, int(bl.numel()), E, stream())
         if out is not None:
             return out.recompute()
         return StencilOperator(gc, E, self.code)
+
+    def _constrained_coarse_elements(self):
+        """Indices (int32, device) of the coarse elements with a constrained fine node; cached per BC mask."""
+        key = (self.bcmask.data_ptr() if self.bcmask is not None else 0, self.grid.dims)
+        cache = getattr(self, "_bclist", None)
+        if cache is not None and cache[0] == key:
+            return cache[1]
+        g = self.grid
+        gc = g.coarse()
+        if self.bcmask is None:
+            lst = torch.zeros(0, dtype=torch.int32, device=self.device)
+        else:
+            m = (self.bcmask != 0).to(torch.float32)
+            if g.dim == 3:
+                m = m.reshape(1, 1, g.nelz + 1, g.nely + 1, g.nelx + 1)
+                hit = torch.nn.functional.max_pool3d(m, kernel_size=3, stride=2).reshape(-1)
+            else:
+                m = m.reshape(1, 1, g.nely + 1, g.nelx + 1)
+                hit = torch.nn.functional.max_pool2d(m, kernel_size=3, stride=2).reshape(-1)
+            lst = torch.nonzero(hit > 0).reshape(-1).to(torch.int32)
+            assert hit.numel() == gc.nel
+        self._bclist = (key, lst)
+        return lst
 
     def __repr__(self):
         return f"StiffnessOperator({self.grid}, {self.dtype})"

@@ -179,7 +179,13 @@ class DenseCholesky(LinearSolver):
     MAX_DOFS = 20000
     INVERSE_MAX_DOFS = 4096   # FP64: up to this size the solve is one dense product with the explicit inverse
 
-    def __init__(self, A=None):
+    def __init__(self, A=None, lag=False):
+        """lag=True (FP32 operators with the explicit inverse): update() makes the inverse computed in the
+        previous update the active one and computes the inverse of the new matrix for the next update, so the
+        factorisation runs off the critical path (the coarse solve lags the design by one update)."""
+        self.lag = lag
+        self.ready_event = None
+        self._pending = False
         self.L = None
         self.L32 = None
         self.Dinv32 = None
@@ -202,6 +208,20 @@ class DenseCholesky(LinearSolver):
             self.L = torch.empty((n, n), dtype=torch.float64, device=dev)
             self._info = torch.zeros(1, dtype=torch.int32, device=dev)
             self.Ainv = self.L32 = self.Dinv32 = self.Ainv32 = None
+            self._pending = False
+        lagged = self.lag and A.code == F32 and n <= self.INVERSE_MAX_DOFS
+        if lagged:
+            if self.ready_event is None:
+                self.ready_event = torch.cuda.Event()
+            if getattr(self, "Ainv32", None) is None:
+                nbytes = _lib.load().pmg_cholesky_inverse_f32_scratch_bytes(n)
+                self._inv_scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+                self.Ainv32 = torch.empty((n, n), dtype=torch.float32, device=dev)
+                self._Ainv32_next = torch.empty((n, n), dtype=torch.float32, device=dev)
+                self._pending = False
+            if self._pending:
+                self.Ainv32.copy_(self._Ainv32_next)          # the inverse of the previous update's matrix
+                self.ready_event.record()
         L = A.to_dense(out=self.L)
         call("pmg_cholesky_factor", n, L, self.bw, self._info, stream())
         # the pivot check is read back without blocking the host (check() raises once it has arrived), so
@@ -212,6 +232,13 @@ class DenseCholesky(LinearSolver):
         self._info_host.copy_(self._info, non_blocking=True)
         self._info_event.record()
         self._checked = False
+        if lagged:
+            call("pmg_cholesky_inverse_f32", n, L, self.bw, self._inv_scratch, self._Ainv32_next, stream())
+            if not self._pending:                         # first update: no previous inverse to use
+                self.Ainv32.copy_(self._Ainv32_next)
+                self.ready_event.record()
+            self._pending = True
+            return
         if A.code == F64 and n <= self.INVERSE_MAX_DOFS:
             if self.Ainv is None:
                 self.Ainv = torch.empty_like(self.L)
@@ -423,12 +450,14 @@ class GeometricMultigrid(Preconditioner):
 
     @classmethod
     def hierarchy(cls, domain, levels=None, smoother_w=0.5, smooth_steps=5, precision=None, max_coarse_dofs=3000,
-                  coarse_smooth_steps=None, smoother="jacobi", cheb_ratio=10.0):
+                  coarse_smooth_steps=None, smoother="jacobi", cheb_ratio=10.0, coarse_lag=False):
         """Chain of GeometricMultigrid levels as ex_compliance_multigrid.py:108-121 builds it.  With
         levels=None, coarsen while the grid halves evenly and the coarse level has > max_coarse_dofs.
         `coarse_smooth_steps` (default: smooth_steps) applies to every level below the finest.
         smoother="chebyshev" replaces the damped-Jacobi sweeps by a Chebyshev smoother of degree
-        smooth_steps (coarse_smooth_steps below the finest level) on [lmax/cheb_ratio, lmax]."""
+        smooth_steps (coarse_smooth_steps below the finest level) on [lmax/cheb_ratio, lmax].
+        coarse_lag=True: the coarsest direct solve of an FP32 hierarchy uses the inverse of the previous
+        update's coarse matrix while the current one is factorised (see DenseCholesky)."""
         css = smooth_steps if coarse_smooth_steps is None else coarse_smooth_steps
         if smoother not in ("jacobi", "chebyshev"):
             raise ValueError("smoother must be 'jacobi' or 'chebyshev'")
@@ -450,6 +479,8 @@ class GeometricMultigrid(Preconditioner):
                 raise ValueError(f"cannot build {levels} levels: grid {g.dims} does not halve evenly")
             mgs.append(cls(sub, smoother=make(css), smooth_steps=css, precision=precision))
             mgs[-2].inner_level = mgs[-1]
+        if coarse_lag:
+            mgs[-1].inner_level = DenseCholesky(lag=True)
         return mgs
 
 
@@ -685,8 +716,13 @@ class MixedPrecisionCG(LinearSolver):
             else:
                 self.A32 = A.astype(F32)
         # joined just before the first preconditioner application of the next solve, so the FP64 work that
-        # precedes it (initial residual, warm-start products) also overlaps the hierarchy set-up
-        self._side_pending = side
+        # precedes it (initial residual, warm-start products) also overlaps the hierarchy set-up; with a lagged
+        # coarsest solve only up to the event that marks the hierarchy ready (its factorisation keeps running)
+        lv = self.preconditioner
+        while isinstance(lv, GeometricMultigrid):
+            lv = lv.inner_level
+        ev = getattr(lv, "ready_event", None) if isinstance(lv, DenseCholesky) and lv.lag else None
+        self._side_pending = ev if ev is not None else side
         self._fallback_ready = False
         n, dev = self.A64.grid.ndof, self.A64.device
         if getattr(self, "_r32", None) is None or self._r32.numel() != n or self._r32.device != dev:
@@ -799,7 +835,10 @@ class MixedPrecisionCG(LinearSolver):
     def _join_setup(self):
         side = getattr(self, "_side_pending", None)
         if side is not None:
-            torch.cuda.current_stream().wait_stream(side)
+            if isinstance(side, torch.cuda.Event):
+                torch.cuda.current_stream().wait_event(side)
+            else:
+                torch.cuda.current_stream().wait_stream(side)
             self._side_pending = None
 
     def _run_step(self, slot):
