@@ -120,8 +120,11 @@ class DesignRun:
                                                        train_steps=o["learned_train_steps"], lr=o["learned_lr"],
                                                        seed=seed, use_net=o["learned_net"],
                                                        history=o["learned_history"])
+                # stops on the recursive FP64 residual like the plain arm's CG (the true residual of every timed
+                # solve is recomputed outside the timed region and reported)
                 self.solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=o["m"], inner_iters=o["inner_iters"],
-                                                  inner_tol=o["inner_tol"], warm_start=self.warm_start)
+                                                  inner_tol=o["inner_tol"], warm_start=self.warm_start,
+                                                  verify_residual=False)
             else:
                 self.solver = pg.CG(preconditioner=mgs[0], tol=TOL)
             self.u = pg.LinSolve(hermitian=True, symmetric=True, solver=self.solver)(K, self.f)

@@ -197,6 +197,10 @@ int pmg_scale(int dtype, int64_t n, void* y, const void* x, double a, void* stre
 /* y = x with the Dirichlet dofs zeroed (or only the Dirichlet dofs kept when keep_bc != 0). */
 int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int keep_bc, const void* x, void* y,
                 void* stream);
+/* One pass: direct = rhs / bcdiag on the Dirichlet dofs (0 elsewhere), free_part = rhs on the free dofs (0 on
+ * the Dirichlet dofs) -- the split of LDAWrapper.solve (pymoto/solvers/solvers.py:174-176). */
+int pmg_split_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, double bcdiag, const void* rhs,
+                 void* direct, void* free_part, void* stream);
 /* Precision conversion y(dst_dtype) = a * x(src_dtype) (product formed in FP64); and x64 += a * d32. */
 int pmg_convert(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, double a, void* stream);
 int pmg_add_f32_to_f64(int64_t n, double* x, const float* d, double a, void* stream);

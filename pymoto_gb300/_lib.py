@@ -62,6 +62,7 @@ SIGNATURES = {
     "pmg_scale_rsqrt": (I, [I, L, P, P, P, P]),
     "pmg_scale": (I, [I, L, P, P, D, P]),
     "pmg_mask_bc": (I, [I, I, L, P, I, P, P, P]),
+    "pmg_split_bc": (I, [I, I, L, P, D, P, P, P, P]),
     "pmg_convert": (I, [I, I, L, P, P, D, P]),
     "pmg_add_f32_to_f64": (I, [L, P, P, D, P]),
     "pmg_convert_dscale": (I, [I, I, L, P, P, P, I, P]),

@@ -1,6 +1,7 @@
 // Design-variable kernels: density filters and their adjoints, SIMP, the adjoint sensitivity contraction
 // and the optimality-criteria update.  All FP64 (these streams are small next to the solve).
 #include <algorithm>
+#include <cmath>
 
 #include "common.cuh"
 
@@ -245,12 +246,16 @@ __global__ void sens_mixed_kernel(Grid g, ElemMat<float, Traits<DIM>::NDE> K0, c
 // each bisection step costs one multiply and a clip per element (the two forms differ in the last bits).
 constexpr int OC_THREADS = 256;
 constexpr int OC_MAX_BLOCKS = 1024;
+constexpr int OC_TREE = 5;                      // bisection levels resolved per pass of the single launch
+constexpr int OC_CAND = (1 << OC_TREE) - 1;     // midpoints of a depth-5 bisection tree
 struct OCScratch {
   double partial[OC_MAX_BLOCKS];
   double l1, l2, lmid, lmid_last;
   unsigned int ticket;
   unsigned int generation, error;           // release counter and error flag of the single-launch bisection
-  unsigned int arrived[OC_MAX_BLOCKS];      // per-CTA step counters (arrival flags, no shared atomics)
+  unsigned int arrived[OC_MAX_BLOCKS];      // per-CTA pass counters (arrival flags, no shared atomics)
+  int steps_left, exact;                    // bisection steps still to take; next pass evaluates lmid in FP64
+  double cpartial[OC_MAX_BLOCKS][OC_CAND];  // per-CTA sums of the candidates of a pass
 };
 
 __device__ __forceinline__ double oc_warp_sum(double v) {
@@ -274,7 +279,7 @@ __device__ double oc_block_sum(double v) {
   return t;
 }
 
-__global__ void oc_init_kernel(OCScratch* s, double l1, double l2) {
+__global__ void oc_init_kernel(OCScratch* s, double l1, double l2, int steps) {
   for (int b = threadIdx.x; b < OC_MAX_BLOCKS; b += blockDim.x) s->arrived[b] = 0u;
   if (threadIdx.x == 0) {
     s->l1 = l1;
@@ -284,6 +289,8 @@ __global__ void oc_init_kernel(OCScratch* s, double l1, double l2) {
     s->ticket = 0u;
     s->generation = 0u;
     s->error = 0u;
+    s->steps_left = steps;
+    s->exact = 0;
   }
 }
 
@@ -338,57 +345,122 @@ __global__ void __launch_bounds__(OC_THREADS) oc_step_kernel(int64_t n, const do
   }
 }
 
-// All bisection steps in one cooperative launch (every CTA resident): each thread keeps its elements in
-// registers (x, x sqrt(-dg), lower and upper bound).  Per step every CTA writes its partial volume and then
-// its step counter; CTA 0 waits for all counters (one thread per CTA), sums the partials in CTA order,
-// updates the interval exactly as oc_step_kernel and publishes the step through a generation counter that
-// the other CTAs wait for.  No shared-address atomics; every wait is bounded: after OC_SPIN_LIMIT polls the
-// kernel sets s->error and returns.  Finally xnew = the design of the last step.
+// All bisection steps in one cooperative launch (every CTA resident), with the decisions of the sequential
+// bisection reproduced exactly but several taken per grid-wide exchange.  A pass evaluates the volume at the
+// 31 midpoints of the next 5 bisection levels (each midpoint formed by the same repeated 0.5 (a + b) as the
+// sequential loop) in FP32, from FP32 copies of x sqrt(-dg) and the bounds kept in registers; a decision is
+// taken from that value only when it is farther from the target than `margin`, a bound of the FP32 error of
+// the sum; the first undecided midpoint is evaluated in FP64 in the next pass, exactly as oc_step_kernel does.
+// Each pass: every CTA writes its partial sums and then its pass counter; CTA 0 waits for all counters, walks
+// the tree and publishes the new state through a generation counter.  No shared-address atomics; every wait is
+// bounded: after OC_SPIN_LIMIT polls the kernel sets s->error and returns.  Finally xnew = the design of the
+// last step, in FP64.
 constexpr int OCP_PER_THREAD = 8;
 constexpr unsigned OC_SPIN_LIMIT = 1u << 24;   // polls of about 0.1-0.5 us each: a few seconds at most
+
+__device__ __forceinline__ double oc_exact_value(double xi, double gi, double sc, double move, double xmin,
+                                                 double xmax) {
+  const double g = gi < 0.0 ? gi : 0.0;
+  const double lb = fmax(xmin, xi - move), ub = fmin(xmax, xi + move);
+  return fmin(fmax(xi * sqrt(-g) * sc, lb), ub);
+}
 
 __global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, const double* __restrict__ x,
                                                                    const double* __restrict__ dg,
                                                                    double* __restrict__ xnew, double target,
-                                                                   double move, double xmin, double xmax, int steps,
-                                                                   OCScratch* s) {
+                                                                   double move, double xmin, double xmax,
+                                                                   double margin, OCScratch* s) {
+  __shared__ double s_lm[OC_CAND];
+  __shared__ float s_sc[OC_CAND];
+  __shared__ double s_red[OC_CAND];
+  __shared__ int s_abort, s_mode, s_depth;
   __shared__ double s_lmid;
-  __shared__ int s_abort;
   volatile OCScratch* vs = (volatile OCScratch*)s;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double tv[OCP_PER_THREAD], lo[OCP_PER_THREAD], hi[OCP_PER_THREAD];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float t32[OCP_PER_THREAD], lo32[OCP_PER_THREAD], hi32[OCP_PER_THREAD];
 #pragma unroll
   for (int k = 0; k < OCP_PER_THREAD; ++k) {
     const int64_t i = i0 + k * stride;
     if (i < n) {
       const double g = dg[i] < 0.0 ? dg[i] : 0.0;
       const double xv = x[i];
-      tv[k] = xv * sqrt(-g);
-      lo[k] = fmax(xmin, xv - move);
-      hi[k] = fmin(xmax, xv + move);
+      t32[k] = (float)(xv * sqrt(-g));
+      lo32[k] = (float)fmax(xmin, xv - move);
+      hi32[k] = (float)fmin(xmax, xv + move);
     } else {
-      tv[k] = lo[k] = hi[k] = 0.0;
+      t32[k] = lo32[k] = hi32[k] = 0.f;
     }
   }
   if (threadIdx.x == 0) s_abort = 0;
-  for (int step = 0; step < steps; ++step) {
-    if (threadIdx.x == 0) s_lmid = vs->lmid;
-    __syncthreads();
-    const double sc = 1.0 / sqrt(s_lmid);
-    double acc = 0.0;
-#pragma unroll
-    for (int k = 0; k < OCP_PER_THREAD; ++k)
-      if (i0 + k * stride < n) acc += fmin(fmax(tv[k] * sc, lo[k]), hi[k]);
-    acc = oc_block_sum(acc);
-    const unsigned gen = (unsigned)(step + 1);
+  for (unsigned gen = 1;; ++gen) {
     if (threadIdx.x == 0) {
-      vs->partial[blockIdx.x] = acc;
+      const int left = vs->steps_left;
+      s_mode = left <= 0 ? -1 : vs->exact;
+      s_depth = left < OC_TREE ? left : OC_TREE;
+      s_lmid = vs->lmid;
+    }
+    __syncthreads();
+    const int mode = s_mode;
+    if (mode < 0) break;
+    if (mode == 0) {
+      // candidate midpoints: node j of level d (j = 2^d - 1 + m) follows the bits of m from the root
+      const int ncand = (1 << s_depth) - 1;
+      if (threadIdx.x < ncand) {
+        const int j = threadIdx.x;
+        int d = 0;
+        while ((2 << d) - 1 <= j) ++d;
+        const int m = j - ((1 << d) - 1);
+        double a = vs->l1, b = vs->l2;
+        for (int q = d - 1; q >= 0; --q) {
+          const double mid = 0.5 * (a + b);
+          if ((m >> q) & 1) a = mid; else b = mid;
+        }
+        const double lm = 0.5 * (a + b);
+        s_lm[j] = lm;
+        s_sc[j] = (float)(1.0 / sqrt(lm));
+      }
+      __syncthreads();
+      float acc[OC_CAND];
+#pragma unroll
+      for (int j = 0; j < OC_CAND; ++j) acc[j] = 0.f;
+#pragma unroll
+      for (int k = 0; k < OCP_PER_THREAD; ++k) {
+#pragma unroll
+        for (int j = 0; j < OC_CAND; ++j) acc[j] += fminf(fmaxf(t32[k] * s_sc[j], lo32[k]), hi32[k]);
+      }
+      // block sums in FP64: warp shuffles, then the warps in order
+      __shared__ double s_wsum[OC_THREADS / 32][OC_CAND];
+#pragma unroll
+      for (int j = 0; j < OC_CAND; ++j) {
+        const double v = oc_warp_sum((double)acc[j]);
+        if (lane == 0) s_wsum[warp][j] = v;
+      }
+      __syncthreads();
+      if (threadIdx.x < ncand) {
+        double v = 0.0;
+#pragma unroll
+        for (int w = 0; w < OC_THREADS / 32; ++w) v += s_wsum[w][threadIdx.x];
+        vs->cpartial[blockIdx.x][threadIdx.x] = v;
+      }
+    } else {
+      const double sc = 1.0 / sqrt(s_lmid);
+      double acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < OCP_PER_THREAD; ++k) {
+        const int64_t i = i0 + k * stride;
+        if (i < n) acc += oc_exact_value(x[i], dg[i], sc, move, xmin, xmax);
+      }
+      acc = oc_block_sum(acc);
+      if (threadIdx.x == 0) vs->partial[blockIdx.x] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
       __threadfence();
       vs->arrived[blockIdx.x] = gen;
     }
     if (blockIdx.x == 0) {
-      // wait for every CTA (one polling thread per CTA), then decide
       for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
         unsigned polls = 0;
         while (vs->arrived[b] < gen) {
@@ -401,19 +473,59 @@ __global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, co
       }
       __syncthreads();
       __threadfence();
-      double tot = 0.0;
-      for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) tot += vs->partial[b];
-      tot = oc_block_sum(tot);
-      if (threadIdx.x == 0) {
-        const double lmid = vs->lmid;
-        if (tot - target > 0.0)
-          vs->l1 = lmid;
-        else
-          vs->l2 = lmid;
-        vs->lmid_last = lmid;
-        vs->lmid = 0.5 * (vs->l1 + vs->l2);
-        __threadfence();
-        vs->generation = gen;
+      if (mode == 0) {
+        const int ncand = (1 << s_depth) - 1;
+        // totals of the candidates, one warp per candidate (CTA order within the lanes' strided sums)
+        for (int j = warp; j < ncand; j += OC_THREADS / 32) {
+          double v = 0.0;
+          for (int b = lane; b < (int)gridDim.x; b += 32) v += vs->cpartial[b][j];
+          v = oc_warp_sum(v);
+          if (lane == 0) s_red[j] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double a = vs->l1, b = vs->l2;
+          int j = 0, left = vs->steps_left, exact = 0;
+          double lmid_last = vs->lmid_last, lmid = vs->lmid;
+          for (int d = 0; d < s_depth; ++d) {
+            const double lm = s_lm[j], diff = s_red[j] - target;
+            if (!(fabs(diff) > margin)) {   // too close to call in FP32: evaluate this midpoint in FP64
+              exact = 1;
+              lmid = lm;
+              break;
+            }
+            const bool up = diff > 0.0;
+            if (up) a = lm; else b = lm;
+            lmid_last = lm;
+            --left;
+            j = 2 * j + 1 + (up ? 1 : 0);
+          }
+          vs->l1 = a;
+          vs->l2 = b;
+          vs->lmid_last = lmid_last;
+          vs->lmid = exact ? lmid : 0.5 * (a + b);
+          vs->steps_left = left;
+          vs->exact = exact;
+          __threadfence();
+          vs->generation = gen;
+        }
+      } else {
+        double tot = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) tot += vs->partial[b];
+        tot = oc_block_sum(tot);
+        if (threadIdx.x == 0) {
+          const double lmid = vs->lmid;
+          if (tot - target > 0.0)
+            vs->l1 = lmid;
+          else
+            vs->l2 = lmid;
+          vs->lmid_last = lmid;
+          vs->lmid = 0.5 * (vs->l1 + vs->l2);
+          vs->steps_left = vs->steps_left - 1;
+          vs->exact = 0;
+          __threadfence();
+          vs->generation = gen;
+        }
       }
     } else if (threadIdx.x == 0) {
       unsigned polls = 0;
@@ -433,7 +545,7 @@ __global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, co
 #pragma unroll
   for (int k = 0; k < OCP_PER_THREAD; ++k) {
     const int64_t i = i0 + k * stride;
-    if (i < n) xnew[i] = fmin(fmax(tv[k] * sc, lo[k]), hi[k]);
+    if (i < n) xnew[i] = oc_exact_value(x[i], dg[i], sc, move, xmin, xmax);
   }
 }
 
@@ -569,7 +681,7 @@ int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, do
     a = 0.5 * (a + b);  // only the interval width matters for the count
     if (++steps > 200) return PMG_BAD_ARG;
   }
-  oc_init_kernel<<<1, 256, 0, st>>>(s, l1, l2);
+  oc_init_kernel<<<1, 256, 0, st>>>(s, l1, l2, steps);
   // single cooperative launch when every element fits in the registers of co-resident CTAs
   static int coop_blocks[64] = {0};
   int dev = 0;
@@ -584,8 +696,14 @@ int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, do
     const int cb = coop_blocks[dev];
     if (cb > 0 && n <= (int64_t)cb * OC_THREADS * OCP_PER_THREAD) {
       const int grid = cb;   // all co-resident slots: the fewest elements per thread
+      // bound of the FP32 error of a candidate volume: per element 3 roundings of a value up to M, plus the
+      // FP32 sum of at most OCP_PER_THREAD values per thread (each addition off by <= u32 * OCP_PER_THREAD * M,
+      // at most one addition per element; the sums over threads are FP64); doubled for safety
+      const double M = std::max({1.0, std::fabs(xmin), std::fabs(xmax)});
+      const double u32 = std::ldexp(1.0, -24);
+      const double margin = 2.0 * (3.0 + OCP_PER_THREAD) * (double)n * u32 * M;
       void* args[] = {(void*)&n, (void*)&x, (void*)&dg, (void*)&xnew, (void*)&target, (void*)&move,
-                      (void*)&xmin, (void*)&xmax, (void*)&steps, (void*)&s};
+                      (void*)&xmin, (void*)&xmax, (void*)&margin, (void*)&s};
       cudaError_t e = cudaLaunchCooperativeKernel((const void*)oc_persistent_kernel, dim3(grid), dim3(OC_THREADS),
                                                   args, 0, st);
       if (e != cudaSuccess) {

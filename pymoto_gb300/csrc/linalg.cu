@@ -176,6 +176,23 @@ __global__ void mask_bc_kernel(int64_t nnodes, const uint8_t* __restrict__ m, in
   }
 }
 
+// Dirichlet split of a right-hand side in one pass: direct = rhs / bcdiag on constrained dofs (0 elsewhere),
+// free = rhs on free dofs (0 on constrained ones).
+template <typename T, int DIM>
+__global__ void split_bc_kernel(int64_t nnodes, const uint8_t* __restrict__ m, T inv_bcdiag, const T* __restrict__ rhs,
+                                T* __restrict__ direct, T* __restrict__ free_part) {
+  for (int64_t nd = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; nd < nnodes; nd += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned mm = m[nd];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const T v = rhs[nd * DIM + d];
+      const bool bc = (mm >> d) & 1u;
+      direct[nd * DIM + d] = bc ? v * inv_bcdiag : T(0);
+      free_part[nd * DIM + d] = bc ? T(0) : v;
+    }
+  }
+}
+
 template <typename S, typename D>
 __global__ void convert_kernel(int64_t n, const S* __restrict__ x, D* __restrict__ y, double a) {
   if (a == 1.0) {
@@ -812,6 +829,30 @@ int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int k
     mask_bc_kernel<float, 3><<<g, 256, 0, st>>>(nnodes, bcmask, keep_bc, (const float*)x, (float*)y);
   else if (dtype == PMG_F32)
     mask_bc_kernel<float, 2><<<g, 256, 0, st>>>(nnodes, bcmask, keep_bc, (const float*)x, (float*)y);
+  else
+    return PMG_BAD_ARG;
+  return check_launch();
+}
+
+int pmg_split_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, double bcdiag, const void* rhs,
+                 void* direct, void* free_part, void* stream) {
+  if (nnodes < 0 || (dim != 2 && dim != 3) || !bcmask || !rhs || !direct || !free_part || !(bcdiag != 0.0))
+    return PMG_BAD_ARG;
+  if (nnodes == 0) return PMG_OK;
+  cudaStream_t st = as_stream(stream);
+  const unsigned g = blocks_for(nnodes, 256);
+  if (dtype == PMG_F64 && dim == 3)
+    split_bc_kernel<double, 3><<<g, 256, 0, st>>>(nnodes, bcmask, 1.0 / bcdiag, (const double*)rhs, (double*)direct,
+                                                 (double*)free_part);
+  else if (dtype == PMG_F64)
+    split_bc_kernel<double, 2><<<g, 256, 0, st>>>(nnodes, bcmask, 1.0 / bcdiag, (const double*)rhs, (double*)direct,
+                                                 (double*)free_part);
+  else if (dtype == PMG_F32 && dim == 3)
+    split_bc_kernel<float, 3><<<g, 256, 0, st>>>(nnodes, bcmask, (float)(1.0 / bcdiag), (const float*)rhs,
+                                                (float*)direct, (float*)free_part);
+  else if (dtype == PMG_F32)
+    split_bc_kernel<float, 2><<<g, 256, 0, st>>>(nnodes, bcmask, (float)(1.0 / bcdiag), (const float*)rhs,
+                                                (float*)direct, (float*)free_part);
   else
     return PMG_BAD_ARG;
   return check_launch();

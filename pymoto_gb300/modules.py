@@ -328,12 +328,9 @@ class LinSolve(Module):
 
     def _split(self, A, rhs):
         """(direct part on Dirichlet dofs, rhs with those dofs zeroed)."""
-        n = A.grid.nnodes
         direct = torch.empty_like(rhs)
-        call("pmg_mask_bc", F64, A.grid.dim, n, A.bcmask, 1, rhs, direct, stream())
-        call("pmg_scale", F64, rhs.numel(), direct, direct, 1.0 / A.bcdiag, stream())
         rl = torch.empty_like(rhs)
-        call("pmg_mask_bc", F64, A.grid.dim, n, A.bcmask, 0, rhs, rl, stream())
+        call("pmg_split_bc", F64, A.grid.dim, A.grid.nnodes, A.bcmask, A.bcdiag, rhs, direct, rl, stream())
         return direct, rl
 
     def _mask(self, A, v):

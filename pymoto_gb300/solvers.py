@@ -679,7 +679,12 @@ class MixedPrecisionCG(LinearSolver):
     """
 
     def __init__(self, A=None, preconditioner=None, tol=1e-6, m=2, inner_iters=0, inner_tol=0.1, maxit=500,
-                 restart=50, verbosity=0, warm_start=None, coarse_correction=None, fallback=True, stall_window=30):
+                 restart=50, verbosity=0, warm_start=None, coarse_correction=None, fallback=True, stall_window=30,
+                 verify_residual=True):
+        """verify_residual: recompute ||f - K u|| explicitly in FP64 once the recursive residual is below tol
+        (and continue if it is not); False stops on the recursive residual like the reference CG
+        (pymoto/solvers/iterative.py:386-390)."""
+        self.verify_residual = verify_residual
         self.preconditioner = preconditioner
         self.fallback = fallback
         self.stall_window = stall_window
@@ -937,6 +942,8 @@ class MixedPrecisionCG(LinearSolver):
                     best, best_it = res, it
                 if not math.isfinite(res):
                     break
+            if not self.verify_residual:
+                break
             # true FP64 residual; continue from it if the recursive residual drifted
             A.apply(RESIDUAL, x, b, out=r)
             call("pmg_dot", F64, n, r, r, s[1:2], ws.reduce, st)
