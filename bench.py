@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--shape", default=None, help="override the grid, e.g. 64x32x32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-breakdown", action="store_true", help="print a per-kernel time table")
-    ap.add_argument("--inner-iters", type=int, default=0, help="FP32 PCG iterations per FCG preconditioning")
+    ap.add_argument("--inner-iters", type=int, default=3, help="FP32 PCG iterations per FCG preconditioning")
     ap.add_argument("--inner-tol", type=float, default=0.1)
     ap.add_argument("--fcg-m", type=int, default=1)
     ap.add_argument("--levels", type=int, default=GPU_LEVELS)
@@ -77,10 +77,10 @@ def cantilever(shape):
 class DesignRun:
     """The network of the workload on the device, for one solver arm."""
 
-    opts = {"inner_iters": 0, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None,
-            "smoother": "chebyshev", "cheb_degree": 2, "cheb_coarse_degree": 3, "cheb_ratio": 10.0,
+    opts = {"inner_iters": 3, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None,
+            "smoother": "chebyshev", "cheb_degree": 1, "cheb_coarse_degree": 3, "cheb_ratio": 10.0,
             "learned_train_steps": 1, "learned_stride": 4, "learned_lr": 2e-3, "learned_net": True,
-            "learned_history": 1, "coarse_lag": False}
+            "learned_history": 1, "coarse_lag": True}
 
     def __init__(self, arm, shape, seed, torch, pg):
         o = DesignRun.opts
@@ -455,11 +455,13 @@ def main():
                 "config": {"workload": f"3D cantilever hex8 {shape[0]}x{shape[1]}x{shape[2]} "
                                        f"({3 * (shape[0] + 1) * (shape[1] + 1) * (shape[2] + 1)} dofs), FilterConv "
                                        f"r=2.5, SIMP p=3, OC move 0.2, rel. residual 1e-6",
-                           "solver": f"FP64 FCG({args.fcg_m}) + FP32 GMG {args.levels} levels (l1-Jacobi "
-                                     f"Chebyshev degree {DesignRun.opts['cheb_degree']}/"
-                                     f"{DesignRun.opts['cheb_coarse_degree']} fine/coarse), FP64 Cholesky coarsest "
-                                     f"with FP32 inverse; plain arm: FP64 CG + FP64 GMG, damped Jacobi w=0.6, "
-                                     f"2 sweeps, FP64 inverse", "learned_warm_start": False,
+                           "solver": f"FP64 FCG({args.fcg_m}) preconditioned by {args.inner_iters} FP32 PCG "
+                                     f"iterations on FP32 GMG {args.levels} levels (l1-Jacobi Chebyshev degree "
+                                     f"{DesignRun.opts['cheb_degree']}/{DesignRun.opts['cheb_coarse_degree']} "
+                                     f"fine/coarse), FP64 Cholesky coarsest with FP32 inverse"
+                                     f"{' (previous inverse until the new one is ready)' if DesignRun.opts['coarse_lag'] else ''}"
+                                     f"; plain arm: FP64 CG + FP64 GMG, damped Jacobi w=0.6, 2 sweeps, FP64 inverse",
+                           "learned_warm_start": False,
                            "learned_warm_start_note": "measured as arms.mixed_learned (network + previous solution "
                                                       "in a Rayleigh-Ritz initial guess); not in the headline",
                            "parallelism": f"replicas x{world}", "l2": "flushed before every step (256 MB write)"},

@@ -112,6 +112,14 @@ int pmg_ebe_stencil(int dtype, int nelx, int nely, int nelz, const void* xe, con
                     const uint8_t* bcmask, double bcdiag, void* S, void* stream);
 /* Dense FP64 matrix (ndof x ndof, row-major) of a stencil operator: the coarsest-level system. */
 int pmg_stencil_to_dense(int dtype, int nelx, int nely, int nelz, const void* S, double* A, void* stream);
+/* The same in a permuted numbering: dof q goes to row/column pos[q] (pos == NULL: natural numbering). */
+int pmg_stencil_to_dense_perm(int dtype, int nelx, int nely, int nelz, const void* S, const int32_t* pos, double* A,
+                              void* stream);
+/* Host-only: band-reducing numbering of the dofs of a grid (the axis with the fewest nodes fastest, the one with
+ * the most slowest) into pos[ndof], and the half bandwidth *bw of a stencil matrix in that numbering.  On the
+ * 9 x 5 x 5-node coarsest grid of a 128 x 64 x 64 hierarchy the band shrinks from 167 to 95, and the banded
+ * Cholesky work (n bw^2 / 2) by 3x. */
+int pmg_coarse_ordering(int nelx, int nely, int nelz, int32_t* pos, int* bw);
 /* Half bandwidth of the dense coarsest matrix of a grid. */
 int pmg_stencil_bandwidth(int nelx, int nely, int nelz);
 
@@ -162,6 +170,9 @@ size_t pmg_cholesky_inverse_f32_scratch_bytes(int n);
 int pmg_cholesky_inverse_f32(int n, const double* L, int bw, void* scratch, float* Ainv, void* stream);
 /* y = A x, dense row-major n x n, FP64 or FP32 storage with FP64 accumulation. */
 int pmg_dense_gemv(int dtype, int n, const void* A, const void* x, void* y, void* stream);
+/* out[i][j] = in[pos[i]][pos[j]] (n x n row-major, f64 or f32): returns a matrix computed in a permuted numbering
+ * (pmg_stencil_to_dense_perm) to the natural one. */
+int pmg_dense_permute(int dtype, int n, const int32_t* pos, const void* in, void* out, void* stream);
 
 /* ---- reductions and vector updates of CG (pymoto/solvers/iterative.py:340-403) -----------------
  * Deterministic single-launch reductions with FP64 accumulation (CTA partials summed in CTA order by the

@@ -37,6 +37,8 @@ SIGNATURES = {
     "pmg_galerkin_from_elements": (I, [I, I, I, I, P, P, P]),
     "pmg_stencil_from_elements": (I, [I, I, I, I, P, P, P]),
     "pmg_stencil_to_dense": (I, [I, I, I, I, P, P, P]),
+    "pmg_stencil_to_dense_perm": (I, [I, I, I, I, P, P, P, P]),
+    "pmg_coarse_ordering": (I, [I, I, I, P, P]),
     "pmg_ebe_stencil": (I, [I, I, I, I, P, P, P, D, P, P]),
     "pmg_stencil_bandwidth": (I, [I, I, I]),
     "pmg_stencil_rowabs": (I, [I, I, I, I, P, P, P]),
@@ -52,6 +54,7 @@ SIGNATURES = {
     "pmg_cholesky_inverse_f32_scratch_bytes": (c_size_t, [I]),
     "pmg_cholesky_inverse_f32": (I, [I, P, I, P, P, P]),
     "pmg_dense_gemv": (I, [I, I, P, P, P, P]),
+    "pmg_dense_permute": (I, [I, I, P, P, P, P]),
     "pmg_reduce_scratch_bytes": (c_size_t, []),
     "pmg_dot": (I, [I, L, P, P, P, P, P]),
     "pmg_dot2": (I, [I, L, P, P, P, P, P, P, P]),
@@ -149,7 +152,8 @@ def _arg(a):
 # kernels launched per call where it is not exactly one (host-only entry points launch none)
 _HOST_ONLY = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_element_stiffness", "pmg_galerkin_table",
               "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth",
-              "pmg_cholesky_inverse_f32_scratch_bytes", "pmg_nn_wgrad_scratch_bytes", "pmg_oc_status"}
+              "pmg_cholesky_inverse_f32_scratch_bytes", "pmg_nn_wgrad_scratch_bytes", "pmg_oc_status",
+              "pmg_coarse_ordering"}
 
 
 def _launches(name, args):

@@ -58,6 +58,19 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
+// Multiprocessor count of the current device (cached per device).
+inline int sm_count() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  if (!cache[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = v > 0 ? v : 1;
+  }
+  return cache[dev];
+}
+
 template <typename T, int NDE>
 inline ElemMat<T, NDE> make_elem_mat(const double* K0) {
   ElemMat<T, NDE> m;

@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
   const int iy_n = tid / nxw, ix_n = tid - iy_n * nxw;
   const bool has_node = tid < nxw * nyw;
   const int64_t node_xy = (int64_t)(j0 + iy_n) * nnx + i0 + ix_n;
-  float ob[3], od[3], ou[3];
+  float ob[3], od[3], ou[3], oc[3];
   uint8_t omask = 0;
   auto node_operands = [&](int t) {
     if (!has_node) return;
@@ -252,6 +252,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
         od[d] = diag[n * 3 + d];
         ou[d] = u[n * 3 + d];
       }
+      if (MODE == 3) oc[d] = ch.step == 0 ? 0.f : ch.d[n * 3 + d];   // the previous step's increment
     }
   };
 
@@ -285,7 +286,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
         y[q] = ou[d] + w * __fdividef(ob[d] - Au, od[d]);
       } else {
         const float Au = fixed ? bcdiag * ou[d] : acc[d];
-        const float dn = (ch.step == 0 ? 0.f : ca * ch.d[q]) + cc * __fdividef(ob[d] - Au, od[d]);
+        const float dn = ca * oc[d] + cc * __fdividef(ob[d] - Au, od[d]);
         ch.d[q] = dn;
         y[q] = ou[d] + dn;
       }

@@ -75,14 +75,45 @@ __device__ __forceinline__ void finish_reduction(double (&v)[NOUT], RedScratch* 
   }
 }
 
-// Two CTAs per SM at most: each thread then reduces ~20 elements of a 1.6M vector in registers and the last
-// CTA sums few partials.
+// Four CTAs per SM at most (grid-stride): each thread reduces ~10 elements of a 1.6M vector in registers, so
+// the FP64 block and grid sums (a warp-wide FP64 add costs 16 cycles of an SM on GB300) stay a small part.
 inline unsigned red_blocks(int64_t n) {
   int64_t b = (n + RED_THREADS * ILP - 1) / (RED_THREADS * ILP);
+  const int64_t cap = std::min<int64_t>(RED_MAX_BLOCKS, 4 * (int64_t)sm_count());
+  if (b > cap) b = cap;
   if (b < 1) b = 1;
-  if (b > RED_MAX_BLOCKS) b = RED_MAX_BLOCKS;
   return (unsigned)b;
 }
+
+// Dot-product accumulators.  FP64 data: one FP64 FMA per element.  FP32 data: no FP64 arithmetic per element
+// (GB300 runs FP64 at 1/64 of the FP32 rate); the product is split exactly into p + e with an FMA and added
+// to an unevaluated sum s + c by Knuth's TwoSum (Ogita, Rump, Oishi, "Accurate sum and dot product", SIAM J.
+// Sci. Comput. 26 (2005), Dot2), which is as accurate as FP64 accumulation of the exact products.  The
+// explicitly rounded intrinsics keep the compiler from contracting the error terms into FMAs.
+template <typename T>
+struct DotAcc;
+
+template <>
+struct DotAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+template <>
+struct DotAcc<float> {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = fmaf(a, b, -p);                  // a b - p, exact
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));   // s + p - t, exact
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, e));
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
 
 // Scalar num/den (times scale) computed once per CTA: an FP64 division per thread is expensive on GB300.
 // A zero denominator gives a zero ratio (no update) instead of inf/nan.
@@ -107,8 +138,9 @@ __device__ __forceinline__ double cta_ratio(const double* num, const double* den
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) dot_kernel(int64_t n, const T* __restrict__ a, const T* __restrict__ b,
                                                          double* out, RedScratch* scr) {
-  double v[1] = {0.0};
-  PMG_ILP_LOOP(n, v[0] = fma((double)a[i], (double)b[i], v[0]))
+  DotAcc<T> acc;
+  PMG_ILP_LOOP(n, acc.add(a[i], b[i]))
+  double v[1] = {acc.value()};
   finish_reduction<1>(v, scr, out);
 }
 
@@ -116,8 +148,9 @@ template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) dot2_kernel(int64_t n, const T* __restrict__ a, const T* __restrict__ b,
                                                           const T* __restrict__ c, const T* __restrict__ d, double* out,
                                                           RedScratch* scr) {
-  double v[2] = {0.0, 0.0};
-  PMG_ILP_LOOP(n, v[0] = fma((double)a[i], (double)b[i], v[0]); v[1] = fma((double)c[i], (double)d[i], v[1]))
+  DotAcc<T> acc0, acc1;
+  PMG_ILP_LOOP(n, acc0.add(a[i], b[i]); acc1.add(c[i], d[i]))
+  double v[2] = {acc0.value(), acc1.value()};
   finish_reduction<2>(v, scr, out);
 }
 
@@ -127,8 +160,9 @@ __global__ void __launch_bounds__(RED_THREADS) cg_update_kernel(int64_t n, T* __
                                                                const double* num, const double* den, double* rr,
                                                                RedScratch* scr) {
   const T a = (T)cta_ratio(num, den, 1.0);
-  double v[1] = {0.0};
-  PMG_ILP_LOOP(n, x[i] = x[i] + p[i] * a; const T ri = r[i] - q[i] * a; r[i] = ri; v[0] = fma((double)ri, (double)ri, v[0]))
+  DotAcc<T> acc;
+  PMG_ILP_LOOP(n, x[i] = x[i] + p[i] * a; const T ri = r[i] - q[i] * a; r[i] = ri; acc.add(ri, ri))
+  double v[1] = {acc.value()};
   finish_reduction<1>(v, scr, rr);
 }
 
@@ -151,9 +185,15 @@ __global__ void scale_rsqrt_kernel(int64_t n, T* __restrict__ y, const T* __rest
   __shared__ double s_inv;
   if (threadIdx.x == 0) s_inv = nrm2[0] > 0.0 ? 1.0 / sqrt(nrm2[0]) : 0.0;
   __syncthreads();
-  const double s = s_inv;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = (T)((double)x[i] * s);
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, step = (int64_t)gridDim.x * blockDim.x;
+  if (sizeof(T) == 4 && s_inv < 1e37) {
+    // FP32 data with a representable scale: rounded once, no FP64 arithmetic per element
+    const T s = (T)s_inv;
+    for (int64_t i = i0; i < n; i += step) y[i] = x[i] * s;
+  } else {
+    const double s = s_inv;
+    for (int64_t i = i0; i < n; i += step) y[i] = (T)((double)x[i] * s);
+  }
 }
 
 template <typename T>
@@ -269,18 +309,21 @@ inline unsigned stream_blocks(int64_t n) {
   return (unsigned)b;
 }
 
+// out[i][j] = in[pos[i]][pos[j]]: a matrix of a permuted numbering back in the natural one
+template <typename T>
+__global__ void dense_permute_kernel(int n, const int32_t* __restrict__ pos, const T* __restrict__ in, T* __restrict__ out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * n) return;
+  const int i = (int)(t / n), j = (int)(t - (int64_t)i * n);
+  out[t] = in[(int64_t)pos[i] * n + pos[j]];
+}
+
 // ------------------------------------------------------------------------------------------ Cholesky
 // Right-looking blocked Cholesky (lower, row-major, in place) with TB x TB tiles; tiles entirely outside
 // the band stay zero and are skipped.
 constexpr int TB = 32;
 constexpr int CHOL_SMEM_MAX_N = 20000;  // x of a solve lives in shared memory (<= 160 KB in FP64)
 
-// Diagonal tile kb, factored in shared memory by one CTA with one barrier per column (right-looking, on the
-// unscaled columns: T[r][c] -= T[r][k] T[c][k] / T[k][k]; column c is scaled by 1/sqrt(T[c][c]) at the end).
-// FP64 throughput is the limit here, so every thread owns fixed elements of the lower triangle, numbered
-// column by column: at step k only the elements of columns > k are live, and whole warps drop out as k
-// grows.  The reciprocal pivot of step k+1 is computed once, by the owner of (k+1, k+1), right after its
-// step-k update.  A non-positive pivot is recorded in *info and replaced by 1 so the sweep stays finite.
 // 1/d in FP64 from the FP32 reciprocal by two Newton-Raphson steps r <- r + r (1 - d r) (quadratic
 // convergence: 2^-23 -> 2^-46 -> below FP64 rounding).  Used for the pivots of the factorisation, which
 // lie well inside the FP32 range for stiffness matrices.
@@ -292,68 +335,62 @@ __device__ __forceinline__ double recip_newton(double d) {
 }
 
 constexpr int CHOL_THREADS = 256;
-constexpr int TRI_ELEMS = TB * (TB + 1) / 2;                              // 528
-constexpr int TRI_PER_THREAD = (TRI_ELEMS + CHOL_THREADS - 1) / CHOL_THREADS;   // 3
 
+// Diagonal tile kb, factored in shared memory by one CTA, right-looking in LDL^T form: at step k warp 0 forms
+// the pivot reciprocal and the multipliers l_rk = T[r][k] / d_k of column k, then every thread updates
+// T[r][c] -= l_rk T[c][k] over the live lower triangle (rows and columns > k), which is enumerated in packed
+// order so that all warps but the last are full: one FP64 FMA per live element and no idle issue slots on a
+// GPU whose FP64 rate (1/64 of FP32 on GB300) is the limit here.  The Cholesky factor L_unit sqrt(D) is
+// written at the end, the square roots of all pivots taken together.  A non-positive pivot is recorded in
+// *info and replaced by 1 so the sweep stays finite.
 __global__ void __launch_bounds__(CHOL_THREADS) chol_diag_kernel(int n, double* A, int kb, int* info) {
   __shared__ double T[TB][TB + 1];
-  __shared__ double rinv[TB];
-  __shared__ double rsq[TB];
+  __shared__ double ucol[TB];   // column k before scaling (d_k l_rk)
+  __shared__ double dpiv[TB];
   const int k0 = kb * TB;
   const int nb = min(TB, n - k0);
+  const int lane = threadIdx.x & 31;
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
     const int r = e / TB, c = e % TB;
     T[r][c] = (r < nb && c < nb) ? A[(int64_t)(k0 + r) * n + k0 + c] : (r == c ? 1.0 : 0.0);
   }
-  // owned elements: packed column-major index q -> (r, c), r >= c
-  int er[TRI_PER_THREAD], ec[TRI_PER_THREAD];
-#pragma unroll
-  for (int m = 0; m < TRI_PER_THREAD; ++m) {
-    const int q = threadIdx.x + m * CHOL_THREADS;
-    int c = 0, off = 0;
-    while (c < TB && off + (TB - c) <= q) {   // at most 32 steps, once per kernel
-      off += TB - c;
-      ++c;
-    }
-    ec[m] = q < TRI_ELEMS ? c : -1;
-    er[m] = q < TRI_ELEMS ? c + (q - off) : -1;
-  }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double d = T[0][0];
-    if (!(d > 0.0)) d = 1.0;
-    rinv[0] = recip_newton(d);
-  }
-  __syncthreads();
-  for (int k = 0; k < nb - 1; ++k) {
-    const double rk = rinv[k];
-#pragma unroll
-    for (int m = 0; m < TRI_PER_THREAD; ++m) {
-      const int r = er[m], c = ec[m];
-      if (c > k) {
-        T[r][c] = fma(-T[r][k] * rk, T[c][k], T[r][c]);
-        if (r == k + 1 && c == k + 1) {
-          double d = T[r][c];
-          if (!(d > 0.0)) d = 1.0;
-          rinv[k + 1] = recip_newton(d);
-        }
+  for (int k = 0; k < nb; ++k) {
+    // warp 0: pivot d_k and the multipliers l_rk = T[r][k] / d_k of column k (lane = row)
+    if (threadIdx.x < 32) {
+      double d = T[k][k];
+      if (!(d > 0.0)) {
+        if (lane == 0) atomicCAS(info, 0, k0 + k + 1);
+        d = 1.0;
+      }
+      const double y = recip_newton(d);
+      if (lane == 0) dpiv[k] = d;
+      if (lane > k && lane < nb) {
+        const double u = T[lane][k];
+        ucol[lane] = u;
+        T[lane][k] = u * y;
       }
     }
     __syncthreads();
-  }
-  if (threadIdx.x < nb) {
-    const int c = threadIdx.x;
-    double d = T[c][c];
-    if (!(d > 0.0)) {
-      atomicCAS(info, 0, k0 + c + 1);
-      d = 1.0;
+    // trailing update of the lower triangle (rows and columns k+1 .. nb-1) in packed order, so that every
+    // warp but the last is fully occupied: one FP64 FMA per element
+    const int t = nb - 1 - k;
+    const int m = t * (t + 1) / 2;
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+      int a = (int)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
+      if ((a + 1) * (a + 2) / 2 <= q) ++a;
+      if (a * (a + 1) / 2 > q) --a;
+      const int r = k + 1 + a, c = k + 1 + (q - a * (a + 1) / 2);
+      T[r][c] = fma(-T[r][k], ucol[c], T[r][c]);
     }
-    rsq[c] = rsqrt(d);
+    __syncthreads();
   }
+  // Cholesky factor L = L_unit sqrt(D): column c scaled by sqrt(d_c) (all pivots at once)
+  if (threadIdx.x < TB) dpiv[threadIdx.x] = threadIdx.x < nb ? sqrt(dpiv[threadIdx.x]) : 1.0;
   __syncthreads();
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
     const int r = e / TB, c = e % TB;
-    if (r < nb && c < nb) A[(int64_t)(k0 + r) * n + k0 + c] = c <= r ? T[r][c] * rsq[c] : 0.0;
+    if (r < nb && c < nb) A[(int64_t)(k0 + r) * n + k0 + c] = c < r ? T[r][c] * dpiv[c] : (c == r ? dpiv[c] : 0.0);
   }
 }
 
@@ -964,6 +1001,19 @@ int pmg_cholesky_block_inverses(int dtype, int n, const double* L, void* Dinv, v
     chol_block_inverse_kernel<double><<<nblk, 256, 0, st>>>(n, L, (double*)Dinv);
   else if (dtype == PMG_F32)
     chol_block_inverse_kernel<float><<<nblk, 256, 0, st>>>(n, L, (float*)Dinv);
+  else
+    return PMG_BAD_ARG;
+  return check_launch();
+}
+
+int pmg_dense_permute(int dtype, int n, const int32_t* pos, const void* in, void* out, void* stream) {
+  if (n <= 0 || !pos || !in || !out || in == out) return PMG_BAD_ARG;
+  cudaStream_t st = as_stream(stream);
+  const int64_t nn = (int64_t)n * n;
+  if (dtype == PMG_F64)
+    dense_permute_kernel<double><<<blocks_for(nn, 256), 256, 0, st>>>(n, pos, (const double*)in, (double*)out);
+  else if (dtype == PMG_F32)
+    dense_permute_kernel<float><<<blocks_for(nn, 256), 256, 0, st>>>(n, pos, (const float*)in, (float*)out);
   else
     return PMG_BAD_ARG;
   return check_launch();

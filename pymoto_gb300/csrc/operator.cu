@@ -273,6 +273,74 @@ __global__ void __launch_bounds__(256) stencil_apply_kernel(Grid g, const T* __r
   }
 }
 
+// The same products for small levels, where one thread per row leaves most SMs idle and each thread waits
+// through a long chain of dependent loads: the 3^dim offsets of a row are split over NOFF/3 threads (one
+// x-line of 3 offsets each, so every thread issues its 3 DIM coefficient and 3 DIM value loads at once), and
+// the partial sums are added in a fixed order in shared memory.  Block: 32 rows x NOFF/3 parts x SPLIT_G.
+template <int DIM>
+struct SplitShape {
+  static constexpr int P = Traits<DIM>::NOFF / 3;   // parts per row: 9 (3D), 3 (2D)
+  static constexpr int G = DIM == 3 ? 1 : 3;        // 32-row groups per block
+  static constexpr int THREADS = 32 * P * G;        // 288
+};
+
+template <typename T, int DIM, int MODE>
+__global__ void __launch_bounds__(SplitShape<DIM>::THREADS)
+    stencil_apply_split_kernel(Grid g, const T* __restrict__ S, const T* __restrict__ u, const T* __restrict__ b,
+                               const T* __restrict__ diag, T w, T* __restrict__ y, ChebArgs<T> ch) {
+  constexpr int P = SplitShape<DIM>::P, G = SplitShape<DIM>::G;
+  __shared__ T part[G][P][32];
+  const int nn = (int)g.nnodes();
+  const int lane = threadIdx.x, p = threadIdx.y, grp = threadIdx.z;
+  const int t = (blockIdx.x * G + grp) * 32 + lane;
+  const bool active = t < nn * DIM;
+  const int d = active ? t / nn : 0, n = active ? t - d * nn : 0;
+  const int64_t q = (int64_t)n * DIM + d;
+  T bq = T(0), dq = T(1), uq = T(0), cq = T(0);
+  if (active && p == 0) {   // epilogue operands, in flight together with the products
+    if (MODE >= 1) bq = b[q];
+    if (MODE >= 2) {
+      dq = diag[q];
+      uq = u[q];
+    }
+    if (MODE == 3 && ch.step != 0) cq = ch.d[q];
+  }
+  T acc = T(0);
+  if (active) {
+    int i, j, k;
+    node_ijk(g, n, i, j, k);
+    const int dy = p % 3 - 1, dz = DIM == 3 ? p / 3 - 1 : 0;
+    const int jj = min(max(j + dy, 0), g.ny), kk = min(max(k + dz, 0), g.nz);
+    const int row = (kk * (g.ny + 1) + jj) * (g.nx + 1);
+#pragma unroll
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int o = 3 * p + dx + 1;
+      const int m = row + min(max(i + dx, 0), g.nx);
+      const T* Sd = S + (int64_t)((o * DIM + d) * DIM) * nn + n;
+#pragma unroll
+      for (int c = 0; c < DIM; ++c) acc = fma(Sd[(int64_t)c * nn], u[(int64_t)m * DIM + c], acc);
+    }
+  }
+  part[grp][p][lane] = acc;
+  __syncthreads();
+  if (!active || p != 0) return;
+  acc = T(0);
+#pragma unroll
+  for (int r = 0; r < P; ++r) acc += part[grp][r][lane];
+  if (MODE == 0) {
+    y[q] = acc;
+  } else if (MODE == 1) {
+    y[q] = bq - acc;
+  } else if (MODE == 2) {
+    y[q] = uq + w * ((bq - acc) / dq);
+  } else {
+    const T a = (T)ch.coef[2 * ch.step], c = (T)ch.coef[2 * ch.step + 1];
+    const T dn = a * cq + c * ((bq - acc) / dq);
+    ch.d[q] = dn;
+    y[q] = uq + dn;
+  }
+}
+
 template <typename T, int DIM>
 __global__ void stencil_diag_kernel(Grid g, const T* __restrict__ S, T* __restrict__ diag) {
   constexpr int C = DIM == 3 ? 13 : 4;
@@ -789,7 +857,8 @@ __global__ void ebe_stencil_kernel(Grid g, const T* __restrict__ xe, ElemMat<T, 
 }
 
 template <typename T, int DIM>
-__global__ void stencil_to_dense_kernel(Grid g, const T* __restrict__ S, double* __restrict__ A) {
+__global__ void stencil_to_dense_kernel(Grid g, const T* __restrict__ S, const int32_t* __restrict__ pos,
+                                        double* __restrict__ A) {
   constexpr int NOFF = Traits<DIM>::NOFF;
   const int64_t nn = g.nnodes();
   const int64_t ndof = nn * DIM;
@@ -805,8 +874,10 @@ __global__ void stencil_to_dense_kernel(Grid g, const T* __restrict__ S, double*
 #pragma unroll
   for (int d = 0; d < DIM; ++d)
 #pragma unroll
-    for (int c = 0; c < DIM; ++c)
-      A[(n * DIM + d) * ndof + m * DIM + c] = (double)S[((int64_t)(o * DIM + d) * DIM + c) * nn + n];
+    for (int c = 0; c < DIM; ++c) {
+      const int64_t row = pos ? pos[n * DIM + d] : n * DIM + d, col = pos ? pos[m * DIM + c] : m * DIM + c;
+      A[row * ndof + col] = (double)S[((int64_t)(o * DIM + d) * DIM + c) * nn + n];
+    }
 }
 
 __global__ void dofconn_kernel(Grid g, int64_t* __restrict__ dc) {
@@ -861,16 +932,34 @@ int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_
   return check_launch();
 }
 
+// Levels with at most this many rows use the split-row kernel.
+constexpr int64_t SPLIT_MAX_ROWS = int64_t(1) << 16;
+
 template <typename T, int DIM>
 int stencil_apply_t(int mode, Grid g, const void* S, const void* u, const void* b, const void* diag, double w,
                     void* y, cudaStream_t st, ChebArgs<T> ch = ChebArgs<T>{nullptr, nullptr, 0}) {
   const int threads = 256;
-  const unsigned blocks = blocks_for(g.nnodes() * DIM, threads);
+  const int64_t rows = g.nnodes() * DIM;
+  const unsigned blocks = blocks_for(rows, threads);
   const T* S_ = (const T*)S;
   const T* u_ = (const T*)u;
   const T* b_ = (const T*)b;
   const T* d_ = (const T*)diag;
   T* y_ = (T*)y;
+  if (rows <= SPLIT_MAX_ROWS) {
+    using SS = SplitShape<DIM>;
+    const dim3 blk(32, SS::P, SS::G);
+    const unsigned nb = blocks_for(rows, 32 * SS::G);
+    if (mode == PMG_APPLY_MATVEC)
+      stencil_apply_split_kernel<T, DIM, 0><<<nb, blk, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    else if (mode == PMG_APPLY_RESIDUAL)
+      stencil_apply_split_kernel<T, DIM, 1><<<nb, blk, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    else if (mode == PMG_APPLY_JACOBI)
+      stencil_apply_split_kernel<T, DIM, 2><<<nb, blk, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    else
+      stencil_apply_split_kernel<T, DIM, 3><<<nb, blk, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    return check_launch();
+  }
   if (mode == PMG_APPLY_MATVEC)
     stencil_apply_kernel<T, DIM, 0><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
   else if (mode == PMG_APPLY_RESIDUAL)
@@ -1140,6 +1229,11 @@ int pmg_ebe_stencil(int dtype, int nelx, int nely, int nelz, const void* xe, con
 }
 
 int pmg_stencil_to_dense(int dtype, int nelx, int nely, int nelz, const void* S, double* A, void* stream) {
+  return pmg_stencil_to_dense_perm(dtype, nelx, nely, nelz, S, nullptr, A, stream);
+}
+
+int pmg_stencil_to_dense_perm(int dtype, int nelx, int nely, int nelz, const void* S, const int32_t* pos, double* A,
+                              void* stream) {
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !S || !A) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
   const int64_t ndof = g.nnodes() * g.dim();
@@ -1152,7 +1246,31 @@ int pmg_stencil_to_dense(int dtype, int nelx, int nely, int nelz, const void* S,
   }
   const int64_t work = g.nnodes() * (g.dim() == 3 ? 27 : 9);
   PMG_DISPATCH(dtype, g.dim(),
-               (launch_simple<T, DIM>(stencil_to_dense_kernel<T, DIM>, work, st, g, (const T*)S, A)));
+               (launch_simple<T, DIM>(stencil_to_dense_kernel<T, DIM>, work, st, g, (const T*)S, pos, A)));
+}
+
+int pmg_coarse_ordering(int nelx, int nely, int nelz, int32_t* pos, int* bw) {
+  if (!grid_ok(nelx, nely, nelz) || !pos || !bw) return PMG_BAD_ARG;
+  const int dim = nelz == 0 ? 2 : 3;
+  const int cnt[3] = {nelx + 1, nely + 1, dim == 3 ? nelz + 1 : 1};
+  // axes by node count, fewest first (fastest): a band of (count0 * count1 + count0 + 1) nodes
+  int ax[3] = {0, 1, 2};
+  for (int a = 0; a < dim; ++a)
+    for (int b = a + 1; b < dim; ++b)
+      if (cnt[ax[b]] < cnt[ax[a]]) std::swap(ax[a], ax[b]);
+  const int c0 = cnt[ax[0]], c1 = cnt[ax[1]];
+  int idx[3];
+  for (idx[2] = 0; idx[2] < cnt[2]; ++idx[2])
+    for (idx[1] = 0; idx[1] < cnt[1]; ++idx[1])
+      for (idx[0] = 0; idx[0] < cnt[0]; ++idx[0]) {
+        const int64_t nat = ((int64_t)idx[2] * cnt[1] + idx[1]) * cnt[0] + idx[0];
+        const int64_t p = dim == 3 ? ((int64_t)idx[ax[2]] * c1 + idx[ax[1]]) * c0 + idx[ax[0]]
+                                   : (int64_t)idx[ax[1]] * c0 + idx[ax[0]];
+        for (int d = 0; d < dim; ++d) pos[nat * dim + d] = (int32_t)(p * dim + d);
+      }
+  const int64_t dn = 1 + c0 + (dim == 3 ? (int64_t)c0 * c1 : 0);
+  *bw = (int)(dn * dim + dim - 1);
+  return PMG_OK;
 }
 
 int pmg_stencil_bandwidth(int nelx, int nely, int nelz) {

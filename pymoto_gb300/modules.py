@@ -345,30 +345,34 @@ class LinSolve(Module):
         n = rhs.numel()
         sol, rl = self._split(A, rhs)
         sc = torch.zeros(4, dtype=torch.float64, device=rhs.device)
+        # projection coefficients stay on the device (num / den, zero for a zero pair): no host round trip
         for xs, bs in self._pairs:   # modified Gram-Schmidt projection on the stored pairs
             call("pmg_dot2", F64, n, rl, bs, bs, bs, sc[0:1], ws.reduce, st)
-            alpha = (sc[0] / sc[1])
-            rl.sub_(alpha * bs)
-            sol.add_(alpha * xs)
-        # residual of the projection: the stored pairs satisfy b_s = A x_s, so rhs - A sol is exactly the
-        # projected right-hand side rl (no operator product needed)
-        call("pmg_dot2", F64, n, rl, rl, rhs, rhs, sc[2:3], ws.reduce, st)
-        rn, bn = sc[2:4].sqrt().tolist()
-        rtol = rn / (bn if bn != 0 else 1.0)
-        self.last_rtol = rtol
-        if rtol <= self.lda_tol:
-            return sol
+            call("pmg_axpy_ratio", F64, n, rl, bs, sc[0:1], sc[1:2], -1.0, st)
+            call("pmg_axpy_ratio", F64, n, sol, xs, sc[0:1], sc[1:2], 1.0, st)
+        self.last_rtol = None
+        if self._pairs:
+            # residual of the projection: the stored pairs satisfy b_s = A x_s, so rhs - A sol is exactly the
+            # projected right-hand side rl (no operator product needed).  Without stored pairs the solver's own
+            # initial residual test decides.
+            call("pmg_dot2", F64, n, rl, rl, rhs, rhs, sc[2:3], ws.reduce, st)
+            rn, bn = sc[2:4].sqrt().tolist()
+            rtol = rn / (bn if bn != 0 else 1.0)
+            self.last_rtol = rtol
+            if rtol <= self.lda_tol:
+                return sol
         x0l = None
         if x0 is not None:
             x0l = self._mask(A, x0)
             for xs, _ in self._pairs:
                 call("pmg_dot2", F64, n, x0l, xs, xs, xs, sc[0:1], ws.reduce, st)
-                x0l.sub_((sc[0] / sc[1]) * xs)
+                call("pmg_axpy_ratio", F64, n, x0l, xs, sc[0:1], sc[1:2], -1.0, st)
         xnew = self.solver.solve(rl, x0=x0l)
         xnew = self._mask(A, xnew)
         sol.add_(xnew)
-        # store the new (x, A x) pair, orthogonalised against the stored ones and normalised; a solver that
-        # finished with an explicit FP64 residual r = rl - A xnew gives A xnew = rl - r without a product
+        # store the new (x, A x) pair, orthogonalised against the stored ones and normalised on the device; a
+        # solver that finished with an explicit FP64 residual r = rl - A xnew gives A xnew = rl - r without a
+        # product
         r_fin = getattr(self.solver, "final_residual", None)
         if r_fin is not None and r_fin.shape == rl.shape and r_fin.dtype == rl.dtype:
             ba = self._mask(A, rl - r_fin)
@@ -377,13 +381,13 @@ class LinSolve(Module):
         xa = xnew
         for xs, bs in self._pairs:
             call("pmg_dot2", F64, n, ba, bs, bs, bs, sc[0:1], ws.reduce, st)
-            beta = sc[0] / sc[1]
-            ba = ba - beta * bs
-            xa = xa - beta * xs
+            call("pmg_axpy_ratio", F64, n, ba, bs, sc[0:1], sc[1:2], -1.0, st)
+            call("pmg_axpy_ratio", F64, n, xa, xs, sc[0:1], sc[1:2], -1.0, st)
         call("pmg_dot", F64, n, ba, ba, sc[2:3], ws.reduce, st)
-        bnrm = float(sc[2].sqrt().item())
-        if np.isfinite(bnrm) and bnrm != 0.0:
-            self._pairs.append((xa / bnrm, ba / bnrm))
+        xn, bnv = torch.empty_like(xa), torch.empty_like(ba)
+        call("pmg_scale_rsqrt", F64, n, xn, xa, sc[2:3], st)    # zero (a harmless pair) when ||ba|| is 0
+        call("pmg_scale_rsqrt", F64, n, bnv, ba, sc[2:3], st)
+        self._pairs.append((xn, bnv))
         return sol
 
     def __call__(self, mat, rhs):

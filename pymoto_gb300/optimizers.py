@@ -47,13 +47,13 @@ class OC:
         if self.maxvol is None:
             self.maxvol = float(x.sum().item()) / x.numel()
         g = self.calculate_g()
-        dg = _to_device(self.calculate_dg(), device=x.device)[0]
-        xnew = torch.empty_like(x)
         ws = Workspace.get(x.device)
         if getattr(self, "_issued", False):
-            # status of the previous update's bisection (a bounded wait that expired), read after the host has
-            # synchronised on the response anyway
+            # status of the previous update's bisection (a bounded wait that expired): the host has just
+            # synchronised on the response, which the device computed after that update
             call("pmg_oc_status", ws.oc)
+        dg = _to_device(self.calculate_dg(), device=x.device)[0]
+        xnew = torch.empty_like(x)
         call("pmg_oc_update", x.numel(), x, dg, xnew, self.maxvol, self.move, self.xmin, self.xmax, self.l1init,
              self.l2init, self.l1l2tol, ws.oc, stream())
         self._issued = True

@@ -180,9 +180,10 @@ class DenseCholesky(LinearSolver):
     INVERSE_MAX_DOFS = 4096   # FP64: up to this size the solve is one dense product with the explicit inverse
 
     def __init__(self, A=None, lag=False):
-        """lag=True (FP32 operators with the explicit inverse): update() makes the inverse computed in the
-        previous update the active one and computes the inverse of the new matrix for the next update, so the
-        factorisation runs off the critical path (the coarse solve lags the design by one update)."""
+        """lag=True (FP32 operators with the explicit inverse): update() leaves the inverse of the previous
+        update active and factorises the new matrix behind it (on the caller's stream, typically a side
+        stream); promote_if_ready() makes the new inverse the active one as soon as it exists, so the
+        factorisation runs off the critical path and a solver switches to the exact coarse solve mid-solve."""
         self.lag = lag
         self.ready_event = None
         self._pending = False
@@ -193,6 +194,22 @@ class DenseCholesky(LinearSolver):
         self.Ainv32 = None
         super().__init__(A)
 
+    def _ordering(self, A):
+        """Band-reducing dof numbering for the explicit-inverse path (the inverse is returned to the natural
+        numbering, so solves are unchanged); the blocked substitution paths keep the natural numbering."""
+        g = A.grid
+        if self.n > self.INVERSE_MAX_DOFS:
+            return None, A.bandwidth()
+        key = (g.dims, A.device)
+        if getattr(self, "_order_key", None) != key:
+            pos = np.empty(self.n, dtype=np.int32)
+            bw = np.zeros(1, dtype=np.int32)
+            call("pmg_coarse_ordering", g.nelx, g.nely, g.nelz, pos, bw)
+            self._pos = torch.from_numpy(pos).to(A.device)
+            self._order_bw = int(bw[0])
+            self._order_key = key
+        return self._pos, self._order_bw
+
     def update(self, A):
         if not isinstance(A, StencilOperator):
             raise TypeError("DenseCholesky expects a coarse StencilOperator")
@@ -200,8 +217,8 @@ class DenseCholesky(LinearSolver):
         if n > self.MAX_DOFS:
             raise ValueError(f"coarsest level has {n} dofs (> {self.MAX_DOFS}); add multigrid levels")
         self.n = n
-        self.bw = A.bandwidth()
         self.code = A.code
+        pos, self.bw = self._ordering(A)
         dev = A.device
         if self.L is None or self.L.shape[0] != n or self.L.device != dev:
             # device buffers kept across updates (stable addresses for captured CUDA graphs)
@@ -219,10 +236,15 @@ class DenseCholesky(LinearSolver):
                 self.Ainv32 = torch.empty((n, n), dtype=torch.float32, device=dev)
                 self._Ainv32_next = torch.empty((n, n), dtype=torch.float32, device=dev)
                 self._pending = False
-            if self._pending:
-                self.Ainv32.copy_(self._Ainv32_next)          # the inverse of the previous update's matrix
-                self.ready_event.record()
-        L = A.to_dense(out=self.L)
+                self._have_inverse = False
+                self._next_event = None
+            if self._pending:                                 # never promoted: the previous update's inverse
+                self.Ainv32.copy_(self._Ainv32_next)
+                self._pending = False
+            self.ready_event.record()
+        L = self.L
+        g = A.grid
+        call("pmg_stencil_to_dense_perm", A.code, g.nelx, g.nely, g.nelz, A.S, pos, L, stream())
         call("pmg_cholesky_factor", n, L, self.bw, self._info, stream())
         # the pivot check is read back without blocking the host (check() raises once it has arrived), so
         # that the host can queue the next work while the factorisation runs
@@ -233,18 +255,45 @@ class DenseCholesky(LinearSolver):
         self._info_event.record()
         self._checked = False
         if lagged:
-            call("pmg_cholesky_inverse_f32", n, L, self.bw, self._inv_scratch, self._Ainv32_next, stream())
-            if not self._pending:                         # first update: no previous inverse to use
+            self._inverse_f32(self._Ainv32_next)
+            if not self._have_inverse:                    # first update: no previous inverse to use
                 self.Ainv32.copy_(self._Ainv32_next)
                 self.ready_event.record()
+                self._have_inverse = True
+                return
+            if self._next_event is None:
+                self._next_event = torch.cuda.Event()
+            self._next_event.record()
             self._pending = True
             return
         if A.code == F64 and n <= self.INVERSE_MAX_DOFS:
             if self.Ainv is None:
                 self.Ainv = torch.empty_like(self.L)
-            call("pmg_cholesky_inverse", n, L, self.bw, self.Ainv, stream())
+                self._Ainv_perm = torch.empty_like(self.L)
+            call("pmg_cholesky_inverse", n, L, self.bw, self._Ainv_perm, stream())
+            call("pmg_dense_permute", F64, n, self._pos, self._Ainv_perm, self.Ainv, stream())
         elif A.code == F32:
             self._prepare_f32()
+
+    def _inverse_f32(self, out):
+        """FP32 inverse of the (permuted) factor, returned to the natural numbering in `out`."""
+        n = self.n
+        if getattr(self, "_Ainv32_perm", None) is None or self._Ainv32_perm.shape[0] != n:
+            self._Ainv32_perm = torch.empty((n, n), dtype=torch.float32, device=self.L.device)
+        call("pmg_cholesky_inverse_f32", n, self.L, self.bw, self._inv_scratch, self._Ainv32_perm, stream())
+        call("pmg_dense_permute", F32, n, self._pos, self._Ainv32_perm, out, stream())
+
+    def promote_if_ready(self):
+        """Lagged mode: once the factorisation of the latest update has finished (checked without blocking),
+        make its inverse the active one, ordered on the current stream before the solves that follow.
+        Returns True when the active inverse is the current one."""
+        if not self._pending:
+            return True
+        if not self._next_event.query():
+            return False
+        self.Ainv32.copy_(self._Ainv32_next)
+        self._pending = False
+        return True
 
     def check(self):
         """Raise LinAlgError if the last factorisation met a non-positive pivot (waits for the factorisation)."""
@@ -264,7 +313,7 @@ class DenseCholesky(LinearSolver):
                 nbytes = _lib.load().pmg_cholesky_inverse_f32_scratch_bytes(n)
                 self._inv_scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
                 self.Ainv32 = torch.empty((n, n), dtype=torch.float32, device=dev)
-            call("pmg_cholesky_inverse_f32", n, self.L, self.bw, self._inv_scratch, self.Ainv32, stream())
+            self._inverse_f32(self.Ainv32)
             return
         if self.L32 is None:
             self.L32 = torch.empty((n, n), dtype=torch.float32, device=dev)
@@ -456,8 +505,9 @@ class GeometricMultigrid(Preconditioner):
         `coarse_smooth_steps` (default: smooth_steps) applies to every level below the finest.
         smoother="chebyshev" replaces the damped-Jacobi sweeps by a Chebyshev smoother of degree
         smooth_steps (coarse_smooth_steps below the finest level) on [lmax/cheb_ratio, lmax].
-        coarse_lag=True: the coarsest direct solve of an FP32 hierarchy uses the inverse of the previous
-        update's coarse matrix while the current one is factorised (see DenseCholesky)."""
+        coarse_lag=True: the coarsest direct solve of an FP32 hierarchy keeps using the inverse of the previous
+        update's coarse matrix until the current one is factorised (see DenseCholesky; MixedPrecisionCG
+        switches to the new inverse between two iterations as soon as it exists)."""
         css = smooth_steps if coarse_smooth_steps is None else coarse_smooth_steps
         if smoother not in ("jacobi", "chebyshev"):
             raise ValueError("smoother must be 'jacobi' or 'chebyshev'")
@@ -728,6 +778,7 @@ class MixedPrecisionCG(LinearSolver):
             lv = lv.inner_level
         ev = getattr(lv, "ready_event", None) if isinstance(lv, DenseCholesky) and lv.lag else None
         self._side_pending = ev if ev is not None else side
+        self._lagged_coarse = lv if ev is not None else None
         self._fallback_ready = False
         n, dev = self.A64.grid.ndof, self.A64.device
         if getattr(self, "_r32", None) is None or self._r32.numel() != n or self._r32.device != dev:
@@ -936,6 +987,8 @@ class MixedPrecisionCG(LinearSolver):
                 slot = (slot + 1) % B["k"]
                 it += 1
                 res = math.sqrt(max(s[1].item(), 0.0)) / bn
+                if getattr(self, "_lagged_coarse", None) is not None and self._lagged_coarse.promote_if_ready():
+                    self._lagged_coarse = None    # the exact coarse solve of this update from the next step on
                 if self.verbosity >= 2:
                     print(f"FCG it {it}: residual {res:.3e}")
                 if res < 0.5 * best:

@@ -73,6 +73,27 @@ def test_galerkin_table_is_child_transfer_product(dim):
         np.testing.assert_allclose(table[s], M.T @ K0 @ M, rtol=0, atol=1e-14 * np.abs(K0).max())
 
 
+@pytest.mark.parametrize("shape", [(8, 4, 4), (4, 8, 2), (6, 0, 0), (3, 5, 0), (2, 2, 6)])
+def test_coarse_ordering_is_a_band_reducing_permutation(shape):
+    """pmg_coarse_ordering: a permutation of the dofs under which every stencil coupling of the grid (the
+    nonzeros of the coarsest matrix) lies within the reported half bandwidth, at most the natural one."""
+    from pymoto_gb300._lib import call
+    nx, ny, nz = shape
+    if ny == 0:
+        ny = nx
+    g = O.Grid(nx, ny, nz)
+    n = g.nnodes * g.dim
+    pos = np.empty(n, dtype=np.int32)
+    bw = np.zeros(1, dtype=np.int32)
+    call("pmg_coarse_ordering", nx, ny, nz, pos, bw)
+    assert np.array_equal(np.sort(pos), np.arange(n))
+    K = O.assemble(g, O.element_stiffness(g), np.ones(g.nel), np.zeros(0, dtype=np.int64)).tocoo()
+    band = np.abs(pos[K.row] - pos[K.col]).max()
+    assert band <= bw[0] <= call("pmg_stencil_bandwidth", nx, ny, nz)
+    if shape == (8, 4, 4):                    # the coarsest grid of a 128 x 64 x 64 five-level hierarchy
+        assert (call("pmg_stencil_bandwidth", nx, ny, nz), int(bw[0])) == (167, 95)
+
+
 def test_invalid_arguments_fail_before_any_launch():
     from pymoto_gb300._lib import PMGError, call
     with pytest.raises(PMGError) as e:

@@ -76,6 +76,63 @@ def test_fp64_stencil_and_matrix_free_agree(pg, shape):
     np.testing.assert_allclose(js, jm, rtol=1e-12, atol=1e-12 * np.abs(jm).max())
 
 
+@pytest.mark.parametrize("code", ["f64", "f32"])
+def test_stencil_row_and_split_kernels(pg, code):
+    """Stencil products on both sides of the split-row threshold (2^16 rows): the fine level (263,835 rows,
+    one thread per row) against the matrix-free product, and its Galerkin level (35,343 rows, split rows)
+    against R^T (K (R u)) through the fine level, in all four modes."""
+    from pymoto_gb300._lib import F32, F64, JACOBI, RESIDUAL, call, stream
+    shape = (64, 32, 40)
+    rng = np.random.default_rng(3)
+    g = pg.Grid(*shape)
+    x = dev(rng.uniform(1e-3, 1.0, g.nel) ** 3)
+    gg = O.Grid(*shape)
+    K0 = O.element_stiffness(gg)
+    mask = torch.zeros(g.nnodes, dtype=torch.uint8, device="cuda")
+    op = pg.StiffnessOperator(g, x, K0, mask, O.default_bcdiagval(K0))
+    c = F64 if code == "f64" else F32
+    dt = torch.float64 if code == "f64" else torch.float32
+    tol = 1e-12 if code == "f64" else 2e-5
+    if code == "f32":
+        op = op.astype(F32)
+    # fine level: assembled stencil (row kernel) vs the matrix-free product of the same operator
+    S = op.stencil() if code == "f64" else None
+    u = torch.randn(g.ndof, dtype=dt, device="cuda")
+    b = torch.randn_like(u)
+    if code == "f64":
+        y_row = torch.empty_like(u)
+        call("pmg_stencil_apply", 0, c, *shape, S, u, b, u, 0.0, y_row, stream())
+        y_mf = op.matvec(u)
+        assert float((y_row - y_mf).abs().max()) <= tol * float(y_mf.abs().max())
+    # coarse level (split kernel) vs restriction of the fine product of the prolonged vector
+    A1 = op.galerkin()
+    gc = A1.grid
+    uc = torch.randn(gc.ndof, dtype=dt, device="cuda")
+    bc = torch.randn_like(uc)
+    uf = torch.zeros(g.ndof, dtype=dt, device="cuda")
+    call("pmg_prolong_add", c, *shape, uc, uf, stream())
+    kf = op.matvec(uf)
+    ref = torch.empty_like(uc)
+    call("pmg_restrict", c, *shape, kf, ref, stream())
+    y = A1.matvec(uc)
+    scale = float(ref.abs().max())
+    assert float((y - ref).abs().max()) <= tol * scale
+    D = A1.diagonal()
+    r = A1.apply(RESIDUAL, uc, bc)
+    assert float((r - (bc - ref)).abs().max()) <= tol * scale
+    j = A1.apply(JACOBI, uc, bc, D, 0.6)
+    jref = uc + 0.6 * ((bc - ref) / D)
+    assert float((j - jref).abs().max()) <= tol * float(jref.abs().max()) * 10
+    coef = torch.tensor([0.5, 0.7, 0.3, 0.9], dtype=torch.float64, device="cuda")
+    d0 = torch.randn_like(uc)
+    dd = d0.clone()
+    yc = torch.empty_like(uc)
+    assert A1.cheb_step(uc, bc, D, dd, coef, 1, out=yc) is not None
+    dref = 0.3 * d0 + 0.9 * ((bc - ref) / D)
+    assert float((dd - dref).abs().max()) <= tol * float(dref.abs().max()) * 10
+    assert float((yc - (uc + dref)).abs().max()) <= tol * float((uc + dref).abs().max()) * 10
+
+
 @pytest.mark.parametrize("shape", SHAPES)
 def test_matvec_fp32_and_modes(pg, shape):
     from pymoto_gb300._lib import F32, JACOBI, RESIDUAL

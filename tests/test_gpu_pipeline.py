@@ -151,6 +151,36 @@ def test_mixed_precision_reaches_fp64_residual(pg, shape):
     assert not solver.fell_back
 
 
+def test_lagged_coarse_inverse_is_promoted(pg):
+    """coarse_lag: the first update factorises synchronously; a later update keeps the previous coarse inverse
+    active until its own factorisation finishes, the solver promotes the new one mid-solve, and the solve
+    reaches the FP64 tolerance.  After the solve the active inverse is that of the current coarse matrix."""
+    shape = (32, 16, 16)
+    g = O.Grid(*shape)
+    bc = clamp_face_dofs(g)
+    f = _cantilever_rhs(g)
+    f[bc] = 0
+    rng = np.random.default_rng(4)
+    w = O.conv_filter_weights(g, 2.5)
+    d = pg.VoxelDomain(*shape)
+    mgs = pg.GeometricMultigrid.hierarchy(d, levels=4, smooth_steps=1, coarse_smooth_steps=3, precision="fp32",
+                                          smoother="chebyshev", coarse_lag=True)
+    solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=1e-6, inner_iters=3)
+    coarse = mgs[-1].inner_level
+    assert isinstance(coarse, pg.DenseCholesky) and coarse.lag
+    for it in range(3):
+        x = O.simp(O.conv_filter(g, w, rng.uniform(1e-3, 1.0, g.nel)))
+        Kop = pg.AssembleStiffness(d, bc=bc)(dev(x))
+        solver.update(Kop)
+        u = solver.solve(dev(f))
+        assert pg.LinearSolver.residual(Kop, u, dev(f)) <= 1e-6
+        torch.cuda.synchronize()
+        assert coarse.promote_if_ready()
+        fresh = pg.DenseCholesky()
+        fresh.update(mgs[-1]._Ac)
+        assert torch.equal(coarse.Ainv32, fresh.Ainv32)
+
+
 def test_mixed_precision_falls_back_on_extreme_contrast(pg):
     """Unfiltered SIMP noise (element-to-element contrast up to 1e9): the FP32 preconditioner stalls, the
     solver switches to the FP64 hierarchy and still reaches the FP64 residual tolerance."""
