@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--shape", default=None, help="override the grid, e.g. 64x32x32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-breakdown", action="store_true", help="print a per-kernel time table")
-    ap.add_argument("--inner-iters", type=int, default=3, help="FP32 PCG iterations per FCG preconditioning")
+    ap.add_argument("--inner-iters", type=int, default=4, help="FP32 PCG iterations per FCG preconditioning")
     ap.add_argument("--inner-tol", type=float, default=0.1)
     ap.add_argument("--fcg-m", type=int, default=1)
     ap.add_argument("--levels", type=int, default=GPU_LEVELS)
@@ -77,7 +77,7 @@ def cantilever(shape):
 class DesignRun:
     """The network of the workload on the device, for one solver arm."""
 
-    opts = {"inner_iters": 3, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None,
+    opts = {"inner_iters": 4, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None,
             "smoother": "chebyshev", "cheb_degree": 1, "cheb_coarse_degree": 3, "cheb_ratio": 10.0,
             "learned_train_steps": 1, "learned_stride": 4, "learned_lr": 2e-3, "learned_net": True,
             "learned_history": 1, "coarse_lag": True}

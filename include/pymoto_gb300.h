@@ -74,8 +74,11 @@ int pmg_ebe_diagonal(int dtype, int nelx, int nely, int nelz, const void* xe, co
                      const uint8_t* bcmask, double bcdiag, void* diag, void* stream);
 
 /* ---- assembled node-stencil operator of the coarse multigrid levels ---------------------------
- * S holds, per node, the (3^dim) x dim x dim coupling blocks in structure-of-arrays order
- * S[(o*dim + d)*dim + c][node], o = (dz+1)*9 + (dy+1)*3 + (dx+1) (3D) or (dy+1)*3 + (dx+1) (2D).
+ * The operators are symmetric, so S holds per node only the centre block and the blocks of the forward
+ * offsets o > C, o = (dz+1)*9 + (dy+1)*3 + (dx+1) (3D, C = 13) or (dy+1)*3 + (dx+1) (2D, C = 4), in
+ * structure-of-arrays order S[(h*dim + d)*dim + c][node] with h = o - C: 14 x 3 x 3 values per node in 3D,
+ * 5 x 2 x 2 in 2D.  The block of a backward offset o < C at node n is the transpose of the block stored at
+ * its neighbour n + off(o) for offset 2C - o.  Entries of offsets that leave the grid are zero.
  * Replaces the CSR products with the Galerkin operators R^T A R (pymoto/solvers/iterative.py:173,
  * :233-255). */
 int pmg_stencil_apply(int mode, int dtype, int nelx, int nely, int nelz, const void* S, const void* u,
@@ -265,6 +268,10 @@ int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, do
 /* Status of the last pmg_oc_update on `scratch` (host-synchronous read): PMG_OK, or PMG_TIMEOUT if a
  * bounded wait of the single-launch bisection expired (its CTAs were not all resident). */
 int pmg_oc_status(const void* scratch);
+/* The same status word copied into host memory (`status`, pinned for an asynchronous copy) in stream order:
+ * nonzero once the copy has completed means the bisection's bounded wait expired.  Lets a host loop read
+ * the status at its next synchronisation instead of adding one. */
+int pmg_oc_status_async(const void* scratch, unsigned* status, void* stream);
 
 /* ---- learned warm start (no counterpart in the reference: the reference solves every design from the
  * previous solution only).  A 3-level convolutional encoder-decoder on the voxel grid of a coarse

@@ -80,6 +80,7 @@ SIGNATURES = {
     "pmg_sens_contract_mixed": (I, [I, I, I, P, P, P, P, D, I, P, P]),
     "pmg_oc_scratch_bytes": (c_size_t, []),
     "pmg_oc_status": (I, [P]),
+    "pmg_oc_status_async": (I, [P, P, P]),
     "pmg_oc_update": (I, [L, P, P, P, D, D, D, D, D, D, D, P, P]),
     "pmg_nn_conv3d_forward": (I, [I, I, I, I, I, I, P, P, P, I, P, P, P]),
     "pmg_nn_conv3d_backward_data": (I, [I, I, I, I, I, P, P, P, P]),
@@ -153,7 +154,7 @@ def _arg(a):
 _HOST_ONLY = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_element_stiffness", "pmg_galerkin_table",
               "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth",
               "pmg_cholesky_inverse_f32_scratch_bytes", "pmg_nn_wgrad_scratch_bytes", "pmg_oc_status",
-              "pmg_coarse_ordering"}
+              "pmg_coarse_ordering", "pmg_oc_status_async"}
 
 
 def _launches(name, args):

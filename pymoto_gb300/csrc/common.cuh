@@ -27,8 +27,22 @@ struct Traits {
   static constexpr int NN = 1 << DIM;         // nodes per element
   static constexpr int NDE = NN * DIM;        // dofs per element
   static constexpr int NOFF = DIM == 3 ? 27 : 9;  // node-stencil offsets
-  static constexpr int NSB = NOFF * DIM * DIM;     // stencil values per node
+  // Node stencils of the (symmetric) operators are stored half: the centre block and the blocks of the
+  // forward offsets o > CENTER, o = (dz+1)*9 + (dy+1)*3 + (dx+1), as S[(h*DIM + d)*DIM + c][node] with
+  // h = o - CENTER.  The block of a backward offset o < CENTER at node n is the transpose of the stored block
+  // of the neighbour m = n + off(o) at offset NOFF-1-o.
+  static constexpr int CENTER = NOFF / 2;          // 13 (3D), 4 (2D)
+  static constexpr int NH = NOFF - CENTER;         // stored offsets per node: 14, 5
+  static constexpr int NSB = NH * DIM * DIM;       // stored stencil values per node: 126, 20
 };
+
+// (dx, dy, dz) of node-stencil offset o
+template <int DIM>
+__host__ __device__ __forceinline__ void stencil_offset(int o, int& dx, int& dy, int& dz) {
+  dx = o % 3 - 1;
+  dy = (o / 3) % 3 - 1;
+  dz = DIM == 3 ? o / 9 - 1 : 0;
+}
 
 // Element matrix passed by value in the kernel parameter space (constant bank): all threads of a warp
 // read the same entry at the same time, so the FMAs take it as a uniform operand.

@@ -664,6 +664,17 @@ int pmg_oc_status(const void* scratch) {
   return err ? PMG_TIMEOUT : PMG_OK;
 }
 
+int pmg_oc_status_async(const void* scratch, unsigned* status, void* stream) {
+  if (!scratch || !status) return PMG_BAD_ARG;
+  cudaError_t e = cudaMemcpyAsync(status, &((const OCScratch*)scratch)->error, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                  as_stream(stream));
+  if (e != cudaSuccess) {
+    set_error(cudaGetErrorString(e));
+    return PMG_CUDA_ERR;
+  }
+  return PMG_OK;
+}
+
 int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, double volfrac, double move, double xmin,
                   double xmax, double l1, double l2, double l1l2tol, void* scratch, void* stream) {
   if (n <= 0 || !x || !dg || !xnew || !scratch || !(l1l2tol > 0.0) || !(l2 >= l1)) return PMG_BAD_ARG;

@@ -234,9 +234,33 @@ __global__ void ebe_diag_kernel(Grid g, const T* __restrict__ xe, ElemMat<T, Tra
 }
 
 // ------------------------------------------------------------------------------------------ stencils
+// Coefficient (d, c) of the block of node n at offset o, whose neighbour m = n + off(o) is clamped into the
+// grid (`in`: the neighbour exists).  Forward offsets are stored at n, and their entries are exactly zero
+// where the neighbour does not exist; a backward block is the transpose of the neighbour's stored forward
+// block, read at the clamped index and replaced by zero when the neighbour does not exist, so that every
+// load is unconditional and all of them can be in flight together.
+// The DIM coefficients (d, 0..DIM-1) of row d of that block: base pointer and stride between them.
+template <typename T>
+struct StencilRow {
+  const T* p;
+  int stride;
+};
+
+template <typename T, int DIM>
+__device__ __forceinline__ StencilRow<T> stencil_row(const T* __restrict__ S, int nn, int o, int d, int n, int m) {
+  constexpr int CENTER = Traits<DIM>::CENTER, NOFF = Traits<DIM>::NOFF;
+  if (o >= CENTER) return {S + (int64_t)(((o - CENTER) * DIM + d) * DIM) * nn + n, nn};
+  return {S + (int64_t)((NOFF - 1 - o - CENTER) * DIM * DIM + d) * nn + m, DIM * nn};
+}
+
+template <typename T, int DIM>
+__device__ __forceinline__ T stencil_coef(const T* __restrict__ S, int nn, int o, int d, int c, int n, int m, bool in) {
+  const StencilRow<T> r = stencil_row<T, DIM>(S, nn, o, d, n, m);
+  const T v = r.p[(int64_t)c * r.stride];
+  return (o >= Traits<DIM>::CENTER || in) ? v : T(0);
+}
+
 // One thread per (component d, node n), d slowest so that the stencil loads of a warp are coalesced.
-// Neighbours outside the grid are read at a clamped (valid) index: their stencil entries are exactly zero,
-// so the loads need no branches and can all be in flight together.
 template <typename T, int DIM, int MODE>
 __global__ void __launch_bounds__(256) stencil_apply_kernel(Grid g, const T* __restrict__ S, const T* __restrict__ u,
                                                             const T* __restrict__ b, const T* __restrict__ diag, T w,
@@ -251,12 +275,19 @@ __global__ void __launch_bounds__(256) stencil_apply_kernel(Grid g, const T* __r
   T acc = T(0);
 #pragma unroll
   for (int o = 0; o < NOFF; ++o) {
-    const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dz = DIM == 3 ? o / 9 - 1 : 0;
+    int dx, dy, dz;
+    stencil_offset<DIM>(o, dx, dy, dz);
+    const bool in = i + dx >= 0 && i + dx <= g.nx && j + dy >= 0 && j + dy <= g.ny && k + dz >= 0 && k + dz <= g.nz;
     const int ii = min(max(i + dx, 0), g.nx), jj = min(max(j + dy, 0), g.ny), kk = min(max(k + dz, 0), g.nz);
     const int m = (kk * (g.ny + 1) + jj) * (g.nx + 1) + ii;
-    const T* Sd = S + (int64_t)((o * DIM + d) * DIM) * nn + n;
+    const StencilRow<T> row = stencil_row<T, DIM>(S, nn, o, d, n, m);
+    const T* um = u + (int64_t)m * DIM;
+    const bool live = o >= Traits<DIM>::CENTER || in;   // coefficient selects, not extra FP64 adds
 #pragma unroll
-    for (int c = 0; c < DIM; ++c) acc = fma(Sd[(int64_t)c * nn], u[(int64_t)m * DIM + c], acc);
+    for (int c = 0; c < DIM; ++c) {
+      const T a = row.p[(int64_t)c * row.stride];
+      acc = fma(live ? a : T(0), um[c], acc);
+    }
   }
   const int64_t q = (int64_t)n * DIM + d;
   if (MODE == 0) {
@@ -310,15 +341,22 @@ __global__ void __launch_bounds__(SplitShape<DIM>::THREADS)
     int i, j, k;
     node_ijk(g, n, i, j, k);
     const int dy = p % 3 - 1, dz = DIM == 3 ? p / 3 - 1 : 0;
+    const bool in_yz = j + dy >= 0 && j + dy <= g.ny && k + dz >= 0 && k + dz <= g.nz;
     const int jj = min(max(j + dy, 0), g.ny), kk = min(max(k + dz, 0), g.nz);
     const int row = (kk * (g.ny + 1) + jj) * (g.nx + 1);
 #pragma unroll
     for (int dx = -1; dx <= 1; ++dx) {
-      const int o = 3 * p + dx + 1;
+      const int o = 3 * p + dx + 1;     // p is the same across a warp: the forward/backward branch is uniform
+      const bool in = in_yz && i + dx >= 0 && i + dx <= g.nx;
       const int m = row + min(max(i + dx, 0), g.nx);
-      const T* Sd = S + (int64_t)((o * DIM + d) * DIM) * nn + n;
+      const StencilRow<T> srow = stencil_row<T, DIM>(S, nn, o, d, n, m);
+      const T* um = u + (int64_t)m * DIM;
+      const bool live = o >= Traits<DIM>::CENTER || in;
 #pragma unroll
-      for (int c = 0; c < DIM; ++c) acc = fma(Sd[(int64_t)c * nn], u[(int64_t)m * DIM + c], acc);
+      for (int c = 0; c < DIM; ++c) {
+        const T a = srow.p[(int64_t)c * srow.stride];
+        acc = fma(live ? a : T(0), um[c], acc);
+      }
     }
   }
   part[grp][p][lane] = acc;
@@ -343,12 +381,11 @@ __global__ void __launch_bounds__(SplitShape<DIM>::THREADS)
 
 template <typename T, int DIM>
 __global__ void stencil_diag_kernel(Grid g, const T* __restrict__ S, T* __restrict__ diag) {
-  constexpr int C = DIM == 3 ? 13 : 4;
   const int64_t nn = g.nnodes();
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nn) return;
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) diag[n * DIM + d] = S[((int64_t)(C * DIM + d) * DIM + d) * nn + n];
+  for (int d = 0; d < DIM; ++d) diag[n * DIM + d] = S[((int64_t)d * DIM + d) * nn + n];   // centre block, h = 0
 }
 
 // Row sums of |A| of a stencil operator, per dof (the l1-Jacobi diagonal: with it the spectrum of
@@ -356,17 +393,24 @@ __global__ void stencil_diag_kernel(Grid g, const T* __restrict__ S, T* __restri
 template <typename T, int DIM>
 __global__ void __launch_bounds__(256) stencil_rowabs_kernel(Grid g, const T* __restrict__ S, T* __restrict__ out) {
   constexpr int NOFF = Traits<DIM>::NOFF;
-  const int64_t nn = g.nnodes();
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nn = (int)g.nnodes();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nn * DIM) return;
-  const int d = (int)(t / nn);
-  const int64_t n = t - (int64_t)d * nn;
+  const int d = t / nn, n = t - d * nn;
+  int i, j, k;
+  node_ijk(g, n, i, j, k);
   T sum = T(0);
 #pragma unroll
-  for (int o = 0; o < NOFF; ++o)
+  for (int o = 0; o < NOFF; ++o) {
+    int dx, dy, dz;
+    stencil_offset<DIM>(o, dx, dy, dz);
+    const bool in = i + dx >= 0 && i + dx <= g.nx && j + dy >= 0 && j + dy <= g.ny && k + dz >= 0 && k + dz <= g.nz;
+    const int m = (min(max(k + dz, 0), g.nz) * (g.ny + 1) + min(max(j + dy, 0), g.ny)) * (g.nx + 1) +
+                  min(max(i + dx, 0), g.nx);
 #pragma unroll
-    for (int c = 0; c < DIM; ++c) sum += fabs(S[((int64_t)(o * DIM + d) * DIM + c) * nn + n]);
-  out[n * DIM + d] = sum;
+    for (int c = 0; c < DIM; ++c) sum += fabs(stencil_coef<T, DIM>(S, nn, o, d, c, n, m, in));
+  }
+  out[(int64_t)n * DIM + d] = sum;
 }
 
 // ------------------------------------------------------------------------------------------ transfers
@@ -760,20 +804,19 @@ __global__ void __launch_bounds__(GAL_THREADS) galerkin_from_elements_kernel(Gri
   }
 }
 
-// Node stencils from element matrices: thread per (offset o, node n).
+// Node stencils from element matrices: thread per (node n = x index, stored offset h = blockIdx.y).
 template <typename T, int DIM>
 __global__ void stencil_from_elements_kernel(Grid g, const T* __restrict__ E, T* __restrict__ S) {
   constexpr int NDE = Traits<DIM>::NDE;
   constexpr int NE = NDE * NDE;
-  constexpr int NOFF = Traits<DIM>::NOFF;
   const int64_t nn = g.nnodes();
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nn * NOFF) return;
-  const int o = (int)(t / nn);
-  const int64_t n = t % nn;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nn) return;
+  const int h = blockIdx.y, o = Traits<DIM>::CENTER + h;
   int i, j, k;
   node_ijk(g, n, i, j, k);
-  const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dz = DIM == 3 ? o / 9 - 1 : 0;
+  int dx, dy, dz;
+  stencil_offset<DIM>(o, dx, dy, dz);
   T acc[DIM * DIM];
 #pragma unroll
   for (int q = 0; q < DIM * DIM; ++q) acc[q] = T(0);
@@ -799,7 +842,7 @@ __global__ void stencil_from_elements_kernel(Grid g, const T* __restrict__ E, T*
 #pragma unroll
   for (int d = 0; d < DIM; ++d)
 #pragma unroll
-    for (int c = 0; c < DIM; ++c) S[((int64_t)(o * DIM + d) * DIM + c) * nn + n] = acc[d * DIM + c];
+    for (int c = 0; c < DIM; ++c) S[((int64_t)(h * DIM + d) * DIM + c) * nn + n] = acc[d * DIM + c];
 }
 
 // Level-0 node stencils of K(x) (Dirichlet rows: bcdiag on the diagonal only; Dirichlet columns: zero).
@@ -808,16 +851,15 @@ template <typename T, int DIM>
 __global__ void ebe_stencil_kernel(Grid g, const T* __restrict__ xe, ElemMat<T, Traits<DIM>::NDE> K0,
                                    const uint8_t* __restrict__ bcmask, T bcdiag, T* __restrict__ S) {
   constexpr int NDE = Traits<DIM>::NDE;
-  constexpr int NOFF = Traits<DIM>::NOFF;
-  constexpr int CENTER = DIM == 3 ? 13 : 4;
+  constexpr int CENTER = Traits<DIM>::CENTER;
   const int64_t nn = g.nnodes();
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nn * NOFF) return;
-  const int o = (int)(t / nn);
-  const int64_t n = t % nn;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nn) return;
+  const int h = blockIdx.y, o = CENTER + h;   // stored (forward) offsets only: half the FP64 work
   int i, j, k;
   node_ijk(g, n, i, j, k);
-  const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dz = DIM == 3 ? o / 9 - 1 : 0;
+  int dx, dy, dz;
+  stencil_offset<DIM>(o, dx, dy, dz);
   const int ii = i + dx, jj = j + dy, kk = k + dz;
   const bool nbr_in = ii >= 0 && ii <= g.nx && jj >= 0 && jj <= g.ny && kk >= 0 && kk <= g.nz;
   const uint8_t mrow = bcmask ? bcmask[n] : 0;
@@ -852,31 +894,34 @@ __global__ void ebe_stencil_kernel(Grid g, const T* __restrict__ xe, ElemMat<T, 
       T v = acc[d * DIM + c];
       if (((mrow >> d) & 1) || ((mcol >> c) & 1)) v = T(0);
       if (((mrow >> d) & 1) && o == CENTER && c == d) v = bcdiag;
-      S[((int64_t)(o * DIM + d) * DIM + c) * nn + n] = v;
+      S[((int64_t)(h * DIM + d) * DIM + c) * nn + n] = v;
     }
 }
 
 template <typename T, int DIM>
 __global__ void stencil_to_dense_kernel(Grid g, const T* __restrict__ S, const int32_t* __restrict__ pos,
                                         double* __restrict__ A) {
-  constexpr int NOFF = Traits<DIM>::NOFF;
   const int64_t nn = g.nnodes();
   const int64_t ndof = nn * DIM;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nn * NOFF) return;
-  const int o = (int)(t / nn);
-  const int64_t n = t % nn;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nn) return;
+  const int h = blockIdx.y, o = Traits<DIM>::CENTER + h;
   int i, j, k;
   node_ijk(g, n, i, j, k);
-  const int ii = i + o % 3 - 1, jj = j + (o / 3) % 3 - 1, kk = k + (DIM == 3 ? o / 9 - 1 : 0);
+  int dx, dy, dz;
+  stencil_offset<DIM>(o, dx, dy, dz);
+  const int ii = i + dx, jj = j + dy, kk = k + dz;
   if (ii < 0 || ii > g.nx || jj < 0 || jj > g.ny || kk < 0 || kk > g.nz) return;
   const int64_t m = node_id(g, ii, jj, kk);
+  // the stored block (n, m) and, for a forward offset, its transpose (m, n): every entry written once
 #pragma unroll
   for (int d = 0; d < DIM; ++d)
 #pragma unroll
     for (int c = 0; c < DIM; ++c) {
       const int64_t row = pos ? pos[n * DIM + d] : n * DIM + d, col = pos ? pos[m * DIM + c] : m * DIM + c;
-      A[row * ndof + col] = (double)S[((int64_t)(o * DIM + d) * DIM + c) * nn + n];
+      const double v = (double)S[((int64_t)(h * DIM + d) * DIM + c) * nn + n];
+      A[row * ndof + col] = v;
+      if (h > 0) A[col * ndof + row] = v;
     }
 }
 
@@ -991,6 +1036,14 @@ int stencil_apply_t(int mode, Grid g, const void* S, const void* u, const void* 
       return CALL;                                      \
     }                                                   \
   } while (0)
+
+// Thread per (node = x index, stored stencil offset = blockIdx.y).
+template <typename T, int DIM, typename Kern, typename... Args>
+int launch_per_stored_offset(Kern kernel, const Grid& g, cudaStream_t st, Args... args) {
+  const dim3 grid(blocks_for(g.nnodes(), 256), Traits<DIM>::NH);
+  kernel<<<grid, 256, 0, st>>>(args...);
+  return check_launch();
+}
 
 template <typename T, int DIM, typename Kern, typename... Args>
 int launch_simple(Kern kernel, int64_t n, cudaStream_t st, Args... args) {
@@ -1212,20 +1265,19 @@ int pmg_galerkin_from_elements(int dtype, int nelx, int nely, int nelz, const vo
 int pmg_stencil_from_elements(int dtype, int nelx, int nely, int nelz, const void* E, void* S, void* stream) {
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !E || !S) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
-  const int64_t work = g.nnodes() * (g.dim() == 3 ? 27 : 9);
   PMG_DISPATCH(dtype, g.dim(),
-               (launch_simple<T, DIM>(stencil_from_elements_kernel<T, DIM>, work, as_stream(stream), g, (const T*)E,
-                                      (T*)S)));
+               (launch_per_stored_offset<T, DIM>(stencil_from_elements_kernel<T, DIM>, g, as_stream(stream), g,
+                                                 (const T*)E, (T*)S)));
 }
 
 int pmg_ebe_stencil(int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
                     const uint8_t* bcmask, double bcdiag, void* S, void* stream) {
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !xe || !K0_host || !S) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
-  const int64_t work = g.nnodes() * (g.dim() == 3 ? 27 : 9);
   PMG_DISPATCH(dtype, g.dim(),
-               (launch_simple<T, DIM>(ebe_stencil_kernel<T, DIM>, work, as_stream(stream), g, (const T*)xe,
-                                      make_elem_mat<T, Traits<DIM>::NDE>(K0_host), bcmask, (T)bcdiag, (T*)S)));
+               (launch_per_stored_offset<T, DIM>(ebe_stencil_kernel<T, DIM>, g, as_stream(stream), g, (const T*)xe,
+                                                 make_elem_mat<T, Traits<DIM>::NDE>(K0_host), bcmask, (T)bcdiag,
+                                                 (T*)S)));
 }
 
 int pmg_stencil_to_dense(int dtype, int nelx, int nely, int nelz, const void* S, double* A, void* stream) {
@@ -1244,9 +1296,8 @@ int pmg_stencil_to_dense_perm(int dtype, int nelx, int nely, int nelz, const voi
     set_error(cudaGetErrorString(e));
     return PMG_CUDA_ERR;
   }
-  const int64_t work = g.nnodes() * (g.dim() == 3 ? 27 : 9);
   PMG_DISPATCH(dtype, g.dim(),
-               (launch_simple<T, DIM>(stencil_to_dense_kernel<T, DIM>, work, st, g, (const T*)S, pos, A)));
+               (launch_per_stored_offset<T, DIM>(stencil_to_dense_kernel<T, DIM>, g, st, g, (const T*)S, pos, A)));
 }
 
 int pmg_coarse_ordering(int nelx, int nely, int nelz, int32_t* pos, int* bw) {

@@ -436,6 +436,8 @@ class EinSum(Module):
         a = devs[0][0]
         b = devs[1][0] if self.expr == "i,i->" else torch.ones_like(a)
         call("pmg_dot", F64, a.numel(), a, b, out, ws.reduce, stream())
+        if all(kind == "torch" for _, kind in devs):
+            return out.reshape(())      # device scalar: read by the caller when it needs the value
         return np.float64(out.item())
 
     def _sensitivity(self, df):

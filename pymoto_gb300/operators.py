@@ -15,6 +15,12 @@ from ._lib import F32, F64, JACOBI, MATVEC, RESIDUAL, call, stream
 TORCH_DTYPE = {F64: torch.float64, F32: torch.float32}
 
 
+def stencil_values_per_node(dim):
+    """Stored node-stencil values per node: the centre block and the forward-offset blocks of a symmetric
+    operator (14 of the 27 blocks in 3D, 5 of 9 in 2D; the others are their neighbours' transposes)."""
+    return (14 if dim == 3 else 5) * dim * dim
+
+
 class Grid:
     """Element counts of a structured grid; nelz == 0 is 2D."""
 
@@ -205,8 +211,8 @@ class StiffnessOperator:
         """Node stencils of this operator (assembled on first use, same precision)."""
         if self._S is None:
             g = self.grid
-            nsb = (27 if g.dim == 3 else 9) * g.dim * g.dim
-            self._S = torch.empty((nsb, g.nnodes), dtype=self.torch_dtype, device=self.device)
+            self._S = torch.empty((stencil_values_per_node(g.dim), g.nnodes), dtype=self.torch_dtype,
+                                  device=self.device)
             self._assemble_stencil(self._S)
         return self._S
 
@@ -303,8 +309,7 @@ class StencilOperator:
         self.E = E
         self.code = code
         g = grid
-        nsb = (27 if g.dim == 3 else 9) * g.dim * g.dim
-        self.S = torch.empty((nsb, g.nnodes), dtype=TORCH_DTYPE[code], device=E.device)
+        self.S = torch.empty((stencil_values_per_node(g.dim), g.nnodes), dtype=TORCH_DTYPE[code], device=E.device)
         self._diag = None
         self.recompute()
 

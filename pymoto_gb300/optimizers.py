@@ -8,7 +8,7 @@ design Signal holds a numpy array.
 import numpy as np
 import torch
 
-from ._lib import call, stream
+from ._lib import PMGError, call, stream
 from .operators import Workspace
 from .solvers import _from_device, _to_device
 
@@ -46,18 +46,38 @@ class OC:
         x, kind = self._x()
         if self.maxvol is None:
             self.maxvol = float(x.sum().item()) / x.numel()
-        g = self.calculate_g()
+        self.function.response()
         ws = Workspace.get(x.device)
+        if getattr(self, "_status", None) is None:
+            self._status = torch.zeros(1, dtype=torch.int32).pin_memory()
+            self._g_host = torch.zeros(1, dtype=torch.float64).pin_memory()
+            self._g_event = torch.cuda.Event()
+            self._status_event = torch.cuda.Event()
         if getattr(self, "_issued", False):
-            # status of the previous update's bisection (a bounded wait that expired): the host has just
-            # synchronised on the response, which the device computed after that update
-            call("pmg_oc_status", ws.oc)
+            # status of the previous update's bisection (a bounded wait that expired), copied to the host in
+            # stream order after that update (complete by now when the response synchronised with the device)
+            self._status_event.synchronize()
+            if int(self._status[0]) != 0:
+                raise PMGError("pmg_oc_update", 3, "the single-launch bisection's bounded wait expired")
+        gs = self.response.state
+        if isinstance(gs, torch.Tensor) and gs.is_cuda:
+            # the response value is read once everything below is queued: no device idle time for it
+            self._g_host.copy_(gs.reshape(1), non_blocking=True)
+            self._g_event.record()
+            g = None
+        else:
+            g = float(gs)
         dg = _to_device(self.calculate_dg(), device=x.device)[0]
         xnew = torch.empty_like(x)
         call("pmg_oc_update", x.numel(), x, dg, xnew, self.maxvol, self.move, self.xmin, self.xmax, self.l1init,
              self.l2init, self.l1l2tol, ws.oc, stream())
+        call("pmg_oc_status_async", ws.oc, self._status, stream())
+        self._status_event.record()
         self._issued = True
         self.variable.state = _from_device(xnew, kind)
+        if g is None:
+            self._g_event.synchronize()
+            g = float(self._g_host[0])
         self.history.append(g)
         return xnew, g, dg
 

@@ -570,11 +570,14 @@ def _check_coarsest(pc):
 
 
 def _side_stream(owner):
-    """A second CUDA stream of `owner` (created once per device), for setup work that overlaps the main one."""
+    """A second CUDA stream of `owner` (created once per device), for setup work that overlaps the main one.
+    It has the higher priority: its kernels are small and on the critical path (the hierarchy the first
+    preconditioner application waits for, the coarsest factorisation a lagged solve waits to promote), so
+    the CTA scheduler should start them ahead of the bulk of the main stream's work."""
     dev = torch.cuda.current_device()
     s = getattr(owner, "_side", None)
     if s is None or s.device.index != dev:
-        s = owner._side = torch.cuda.Stream(device=dev)
+        s = owner._side = torch.cuda.Stream(device=dev, priority=-1)
     return s
 
 
