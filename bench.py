@@ -33,6 +33,9 @@ RADIUS, PENAL, XMIN, TOL, MOVE, OMEGA, SWEEPS = 2.5, 3.0, 1e-9, 1e-6, 0.2, 0.6, 
 GPU_LEVELS = 5          # 128x64x64 -> 8x4x4 coarsest (675 dofs, dense FP64 Cholesky + explicit inverse)
 REF_LEVELS = 4          # the reference example's hierarchy: coarsest 16x8x8 (SuperLU)
 L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes (read + write) per launch of the roofline kernel at the bench workload, from the ncu capture
+# summarised in profiles/ebe_apply_mma_residual_hex8_128x64x64.md
+NCU_TRAFFIC_PER_LAUNCH = {"ebe_apply_mma_residual_f32": 15.756e6}
 
 
 def parse():
@@ -43,6 +46,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--shape", default=None, help="override the grid, e.g. 64x32x32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--timed-only", action="store_true",
+                    help="stop after the timed design iterations (no parity, e2e or kernel timing): for launch lists")
     ap.add_argument("--profile-breakdown", action="store_true", help="print a per-kernel time table")
     ap.add_argument("--inner-iters", type=int, default=4, help="FP32 PCG iterations per FCG preconditioning")
     ap.add_argument("--inner-tol", type=float, default=0.1)
@@ -219,24 +224,46 @@ def time_arm(run, steps, warmup, torch, flush, probe_targets=None, pg=None):
     return durs, probe
 
 
-def kernel_bytes(key, shape):
-    """Algorithmic bytes of one launch of the entry points we report a roofline for."""
-    nx, ny, nz = shape
-    nel = nx * ny * nz
-    nn = (nx + 1) * (ny + 1) * (nz + 1)
-    ndof = 3 * nn
-    name = key[0]
-    if name == "pmg_ebe_apply":
-        mode, dtype = key[1], key[2]
-        s = 8 if dtype == 0 else 4
-        vec_reads = {0: 1, 1: 2, 2: 3}[mode]       # u (+ b) (+ diag)
-        return ndof * s * (vec_reads + 1) + nel * s + nn
-    if name == "pmg_stencil_apply" and len(key) > 3 and key[3] == nx:
-        mode, dtype = key[1], key[2]
-        s = 8 if dtype == 0 else 4
-        vec_reads = {0: 1, 1: 2, 2: 3}[mode]
-        return ndof * s * (vec_reads + 1) + 243 * nn * s      # u (+ b, diag), y, the 243-entry node stencils
-    return None
+def kernel_rooflines(run, flush, torch, reps=20):
+    """Live CUDA-event times of the two level-0 operator kernels on the headline arm's final operators, one
+    launch at a time on the current stream with the L2 flushed (256 MB write) before each launch:
+      * the FP32 tensor-core operator (ebe_apply_mma, residual mode): the most launched kernel of a design
+        iteration (one matvec, one residual and one Chebyshev step per inner iteration);
+      * the FP64 node-stencil product (the outer FCG operator), whose bound is the FP64 pipe.
+    Returns per kernel: seconds per launch, algorithmic bytes and flops per launch."""
+    from pymoto_gb300._lib import MATVEC, RESIDUAL
+    sol = run.solver
+    A32, A64 = sol.A32, sol.A64
+    g = A64.grid
+    nel, nn, ndof = g.nel, g.nnodes, g.ndof
+    u32 = torch.randn(ndof, device="cuda")
+    b32, y32 = torch.randn_like(u32), torch.empty_like(u32)
+    u64 = torch.randn(ndof, dtype=torch.float64, device="cuda")
+    y64 = torch.empty_like(u64)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(reps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / reps * 1e-3
+
+    out = {}
+    t = timed(lambda: A32.apply(RESIDUAL, u32, b32, out=y32))
+    # u, b read and y written once (FP32), element scaling (FP32) and the node constraint mask (bytes)
+    out["ebe_apply_mma_residual_f32"] = {"s": t, "bytes": 3 * 4 * ndof + 4 * nel + nn,
+                                         "flops": 3 * 2 * 24 * 24 * nel}     # three TF32 products per element
+    t = timed(lambda: A64.apply(MATVEC, u64, out=y64))
+    # 27 blocks of 3 x 3 per row of 3 dofs: 81 FP64 FMA per dof; stored stencils (14 blocks) + u + y once
+    out["stencil_apply_f64_matvec"] = {"s": t, "bytes": 8 * (126 * nn + 2 * ndof), "flops": 2 * 81 * ndof}
+    return out
 
 
 def measure_gb300(args, rank, world, local_rank):
@@ -286,6 +313,12 @@ def measure_gb300(args, rank, world, local_rank):
         results[arm]["true_residual"] = res
         results[arm]["compliance"] = float(run.c.state)
 
+    if args.timed_only:           # profiling runs: the timed design iterations and nothing after them
+        if rank == 0:
+            print(json.dumps({"timed_only": True, "arms": {a: {"ms_per_step": r["total_ms"] / args.steps,
+                                                               "solver_iterations": r["iters"]}
+                                                           for a, r in results.items()}}))
+        return None
     # same-design parity: solve the plain arm's final design with both solvers
     run_p = results[next(iter(results))]["run"]
     lin_p = run_p.fn.mods[3]
@@ -330,8 +363,10 @@ def measure_gb300(args, rank, world, local_rank):
         e2e_durs.append(time.perf_counter() - t0)
     e2e_total = max_over_ranks(sum(e2e_durs))
 
+    kernels = kernel_rooflines(results["mixed"]["run"], flush, torch) if rank == 0 else None
     out = {"results": results, "shape": shape, "hbm_peak": hbm_peak, "peak_src": peak_src, "c_mixed": c_m,
-           "c_tight": c_t, "e2e_total_s": e2e_total, "nel": nel, "res_mixed_same_design": ms.last_residual}
+           "c_tight": c_t, "e2e_total_s": e2e_total, "nel": nel, "res_mixed_same_design": ms.last_residual,
+           "kernels": kernels, "peaks": peaks}
     if args.profile_breakdown and rank == 0:
         run = DesignRun("mixed", shape, seed=99, torch=torch, pg=pg)
         for _ in range(2):
@@ -422,24 +457,36 @@ def main():
     if world > 1:
         torch.distributed.init_process_group("nccl")
     m = measure_gb300(args, rank, world, local_rank)
+    if m is None:
+        return
     if rank == 0:
         shape = m["shape"]
         R = m["results"]
         steps = args.steps
         val_mixed = world * steps / (R["mixed"]["total_ms"] / 1e3)
         val_plain = world * steps / (R["plain_fp64"]["total_ms"] / 1e3) if "plain_fp64" in R else None
-        # roofline of the dominant probed kernel of the headline arm
-        summ = {k: v for k, v in R["mixed"]["probe"].summary().items() if kernel_bytes(k, shape)}
-        top = max(summ.items(), key=lambda kv: kv[1]["total_ms"])
-        key, st = top
-        nbytes = kernel_bytes(key, shape)
-        achieved = nbytes / (st["avg_ms"] * 1e-3) / 1e9 if nbytes else None
-        roofline = {"bound": "hbm", "kernel": "%s(mode=%s,dtype=%s,grid=%s)" % (
-                        key[0], key[1], "f64" if key[2] == 0 else "f32", "x".join(map(str, shape))),
-                    "achieved": achieved, "peak": m["hbm_peak"], "unit": "GB/s",
-                    "frac": achieved / m["hbm_peak"] if achieved else None, "traffic": None,
-                    "bytes_per_launch": nbytes, "avg_launch_ms": st["avg_ms"], "launches": st["launches"],
-                    "peak_source": m["peak_src"], "share_of_step": st["total_ms"] / R["mixed"]["total_ms"]}
+        # rooflines of the level-0 operator kernels, timed live after the timed region (kernel_rooflines)
+        K = m["kernels"]
+        km = K["ebe_apply_mma_residual_f32"]
+        achieved = km["bytes"] / km["s"] / 1e9
+        tf32_peak = m["peaks"].get("bf16_tflops", 1900.0) / 2.0       # dense TF32 runs at half the BF16 rate
+        roofline = {"bound": "hbm", "kernel": "ebe_apply_mma_kernel<residual> (FP32 operator, 3xTF32 mma.sync, "
+                                               "grid %s)" % "x".join(map(str, shape)),
+                    "achieved": achieved, "peak": m["hbm_peak"], "unit": "GB/s", "frac": achieved / m["hbm_peak"],
+                    "traffic": NCU_TRAFFIC_PER_LAUNCH.get("ebe_apply_mma_residual_f32"),
+                    "bytes_per_launch": km["bytes"], "avg_launch_us": km["s"] * 1e6,
+                    "tensor_tflops": km["flops"] / km["s"] / 1e12, "tensor_frac_of_tf32": km["flops"] / km["s"] / 1e12
+                    / tf32_peak, "peak_source": m["peak_src"],
+                    "launches_per_step": "3 per inner FP32 PCG iteration (matvec, V-cycle residual, Chebyshev step)",
+                    "note": "one launch at a time after a 256 MB L2 flush, CUDA events on the launching stream"}
+        ks = K["stencil_apply_f64_matvec"]
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        fp64_peak = 2 * 2 * sms * m["peaks"].get("sm_max_mhz", 2070.0) * 1e6 / 1e12   # 2 DFMA/clk/SM nominal
+        roofline_fp64 = {"bound": "fp64", "kernel": "stencil_apply_kernel<double> (outer FP64 operator)",
+                         "achieved": ks["flops"] / ks["s"] / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": ks["flops"] / ks["s"] / 1e12 / fp64_peak, "avg_launch_us": ks["s"] * 1e6,
+                         "hbm_gbs": ks["bytes"] / ks["s"] / 1e9, "peak_source": "nominal 2 FP64 FMA/clk/SM x SMs x "
+                                                                                "max SM clock"}
         cpu = None
         if not args.no_cpu_baseline and world == 1:
             times, L = cpu_reference_sample(shape, warm_steps=1)
@@ -473,7 +520,7 @@ def main():
                 "parity": {"same_design_compliance_mixed": m["c_mixed"], "same_design_compliance_fp64_tol1e-11":
                            m["c_tight"], "rel_diff": abs(m["c_mixed"] - m["c_tight"]) / abs(m["c_tight"]),
                            "mixed_true_rel_residual": m["res_mixed_same_design"]},
-                "roofline": roofline, "cpu_baseline": cpu,
+                "roofline": roofline, "roofline_fp64_stencil": roofline_fp64, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": "design it/s", "h2d_bytes_per_step": 8 * m["nel"],
                         "d2h_bytes_per_step": 8 * m["nel"] + 8},
                 "gpu_launches": launches, "clocks": R["mixed"]["clocks"]}
