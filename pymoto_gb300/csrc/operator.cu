@@ -308,18 +308,18 @@ __global__ void __launch_bounds__(256) stencil_apply_kernel(Grid g, const T* __r
 // through a long chain of dependent loads: the 3^dim offsets of a row are split over NOFF/3 threads (one
 // x-line of 3 offsets each, so every thread issues its 3 DIM coefficient and 3 DIM value loads at once), and
 // the partial sums are added in a fixed order in shared memory.  Block: 32 rows x NOFF/3 parts x SPLIT_G.
-template <int DIM>
+template <int DIM, int LINES>
 struct SplitShape {
-  static constexpr int P = Traits<DIM>::NOFF / 3;   // parts per row: 9 (3D), 3 (2D)
-  static constexpr int G = DIM == 3 ? 1 : 3;        // 32-row groups per block
-  static constexpr int THREADS = 32 * P * G;        // 288
+  static constexpr int P = Traits<DIM>::NOFF / 3 / LINES;   // parts per row (LINES x-lines each): 9 or 3 in 3D
+  static constexpr int G = 288 / (32 * P);                  // 32-row groups per block
+  static constexpr int THREADS = 32 * P * G;                // 288
 };
 
-template <typename T, int DIM, int MODE>
-__global__ void __launch_bounds__(SplitShape<DIM>::THREADS)
+template <typename T, int DIM, int MODE, int LINES>
+__global__ void __launch_bounds__(SplitShape<DIM, LINES>::THREADS)
     stencil_apply_split_kernel(Grid g, const T* __restrict__ S, const T* __restrict__ u, const T* __restrict__ b,
                                const T* __restrict__ diag, T w, T* __restrict__ y, ChebArgs<T> ch) {
-  constexpr int P = SplitShape<DIM>::P, G = SplitShape<DIM>::G;
+  constexpr int P = SplitShape<DIM, LINES>::P, G = SplitShape<DIM, LINES>::G;
   __shared__ T part[G][P][32];
   const int nn = (int)g.nnodes();
   const int lane = threadIdx.x, p = threadIdx.y, grp = threadIdx.z;
@@ -340,22 +340,26 @@ __global__ void __launch_bounds__(SplitShape<DIM>::THREADS)
   if (active) {
     int i, j, k;
     node_ijk(g, n, i, j, k);
-    const int dy = p % 3 - 1, dz = DIM == 3 ? p / 3 - 1 : 0;
-    const bool in_yz = j + dy >= 0 && j + dy <= g.ny && k + dz >= 0 && k + dz <= g.nz;
-    const int jj = min(max(j + dy, 0), g.ny), kk = min(max(k + dz, 0), g.nz);
-    const int row = (kk * (g.ny + 1) + jj) * (g.nx + 1);
 #pragma unroll
-    for (int dx = -1; dx <= 1; ++dx) {
-      const int o = 3 * p + dx + 1;     // p is the same across a warp: the forward/backward branch is uniform
-      const bool in = in_yz && i + dx >= 0 && i + dx <= g.nx;
-      const int m = row + min(max(i + dx, 0), g.nx);
-      const StencilRow<T> srow = stencil_row<T, DIM>(S, nn, o, d, n, m);
-      const T* um = u + (int64_t)m * DIM;
-      const bool live = o >= Traits<DIM>::CENTER || in;
+    for (int li = 0; li < LINES; ++li) {
+      const int l = p * LINES + li;     // x-line (dy, dz); the same across a warp: uniform branches
+      const int dy = l % 3 - 1, dz = DIM == 3 ? l / 3 - 1 : 0;
+      const bool in_yz = j + dy >= 0 && j + dy <= g.ny && k + dz >= 0 && k + dz <= g.nz;
+      const int jj = min(max(j + dy, 0), g.ny), kk = min(max(k + dz, 0), g.nz);
+      const int row = (kk * (g.ny + 1) + jj) * (g.nx + 1);
 #pragma unroll
-      for (int c = 0; c < DIM; ++c) {
-        const T a = srow.p[(int64_t)c * srow.stride];
-        acc = fma(live ? a : T(0), um[c], acc);
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int o = 3 * l + dx + 1;
+        const bool in = in_yz && i + dx >= 0 && i + dx <= g.nx;
+        const int m = row + min(max(i + dx, 0), g.nx);
+        const StencilRow<T> srow = stencil_row<T, DIM>(S, nn, o, d, n, m);
+        const T* um = u + (int64_t)m * DIM;
+        const bool live = o >= Traits<DIM>::CENTER || in;
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) {
+          const T a = srow.p[(int64_t)c * srow.stride];
+          acc = fma(live ? a : T(0), um[c], acc);
+        }
       }
     }
   }
@@ -977,8 +981,27 @@ int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_
   return check_launch();
 }
 
-// Levels with at most this many rows use the split-row kernel.
+// Levels with at most this many rows use the split-row kernel with one x-line per part (9 parts per 3D row);
+// larger levels one row per thread (measured at 64x32x32: 10.1 us per product against 12.4 us with one z-plane
+// of 9 offsets per part and 15.5 us with one x-line per part).
 constexpr int64_t SPLIT_MAX_ROWS = int64_t(1) << 16;
+
+template <typename T, int DIM, int LINES>
+int split_apply(int mode, Grid g, int64_t rows, const T* S, const T* u, const T* b, const T* d, T w, T* y,
+                ChebArgs<T> ch, cudaStream_t st) {
+  using SS = SplitShape<DIM, LINES>;
+  const dim3 blk(32, SS::P, SS::G);
+  const unsigned nb = blocks_for(rows, 32 * SS::G);
+  if (mode == PMG_APPLY_MATVEC)
+    stencil_apply_split_kernel<T, DIM, 0, LINES><<<nb, blk, 0, st>>>(g, S, u, b, d, w, y, ch);
+  else if (mode == PMG_APPLY_RESIDUAL)
+    stencil_apply_split_kernel<T, DIM, 1, LINES><<<nb, blk, 0, st>>>(g, S, u, b, d, w, y, ch);
+  else if (mode == PMG_APPLY_JACOBI)
+    stencil_apply_split_kernel<T, DIM, 2, LINES><<<nb, blk, 0, st>>>(g, S, u, b, d, w, y, ch);
+  else
+    stencil_apply_split_kernel<T, DIM, 3, LINES><<<nb, blk, 0, st>>>(g, S, u, b, d, w, y, ch);
+  return check_launch();
+}
 
 template <typename T, int DIM>
 int stencil_apply_t(int mode, Grid g, const void* S, const void* u, const void* b, const void* diag, double w,
@@ -991,20 +1014,7 @@ int stencil_apply_t(int mode, Grid g, const void* S, const void* u, const void* 
   const T* b_ = (const T*)b;
   const T* d_ = (const T*)diag;
   T* y_ = (T*)y;
-  if (rows <= SPLIT_MAX_ROWS) {
-    using SS = SplitShape<DIM>;
-    const dim3 blk(32, SS::P, SS::G);
-    const unsigned nb = blocks_for(rows, 32 * SS::G);
-    if (mode == PMG_APPLY_MATVEC)
-      stencil_apply_split_kernel<T, DIM, 0><<<nb, blk, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
-    else if (mode == PMG_APPLY_RESIDUAL)
-      stencil_apply_split_kernel<T, DIM, 1><<<nb, blk, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
-    else if (mode == PMG_APPLY_JACOBI)
-      stencil_apply_split_kernel<T, DIM, 2><<<nb, blk, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
-    else
-      stencil_apply_split_kernel<T, DIM, 3><<<nb, blk, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
-    return check_launch();
-  }
+  if (rows <= SPLIT_MAX_ROWS) return split_apply<T, DIM, 1>(mode, g, rows, S_, u_, b_, d_, (T)w, y_, ch, st);
   if (mode == PMG_APPLY_MATVEC)
     stencil_apply_kernel<T, DIM, 0><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
   else if (mode == PMG_APPLY_RESIDUAL)
