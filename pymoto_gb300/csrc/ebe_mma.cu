@@ -24,20 +24,30 @@ constexpr int NMT = (NEMAX + 15) / 16;      // 19 MMA row tiles
 constexpr int EPAD = 324;                   // force row pitch: >= 16*NMT and == 4 (mod 32), conflict-free stores
 constexpr int NTHREADS = 256;
 static_assert(MX * MY <= NTHREADS, "one owned node per thread");
-constexpr int PF = (3 * PLANE + NTHREADS - 1) / NTHREADS;   // u values staged per thread per layer
-constexpr int PFX = (NEMAX + NTHREADS - 1) / NTHREADS;      // x values staged per thread per layer
+constexpr int PFN = (PLANE + NTHREADS - 1) / NTHREADS;     // staged nodes per thread per layer
+constexpr int PFX = (16 * NMT + NTHREADS - 1) / NTHREADS;  // staged x values per thread per layer
 
-// Ring buffers (one barrier per layer): node layer L of u lives in u[(L+1)&3]; element layer L of x in
-// x[(L+1)&1]; the forces of element layer L on its lower 4 nodes (rows 0..11, summed into node layer L) in
-// lo[(L+1)&1], on its upper 4 nodes (rows 12..23, summed into node layer L+1) in hi[(L+1)%3].
+// Ring buffers (one barrier per layer; copies issued two layers ahead with cp.async): node layer L of u lives
+// in u[(L+1)&3] and its constraint-mask words in m[(L+1)&3]; element layer L of x in x[(L+1)&3]; the forces
+// of element layer L on its lower 4 nodes (rows 0..11, summed into node layer L) in lo[(L+1)&1], on its upper
+// 4 nodes (rows 12..23, summed into node layer L+1) in hi[(L+1)%3].
 struct MmaSmem {
   float u[4][3][PLANE];
-  float x[2][16 * NMT];
+  float x[4][16 * NMT];
+  uint32_t m[4][PLANE];        // the aligned 4-byte word of bcmask holding each staged node's mask byte
   float lo[2][12][EPAD];
   float hi[3][12][EPAD];
   int etab[16 * NMT];          // element -> offset of its first node in the staged node tile
   float k0[576];
 };
+
+// 4-byte asynchronous global -> shared copy; src_bytes < 4 zero-fills the rest (0: no global read at all)
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, int src_bytes) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 __device__ __forceinline__ uint32_t to_tf32(float v) {
   uint32_t r;
@@ -115,16 +125,15 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     cz |= ((a >> 2) & 1) << j;
   }
 
-  // staging offsets (layer independent): value q of a node layer -> node (row, cx), component c
-  int gnode[PF], sdst[PF];
+  // staging (layer independent): node slot v of a layer -> tile position (row, cx) and node index in its layer
+  int gnode[PFN], spos[PFN];
 #pragma unroll
-  for (int s = 0; s < PF; ++s) {
-    const int q = tid + s * NTHREADS;
-    const int row = q / (3 * PX), wq = q - row * 3 * PX;
-    const int cx = wq / 3, c = wq - cx * 3;
+  for (int s = 0; s < PFN; ++s) {
+    const int v = tid + s * NTHREADS;
+    const int row = v / PX, cx = v - row * PX;
     const int gi = i0 - 1 + cx, gj = j0 - 1 + row;
-    const bool inside = q < 3 * PLANE && row < nyw + 2 && cx < nxw + 2;
-    sdst[s] = inside ? (c << 16) | (c * PLANE + row * PX + cx) : -1;
+    const bool inside = v < PLANE && row < nyw + 2 && cx < nxw + 2;
+    spos[s] = inside ? row * PX + cx : -1;
     gnode[s] = (inside && gi >= 0 && gi < nnx && gj >= 0 && gj < nny) ? gj * nnx + gi : -1;
   }
   int gelem[PFX];
@@ -147,44 +156,56 @@ __global__ void __launch_bounds__(NTHREADS, 2)
 #pragma unroll
     for (int d = 0; d < 3; ++d) cref[d] = u[n0 * 3 + d];
   }
+  const int64_t nn_total = (int64_t)nnx * nny * nnz;
 
-  float pu[PF];
-  float px[PFX];
-  uint32_t pkeep = 0;   // bit s: value s of the staged layer is a free (unconstrained) dof
-  // loads only: the mask is applied when the staged values are written to shared memory, so that no load
-  // waits for another and all of them are in flight during the element products
-  auto prefetch = [&](int ulay, int xlay) {   // node layer and element layer, relative to kz0
-    const int ku = kz0 + ulay, kx = kz0 + xlay;
+  // copies of node layer L (u and its mask words) and element layer L - 1 (x), relative to kz0, one cp.async
+  // group; nothing is held in registers, so the copies can be issued two layers ahead.  Slots outside the
+  // grid are zero-filled without a global read.
+  auto issue = [&](int L) {
+    const int ku = kz0 + L, kx = kz0 + L - 1;
     const bool uok = ku >= 0 && ku < nnz, xok = kx >= 0 && kx < g.nz;
-    pkeep = 0;
+    const int ub = (L + 1) & 3;
 #pragma unroll
-    for (int s = 0; s < PF; ++s) {
-      float v = 0.f;
-      if (uok && gnode[s] >= 0) {
-        const int64_t m = ku * nlayer + gnode[s];
-        const int c = sdst[s] >> 16;
-        const uint8_t msk = bcmask ? bcmask[m] : 0;
-        v = u[m * 3 + c];
-        pkeep |= (uint32_t)(((msk >> c) & 1) ^ 1) << s;
+    for (int s = 0; s < PFN; ++s) {
+      if (spos[s] < 0) continue;
+      const bool live = uok && gnode[s] >= 0;
+      const int64_t m = live ? ku * nlayer + gnode[s] : 0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) cp_async4(&S.u[ub][c][spos[s]], u + m * 3 + c, live ? 4 : 0);
+      if (bcmask) {
+        const int64_t w = m & ~int64_t(3);    // aligned word holding the mask byte of node m
+        const int64_t left = nn_total - w;
+        const int bytes = live ? (left < 4 ? (int)left : 4) : 0;
+        cp_async4(&S.m[ub][spos[s]], bcmask + w, bytes);
       }
-      pu[s] = v;
     }
-#pragma unroll
-    for (int s = 0; s < PFX; ++s) px[s] = (xok && gelem[s] >= 0) ? xe[(int64_t)kx * g.nx * g.ny + gelem[s]] : 0.f;
-  };
-  auto commit = [&](int ubuf, int xbuf) {
-#pragma unroll
-    for (int s = 0; s < PF; ++s)
-      if (sdst[s] >= 0) {
-        const int c = sdst[s] >> 16;
-        const float r = c == 0 ? cref[0] : (c == 1 ? cref[1] : cref[2]);
-        Su[ubuf * 3 * PLANE + (sdst[s] & 0xffff)] = (((pkeep >> s) & 1) ? pu[s] : 0.f) - r;
-      }
-    if (xbuf < 0) return;
 #pragma unroll
     for (int s = 0; s < PFX; ++s) {
       const int e = tid + s * NTHREADS;
-      if (e < 16 * NMT) S.x[xbuf][e] = px[s];
+      if (e >= 16 * NMT) continue;
+      const bool live = xok && gelem[s] >= 0;
+      cp_async4(&S.x[(L) & 3][e], xe + (live ? (int64_t)kx * g.nx * g.ny + gelem[s] : 0), live ? 4 : 0);
+    }
+    cp_async_commit();
+  };
+  // after this thread's copies of node layer L have landed: zero its constrained dofs and apply the shift
+  // (run by the issuing thread before the barrier that publishes the layer)
+  auto fixup = [&](int L) {
+    const int ub = (L + 1) & 3;
+    const int ku = kz0 + L;
+#pragma unroll
+    for (int s = 0; s < PFN; ++s) {
+      if (spos[s] < 0) continue;
+      unsigned keep = 7u;
+      if (bcmask && gnode[s] >= 0 && ku >= 0 && ku < nnz) {
+        const int64_t m = ku * nlayer + gnode[s];
+        keep = ~(S.m[ub][spos[s]] >> (8 * (int)(m & 3))) & 7u;
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float* p = &S.u[ub][c][spos[s]];
+        *p = (((keep >> c) & 1u) ? *p : 0.f) - cref[c];
+      }
     }
   };
 
@@ -293,21 +314,25 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     }
   };
 
-  // prologue: node layers -1 and 0, element layer -1
-  prefetch(-1, -1);
-  commit(0, 0);
-  prefetch(0, -1);
-  commit(1, -1);
+  // prologue: node layers -1, 0 (and element layer -1) ready, node layer 1 in flight
+  issue(-1);
+  issue(0);
+  issue(1);
+  cp_async_wait1();
+  fixup(-1);
+  fixup(0);
   __syncthreads();
   element_layer(0, 1, 0, 0, 0);
-  prefetch(1, 0);
+  issue(2);
 
   for (int t = 0; t < nlay; ++t) {
-    commit((t + 2) & 3, (t + 1) & 1);   // node layer t+1, element layer t
+    cp_async_wait1();                   // node layer t+1 and element layer t have landed (t+2 may be in flight)
+    fixup(t + 1);
     __syncthreads();
-    if (t + 1 < nlay) prefetch(t + 2, t + 1);
+    if (t + 3 <= nlay) issue(t + 3);
+    else cp_async_commit();             // empty group: keeps the wait counts uniform
     if (t >= 1) node_operands(t - 1);
-    element_layer((t + 1) & 3, (t + 2) & 3, (t + 1) & 1, (t + 1) & 1, (t + 1) % 3);
+    element_layer((t + 1) & 3, (t + 2) & 3, (t + 1) & 3, (t + 1) & 1, (t + 1) % 3);
     if (t >= 1) node_layer(t - 1, t & 1, (t - 1) % 3);
   }
   node_operands(nlay - 1);
@@ -329,6 +354,10 @@ int ebe_apply_mma_f32(int mode, Grid g, const float* xe, const double* K0, const
     int v = 0;
     cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
     sm_count[dev] = v > 0 ? v : 1;
+  }
+  if (bcmask && (reinterpret_cast<uintptr_t>(bcmask) & 3u)) {   // the mask is copied in aligned 4-byte words
+    set_error("ebe_apply_mma_f32: bcmask must be 4-byte aligned");
+    return PMG_BAD_ARG;
   }
   const size_t smem = sizeof(MmaSmem);
   const int tx = (g.nx + 1 + MX - 1) / MX, ty = (g.ny + 1 + MY - 1) / MY;
