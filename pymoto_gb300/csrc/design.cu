@@ -365,6 +365,19 @@ __device__ __forceinline__ double oc_exact_value(double xi, double gi, double sc
   return fmin(fmax(xi * sqrt(-g) * sc, lb), ub);
 }
 
+// The same value from t = x sqrt(-min(dg, 0)) computed once (identical operations, identical result).
+__device__ __forceinline__ double oc_exact_value_t(double xi, double ti, double sc, double move, double xmin,
+                                                   double xmax) {
+  const double lb = fmax(xmin, xi - move), ub = fmin(xmax, xi + move);
+  return fmin(fmax(ti * sc, lb), ub);
+}
+
+__device__ __forceinline__ float oc_warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
 __global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, const double* __restrict__ x,
                                                                    const double* __restrict__ dg,
                                                                    double* __restrict__ xnew, double target,
@@ -380,16 +393,20 @@ __global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, co
   const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float t32[OCP_PER_THREAD], lo32[OCP_PER_THREAD], hi32[OCP_PER_THREAD];
+  double t64[OCP_PER_THREAD], x64[OCP_PER_THREAD];   // x sqrt(-g) and x in FP64: no FP64 sqrt per pass
 #pragma unroll
   for (int k = 0; k < OCP_PER_THREAD; ++k) {
     const int64_t i = i0 + k * stride;
     if (i < n) {
       const double g = dg[i] < 0.0 ? dg[i] : 0.0;
       const double xv = x[i];
-      t32[k] = (float)(xv * sqrt(-g));
+      t64[k] = xv * sqrt(-g);
+      x64[k] = xv;
+      t32[k] = (float)t64[k];
       lo32[k] = (float)fmax(xmin, xv - move);
       hi32[k] = (float)fmin(xmax, xv + move);
     } else {
+      t64[k] = x64[k] = 0.0;
       t32[k] = lo32[k] = hi32[k] = 0.f;
     }
   }
@@ -430,12 +447,13 @@ __global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, co
 #pragma unroll
         for (int j = 0; j < OC_CAND; ++j) acc[j] += fminf(fmaxf(t32[k] * s_sc[j], lo32[k]), hi32[k]);
       }
-      // block sums in FP64: warp shuffles, then the warps in order
+      // warp sums in FP32 (FP64 shuffles and adds would make the pass FP64-bound on GB300; their rounding is
+      // in the margin), then the warps of the CTA in FP64, in order
       __shared__ double s_wsum[OC_THREADS / 32][OC_CAND];
 #pragma unroll
       for (int j = 0; j < OC_CAND; ++j) {
-        const double v = oc_warp_sum((double)acc[j]);
-        if (lane == 0) s_wsum[warp][j] = v;
+        const float v = oc_warp_sum_f(acc[j]);
+        if (lane == 0) s_wsum[warp][j] = (double)v;
       }
       __syncthreads();
       if (threadIdx.x < ncand) {
@@ -450,7 +468,7 @@ __global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, co
 #pragma unroll
       for (int k = 0; k < OCP_PER_THREAD; ++k) {
         const int64_t i = i0 + k * stride;
-        if (i < n) acc += oc_exact_value(x[i], dg[i], sc, move, xmin, xmax);
+        if (i < n) acc += oc_exact_value_t(x64[k], t64[k], sc, move, xmin, xmax);
       }
       acc = oc_block_sum(acc);
       if (threadIdx.x == 0) vs->partial[blockIdx.x] = acc;
@@ -545,7 +563,7 @@ __global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, co
 #pragma unroll
   for (int k = 0; k < OCP_PER_THREAD; ++k) {
     const int64_t i = i0 + k * stride;
-    if (i < n) xnew[i] = oc_exact_value(x[i], dg[i], sc, move, xmin, xmax);
+    if (i < n) xnew[i] = oc_exact_value_t(x64[k], t64[k], sc, move, xmin, xmax);
   }
 }
 
@@ -707,12 +725,14 @@ int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, do
     const int cb = coop_blocks[dev];
     if (cb > 0 && n <= (int64_t)cb * OC_THREADS * OCP_PER_THREAD) {
       const int grid = cb;   // all co-resident slots: the fewest elements per thread
-      // bound of the FP32 error of a candidate volume: per element 3 roundings of a value up to M, plus the
-      // FP32 sum of at most OCP_PER_THREAD values per thread (each addition off by <= u32 * OCP_PER_THREAD * M,
-      // at most one addition per element; the sums over threads are FP64); doubled for safety
+      // bound of the FP32 error of a candidate volume: per element 3 roundings of a value up to M, the FP32
+      // sum of at most OCP_PER_THREAD values per thread (each addition off by <= u32 * OCP_PER_THREAD * M, at
+      // most one addition per element), and the 5 levels of the FP32 warp sum (each level off by u32 times the
+      // partial sums, at most 32 * OCP_PER_THREAD * M per lane pair: <= 5 u32 M per element in total); the
+      // sums over warps and CTAs are FP64; doubled for safety
       const double M = std::max({1.0, std::fabs(xmin), std::fabs(xmax)});
       const double u32 = std::ldexp(1.0, -24);
-      const double margin = 2.0 * (3.0 + OCP_PER_THREAD) * (double)n * u32 * M;
+      const double margin = 2.0 * (3.0 + OCP_PER_THREAD + 5.0) * (double)n * u32 * M;
       void* args[] = {(void*)&n, (void*)&x, (void*)&dg, (void*)&xnew, (void*)&target, (void*)&move,
                       (void*)&xmin, (void*)&xmax, (void*)&margin, (void*)&s};
       cudaError_t e = cudaLaunchCooperativeKernel((const void*)oc_persistent_kernel, dim3(grid), dim3(OC_THREADS),
