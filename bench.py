@@ -397,8 +397,9 @@ def cpu_reference_sample(shape, warm_steps=1, budget_s=None):
 
 
 def operator_case(args):
-    """Level-0 products of the workload alone: FP32 tensor-core operator (residual mode), FP64 stencil
-    product; 3 launches each after 2 warm-up launches, CUDA-event times printed as JSON."""
+    """Operator products of the workload alone: FP32 tensor-core operator (residual mode), FP64 stencil
+    product, FP32 level-1 stencil residual; 3 launches each after 2 warm-up launches, CUDA-event times
+    printed as JSON (a small case for ncu)."""
     import torch
     import pymoto_gb300 as pg
     from pymoto_gb300._lib import F32, F64, RESIDUAL, MATVEC
@@ -410,9 +411,13 @@ def operator_case(args):
     K32 = K.astype(F32)
     u = torch.randn(K.grid.ndof, dtype=torch.float64, device="cuda")
     u32, b32 = u.float(), torch.randn_like(u.float())
+    A1 = K32.galerkin()            # level 1 (FP32 Galerkin stencils, half-symmetric)
+    u1 = torch.randn(A1.grid.ndof, device="cuda")
+    b1 = torch.randn_like(u1)
     out = {}
     for name, fn in [("ebe_apply_mma_f32_residual", lambda: K32.apply(RESIDUAL, u32, b32)),
-                     ("stencil_apply_f64_matvec", lambda: K.apply(MATVEC, u))]:
+                     ("stencil_apply_f64_matvec", lambda: K.apply(MATVEC, u)),
+                     ("stencil_apply_f32_level1_residual", lambda: A1.apply(RESIDUAL, u1, b1))]:
         for _ in range(2):
             fn()
         torch.cuda.synchronize()

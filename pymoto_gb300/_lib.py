@@ -141,7 +141,7 @@ def load():
 def _arg(a):
     if a is None:
         return None
-    if isinstance(a, torch.Tensor):
+    if type(a) is torch.Tensor or isinstance(a, torch.Tensor):
         return a.data_ptr()
     if isinstance(a, np.ndarray):
         return a.ctypes.data
@@ -231,10 +231,15 @@ def replay(key, graph, launches):
         graph.replay()
 
 
+_fns = {}
+
+
 def call(name, *args):
     """Call a C-ABI function; raise PMGError on a non-zero status."""
-    lib = load()
-    fn = getattr(lib, name)
+    fn = _fns.get(name)
+    if fn is None:
+        fn = _fns[name] = getattr(load(), name)
+    lib = _lib
     pr = Probe.active
     if pr is not None:
         pr.launches += _launches(name, args)
@@ -262,8 +267,16 @@ def call(name, *args):
     return rc
 
 
+_raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+_cur_device = getattr(torch._C, "_cuda_getDevice", None)
+
+
 def stream():
-    """Handle of the current torch CUDA stream (all library calls are ordered on it)."""
+    """Handle of the current torch CUDA stream (all library calls are ordered on it).  Read through torch's
+    raw-handle accessor where it exists: torch.cuda.current_stream() builds a Stream object per call, which
+    is most of the host cost of a small library call."""
+    if _raw_stream is not None and _cur_device is not None:
+        return _raw_stream(_cur_device())
     return torch.cuda.current_stream().cuda_stream
 
 

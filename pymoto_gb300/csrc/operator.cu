@@ -260,9 +260,12 @@ __device__ __forceinline__ T stencil_coef(const T* __restrict__ S, int nn, int o
   return (o >= Traits<DIM>::CENTER || in) ? v : T(0);
 }
 
-// One thread per (component d, node n), d slowest so that the stencil loads of a warp are coalesced.
+// One thread per (component d, node n), d slowest so that the stencil loads of a warp are coalesced.  The
+// bound of 4 CTAs per SM caps the registers at 64: enough to keep most of a row's 162 loads in flight (without
+// it the compiler settles at 32 registers and the level-1 product waits on each load: 10.2 vs 8.8 us at
+// 64x32x32; with 2 CTAs per SM the FP64 level-0 product loses occupancy: 265 vs 225 us).
 template <typename T, int DIM, int MODE>
-__global__ void __launch_bounds__(256) stencil_apply_kernel(Grid g, const T* __restrict__ S, const T* __restrict__ u,
+__global__ void __launch_bounds__(256, 4) stencil_apply_kernel(Grid g, const T* __restrict__ S, const T* __restrict__ u,
                                                             const T* __restrict__ b, const T* __restrict__ diag, T w,
                                                             T* __restrict__ y, ChebArgs<T> ch) {
   constexpr int NOFF = Traits<DIM>::NOFF;
