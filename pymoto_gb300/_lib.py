@@ -161,8 +161,7 @@ def _launches(name, args):
     if name in _HOST_ONLY:
         return 0
     if name == "pmg_cholesky_factor":
-        nblk = (int(args[0]) + 31) // 32
-        return 3 * nblk - 2 if int(args[2]) > 0 else nblk
+        return 1          # one thread-block cluster for the whole factorisation
     if name == "pmg_cholesky_inverse_f32":
         return 4
     if name == "pmg_galerkin_from_ebe":

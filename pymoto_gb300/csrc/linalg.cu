@@ -343,13 +343,14 @@ constexpr int CHOL_THREADS = 256;
 // GPU whose FP64 rate (1/64 of FP32 on GB300) is the limit here.  The Cholesky factor L_unit sqrt(D) is
 // written at the end, the square roots of all pivots taken together.  A non-positive pivot is recorded in
 // *info and replaced by 1 so the sweep stays finite.
-__global__ void __launch_bounds__(CHOL_THREADS) chol_diag_kernel(int n, double* A, int kb, int* info) {
+__device__ void chol_diag_tile(int n, double* A, int kb, int* info) {
   __shared__ double T[TB][TB + 1];
   __shared__ double ucol[TB];   // column k before scaling (d_k l_rk)
   __shared__ double dpiv[TB];
   const int k0 = kb * TB;
   const int nb = min(TB, n - k0);
   const int lane = threadIdx.x & 31;
+  __syncthreads();              // the shared tile may still be read by a previous call of this CTA
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
     const int r = e / TB, c = e % TB;
     T[r][c] = (r < nb && c < nb) ? A[(int64_t)(k0 + r) * n + k0 + c] : (r == c ? 1.0 : 0.0);
@@ -394,14 +395,19 @@ __global__ void __launch_bounds__(CHOL_THREADS) chol_diag_kernel(int n, double* 
   }
 }
 
+__global__ void __launch_bounds__(CHOL_THREADS) chol_diag_kernel(int n, double* A, int kb, int* info) {
+  chol_diag_tile(n, A, kb, info);
+}
+
 // Panel: L[i, kb] = A[i, kb] L[kb,kb]^{-T} for the rows i below the diagonal tile within the band, one warp
 // per row (lane c holds entry c; forward substitution with the reciprocal pivots, broadcast by shuffles).
 constexpr int PANEL_WARPS = 8;
-__global__ void __launch_bounds__(PANEL_WARPS * 32) chol_panel_kernel(int n, double* A, int kb, int bw) {
+__device__ void chol_panel_block(int n, double* A, int kb, int bw, int blk) {
   __shared__ double L[TB][TB + 1];
   __shared__ double rp[TB];
   const int k0 = kb * TB;
   const int nb = min(TB, n - k0);
+  __syncthreads();
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
     const int r = e / TB, c = e % TB;
     L[r][c] = (r < nb && c < nb && c <= r) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
@@ -410,7 +416,7 @@ __global__ void __launch_bounds__(PANEL_WARPS * 32) chol_panel_kernel(int n, dou
   if (threadIdx.x < TB) rp[threadIdx.x] = threadIdx.x < nb ? recip_newton(L[threadIdx.x][threadIdx.x]) : 0.0;
   __syncthreads();
   const int lane = threadIdx.x & 31;
-  const int row = k0 + nb + blockIdx.x * PANEL_WARPS + (threadIdx.x >> 5);
+  const int row = k0 + nb + blk * PANEL_WARPS + (threadIdx.x >> 5);
   if (row >= n || row - (k0 + nb - 1) > bw) return;   // whole warps exit together
   double x = lane < nb ? A[(int64_t)row * n + k0 + lane] : 0.0;
   for (int c = 0; c < nb; ++c) {
@@ -421,19 +427,23 @@ __global__ void __launch_bounds__(PANEL_WARPS * 32) chol_panel_kernel(int n, dou
   if (lane < nb) A[(int64_t)row * n + k0 + lane] = x;
 }
 
+__global__ void __launch_bounds__(PANEL_WARPS * 32) chol_panel_kernel(int n, double* A, int kb, int bw) {
+  chol_panel_block(n, A, kb, bw, blockIdx.x);
+}
+
 // Trailing update A[i][j] -= sum_q L[i][k0+q] L[j][k0+q] over the rows/columns below the diagonal tile within
 // the band (j <= i), one 16 x 16 output tile per CTA (one element per thread).
 constexpr int UT = 16;
-__global__ void __launch_bounds__(UT * UT) chol_update_kernel(int n, double* A, int kb, int bw, int nt) {
+__device__ void chol_update_tile(int n, double* A, int kb, int bw, int nt, int t) {
   __shared__ double Li[UT][TB + 1];
   __shared__ double Lj[UT][TB + 1];
   const int k0 = kb * TB;
   const int nb = min(TB, n - k0);
   const int base = k0 + nb;
   const int last = min(n - 1, k0 + nb - 1 + bw);   // last row with a nonzero in this block column
+  __syncthreads();
   // lower-triangular tile enumeration: t -> (ti, tj), tj <= ti
-  const int t = blockIdx.x;
-  int ti = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+  int ti = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
   while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
   while (ti * (ti + 1) / 2 > t) --ti;
   const int tj = t - ti * (ti + 1) / 2;
@@ -454,6 +464,42 @@ __global__ void __launch_bounds__(UT * UT) chol_update_kernel(int n, double* A, 
 #pragma unroll 8
   for (int q = 0; q < TB; ++q) s = fma(Li[r][q], Lj[c][q], s);
   A[(int64_t)row * n + col] -= s;
+}
+
+__global__ void __launch_bounds__(UT * UT) chol_update_kernel(int n, double* A, int kb, int bw, int nt) {
+  chol_update_tile(n, A, kb, bw, nt, blockIdx.x);
+}
+
+// The whole banded factorisation in one launch: one thread-block cluster of CHOL_CLUSTER CTAs steps through
+// the tile columns (diagonal tile on CTA 0, panel rows and trailing-update tiles spread over the cluster),
+// separated by the hardware cluster barrier (release/acquire, so the global writes of one phase are visible
+// to the next).  One launch instead of three per tile column: on a busy GPU every launch waits for a free
+// CTA slot, which made the 66 launches of the 675-dof factorisation take milliseconds behind a solve.
+constexpr int CHOL_CLUSTER = 8;
+static_assert(CHOL_THREADS == PANEL_WARPS * 32 && CHOL_THREADS == UT * UT, "one block size for all phases");
+
+__device__ __forceinline__ void cluster_sync_all() {
+  __threadfence();
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+__global__ void __cluster_dims__(CHOL_CLUSTER, 1, 1) __launch_bounds__(CHOL_THREADS)
+    chol_cluster_kernel(int n, double* A, int bw, int* info) {
+  const int rank = blockIdx.x;   // the grid is one cluster
+  const int nblk = (n + TB - 1) / TB;
+  for (int kb = 0; kb < nblk; ++kb) {
+    if (rank == 0) chol_diag_tile(n, A, kb, info);
+    cluster_sync_all();
+    const int k0 = kb * TB, nb = min(TB, n - k0);
+    const int rows = min(n - (k0 + nb), bw);
+    if (rows <= 0) continue;     // uniform: the last tile column
+    const int pblocks = (rows + PANEL_WARPS - 1) / PANEL_WARPS;
+    for (int pb = rank; pb < pblocks; pb += CHOL_CLUSTER) chol_panel_block(n, A, kb, bw, pb);
+    cluster_sync_all();
+    const int nt = (rows + UT - 1) / UT;
+    for (int t = rank; t < nt * (nt + 1) / 2; t += CHOL_CLUSTER) chol_update_tile(n, A, kb, bw, nt, t);
+    cluster_sync_all();
+  }
 }
 
 // Inverses of the diagonal tiles of the factor, for the blocked triangular solves: Dinv[b] = L[b,b]^{-1}
@@ -977,6 +1023,19 @@ int pmg_cholesky_factor(int n, double* A, int bw, int* info, void* stream) {
   if (e != cudaSuccess) {
     set_error(cudaGetErrorString(e));
     return PMG_CUDA_ERR;
+  }
+  static int cluster_ok[64] = {0};   // 0 unknown, 1 yes, -1 no
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) {
+    if (cluster_ok[dev] == 0) {
+      int v = 0;
+      cudaDeviceGetAttribute(&v, cudaDevAttrClusterLaunch, dev);
+      cluster_ok[dev] = v ? 1 : -1;
+    }
+    if (cluster_ok[dev] > 0) {
+      chol_cluster_kernel<<<CHOL_CLUSTER, CHOL_THREADS, 0, st>>>(n, A, bw, info);
+      return check_launch();
+    }
   }
   const int nblk = (n + TB - 1) / TB;
   for (int kb = 0; kb < nblk; ++kb) {
