@@ -39,7 +39,9 @@ class Signal:
         if ds is None:
             return self
         if self.sensitivity is None:
-            self.sensitivity = copy.deepcopy(ds)
+            clone = getattr(ds, "clone", None)
+            # a device tensor is copied with clone() (deepcopy takes the slow Python-level path for the same copy)
+            self.sensitivity = clone() if callable(clone) else copy.deepcopy(ds)
         elif hasattr(self.sensitivity, "add_sensitivity"):
             self.sensitivity.add_sensitivity(ds)
         else:

@@ -235,12 +235,13 @@ __global__ void __launch_bounds__(NTHREADS, 2)
           ah[2 * h + 1] = to_tf32(v1);                                   // a1 / a3: row gid + 8
           al[2 * h + 1] = __float_as_uint(v1 - __uint_as_float(ah[2 * h + 1]));
         }
+        // consecutive MMAs go to different accumulators (dependency distance 3, not 1); small terms first
 #pragma unroll
-        for (int nt = 0; nt < 3; ++nt) {
-          mma_tf32(c[nt], al, bh[ks][nt][0], bh[ks][nt][1]);
-          mma_tf32(c[nt], ah, bl[ks][nt][0], bl[ks][nt][1]);
-          mma_tf32(c[nt], ah, bh[ks][nt][0], bh[ks][nt][1]);
-        }
+        for (int nt = 0; nt < 3; ++nt) mma_tf32(c[nt], al, bh[ks][nt][0], bh[ks][nt][1]);
+#pragma unroll
+        for (int nt = 0; nt < 3; ++nt) mma_tf32(c[nt], ah, bl[ks][nt][0], bl[ks][nt][1]);
+#pragma unroll
+        for (int nt = 0; nt < 3; ++nt) mma_tf32(c[nt], ah, bh[ks][nt][0], bh[ks][nt][1]);
       }
       const float x0 = S.x[xbuf][e0], x1 = S.x[xbuf][e1];
 #pragma unroll

@@ -237,7 +237,9 @@ class DeviceDyad:
         return self
 
     def __deepcopy__(self, memo):
-        return DeviceDyad([x.clone() for x in self.u], [x.clone() for x in self.v], self.shape)
+        # new term lists, shared vectors: a dyad only ever grows by new terms and is scaled out of place
+        # (__imul__), so its vectors are never written through it
+        return DeviceDyad(list(self.u), list(self.v), self.shape)
 
     def todense(self):
         return sum(torch.outer(a, b) for a, b in zip(self.u, self.v))
