@@ -502,13 +502,15 @@ class GeometricMultigrid(Preconditioner):
                   coarse_smooth_steps=None, smoother="jacobi", cheb_ratio=10.0, coarse_lag=False):
         """Chain of GeometricMultigrid levels as ex_compliance_multigrid.py:108-121 builds it.  With
         levels=None, coarsen while the grid halves evenly and the coarse level has > max_coarse_dofs.
-        `coarse_smooth_steps` (default: smooth_steps) applies to every level below the finest.
+        `coarse_smooth_steps` (default: smooth_steps) applies to every level below the finest; a list gives
+        the levels below the finest their own values (the last entry repeats).
         smoother="chebyshev" replaces the damped-Jacobi sweeps by a Chebyshev smoother of degree
         smooth_steps (coarse_smooth_steps below the finest level) on [lmax/cheb_ratio, lmax].
         coarse_lag=True: the coarsest direct solve of an FP32 hierarchy keeps using the inverse of the previous
         update's coarse matrix until the current one is factorised (see DenseCholesky; MixedPrecisionCG
         switches to the new inverse between two iterations as soon as it exists)."""
         css = smooth_steps if coarse_smooth_steps is None else coarse_smooth_steps
+        css_of = (lambda i: css[min(i, len(css) - 1)]) if isinstance(css, (list, tuple)) else (lambda i: css)
         if smoother not in ("jacobi", "chebyshev"):
             raise ValueError("smoother must be 'jacobi' or 'chebyshev'")
 
@@ -527,7 +529,8 @@ class GeometricMultigrid(Preconditioner):
                 break
             if not g.can_coarsen():
                 raise ValueError(f"cannot build {levels} levels: grid {g.dims} does not halve evenly")
-            mgs.append(cls(sub, smoother=make(css), smooth_steps=css, precision=precision))
+            steps = css_of(len(mgs) - 1)
+            mgs.append(cls(sub, smoother=make(steps), smooth_steps=steps, precision=precision))
             mgs[-2].inner_level = mgs[-1]
         if coarse_lag:
             mgs[-1].inner_level = DenseCholesky(lag=True)
