@@ -67,3 +67,24 @@ def test_module_added_to_active_networks_once():
 
 def test_constant_inputs_give_plain_values():
     assert Square()(3.0) == 9.0
+
+
+def test_add_sensitivity_copies_tensors_with_clone():
+    """A tensor's first contribution is copied (clone), so later in-place accumulation leaves the producer's
+    tensor untouched."""
+    torch = pytest.importorskip("torch")
+    s = G.Signal("s")
+    first = torch.ones(4)
+    s.add_sensitivity(first)
+    s.add_sensitivity(torch.ones(4))
+    assert torch.equal(s.sensitivity, torch.full((4,), 2.0)) and torch.equal(first, torch.ones(4))
+
+
+def test_hierarchy_per_level_coarse_smoothing():
+    """coarse_smooth_steps as a list: one value per level below the finest, the last one repeated."""
+    import pymoto_gb300 as pg
+    d = pg.VoxelDomain(32, 16, 16)
+    mgs = pg.GeometricMultigrid.hierarchy(d, levels=5, smooth_steps=1, coarse_smooth_steps=[2, 3],
+                                          smoother="chebyshev")
+    assert [m.smooth_steps for m in mgs] == [1, 2, 3, 3]
+    assert [m.smoother.degree for m in mgs] == [1, 2, 3, 3]
