@@ -424,18 +424,20 @@ __global__ void __launch_bounds__(256) stencil_rowabs_kernel(Grid g, const T* __
 // weight of a fine node at signed offset a (in fine units) from a coarse node: 1 at 0, 1/2 at +-1
 __device__ __forceinline__ double tw(int a) { return a == 0 ? 1.0 : 0.5; }
 
-// rc = R^T rf: one thread per (component d, coarse node N), gathering the 3^dim fine neighbours of the
-// coarse node with branch-free clamped loads (weight zero outside the grid).
+// rc = R^T rf: one thread per coarse node N (all DIM components: one set of index arithmetic, contiguous
+// component loads), gathering the 3^dim fine neighbours of the coarse node with branch-free clamped loads
+// (weight zero outside the grid).
 template <typename T, int DIM>
 __global__ void __launch_bounds__(256) restrict_kernel(Grid gf, const T* __restrict__ rf, T* __restrict__ rc) {
   const Grid gc = gf.coarse();
   const int ncn = (int)gc.nnodes();
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncn * DIM) return;
-  const int d = t / ncn, N = t - d * ncn;
+  const int N = blockIdx.x * blockDim.x + threadIdx.x;
+  if (N >= ncn) return;
   int I, J, K;
   node_ijk(gc, N, I, J, K);
-  T acc = T(0);
+  T acc[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) acc[d] = T(0);
 #pragma unroll
   for (int c = (DIM == 3 ? -1 : 0); c <= (DIM == 3 ? 1 : 0); ++c)
 #pragma unroll
@@ -446,20 +448,22 @@ __global__ void __launch_bounds__(256) restrict_kernel(Grid gf, const T* __restr
         const bool in = i >= 0 && i <= gf.nx && j >= 0 && j <= gf.ny && k >= 0 && k <= gf.nz;
         const T wgt = in ? (T)(tw(a) * tw(bb) * tw(c)) : T(0);
         const int m = (min(max(k, 0), gf.nz) * (gf.ny + 1) + min(max(j, 0), gf.ny)) * (gf.nx + 1) + min(max(i, 0), gf.nx);
-        acc = fma(wgt, rf[(int64_t)m * DIM + d], acc);
+        const T* src = rf + (int64_t)m * DIM;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) acc[d] = fma(wgt, src[d], acc[d]);
       }
-  rc[(int64_t)N * DIM + d] = acc;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) rc[(int64_t)N * DIM + d] = acc[d];
 }
 
-// uf += R uc: one thread per (component d, fine node n); the 2^dim candidate parents are read at clamped
-// indices with weight zero where a parent does not exist (even coordinate).
+// uf += R uc: one thread per fine node n (all DIM components); the 2^dim candidate parents are read at
+// clamped indices with weight zero where a parent does not exist (even coordinate).
 template <typename T, int DIM>
 __global__ void __launch_bounds__(256) prolong_add_kernel(Grid gf, const T* __restrict__ uc, T* __restrict__ uf) {
   const Grid gc = gf.coarse();
   const int nfn = (int)gf.nnodes();
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nfn * DIM) return;
-  const int d = t / nfn, n = t - d * nfn;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nfn) return;
   int i, j, k;
   node_ijk(gf, n, i, j, k);
   const int i0 = i >> 1, j0 = j >> 1, k0 = k >> 1;
@@ -468,18 +472,19 @@ __global__ void __launch_bounds__(256) prolong_add_kernel(Grid gf, const T* __re
   const T wy0 = (j & 1) ? T(0.5) : T(1), wy1 = (j & 1) ? T(0.5) : T(0);
   const T wz0 = (DIM == 3 && (k & 1)) ? T(0.5) : T(1), wz1 = (DIM == 3 && (k & 1)) ? T(0.5) : T(0);
   const int cx = gc.nx + 1, cxy = (gc.nx + 1) * (gc.ny + 1);
-  T acc = T(0);
-  acc = fma(wz0 * wy0 * wx0, uc[(int64_t)(k0 * cxy + j0 * cx + i0) * DIM + d], acc);
-  acc = fma(wz0 * wy0 * wx1, uc[(int64_t)(k0 * cxy + j0 * cx + i1) * DIM + d], acc);
-  acc = fma(wz0 * wy1 * wx0, uc[(int64_t)(k0 * cxy + j1 * cx + i0) * DIM + d], acc);
-  acc = fma(wz0 * wy1 * wx1, uc[(int64_t)(k0 * cxy + j1 * cx + i1) * DIM + d], acc);
-  if (DIM == 3) {
-    acc = fma(wz1 * wy0 * wx0, uc[(int64_t)(k1 * cxy + j0 * cx + i0) * DIM + d], acc);
-    acc = fma(wz1 * wy0 * wx1, uc[(int64_t)(k1 * cxy + j0 * cx + i1) * DIM + d], acc);
-    acc = fma(wz1 * wy1 * wx0, uc[(int64_t)(k1 * cxy + j1 * cx + i0) * DIM + d], acc);
-    acc = fma(wz1 * wy1 * wx1, uc[(int64_t)(k1 * cxy + j1 * cx + i1) * DIM + d], acc);
+  const int par[8] = {k0 * cxy + j0 * cx + i0, k0 * cxy + j0 * cx + i1, k0 * cxy + j1 * cx + i0,
+                      k0 * cxy + j1 * cx + i1, k1 * cxy + j0 * cx + i0, k1 * cxy + j0 * cx + i1,
+                      k1 * cxy + j1 * cx + i0, k1 * cxy + j1 * cx + i1};
+  const T wgt[8] = {wz0 * wy0 * wx0, wz0 * wy0 * wx1, wz0 * wy1 * wx0, wz0 * wy1 * wx1,
+                    wz1 * wy0 * wx0, wz1 * wy0 * wx1, wz1 * wy1 * wx0, wz1 * wy1 * wx1};
+  T* dst = uf + (int64_t)n * DIM;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    T acc = T(0);
+#pragma unroll
+    for (int p = 0; p < (DIM == 3 ? 8 : 4); ++p) acc = fma(wgt[p], uc[(int64_t)par[p] * DIM + d], acc);
+    dst[d] += acc;
   }
-  uf[(int64_t)n * DIM + d] += acc;
 }
 
 // ------------------------------------------------------------------------------------------ Galerkin
@@ -1171,7 +1176,7 @@ int pmg_restrict(int dtype, int nelx, int nely, int nelz, const void* rf, void* 
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !even_grid(nelx, nely, nelz) || !rf || !rc) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
   PMG_DISPATCH(dtype, g.dim(),
-               (launch_simple<T, DIM>(restrict_kernel<T, DIM>, g.coarse().nnodes() * DIM, as_stream(stream), g,
+               (launch_simple<T, DIM>(restrict_kernel<T, DIM>, g.coarse().nnodes(), as_stream(stream), g,
                                       (const T*)rf, (T*)rc)));
 }
 
@@ -1179,7 +1184,7 @@ int pmg_prolong_add(int dtype, int nelx, int nely, int nelz, const void* uc, voi
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !even_grid(nelx, nely, nelz) || !uc || !uf) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
   PMG_DISPATCH(dtype, g.dim(),
-               (launch_simple<T, DIM>(prolong_add_kernel<T, DIM>, g.nnodes() * DIM, as_stream(stream), g,
+               (launch_simple<T, DIM>(prolong_add_kernel<T, DIM>, g.nnodes(), as_stream(stream), g,
                                       (const T*)uc, (T*)uf)));
 }
 
