@@ -83,7 +83,7 @@ class DesignRun:
     """The network of the workload on the device, for one solver arm."""
 
     opts = {"inner_iters": 4, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None,
-            "smoother": "chebyshev", "cheb_degree": 1, "cheb_coarse_degree": [2, 3, 6], "cheb_ratio": 10.0,
+            "smoother": "chebyshev", "cheb_degree": 1, "cheb_coarse_degree": [2, 3, 6], "cheb_ratio": 15.0,
             "learned_train_steps": 1, "learned_stride": 4, "learned_lr": 2e-3, "learned_net": True,
             "learned_history": 1, "coarse_lag": True}
 
