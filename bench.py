@@ -85,7 +85,8 @@ class DesignRun:
     opts = {"inner_iters": 4, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None,
             "smoother": "chebyshev", "cheb_degree": 1, "cheb_coarse_degree": [2, 3, 6], "cheb_ratio": 15.0,
             "learned_train_steps": 1, "learned_stride": 4, "learned_lr": 2e-3, "learned_net": True,
-            "learned_history": 1, "coarse_lag": True}
+            "learned_history": 0, "learned_train_every": 4, "learned_gate": 0.02, "learned_gate_skip": 3,
+            "coarse_lag": True}
 
     def __init__(self, arm, shape, seed, torch, pg):
         o = DesignRun.opts
@@ -124,7 +125,9 @@ class DesignRun:
                     self.warm_start = LearnedWarmStart(shape, stride=o["learned_stride"], capacity=8,
                                                        train_steps=o["learned_train_steps"], lr=o["learned_lr"],
                                                        seed=seed, use_net=o["learned_net"],
-                                                       history=o["learned_history"])
+                                                       history=o["learned_history"],
+                                                       train_every=o["learned_train_every"],
+                                                       gate=o["learned_gate"], gate_skip=o["learned_gate_skip"])
                 # stops on the recursive FP64 residual like the plain arm's CG (the true residual of every timed
                 # solve is recomputed outside the timed region and reported)
                 self.solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=o["m"], inner_iters=o["inner_iters"],

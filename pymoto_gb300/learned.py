@@ -22,7 +22,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import F64, MATVEC, call, stream
+from ._lib import F32, F64, MATVEC, RESIDUAL, call, stream
 
 # (name, cin, cout, relu)
 LAYERS = [("enc1a", 4, 16, True), ("enc1b", 16, 16, True), ("enc2a", 16, 32, True), ("enc2b", 32, 32, True),
@@ -202,9 +202,16 @@ class LearnedWarmStart:
     """
 
     def __init__(self, grid, stride=4, capacity=8, train_steps=2, lr=1e-3, min_samples=1, seed=0, device="cuda",
-                 use_net=True, history=1):
+                 use_net=True, history=1, train_every=1, gate=0.0, gate_skip=3):
+        """train_every: train on every k-th observed solution (the pairs are stored every time).
+        gate, gate_skip: when the network's prediction carried less than `gate` of the energy norm of the
+        Rayleigh-Ritz initial guess, skip the next `gate_skip` predictions (then predict again); 0 disables."""
         nx, ny, nz = grid
         self.use_net = use_net
+        self.train_every, self.gate, self.gate_skip = max(1, int(train_every)), float(gate), int(gate_skip)
+        self._skip = 0
+        self._predicted = False
+        self.predictions = 0
         self.history = int(history)
         self._hist = []             # older solutions (FP64, fine grid), most recent first
         if nz == 0:
@@ -261,9 +268,21 @@ class LearnedWarmStart:
         and the network's prediction."""
         hist = [h for h in self._hist if h.numel() == A.grid.ndof]
         vecs = hist[1:1 + self.history] if x0 is not None else hist[:self.history]
+        self._predicted = False
         if self.use_net and self.ready:
-            vecs.append(self.predict(A))
+            if self._skip > 0:
+                self._skip -= 1
+            else:
+                vecs.append(self.predict(A))
+                self._predicted = True
+                self.predictions += 1
         return vecs
+
+    def report(self, shares):
+        """Energy shares of the Rayleigh-Ritz directions of the last solve (the prediction is the last one when
+        it was used): a prediction below the gate suspends the next `gate_skip` predictions."""
+        if self._predicted and self.gate > 0.0 and len(shares) and float(shares[-1]) < self.gate:
+            self._skip = self.gate_skip
 
     def observe(self, A, u):
         """Store the pair (stiffness field of A, solution u) and train on the stored pairs."""
@@ -283,8 +302,9 @@ class LearnedWarmStart:
         call("pmg_dot", F64, self.ncn, t, t, self._sc[0:1], ws.reduce, stream())
         call("pmg_scale_rsqrt", F64, self.ncn, t, t, self._sc[0:1], stream())   # unit 2-norm
         self.count += 1
-        for _ in range(self.train_steps):
-            self.train_step(int(self.rng.integers(min(self.count, self.capacity))))
+        if (self.count - 1) % self.train_every == 0:
+            for _ in range(self.train_steps):
+                self.train_step(int(self.rng.integers(min(self.count, self.capacity))))
 
     def train_step(self, slot):
         net = self.net
@@ -306,16 +326,25 @@ def _workspace(device):
     return Workspace.get(device)
 
 
-def rayleigh_ritz(A, b, vectors, out_x, out_r, work):
+def rayleigh_ritz(A, b, vectors, out_x, out_r, work, A32=None, work32=None):
     """x = sum c_i v_i minimising the energy error over span(vectors) (Galerkin: G c = h with
-    G_ij = v_i^T A v_j, h_i = v_i^T b), and r = b - A x from the same products.  `work` holds one FP64
-    vector per basis vector (A v_i).  Returns the coefficients.  Linearly dependent directions are dropped."""
+    G_ij = v_i^T A v_j, h_i = v_i^T b), and r = b - A x.  `work` holds one FP64 vector per basis vector.
+    Returns the coefficients.  Linearly dependent directions are dropped.
+    With A32 (the FP32 operator of the same matrix) and work32 (two FP32 vectors) the Gram products use the
+    FP32 tensor-core operator, and r = b - A x is one FP64 product: the coefficients carry the FP32 rounding
+    of the products, the residual is the exact FP64 residual of the returned x."""
     n = b.numel()
     st = stream()
     ws = _workspace(b.device)
     k = len(vectors)
     for v, q in zip(vectors, work):
-        A.apply(MATVEC, v, out=q)
+        if A32 is None:
+            A.apply(MATVEC, v, out=q)
+        else:
+            u32, y32 = work32
+            call("pmg_convert", F64, F32, n, v, u32, 1.0, st)
+            A32.apply(MATVEC, u32, out=y32)
+            call("pmg_convert", F32, F64, n, y32, q, 1.0, st)
     sc = torch.zeros(k * k + k, dtype=torch.float64, device=b.device)
     for i in range(k):
         for j in range(i, k):
@@ -336,9 +365,17 @@ def rayleigh_ritz(A, b, vectors, out_x, out_r, work):
         ck = (V[:, good] @ ((V[:, good].T @ (h[keep] / d)) / w[good])) / d
         c[keep] = ck
     out_x.zero_()
-    out_r.copy_(b)
-    for ci, v, q in zip(c, vectors, work):
+    for ci, v in zip(c, vectors):
         if ci != 0.0:
             out_x.add_(v, alpha=float(ci))
-            out_r.add_(q, alpha=-float(ci))
+    if A32 is None:
+        out_r.copy_(b)
+        for ci, q in zip(c, work):
+            if ci != 0.0:
+                out_r.add_(q, alpha=-float(ci))
+    else:
+        A.apply(RESIDUAL, out_x, b, out=out_r)
+    # energy share of each direction in the combination: |c_i| sqrt(G_ii) / sqrt(c^T G c)
+    e = float(c @ G @ c) if keep else 0.0
+    rayleigh_ritz.last_shares = (np.abs(c) * np.sqrt(np.maximum(np.diag(G), 0.0)) / np.sqrt(e)) if e > 0 else c * 0
     return c

@@ -392,6 +392,11 @@ class GeometricMultigrid(Preconditioner):
             op = A
         if op.code != code:
             raise TypeError("coarse operators keep the precision of their parent level")
+        if not torch.cuda.is_current_stream_capturing():
+            # the level-0 operator of this level is final here (the rest of the hierarchy follows)
+            if getattr(self, "level0_ready", None) is None:
+                self.level0_ready = torch.cuda.Event()
+            self.level0_ready.record()
         if self.A is not op:
             self._graph = None
         self.A = op
@@ -956,7 +961,18 @@ class MixedPrecisionCG(LinearSolver):
             for v, buf in zip(extra, B["wsv"]):
                 call("pmg_mask_bc", F64, A.grid.dim, A.grid.nnodes, A.bcmask, 0, v, buf, st)
                 vecs.append(buf)
-            self.warm_start_coefficients = rayleigh_ritz(A, b, vecs, x, r, B["wsq"])
+            # Gram products on the FP32 level-0 operator of the hierarchy once the set-up stream has it
+            pc = self.preconditioner
+            ev = getattr(pc, "level0_ready", None)
+            a32 = getattr(self, "A32", None)
+            if ev is not None and a32 is not None and a32 is getattr(pc, "A", None) and a32.grid.ndof == n:
+                torch.cuda.current_stream().wait_event(ev)
+                self.warm_start_coefficients = rayleigh_ritz(A, b, vecs, x, r, B["wsq"], A32=a32,
+                                                             work32=(self._r32, self._z32))
+            else:
+                self.warm_start_coefficients = rayleigh_ritz(A, b, vecs, x, r, B["wsq"])
+            if hasattr(self.warm_start, "report"):
+                self.warm_start.report(getattr(rayleigh_ritz, "last_shares", []))
         else:
             if x0 is not None:
                 x.copy_(_to_device(x0, torch.float64)[0])
