@@ -6,9 +6,11 @@ nu=0.3, SIMP p=3 (xmin=1e-9), FilterConv r=2.5, left face clamped, unit -y point
 the previous solution) -> compliance -> adjoint (LDA projection) -> sensitivity -> filter transpose ->
 OC update (move 0.2), all on the device.  Initial density: seeded U(1e-3, 1).
 
-Arms: "plain_fp64" (FP64 CG with an FP64 geometric-multigrid preconditioner, pyMOTO's algorithm) and the
-headline "mixed" arm (FP64 flexible CG around an FP32 multigrid preconditioner).  `value` is the headline
-arm.  `--impl reference` times the CPU restatement of pyMOTO's own path (oracle) on the host cores.
+Arms: "plain_fp64" (FP64 CG with an FP64 geometric-multigrid preconditioner, pyMOTO's algorithm), "mixed"
+(FP64 flexible CG around FP32 PCG iterations with an FP32 multigrid preconditioner) and the headline
+"mixed_learned" (the mixed arm with the learned warm start, as the metric is defined).  `value` is the
+headline arm (the mixed arm when the learned one is not run).  `--impl reference` times the CPU restatement of
+pyMOTO's own path (oracle) on the host cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
@@ -58,7 +60,7 @@ def parse():
     ap.add_argument("--case", default=None, choices=["operator"],
                     help="instead of the bench: time the level-0 operator kernels alone (a small case for ncu)")
     ap.add_argument("--arms", default="plain_fp64,mixed,mixed_learned",
-                    help="plain_fp64 (the reference's method), mixed (headline), mixed_learned (with the learned "
+                    help="plain_fp64 (the reference's method), mixed, mixed_learned (headline: with the learned "
                          "warm start), ablations: mixed_jacobi, plain_fp64_cheb")
     return ap.parse_args()
 
@@ -227,6 +229,11 @@ def time_arm(run, steps, warmup, torch, flush, probe_targets=None, pg=None):
     return durs, probe
 
 
+def headline_arm(results):
+    """The arm `value` reports: the learned + mixed-precision arm of the metric, else the mixed one."""
+    return "mixed_learned" if "mixed_learned" in results else "mixed"
+
+
 def kernel_rooflines(run, flush, torch, reps=20):
     """Live CUDA-event times of the two level-0 operator kernels on the headline arm's final operators, one
     launch at a time on the current stream with the L2 flushed (256 MB write) before each launch:
@@ -300,7 +307,7 @@ def measure_gb300(args, rank, world, local_rank):
     results = {}
     for arm in args.arms.split(","):
         run = DesignRun(arm, shape, seed=1234 + rank, torch=torch, pg=pg)
-        targets = {"pmg_ebe_apply", "pmg_stencil_apply"} if arm == "mixed" else None
+        targets = set()          # count launches only: no events inside the timed region
         barrier()
         torch.cuda.synchronize()
         with ClockSampler(local_rank) as clk:
@@ -345,8 +352,8 @@ def measure_gb300(args, rank, world, local_rank):
     c_m = float(torch.dot(mask, u_m).item())
     c_t = float(torch.dot(mask, u_t).item())
 
-    # end-to-end through the public API with host buffers (mixed arm)
-    run = results["mixed"]["run"]
+    # end-to-end through the public API with host buffers (headline arm)
+    run = results[headline_arm(results)]["run"]
     nel = run.nel
     x_host = torch.empty(nel, dtype=torch.float64).pin_memory()
     x_host.copy_(run.sx.state.cpu())
@@ -366,7 +373,7 @@ def measure_gb300(args, rank, world, local_rank):
         e2e_durs.append(time.perf_counter() - t0)
     e2e_total = max_over_ranks(sum(e2e_durs))
 
-    kernels = kernel_rooflines(results["mixed"]["run"], flush, torch) if rank == 0 else None
+    kernels = kernel_rooflines(results[headline_arm(results)]["run"], flush, torch) if rank == 0 else None
     out = {"results": results, "shape": shape, "hbm_peak": hbm_peak, "peak_src": peak_src, "c_mixed": c_m,
            "c_tight": c_t, "e2e_total_s": e2e_total, "nel": nel, "res_mixed_same_design": ms.last_residual,
            "kernels": kernels, "peaks": peaks}
@@ -471,7 +478,9 @@ def main():
         shape = m["shape"]
         R = m["results"]
         steps = args.steps
-        val_mixed = world * steps / (R["mixed"]["total_ms"] / 1e3)
+        H = headline_arm(R)
+        val_head = world * steps / (R[H]["total_ms"] / 1e3)
+        val_mixed = world * steps / (R["mixed"]["total_ms"] / 1e3) if "mixed" in R else None
         val_plain = world * steps / (R["plain_fp64"]["total_ms"] / 1e3) if "plain_fp64" in R else None
         # rooflines of the level-0 operator kernels, timed live after the timed region (kernel_rooflines)
         K = m["kernels"]
@@ -502,9 +511,9 @@ def main():
                    "kind": "port", "sample": "1 warm design iteration of the same workload (after 1 cold one) with "
                                              "the numpy/scipy restatement of pyMOTO's path, 4-level CG+GMG"}
         e2e_val = world * steps / m["e2e_total_s"]
-        launches = R["mixed"]["probe"].launches
-        line = {"metric": METRIC, "value": val_mixed, "unit": "design it/s", "n_gpus": world, "steps": steps,
-                "warmup": args.warmup, "ms_per_step": R["mixed"]["total_ms"] / steps, "higher_is_better": True,
+        launches = R[H]["probe"].launches
+        line = {"metric": METRIC, "value": val_head, "unit": "design it/s", "n_gpus": world, "steps": steps,
+                "warmup": args.warmup, "ms_per_step": R[H]["total_ms"] / steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32",
                 "data": "synthetic (seeded U(1e-3,1) initial density, replicas seeded per rank)",
                 "config": {"workload": f"3D cantilever hex8 {shape[0]}x{shape[1]}x{shape[2]} "
@@ -516,22 +525,26 @@ def main():
                                      f"fine/coarse), FP64 Cholesky coarsest with FP32 inverse"
                                      f"{' (previous inverse until the new one is ready)' if DesignRun.opts['coarse_lag'] else ''}"
                                      f"; plain arm: FP64 CG + FP64 GMG, damped Jacobi w=0.6, 2 sweeps, FP64 inverse",
-                           "learned_warm_start": False,
-                           "learned_warm_start_note": "measured as arms.mixed_learned (network + previous solution "
-                                                      "in a Rayleigh-Ritz initial guess); not in the headline",
+                           "headline_arm": H, "learned_warm_start": H == "mixed_learned",
+                           "learned_warm_start_note": "3-level BF16 conv net on the stride-4 voxels, trained on "
+                                                      "the device every 4th solve; its prediction enters a "
+                                                      "Rayleigh-Ritz initial guess with the previous solution and "
+                                                      "is skipped for 3 designs when it carried < 2 % of its "
+                                                      "energy; arms.mixed is the same solver without it",
                            "parallelism": f"replicas x{world}", "l2": "flushed before every step (256 MB write)"},
                 "arms": {arm: {"design_it_per_s": world * steps / (R[arm]["total_ms"] / 1e3),
                                "ms_per_step": R[arm]["total_ms"] / steps,
                                "solver_iterations": R[arm]["iters"], "true_rel_residual_last": R[arm]["true_residual"],
                                "compliance_last": R[arm]["compliance"]} for arm in R},
-                "speedup_mixed_vs_plain_fp64": val_mixed / val_plain if val_plain else None,
+                "speedup_headline_vs_plain_fp64": val_head / val_plain if val_plain else None,
+                "speedup_mixed_vs_plain_fp64": val_mixed / val_plain if (val_plain and val_mixed) else None,
                 "parity": {"same_design_compliance_mixed": m["c_mixed"], "same_design_compliance_fp64_tol1e-11":
                            m["c_tight"], "rel_diff": abs(m["c_mixed"] - m["c_tight"]) / abs(m["c_tight"]),
                            "mixed_true_rel_residual": m["res_mixed_same_design"]},
                 "roofline": roofline, "roofline_fp64_stencil": roofline_fp64, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": "design it/s", "h2d_bytes_per_step": 8 * m["nel"],
                         "d2h_bytes_per_step": 8 * m["nel"] + 8},
-                "gpu_launches": launches, "clocks": R["mixed"]["clocks"]}
+                "gpu_launches": launches, "clocks": R[H]["clocks"]}
         if "breakdown" in m:
             print(json.dumps({"breakdown": {"|".join(map(str, k)): v for k, v in sorted(
                 m["breakdown"].items(), key=lambda kv: -kv[1]["total_ms"])}}), file=sys.stderr)
