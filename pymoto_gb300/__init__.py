@@ -15,10 +15,11 @@ from .operators import Grid, StencilOperator, StiffnessOperator, element_stiffne
 from .optimizers import OC
 from .solvers import (CG, Chebyshev, DampedJacobi, DenseCholesky, GeometricMultigrid, LinearSolver,
                       MixedPrecisionCG, Preconditioner)
+from .autograd import ComplianceObjective
 
 __version__ = "0.1.0"
 
 __all__ = ["AssembleStiffness", "DensityFilter", "DeviceDyad", "EinSum", "FilterConv", "LinSolve", "MathExpression",
            "SIMP", "Grid", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "Chebyshev", "DampedJacobi",
            "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
-           "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME"]
+           "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective"]
