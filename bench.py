@@ -88,6 +88,7 @@ class DesignRun:
             "smoother": "chebyshev", "cheb_degree": 1, "cheb_coarse_degree": [2, 3, 6], "cheb_ratio": 15.0,
             "learned_train_steps": 1, "learned_stride": 4, "learned_lr": 2e-3, "learned_net": True,
             "learned_history": 0, "learned_train_every": 4, "learned_gate": 0.02, "learned_gate_skip": 3,
+            "learned_cc": True,
             "coarse_lag": True}
 
     def __init__(self, arm, shape, seed, torch, pg):
@@ -129,7 +130,8 @@ class DesignRun:
                                                        seed=seed, use_net=o["learned_net"],
                                                        history=o["learned_history"],
                                                        train_every=o["learned_train_every"],
-                                                       gate=o["learned_gate"], gate_skip=o["learned_gate_skip"])
+                                                       gate=o["learned_gate"], gate_skip=o["learned_gate_skip"],
+                                                       coarse_correction=o["learned_cc"])
                 # stops on the recursive FP64 residual like the plain arm's CG (the true residual of every timed
                 # solve is recomputed outside the timed region and reported)
                 self.solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=o["m"], inner_iters=o["inner_iters"],
@@ -529,8 +531,9 @@ def main():
                            "learned_warm_start_note": "3-level BF16 conv net on the stride-4 voxels, trained on "
                                                       "the device every 4th solve; its prediction enters a "
                                                       "Rayleigh-Ritz initial guess with the previous solution and "
-                                                      "is skipped for 3 designs when it carried < 2 % of its "
-                                                      "energy; arms.mixed is the same solver without it",
+                                                      "spans a one-dimensional coarse correction in every FCG "
+                                                      "iteration; skipped for 3 designs when it carried < 2 % of "
+                                                      "the guess's energy; arms.mixed is the solver without it",
                            "parallelism": f"replicas x{world}", "l2": "flushed before every step (256 MB write)"},
                 "arms": {arm: {"design_it_per_s": world * steps / (R[arm]["total_ms"] / 1e3),
                                "ms_per_step": R[arm]["total_ms"] / steps,

@@ -202,12 +202,15 @@ class LearnedWarmStart:
     """
 
     def __init__(self, grid, stride=4, capacity=8, train_steps=2, lr=1e-3, min_samples=1, seed=0, device="cuda",
-                 use_net=True, history=1, train_every=1, gate=0.0, gate_skip=3):
+                 use_net=True, history=1, train_every=1, gate=0.0, gate_skip=3, coarse_correction=False):
         """train_every: train on every k-th observed solution (the pairs are stored every time).
         gate, gate_skip: when the network's prediction carried less than `gate` of the energy norm of the
-        Rayleigh-Ritz initial guess, skip the next `gate_skip` predictions (then predict again); 0 disables."""
+        Rayleigh-Ritz initial guess, skip the next `gate_skip` predictions (then predict again); 0 disables.
+        coarse_correction: MixedPrecisionCG also uses the prediction w of a solve as a one-dimensional coarse
+        space, z += (w.r / w.Kw) w in every flexible-CG iteration."""
         nx, ny, nz = grid
         self.use_net = use_net
+        self.coarse_correction = bool(coarse_correction)
         self.train_every, self.gate, self.gate_skip = max(1, int(train_every)), float(gate), int(gate_skip)
         self._skip = 0
         self._predicted = False

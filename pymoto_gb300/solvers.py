@@ -885,6 +885,13 @@ class MixedPrecisionCG(LinearSolver):
             call("pmg_convert_dscale", F32, F64, n, z32, z, s[1:2], 0, st)
         if self.coarse_correction is not None:
             z.add_(self.coarse_correction(r))
+        lc = B.get("learned_cc")
+        if lc is not None:
+            # coarse correction on the span of the network's prediction w: z += (w.r / w.Kw) w (a no-op while
+            # w.Kw is zero, i.e. when no prediction was used in this solve)
+            w, num, den = lc
+            call("pmg_dot", F64, n, w, r, num, ws.reduce, st)
+            call("pmg_axpy_ratio", F64, n, z, w, num, den, 1.0, st)
         p, q = P[slot], Q[slot]
         p.copy_(z)
         for j in range(k):           # K-orthogonalise against the other (older) directions
@@ -898,6 +905,28 @@ class MixedPrecisionCG(LinearSolver):
         pq.copy_(self._pqpr[0:1])
         s[2:3].copy_(self._pqpr[1:2])
         call("pmg_cg_update", F64, n, x, r, p, q, s[2:3], pq, s[1:2], ws.reduce, st)
+
+    def _set_learned_correction(self, A, B, vecs, n, dev):
+        """Coarse space of the learned warm start (`coarse_correction=True` on it): the masked prediction of
+        this solve and its energy w.Kw, or w.Kw = 0 (correction off) when no prediction was used.  The buffers
+        keep their addresses, so the captured FCG step stays valid."""
+        ws_ = self.warm_start
+        if ws_ is None or not getattr(ws_, "coarse_correction", False):
+            return
+        if B.get("learned_cc") is None:
+            f64 = dict(dtype=torch.float64, device=dev)
+            B["learned_cc"] = (torch.zeros(n, **f64), torch.zeros(1, **f64), torch.zeros(1, **f64))
+            for j in range(B["k"]):              # graphs captured without the correction: recapture
+                B["graphs"][j] = None
+        w, num, den = B["learned_cc"]
+        if getattr(ws_, "_predicted", False) and vecs:
+            st = stream()
+            w.copy_(vecs[-1])                    # the masked prediction (last Rayleigh-Ritz direction)
+            kw = B["wsq"][0] if B.get("wsq") else torch.empty_like(w)
+            A.apply(MATVEC, w, out=kw)
+            call("pmg_dot", F64, n, w, kw, den, Workspace.get(dev).reduce, st)
+        else:
+            den.zero_()
 
     def _join_setup(self):
         side = getattr(self, "_side_pending", None)
@@ -974,11 +1003,14 @@ class MixedPrecisionCG(LinearSolver):
             if hasattr(self.warm_start, "report"):
                 self.warm_start.report(getattr(rayleigh_ritz, "last_shares", []))
         else:
+            vecs = []
             if x0 is not None:
                 x.copy_(_to_device(x0, torch.float64)[0])
             else:
                 x.zero_()
             A.apply(RESIDUAL, x, b, out=r)
+        if trans == "N":
+            self._set_learned_correction(A, B, vecs, n, dev)
         call("pmg_dot2", F64, n, b, b, r, r, s[0:1], ws.reduce, st)
         bb, rr = s[0:2].tolist()
         bn = math.sqrt(bb) or 1.0

@@ -241,12 +241,14 @@ def test_learned_warm_start_gain(pg):
     nnx, nny = shape[0] + 1, shape[1] + 1
     f[3 * (((shape[2] // 2) * nny + shape[1] // 2) * nnx + shape[0]) + 1] = -1.0
     results = {}
-    for learned in (False, True):
+    active = []
+    for learned in (False, True, "cc"):
         rng = np.random.default_rng(7)
         sx = pg.Signal("x", torch.from_numpy(rng.uniform(0.2, 0.8, g.nel)).cuda())
         mgs = pg.GeometricMultigrid.hierarchy(d, levels=3, smooth_steps=2, coarse_smooth_steps=3, precision="fp32",
                                               smoother="chebyshev")
-        ws = LearnedWarmStart(shape, stride=4, capacity=8, train_steps=4, lr=2e-3) if learned else None
+        ws = LearnedWarmStart(shape, stride=4, capacity=8, train_steps=4, lr=2e-3,
+                              coarse_correction=learned == "cc") if learned else None
         solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=1e-6, m=1, warm_start=ws)
         with pg.Network() as fn:
             xf = pg.FilterConv(d, radius=2.0)(sx)
@@ -260,8 +262,13 @@ def test_learned_warm_start_gain(pg):
             oc.step()
             its.append(solver.iterations)
             assert solver.last_residual <= 1e-6
+            if learned == "cc":
+                active.append(float(solver._fcg["learned_cc"][2]) > 0.0)
         results[learned] = its
-    base, lrn = results[False], results[True]
-    print(f"FCG iterations per design without / with the learned warm start: {base} / {lrn}")
+    base, lrn, lcc = results[False], results[True], results["cc"]
+    print(f"FCG iterations per design without / with the learned warm start / with it and the learned coarse "
+          f"correction: {base} / {lrn} / {lcc}")
     # the network starts untrained: compare the designs after the first few
     assert sum(lrn[4:]) <= sum(base[4:])
+    # the one-dimensional learned coarse space was in use and the solves still reach the FP64 tolerance
+    assert any(active) and sum(lcc[4:]) <= sum(base[4:]) + 2
