@@ -88,7 +88,7 @@ class DesignRun:
             "smoother": "chebyshev", "cheb_degree": 1, "cheb_coarse_degree": [2, 3, 6], "cheb_ratio": 15.0,
             "learned_train_steps": 1, "learned_stride": 4, "learned_lr": 2e-3, "learned_net": True,
             "learned_history": 0, "learned_train_every": 4, "learned_gate": 0.02, "learned_gate_skip": 3,
-            "learned_cc": True,
+            "learned_cc": False,
             "coarse_lag": True}
 
     def __init__(self, arm, shape, seed, torch, pg):
@@ -530,10 +530,10 @@ def main():
                            "headline_arm": H, "learned_warm_start": H == "mixed_learned",
                            "learned_warm_start_note": "3-level BF16 conv net on the stride-4 voxels, trained on "
                                                       "the device every 4th solve; its prediction enters a "
-                                                      "Rayleigh-Ritz initial guess with the previous solution and "
-                                                      "spans a one-dimensional coarse correction in every FCG "
-                                                      "iteration; skipped for 3 designs when it carried < 2 % of "
-                                                      "the guess's energy; arms.mixed is the solver without it",
+                                                      "Rayleigh-Ritz initial guess with the previous solution, "
+                                                      "skipped for 3 designs when it carried < 2 % of the guess's "
+                                                      "energy (the deflation on its span, learned_cc, is off: no "
+                                                      "gain at this size); arms.mixed is the solver without it",
                            "parallelism": f"replicas x{world}", "l2": "flushed before every step (256 MB write)"},
                 "arms": {arm: {"design_it_per_s": world * steps / (R[arm]["total_ms"] / 1e3),
                                "ms_per_step": R[arm]["total_ms"] / steps,

@@ -207,7 +207,8 @@ class LearnedWarmStart:
         gate, gate_skip: when the network's prediction carried less than `gate` of the energy norm of the
         Rayleigh-Ritz initial guess, skip the next `gate_skip` predictions (then predict again); 0 disables.
         coarse_correction: MixedPrecisionCG also uses the prediction w of a solve as a one-dimensional coarse
-        space, z += (w.r / w.Kw) w in every flexible-CG iteration."""
+        space in every flexible-CG iteration, deflated (A-DEF2, Tang, Nabben, Vuik, Erlangga, J. Sci. Comput.
+        39 (2009)): z = M(r - (w.r / w.Kw) Kw) + (w.r / w.Kw) w."""
         nx, ny, nz = grid
         self.use_net = use_net
         self.coarse_correction = bool(coarse_correction)

@@ -871,10 +871,20 @@ class MixedPrecisionCG(LinearSolver):
         ws = Workspace.get(B["dev"])
         st = stream()
         r, z, x = B["r"], B["z"], B["x"]
+        lc = B.get("learned_cc")
+        rin = r
+        if lc is not None:
+            # deflation on the span of the network's prediction w (A-DEF2): the preconditioner sees
+            # r - (w.r / w.Kw) Kw, and (w.r / w.Kw) w is added to its output; no-ops while w.Kw = 0
+            w, kw, rdef, num, den = lc
+            call("pmg_dot", F64, n, w, r, num, ws.reduce, st)
+            rdef.copy_(r)
+            call("pmg_axpy_ratio", F64, n, rdef, kw, num, den, -1.0, st)
+            rin = rdef
         if self.fell_back:
-            z.copy_(self._fp64_preconditioner().solve(r))
+            z.copy_(self._fp64_preconditioner().solve(rin))
         else:
-            call("pmg_convert_dscale", F64, F32, n, r, self._r32, s[1:2], 1, st)
+            call("pmg_convert_dscale", F64, F32, n, rin, self._r32, s[1:2], 1, st)
             if self.preconditioner is None:
                 z32 = self._r32
             elif self.inner_iters > 0:
@@ -885,12 +895,7 @@ class MixedPrecisionCG(LinearSolver):
             call("pmg_convert_dscale", F32, F64, n, z32, z, s[1:2], 0, st)
         if self.coarse_correction is not None:
             z.add_(self.coarse_correction(r))
-        lc = B.get("learned_cc")
         if lc is not None:
-            # coarse correction on the span of the network's prediction w: z += (w.r / w.Kw) w (a no-op while
-            # w.Kw is zero, i.e. when no prediction was used in this solve)
-            w, num, den = lc
-            call("pmg_dot", F64, n, w, r, num, ws.reduce, st)
             call("pmg_axpy_ratio", F64, n, z, w, num, den, 1.0, st)
         p, q = P[slot], Q[slot]
         p.copy_(z)
@@ -907,22 +912,22 @@ class MixedPrecisionCG(LinearSolver):
         call("pmg_cg_update", F64, n, x, r, p, q, s[2:3], pq, s[1:2], ws.reduce, st)
 
     def _set_learned_correction(self, A, B, vecs, n, dev):
-        """Coarse space of the learned warm start (`coarse_correction=True` on it): the masked prediction of
-        this solve and its energy w.Kw, or w.Kw = 0 (correction off) when no prediction was used.  The buffers
-        keep their addresses, so the captured FCG step stays valid."""
+        """Coarse space of the learned warm start (`coarse_correction=True` on it): the masked prediction w of
+        this solve, Kw and w.Kw, or w.Kw = 0 (deflation off) when no prediction was used.  The buffers keep
+        their addresses, so the captured FCG step stays valid."""
         ws_ = self.warm_start
         if ws_ is None or not getattr(ws_, "coarse_correction", False):
             return
         if B.get("learned_cc") is None:
             f64 = dict(dtype=torch.float64, device=dev)
-            B["learned_cc"] = (torch.zeros(n, **f64), torch.zeros(1, **f64), torch.zeros(1, **f64))
+            B["learned_cc"] = (torch.zeros(n, **f64), torch.zeros(n, **f64), torch.zeros(n, **f64),
+                               torch.zeros(1, **f64), torch.zeros(1, **f64))
             for j in range(B["k"]):              # graphs captured without the correction: recapture
                 B["graphs"][j] = None
-        w, num, den = B["learned_cc"]
+        w, kw, _, _, den = B["learned_cc"]
         if getattr(ws_, "_predicted", False) and vecs:
             st = stream()
             w.copy_(vecs[-1])                    # the masked prediction (last Rayleigh-Ritz direction)
-            kw = B["wsq"][0] if B.get("wsq") else torch.empty_like(w)
             A.apply(MATVEC, w, out=kw)
             call("pmg_dot", F64, n, w, kw, den, Workspace.get(dev).reduce, st)
         else:
