@@ -30,14 +30,14 @@ def _shape3(s):
 
 
 def build_network(pg, shape, bc, f, filt, radius, levels, tol, plane="strain", mixed=False, w=0.6, steps=2,
-                  state_kind="numpy"):
+                  state_kind="numpy", sens_precision="fp64"):
     d = pg.VoxelDomain(*shape)
     x0 = np.full(d.nel, 0.5)
     sx = pg.Signal("x", x0 if state_kind == "numpy" else dev(x0))
     with pg.Network() as fn:
         xf = (pg.DensityFilter(d, radius=radius) if filt == "density" else pg.FilterConv(d, radius=radius))(sx)
         xs = pg.MathExpression("1e-9 + (1-1e-9)*inp0^3")(xf)
-        sK = pg.AssembleStiffness(d, bc=bc, plane=plane)(xs)
+        sK = pg.AssembleStiffness(d, bc=bc, plane=plane, sensitivity_precision=sens_precision)(xs)
         if levels > 0:
             mgs = pg.GeometricMultigrid.hierarchy(d, levels=levels, smoother_w=w, smooth_steps=steps,
                                                   precision="fp32" if mixed else None)
@@ -90,6 +90,23 @@ def test_pipeline_fp64_matches_reference(pg, golden, name, state_kind):
         u = host(su.state)
         np.testing.assert_allclose(u, g[f"u{it}"], rtol=0, atol=1e-8 * np.abs(u).max())
         np.testing.assert_allclose(dx, g[f"dx{it}"], rtol=0, atol=1e-8 * np.abs(dx).max())
+
+
+@pytest.mark.parametrize("sens_precision", ["fp64", "mixed"])
+def test_pipeline_mixed_matches_reference(pg, golden, sens_precision):
+    """Mixed path (FP64 flexible CG around the FP32 multigrid preconditioner; FP32 sensitivity contraction
+    of FP64-shifted element vectors for "mixed") vs pyMOTO's own FP64 results on the hex8 pipeline, with the
+    solve driven to an FP64 relative residual of 1e-8: compliance, u and sensitivities to 1e-6 relative."""
+    g = golden("pipeline_h8_mg.npz")
+    shape = _shape3(g["shape"])
+    d, sx, su, sc, fn = build_network(pg, shape, g["bc"], g["f"], "conv", float(g["radius"]), int(g["levels"]),
+                                      1e-8, mixed=True, sens_precision=sens_precision)
+    for it in range(2):
+        c, dx = run_design(fn, sx, sc, g[f"x{it}"])
+        assert abs(c - float(g[f"c{it}"])) <= 1e-6 * abs(c), (c, float(g[f"c{it}"]))
+        u = host(su.state)
+        np.testing.assert_allclose(u, g[f"u{it}"], rtol=0, atol=1e-6 * np.abs(u).max())
+        np.testing.assert_allclose(dx, g[f"dx{it}"], rtol=0, atol=1e-6 * np.abs(dx).max())
 
 
 def test_cg_iterations_match_reference_algorithm(pg):
