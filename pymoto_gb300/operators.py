@@ -115,9 +115,10 @@ class _GalerkinTables:
 class StiffnessOperator:
     """K(x) = sum_e x_e K0 with Dirichlet rows/columns (level 0 of the hierarchy).
 
-    FP32 products are matrix-free (600 FMA per node, memory-light).  FP64 products use node stencils
-    assembled once on the first FP64 product (243 FMA per node in 3D; FP64 throughput is 1/58 of FP32 on
-    GB300, so fewer FMAs win over the extra 1 GB of stencil traffic) unless `fp64_stencil` is False."""
+    FP32 products are matrix-free on the tensor cores (3D) or the CUDA cores (2D).  FP64 products use
+    half-symmetric node stencils assembled once per operator on the first FP64 product (81 FMA per dof; the
+    FP64 pipe of GB300 runs at 1/64 of the FP32 rate, so fewer FMAs win over the 549 MB of stencils at
+    128x64x64) unless `fp64_stencil` is False."""
 
     fp64_stencil = True
 

@@ -735,8 +735,11 @@ class MixedPrecisionCG(LinearSolver):
     the last `m` directions (FCG(m)); the reference's beta = -(q.z)/(p.q) is the m = 1 case.
     `warm_start` is an optional learned predictor (pymoto_gb300.learned.LearnedWarmStart): its prediction and
     the given x0 span the space in which the initial guess is the energy-optimal (Rayleigh-Ritz)
-    combination, and every converged solution is passed back to it for training; `coarse_correction` an
-    optional callable r64 -> z64 added to the preconditioned residual.
+    combination (Gram products on the FP32 operator, one FP64 residual), every converged solution is passed
+    back to it for training, and with its `coarse_correction` the prediction also deflates every
+    preconditioner application (A-DEF2); `coarse_correction` here is an optional callable r64 -> z64 added to
+    the preconditioned residual.  With a lagged coarsest solve (DenseCholesky(lag=True)) the new coarse
+    inverse is promoted between two iterations as soon as its factorisation has finished.
     """
 
     def __init__(self, A=None, preconditioner=None, tol=1e-6, m=2, inner_iters=0, inner_tol=0.1, maxit=500,
