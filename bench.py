@@ -69,6 +69,29 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+# ------------------------------------------------------------------------------------------ replicas
+# The path does not shard across GPUs here (one GPU per box): N ranks run N independent design loops with
+# their own seeds; the only collectives are a barrier around the timed region and the maximum of the timed
+# totals over the ranks.
+def replica_seed(rank):
+    return 1234 + rank
+
+
+def max_over_ranks(v, world, device):
+    """The largest value of v over the ranks (v itself with one rank)."""
+    if world <= 1:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(world, steps, slowest_total_s):
+    """Whole-job design iterations per second: every rank did `steps`, the job took the slowest rank's time."""
+    return world * steps / slowest_total_s
+
+
 # ------------------------------------------------------------------------------------------ problem
 def cantilever(shape):
     nx, ny, nz = shape
@@ -297,25 +320,21 @@ def measure_gb300(args, rank, world, local_rank):
         if world > 1:
             torch.distributed.barrier()
 
-    def max_over_ranks(v):
-        if world > 1:
-            t = torch.tensor([v], dtype=torch.float64, device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return v
+    def slowest(v):
+        return max_over_ranks(v, world, "cuda")
 
     DesignRun.opts.update({"inner_iters": args.inner_iters, "inner_tol": args.inner_tol, "m": args.fcg_m,
                            "levels": args.levels, "sweeps": args.sweeps, "coarse_sweeps": args.coarse_sweeps})
     results = {}
     for arm in args.arms.split(","):
-        run = DesignRun(arm, shape, seed=1234 + rank, torch=torch, pg=pg)
+        run = DesignRun(arm, shape, seed=replica_seed(rank), torch=torch, pg=pg)
         targets = set()          # count launches only: no events inside the timed region
         barrier()
         torch.cuda.synchronize()
         with ClockSampler(local_rank) as clk:
             durs, probe = time_arm(run, args.steps, args.warmup, torch, flush, targets, pg)
         barrier()
-        total = max_over_ranks(sum(durs))
+        total = slowest(sum(durs))
         results[arm] = {"durs": durs, "total_ms": total, "iters": list(run.iters), "probe": probe,
                         "clocks": clk.summary(), "run": run}
         # true FP64 residual of the last solve
@@ -373,7 +392,7 @@ def measure_gb300(args, rank, world, local_rank):
         x_host.copy_(run.sx.state, non_blocking=True)                  # D2H of the new design
         torch.cuda.synchronize()
         e2e_durs.append(time.perf_counter() - t0)
-    e2e_total = max_over_ranks(sum(e2e_durs))
+    e2e_total = slowest(sum(e2e_durs))
 
     kernels = kernel_rooflines(results[headline_arm(results)]["run"], flush, torch) if rank == 0 else None
     out = {"results": results, "shape": shape, "hbm_peak": hbm_peak, "peak_src": peak_src, "c_mixed": c_m,
@@ -481,9 +500,9 @@ def main():
         R = m["results"]
         steps = args.steps
         H = headline_arm(R)
-        val_head = world * steps / (R[H]["total_ms"] / 1e3)
-        val_mixed = world * steps / (R["mixed"]["total_ms"] / 1e3) if "mixed" in R else None
-        val_plain = world * steps / (R["plain_fp64"]["total_ms"] / 1e3) if "plain_fp64" in R else None
+        val_head = aggregate_rate(world, steps, R[H]["total_ms"] / 1e3)
+        val_mixed = aggregate_rate(world, steps, R["mixed"]["total_ms"] / 1e3) if "mixed" in R else None
+        val_plain = aggregate_rate(world, steps, R["plain_fp64"]["total_ms"] / 1e3) if "plain_fp64" in R else None
         # rooflines of the level-0 operator kernels, timed live after the timed region (kernel_rooflines)
         K = m["kernels"]
         km = K["ebe_apply_mma_residual_f32"]
@@ -512,7 +531,7 @@ def main():
             cpu = {"value": 1.0 / statistics.mean(times), "unit": "design it/s", "cores": os.cpu_count(),
                    "kind": "port", "sample": "1 warm design iteration of the same workload (after 1 cold one) with "
                                              "the numpy/scipy restatement of pyMOTO's path, 4-level CG+GMG"}
-        e2e_val = world * steps / m["e2e_total_s"]
+        e2e_val = aggregate_rate(world, steps, m["e2e_total_s"])
         launches = R[H]["probe"].launches
         line = {"metric": METRIC, "value": val_head, "unit": "design it/s", "n_gpus": world, "steps": steps,
                 "warmup": args.warmup, "ms_per_step": R[H]["total_ms"] / steps, "higher_is_better": True,
@@ -535,7 +554,7 @@ def main():
                                                       "energy (the deflation on its span, learned_cc, is off: no "
                                                       "gain at this size); arms.mixed is the solver without it",
                            "parallelism": f"replicas x{world}", "l2": "flushed before every step (256 MB write)"},
-                "arms": {arm: {"design_it_per_s": world * steps / (R[arm]["total_ms"] / 1e3),
+                "arms": {arm: {"design_it_per_s": aggregate_rate(world, steps, R[arm]["total_ms"] / 1e3),
                                "ms_per_step": R[arm]["total_ms"] / steps,
                                "solver_iterations": R[arm]["iters"], "true_rel_residual_last": R[arm]["true_residual"],
                                "compliance_last": R[arm]["compliance"]} for arm in R},
