@@ -2,7 +2,7 @@
 
 Drop-in GPU Modules and LinearSolvers with pyMOTO's API:
   DensityFilter, FilterConv, SIMP / MathExpression (SIMP form), AssembleStiffness, LinSolve, EinSum,
-  CG, GeometricMultigrid, DampedJacobi, DenseCholesky, MixedPrecisionCG, OC.
+  CG, GeometricMultigrid, DampedJacobi, DenseCholesky, MixedPrecisionCG, OC, WriteToVTI (VoxelDomain.write_to_vti).
 The arithmetic runs in hand-written CUDA kernels of libpymoto_gb300.so through its C ABI
 (include/pymoto_gb300.h); there is no CPU fallback.
 """
@@ -16,10 +16,11 @@ from .optimizers import OC
 from .solvers import (CG, Chebyshev, DampedJacobi, DenseCholesky, GeometricMultigrid, LinearSolver,
                       MixedPrecisionCG, Preconditioner)
 from .autograd import ComplianceObjective
+from .vti import WriteToVTI
 
 __version__ = "0.1.0"
 
 __all__ = ["AssembleStiffness", "DensityFilter", "DeviceDyad", "EinSum", "FilterConv", "LinSolve", "MathExpression",
            "SIMP", "Grid", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "Chebyshev", "DampedJacobi",
            "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
-           "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective"]
+           "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI"]

@@ -111,7 +111,7 @@ class Module:
             out = fn(self, *states)
             if constant:
                 return out
-            outs = _as_list(out) if isinstance(out, (list, tuple)) else [out]
+            outs = _as_list(out) if isinstance(out, (list, tuple)) or out is None else [out]
             if create:
                 if self.sig_out is None:
                     self.sig_out = [Signal(f"{type(self).__name__}_output{i}") for i in range(len(outs))]

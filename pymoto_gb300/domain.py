@@ -13,6 +13,7 @@ class VoxelDomain:
                  unitz: float = 1.0):
         self.nelx, self.nely, self.nelz = int(nelx), int(nely), int(nelz or 0)
         self.dim = 2 if self.nelz == 0 else 3
+        self.origin = np.array([0.0, 0.0, 0.0])
         self.unitx, self.unity, self.unitz = float(unitx), float(unity), float(unitz)
         if np.prod(self.element_size[: self.dim]) <= 0:
             raise ValueError("Element volume needs to be positive")
@@ -58,6 +59,14 @@ class VoxelDomain:
     def get_dofconnectivity(self, ndof):
         c = self.conn
         return (c[:, :, None] * ndof + np.arange(ndof)).reshape(c.shape[0], -1)
+
+    def write_to_vti(self, vectors: dict, filename="out.vti", scale=1.0, wait=True):
+        """Write `vectors` (numpy arrays or CUDA tensors of size a multiple of nel or nnodes) to a Paraview VTI
+        file, as pyMOTO's VoxelDomain.write_to_vti (pymoto/common/domain.py:452-604).  With wait=False the
+        device-to-host copies are queued on the current stream and the file is written by a background
+        thread (pymoto_gb300.vti.flush() waits for it)."""
+        from .vti import write_to_vti
+        return write_to_vti(self, vectors, filename, scale, wait=wait)
 
     def coarse(self):
         return VoxelDomain(self.nelx // 2, self.nely // 2, self.nelz // 2, 2 * self.unitx, 2 * self.unity,

@@ -4,7 +4,8 @@ Run in a container where the pyMOTO sources are available (default: /root/refere
 $PYMOTO_REFERENCE).  matplotlib is not needed: a module stub stands in for it, because pyMOTO imports it
 at module level for plotting only.  The fixtures are small .npz files; the tests never import pyMOTO.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # every fixture
+    python tests/golden/make_golden.py vti      # the VTI files only
 """
 import os
 import sys
@@ -184,14 +185,50 @@ def oc_mbb(pym):
     save("oc_mbb.npz", bc=bc, f=f, c_hist=np.array(hist), x_final=sx.state.copy())
 
 
+def vti_cases():
+    """The VTI output cases: (name, (nelx, nely, nelz), element size, origin, scale, vectors).  Pure numpy, so
+    the tests rebuild the same inputs without pyMOTO."""
+    rng = np.random.default_rng(20251204)
+    cases = []
+    nel, nn = 4 * 3 * 2, 5 * 4 * 3
+    cases.append(("h8", (4, 3, 2), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), 1.0, {
+        "u": rng.standard_normal(3 * nn),
+        "x": rng.random(nel),
+        "modes": rng.standard_normal((11, 3 * nn)),         # point block vector, two-digit suffixes
+        "fields": rng.random((nel, 2)),                     # cell block vector along the second axis
+        "z": rng.standard_normal(nn) + 1j * rng.standard_normal(nn),
+        "bad": rng.random(7),                               # neither cell nor point data: skipped
+    }))
+    nel, nn = 5 * 3, 6 * 4
+    cases.append(("q4", (5, 3, 0), (0.5, 0.25, 1.0), (1.0, -2.0, 0.0), 2.5, {
+        "u": rng.standard_normal(2 * nn),                   # padded to three components
+        "uc": rng.standard_normal(2 * nn) + 1j * rng.standard_normal(2 * nn),
+        "x": rng.random(nel).astype(np.float32),
+        "xc": rng.random((3, nel)) + 1j * rng.random((3, nel)),
+    }))
+    return cases
+
+
+def vti_files(pym):
+    for name, shp, size, origin, scale, vecs in vti_cases():
+        d = pym.VoxelDomain(*shp, *size)
+        d.origin = np.array(origin)
+        d.write_to_vti(vecs, filename=os.path.join(OUT, f"vti_{name}.vti"), scale=scale)
+        print("wrote", f"vti_{name}.vti")
+
+
 if __name__ == "__main__":
     warnings.filterwarnings("ignore")
     pym = import_reference()
-    maps_and_k0(pym)
-    assembly(pym)
-    filters(pym)
-    multigrid(pym)
-    pipeline(pym, "h8_mg", (8, 4, 4), "conv", 1.5, 3, 1e-8)
-    pipeline(pym, "q4_mg", (16, 8), "density", 2.0, 3, 1e-8, plane="stress")
-    pipeline(pym, "h8_direct", (6, 4, 2), "density", 1.5, 0, 1e-8)
-    oc_mbb(pym)
+    which = sys.argv[1:] or ["all"]
+    if "all" in which:
+        maps_and_k0(pym)
+        assembly(pym)
+        filters(pym)
+        multigrid(pym)
+        pipeline(pym, "h8_mg", (8, 4, 4), "conv", 1.5, 3, 1e-8)
+        pipeline(pym, "q4_mg", (16, 8), "density", 2.0, 3, 1e-8, plane="stress")
+        pipeline(pym, "h8_direct", (6, 4, 2), "density", 1.5, 0, 1e-8)
+        oc_mbb(pym)
+    if "all" in which or "vti" in which:
+        vti_files(pym)
