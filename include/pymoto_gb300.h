@@ -273,6 +273,34 @@ int pmg_oc_status(const void* scratch);
  * the status at its next synchronisation instead of adding one. */
 int pmg_oc_status_async(const void* scratch, unsigned* status, void* stream);
 
+/* ---- Method of Moving Asymptotes (MMA.step / mmasub / subsolv, pymoto/common/mma.py:96-474) ----------
+ * One design update: the asymptote offsets adapt from xold1/xold2 (when params.adapt), the convex separable
+ * approximation is built from the responses g[m+1] and their sensitivities dg[(m+1) x n] (row-major; row 0 the
+ * objective), and its subproblem is solved by the primal-dual Newton method down to params.epsimin (already
+ * scaled by sqrt(m + n)), all in one cooperative launch (plus a reset and a status kernel).  The unconstrained
+ * problem is passed with pyMOTO's dummy constraint (g = -1, zero sensitivities).  xmin, xmax, move are
+ * per-variable arrays; offset is updated in place; low/upp receive the asymptotes, xnew the new design and
+ * info (device, m + 6 doubles): gest[0..m], dk, status (0 ok, 1 a bounded wait expired, 2 singular Newton
+ * system), epsilon levels, Newton iterations, line-search trials.  scratch >= pmg_mma_scratch_bytes(n, m). */
+#define PMG_MMA_MAX_M 4
+enum { PMG_MMA_1987 = 0, PMG_MMA_2007 = 1, PMG_MMA_GCMMA = 2 };
+typedef struct {
+  int version;   /* PMG_MMA_1987, PMG_MMA_2007 or PMG_MMA_GCMMA */
+  int m;         /* general constraints, 1..PMG_MMA_MAX_M */
+  int adapt;     /* adapt the asymptote offsets from xold1, xold2 */
+  int maxit;     /* Newton and line-search iteration limit (pyMOTO: 400) */
+  double a0, albefa, asyincr, asydecr;
+  double offmin, offmax;          /* offset clip: 1/asybound^2, asybound */
+  double epsimin;                 /* epsimin * sqrt(m + n) */
+  double rho[PMG_MMA_MAX_M + 1];  /* MMA2007: rho[0]; GCMMA: one per response */
+  double a[PMG_MMA_MAX_M], c[PMG_MMA_MAX_M], d[PMG_MMA_MAX_M];
+} pmg_mma_params;
+size_t pmg_mma_scratch_bytes(int64_t n, int m);
+int pmg_mma_update(int64_t n, const pmg_mma_params* params_host, const double* xval, const double* xold1,
+                   const double* xold2, const double* xmin, const double* xmax, const double* move, const double* g,
+                   const double* dg, double* offset, double* low, double* upp, double* xnew, double* info,
+                   void* scratch, void* stream);
+
 /* ---- learned warm start (no counterpart in the reference: the reference solves every design from the
  * previous solution only).  A 3-level convolutional encoder-decoder on the voxel grid of a coarse
  * multigrid level, trained on the device on (density, displacement) pairs of the solver.  Layout

@@ -2,7 +2,8 @@
 
 Drop-in GPU Modules and LinearSolvers with pyMOTO's API:
   DensityFilter, FilterConv, SIMP / MathExpression (SIMP form), AssembleStiffness, LinSolve, EinSum,
-  CG, GeometricMultigrid, DampedJacobi, DenseCholesky, MixedPrecisionCG, OC, WriteToVTI (VoxelDomain.write_to_vti).
+  CG, GeometricMultigrid, DampedJacobi, DenseCholesky, MixedPrecisionCG, OC, MMA (MMA1987 / MMA2007 / GCMMA), Scaling,
+  WriteToVTI (VoxelDomain.write_to_vti).
 The arithmetic runs in hand-written CUDA kernels of libpymoto_gb300.so through its C ABI
 (include/pymoto_gb300.h); there is no CPU fallback.
 """
@@ -10,9 +11,10 @@ from . import _lib
 from .core import HOST_RUNTIME, Module, Network, Signal
 from .domain import VoxelDomain
 from .modules import (AssembleStiffness, DensityFilter, DeviceDyad, EinSum, FilterConv, LinSolve, MathExpression,
-                      SIMP)
+                      SIMP, Scaling)
 from .operators import Grid, StencilOperator, StiffnessOperator, element_stiffness
 from .optimizers import OC
+from .mma import MMA
 from .solvers import (CG, Chebyshev, DampedJacobi, DenseCholesky, GeometricMultigrid, LinearSolver,
                       MixedPrecisionCG, Preconditioner)
 from .autograd import ComplianceObjective
@@ -23,4 +25,5 @@ __version__ = "0.1.0"
 __all__ = ["AssembleStiffness", "DensityFilter", "DeviceDyad", "EinSum", "FilterConv", "LinSolve", "MathExpression",
            "SIMP", "Grid", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "Chebyshev", "DampedJacobi",
            "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
-           "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI"]
+           "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI", "Scaling",
+           "MMA"]

@@ -82,6 +82,8 @@ SIGNATURES = {
     "pmg_oc_status": (I, [P]),
     "pmg_oc_status_async": (I, [P, P, P]),
     "pmg_oc_update": (I, [L, P, P, P, D, D, D, D, D, D, D, P, P]),
+    "pmg_mma_scratch_bytes": (c_size_t, [L, I]),
+    "pmg_mma_update": (I, [L] + [P] * 16),
     "pmg_nn_conv3d_forward": (I, [I, I, I, I, I, I, P, P, P, I, P, P, P]),
     "pmg_nn_conv3d_backward_data": (I, [I, I, I, I, I, P, P, P, P]),
     "pmg_nn_wgrad_scratch_bytes": (c_size_t, [I, I, I, I, I]),
@@ -100,7 +102,7 @@ SIGNATURES = {
 
 # Returns that are values, not statuses
 _VALUE_RETURNING = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_reduce_scratch_bytes",
-                    "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth"}
+                    "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth", "pmg_mma_scratch_bytes"}
 
 F64, F32 = 0, 1
 MATVEC, RESIDUAL, JACOBI = 0, 1, 2
@@ -154,7 +156,7 @@ def _arg(a):
 _HOST_ONLY = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_element_stiffness", "pmg_galerkin_table",
               "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth",
               "pmg_cholesky_inverse_f32_scratch_bytes", "pmg_nn_wgrad_scratch_bytes", "pmg_oc_status",
-              "pmg_coarse_ordering", "pmg_oc_status_async"}
+              "pmg_coarse_ordering", "pmg_oc_status_async", "pmg_mma_scratch_bytes"}
 
 
 def _launches(name, args):
@@ -168,6 +170,8 @@ def _launches(name, args):
         return 2 if args[9] is not None and int(args[10]) > 0 else 1
     if name == "pmg_nn_conv3d_backward_weights":
         return 2
+    if name == "pmg_mma_update":
+        return 3          # reset, the cooperative solve, status
     if name == "pmg_oc_update":
         # init + one cooperative launch while the design fits the registers of the resident CTAs (2 CTAs of
         # 256 threads x 8 elements per SM); above that init + prepare + one launch per step + final

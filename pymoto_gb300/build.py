@@ -20,6 +20,8 @@ BUILD_DIR = os.path.join(ROOT, "_build")
 LIB_NAME = "libpymoto_gb300.so"
 LIB_PATH = os.path.join(HERE, LIB_NAME)
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+# per-file flags: the MMA update keeps numpy's rounding of every element-wise expression (no FMA contraction)
+FILE_FLAGS = {"mma.cu": ["--fmad=false"]}
 
 
 def _nvcc():
@@ -45,6 +47,7 @@ def _fingerprint():
         with open(path, "rb") as f:
             h.update(path.encode() + f.read())
     h.update(" ".join(_flags()).encode())
+    h.update(repr(sorted(FILE_FLAGS.items())).encode())
     return h.hexdigest()
 
 
@@ -62,7 +65,7 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(BUILD_DIR, os.path.basename(src)[:-3] + ".o")
-        cmd = [nvcc] + _flags() + ["-c", src, "-o", obj]
+        cmd = [nvcc] + _flags() + FILE_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")

@@ -453,3 +453,61 @@ class EinSum(Module):
         call("pmg_scale", F64, b.numel(), da, b, df, stream())
         call("pmg_scale", F64, a.numel(), db, a, df, stream())
         return [_from_device(da, ka), _from_device(db, kb)]
+
+
+def _sqrt(v):
+    return torch.sqrt(v) if isinstance(v, torch.Tensor) else np.sqrt(v)
+
+
+def _norm(v):
+    return torch.linalg.vector_norm(v) if isinstance(v, torch.Tensor) else np.linalg.norm(v)
+
+
+class Scaling(Module):
+    """pyMOTO's Scaling of a scalar response (pymoto/modules/scaling.py:5-83): objective y = s x / |x0|, upper
+    limit s (x - max) / |max|, lower limit s (min - x) / |min|, or the smoothed two-sided form.  A device
+    scalar (0-d CUDA tensor, e.g. EinSum's output) stays on the device; the factor of the objective form is
+    taken from the first input, as in pyMOTO."""
+
+    def __init__(self, scaling: float = 100.0, minval: float = None, maxval: float = None, minmax_smooth: float = 1.0):
+        self.minval = minval
+        self.maxval = maxval
+        self.scaling = scaling
+        self.minmax_smooth = minmax_smooth
+        self.sf = None
+        self.reset_scaling()
+
+    def __call__(self, x):
+        if self.sf is None:
+            self.sf = self.scaling / _norm(x)
+        if self.minval is not None and self.maxval is not None:
+            midp = (self.minval + self.maxval) / 2
+            diff = (self.maxval - self.minval) / 2
+            g = _sqrt((x - midp) ** 2 + self.minmax_smooth * diff ** 2) - np.sqrt((1 + self.minmax_smooth) * diff ** 2)
+        elif self.minval is not None:
+            nrm = 1 if self.minval == 0 else abs(self.minval)
+            g = (self.minval - x) / nrm
+        elif self.maxval is not None:
+            nrm = 1 if self.maxval == 0 else abs(self.maxval)
+            g = (x - self.maxval) / nrm
+        else:
+            g = x
+        return g * self.sf
+
+    def _sensitivity(self, dy):
+        dg = dy * self.sf
+        if self.minval is not None and self.maxval is not None:
+            midp = (self.minval + self.maxval) / 2
+            diff = (self.maxval - self.minval) / 2
+            x = self.get_input_states()
+            return dg * (x - midp) / _sqrt((x - midp) ** 2 + self.minmax_smooth * diff ** 2)
+        if self.minval is not None:
+            nrm = 1 if self.minval == 0 else abs(self.minval)
+            return -dg / nrm
+        if self.maxval is not None:
+            nrm = 1 if self.maxval == 0 else abs(self.maxval)
+            return dg / nrm
+        return dg
+
+    def reset_scaling(self):
+        self.sf = self.scaling if (self.minval is not None or self.maxval is not None) else None

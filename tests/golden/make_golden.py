@@ -6,6 +6,7 @@ at module level for plotting only.  The fixtures are small .npz files; the tests
 
     python tests/golden/make_golden.py          # every fixture
     python tests/golden/make_golden.py vti      # the VTI files only
+    python tests/golden/make_golden.py mma      # the MMA steps only
 """
 import os
 import sys
@@ -185,6 +186,45 @@ def oc_mbb(pym):
     save("oc_mbb.npz", bc=bc, f=f, c_hist=np.array(hist), x_final=sx.state.copy())
 
 
+def mma_mbb(pym):
+    """pyMOTO's MMA on a 30x10 half-MBB beam (DensityFilter r=1.5, plane stress, direct solve): objective
+    Scaling(100) of the compliance, constraint 10 (sum(xf)/nel - 0.5).  Per step the inputs (x, g, dg) and the
+    outputs (xnew, low, upp, gest, dk) are stored, for MMA2007 (8 steps), MMA1987 (5 steps) and the unconstrained
+    form (objective only, 4 steps), so that the MMA update can be checked without the network, and for GCMMA
+    (4 outer steps, whose inner iterations evaluate the network)."""
+    out = {}
+    for tag, version, constrained, steps in [("v2007", "MMA2007", True, 8), ("v1987", "MMA1987", True, 5),
+                                             ("unc", "MMA2007", False, 4), ("gcmma", "GCMMA", True, 4)]:
+        d = pym.VoxelDomain(30, 10)
+        bc = np.concatenate([2 * d.nodes[0, :].flatten(), [2 * d.get_nodenumber(30, 0) + 1]])
+        f = np.zeros(d.nnodes * 2)
+        f[2 * d.get_nodenumber(0, 10) + 1] = -1.0
+        sx = pym.Signal("x", np.full(d.nel, 0.5))
+        with pym.Network() as fn:
+            xf = pym.DensityFilter(d, radius=1.5)(sx)
+            xs = pym.MathExpression("1e-9 + (1-1e-9)*inp0^3")(xf)
+            K = pym.AssembleStiffness(d, bc=bc, plane="stress")(xs)
+            u = pym.LinSolve(hermitian=True, symmetric=True)(K, f)
+            c = pym.EinSum("i,i->")(u, f)
+            g0 = pym.Scaling(scaling=100.0)(c)
+            vol = pym.EinSum("i->")(xf)
+            g1 = pym.MathExpression(f"10*(inp0/{d.nel} - 0.5)")(vol)
+        resp = [g0, g1] if constrained else [g0]
+        mma = pym.MMA(sx, resp, fn, move=0.2, verbosity=0, mmaversion=version)
+        rec = {k: [] for k in ["x", "g", "dg", "xnew", "low", "upp", "offset", "gest", "dk"]}
+        xval = mma.x
+        for _ in range(steps):
+            xnew, g, dg = mma.step(x=xval)
+            for k, v in [("x", xval), ("g", g), ("dg", dg), ("xnew", xnew), ("low", mma.low), ("upp", mma.upp),
+                         ("offset", mma.offset), ("gest", mma.gest), ("dk", mma.dk)]:
+                rec[k].append(np.array(v, dtype=float).copy())
+            xval = xnew
+        for k, v in rec.items():
+            out[f"{tag}_{k}"] = np.array(v)
+        out[f"{tag}_bc"], out[f"{tag}_f"] = bc, f
+    save("mma_mbb.npz", **out)
+
+
 def vti_cases():
     """The VTI output cases: (name, (nelx, nely, nelz), element size, origin, scale, vectors).  Pure numpy, so
     the tests rebuild the same inputs without pyMOTO."""
@@ -232,3 +272,5 @@ if __name__ == "__main__":
         oc_mbb(pym)
     if "all" in which or "vti" in which:
         vti_files(pym)
+    if "all" in which or "mma" in which:
+        mma_mbb(pym)
