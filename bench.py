@@ -57,8 +57,9 @@ def parse():
     ap.add_argument("--levels", type=int, default=GPU_LEVELS)
     ap.add_argument("--sweeps", type=int, default=SWEEPS)
     ap.add_argument("--coarse-sweeps", type=int, default=None)
-    ap.add_argument("--case", default=None, choices=["operator"],
-                    help="instead of the bench: time the level-0 operator kernels alone (a small case for ncu)")
+    ap.add_argument("--case", default=None, choices=["operator", "mma"],
+                    help="instead of the bench: time the level-0 operator kernels alone (a small case for ncu), or "
+                         "the device MMA update of the 96x48x48 design against the numpy MMA")
     ap.add_argument("--arms", default="plain_fp64,mixed,mixed_learned",
                     help="plain_fp64 (the reference's method), mixed, mixed_learned (headline: with the learned "
                          "warm start), ablations: mixed_jacobi, plain_fp64_cheb")
@@ -462,10 +463,56 @@ def operator_case(args):
     print(json.dumps({"case": "operator", "shape": list(shape), **out}))
 
 
+def mma_case(args):
+    """The MMA update of a 96x48x48 design (221,184 variables, one volume constraint) on the device: 2 warm-up
+    and 5 timed updates chained on their own output (CUDA events around each), then the numpy MMA of the
+    oracle on the host cores for the first update with the same inputs, and the largest difference of the two
+    designs.  Synthetic compliance-like inputs: x ~ U(0.2, 0.8), objective 10 with dc/dx ~ -U(0, 20)/n, volume
+    constraint mean(x) - 0.45 with gradient 1/n."""
+    import torch
+    from pymoto_gb300.mma import MMAUpdate
+    from oracle.mma import MMAOracle
+    shape = (96, 48, 48) if args.shape is None else tuple(int(v) for v in args.shape.split("x"))
+    n = int(np.prod([max(v, 1) for v in shape]))
+    rng = np.random.default_rng(7)
+    x0 = rng.uniform(0.2, 0.8, n)
+    dg = np.vstack([-rng.uniform(0.0, 2.0, n) * 10.0 / n, np.full(n, 1.0 / n)])
+    g = np.array([10.0, float(x0.mean() - 0.45)])
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    up = MMAUpdate(n, 2, 0.0, 1.0, move=0.2)
+    x, gd, dgd = dev(x0), dev(g), dev(dg)
+    first = None
+    times, newton = [], []
+    for k in range(7):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        xn = up.step(x, gd, dgd)
+        e1.record()
+        torch.cuda.synchronize()
+        if k == 0:
+            first = xn.cpu().numpy()
+        if k >= 2:
+            times.append(e0.elapsed_time(e1) * 1e3)
+            newton.append(up.stats["newton"])
+        x = xn
+    o = MMAOracle(n, 2, move=0.2)
+    t0 = time.perf_counter()
+    xo = o.step(x0, g, dg)
+    t_cpu = time.perf_counter() - t0
+    print(json.dumps({"case": "mma", "n": n, "m": 1, "update_us": float(np.mean(times)),
+                      "update_us_all": times, "newton_iterations": newton, "oracle_update_s": t_cpu,
+                      "oracle_newton_iterations": o.stats["newton"], "cpu_threads": os.cpu_count(),
+                      "max_abs_diff_first_update": float(np.abs(first - xo).max())}))
+
+
 def main():
     args = parse()
     if args.case == "operator":
         operator_case(args)
+        return
+    if args.case == "mma":
+        mma_case(args)
         return
     rank, world, local_rank = dist_info()
     threads = os.cpu_count() or 1
