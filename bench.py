@@ -464,11 +464,11 @@ def operator_case(args):
 
 
 def mma_case(args):
-    """The MMA update of a 96x48x48 design (221,184 variables, one volume constraint) on the device: 2 warm-up
-    and 5 timed updates chained on their own output (CUDA events around each), then the numpy MMA of the
-    oracle on the host cores for the first update with the same inputs, and the largest difference of the two
-    designs.  Synthetic compliance-like inputs: x ~ U(0.2, 0.8), objective 10 with dc/dx ~ -U(0, 20)/n, volume
-    constraint mean(x) - 0.45 with gradient 1/n."""
+    """The MMA update of a 96x48x48 design (221,184 variables, one volume constraint) on the device, fast and exact
+    variants: 2 warm-up and 5 timed updates chained on their own output (CUDA events around each), then the numpy
+    MMA of the oracle on the host cores for the first update with the same inputs, and the largest difference of
+    the designs.  Synthetic compliance-like inputs: x ~ U(0.2, 0.8), objective 10 with dc/dx ~ -U(0, 20)/n,
+    volume constraint mean(x) - 0.45 with gradient 1/n."""
     import torch
     from pymoto_gb300.mma import MMAUpdate
     from oracle.mma import MMAOracle
@@ -479,31 +479,33 @@ def mma_case(args):
     dg = np.vstack([-rng.uniform(0.0, 2.0, n) * 10.0 / n, np.full(n, 1.0 / n)])
     g = np.array([10.0, float(x0.mean() - 0.45)])
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
-    up = MMAUpdate(n, 2, 0.0, 1.0, move=0.2)
-    x, gd, dgd = dev(x0), dev(g), dev(dg)
-    first = None
-    times, newton = [], []
-    for k in range(7):
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        xn = up.step(x, gd, dgd)
-        e1.record()
-        torch.cuda.synchronize()
-        if k == 0:
-            first = xn.cpu().numpy()
-        if k >= 2:
-            times.append(e0.elapsed_time(e1) * 1e3)
-            newton.append(up.stats["newton"])
-        x = xn
     o = MMAOracle(n, 2, move=0.2)
     t0 = time.perf_counter()
     xo = o.step(x0, g, dg)
     t_cpu = time.perf_counter() - t0
-    print(json.dumps({"case": "mma", "n": n, "m": 1, "update_us": float(np.mean(times)),
-                      "update_us_all": times, "newton_iterations": newton, "oracle_update_s": t_cpu,
-                      "oracle_newton_iterations": o.stats["newton"], "cpu_threads": os.cpu_count(),
-                      "max_abs_diff_first_update": float(np.abs(first - xo).max())}))
+    out = {"case": "mma", "n": n, "m": 1, "oracle_update_s": t_cpu, "oracle_newton_iterations": o.stats["newton"],
+           "cpu_threads": os.cpu_count()}
+    for variant, exact in (("fast", False), ("exact", True)):
+        up = MMAUpdate(n, 2, 0.0, 1.0, move=0.2, exact=exact)
+        x, gd, dgd = dev(x0), dev(g), dev(dg)
+        first = None
+        times, newton = [], []
+        for k in range(7):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            xn = up.step(x, gd, dgd)
+            e1.record()
+            torch.cuda.synchronize()
+            if k == 0:
+                first = xn.cpu().numpy()
+            if k >= 2:
+                times.append(e0.elapsed_time(e1) * 1e3)
+                newton.append(up.stats["newton"])
+            x = xn
+        out[variant] = {"update_us": float(np.mean(times)), "update_us_all": times, "newton_iterations": newton,
+                        "max_abs_diff_first_update": float(np.abs(first - xo).max())}
+    print(json.dumps(out))
 
 
 def main():

@@ -289,6 +289,8 @@ typedef struct {
   int m;         /* general constraints, 1..PMG_MMA_MAX_M */
   int adapt;     /* adapt the asymptote offsets from xold1, xold2 */
   int maxit;     /* Newton and line-search iteration limit (pyMOTO: 400) */
+  int exact;     /* 1: divide wherever pyMOTO divides (numpy's rounding); 0: one reciprocal per denominator */
+  int reserved;  /* 0 */
   double a0, albefa, asyincr, asydecr;
   double offmin, offmax;          /* offset clip: 1/asybound^2, asybound */
   double epsimin;                 /* epsimin * sqrt(m + n) */

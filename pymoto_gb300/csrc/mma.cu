@@ -15,9 +15,10 @@
 // thread in every pass.  A line-search trial is x_base + steg * dx evaluated on the fly; the accepted step is
 // written back by the next pass that starts from the iterate.
 //
-// Arithmetic is FP64 with the operation order of the reference, and this file is compiled without FMA
-// contraction, so the element-wise values round as numpy's do; only the order of the sums over elements (and
-// the (m+1)-system's elimination) differ.  Every wait is bounded (MMA_SPIN_LIMIT polls), every loop has the
+// Arithmetic is FP64.  The exact variant keeps the operation order of the reference, and this file is compiled
+// without FMA contraction, so its element-wise values round as numpy's do; only the order of the sums over
+// elements (and the (m+1)-system's elimination) differ.  The fast variant (the default of the host class)
+// replaces repeated divisions by one reciprocal each; FP64 division, not memory, bounds this kernel on GB300.  Every wait is bounded (MMA_SPIN_LIMIT polls), every loop has the
 // reference's iteration limits, and a singular Newton system stops the solve with a status instead of a fault.
 #include <algorithm>
 #include <cmath>
@@ -44,7 +45,7 @@ struct MMAArrays {
   int64_t n;
   const double *xval, *xold1, *xold2, *xmin, *xmax, *move, *g, *dg;
   double *offset, *low, *upp, *xnew, *info;
-  double *xb, *xsib, *etab, *dxv, *dxsiv, *detav, *alfa, *beta, *P, *Q, *GG;
+  double *xb, *xsib, *etab, *dxv, *dxsiv, *detav, *alfa, *beta, *rxa, *rbx, *P, *Q, *GG;
 };
 
 enum { RED_SUM = 0, RED_MAX = 1, RED_MIN = 2 };
@@ -128,6 +129,15 @@ __device__ bool mma_reduce(const double (&acc)[R], int nsum, int nmax, MMAHeader
   return true;
 }
 
+// acc + a * b: two roundings in the exact variant (numpy's), one fused rounding in the fast one
+template <bool EXACT>
+__device__ __forceinline__ double macc(double acc, double a, double b) {
+  if constexpr (EXACT)
+    return acc + a * b;
+  else
+    return fma(a, b, acc);
+}
+
 // Python's max(a, b, ...): the first of the largest (a later value replaces the current one only if greater).
 __device__ __forceinline__ double py_max(const double* v, int k) {
   double r = v[0];
@@ -146,7 +156,11 @@ struct MMAScalars {
   int has_pend, err;
 };
 
-template <int M>
+// EXACT: every element-wise expression divides where the reference divides (values round as numpy's).
+// Fast: each distinct denominator is inverted once and the quotients become products (1/(x-alfa), 1/(beta-x)
+// and 1/diagx are kept from the Newton pass for the direction pass): 9 instead of 28 FP64 divisions per
+// Newton iteration, each result within a few ulp of the exact one.
+template <int M, bool EXACT>
 __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAArrays A, MMAHeader* h) {
   constexpr int M1 = M + 1;
   __shared__ MMAScalars<M> S;
@@ -265,10 +279,14 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
       const double ru = 1.0 / ux1, rl = 1.0 / xl1;
 #pragma unroll
       for (int i = 0; i < M; ++i) {
-        acc[i] += A.P[(i + 1) * n + j] * ru;
-        acc[M + i] += A.Q[(i + 1) * n + j] * rl;
+        acc[i] = macc<EXACT>(acc[i], A.P[(i + 1) * n + j], ru);
+        acc[M + i] = macc<EXACT>(acc[M + i], A.Q[(i + 1) * n + j], rl);
       }
-      const double dpsidx = plam / (ux1 * ux1) - qlam / (xl1 * xl1);
+      double dpsidx;
+      if constexpr (EXACT)
+        dpsidx = plam / (ux1 * ux1) - qlam / (xl1 * xl1);
+      else
+        dpsidx = plam * (ru * ru) - qlam * (rl * rl);
       const double rex = (dpsidx - xsi) + eta;
       const double rexsi = xsi * (x - A.alfa[j]) - epsi;
       const double reeta = eta * (A.beta[j] - x) - epsi;
@@ -333,31 +351,50 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
         A.etab[j] = eta;
       }
       const double ux1 = A.upp[j] - x, xl1 = x - A.low[j];
-      const double ux2 = ux1 * ux1, xl2 = xl1 * xl1;
-      const double uxinv1 = 1.0 / ux1, xlinv1 = 1.0 / xl1, uxinv2 = 1.0 / ux2, xlinv2 = 1.0 / xl2;
       const double plam = lam_dot(lam, A.P, j), qlam = lam_dot(lam, A.Q, j);
-      double gg[M];
-#pragma unroll
-      for (int i = 0; i < M; ++i) {
-        const double P1 = A.P[(i + 1) * n + j], Q1 = A.Q[(i + 1) * n + j];
-        acc[i] += P1 * uxinv1;
-        acc[M + i] += Q1 * xlinv1;
-        gg[i] = P1 * uxinv2 - Q1 * xlinv2;
-      }
-      const double dpsidx = plam / ux2 - qlam / xl2;
       const double xa = x - A.alfa[j], bx = A.beta[j] - x;
-      const double delx = (dpsidx - epsi / xa) + epsi / bx;
-      const double diagx = ((2.0 * (plam / (ux1 * ux2) + qlam / (xl1 * xl2))) + xsi / xa) + eta / bx;
-      const double dd = delx / diagx;
+      double gg[M], delx, diagx, rdg;
+      if constexpr (EXACT) {
+        const double ux2 = ux1 * ux1, xl2 = xl1 * xl1;
+        const double uxinv1 = 1.0 / ux1, xlinv1 = 1.0 / xl1, uxinv2 = 1.0 / ux2, xlinv2 = 1.0 / xl2;
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+          const double P1 = A.P[(i + 1) * n + j], Q1 = A.Q[(i + 1) * n + j];
+          acc[i] += P1 * uxinv1;
+          acc[M + i] += Q1 * xlinv1;
+          gg[i] = P1 * uxinv2 - Q1 * xlinv2;
+        }
+        const double dpsidx = plam / ux2 - qlam / xl2;
+        delx = (dpsidx - epsi / xa) + epsi / bx;
+        diagx = ((2.0 * (plam / (ux1 * ux2) + qlam / (xl1 * xl2))) + xsi / xa) + eta / bx;
+        rdg = 0.0;
+      } else {
+        const double ru = 1.0 / ux1, rl = 1.0 / xl1, ru2 = ru * ru, rl2 = rl * rl;
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+          const double P1 = A.P[(i + 1) * n + j], Q1 = A.Q[(i + 1) * n + j];
+          acc[i] = fma(P1, ru, acc[i]);
+          acc[M + i] = fma(Q1, rl, acc[M + i]);
+          gg[i] = P1 * ru2 - Q1 * rl2;
+        }
+        const double dpsidx = plam * ru2 - qlam * rl2;
+        const double rxa = 1.0 / xa, rbx = 1.0 / bx;
+        delx = (dpsidx - epsi * rxa) + epsi * rbx;
+        diagx = ((2.0 * (plam * (ru2 * ru) + qlam * (rl2 * rl))) + xsi * rxa) + eta * rbx;
+        rdg = 1.0 / diagx;
+        A.rxa[j] = rxa;
+        A.rbx[j] = rbx;
+      }
+      const double dd = EXACT ? delx / diagx : delx * rdg;
 #pragma unroll
       for (int i = 0; i < M; ++i) {
-        acc[2 * M + i] += gg[i] * dd;
-        const double gi = gg[i] / diagx;
+        acc[2 * M + i] = macc<EXACT>(acc[2 * M + i], gg[i], dd);
+        const double gi = EXACT ? gg[i] / diagx : gg[i] * rdg;
 #pragma unroll
-        for (int l = 0; l < M; ++l) acc[3 * M + i * M + l] += gi * gg[l];
+        for (int l = 0; l < M; ++l) acc[3 * M + i * M + l] = macc<EXACT>(acc[3 * M + i * M + l], gi, gg[l]);
       }
       A.dxv[j] = delx;
-      A.dxsiv[j] = diagx;
+      A.dxsiv[j] = EXACT ? diagx : rdg;   // the fast variant keeps 1/diagx
 #pragma unroll
       for (int i = 0; i < M; ++i) A.GG[i * n + j] = gg[i];
     }
@@ -444,22 +481,35 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
 #pragma unroll
     for (int i = 0; i < M; ++i) dlam[i] = S.dlam[i];
     for (int64_t j = j0; j < n; j += stride) {
-      const double x = A.xb[j], xsi = A.xsib[j], eta = A.etab[j];
-      const double delx = A.dxv[j], diagx = A.dxsiv[j];
+      const double xsi = A.xsib[j], eta = A.etab[j];
+      const double delx = A.dxv[j];
       double dlg = dlam[0] * A.GG[j];
 #pragma unroll
       for (int i = 1; i < M; ++i) dlg = dlg + dlam[i] * A.GG[i * n + j];
-      const double dx = -delx / diagx - dlg / diagx;
-      const double xa = x - A.alfa[j], bx = A.beta[j] - x;
-      const double dxsi = (-xsi + epsi / xa) - (xsi * dx) / xa;
-      const double deta = (-eta + epsi / bx) + (eta * dx) / bx;
+      double dx, dxsi, deta, rb, ra;
+      if constexpr (EXACT) {
+        const double x = A.xb[j], diagx = A.dxsiv[j];
+        dx = -delx / diagx - dlg / diagx;
+        const double xa = x - A.alfa[j], bx = A.beta[j] - x;
+        dxsi = (-xsi + epsi / xa) - (xsi * dx) / xa;
+        deta = (-eta + epsi / bx) + (eta * dx) / bx;
+        rb = dx / bx;
+        ra = dx / xa;
+      } else {
+        const double rdg = A.dxsiv[j], rxa = A.rxa[j], rbx = A.rbx[j];
+        dx = (-delx - dlg) * rdg;
+        dxsi = (-xsi + epsi * rxa) - (xsi * dx) * rxa;
+        deta = (-eta + epsi * rbx) + (eta * dx) * rbx;
+        rb = dx * rbx;
+        ra = dx * rxa;
+      }
       A.dxv[j] = dx;
       A.dxsiv[j] = dxsi;
       A.detav[j] = deta;
-      acc[0] = nmax(acc[0], dx / bx);
+      acc[0] = nmax(acc[0], rb);
       acc[1] = nmin(acc[1], dxsi / xsi);
       acc[2] = nmin(acc[2], deta / eta);
-      acc[3] = nmin(acc[3], dx / xa);
+      acc[3] = nmin(acc[3], ra);
     }
     if (!mma_reduce<4>(acc, 0, 1, h, ++gen, tot, wsum)) return false;
     if (threadIdx.x == 0) {
@@ -578,7 +628,7 @@ __global__ void mma_status_kernel(const MMAHeader* h, double* info, int m) {
 
 inline size_t mma_header_bytes() { return (sizeof(MMAHeader) + 255) & ~size_t(255); }
 
-template <int M>
+template <int M, bool EXACT>
 int mma_launch(const pmg_mma_params& p, const MMAArrays& A, MMAHeader* h, cudaStream_t st) {
   static int max_blocks[64] = {0};
   int dev = 0;
@@ -590,7 +640,7 @@ int mma_launch(const pmg_mma_params& p, const MMAArrays& A, MMAHeader* h, cudaSt
     int sms = 0, per_sm = 0, coop = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mma_kernel<M>, MMA_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mma_kernel<M, EXACT>, MMA_THREADS, 0);
     max_blocks[dev] = coop && per_sm > 0 ? std::min(sms * per_sm, MMA_MAX_BLOCKS) : -1;
   }
   if (max_blocks[dev] < 0) {
@@ -602,7 +652,7 @@ int mma_launch(const pmg_mma_params& p, const MMAArrays& A, MMAHeader* h, cudaSt
   pmg_mma_params pc = p;
   MMAArrays Ac = A;
   void* args[] = {(void*)&pc, (void*)&Ac, (void*)&h};
-  cudaError_t e = cudaLaunchCooperativeKernel((const void*)mma_kernel<M>, dim3(grid), dim3(MMA_THREADS), args, 0, st);
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)mma_kernel<M, EXACT>, dim3(grid), dim3(MMA_THREADS), args, 0, st);
   if (e != cudaSuccess) {
     set_error(cudaGetErrorString(e));
     return PMG_CUDA_ERR;
@@ -618,7 +668,7 @@ extern "C" {
 
 size_t pmg_mma_scratch_bytes(int64_t n, int m) {
   if (n <= 0 || m < 1 || m > PMG_MMA_MAX_M) return 0;
-  return mma_header_bytes() + (size_t)(8 + 2 * (m + 1) + m) * (size_t)n * sizeof(double);
+  return mma_header_bytes() + (size_t)(10 + 2 * (m + 1) + m) * (size_t)n * sizeof(double);
 }
 
 int pmg_mma_update(int64_t n, const pmg_mma_params* params_host, const double* xval, const double* xold1,
@@ -630,6 +680,7 @@ int pmg_mma_update(int64_t n, const pmg_mma_params* params_host, const double* x
     return PMG_BAD_ARG;
   const pmg_mma_params& p = *params_host;
   if (p.m < 1 || p.m > PMG_MMA_MAX_M || p.maxit < 1 || p.maxit > 100000 || !(p.epsimin > 0.0)) return PMG_BAD_ARG;
+  if (p.exact != 0 && p.exact != 1) return PMG_BAD_ARG;
   if (p.version != PMG_MMA_1987 && p.version != PMG_MMA_2007 && p.version != PMG_MMA_GCMMA) return PMG_BAD_ARG;
   if (p.adapt && (!xold1 || !xold2)) return PMG_BAD_ARG;
   if (xnew == xval || xnew == low || xnew == upp || low == upp || offset == xnew) return PMG_BAD_ARG;
@@ -652,7 +703,7 @@ int pmg_mma_update(int64_t n, const pmg_mma_params* params_host, const double* x
   A.upp = upp;
   A.xnew = xnew;
   A.info = info;
-  double** slots[] = {&A.xb, &A.xsib, &A.etab, &A.dxv, &A.dxsiv, &A.detav, &A.alfa, &A.beta};
+  double** slots[] = {&A.xb, &A.xsib, &A.etab, &A.dxv, &A.dxsiv, &A.detav, &A.alfa, &A.beta, &A.rxa, &A.rbx};
   for (double** s : slots) {
     *s = arr;
     arr += n;
@@ -664,11 +715,20 @@ int pmg_mma_update(int64_t n, const pmg_mma_params* params_host, const double* x
   A.GG = arr;
   mma_init_kernel<<<1, 256, 0, st>>>(h);
   int rc;
-  switch (p.m) {
-    case 1: rc = mma_launch<1>(p, A, h, st); break;
-    case 2: rc = mma_launch<2>(p, A, h, st); break;
-    case 3: rc = mma_launch<3>(p, A, h, st); break;
-    default: rc = mma_launch<4>(p, A, h, st); break;
+  if (p.exact) {
+    switch (p.m) {
+      case 1: rc = mma_launch<1, true>(p, A, h, st); break;
+      case 2: rc = mma_launch<2, true>(p, A, h, st); break;
+      case 3: rc = mma_launch<3, true>(p, A, h, st); break;
+      default: rc = mma_launch<4, true>(p, A, h, st); break;
+    }
+  } else {
+    switch (p.m) {
+      case 1: rc = mma_launch<1, false>(p, A, h, st); break;
+      case 2: rc = mma_launch<2, false>(p, A, h, st); break;
+      case 3: rc = mma_launch<3, false>(p, A, h, st); break;
+      default: rc = mma_launch<4, false>(p, A, h, st); break;
+    }
   }
   if (rc != PMG_OK) return rc;
   mma_status_kernel<<<1, 32, 0, st>>>(h, info, p.m);

@@ -3,7 +3,7 @@
 Same interface as pyMOTO's MMA: MMA(variables, responses, function, slice_network=False, move=0.1, xmin=0.0,
 xmax=1.0, verbosity=2, mmaversion="MMA2007", **kwargs).step(x, g, dg) / optimize(maxiter, tolx, tolf), with
 pyMOTO's options (a0, epsimin, cCoef, albefa, asyinit, asyincr, asydecr, asybound, gcmma_maxit, a, c) and
-versions MMA1987, MMA2007 and GCMMA.  The asymptote adaptation, the separable approximation and the whole
+versions MMA1987, MMA2007 and GCMMA, plus exact=True for numpy's rounding of every element-wise value.  The asymptote adaptation, the separable approximation and the whole
 interior-point subproblem solve run in one cooperative CUDA launch (pmg_mma_update); design, sensitivities,
 offsets and asymptotes stay on the device.  The responses are read on the host only where pyMOTO reads them
 (the convergence test of optimize, the GCMMA acceptance test).
@@ -24,6 +24,7 @@ _VERSIONS = {"1987": 0, "2007": 1, "gcmma": 2}
 class _Params(ctypes.Structure):
     """pmg_mma_params of include/pymoto_gb300.h."""
     _fields_ = [("version", ctypes.c_int), ("m", ctypes.c_int), ("adapt", ctypes.c_int), ("maxit", ctypes.c_int),
+                ("exact", ctypes.c_int), ("reserved", ctypes.c_int),
                 ("a0", ctypes.c_double), ("albefa", ctypes.c_double), ("asyincr", ctypes.c_double),
                 ("asydecr", ctypes.c_double), ("offmin", ctypes.c_double), ("offmax", ctypes.c_double),
                 ("epsimin", ctypes.c_double), ("rho", ctypes.c_double * (MAX_M + 1)),
@@ -40,11 +41,15 @@ def _version_code(name):
 
 class MMAUpdate:
     """The device state of an MMA run (offsets, previous designs, asymptotes) and its update
-    x, g, dg -> xnew (mma.py:96-234).  Used by MMA; usable alone with device tensors."""
+    x, g, dg -> xnew (mma.py:96-234).  Used by MMA; usable alone with device tensors.
+
+    exact=True divides wherever pyMOTO divides, so every element-wise value rounds as numpy's; the default
+    (False) inverts each denominator once, about 3x fewer FP64 divisions, with the same subproblem solution to
+    its tolerance."""
 
     def __init__(self, n, m_resp, xmin, xmax, move=0.1, mmaversion="MMA2007", a0=1.0, epsimin=1e-10, cCoef=1e3,
                  albefa=0.1, asyinit=0.5, asyincr=1.2, asydecr=0.7, asybound=10.0, a=None, c=None, device=None,
-                 maxit=400):
+                 maxit=400, exact=False):
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self.n = int(n)
         self.m = max(1, int(m_resp) - 1)
@@ -59,6 +64,7 @@ class MMAUpdate:
         self.a0, self.epsimin, self.albefa = float(a0), float(epsimin), float(albefa)
         self.asyincr, self.asydecr, self.asybound = float(asyincr), float(asydecr), float(asybound)
         self.maxit = int(maxit)
+        self.exact = bool(exact)
         self.offset = full(asyinit)
         self.xold1 = self.xold2 = None
         self.low = self.upp = None
@@ -99,6 +105,7 @@ class MMAUpdate:
         g, dg = g.contiguous(), dg.contiguous()
         p = _Params()
         p.version, p.m, p.adapt, p.maxit = self.version, self.m, int(bool(adapt) and self.adapt_ready()), self.maxit
+        p.exact = int(self.exact)
         p.a0, p.albefa, p.asyincr, p.asydecr = self.a0, self.albefa, self.asyincr, self.asydecr
         p.offmin, p.offmax = 1 / (self.asybound ** 2), self.asybound
         p.epsimin = self.epsimin * math.sqrt(self.m + self.n)
@@ -187,7 +194,7 @@ class MMA:
         self.mmaversion = mmaversion
         self.gcmma_maxit = kwargs.get("gcmma_maxit", 20)
         opts = {k: kwargs[k] for k in ("a0", "epsimin", "cCoef", "albefa", "asyinit", "asyincr", "asydecr",
-                                       "asybound", "a", "c") if k in kwargs}
+                                       "asybound", "a", "c", "exact") if k in kwargs}
         self.core = MMAUpdate(self.n, len(self.responses), self.xmin, self.xmax, self.move, mmaversion,
                               device=self.device, **opts)
         self.m = self.core.m

@@ -34,8 +34,8 @@ def test_oracle_reproduces_pymoto_mma_steps(tag, version, golden):
 def test_params_struct_layout_and_argument_checks():
     from pymoto_gb300._lib import PMGError, call
     from pymoto_gb300.mma import _Params
-    # 4 ints, 7 doubles, rho[5], a[4], c[4], d[4] (include/pymoto_gb300.h)
-    assert ctypes.sizeof(_Params) == 16 + 7 * 8 + 5 * 8 + 3 * 4 * 8
+    # 6 ints, 7 doubles, rho[5], a[4], c[4], d[4] (include/pymoto_gb300.h)
+    assert ctypes.sizeof(_Params) == 24 + 7 * 8 + 5 * 8 + 3 * 4 * 8
     assert call("pmg_mma_scratch_bytes", 100, 5) == 0 and call("pmg_mma_scratch_bytes", 0, 1) == 0
     assert call("pmg_mma_scratch_bytes", 1000, 2) > (8 + 6 + 2) * 1000 * 8
     p = _Params()
@@ -64,19 +64,20 @@ def test_scaling_module_formulas():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
 @pytest.mark.parametrize("tag,version", CASES)
-def test_device_update_matches_pymoto_steps(tag, version, golden):
+def test_device_update_matches_pymoto_steps(tag, version, exact, golden):
     from pymoto_gb300.mma import MMAUpdate
     g = golden("mma_mbb.npz")
     X, G, DG = g[f"{tag}_x"], g[f"{tag}_g"], g[f"{tag}_dg"]
-    up = MMAUpdate(X.shape[1], G.shape[1], 0.0, 1.0, move=0.2, mmaversion=version)
+    up = MMAUpdate(X.shape[1], G.shape[1], 0.0, 1.0, move=0.2, mmaversion=version, exact=exact)
     o = MMAOracle(X.shape[1], G.shape[1], move=0.2, mmaversion=version)
     for k in range(X.shape[0]):
         xn = up.step(dev(X[k]), dev(G[k]), dev(DG[k])).cpu().numpy()
         o.step(X[k], G[k], DG[k])
-        # element-wise values round as numpy's (no FMA contraction); the sums over elements are in another order,
-        # so the interior-point iterates differ in the last bits: x to 1e-8 (the subproblem's tolerance is
-        # epsimin sqrt(n+m) ~ 2e-9), asymptotes and offsets exactly
+        # exact: element-wise values round as numpy's (no FMA contraction); fast: within a few ulp.  The sums over
+        # elements are in another order, so the interior-point iterates differ in the last bits: x to 1e-8 (the
+        # subproblem's tolerance is epsimin sqrt(n+m) ~ 2e-9); asymptotes and offsets exactly
         np.testing.assert_allclose(xn, g[f"{tag}_xnew"][k], rtol=0, atol=1e-8)
         np.testing.assert_allclose(up.low.cpu().numpy(), g[f"{tag}_low"][k], rtol=1e-15)
         np.testing.assert_allclose(up.upp.cpu().numpy(), g[f"{tag}_upp"][k], rtol=1e-15)
