@@ -10,10 +10,12 @@
 // second exchange.  Partials are double-buffered by barrier parity: a CTA can only overwrite a buffer after
 // every CTA has passed the barrier that follows its reads.
 //
-// Element state (x, xsi, eta of the current iterate; the Newton direction; asymptotes, bounds, P, Q and the
-// constraint gradients GG) lives in the scratch arrays, one FP64 array each, read coalesced by the same
-// thread in every pass.  A line-search trial is x_base + steg * dx evaluated on the fly; the accepted step is
-// written back by the next pass that starts from the iterate.
+// Element state (x, xsi, eta of the current iterate; the Newton direction; asymptotes, bounds, P, Q, the
+// constraint gradients GG and the Newton terms delx, diagx) lives in the scratch arrays, one FP64 array each,
+// read coalesced by the same thread in every pass.  A line-search trial is x_base + steg * dx evaluated on the
+// fly; the accepted step is written back by the next pass that starts from the iterate.  One pass evaluates both
+// the residual and the Newton system at a point, so a Newton iteration costs two passes: the direction and the
+// (almost always single) line-search trial, whose pass already holds the next Newton system.
 //
 // Arithmetic is FP64.  The exact variant keeps the operation order of the reference, and this file is compiled
 // without FMA contraction, so its element-wise values round as numpy's do; only the order of the sums over
@@ -45,7 +47,7 @@ struct MMAArrays {
   int64_t n;
   const double *xval, *xold1, *xold2, *xmin, *xmax, *move, *g, *dg;
   double *offset, *low, *upp, *xnew, *info;
-  double *xb, *xsib, *etab, *dxv, *dxsiv, *detav, *alfa, *beta, *rxa, *rbx, *P, *Q, *GG;
+  double *xb, *xsib, *etab, *dxv, *dxsiv, *detav, *alfa, *beta, *rxa, *rbx, *dlx, *dgx, *P, *Q, *GG;
 };
 
 enum { RED_SUM = 0, RED_MAX = 1, RED_MIN = 2 };
@@ -118,10 +120,20 @@ __device__ bool mma_reduce(const double (&acc)[R], int nsum, int nmax, MMAHeader
     __threadfence();
   }
   if (!mma_barrier(h, gen)) return false;
+  // the partials of all CTAs, read from L2 (the barrier's fence orders them after the arrivals), four loads in
+  // flight per lane, combined in the same order in every CTA
+  const int nb = (int)gridDim.x;
   for (int r = warp; r < R; r += MMA_NW) {
     const int op = r < nsum ? RED_SUM : (r < nsum + nmax ? RED_MAX : RED_MIN);
+    const double* col = &h->partial[gen & 1u][0][r];
     double v = op == RED_SUM ? 0.0 : (op == RED_MAX ? -INFINITY : INFINITY);
-    for (int b = lane; b < (int)gridDim.x; b += 32) v = red_op(op, v, ((volatile double*)h->partial[gen & 1u][b])[r]);
+    int b = lane;
+    for (; b + 96 < nb; b += 128) {
+      const double a0 = __ldcg(col + (size_t)b * MMA_RED), a1 = __ldcg(col + (size_t)(b + 32) * MMA_RED);
+      const double a2 = __ldcg(col + (size_t)(b + 64) * MMA_RED), a3 = __ldcg(col + (size_t)(b + 96) * MMA_RED);
+      v = red_op(op, red_op(op, red_op(op, red_op(op, v, a0), a1), a2), a3);
+    }
+    for (; b < nb; b += 32) v = red_op(op, v, __ldcg(col + (size_t)b * MMA_RED));
     v = warp_red(op, v);
     if (lane == 0) tot[r] = v;
   }
@@ -151,9 +163,10 @@ struct MMAScalars {
   double y[M], lam[M], mu[M], s[M], z, zet;          // current iterate
   double y0[M], lam0[M], mu0[M], s0[M], z0, zet0;    // iterate at the start of the line search
   double dy[M], dlam[M], dmu[M], ds[M], dz, dzet;    // Newton direction
+  double ndy[M], ndlam[M], ndmu[M], nds[M], ndz, ndzet;   // Newton solution at the last evaluated point
   double b[M], rhs[M + 1];
   double epsi, steg, steg_used, pend, rnorm, rmax, rtry, rmaxtry;
-  int has_pend, err;
+  int has_pend, err, nbad;
 };
 
 // EXACT: every element-wise expression divides where the reference divides (values round as numpy's).
@@ -238,6 +251,7 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
       S.has_pend = 0;
       S.pend = 0.0;
       S.err = 0;
+      S.nbad = 0;
     }
     __syncthreads();
   }
@@ -250,12 +264,88 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
     return PQ[j] + v;
   };
 
-  // ---- KKT residual of the perturbed subproblem (mma.py:302-325).  trial: at x_base + steg * direction;
-  // otherwise at the iterate, writing back a pending accepted step first.
-  auto residual = [&](bool trial) -> bool {
-    double acc[2 * M + 2];
+  // Slots of the evaluation pass: [0, M) P1.(1/(upp-x)), [M, 2M) Q1.(1/(x-low)), [2M] sum of squared element
+  // residuals, [2M+1, 3M+1) GG.(delx/diagx), [3M+1, 3M+1+M^2) (GG/diagx).GG^T, then the largest squared residual.
+  constexpr int RS = 3 * M + 1 + M * M;
+  constexpr int RE = RS + 1;
+
+  // Newton system of dlam, dz at the evaluated point (mma.py:371-390), thread 0, from the totals in tot[].  The
+  // solution goes to the n* fields: it becomes the Newton direction only if this point is kept.
+  auto solve_newton = [&](double epsi) {
+    double dely[M], diagy[M], AA[M1][M1], bb[M1], sol[M1];
+    double alam = p.a[0] * S.lam[0];
+    for (int i = 1; i < M; ++i) alam = alam + p.a[i] * S.lam[i];
+    for (int i = 0; i < M; ++i) {
+      const double gvec = tot[i] + tot[M + i];
+      dely[i] = ((p.c[i] + p.d[i] * S.y[i]) - S.lam[i]) - epsi / S.y[i];
+      const double dellam = (((gvec - p.a[i] * S.z) - S.y[i]) - S.b[i]) + epsi / S.lam[i];
+      diagy[i] = p.d[i] + S.mu[i] / S.y[i];
+      const double diaglamyi = S.s[i] / S.lam[i] + 1.0 / diagy[i];
+      bb[i] = (dellam + dely[i] / diagy[i]) - tot[2 * M + 1 + i];
+      for (int l = 0; l < M; ++l) AA[i][l] = (i == l ? diaglamyi : 0.0) + tot[3 * M + 1 + i * M + l];
+      AA[i][M] = p.a[i];
+      AA[M][i] = p.a[i];
+    }
+    AA[M][M] = -S.zet / S.z;
+    bb[M] = (p.a0 - alam) - epsi / S.z;
+    // LU with partial pivoting (largest magnitude in the column, first on ties), then the two triangles
+    int bad = 0;
+    for (int k = 0; k < M1 && !bad; ++k) {
+      int pr = k;
+      double amax = fabs(AA[k][k]);
+      for (int i = k + 1; i < M1; ++i)
+        if (fabs(AA[i][k]) > amax) {
+          amax = fabs(AA[i][k]);
+          pr = i;
+        }
+      if (!(amax > 0.0) || !isfinite(amax)) {
+        bad = 1;
+        break;
+      }
+      if (pr != k) {
+        for (int c = 0; c < M1; ++c) {
+          const double tmp = AA[k][c];
+          AA[k][c] = AA[pr][c];
+          AA[pr][c] = tmp;
+        }
+        const double tb = bb[k];
+        bb[k] = bb[pr];
+        bb[pr] = tb;
+      }
+      const double rinv = 1.0 / AA[k][k];
+      for (int i = k + 1; i < M1; ++i) {
+        const double l = AA[i][k] * rinv;
+        for (int c = k + 1; c < M1; ++c) AA[i][c] = AA[i][c] - l * AA[k][c];
+        bb[i] = bb[i] - l * bb[k];
+      }
+    }
+    if (!bad) {
+      for (int k = M; k >= 0; --k) {
+        double v = bb[k];
+        for (int c = k + 1; c < M1; ++c) v = v - AA[k][c] * sol[c];
+        sol[k] = v / AA[k][k];
+      }
+      for (int i = 0; i < M; ++i) {
+        S.ndlam[i] = sol[i];
+        S.ndy[i] = -dely[i] / diagy[i] + sol[i] / diagy[i];
+        S.ndmu[i] = (-S.mu[i] + epsi / S.y[i]) - (S.mu[i] * S.ndy[i]) / S.y[i];
+        S.nds[i] = (-S.s[i] + epsi / S.lam[i]) - (S.s[i] * sol[i]) / S.lam[i];
+      }
+      S.ndz = sol[M];
+      S.ndzet = (-S.zet + epsi / S.z) - (S.zet * S.ndz) / S.z;
+    }
+    S.nbad = bad;
+  };
+
+  // ---- one pass at a point: the KKT residual of the perturbed subproblem (mma.py:302-325) and the element terms
+  // of its Newton system (mma.py:336-390).  trial: the point x_base + steg * direction of the line search;
+  // otherwise the iterate, writing back a pending accepted step first.  The residual and the Newton terms share
+  // 1/(upp-x), 1/(x-low), plam, qlam, dpsidx, x-alfa and beta-x, and the pass of the accepted trial already holds
+  // the next Newton system, so a Newton iteration needs two passes (direction, trial) instead of three.
+  auto evaluate = [&](bool trial) -> bool {
+    double acc[RE];
 #pragma unroll
-    for (int r = 0; r < 2 * M + 2; ++r) acc[r] = 0.0;
+    for (int r = 0; r < RE; ++r) acc[r] = 0.0;
     const double epsi = S.epsi;
     const bool upd = trial || S.has_pend;
     const double t = trial ? S.steg : S.pend;
@@ -276,27 +366,65 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
       }
       const double ux1 = A.upp[j] - x, xl1 = x - A.low[j];
       const double plam = lam_dot(lam, A.P, j), qlam = lam_dot(lam, A.Q, j);
+      const double xa = x - A.alfa[j], bx = A.beta[j] - x;
       const double ru = 1.0 / ux1, rl = 1.0 / xl1;
+      double gg[M], dpsidx, delx, diagx, rdg;
+      if constexpr (EXACT) {
+        const double ux2 = ux1 * ux1, xl2 = xl1 * xl1;
+        const double uxinv2 = 1.0 / ux2, xlinv2 = 1.0 / xl2;
 #pragma unroll
-      for (int i = 0; i < M; ++i) {
-        acc[i] = macc<EXACT>(acc[i], A.P[(i + 1) * n + j], ru);
-        acc[M + i] = macc<EXACT>(acc[M + i], A.Q[(i + 1) * n + j], rl);
+        for (int i = 0; i < M; ++i) {
+          const double P1 = A.P[(i + 1) * n + j], Q1 = A.Q[(i + 1) * n + j];
+          acc[i] += P1 * ru;
+          acc[M + i] += Q1 * rl;
+          gg[i] = P1 * uxinv2 - Q1 * xlinv2;
+        }
+        dpsidx = plam / ux2 - qlam / xl2;
+        delx = (dpsidx - epsi / xa) + epsi / bx;
+        diagx = ((2.0 * (plam / (ux1 * ux2) + qlam / (xl1 * xl2))) + xsi / xa) + eta / bx;
+        rdg = 0.0;
+      } else {
+        const double ru2 = ru * ru, rl2 = rl * rl;
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+          const double P1 = A.P[(i + 1) * n + j], Q1 = A.Q[(i + 1) * n + j];
+          acc[i] = fma(P1, ru, acc[i]);
+          acc[M + i] = fma(Q1, rl, acc[M + i]);
+          gg[i] = P1 * ru2 - Q1 * rl2;
+        }
+        dpsidx = plam * ru2 - qlam * rl2;
+        const double rxa = 1.0 / xa, rbx = 1.0 / bx;
+        delx = (dpsidx - epsi * rxa) + epsi * rbx;
+        diagx = ((2.0 * (plam * (ru2 * ru) + qlam * (rl2 * rl))) + xsi * rxa) + eta * rbx;
+        rdg = 1.0 / diagx;
+        A.rxa[j] = rxa;
+        A.rbx[j] = rbx;
       }
-      double dpsidx;
-      if constexpr (EXACT)
-        dpsidx = plam / (ux1 * ux1) - qlam / (xl1 * xl1);
-      else
-        dpsidx = plam * (ru * ru) - qlam * (rl * rl);
+      // residual
       const double rex = (dpsidx - xsi) + eta;
-      const double rexsi = xsi * (x - A.alfa[j]) - epsi;
-      const double reeta = eta * (A.beta[j] - x) - epsi;
+      const double rexsi = xsi * xa - epsi;
+      const double reeta = eta * bx - epsi;
       const double q1 = rex * rex, q2 = rexsi * rexsi, q3 = reeta * reeta;
       acc[2 * M] += (q1 + q2) + q3;
-      acc[2 * M + 1] = nmax(acc[2 * M + 1], nmax(nmax(q1, q2), q3));
+      acc[RS] = nmax(acc[RS], nmax(nmax(q1, q2), q3));
+      // Newton terms
+      const double dd = EXACT ? delx / diagx : delx * rdg;
+#pragma unroll
+      for (int i = 0; i < M; ++i) {
+        acc[2 * M + 1 + i] = macc<EXACT>(acc[2 * M + 1 + i], gg[i], dd);
+        const double gi = EXACT ? gg[i] / diagx : gg[i] * rdg;
+#pragma unroll
+        for (int l = 0; l < M; ++l)
+          acc[3 * M + 1 + i * M + l] = macc<EXACT>(acc[3 * M + 1 + i * M + l], gi, gg[l]);
+      }
+      A.dlx[j] = delx;
+      A.dgx[j] = EXACT ? diagx : rdg;   // the fast variant keeps 1/diagx
+#pragma unroll
+      for (int i = 0; i < M; ++i) A.GG[i * n + j] = gg[i];
     }
-    if (!mma_reduce<2 * M + 2>(acc, 2 * M + 1, 1, h, ++gen, tot, wsum)) return false;
+    if (!mma_reduce<RE>(acc, RS, 1, h, ++gen, tot, wsum)) return false;
     if (threadIdx.x == 0) {
-      double sum = tot[2 * M], mx = tot[2 * M + 1];
+      double sum = tot[2 * M], mx = tot[RS];
       double alam = p.a[0] * S.lam[0];
       for (int i = 1; i < M; ++i) alam = alam + p.a[i] * S.lam[i];
       double r[4 * M + 2];
@@ -323,23 +451,35 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
         S.rmax = mx;
         S.has_pend = 0;
       }
+      // the Newton system is needed only while the largest residual is above (0.9 epsilon)^2
+      const double e9 = 0.9 * epsi;
+      if (mx > e9 * e9) solve_newton(epsi);
     }
     __syncthreads();
     return true;
   };
 
-  // ---- Newton system (mma.py:336-390): element terms, then the (m+1)x(m+1) system in every CTA
-  auto newton_system = [&]() -> bool {
-    constexpr int RN = 3 * M + M * M;
-    double acc[RN];
-#pragma unroll
-    for (int r = 0; r < RN; ++r) acc[r] = 0.0;
+  // ---- Newton direction of x, xsi, eta and the step length (mma.py:392-421), from the Newton system solved at
+  // the kept point; writes back a pending accepted step first
+  auto direction = [&]() -> bool {
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < M; ++i) {
+        S.dy[i] = S.ndy[i];
+        S.dlam[i] = S.ndlam[i];
+        S.dmu[i] = S.ndmu[i];
+        S.ds[i] = S.nds[i];
+      }
+      S.dz = S.ndz;
+      S.dzet = S.ndzet;
+    }
+    __syncthreads();
+    double acc[4] = {-INFINITY, INFINITY, INFINITY, INFINITY};   // max dx/(beta-x); min dxsi/xsi, deta/eta, dx/(x-alfa)
     const double epsi = S.epsi;
     const bool upd = S.has_pend;
     const double t = S.pend;
-    double lam[M];
+    double dlam[M];
 #pragma unroll
-    for (int i = 0; i < M; ++i) lam[i] = S.lam[i];
+    for (int i = 0; i < M; ++i) dlam[i] = S.dlam[i];
     for (int64_t j = j0; j < n; j += stride) {
       double x = A.xb[j], xsi = A.xsib[j], eta = A.etab[j];
       if (upd) {
@@ -350,145 +490,13 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
         A.xsib[j] = xsi;
         A.etab[j] = eta;
       }
-      const double ux1 = A.upp[j] - x, xl1 = x - A.low[j];
-      const double plam = lam_dot(lam, A.P, j), qlam = lam_dot(lam, A.Q, j);
-      const double xa = x - A.alfa[j], bx = A.beta[j] - x;
-      double gg[M], delx, diagx, rdg;
-      if constexpr (EXACT) {
-        const double ux2 = ux1 * ux1, xl2 = xl1 * xl1;
-        const double uxinv1 = 1.0 / ux1, xlinv1 = 1.0 / xl1, uxinv2 = 1.0 / ux2, xlinv2 = 1.0 / xl2;
-#pragma unroll
-        for (int i = 0; i < M; ++i) {
-          const double P1 = A.P[(i + 1) * n + j], Q1 = A.Q[(i + 1) * n + j];
-          acc[i] += P1 * uxinv1;
-          acc[M + i] += Q1 * xlinv1;
-          gg[i] = P1 * uxinv2 - Q1 * xlinv2;
-        }
-        const double dpsidx = plam / ux2 - qlam / xl2;
-        delx = (dpsidx - epsi / xa) + epsi / bx;
-        diagx = ((2.0 * (plam / (ux1 * ux2) + qlam / (xl1 * xl2))) + xsi / xa) + eta / bx;
-        rdg = 0.0;
-      } else {
-        const double ru = 1.0 / ux1, rl = 1.0 / xl1, ru2 = ru * ru, rl2 = rl * rl;
-#pragma unroll
-        for (int i = 0; i < M; ++i) {
-          const double P1 = A.P[(i + 1) * n + j], Q1 = A.Q[(i + 1) * n + j];
-          acc[i] = fma(P1, ru, acc[i]);
-          acc[M + i] = fma(Q1, rl, acc[M + i]);
-          gg[i] = P1 * ru2 - Q1 * rl2;
-        }
-        const double dpsidx = plam * ru2 - qlam * rl2;
-        const double rxa = 1.0 / xa, rbx = 1.0 / bx;
-        delx = (dpsidx - epsi * rxa) + epsi * rbx;
-        diagx = ((2.0 * (plam * (ru2 * ru) + qlam * (rl2 * rl))) + xsi * rxa) + eta * rbx;
-        rdg = 1.0 / diagx;
-        A.rxa[j] = rxa;
-        A.rbx[j] = rbx;
-      }
-      const double dd = EXACT ? delx / diagx : delx * rdg;
-#pragma unroll
-      for (int i = 0; i < M; ++i) {
-        acc[2 * M + i] = macc<EXACT>(acc[2 * M + i], gg[i], dd);
-        const double gi = EXACT ? gg[i] / diagx : gg[i] * rdg;
-#pragma unroll
-        for (int l = 0; l < M; ++l) acc[3 * M + i * M + l] = macc<EXACT>(acc[3 * M + i * M + l], gi, gg[l]);
-      }
-      A.dxv[j] = delx;
-      A.dxsiv[j] = EXACT ? diagx : rdg;   // the fast variant keeps 1/diagx
-#pragma unroll
-      for (int i = 0; i < M; ++i) A.GG[i * n + j] = gg[i];
-    }
-    if (!mma_reduce<RN>(acc, RN, 0, h, ++gen, tot, wsum)) return false;
-    if (threadIdx.x == 0) {
-      S.has_pend = 0;
-      double dely[M], diagy[M], AA[M1][M1], bb[M1], sol[M1];
-      double alam = p.a[0] * S.lam[0];
-      for (int i = 1; i < M; ++i) alam = alam + p.a[i] * S.lam[i];
-      for (int i = 0; i < M; ++i) {
-        const double gvec = tot[i] + tot[M + i];
-        dely[i] = ((p.c[i] + p.d[i] * S.y[i]) - S.lam[i]) - epsi / S.y[i];
-        const double dellam = (((gvec - p.a[i] * S.z) - S.y[i]) - S.b[i]) + epsi / S.lam[i];
-        diagy[i] = p.d[i] + S.mu[i] / S.y[i];
-        const double diaglamyi = S.s[i] / S.lam[i] + 1.0 / diagy[i];
-        bb[i] = (dellam + dely[i] / diagy[i]) - tot[2 * M + i];
-        for (int l = 0; l < M; ++l) AA[i][l] = (i == l ? diaglamyi : 0.0) + tot[3 * M + i * M + l];
-        AA[i][M] = p.a[i];
-        AA[M][i] = p.a[i];
-      }
-      AA[M][M] = -S.zet / S.z;
-      bb[M] = (p.a0 - alam) - epsi / S.z;
-      // LU with partial pivoting (largest magnitude in the column, first on ties), then the two triangles
-      int bad = 0;
-      for (int k = 0; k < M1 && !bad; ++k) {
-        int pr = k;
-        double amax = fabs(AA[k][k]);
-        for (int i = k + 1; i < M1; ++i)
-          if (fabs(AA[i][k]) > amax) {
-            amax = fabs(AA[i][k]);
-            pr = i;
-          }
-        if (!(amax > 0.0) || !isfinite(amax)) {
-          bad = 1;
-          break;
-        }
-        if (pr != k) {
-          for (int c = 0; c < M1; ++c) {
-            const double tmp = AA[k][c];
-            AA[k][c] = AA[pr][c];
-            AA[pr][c] = tmp;
-          }
-          const double tb = bb[k];
-          bb[k] = bb[pr];
-          bb[pr] = tb;
-        }
-        const double rinv = 1.0 / AA[k][k];
-        for (int i = k + 1; i < M1; ++i) {
-          const double l = AA[i][k] * rinv;
-          for (int c = k + 1; c < M1; ++c) AA[i][c] = AA[i][c] - l * AA[k][c];
-          bb[i] = bb[i] - l * bb[k];
-        }
-      }
-      if (!bad) {
-        for (int k = M; k >= 0; --k) {
-          double v = bb[k];
-          for (int c = k + 1; c < M1; ++c) v = v - AA[k][c] * sol[c];
-          sol[k] = v / AA[k][k];
-        }
-        for (int i = 0; i < M; ++i) {
-          S.dlam[i] = sol[i];
-          S.dy[i] = -dely[i] / diagy[i] + sol[i] / diagy[i];
-          S.dmu[i] = (-S.mu[i] + epsi / S.y[i]) - (S.mu[i] * S.dy[i]) / S.y[i];
-          S.ds[i] = (-S.s[i] + epsi / S.lam[i]) - (S.s[i] * sol[i]) / S.lam[i];
-        }
-        S.dz = sol[M];
-        S.dzet = (-S.zet + epsi / S.z) - (S.zet * S.dz) / S.z;
-      }
-      S.err = bad;
-    }
-    __syncthreads();
-    if (S.err) {
-      if (threadIdx.x == 0) atomicCAS(&h->error, 0u, 2u);
-      return false;
-    }
-    return true;
-  };
-
-  // ---- Newton direction of x, xsi, eta and the step length (mma.py:392-421)
-  auto direction = [&]() -> bool {
-    double acc[4] = {-INFINITY, INFINITY, INFINITY, INFINITY};   // max dx/(beta-x); min dxsi/xsi, deta/eta, dx/(x-alfa)
-    const double epsi = S.epsi;
-    double dlam[M];
-#pragma unroll
-    for (int i = 0; i < M; ++i) dlam[i] = S.dlam[i];
-    for (int64_t j = j0; j < n; j += stride) {
-      const double xsi = A.xsib[j], eta = A.etab[j];
-      const double delx = A.dxv[j];
+      const double delx = A.dlx[j];
       double dlg = dlam[0] * A.GG[j];
 #pragma unroll
       for (int i = 1; i < M; ++i) dlg = dlg + dlam[i] * A.GG[i * n + j];
       double dx, dxsi, deta, rb, ra;
       if constexpr (EXACT) {
-        const double x = A.xb[j], diagx = A.dxsiv[j];
+        const double diagx = A.dgx[j];
         dx = -delx / diagx - dlg / diagx;
         const double xa = x - A.alfa[j], bx = A.beta[j] - x;
         dxsi = (-xsi + epsi / xa) - (xsi * dx) / xa;
@@ -496,7 +504,7 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
         rb = dx / bx;
         ra = dx / xa;
       } else {
-        const double rdg = A.dxsiv[j], rxa = A.rxa[j], rbx = A.rbx[j];
+        const double rdg = A.dgx[j], rxa = A.rxa[j], rbx = A.rbx[j];
         dx = (-delx - dlg) * rdg;
         dxsi = (-xsi + epsi * rxa) - (xsi * dx) * rxa;
         deta = (-eta + epsi * rbx) + (eta * dx) * rbx;
@@ -513,6 +521,7 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
     }
     if (!mma_reduce<4>(acc, 0, 1, h, ++gen, tot, wsum)) return false;
     if (threadIdx.x == 0) {
+      S.has_pend = 0;
       double my = S.dy[0] / S.y[0], ml = S.dlam[0] / S.lam[0], mm = S.dmu[0] / S.mu[0], ms = S.ds[0] / S.s[0];
       for (int i = 1; i < M; ++i) {
         my = nmin(my, S.dy[i] / S.y[i]);
@@ -544,14 +553,18 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
     __syncthreads();
     if (!more) break;
     ++outer;
-    if (!residual(false)) return;
+    if (!evaluate(false)) return;
     for (int it = 0; it < p.maxit; ++it) {
       const double e9 = 0.9 * S.epsi;
       const bool go = S.rmax > e9 * e9;
+      const int bad = S.nbad;
       __syncthreads();
       if (!go) break;
       ++newton;
-      if (!newton_system()) return;
+      if (bad) {   // the reference's linear solve would raise here
+        if (threadIdx.x == 0) atomicCAS(&h->error, 0u, 2u);
+        return;
+      }
       if (!direction()) return;
       // line search: halve the step until the residual norm decreases (mma.py:436-468)
       for (int ls = 0; ls < p.maxit; ++ls) {
@@ -569,7 +582,7 @@ __global__ void __launch_bounds__(MMA_THREADS) mma_kernel(pmg_mma_params p, MMAA
           S.steg_used = st;
         }
         __syncthreads();
-        if (!residual(true)) return;
+        if (!evaluate(true)) return;
         const bool accept = S.rtry < S.rnorm;
         __syncthreads();
         if (accept) break;
@@ -668,7 +681,7 @@ extern "C" {
 
 size_t pmg_mma_scratch_bytes(int64_t n, int m) {
   if (n <= 0 || m < 1 || m > PMG_MMA_MAX_M) return 0;
-  return mma_header_bytes() + (size_t)(10 + 2 * (m + 1) + m) * (size_t)n * sizeof(double);
+  return mma_header_bytes() + (size_t)(12 + 2 * (m + 1) + m) * (size_t)n * sizeof(double);
 }
 
 int pmg_mma_update(int64_t n, const pmg_mma_params* params_host, const double* xval, const double* xold1,
@@ -703,7 +716,8 @@ int pmg_mma_update(int64_t n, const pmg_mma_params* params_host, const double* x
   A.upp = upp;
   A.xnew = xnew;
   A.info = info;
-  double** slots[] = {&A.xb, &A.xsib, &A.etab, &A.dxv, &A.dxsiv, &A.detav, &A.alfa, &A.beta, &A.rxa, &A.rbx};
+  double** slots[] = {&A.xb, &A.xsib, &A.etab, &A.dxv, &A.dxsiv, &A.detav, &A.alfa, &A.beta, &A.rxa, &A.rbx,
+                      &A.dlx, &A.dgx};
   for (double** s : slots) {
     *s = arr;
     arr += n;
