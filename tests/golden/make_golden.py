@@ -7,6 +7,7 @@ at module level for plotting only.  The fixtures are small .npz files; the tests
     python tests/golden/make_golden.py          # every fixture
     python tests/golden/make_golden.py vti      # the VTI files only
     python tests/golden/make_golden.py mma      # the MMA steps only
+    python tests/golden/make_golden.py scalars  # the ScalarToFile logs only
 """
 import os
 import sys
@@ -249,6 +250,28 @@ def vti_cases():
     return cases
 
 
+def scalar_cases():
+    """ScalarToFile cases: (name, saveto, fmt, separator, states per iteration {tag: value}).  Pure numpy."""
+    rng = np.random.default_rng(20251205)
+    it = []
+    for k in range(3):
+        it.append({"compliance": float(rng.uniform(1, 100)), "volume": np.float64(rng.uniform(0, 1)),
+                   "eig": rng.standard_normal(3), "block": rng.standard_normal((2, 2)), "count": 7 + k})
+    return [("txt", "scalars_txt.txt", ".10e", "\t", it), ("csv", "scalars_csv.csv", ".3f", "\t", it)]
+
+
+def scalar_files(pym):
+    for name, fname, fmt, sep, its in scalar_cases():
+        sigs = [pym.Signal(tag, val) for tag, val in its[0].items()]
+        with pym.Network() as fn:
+            pym.ScalarToFile(os.path.join(OUT, fname), fmt=fmt, separator=sep)(*sigs)
+        for vals in its[1:]:
+            for sg in sigs:
+                sg.state = vals[sg.tag]
+            fn.response()
+        print("wrote", fname)
+
+
 def vti_files(pym):
     for name, shp, size, origin, scale, vecs in vti_cases():
         d = pym.VoxelDomain(*shp, *size)
@@ -274,3 +297,5 @@ if __name__ == "__main__":
         vti_files(pym)
     if "all" in which or "mma" in which:
         mma_mbb(pym)
+    if "all" in which or "scalars" in which:
+        scalar_files(pym)
