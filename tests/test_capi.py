@@ -113,3 +113,50 @@ def test_product_package_never_imports_the_oracle():
     for path in glob.glob(os.path.join(pkg, "**", "*.py"), recursive=True):
         src = open(path).read()
         assert not re.search(r"^\s*(import|from)\s+oracle\b", src, flags=re.M), path
+
+
+def _header_prototypes():
+    """name -> (return type, [parameter types]) of every function declared in include/*.h."""
+    protos = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(pmg_\w+)\s*\(([^;{]*?)\)\s*;", text):
+            ret, name, params = m.group(1).strip(), m.group(2), m.group(3).strip()
+            plist = [] if params in ("", "void") else [p.strip() for p in params.split(",")]
+            types = []
+            for p in plist:
+                p = re.sub(r"\s+", " ", p)
+                if "*" in p:
+                    types.append("ptr")
+                else:
+                    types.append(p.rsplit(" ", 1)[0].replace("const ", "").strip())
+            protos[name] = (ret.split()[-1] if "*" not in ret else "ptr", types)
+    return protos
+
+
+def test_binding_signatures_match_the_header():
+    """Argument count and type class of every ctypes signature against its C declaration: a mismatch would pass
+    wrong values (or pointers) to the library."""
+    from pymoto_gb300 import _lib
+    cmap = {"int": ctypes.c_int, "int64_t": ctypes.c_int64, "double": ctypes.c_double, "float": ctypes.c_float,
+            "size_t": ctypes.c_size_t, "unsigned": ctypes.c_uint}
+    protos = _header_prototypes()
+    assert set(protos) == set(_lib.SIGNATURES)
+    bad = []
+    for name, (res, args) in _lib.SIGNATURES.items():
+        ret, types = protos[name]
+        if len(types) != len(args):
+            bad.append(f"{name}: {len(types)} declared, {len(args)} bound")
+            continue
+        for k, (t, a) in enumerate(zip(types, args)):
+            if t == "ptr":
+                ok = a in (ctypes.c_void_p, ctypes.c_char_p)
+            else:
+                ok = cmap.get(t) is a
+            if not ok:
+                bad.append(f"{name} arg {k}: {t} vs {a.__name__}")
+        want = ctypes.c_char_p if ret == "ptr" else cmap.get(ret)
+        if want is not res:
+            bad.append(f"{name} returns {ret} vs {getattr(res, '__name__', res)}")
+    assert not bad, bad
