@@ -232,7 +232,9 @@ int pmg_density_filter_rowsum(int nelx, int nely, int nelz, double radius, doubl
 int pmg_density_filter(int transpose, int nelx, int nely, int nelz, double radius, const double* s,
                        const double* x, double* y, void* stream);
 /* FilterConv (filter.py:8-220) with per-axis padded index maps pad{x,y,z} (int32, length n+2p, device)
- * and kernel weights w (kx*ky*kz, C order, device).  Forward: y = W * x_pad ('valid', filter.py:207-212). */
+ * and kernel weights w (kx*ky*kz, C order, device).  Forward: y = W * x_pad ('valid', filter.py:207-212).
+ * A map entry -1 marks a padded position of a constant-value side: it contributes nothing, and the caller
+ * adds the constant values' field (linear in the constants, fixed per filter). */
 int pmg_conv_filter(int nelx, int nely, int nelz, const double* w, int kx, int ky, int kz, const int32_t* padx,
                     const int32_t* pady, const int32_t* padz, const double* x, double* y, void* stream);
 /* Its adjoint (filter.py:214-220: full correlation accumulated through the pad maps), with the inverse pad

@@ -12,7 +12,7 @@ from scipy.sparse.linalg import splu
 
 __all__ = [
     "Grid", "element_stiffness", "material_matrix", "assemble", "default_bcdiagval",
-    "density_filter_matrix", "density_filter", "density_filter_T",
+    "density_filter_matrix", "density_filter_nonpadding", "density_filter", "density_filter_T",
     "conv_filter_weights", "conv_filter_index_map", "conv_filter", "conv_filter_T",
     "simp", "simp_derivative", "prolongation", "MGLevel", "build_hierarchy", "vcycle",
     "cg_solve", "LinSolveOracle", "sensitivity_contract", "oc_step", "direct_solve",
@@ -228,6 +228,14 @@ def density_filter_matrix(grid, radius):
                        shape=(grid.nel, grid.nel)).tocsr()
     s = np.asarray(H.sum(axis=1)).ravel()
     return H, s
+
+
+def density_filter_nonpadding(s, nonpadding):
+    """Row sums with `nonpadding`: rows outside it take max(s), which mimics zero densities outside the
+    domain (pymoto/modules/filter.py:241-255)."""
+    s = s.copy()
+    s[~np.isin(np.arange(s.size), nonpadding)] = s.max()
+    return s
 
 
 def density_filter(H, s, x):

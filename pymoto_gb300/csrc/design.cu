@@ -76,7 +76,8 @@ __global__ void density_filter_kernel(Grid g, double r, const double* __restrict
 }
 
 // ------------------------------------------------------------------------------------------ FilterConv
-// Forward: y[o] = sum_m w[m] x[pad(o + (K-1) - m)]  (kernel flipped: 'valid' convolution).
+// Forward: y[o] = sum_m w[m] x[pad(o + (K-1) - m)]  (kernel flipped: 'valid' convolution); pad maps may hold -1
+// for the positions of constant-value sides, which contribute nothing here.
 __global__ void conv_filter_kernel(Grid g, const double* __restrict__ w, int kx, int ky, int kz,
                                    const int32_t* __restrict__ px, const int32_t* __restrict__ py,
                                    const int32_t* __restrict__ pz, const double* __restrict__ x, double* __restrict__ y) {
@@ -87,11 +88,14 @@ __global__ void conv_filter_kernel(Grid g, const double* __restrict__ w, int kx,
   double acc = 0.0;
   for (int c = 0; c < kz; ++c) {
     const int kk = pz[k + (kz - 1) - c];
+    if (kk < 0) continue;   // padded position of a constant-value side: its value enters as a separate field
     for (int b = 0; b < ky; ++b) {
       const int jj = py[j + (ky - 1) - b];
+      if (jj < 0) continue;
       const double* wr = w + ((int64_t)0 * ky + b) * kz + c;
       for (int a = 0; a < kx; ++a) {
         const int ii = px[i + (kx - 1) - a];
+        if (ii < 0) continue;
         acc = fma(wr[(int64_t)a * ky * kz], x[elem_id(g, ii, jj, kk)], acc);
       }
     }

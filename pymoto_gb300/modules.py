@@ -30,18 +30,23 @@ class DensityFilter(Module):
     """y = H x / s with H_ij = max(0, r - |c_i - c_j|) (pymoto/modules/filter.py:273-378, Filter :223-270)."""
 
     def __init__(self, domain, radius=2.0, nonpadding=None):
-        if nonpadding is not None:
-            raise NotImplementedError("DensityFilter(nonpadding=...) is not supported on the GPU path")
         self.domain = domain
         self.grid = Grid(*grid_of(domain))
         self.radius = float(radius)
+        self.nonpadding = None if nonpadding is None else np.asarray(nonpadding, dtype=np.int64).ravel()
         self._s = None
 
     def _rowsum(self, device):
+        """Row sums s of H on the device; with `nonpadding`, every row outside it takes max(s), which mimics
+        zero densities outside the domain (pymoto/modules/filter.py:241-255).  Setup only."""
         if self._s is None or self._s.device != device:
             g = self.grid
             self._s = torch.empty(g.nel, dtype=torch.float64, device=device)
             call("pmg_density_filter_rowsum", g.nelx, g.nely, g.nelz, self.radius, self._s, stream())
+            if self.nonpadding is not None:
+                outside = torch.ones(g.nel, dtype=torch.bool, device=device)
+                outside[torch.from_numpy(self.nonpadding).to(device)] = False
+                self._s[outside] = self._s.max()
         return self._s
 
     def _apply(self, v, transpose):
@@ -59,10 +64,15 @@ class DensityFilter(Module):
         return self._apply(dfdy, True)
 
 
+def _is_value(bc):
+    return isinstance(bc, (int, float, np.integer, np.floating)) and not isinstance(bc, bool)
+
+
 def _pad_map(n, p, low, high):
     """Padded index map of one axis as FilterConv composes it (pymoto/modules/filter.py:98-160): wrapped
-    sides first, then the high side, then the low side; numeric sides pad with index 0 and are
-    overridden by their constant value."""
+    sides first, then the high side, then the low side; numeric sides pad with index 0, and their positions
+    (overridden by the constant value in pyMOTO) are marked -1 here: the kernels skip them, and the constant
+    value enters through FilterConv's constant field."""
     idx = np.arange(n)
     wl = p if low == "wrap" else 0
     wh = p if high == "wrap" else 0
@@ -74,18 +84,25 @@ def _pad_map(n, p, low, high):
         width = (0, p) if side == "high" else (p, 0)
         if mode in ("edge", "symmetric"):
             idx = np.pad(idx, width, mode=mode)
-        elif isinstance(mode, (int, float)):
+        elif _is_value(mode):
             idx = np.pad(idx, width, mode="constant", constant_values=0)
         else:
             raise ValueError(f"unknown padding mode {mode!r}")
+    if _is_value(low):
+        idx[:p] = -1
+    if _is_value(high):
+        idx[len(idx) - p:] = -1
     return idx.astype(np.int32)
 
 
 class FilterConv(Module):
     """Density filter as a padded convolution (pymoto/modules/filter.py:8-220).
 
-    Padding modes 'symmetric' (default), 'edge' and 'wrap' per side; constant-value padding is not
-    supported on the GPU path.
+    Padding modes 'symmetric' (default), 'edge', 'wrap' or a constant value per side.  Constant sides are
+    linear: the kernel skips their padded positions (index -1 in the maps) and adds the fixed field
+    conv(C) of the constant values, computed once on the host with pyMOTO's override order (later sides win
+    at corners); the adjoint's inverse maps omit those positions, as pyMOTO zeroes them
+    (pymoto/modules/filter.py:98-160, 207-220).
     """
 
     def __init__(self, domain, radius=None, relative_units=True, weights=None, xmin_bc="symmetric",
@@ -105,14 +122,36 @@ class FilterConv(Module):
         else:
             self.set_filter_radius(radius, relative_units)
         bcs = [xmin_bc, xmax_bc, ymin_bc, ymax_bc, zmin_bc, zmax_bc]
-        if any(isinstance(b, (int, float)) and not isinstance(b, bool) for b in bcs):
-            raise NotImplementedError("constant-value padding is not supported on the GPU path")
         g = self.grid
         sizes = [g.nelx, g.nely, max(g.nelz, 1)]
         self.pad_sizes = [s // 2 for s in self.weights.shape]
         self._maps_host = [_pad_map(n, p, bcs[2 * a], bcs[2 * a + 1]) for a, (n, p) in
                            enumerate(zip(sizes, self.pad_sizes))]
+        self._const_host = self._constant_field(bcs, sizes)
         self._dev = None
+
+    def _constant_field(self, bcs, sizes):
+        """conv(C) on the element grid (element numbering), C the padded field that holds the constant values on
+        the padded slabs of constant sides and 0 elsewhere; None when no side has a nonzero constant."""
+        if not any(_is_value(b) and float(b) != 0.0 for b in bcs):
+            return None
+        pads = self.pad_sizes
+        C = np.zeros([n + 2 * p for n, p in zip(sizes, pads)])
+        for a in range(3):   # x, y, z; high side before low side, later overrides win (filter.py:123-160)
+            p, n = pads[a], sizes[a]
+            for bc, rng in ((bcs[2 * a + 1], p + n + np.arange(p)), (bcs[2 * a], np.arange(p))):
+                if _is_value(bc) and rng.size:
+                    sl = [slice(None)] * 3
+                    sl[a] = rng
+                    C[tuple(sl)] = float(bc)
+        kx, ky, kz = self.weights.shape
+        y3 = np.zeros(sizes)
+        for a in range(kx):   # 'valid' convolution: output o reads C[o + (k-1) - m]
+            for b in range(ky):
+                for c in range(kz):
+                    y3 += self.weights[a, b, c] * C[kx - 1 - a:kx - 1 - a + sizes[0], ky - 1 - b:ky - 1 - b + sizes[1],
+                                                    kz - 1 - c:kz - 1 - c + sizes[2]]
+        return np.ascontiguousarray(y3.transpose(2, 1, 0)).ravel()   # element (i, j, k) -> (k ny + j) nx + i
 
     def set_filter_radius(self, radius, relative_units=True):
         """Cone kernel max(0, r - |d|) normalised to unit sum (pymoto/modules/filter.py:189-205)."""
@@ -144,13 +183,17 @@ class FilterConv(Module):
             for m, n in zip(self._maps_host, sizes):
                 ptr, pos = self._inverse_map(m, n)
                 inv += [torch.from_numpy(ptr).to(device), torch.from_numpy(pos).to(device)]
-            self._dev = (w, *maps, *inv)
+            const = None
+            if self._const_host is not None:
+                const = (torch.from_numpy(self._const_host).to(device),
+                         torch.ones(1, dtype=torch.float64, device=device))
+            self._dev = (w, *maps, *inv, const)
         return self._dev
 
     def _apply(self, v, transpose):
         vd, kind = _to_device(v)
         g = self.grid
-        w, px, py, pz, ixp, ixs, iyp, iys, izp, izs = self._device_data(vd.device)
+        w, px, py, pz, ixp, ixs, iyp, iys, izp, izs, const = self._device_data(vd.device)
         kx, ky, kz = self.weights.shape
         y = torch.empty_like(vd)
         if transpose:
@@ -158,6 +201,9 @@ class FilterConv(Module):
                  stream())
         else:
             call("pmg_conv_filter", g.nelx, g.nely, g.nelz, w, kx, ky, kz, px, py, pz, vd, y, stream())
+            if const is not None:   # y += conv(C): the constant-value sides
+                field, one = const
+                call("pmg_axpy_ratio", F64, g.nel, y, field, one, one, 1.0, stream())
         return _from_device(y, kind)
 
     def __call__(self, x):

@@ -8,6 +8,7 @@ at module level for plotting only.  The fixtures are small .npz files; the tests
     python tests/golden/make_golden.py vti      # the VTI files only
     python tests/golden/make_golden.py mma      # the MMA steps only
     python tests/golden/make_golden.py scalars  # the ScalarToFile logs only
+    python tests/golden/make_golden.py filters2 # the FilterConv / DensityFilter variants only
 """
 import os
 import sys
@@ -226,6 +227,37 @@ def mma_mbb(pym):
     save("mma_mbb.npz", **out)
 
 
+def filter_variants(pym):
+    """FilterConv with constant-value (and mixed) boundary padding, and DensityFilter with `nonpadding`: outputs
+    and adjoints of pyMOTO's own modules on random inputs."""
+    out = {}
+    cases = [("c3", (7, 5, 4), 2.5, dict(xmin_bc=0.0, xmax_bc=1.0, ymin_bc="edge", ymax_bc="wrap", zmin_bc=0.5,
+                                         zmax_bc="symmetric")),
+             ("c2", (9, 6), 2.0, dict(xmin_bc=1.0, xmax_bc="wrap", ymin_bc=0.0, ymax_bc=0.25)),
+             ("c3b", (6, 6, 5), 1.5, dict(xmin_bc="wrap", xmax_bc="wrap", ymin_bc=0.0, ymax_bc=0.0, zmin_bc=1.0,
+                                          zmax_bc=0.0))]
+    for tag, shp, r, bcs in cases:
+        d = pym.VoxelDomain(*shp)
+        rng = np.random.default_rng(11)
+        x = rng.uniform(0.0, 1.0, d.nel)
+        dy = rng.standard_normal(d.nel)
+        fc = pym.FilterConv(d, radius=r, **bcs)
+        sx = pym.Signal("x", x)
+        sy = fc(sx)
+        out.update({f"{tag}_shape": np.array(shp), f"{tag}_r": np.array(r), f"{tag}_x": x, f"{tag}_dy": dy,
+                    f"{tag}_y": sy.state, f"{tag}_dx": fc._sensitivity(dy)})
+    for tag, shp, r in [("np2", (10, 6), 1.5), ("np3", (6, 5, 4), 2.0)]:
+        d = pym.VoxelDomain(*shp)
+        rng = np.random.default_rng(12)
+        x = rng.uniform(0.0, 1.0, d.nel)
+        dy = rng.standard_normal(d.nel)
+        nonpad = np.sort(rng.choice(d.nel, d.nel // 3, replace=False))
+        df = pym.DensityFilter(d, radius=r, nonpadding=nonpad)
+        out.update({f"{tag}_shape": np.array(shp), f"{tag}_r": np.array(r), f"{tag}_x": x, f"{tag}_dy": dy,
+                    f"{tag}_nonpad": nonpad, f"{tag}_y": df(x), f"{tag}_dx": df._sensitivity(dy)})
+    save("filter_variants.npz", **out)
+
+
 def vti_cases():
     """The VTI output cases: (name, (nelx, nely, nelz), element size, origin, scale, vectors).  Pure numpy, so
     the tests rebuild the same inputs without pyMOTO."""
@@ -299,3 +331,5 @@ if __name__ == "__main__":
         mma_mbb(pym)
     if "all" in which or "scalars" in which:
         scalar_files(pym)
+    if "all" in which or "filters2" in which:
+        filter_variants(pym)

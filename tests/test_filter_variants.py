@@ -1,0 +1,115 @@
+"""FilterConv with constant-value padding and DensityFilter with `nonpadding`, against pyMOTO's own modules.
+
+CPU: the host side (padded index maps with skipped positions, the constant field, the inverse maps of the
+adjoint) evaluated by a numpy restatement of what the conv kernels compute.  GPU: the modules themselves."""
+import numpy as np
+import pytest
+import torch
+
+CONST_CASES = ["c3", "c2", "c3b"]
+BCS = {"c3": dict(xmin_bc=0.0, xmax_bc=1.0, ymin_bc="edge", ymax_bc="wrap", zmin_bc=0.5, zmax_bc="symmetric"),
+       "c2": dict(xmin_bc=1.0, xmax_bc="wrap", ymin_bc=0.0, ymax_bc=0.25),
+       "c3b": dict(xmin_bc="wrap", xmax_bc="wrap", ymin_bc=0.0, ymax_bc=0.0, zmin_bc=1.0, zmax_bc=0.0)}
+
+
+def _emulate(fc, x, d):
+    """What conv_filter_kernel + the constant field and conv_filter_adjoint_kernel compute, in numpy."""
+    g = fc.grid
+    nx, ny, nz = g.nelx, g.nely, max(g.nelz, 1)
+    kx, ky, kz = fc.weights.shape
+    mx, my, mz = fc._maps_host
+    elem = lambda i, j, k: (k * ny + j) * nx + i  # noqa: E731
+    y = np.zeros(nx * ny * nz)
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                acc = 0.0
+                for c in range(kz):
+                    kk = mz[k + kz - 1 - c]
+                    for b in range(ky):
+                        jj = my[j + ky - 1 - b]
+                        for a in range(kx):
+                            ii = mx[i + kx - 1 - a]
+                            if kk < 0 or jj < 0 or ii < 0:
+                                continue
+                            acc += fc.weights[a, b, c] * x[elem(ii, jj, kk)]
+                y[elem(i, j, k)] = acc
+    if fc._const_host is not None:
+        y = y + fc._const_host
+    dx = np.zeros_like(y)
+    inv = [fc._inverse_map(m, n) for m, n in zip(fc._maps_host, (nx, ny, nz))]
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                acc = 0.0
+                for Pz in inv[2][1][inv[2][0][k]:inv[2][0][k + 1]]:
+                    for Py in inv[1][1][inv[1][0][j]:inv[1][0][j + 1]]:
+                        for Px in inv[0][1][inv[0][0][i]:inv[0][0][i + 1]]:
+                            for c in range(kz):
+                                oz = Pz - (kz - 1) + c
+                                if not 0 <= oz < nz:
+                                    continue
+                                for b in range(ky):
+                                    oy = Py - (ky - 1) + b
+                                    if not 0 <= oy < ny:
+                                        continue
+                                    for a in range(kx):
+                                        ox = Px - (kx - 1) + a
+                                        if 0 <= ox < nx:
+                                            acc += fc.weights[a, b, c] * d[elem(ox, oy, oz)]
+                dx[elem(i, j, k)] = acc
+    return y, dx
+
+
+@pytest.mark.parametrize("tag", CONST_CASES)
+def test_constant_padding_host_side_matches_pymoto(tag, golden):
+    import pymoto_gb300 as pg
+    g = golden("filter_variants.npz")
+    d = pg.VoxelDomain(*[int(v) for v in g[f"{tag}_shape"]])
+    fc = pg.FilterConv(d, radius=float(g[f"{tag}_r"]), **BCS[tag])
+    y, dx = _emulate(fc, g[f"{tag}_x"], g[f"{tag}_dy"])
+    np.testing.assert_allclose(y, g[f"{tag}_y"], rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(dx, g[f"{tag}_dx"], rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("tag", ["np2", "np3"])
+def test_oracle_nonpadding_matches_pymoto(tag, golden):
+    import oracle as O
+    g = golden("filter_variants.npz")
+    grid = O.Grid(*[int(v) for v in g[f"{tag}_shape"]])
+    H, s = O.density_filter_matrix(grid, float(g[f"{tag}_r"]))
+    s = O.density_filter_nonpadding(s, g[f"{tag}_nonpad"])
+    np.testing.assert_allclose(O.density_filter(H, s, g[f"{tag}_x"]), g[f"{tag}_y"], rtol=1e-13)
+    np.testing.assert_allclose(O.density_filter_T(H, s, g[f"{tag}_dy"]), g[f"{tag}_dx"], rtol=1e-13, atol=1e-15)
+
+
+def test_constant_zero_sides_need_no_field():
+    import pymoto_gb300 as pg
+    fc = pg.FilterConv(pg.VoxelDomain(6, 4), radius=1.5, xmin_bc=0.0, xmax_bc=0)
+    assert fc._const_host is None and fc._maps_host[0][0] == -1 and fc._maps_host[0][-1] == -1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", CONST_CASES)
+def test_constant_padding_on_device(tag, golden):
+    import pymoto_gb300 as pg
+    g = golden("filter_variants.npz")
+    d = pg.VoxelDomain(*[int(v) for v in g[f"{tag}_shape"]])
+    fc = pg.FilterConv(d, radius=float(g[f"{tag}_r"]), **BCS[tag])
+    x = torch.from_numpy(g[f"{tag}_x"]).cuda()
+    np.testing.assert_allclose(fc(x).cpu().numpy(), g[f"{tag}_y"], rtol=1e-13, atol=1e-15)
+    dy = torch.from_numpy(g[f"{tag}_dy"]).cuda()
+    np.testing.assert_allclose(fc._sensitivity(dy).cpu().numpy(), g[f"{tag}_dx"], rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", ["np2", "np3"])
+def test_density_filter_nonpadding_on_device(tag, golden):
+    import pymoto_gb300 as pg
+    g = golden("filter_variants.npz")
+    d = pg.VoxelDomain(*[int(v) for v in g[f"{tag}_shape"]])
+    df = pg.DensityFilter(d, radius=float(g[f"{tag}_r"]), nonpadding=g[f"{tag}_nonpad"])
+    x = torch.from_numpy(g[f"{tag}_x"]).cuda()
+    np.testing.assert_allclose(df(x).cpu().numpy(), g[f"{tag}_y"], rtol=1e-13, atol=1e-15)
+    dy = torch.from_numpy(g[f"{tag}_dy"]).cuda()
+    np.testing.assert_allclose(df._sensitivity(dy).cpu().numpy(), g[f"{tag}_dx"], rtol=1e-13, atol=1e-15)
