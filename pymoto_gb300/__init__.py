@@ -3,7 +3,7 @@
 Drop-in GPU Modules and LinearSolvers with pyMOTO's API:
   DensityFilter, FilterConv, SIMP / MathExpression (SIMP form), AssembleStiffness, LinSolve, EinSum,
   CG, GeometricMultigrid, DampedJacobi, DenseCholesky, MixedPrecisionCG, OC, MMA (MMA1987 / MMA2007 / GCMMA), Scaling,
-  WriteToVTI (VoxelDomain.write_to_vti), ScalarToFile.
+  WriteToVTI (VoxelDomain.write_to_vti), ScalarToFile, finite_difference.
 The arithmetic runs in hand-written CUDA kernels of libpymoto_gb300.so through its C ABI
 (include/pymoto_gb300.h); there is no CPU fallback.
 """
@@ -20,6 +20,7 @@ from .solvers import (CG, Chebyshev, DampedJacobi, DenseCholesky, GeometricMulti
 from .autograd import ComplianceObjective
 from .vti import WriteToVTI
 from .scalars import ScalarToFile
+from .routines import finite_difference
 
 __version__ = "0.1.0"
 
@@ -27,4 +28,4 @@ __all__ = ["AssembleStiffness", "DensityFilter", "DeviceDyad", "EinSum", "Filter
            "SIMP", "Grid", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "Chebyshev", "DampedJacobi",
            "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
            "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI", "Scaling",
-           "MMA", "ScalarToFile"]
+           "MMA", "ScalarToFile", "finite_difference"]

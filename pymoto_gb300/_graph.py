@@ -246,5 +246,67 @@ class Network(Module):
     def __call__(self, *args):
         raise RuntimeError("Cannot re-connect signals in existing network")
 
+    @staticmethod
+    def _signal_set(sigs):
+        if sigs is None:
+            return set()
+        return {s for s in (_as_list(sigs) if isinstance(sigs, (list, tuple)) else [sigs]) if _is_signal(s)}
+
+    def _stubs(self):
+        all_in, all_out = set(), set()
+        for m in self.mods:
+            all_in |= self._signal_set(m.sig_in)
+            all_out |= self._signal_set(m.sig_out)
+        return all_in, all_out
+
+    @property
+    def sig_in(self):
+        """Input signals no module of the network produces (core_objects.py:895-902)."""
+        all_in, all_out = self._stubs()
+        return list(all_in - all_out)
+
+    @sig_in.setter
+    def sig_in(self, v):
+        raise RuntimeError("Cannot re-connect signals in existing network")
+
+    @property
+    def sig_out(self):
+        """Output signals no module of the network uses (core_objects.py:904-911)."""
+        all_in, all_out = self._stubs()
+        return list(all_out - all_in)
+
+    @sig_out.setter
+    def sig_out(self, v):
+        raise RuntimeError("Cannot re-connect signals in existing network")
+
+    def get_input_cone(self, fromsig=None, frommod=None):
+        """The modules that depend on `fromsig` / `frommod`, in network order (core_objects.py:913-928)."""
+        touched = self._signal_set(fromsig)
+        frommod = set(_as_list(frommod) if isinstance(frommod, (list, tuple)) else ([] if frommod is None else
+                                                                                   [frommod]))
+        if not touched and not frommod:
+            return self
+        cone = Network()
+        for m in self.mods:
+            if m in frommod or self._signal_set(m.sig_in) & touched:
+                touched |= self._signal_set(m.sig_out)
+                cone.mods.append(m)
+        return cone
+
+    def get_output_cone(self, tosig=None, tomod=None):
+        """The modules `tosig` / `tomod` depend on, in network order (core_objects.py:930-945)."""
+        dependent = self._signal_set(tosig)
+        tomod = set(_as_list(tomod) if isinstance(tomod, (list, tuple)) else ([] if tomod is None else [tomod]))
+        if not dependent and not tomod:
+            return self
+        cone = []
+        for m in reversed(self.mods):
+            if m in tomod or self._signal_set(m.sig_out) & dependent:
+                dependent |= self._signal_set(m.sig_in)
+                cone.append(m)
+        out = Network()
+        out.mods = list(reversed(cone))
+        return out
+
 
 Network.active.append(Network())
