@@ -175,6 +175,9 @@ class MMA:
         if function is None:
             from .core import Network
             function = Network.active[0]
+        if slice_network:
+            from .routines import slice_network as _slice
+            function = _slice(function, self.variables, self.responses)
         self.function = function
         self.verbosity = verbosity
         self.response_is_uptodate = not any(s.state is None for s in self.responses)

@@ -18,6 +18,12 @@ class OC:
                  verbosity=2, l1init=0.0, l2init=100000.0, l1l2tol=1e-4, maxvol=None):
         self.variable = variables[0] if isinstance(variables, (list, tuple)) else variables
         self.response = response
+        if function is None:
+            from .core import Network
+            function = Network.active[0]
+        if slice_network:
+            from .routines import slice_network as _slice
+            function = _slice(function, [self.variable], [response])
         self.function = function
         self.move, self.xmin, self.xmax = float(move), float(xmin), float(xmax)
         self.verbosity = verbosity

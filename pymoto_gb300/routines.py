@@ -48,6 +48,21 @@ def _parse(sigs):
     return list(sigs) if isinstance(sigs, (list, tuple)) else [sigs]
 
 
+def slice_network(function, variables, responses):
+    """The modules between the variables and the responses (Optimizer's slice_network,
+    pymoto/common/optimizers.py:55-71); variables without a state are computed first."""
+    sub = function.get_output_cone(responses).get_input_cone(variables)
+    if len(sub) == 0:
+        raise RuntimeError(f"Could not find a network that uses the provided input signals {variables} "
+                           f"and produces the requested output signals {responses}")
+    for s in variables:
+        if s.state is None:
+            function.get_output_cone(tosig=s).response()
+        if s.state is None:
+            raise RuntimeError(f"Input signal {s} has no state.")
+    return sub
+
+
 def finite_difference(fromsig=None, tosig=None, function=None, dx=1e-8, relative_dx=False, tol=1e-5, random=True,
                       use_df=None, test_fn=None, keep_zero_structure=True, verbose=True, entries=None, central=False):
     if function is None:

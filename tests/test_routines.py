@@ -119,3 +119,15 @@ def test_finite_difference_on_the_device_network(capsys):
     out = pg.finite_difference(sx, sc, fn, dx=1e-4, relative_dx=True, tol=1e-5, use_df=[1.0], verbose=False,
                                entries=els, central=True)
     assert out == {"x": (0, 16)}
+
+
+def test_optimizer_slice_network_keeps_only_the_connecting_modules():
+    sx, sz = Signal("x", np.ones(3)), Signal("z", np.ones(2))
+    with Network() as fn:
+        sy = Square()(sx)
+        sc = Sum()(sy)
+        Square()(sz)
+    oc = pg.OC(sx, sc, fn, slice_network=True, verbosity=0)
+    assert [type(m).__name__ for m in oc.function] == ["Square", "Sum"]
+    with pytest.raises(RuntimeError):
+        pg.OC(sz, sc, fn, slice_network=True)
