@@ -20,6 +20,9 @@ class VoxelDomain:
         self.nel = self.nelx * self.nely * max(self.nelz, 1)
         self.nnodes = (self.nelx + 1) * (self.nely + 1) * (self.nelz + 1)
         self.elemnodes = 2 ** self.dim
+        # local node a of an element sits at the corner with signs (x, y, z) = (+-1, +-1, +-1): bit 0 of a is x,
+        # bit 1 is y, bit 2 is z (pyMOTO's local order, domain.py:132-142)
+        self.node_numbering = [[1 if (a >> c) & 1 else -1 for c in range(3)] for a in range(self.elemnodes)]
         I, J, K = np.meshgrid(np.arange(self.nelx), np.arange(self.nely), np.arange(max(self.nelz, 1)),
                               indexing="ij")
         self.elements = self.get_elemnumber(I, J, K)
@@ -34,6 +37,79 @@ class VoxelDomain:
     @property
     def size(self):
         return np.array([self.nelx, self.nely, self.nelz])[: self.dim]
+
+    @property
+    def domain_size(self):
+        return np.array([self.nelx * self.unitx, self.nely * self.unity, self.nelz * self.unitz])[: self.dim]
+
+    def get_node_indices(self, nod_idx=None):
+        """(i, j[, k]) of node number(s), stacked on the first axis (all nodes by default)."""
+        n = np.arange(self.nnodes) if nod_idx is None else np.asarray(nod_idx)
+        nx1, ny1 = self.nelx + 1, self.nely + 1
+        ijk = [n % nx1, (n // nx1) % ny1] + ([n // (nx1 * ny1)] if self.dim == 3 else [])
+        return np.stack(ijk, axis=0)
+
+    def get_node_position(self, nod_idx=None):
+        """Coordinates (dim, #nodes) of node number(s): origin + index * element size."""
+        ijk = self.get_node_indices(nod_idx)
+        return (self.origin[: self.dim] + self.element_size[: self.dim] * ijk.T).T
+
+    def get_element_indices(self, el_idx=None):
+        """(i, j[, k]) of element number(s), stacked on the first axis (all elements by default)."""
+        e = np.arange(self.nel) if el_idx is None else np.asarray(el_idx)
+        ijk = [e % self.nelx, (e // self.nelx) % self.nely] + ([e // (self.nelx * self.nely)] if self.dim == 3 else [])
+        return np.stack(ijk, axis=0)
+
+    def get_element_position(self, el_idx=None):
+        """Centre coordinates (dim, #elements) of element number(s)."""
+        ijk = self.get_element_indices(el_idx)
+        return ((self.origin + self.element_size / 2)[: self.dim] + self.element_size[: self.dim] * ijk.T).T
+
+    def get_elemconnectivity(self, i, j, k=0):
+        """Node numbers (..., nodes per element) of the elements with indices (i, j, k), in the local node order."""
+        i, j, k = np.asarray(i), np.asarray(j), np.asarray(k)
+        return np.stack([self.get_nodenumber(i + (a & 1), j + ((a >> 1) & 1), k + ((a >> 2) & 1))
+                         for a in range(self.elemnodes)], axis=-1)
+
+    def get_rigid_body_modes(self):
+        """Translations and rotations about the origin, (dim * #nodes, dim (dim + 1) / 2): x, y[, z]
+        translations, then [Rx, Ry,] Rz."""
+        d = self.dim
+        rbm = np.zeros((self.nnodes * d, d * (d + 1) // 2))
+        for c in range(d):
+            rbm[c::d, c] = 1.0
+        x = self.get_node_position()
+        if d == 3:
+            rbm[1::d, -3], rbm[2::d, -3] = x[2], -x[1]
+            rbm[0::d, -2], rbm[2::d, -2] = x[2], -x[0]
+        rbm[0::d, -1], rbm[1::d, -1] = -x[1], x[0]
+        return rbm
+
+    def eval_shape_fun(self, pos):
+        """Bilinear / trilinear shape functions at local coordinates pos in [-h/2, h/2]:
+        N_a = prod_c (h_c / 2 + s_ac pos_c) / V, s_ac the corner signs of local node a."""
+        h = self.element_size[: self.dim]
+        v = np.prod(h)
+        if not v > 0.0:
+            raise ValueError("Element volume needs to be positive")
+        n = np.ones(self.elemnodes) / v
+        for c in range(self.dim):
+            n = n * np.array([h[c] / 2 + sg[c] * pos[c] for sg in self.node_numbering])
+        return n
+
+    def eval_shape_fun_der(self, pos):
+        """dN_a/dx_c (dim, nodes per element) at local coordinates pos."""
+        h = self.element_size[: self.dim]
+        v = np.prod(h)
+        if not v > 0.0:
+            raise ValueError("Element volume needs to be positive")
+        dn = np.ones((self.dim, self.elemnodes)) / v
+        for c in range(self.dim):
+            for o in range(self.dim):
+                if o != c:
+                    dn[c] = dn[c] * np.array([h[o] / 2 + sg[o] * pos[o] for sg in self.node_numbering])
+            dn[c] = dn[c] * np.array([sg[c] for sg in self.node_numbering])
+        return dn
 
     def get_elemnumber(self, eli, elj, elk=0):
         return (np.asarray(elk) * self.nely + elj) * self.nelx + eli

@@ -9,6 +9,7 @@ at module level for plotting only.  The fixtures are small .npz files; the tests
     python tests/golden/make_golden.py mma      # the MMA steps only
     python tests/golden/make_golden.py scalars  # the ScalarToFile logs only
     python tests/golden/make_golden.py filters2 # the FilterConv / DensityFilter variants only
+    python tests/golden/make_golden.py domain   # the VoxelDomain geometry helpers only
 """
 import os
 import sys
@@ -258,6 +259,27 @@ def filter_variants(pym):
     save("filter_variants.npz", **out)
 
 
+def domain_helpers(pym):
+    """VoxelDomain's geometry helpers: node / element indices and positions, connectivity, rigid body modes and
+    shape functions (with derivatives) at seeded local points, for a 2D and a 3D domain with a moved origin."""
+    out = {}
+    rng = np.random.default_rng(13)
+    for tag, shp, size, origin in [("d2", (5, 3, 0), (0.5, 0.25, 1.0), (1.0, -2.0, 0.0)),
+                                   ("d3", (4, 3, 2), (0.1, 0.2, 0.3), (0.5, 0.0, -1.0))]:
+        d = pym.VoxelDomain(*shp, *size)
+        d.origin = np.array(origin)
+        pts = (rng.uniform(-0.5, 0.5, (6, d.dim)) * np.array(size[:d.dim]))
+        ii, jj, kk = rng.integers(0, shp[0], 5), rng.integers(0, shp[1], 5), rng.integers(0, max(shp[2], 1), 5)
+        out.update({f"{tag}_pts": pts, f"{tag}_ijk": np.stack([ii, jj, kk]),
+                    f"{tag}_node_idx": d.get_node_indices(), f"{tag}_node_pos": d.get_node_position(),
+                    f"{tag}_el_idx": d.get_element_indices(), f"{tag}_el_pos": d.get_element_position(),
+                    f"{tag}_econn": d.get_elemconnectivity(ii, jj, kk), f"{tag}_rbm": d.get_rigid_body_modes(),
+                    f"{tag}_N": np.array([d.eval_shape_fun(p) for p in pts]),
+                    f"{tag}_dN": np.array([d.eval_shape_fun_der(p) for p in pts]),
+                    f"{tag}_domain_size": d.domain_size})
+    save("domain_helpers.npz", **out)
+
+
 def vti_cases():
     """The VTI output cases: (name, (nelx, nely, nelz), element size, origin, scale, vectors).  Pure numpy, so
     the tests rebuild the same inputs without pyMOTO."""
@@ -333,3 +355,5 @@ if __name__ == "__main__":
         scalar_files(pym)
     if "all" in which or "filters2" in which:
         filter_variants(pym)
+    if "all" in which or "domain" in which:
+        domain_helpers(pym)

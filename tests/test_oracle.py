@@ -75,7 +75,7 @@ def test_prolongation_known_answers():
     """pyMOTO tests/test_solvers_multigrid.py:9-91: R^T 1 = 8/6/4.5/3.375 (3D), R 1 = 1."""
     g = O.Grid(10, 10, 10)
     R = O.prolongation(g)
-    uc = (R.T @ np.ones(g.ndof)).reshape(6, 6, 6, 3, order="F") if False else (R.T @ np.ones(g.ndof))
+    uc = R.T @ np.ones(g.ndof)
     cg = g.coarse()
     I, J, K = np.meshgrid(np.arange(6), np.arange(6), np.arange(6), indexing="ij")
     nb = (I == 0) | (I == 5)
