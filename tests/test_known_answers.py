@@ -137,3 +137,24 @@ def test_conv_filter_close_to_density_filter_somewhere():
     y1 = O.conv_filter(g, O.conv_filter_weights(g, 5.0), x)
     H, s = O.density_filter_matrix(g, 5.0)
     assert np.abs(y1 - O.density_filter(H, s, x)).min() <= 1e-4
+
+
+# ---- dyad contraction ----------------------------------------------------------------------------------
+def test_element_contraction_of_a_dyad_sum():
+    """pyMOTO's batched contract(K0, rows=dofconn, cols=dofconn) of a two-term dyad (test_dyadicmatrix.py:
+    599-704): per element sum_k u_k[dofs_e] . K0 v_k[dofs_e], here with a non-symmetric K0 and u != v, and with
+    the Dirichlet entries of the dyad zeroed first (dyadcarrier.py:179-189)."""
+    rng = np.random.default_rng(0)
+    g = O.Grid(3, 2, 2)
+    K0 = rng.standard_normal((24, 24))
+    us, vs = [rng.random(g.ndof) for _ in range(2)], [rng.random(g.ndof) for _ in range(2)]
+    bc = np.array([0, 4, 17])
+    got = O.sensitivity_contract(g, K0, us, vs, bc=bc)
+    dc = g.dofconn()
+    want = np.zeros(g.nel)
+    for u, v in zip(us, vs):
+        u, v = u.copy(), v.copy()
+        u[bc] = v[bc] = 0.0
+        for e in range(g.nel):
+            want[e] += u[dc[e]] @ K0 @ v[dc[e]]
+    np.testing.assert_allclose(got, want, rtol=1e-13)
