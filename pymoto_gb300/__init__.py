@@ -1,7 +1,7 @@
 """pymoto_gb300 -- pyMOTO's structured-grid topology-optimisation hot path on GB300 (sm_103a).
 
 Drop-in GPU Modules and LinearSolvers with pyMOTO's API:
-  DensityFilter, FilterConv, SIMP / MathExpression (SIMP form), AssembleStiffness, LinSolve, EinSum,
+  DensityFilter, FilterConv, SIMP / MathExpression (SIMP form), AssembleStiffness, AssembleMass, LinSolve, EinSum,
   CG, GeometricMultigrid, DampedJacobi, DenseCholesky, MixedPrecisionCG, OC, MMA (MMA1987 / MMA2007 / GCMMA), Scaling,
   WriteToVTI (VoxelDomain.write_to_vti), ScalarToFile, finite_difference.
 The arithmetic runs in hand-written CUDA kernels of libpymoto_gb300.so through its C ABI
@@ -10,7 +10,7 @@ The arithmetic runs in hand-written CUDA kernels of libpymoto_gb300.so through i
 from . import _lib
 from .core import HOST_RUNTIME, Module, Network, Signal
 from .domain import VoxelDomain
-from .modules import (AssembleStiffness, DensityFilter, DeviceDyad, EinSum, FilterConv, LinSolve, MathExpression,
+from .modules import (AssembleMass, AssembleStiffness, DensityFilter, DeviceDyad, EinSum, FilterConv, LinSolve, MathExpression,
                       SIMP, Scaling)
 from .operators import Grid, StencilOperator, StiffnessOperator, element_stiffness
 from .optimizers import OC
@@ -24,7 +24,7 @@ from .routines import finite_difference
 
 __version__ = "0.1.0"
 
-__all__ = ["AssembleStiffness", "DensityFilter", "DeviceDyad", "EinSum", "FilterConv", "LinSolve", "MathExpression",
+__all__ = ["AssembleMass", "AssembleStiffness", "DensityFilter", "DeviceDyad", "EinSum", "FilterConv", "LinSolve", "MathExpression",
            "SIMP", "Grid", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "Chebyshev", "DampedJacobi",
            "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
            "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI", "Scaling",

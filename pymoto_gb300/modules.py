@@ -15,7 +15,7 @@ from . import _lib
 from ._lib import F64, RESIDUAL, call, stream
 from .core import Module
 from .domain import grid_of
-from .operators import Grid, StiffnessOperator, Workspace, bc_node_mask, element_stiffness
+from .operators import Grid, StiffnessOperator, Workspace, bc_node_mask, element_mass, element_stiffness
 from .solvers import _from_device, _to_device, default_solver
 
 
@@ -346,6 +346,33 @@ class AssembleStiffness(Module):
             call(fn, g.nelx, g.nely, g.nelz, self.stiffness_element, self._mask, ud, vd, 1.0,
                  int(k > 0), dx, stream())
         return _from_device(dx, self._kind)
+
+
+class AssembleMass(AssembleStiffness):
+    """M(x) = sum_e x_e M0 with the consistent element mass matrix (pymoto/modules/assembly.py:466-520), as the
+    same matrix-free device operator as the stiffness (a symmetric element matrix over dim dofs per node).
+    Dirichlet rows and columns hold bcdiagval (default 0, as in pyMOTO).  The device operator carries dim
+    dofs per node, so ndof must equal the domain's dimension; the sensitivity is the FP64 contraction
+    x-derivative u_e^T M0 v_e (the mixed contraction relies on K0 annihilating translations, M0 does not)."""
+
+    def __init__(self, domain, bc=None, bcdiagval=0.0, matrix_type=None, add_constant=None, reuse_sparsity=True,
+                 material_property=1.0, ndof=1):
+        self.domain = domain
+        self.grid = Grid(*grid_of(domain))
+        g = self.grid
+        if add_constant is not None:
+            raise NotImplementedError("add_constant is not supported by the matrix-free operator")
+        if ndof != g.dim:
+            raise NotImplementedError(f"the device operator carries {g.dim} dofs per node: AssembleMass needs "
+                                      f"ndof={g.dim} (got {ndof}); a scalar operator is not provided")
+        self.sensitivity_precision = "fp64"
+        self.material_property = material_property
+        self.el_mat = element_mass(domain, ndof, material_property)
+        self.stiffness_element = self.el_mat      # the operator's element matrix
+        self.bc = None if bc is None else np.asarray(bc, dtype=np.int64).ravel()
+        self.bcdiagval = float(bcdiagval)
+        self._mask_host = bc_node_mask(g.nnodes, g.dim, self.bc)
+        self._mask = None
 
 
 # --------------------------------------------------------------------------------------------- LinSolve

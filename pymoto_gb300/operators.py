@@ -78,6 +78,29 @@ def element_stiffness(dim, e_modulus=1.0, poisson_ratio=0.3, plane="strain", uni
     return K0
 
 
+def element_mass(domain, ndof, material_property=1.0):
+    """Consistent element matrix material_property * int N^T N dV with ndof components per node (pyMOTO's
+    AssembleMass, pymoto/modules/assembly.py:466-520): 2x2(x2) Gauss points at +-h/(2 sqrt 3), weight
+    prod(h/2); in 2D the thickness unitz multiplies the property.  Host-only, setup."""
+    h = np.array([domain.unitx, domain.unity, domain.unitz], dtype=np.float64)
+    dim = 2 if not domain.nelz else 3
+    nn = 2 ** dim
+    w = np.prod(h[:dim] / 2)
+    prop = material_property * (np.prod(h[dim:]) if dim != 3 else 1.0)
+    signs = [[1 if (a >> c) & 1 else -1 for c in range(3)] for a in range(nn)]
+    M = np.zeros((nn * ndof, nn * ndof))
+    Nmat = np.zeros((ndof, nn * ndof))
+    for sg in signs:
+        pos = np.array(sg) * (h / 2) / np.sqrt(3)
+        N = np.ones(nn) / np.prod(h[:dim])
+        for c in range(dim):
+            N = N * np.array([h[c] / 2 + s2[c] * pos[c] for s2 in signs])
+        for a in range(nn):
+            Nmat[:, ndof * a:ndof * (a + 1)] = np.identity(ndof) * N[a]
+        M += w * prop * Nmat.T @ Nmat
+    return M
+
+
 def bc_node_mask(nnodes, dim, bc):
     """One byte per node, bit d set for Dirichlet dof node*dim + d (host array)."""
     m = np.zeros(nnodes, dtype=np.uint8)

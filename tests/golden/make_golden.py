@@ -10,6 +10,7 @@ at module level for plotting only.  The fixtures are small .npz files; the tests
     python tests/golden/make_golden.py scalars  # the ScalarToFile logs only
     python tests/golden/make_golden.py filters2 # the FilterConv / DensityFilter variants only
     python tests/golden/make_golden.py domain   # the VoxelDomain geometry helpers only
+    python tests/golden/make_golden.py mass     # the AssembleMass matrices only
 """
 import os
 import sys
@@ -280,6 +281,26 @@ def domain_helpers(pym):
     save("domain_helpers.npz", **out)
 
 
+def mass_matrices(pym):
+    """AssembleMass element matrices (ndof 1 and dim, non-unit element sizes, density) and one assembled mass
+    matrix with Dirichlet dofs applied to a seeded vector."""
+    out = {}
+    for tag, shp, size, ndof, rho in [("m2", (3, 2, 0), (0.5, 2.0, 0.3), 2, 7.8), ("m2s", (3, 2, 0), (1.0, 1.0, 1.0), 1, 1.0),
+                                      ("m3", (2, 2, 2), (0.1, 0.2, 0.3), 3, 2.5), ("m3s", (2, 2, 2), (1.0, 0.5, 2.0), 1, 3.0)]:
+        d = pym.VoxelDomain(*shp, *size)
+        m = pym.AssembleMass(d, material_property=rho, ndof=ndof)
+        out[f"{tag}_M0"] = m.el_mat
+    d = pym.VoxelDomain(4, 3, 2, 0.5, 1.0, 1.5)
+    rng = np.random.default_rng(14)
+    x = rng.uniform(0.1, 1.0, d.nel)
+    bc = np.array([0, 1, 2, 10, 44])
+    sx = pym.Signal("x", x)
+    M = pym.AssembleMass(d, bc=bc, material_property=2.0, ndof=3)(sx).state
+    u = rng.standard_normal(M.shape[0])
+    out.update({"asm_x": x, "asm_bc": bc, "asm_u": u, "asm_Mu": M @ u})
+    save("mass.npz", **out)
+
+
 def vti_cases():
     """The VTI output cases: (name, (nelx, nely, nelz), element size, origin, scale, vectors).  Pure numpy, so
     the tests rebuild the same inputs without pyMOTO."""
@@ -357,3 +378,5 @@ if __name__ == "__main__":
         filter_variants(pym)
     if "all" in which or "domain" in which:
         domain_helpers(pym)
+    if "all" in which or "mass" in which:
+        mass_matrices(pym)
