@@ -16,7 +16,6 @@ pyMOTO's own path (oracle) on the host cores.
 """
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -434,7 +433,7 @@ def operator_case(args):
     printed as JSON (a small case for ncu)."""
     import torch
     import pymoto_gb300 as pg
-    from pymoto_gb300._lib import F32, F64, RESIDUAL, MATVEC
+    from pymoto_gb300._lib import F32, RESIDUAL, MATVEC
     shape = SHAPE if args.shape is None else tuple(int(v) for v in args.shape.split("x"))
     d = pg.VoxelDomain(*shape)
     bc, f = cantilever(shape)

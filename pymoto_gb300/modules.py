@@ -5,14 +5,12 @@ counterpart and runs on the device through libpymoto_gb300.  Signal states may b
 answer is then numpy, so the modules mix with pyMOTO's own modules and optimizers) or CUDA tensors
 (everything stays on the device).
 """
-import copy
 import re
 
 import numpy as np
 import torch
 
-from . import _lib
-from ._lib import F64, RESIDUAL, call, stream
+from ._lib import F64, call, stream
 from .core import Module
 from .domain import grid_of
 from .operators import Grid, StiffnessOperator, Workspace, bc_node_mask, element_mass, element_stiffness

@@ -10,7 +10,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import F32, F64, JACOBI, MATVEC, RESIDUAL, call, stream
+from ._lib import F32, F64, MATVEC, call, stream
 
 TORCH_DTYPE = {F64: torch.float64, F32: torch.float32}
 

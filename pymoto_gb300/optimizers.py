@@ -5,7 +5,6 @@ optimize().  The bisection on the Lagrange multiplier runs entirely on the devic
 design iteration needs no host copy of x or dg.  pyMOTO's own OC also works with the GPU modules when the
 design Signal holds a numpy array.
 """
-import numpy as np
 import torch
 
 from ._lib import PMGError, call, stream

@@ -21,7 +21,7 @@ import torch
 from . import _lib
 from ._lib import F32, F64, JACOBI, MATVEC, RESIDUAL, call, stream
 from .domain import grid_of
-from .operators import TORCH_DTYPE, Grid, StencilOperator, StiffnessOperator, Workspace
+from .operators import Grid, StencilOperator, StiffnessOperator, Workspace
 
 PRECISIONS = {None: None, "fp64": F64, "float64": F64, "fp32": F32, "float32": F32}
 

@@ -467,7 +467,6 @@ def test_conv_filter_other_paddings_are_adjoint(pg, mode):
     fty = host(fc._sensitivity(dev(y)))
     assert abs(fx @ y - x @ fty) <= 1e-12 * np.abs(fx @ y)
     # forward equals the padded convolution of the oracle's index-map definition
-    from pymoto_gb300.modules import _pad_map
     maps = fc._maps_host
     I, J, K = np.meshgrid(*maps, indexing="ij")
     g = O.Grid(9, 6, 5)

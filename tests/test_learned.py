@@ -22,7 +22,6 @@ def bf(t):
 
 def _weights(net, name):
     """(cout, cin, 3, 3, 3) FP64 weights (BF16-rounded) and bias of one layer, from w[tap][cin][cout]."""
-    from pymoto_gb300.learned import LAYERS
     o, cin, cout = net.offsets[name]
     w = net.w.detach().cpu().double()
     W = bf(w[o:o + 27 * cin * cout]).reshape(3, 3, 3, cin, cout).permute(4, 3, 0, 1, 2).contiguous()

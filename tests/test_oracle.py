@@ -4,7 +4,6 @@ import pytest
 import scipy.sparse as sps
 
 import oracle as O
-from conftest import clamp_face_dofs
 
 
 def grid_of(shape, units=(1.0, 1.0, 1.0)):
