@@ -56,9 +56,13 @@ def parse():
     ap.add_argument("--levels", type=int, default=GPU_LEVELS)
     ap.add_argument("--sweeps", type=int, default=SWEEPS)
     ap.add_argument("--coarse-sweeps", type=int, default=None)
-    ap.add_argument("--case", default=None, choices=["operator", "mma"],
-                    help="instead of the bench: time the level-0 operator kernels alone (a small case for ncu), or "
-                         "the device MMA update of the 96x48x48 design against the numpy MMA")
+    ap.add_argument("--case", default=None, choices=["operator", "mma", "mma_run"],
+                    help="instead of the bench: time the level-0 operator kernels alone (a small case for ncu), "
+                         "the device MMA update of the 96x48x48 design against the numpy MMA, or the 96x48x48 "
+                         "MMA workload (mma_run)")
+    ap.add_argument("--mma-iters", type=int, default=100, help="MMA iterations of --case mma_run")
+    ap.add_argument("--pretrain", type=int, default=256,
+                    help="smoothed-noise fields the learned warm start sees before --case mma_run")
     ap.add_argument("--arms", default="plain_fp64,mixed,mixed_learned",
                     help="plain_fp64 (the reference's method), mixed, mixed_learned (headline: with the learned "
                          "warm start), ablations: mixed_jacobi, plain_fp64_cheb")
@@ -507,6 +511,88 @@ def mma_case(args):
     print(json.dumps(out))
 
 
+def mma_run_case(args):
+    """The 96x48x48 MMA workload: a fixed number of MMA iterations (--mma-iters, default 100) of the compliance
+    cantilever with a volume constraint of 0.5, every module, the sensitivities and the MMA update on the device,
+    for three solver arms: mixed with the learned warm start pretrained on --pretrain (default 256) seeded
+    smoothed-noise fields (Gaussian-smoothed U(0,1), sigma 4 elements, mapped to [1e-3, 1]) and trained online,
+    mixed without it, and plain FP64.  Objective Scaling(100) of the compliance, constraint 10 (mean(xf) - 0.5),
+    MMA2007 with move 0.2, x0 = 0.5.  Whole-loop times with CUDA events (synchronised each iteration, as the
+    optimizer reads its responses), printed as one JSON line."""
+    import torch
+    import pymoto_gb300 as pg
+    from scipy.ndimage import gaussian_filter
+    shape = (96, 48, 48) if args.shape is None else tuple(int(v) for v in args.shape.split("x"))
+    iters = args.mma_iters
+    npre = args.pretrain
+    o = DesignRun.opts
+    out = {"case": "mma_run", "shape": list(shape), "iterations": iters, "pretrain_fields": npre, "arms": {}}
+    for arm in ("mixed_learned", "mixed", "plain_fp64"):
+        d = pg.VoxelDomain(*shape)
+        bc, f = cantilever(shape)
+        fd = torch.from_numpy(f).cuda()
+        sx = pg.Signal("x", torch.full((d.nel,), 0.5, dtype=torch.float64, device="cuda"))
+        mixed = arm.startswith("mixed")
+        ws = None
+        with pg.Network() as fn:
+            xf = pg.FilterConv(d, radius=RADIUS)(sx)
+            xs = pg.SIMP(xmin=XMIN, penal=PENAL)(xf)
+            K = pg.AssembleStiffness(d, bc=bc, sensitivity_precision="mixed" if mixed else "fp64")(xs)
+            if mixed:
+                mgs = pg.GeometricMultigrid.hierarchy(d, levels=o["levels"], smooth_steps=o["cheb_degree"],
+                                                      precision="fp32", coarse_smooth_steps=o["cheb_coarse_degree"],
+                                                      smoother="chebyshev", cheb_ratio=o["cheb_ratio"],
+                                                      coarse_lag=o["coarse_lag"])
+                if arm == "mixed_learned":
+                    from pymoto_gb300.learned import LearnedWarmStart
+                    ws = LearnedWarmStart(shape, stride=o["learned_stride"], capacity=8,
+                                          train_steps=o["learned_train_steps"], lr=o["learned_lr"], seed=1234,
+                                          history=o["learned_history"], train_every=o["learned_train_every"],
+                                          gate=o["learned_gate"], gate_skip=o["learned_gate_skip"])
+                solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=TOL, m=o["m"], inner_iters=o["inner_iters"],
+                                             inner_tol=o["inner_tol"], warm_start=ws, verify_residual=False)
+            else:
+                mgs = pg.GeometricMultigrid.hierarchy(d, levels=o["levels"], smoother_w=OMEGA,
+                                                      smooth_steps=o["sweeps"])
+                solver = pg.CG(preconditioner=mgs[0], tol=TOL)
+            u = pg.LinSolve(hermitian=True, symmetric=True, solver=solver)(K, fd)
+            c = pg.EinSum("i,i->")(u, fd)
+            g0 = pg.Scaling(scaling=100.0)(c)
+            g1 = pg.Scaling(scaling=5.0, maxval=0.5 * d.nel)(pg.EinSum("i->")(xf))
+        t_pre = 0.0
+        if ws is not None and npre > 0:
+            rng = np.random.default_rng(2024)
+            t0 = time.perf_counter()
+            for _ in range(npre):
+                nz = max(shape[2], 1)
+                field = gaussian_filter(rng.uniform(0.0, 1.0, (nz, shape[1], shape[0])), sigma=4.0)
+                field = (field - field.min()) / max(field.max() - field.min(), 1e-300)
+                sx.state = torch.from_numpy(1e-3 + (1.0 - 1e-3) * field.ravel()).cuda()
+                fn.response()
+            torch.cuda.synchronize()
+            t_pre = time.perf_counter() - t0
+            sx.state = torch.full((d.nel,), 0.5, dtype=torch.float64, device="cuda")
+            fn.response()
+        mma = pg.MMA(sx, [g0, g1], fn, move=0.2, verbosity=0)
+        xval = mma.x
+        hist, solves = [], []
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(iters):
+            xnew, gk, _ = mma.step(x=xval)
+            hist.append(gk.cpu().numpy().tolist())
+            solves.append(solver.iterations)
+            xval = xnew
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / iters
+        out["arms"][arm] = {"design_it_per_s": 1e3 / ms, "ms_per_iteration": ms,
+                            "solver_iterations_mean": float(np.mean(solves)), "g_first": hist[0], "g_last": hist[-1],
+                            "mean_x_last": float(xval.mean().item()), "pretrain_s": t_pre}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.case == "operator":
@@ -514,6 +600,9 @@ def main():
         return
     if args.case == "mma":
         mma_case(args)
+        return
+    if args.case == "mma_run":
+        mma_run_case(args)
         return
     rank, world, local_rank = dist_info()
     threads = os.cpu_count() or 1
