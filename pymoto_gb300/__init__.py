@@ -1,7 +1,8 @@
 """pymoto_gb300 -- pyMOTO's structured-grid topology-optimisation hot path on GB300 (sm_103a).
 
 Drop-in GPU Modules and LinearSolvers with pyMOTO's API:
-  DensityFilter, FilterConv, SIMP / MathExpression (SIMP form), AssembleStiffness, AssembleMass, LinSolve, EinSum,
+  DensityFilter, FilterConv, SIMP, MathExpression (any sympy expression; the SIMP form on its kernels),
+  AssembleStiffness, AssembleMass, LinSolve, EinSum,
   CG, GeometricMultigrid, DampedJacobi, DenseCholesky, MixedPrecisionCG, OC, MMA (MMA1987 / MMA2007 / GCMMA), Scaling,
   WriteToVTI (VoxelDomain.write_to_vti), ScalarToFile, finite_difference.
 The arithmetic runs in hand-written CUDA kernels of libpymoto_gb300.so through its C ABI

@@ -239,15 +239,128 @@ _SIMP_EXPR = re.compile(r"^\s*([0-9.eE+-]+)\s*\+\s*\(\s*1\s*-\s*([0-9.eE+-]+)\s*
                         r"([0-9.]+)\s*$")
 
 
-class MathExpression(SIMP):
-    """The SIMP subset of pyMOTO's MathExpression: expressions "a + (1-a)*inp0^p" (any input name)."""
+def _torch_functions():
+    """Names sympy's default printer writes, mapped to torch (device tensors stay on the device)."""
+    def nmax(*a):
+        out = torch.as_tensor(a[0])
+        for v in a[1:]:
+            out = torch.maximum(out, torch.as_tensor(v, dtype=out.dtype, device=out.device))
+        return out
+
+    def nmin(*a):
+        out = torch.as_tensor(a[0])
+        for v in a[1:]:
+            out = torch.minimum(out, torch.as_tensor(v, dtype=out.dtype, device=out.device))
+        return out
+    t = torch
+    return {"sin": t.sin, "cos": t.cos, "tan": t.tan, "asin": t.asin, "acos": t.acos, "atan": t.atan,
+            "atan2": t.atan2, "sinh": t.sinh, "cosh": t.cosh, "tanh": t.tanh, "asinh": t.asinh, "acosh": t.acosh,
+            "atanh": t.atanh, "exp": t.exp, "log": t.log, "sqrt": t.sqrt, "Abs": t.abs, "sign": t.sign,
+            "floor": t.floor, "ceiling": t.ceil, "re": t.real, "im": t.imag, "conjugate": t.conj, "Max": nmax,
+            "Min": nmin, "pi": float(np.pi), "E": float(np.e)}
+
+
+def _zeros_like(v):
+    if isinstance(v, torch.Tensor):
+        return torch.zeros_like(v)
+    try:
+        z = v.copy()
+        z[...] = 0
+        return z
+    except (AttributeError, TypeError):   # a Python number or a numpy scalar
+        return v * 0
+
+
+class MathExpression(Module):
+    """pyMOTO's MathExpression (pymoto/modules/generic.py:14-140): any sympy expression of the inputs, named
+    inp0, inp1, ... or by their signal tags, with sympy's derivatives for the sensitivity.
+
+    The SIMP interpolation "a + (1-a)*inp0^p" of an element field runs in the SIMP kernels (pmg_simp,
+    pmg_simp_backward).  Any other expression is evaluated by sympy's lambdify: with numpy for numpy states (as
+    pyMOTO), with torch functions for tensor states (device scalars and vectors stay on the device); the
+    sensitivity sums over broadcast axes as pyMOTO does."""
 
     def __init__(self, expression):
-        m = _SIMP_EXPR.match(expression)
-        if m is None or float(m.group(1)) != float(m.group(2)):
-            raise NotImplementedError(f"only 'xmin + (1-xmin)*inp0^p' runs on the GPU path, got {expression!r}")
-        super().__init__(xmin=float(m.group(1)), penal=float(m.group(4)))
         self.expression = expression
+        m = _SIMP_EXPR.match(expression)
+        self._simp = None
+        if m is not None and float(m.group(1)) == float(m.group(2)):
+            self._simp = SIMP(xmin=float(m.group(1)), penal=float(m.group(4)))
+            self.xmin, self.penal = self._simp.xmin, self._simp.penal
+        self._mode = None
+        self._fns = {}
+
+    def _parse(self, n):
+        from sympy import lambdify
+        from sympy.parsing.sympy_parser import parse_expr
+        text = self.expression.replace("^", "**").lower()
+        expr = parse_expr(text)
+        names = [f"inp{i}" for i in range(n)]
+        if self.sig_in is not None:
+            rep = {}
+            for i, s in enumerate(self.sig_in):
+                tag = getattr(s, "tag", "")
+                if tag:
+                    t = tag.lower()
+                    if t in names and t in text:
+                        raise RuntimeError(f"Name '{t}' multiple defined")
+                    rep[t] = names[i]
+            expr = expr.subs(rep)
+        ders = [expr.diff(v) for v in names]
+        tf = _torch_functions()
+        self._fns = {"numpy": (lambdify(names, expr, "numpy"), lambdify(names, ders, "numpy")),
+                     "torch": (lambdify(names, expr, [tf]), lambdify(names, ders, [tf]))}
+
+    def __call__(self, *args):
+        field = len(args) == 1 and (getattr(args[0], "ndim", 0) >= 1 and
+                                   (args[0].numel() if isinstance(args[0], torch.Tensor) else np.size(args[0])) > 1)
+        if self._simp is not None and field:
+            self._mode = "simp"
+            return self._simp(args[0])       # a call with plain values: no network connection
+        if not self._fns:
+            self._parse(len(args))
+        self._mode = "torch" if any(isinstance(a, torch.Tensor) for a in args) else "numpy"
+        self.x = args
+        return self._fns[self._mode][0](*args)
+
+    def _sensitivity(self, df_dy):
+        if self._mode == "simp":
+            return self._simp._sensitivity(df_dy)
+        dg_df = self._fns[self._mode][1](*self.x)
+        out = []
+        for i, xi in enumerate(self.x):
+            add = df_dy * dg_df[i]
+            d = _zeros_like(xi)
+            if isinstance(add, torch.Tensor):
+                d_complex = d.is_complex() if isinstance(d, torch.Tensor) else np.iscomplexobj(d)
+                if add.is_complex() and not d_complex:
+                    add = add.real
+                shape_d = tuple(d.shape) if hasattr(d, "shape") else ()
+                if not shape_d:
+                    d = d + torch.sum(torch.as_tensor(add))
+                elif tuple(add.shape) != shape_d:
+                    lead = add.dim() - len(shape_d)
+                    axes = list(range(lead)) + [lead + k for k in range(len(shape_d))
+                                                if shape_d[k] == 1 and add.shape[lead + k] != 1]
+                    red = torch.sum(add, dim=axes, keepdim=True) if axes else add
+                    d = d + red.reshape(shape_d)
+                else:
+                    d = d + add
+            else:
+                if np.isrealobj(d) and np.iscomplexobj(add):
+                    add = np.real(add)
+                if (not hasattr(d, "__len__")) or (hasattr(d, "ndim") and d.ndim == 0):
+                    d += np.sum(add)
+                elif d.shape != np.shape(add):
+                    add = np.asarray(add)
+                    lead = add.ndim - d.ndim
+                    axes = tuple(range(lead)) + tuple(lead + k for k in range(d.ndim)
+                                                      if d.shape[k] == 1 and add.shape[lead + k] != 1)
+                    d += np.squeeze(np.add.reduce(add, axis=axes, keepdims=True), axis=tuple(range(lead)))
+                else:
+                    d += add
+            out.append(d)
+        return out
 
 
 # --------------------------------------------------------------------------------------------- dyad

@@ -11,6 +11,7 @@ at module level for plotting only.  The fixtures are small .npz files; the tests
     python tests/golden/make_golden.py filters2 # the FilterConv / DensityFilter variants only
     python tests/golden/make_golden.py domain   # the VoxelDomain geometry helpers only
     python tests/golden/make_golden.py mass     # the AssembleMass matrices only
+    python tests/golden/make_golden.py math     # the MathExpression cases only
 """
 import os
 import sys
@@ -301,6 +302,35 @@ def mass_matrices(pym):
     save("mass.npz", **out)
 
 
+def math_cases():
+    """MathExpression cases: (name, expression, tags, inputs, output seed).  Pure numpy."""
+    rng = np.random.default_rng(15)
+    return [
+        ("named", "sin(x)*y", ["x", "y"], [rng.uniform(0, 3, 3), 4.8], rng.standard_normal(3)),
+        ("scalar", "10*(inp0/300 - 0.5)", ["vol"], [150.3], 1.0),
+        ("vectors", "inp0^2 + inp1*inp0", ["a", "b"], [rng.standard_normal(4), rng.standard_normal(4)],
+         rng.standard_normal(4)),
+        ("bcast", "exp(-inp0)*inp1 + sqrt(inp1)", ["p", "q"], [rng.standard_normal((2, 3)),
+                                                                      rng.uniform(0.1, 1, 3)],
+         rng.standard_normal((2, 3))),
+        ("simp", "1e-9 + (1-1e-9)*inp0^3", ["xf"], [0.37], 2.0),
+        ("funcs", "tanh(inp0) + log(inp0 + 2)*cos(inp0) - atan(inp0)", [""], [rng.uniform(0, 1, 5)],
+         rng.standard_normal(5)),
+    ]
+
+
+def math_expressions(pym):
+    out = {}
+    for name, expr, tags, inputs, seed in math_cases():
+        sigs = [pym.Signal(t, v) for t, v in zip(tags, inputs)]
+        m = pym.MathExpression(expr)
+        so = m(*sigs)
+        out[f"{name}_y"] = np.asarray(so.state)
+        for i, d in enumerate(m._sensitivity(seed)):
+            out[f"{name}_d{i}"] = np.asarray(d)
+    save("math_expression.npz", **out)
+
+
 def vti_cases():
     """The VTI output cases: (name, (nelx, nely, nelz), element size, origin, scale, vectors).  Pure numpy, so
     the tests rebuild the same inputs without pyMOTO."""
@@ -380,3 +410,5 @@ if __name__ == "__main__":
         domain_helpers(pym)
     if "all" in which or "mass" in which:
         mass_matrices(pym)
+    if "all" in which or "math" in which:
+        math_expressions(pym)
