@@ -4,7 +4,7 @@ Drop-in GPU Modules and LinearSolvers with pyMOTO's API:
   DensityFilter, FilterConv, SIMP, MathExpression (any sympy expression; the SIMP form on its kernels),
   AssembleStiffness, AssembleMass, LinSolve, EinSum,
   CG, GeometricMultigrid, DampedJacobi, DenseCholesky, MixedPrecisionCG, OC, MMA (MMA1987 / MMA2007 / GCMMA), Scaling,
-  WriteToVTI (VoxelDomain.write_to_vti), ScalarToFile, finite_difference.
+  WriteToVTI (VoxelDomain.write_to_vti), ScalarToFile, finite_difference, minimize_oc, minimize_mma.
 The arithmetic runs in hand-written CUDA kernels of libpymoto_gb300.so through its C ABI
 (include/pymoto_gb300.h); there is no CPU fallback.
 """
@@ -21,7 +21,7 @@ from .solvers import (CG, Chebyshev, DampedJacobi, DenseCholesky, GeometricMulti
 from .autograd import ComplianceObjective
 from .vti import WriteToVTI
 from .scalars import ScalarToFile
-from .routines import finite_difference
+from .routines import finite_difference, minimize_mma, minimize_oc
 
 __version__ = "0.1.0"
 
@@ -29,4 +29,5 @@ __all__ = ["AssembleMass", "AssembleStiffness", "DensityFilter", "DeviceDyad", "
            "SIMP", "Grid", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "Chebyshev", "DampedJacobi",
            "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
            "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI", "Scaling",
-           "MMA", "ScalarToFile", "finite_difference"]
+           "MMA", "ScalarToFile", "finite_difference",
+           "minimize_oc", "minimize_mma"]

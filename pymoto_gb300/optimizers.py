@@ -86,19 +86,38 @@ class OC:
         self.history.append(g)
         return xnew, g, dg
 
-    def optimize(self, maxiter=100, tolx=1e-4, tolf=1e-4):
-        gprev = 0.0
+    def optimize(self, maxiter=100, tolx=1e-4, tolf=1e-4, evaluate_last=False):
+        """pyMOTO's optimization loop (pymoto/common/optimizers.py:275-322): stop on the relative change of the
+        response or of the design; the variables are left at the last evaluated design (at the new one, with
+        its response computed, when evaluate_last)."""
+        nom = type(self).__name__
+        gcur = 0.0
+        dxr = self.xmax - self.xmin
+        last = None
         while self.iter < maxiter:
-            x, _ = self._x()
+            xval, kind = self._x()       # the state tensor itself: step() replaces the state, not its values
+            last = (xval, kind)
             xnew, g, _ = self.step()
-            rel_df = abs(g - gprev) / abs(g) if g != 0 else 0.0
-            gprev = g
-            if self.verbosity >= 2:
-                print(f"It. {self.iter}, g = {g:.6e}")
+            gprev, gcur = gcur, g
+            rel_df = abs(gcur - gprev) / abs(gcur) if gcur != 0 else float("inf")
             if rel_df < tolf:
-                self.variable.state = _from_device(x, _to_device(self.variable.state)[1])
+                if self.verbosity >= 1:
+                    print(f"{nom} converged: Relative function change |Δf|/|f| ({rel_df}) below tolerance ({tolf})")
+                self.variable.state = _from_device(xval, kind)
                 break
-            dx = float(torch.linalg.vector_norm(x - xnew).item()) / max(float(torch.linalg.vector_norm(x).item()), 1e-300)
+            if self.verbosity >= 2:
+                print("It. {0: 4d}, g0: {1:+.4e}".format(self.iter, g))
+            rel_step = float((torch.linalg.vector_norm((xval - xnew) / dxr) /
+                              torch.linalg.vector_norm(xval / dxr)).item())
+            if rel_step < tolx:
+                if self.verbosity >= 1:
+                    print(f"{nom} converged: Relative stepsize |Δx|/|x| ({rel_step}) below tolerance ({tolx})")
+                if evaluate_last:
+                    self.function.response()
+                else:
+                    self.variable.state = _from_device(xval, kind)
+                break
             self.iter += 1
-            if dx < tolx:
-                break
+        else:
+            if last is not None:   # maxiter reached: the last new design was computed, not evaluated
+                self.variable.state = _from_device(*last)

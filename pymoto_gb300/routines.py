@@ -191,3 +191,19 @@ def finite_difference(fromsig=None, tosig=None, function=None, dx=1e-8, relative
     print(f'\nFinished finite-difference check of "{type(function).__name__}"\n')
     print("=" * 105 + "\n")
     return summary
+
+
+def minimize_oc(variables, objective, function=None, maxit=100, tolx=1e-4, tolf=1e-4, **kwargs):
+    """pyMOTO's minimize_oc (pymoto/routines.py:300-316) with the device OC update."""
+    from .optimizers import OC
+    oc = OC(variables, objective, function, **kwargs)
+    oc.optimize(maxiter=maxit, tolx=tolx, tolf=tolf)
+    return oc
+
+
+def minimize_mma(variables, responses, function=None, maxit=100, tolx=1e-4, tolf=1e-4, **kwargs):
+    """pyMOTO's minimize_mma (pymoto/routines.py:320-338) with the device MMA update."""
+    from .mma import MMA
+    mma = MMA(variables, responses, function, **kwargs)
+    mma.optimize(maxiter=maxit, tolx=tolx, tolf=tolf)
+    return mma
