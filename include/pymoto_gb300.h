@@ -275,6 +275,22 @@ int pmg_oc_status(const void* scratch);
  * the status at its next synchronisation instead of adding one. */
 int pmg_oc_status_async(const void* scratch, unsigned* status, void* stream);
 
+/* ---- additive-manufacturing overhang filter (OverhangFilter, pymoto/modules/filter.py:381-713) ---------------
+ * One launch per layer `layer` along the print axis `lay` (0 x, 1 y, 2 z), print direction `step` (+1 / -1);
+ * nz >= 1 (a 2D grid passes nz = 1).  The K support kernels kern[K][w0][w1][w2] (C order) span one layer (w_lay
+ * = 1) and an odd window in the other axes, centred: c_lay = step, c_other = (w - 1) / 2.  Forward (layers in
+ * print order): s = (sum_k (v_k + shift)^p)^(1/q) - backshift over the previous printed layer (a baseplate of 1
+ * below the first), y = smooth min of x and s.  Adjoint (layers in reverse print order, `first` for the first
+ * call): dx from dy; the derivatives of this layer's supports go to dsupp_cur[K][plane], those of the layer
+ * processed before are read from dsupp_later (two distinct buffers, swapped between calls). */
+int pmg_overhang_forward(int nx, int ny, int nz, int lay, int step, int layer, int w0, int w1, int w2, int c0, int c1,
+                         int c2, int K, const double* kern, double p, double q, double shift, double backshift,
+                         double eps, const double* x, double* y, double* s, void* stream);
+int pmg_overhang_adjoint(int nx, int ny, int nz, int lay, int step, int layer, int first, int w0, int w1, int w2,
+                         int c0, int c1, int c2, int K, const double* kern, double p, double q, double shift,
+                         double backshift, double eps, const double* x, const double* y, const double* s,
+                         const double* dy, double* dsupp_cur, const double* dsupp_later, double* dx, void* stream);
+
 /* ---- Method of Moving Asymptotes (MMA.step / mmasub / subsolv, pymoto/common/mma.py:96-474) ----------
  * One design update: the asymptote offsets adapt from xold1/xold2 (when params.adapt), the convex separable
  * approximation is built from the responses g[m+1] and their sensitivities dg[(m+1) x n] (row-major; row 0 the

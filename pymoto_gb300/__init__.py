@@ -1,7 +1,7 @@
 """pymoto_gb300 -- pyMOTO's structured-grid topology-optimisation hot path on GB300 (sm_103a).
 
 Drop-in GPU Modules and LinearSolvers with pyMOTO's API:
-  DensityFilter, FilterConv, SIMP, MathExpression (any sympy expression; the SIMP form on its kernels),
+  DensityFilter, FilterConv, OverhangFilter, SIMP, MathExpression (any sympy expression; the SIMP form on its kernels),
   AssembleStiffness, AssembleMass, LinSolve, EinSum,
   CG, GeometricMultigrid, DampedJacobi, DenseCholesky, MixedPrecisionCG, OC, MMA (MMA1987 / MMA2007 / GCMMA), Scaling,
   WriteToVTI (VoxelDomain.write_to_vti), ScalarToFile, finite_difference, minimize_oc, minimize_mma.
@@ -21,6 +21,7 @@ from .solvers import (CG, Chebyshev, DampedJacobi, DenseCholesky, GeometricMulti
 from .autograd import ComplianceObjective
 from .vti import WriteToVTI
 from .scalars import ScalarToFile
+from .overhang import OverhangFilter
 from .routines import finite_difference, minimize_mma, minimize_oc
 
 __version__ = "0.1.0"
@@ -30,4 +31,4 @@ __all__ = ["AssembleMass", "AssembleStiffness", "DensityFilter", "DeviceDyad", "
            "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
            "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI", "Scaling",
            "MMA", "ScalarToFile", "finite_difference",
-           "minimize_oc", "minimize_mma"]
+           "minimize_oc", "minimize_mma", "OverhangFilter"]

@@ -82,6 +82,8 @@ SIGNATURES = {
     "pmg_oc_status": (I, [P]),
     "pmg_oc_status_async": (I, [P, P, P]),
     "pmg_oc_update": (I, [L, P, P, P, D, D, D, D, D, D, D, P, P]),
+    "pmg_overhang_forward": (I, [I] * 13 + [P] + [D] * 5 + [P] * 4),
+    "pmg_overhang_adjoint": (I, [I] * 14 + [P] + [D] * 5 + [P] * 8),
     "pmg_mma_scratch_bytes": (c_size_t, [L, I]),
     "pmg_mma_update": (I, [L] + [P] * 16),
     "pmg_nn_conv3d_forward": (I, [I, I, I, I, I, I, P, P, P, I, P, P, P]),

@@ -12,6 +12,7 @@ at module level for plotting only.  The fixtures are small .npz files; the tests
     python tests/golden/make_golden.py domain   # the VoxelDomain geometry helpers only
     python tests/golden/make_golden.py mass     # the AssembleMass matrices only
     python tests/golden/make_golden.py math     # the MathExpression cases only
+    python tests/golden/make_golden.py overhang # the OverhangFilter cases only
 """
 import os
 import sys
@@ -331,6 +332,33 @@ def math_expressions(pym):
     save("math_expression.npz", **out)
 
 
+def overhang_cases():
+    """OverhangFilter cases: (name, shape, element size, direction, angle, nsampling).  Pure data."""
+    return [("o2y", (12, 8, 0), (1.0, 1.0, 1.0), "y", 45.0, 8),
+            ("o2x", (9, 10, 0), (1.0, 0.7, 1.0), "-x", 60.0, 8),
+            ("o3z", (6, 5, 7), (1.0, 1.0, 1.0), "z", 45.0, 8),
+            ("o3y", (5, 6, 4), (0.8, 1.0, 1.2), "-y", 50.0, 6)]
+
+
+def overhang(pym):
+    out = {}
+    import contextlib
+    import io
+    for name, shp, size, direc, ang, ns in overhang_cases():
+        d = pym.VoxelDomain(*shp, *size)
+        rng = np.random.default_rng(16)
+        x = rng.uniform(0.0, 1.0, d.nel)
+        dy = rng.standard_normal(d.nel)
+        with contextlib.redirect_stdout(io.StringIO()):   # the reference prints the support offsets
+            m = pym.OverhangFilter(d, direction=direc, overhang_angle=ang, nsampling=ns)
+            sx = pym.Signal("x", x)
+            sy = m(sx)
+            dx = m._sensitivity(dy)
+        out.update({f"{name}_x": x, f"{name}_dy": dy, f"{name}_y": sy.state, f"{name}_dx": dx,
+                    f"{name}_offsets": m.layer_offsets, f"{name}_origin": np.asarray(m.origin)})
+    save("overhang.npz", **out)
+
+
 def vti_cases():
     """The VTI output cases: (name, (nelx, nely, nelz), element size, origin, scale, vectors).  Pure numpy, so
     the tests rebuild the same inputs without pyMOTO."""
@@ -412,3 +440,5 @@ if __name__ == "__main__":
         mass_matrices(pym)
     if "all" in which or "math" in which:
         math_expressions(pym)
+    if "all" in which or "overhang" in which:
+        overhang(pym)
