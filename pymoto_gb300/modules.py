@@ -127,6 +127,33 @@ class FilterConv(Module):
                            enumerate(zip(sizes, self.pad_sizes))]
         self._const_host = self._constant_field(bcs, sizes)
         self._dev = None
+        self._overrides = {}      # element -> fixed input value (override_values)
+        self._fzero = None        # the same kernel with zero padding on every side
+        self._ov_dev = None
+
+    def override_values(self, index, value):
+        """Fixed input `value` at the elements that `index` selects in the (nelx, nely, nelz) element array
+        (pymoto/modules/filter.py:162-182); later calls win.  Linear: y = F(x) + F0(1_S (value - x)) with F0 the
+        zero-padded convolution (padding copies still read x, as in pyMOTO), and dx = F^T dy - 1_S F0^T dy
+        (pyMOTO zeroes the overridden positions in the adjoint)."""
+        g = self.grid
+        nz = max(g.nelz, 1)
+        el = np.arange(g.nel).reshape(nz, g.nely, g.nelx).transpose(2, 1, 0)
+        for e in np.atleast_1d(el[index]).ravel():
+            self._overrides[int(e)] = float(value)
+        if self._fzero is None:
+            w = self.weights if g.nelz else self.weights[:, :, 0]
+            zero = dict(xmin_bc=0.0, xmax_bc=0.0, ymin_bc=0.0, ymax_bc=0.0, zmin_bc=0.0, zmax_bc=0.0)
+            self._fzero = FilterConv(self.domain, weights=w, **zero)
+        self._ov_dev = None
+
+    def _override_data(self, device):
+        if self._ov_dev is None or self._ov_dev[0].device != device:
+            idx = np.array(sorted(self._overrides), dtype=np.int64)
+            val = np.array([self._overrides[i] for i in idx], dtype=np.float64)
+            self._ov_dev = (torch.from_numpy(idx).to(device), torch.from_numpy(val).to(device),
+                            torch.ones(1, dtype=torch.float64, device=device))
+        return self._ov_dev
 
     def _constant_field(self, bcs, sizes):
         """conv(C) on the element grid (element numbering), C the padded field that holds the constant values on
@@ -202,6 +229,15 @@ class FilterConv(Module):
             if const is not None:   # y += conv(C): the constant-value sides
                 field, one = const
                 call("pmg_axpy_ratio", F64, g.nel, y, field, one, one, 1.0, stream())
+        if self._overrides:
+            idx, val, one = self._override_data(vd.device)
+            if transpose:             # dx[S] -= (F0^T d)[S]
+                t = self._fzero._apply(vd, True)
+                y.index_add_(0, idx, -t.index_select(0, idx))
+            else:                     # y += F0(1_S (value - x))
+                d = torch.zeros_like(vd)
+                d.index_copy_(0, idx, val - vd.index_select(0, idx))
+                call("pmg_axpy_ratio", F64, g.nel, y, self._fzero._apply(d, False), one, one, 1.0, stream())
         return _from_device(y, kind)
 
     def __call__(self, x):

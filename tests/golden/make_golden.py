@@ -250,6 +250,21 @@ def filter_variants(pym):
         sy = fc(sx)
         out.update({f"{tag}_shape": np.array(shp), f"{tag}_r": np.array(r), f"{tag}_x": x, f"{tag}_dy": dy,
                     f"{tag}_y": sy.state, f"{tag}_dx": fc._sensitivity(dy)})
+    # fixed values inside the domain (override_values), with and without a constant side
+    for tag, shp, r, bcs, ovs in [("ov2", (9, 7), 2.0, {}, [((slice(0, 3), slice(2, 5), 0), 1.0),
+                                                             ((np.array([6, 7]), np.array([1, 1]), 0), 0.0)]),
+                                  ("ov3", (6, 5, 4), 1.5, dict(ymax_bc=0.3), [((slice(None), 0, slice(1, 3)), 0.7),
+                                                                               ((2, slice(None), 3), 0.0)])]:
+        d = pym.VoxelDomain(*shp)
+        rng = np.random.default_rng(17)
+        x = rng.uniform(0.0, 1.0, d.nel)
+        dy = rng.standard_normal(d.nel)
+        fc = pym.FilterConv(d, radius=r, **bcs)
+        for idx, val in ovs:
+            fc.override_values(idx, val)
+        sy = fc(pym.Signal("x", x))
+        out.update({f"{tag}_shape": np.array(shp), f"{tag}_r": np.array(r), f"{tag}_x": x, f"{tag}_dy": dy,
+                    f"{tag}_y": sy.state, f"{tag}_dx": fc._sensitivity(dy)})
     for tag, shp, r in [("np2", (10, 6), 1.5), ("np3", (6, 5, 4), 2.0)]:
         d = pym.VoxelDomain(*shp)
         rng = np.random.default_rng(12)

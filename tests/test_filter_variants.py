@@ -72,6 +72,47 @@ def test_constant_padding_host_side_matches_pymoto(tag, golden):
     np.testing.assert_allclose(dx, g[f"{tag}_dx"], rtol=1e-13, atol=1e-15)
 
 
+OVERRIDES = {"ov2": ({}, [((slice(0, 3), slice(2, 5), 0), 1.0), ((np.array([6, 7]), np.array([1, 1]), 0), 0.0)]),
+             "ov3": (dict(ymax_bc=0.3), [((slice(None), 0, slice(1, 3)), 0.7), ((2, slice(None), 3), 0.0)])}
+
+
+def _override_filter(tag, golden):
+    import pymoto_gb300 as pg
+    g = golden("filter_variants.npz")
+    d = pg.VoxelDomain(*[int(v) for v in g[f"{tag}_shape"]])
+    bcs, ovs = OVERRIDES[tag]
+    fc = pg.FilterConv(d, radius=float(g[f"{tag}_r"]), **bcs)
+    for idx, val in ovs:
+        fc.override_values(idx, val)
+    return fc, g
+
+
+@pytest.mark.parametrize("tag", list(OVERRIDES))
+def test_override_values_host_side_matches_pymoto(tag, golden):
+    """y = F(x) + F0(1_S (v - x)) and dx = F^T dy - 1_S F0^T dy with the kernels' emulation."""
+    fc, g = _override_filter(tag, golden)
+    x, dy = g[f"{tag}_x"], g[f"{tag}_dy"]
+    S = np.array(sorted(fc._overrides))
+    v = np.array([fc._overrides[i] for i in S])
+    d = np.zeros_like(x)
+    d[S] = v - x[S]
+    y, dx = _emulate(fc, x, dy)
+    y0, t0 = _emulate(fc._fzero, d, dy)
+    dx[S] -= t0[S]
+    np.testing.assert_allclose(y + y0, g[f"{tag}_y"], rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(dx, g[f"{tag}_dx"], rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", list(OVERRIDES))
+def test_override_values_on_device(tag, golden):
+    fc, g = _override_filter(tag, golden)
+    y = fc(torch.from_numpy(g[f"{tag}_x"]).cuda())
+    np.testing.assert_allclose(y.cpu().numpy(), g[f"{tag}_y"], rtol=1e-13, atol=1e-15)
+    dx = fc._sensitivity(torch.from_numpy(g[f"{tag}_dy"]).cuda())
+    np.testing.assert_allclose(dx.cpu().numpy(), g[f"{tag}_dx"], rtol=1e-13, atol=1e-15)
+
+
 @pytest.mark.parametrize("tag", ["np2", "np3"])
 def test_oracle_nonpadding_matches_pymoto(tag, golden):
     import oracle as O
