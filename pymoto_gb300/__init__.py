@@ -2,7 +2,7 @@
 
 Drop-in GPU Modules and LinearSolvers with pyMOTO's API:
   DensityFilter, FilterConv, OverhangFilter, SIMP, MathExpression (any sympy expression; the SIMP form on its kernels),
-  AssembleStiffness, AssembleMass, LinSolve, EinSum,
+  AssembleStiffness, AssembleMass, AssemblePoisson, LinSolve, EinSum,
   CG, GeometricMultigrid, DampedJacobi, DenseCholesky, MixedPrecisionCG, OC, MMA (MMA1987 / MMA2007 / GCMMA), Scaling,
   WriteToVTI (VoxelDomain.write_to_vti), ScalarToFile, finite_difference, minimize_oc, minimize_mma.
 The arithmetic runs in hand-written CUDA kernels of libpymoto_gb300.so through its C ABI
@@ -11,7 +11,7 @@ The arithmetic runs in hand-written CUDA kernels of libpymoto_gb300.so through i
 from . import _lib
 from .core import HOST_RUNTIME, Module, Network, Signal
 from .domain import VoxelDomain
-from .modules import (AssembleMass, AssembleStiffness, DensityFilter, DeviceDyad, EinSum, FilterConv, LinSolve, MathExpression,
+from .modules import (AssembleMass, AssemblePoisson, AssembleStiffness, DensityFilter, DeviceDyad, EinSum, FilterConv, LinSolve, MathExpression,
                       SIMP, Scaling)
 from .operators import Grid, StencilOperator, StiffnessOperator, element_stiffness
 from .optimizers import OC
@@ -26,7 +26,7 @@ from .routines import finite_difference, minimize_mma, minimize_oc
 
 __version__ = "0.1.0"
 
-__all__ = ["AssembleMass", "AssembleStiffness", "DensityFilter", "DeviceDyad", "EinSum", "FilterConv", "LinSolve", "MathExpression",
+__all__ = ["AssembleMass", "AssemblePoisson", "AssembleStiffness", "DensityFilter", "DeviceDyad", "EinSum", "FilterConv", "LinSolve", "MathExpression",
            "SIMP", "Grid", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "Chebyshev", "DampedJacobi",
            "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
            "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI", "Scaling",

@@ -13,7 +13,8 @@ import torch
 from ._lib import F64, call, stream
 from .core import Module
 from .domain import grid_of
-from .operators import Grid, StiffnessOperator, Workspace, bc_node_mask, element_mass, element_stiffness
+from .operators import (Grid, StiffnessOperator, Workspace, bc_node_mask, element_mass, element_poisson,
+                        element_stiffness, embed_scalar_element)
 from .solvers import _from_device, _to_device, default_solver
 
 
@@ -522,6 +523,48 @@ class AssembleMass(AssembleStiffness):
         self._mask = None
 
 
+class AssemblePoisson(AssembleStiffness):
+    """P(x) = sum_e x_e P0 of one scalar per node (thermal conductivity, permittivity; pyMOTO's AssemblePoisson,
+    pymoto/modules/assembly.py:523-560).  On the device the scalar field is the first component of the
+    dim-component matrix-free operator: element matrix P0 on those dofs, the other components Dirichlet
+    everywhere (rows bcdiag I, solution 0), so the stiffness operator's kernels, multigrid and solvers run it
+    unchanged, at dim times the work of a one-component operator.  LinSolve widens the right-hand side and
+    narrows the solution: user vectors have one entry per node.  bc: constrained nodes (scalar dofs)."""
+
+    def __init__(self, domain, bc=None, bcdiagval=None, matrix_type=None, add_constant=None, reuse_sparsity=True,
+                 material_property=1.0, sensitivity_precision="fp64"):
+        if add_constant is not None:
+            raise NotImplementedError("add_constant is not supported by the matrix-free operator")
+        if sensitivity_precision not in ("fp64", "mixed"):
+            raise ValueError("sensitivity_precision must be 'fp64' or 'mixed'")
+        self.sensitivity_precision = sensitivity_precision   # P0 annihilates constants, as the mixed form needs
+        self.domain = domain
+        self.grid = Grid(*grid_of(domain))
+        g = self.grid
+        self.material_property = material_property
+        self.poisson_element = element_poisson(domain, material_property)
+        self.stiffness_element = embed_scalar_element(self.poisson_element, g.dim)
+        self.bc = None if bc is None else np.asarray(bc, dtype=np.int64).ravel()
+        self.bcdiagval = float(np.max(self.poisson_element)) if bcdiagval is None else float(bcdiagval)
+        nodes = np.arange(g.nnodes)
+        extra = (nodes[:, None] * g.dim + np.arange(1, g.dim)).ravel()
+        scalar = np.zeros(0, dtype=np.int64) if self.bc is None else self.bc * g.dim
+        self._mask_host = bc_node_mask(g.nnodes, g.dim, np.concatenate([scalar, extra]))
+        self._mask = None
+
+    def __call__(self, x):
+        op = super().__call__(x)
+        op.embedded_scalar = True
+        return op
+
+
+def _widen(v, dim):
+    """Scalar nodal vector -> dim-component vector with the scalar in component 0."""
+    w = torch.zeros(v.numel() * dim, dtype=v.dtype, device=v.device)
+    w[0::dim] = v
+    return w
+
+
 # --------------------------------------------------------------------------------------------- LinSolve
 class LinSolve(Module):
     """Solve K u = f (pymoto/modules/linalg.py:121-219) with the bookkeeping of the linear-dependency-aware
@@ -617,6 +660,9 @@ class LinSolve(Module):
             raise TypeError("LinSolve on the GPU path expects the StiffnessOperator of AssembleStiffness")
         fd, kind = _to_device(rhs, device=mat.device)
         self._kind = kind
+        self._dim_embed = mat.grid.dim if getattr(mat, "embedded_scalar", False) else 0
+        if self._dim_embed:
+            fd = _widen(fd, self._dim_embed)
         if self.solver is None:
             self.solver = default_solver(mat)
         self.solver.update(mat)
@@ -625,15 +671,23 @@ class LinSolve(Module):
         self.A = sa if isinstance(sa, StiffnessOperator) and sa.code == F64 else mat.astype(F64)
         self._pairs = []
         x0 = None if self.u is None else _to_device(self.u, device=mat.device)[0]
+        if self._dim_embed and x0 is not None:
+            x0 = _widen(x0, self._dim_embed)
         u = self._lda_solve(fd, x0)
         self._u_dev = u
+        if self._dim_embed:
+            u = u[0::self._dim_embed].contiguous()
         self.u = _from_device(u, kind)
         return self.u
 
     def _sensitivity(self, dfdv):
         dd, kind = _to_device(dfdv, device=self._u_dev.device)
+        if self._dim_embed:
+            dd = _widen(dd, self._dim_embed)
         lam = self._lda_solve(dd)
         dmat = DeviceDyad([-lam], [self._u_dev])
+        if self._dim_embed:
+            lam = lam[0::self._dim_embed].contiguous()
         return dmat, _from_device(lam, kind)
 
 

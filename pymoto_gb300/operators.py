@@ -101,6 +101,38 @@ def element_mass(domain, ndof, material_property=1.0):
     return M
 
 
+def element_poisson(domain, material_property=1.0):
+    """Element matrix material_property * int grad N^T grad N dV of one scalar per node (pyMOTO's
+    AssemblePoisson, pymoto/modules/assembly.py:523-560): 2x2(x2) Gauss points at +-h/(2 sqrt 3), weight
+    prod(h/2); in 2D the thickness unitz multiplies the property.  Host-only, setup."""
+    h = np.array([domain.unitx, domain.unity, domain.unitz], dtype=np.float64)
+    dim = 2 if not domain.nelz else 3
+    nn = 2 ** dim
+    w = np.prod(h[:dim] / 2)
+    prop = material_property * (h[dim:] if dim != 3 else 1.0)
+    signs = [[1 if (a >> c) & 1 else -1 for c in range(3)] for a in range(nn)]
+    P = np.zeros((nn, nn))
+    for sg in signs:
+        pos = np.array(sg) * (h / 2) / np.sqrt(3)
+        B = np.ones((dim, nn)) / np.prod(h[:dim])
+        for c in range(dim):
+            for o in range(dim):
+                if o != c:
+                    B[c] = B[c] * np.array([h[o] / 2 + s2[o] * pos[o] for s2 in signs])
+            B[c] = B[c] * np.array([s2[c] for s2 in signs])
+        P += w * prop * B.T @ B
+    return P
+
+
+def embed_scalar_element(P, dim):
+    """The element matrix of `dim` components per node whose first component carries the scalar matrix P and
+    the others nothing: P on the dofs node * dim."""
+    nn = P.shape[0]
+    K = np.zeros((nn * dim, nn * dim))
+    K[0::dim, 0::dim] = P
+    return K
+
+
 def bc_node_mask(nnodes, dim, bc):
     """One byte per node, bit d set for Dirichlet dof node*dim + d (host array)."""
     m = np.zeros(nnodes, dtype=np.uint8)

@@ -13,6 +13,7 @@ at module level for plotting only.  The fixtures are small .npz files; the tests
     python tests/golden/make_golden.py mass     # the AssembleMass matrices only
     python tests/golden/make_golden.py math     # the MathExpression cases only
     python tests/golden/make_golden.py overhang # the OverhangFilter cases only
+    python tests/golden/make_golden.py poisson  # the AssemblePoisson cases only
 """
 import os
 import sys
@@ -374,6 +375,31 @@ def overhang(pym):
     save("overhang.npz", **out)
 
 
+def poisson(pym):
+    """AssemblePoisson element matrices, and a thermal compliance network on a 6x4x4 grid (left face held at 0,
+    uniform heat load, density-scaled conductivity): P u, the solution, the compliance and its sensitivities."""
+    out = {}
+    for tag, shp, size, k in [("p2", (3, 2, 0), (0.5, 2.0, 0.3), 2.5), ("p3", (2, 2, 2), (0.1, 0.2, 0.3), 1.7)]:
+        out[f"{tag}_P0"] = pym.AssemblePoisson(pym.VoxelDomain(*shp, *size), material_property=k).poisson_element
+    d = pym.VoxelDomain(6, 4, 4, 1.0, 0.5, 0.8)
+    bc = d.nodes[0, :, :].flatten()
+    f = np.full(d.nnodes, 1.0 / d.nnodes)
+    rng = np.random.default_rng(18)
+    x = rng.uniform(0.1, 1.0, d.nel)
+    u_rand = rng.standard_normal(d.nnodes)
+    sx = pym.Signal("x", x)
+    with pym.Network() as fn:
+        sK = pym.AssemblePoisson(d, bc=bc, material_property=2.0)(sx)
+        su = pym.LinSolve(hermitian=True, symmetric=True)(sK, f)
+        sc = pym.EinSum("i,i->")(su, f)
+    fn.reset()
+    sc.sensitivity = 1.0
+    fn.sensitivity()
+    out.update({"net_bc": bc, "net_f": f, "net_x": x, "net_Pu": sK.state @ u_rand, "net_urand": u_rand,
+                "net_u": su.state, "net_c": np.array(float(sc.state)), "net_dx": sx.sensitivity.copy()})
+    save("poisson.npz", **out)
+
+
 def vti_cases():
     """The VTI output cases: (name, (nelx, nely, nelz), element size, origin, scale, vectors).  Pure numpy, so
     the tests rebuild the same inputs without pyMOTO."""
@@ -457,3 +483,5 @@ if __name__ == "__main__":
         math_expressions(pym)
     if "all" in which or "overhang" in which:
         overhang(pym)
+    if "all" in which or "poisson" in which:
+        poisson(pym)
