@@ -498,10 +498,11 @@ class AssembleStiffness(Module):
 
 class AssembleMass(AssembleStiffness):
     """M(x) = sum_e x_e M0 with the consistent element mass matrix (pymoto/modules/assembly.py:466-520), as the
-    same matrix-free device operator as the stiffness (a symmetric element matrix over dim dofs per node).
-    Dirichlet rows and columns hold bcdiagval (default 0, as in pyMOTO).  The device operator carries dim
-    dofs per node, so ndof must equal the domain's dimension; the sensitivity is the FP64 contraction
-    x-derivative u_e^T M0 v_e (the mixed contraction relies on K0 annihilating translations, M0 does not)."""
+    same matrix-free device operator as the stiffness.  ndof = dim: the element matrix over dim dofs per node;
+    ndof = 1 (pyMOTO's default): the scalar matrix carried as component 0 of that operator with the other
+    components Dirichlet, as AssemblePoisson does (products and LinSolve take one entry per node).  Dirichlet
+    rows and columns hold bcdiagval (default 0, as in pyMOTO).  The sensitivity is the FP64 contraction
+    u_e^T M0 v_e (the mixed contraction relies on the element matrix annihilating translations, M0 does not)."""
 
     def __init__(self, domain, bc=None, bcdiagval=0.0, matrix_type=None, add_constant=None, reuse_sparsity=True,
                  material_property=1.0, ndof=1):
@@ -510,17 +511,30 @@ class AssembleMass(AssembleStiffness):
         g = self.grid
         if add_constant is not None:
             raise NotImplementedError("add_constant is not supported by the matrix-free operator")
-        if ndof != g.dim:
-            raise NotImplementedError(f"the device operator carries {g.dim} dofs per node: AssembleMass needs "
-                                      f"ndof={g.dim} (got {ndof}); a scalar operator is not provided")
+        if ndof not in (1, g.dim):
+            raise NotImplementedError(f"AssembleMass on the device takes ndof=1 or ndof={g.dim} (got {ndof})")
+        self.ndof = ndof
         self.sensitivity_precision = "fp64"
         self.material_property = material_property
         self.el_mat = element_mass(domain, ndof, material_property)
-        self.stiffness_element = self.el_mat      # the operator's element matrix
         self.bc = None if bc is None else np.asarray(bc, dtype=np.int64).ravel()
         self.bcdiagval = float(bcdiagval)
-        self._mask_host = bc_node_mask(g.nnodes, g.dim, self.bc)
+        if ndof == g.dim:
+            self.stiffness_element = self.el_mat      # the operator's element matrix
+            self._mask_host = bc_node_mask(g.nnodes, g.dim, self.bc)
+        else:
+            self.stiffness_element = embed_scalar_element(self.el_mat, g.dim)
+            nodes = np.arange(g.nnodes)
+            extra = (nodes[:, None] * g.dim + np.arange(1, g.dim)).ravel()
+            scalar = np.zeros(0, dtype=np.int64) if self.bc is None else self.bc * g.dim
+            self._mask_host = bc_node_mask(g.nnodes, g.dim, np.concatenate([scalar, extra]))
         self._mask = None
+
+    def __call__(self, x):
+        op = super().__call__(x)
+        if self.ndof == 1:
+            op.embedded_scalar = True
+        return op
 
 
 class AssemblePoisson(AssembleStiffness):

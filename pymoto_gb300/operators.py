@@ -302,7 +302,13 @@ class StiffnessOperator:
     def __matmul__(self, u):
         if isinstance(u, np.ndarray):
             ud = torch.from_numpy(np.ascontiguousarray(u, dtype=self.dtype)).to(self.device)
-            return self.matvec(ud).cpu().numpy()
+            return self.__matmul__(ud).cpu().numpy()
+        d = self.grid.dim
+        if getattr(self, "embedded_scalar", False) and u.numel() == self.grid.nnodes:
+            # a scalar operator carried as component 0: one entry per node in and out
+            w = torch.zeros(self.grid.ndof, dtype=u.dtype, device=u.device)
+            w[0::d] = u
+            return self.matvec(w)[0::d].contiguous()
         return self.matvec(u.contiguous())
 
     def _diagonal_into(self, d):
