@@ -120,9 +120,11 @@ class VTIWriter:
 
     def __init__(self):
         self._threads = []
+        self._errors = []
         atexit.register(self.flush)
 
     def write(self, domain, vectors, filename="out.vti", scale=1.0):
+        self._raise_pending()
         if ".vti" not in os.path.splitext(filename)[-1].lower():
             filename += ".vti"
         staged, event = {}, None
@@ -138,14 +140,17 @@ class VTIWriter:
             event.record()
 
         def work():
-            if event is not None:
-                event.synchronize()
-            data = encode_vti(domain, staged, scale)
-            if data is None:
-                warnings.warn(f"Nothing to write to {filename}. Skipping file...")
-                return
-            with open(filename, "wb") as fh:
-                fh.write(data)
+            try:
+                if event is not None:
+                    event.synchronize()
+                data = encode_vti(domain, staged, scale)
+                if data is None:
+                    warnings.warn(f"Nothing to write to {filename}. Skipping file...")
+                    return
+                with open(filename, "wb") as fh:
+                    fh.write(data)
+            except Exception as e:   # reported by the next write() or flush()
+                self._errors.append((filename, e))
 
         t = threading.Thread(target=work, daemon=True)
         t.start()
@@ -153,9 +158,16 @@ class VTIWriter:
         return t
 
     def flush(self):
+        """Wait for the files written so far; raise if one of them could not be written."""
         for t in self._threads:
             t.join()
         self._threads = []
+        self._raise_pending()
+
+    def _raise_pending(self):
+        if self._errors:
+            (fn, e), self._errors = self._errors[0], []
+            raise RuntimeError(f"could not write {fn}: {e}") from e
 
 
 _default = VTIWriter()
@@ -166,6 +178,7 @@ def write_to_vti(domain, vectors, filename="out.vti", scale=1.0, wait=False):
     t = _default.write(domain, vectors, filename, scale)
     if wait:
         t.join()
+        _default._raise_pending()
     return t
 
 

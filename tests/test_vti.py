@@ -88,3 +88,14 @@ def test_vti_from_device_tensors(tmp_path):
             d.write_to_vti(dv, filename=str(tmp_path / f"{name}.vti"), scale=scale, wait=False)
             vti.flush()
         assert (tmp_path / f"{name}.vti").read_bytes() == _golden(name)
+
+
+def test_vti_write_errors_are_reported(tmp_path):
+    d = VoxelDomain(3, 2)
+    w = vti.VTIWriter()
+    w.write(d, {"x": np.zeros(d.nel)}, str(tmp_path / "missing_dir" / "a.vti"))
+    with pytest.raises(RuntimeError):
+        w.flush()
+    w.write(d, {"x": np.zeros(d.nel)}, str(tmp_path / "ok.vti"))
+    w.flush()
+    assert (tmp_path / "ok.vti").exists()
