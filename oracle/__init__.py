@@ -11,6 +11,9 @@ Only the test-suite, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--
 of ``bench.py`` may import it, and only as the checker or the timed CPU baseline.  The product path
 (``pymoto_gb300``) never imports it and fails loudly when its CUDA library is missing.
 
+Further restatements in their own modules: ``oracle.mma`` (MMA / subsolv, pymoto/common/mma.py) and
+``oracle.overhang`` (the overhang filter's layer sweep, pymoto/modules/filter.py:381-713).
+
 Parity pin: the oracle is checked against golden vectors written by running pyMOTO itself
 (``tests/golden/make_golden.py``) and against pyMOTO's own known-answer tests (analytical bar in
 tension, prolongation row sums, filter stencil placement).
