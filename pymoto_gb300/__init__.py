@@ -22,6 +22,7 @@ from .autograd import ComplianceObjective
 from .vti import WriteToVTI
 from .scalars import ScalarToFile
 from .overhang import OverhangFilter
+from .checkpoint import load_checkpoint, save_checkpoint
 from .routines import finite_difference, minimize_mma, minimize_oc
 
 __version__ = "0.1.0"
@@ -31,4 +32,5 @@ __all__ = ["AssembleMass", "AssemblePoisson", "AssembleStiffness", "DensityFilte
            "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
            "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI", "Scaling",
            "MMA", "ScalarToFile", "finite_difference",
-           "minimize_oc", "minimize_mma", "OverhangFilter"]
+           "minimize_oc", "minimize_mma", "OverhangFilter",
+           "save_checkpoint", "load_checkpoint"]

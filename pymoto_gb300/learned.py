@@ -185,6 +185,15 @@ class ConvNet3D:
         self._wgrad("enc1a", g1, self.feat, self.d_a1)
         return self.grad
 
+    def state_dict(self):
+        """FP32 master weights, their BF16 copy, Adam moments and step (checkpoint)."""
+        return {"w": self.w, "w_bf": self.w_bf, "m": self.m, "v": self.v, "step_count": self.step_count}
+
+    def load_state_dict(self, sd):
+        for k in ("w", "w_bf", "m", "v"):
+            getattr(self, k).copy_(sd[k].to(getattr(self, k).device))
+        self.step_count = int(sd["step_count"])
+
     def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0):
         self.step_count += 1
         call("pmg_nn_adam", self.nparam, self.w, self.grad, self.m, self.v, self.w_bf, lr, beta1, beta2, eps,
@@ -245,6 +254,20 @@ class LearnedWarmStart:
             g = (nx // s, ny // s, nz // s)
             self._levels.append((g, torch.zeros((g[0] + 1) * (g[1] + 1) * (g[2] + 1) * 3, **f64)))
         self.last_loss = None
+
+    def state_dict(self):
+        """Network, training buffer, sample count, random state, gate and history (checkpoint)."""
+        return {"net": self.net.state_dict(), "feats": self.feats, "targets": self.targets, "count": self.count,
+                "rng": self.rng.bit_generator.state, "skip": self._skip, "predictions": self.predictions,
+                "hist": list(self._hist)}
+
+    def load_state_dict(self, sd):
+        self.net.load_state_dict(sd["net"])
+        self.feats.copy_(sd["feats"].to(self.feats.device))
+        self.targets.copy_(sd["targets"].to(self.targets.device))
+        self.count, self._skip, self.predictions = int(sd["count"]), int(sd["skip"]), int(sd["predictions"])
+        self.rng.bit_generator.state = sd["rng"]
+        self._hist = [h.to(self.targets.device) for h in sd["hist"]]
 
     @property
     def ready(self):

@@ -85,6 +85,16 @@ class MMAUpdate:
         self._zero_row = None
         self._minus_one = torch.tensor([-1.0], dtype=torch.float64, device=self.device)
 
+    def state_dict(self):
+        """Asymptote offsets and the two previous designs (checkpoint)."""
+        return {"offset": self.offset, "xold1": self.xold1, "xold2": self.xold2}
+
+    def load_state_dict(self, sd):
+        self._check()
+        self.offset.copy_(sd["offset"].to(self.offset.device))
+        self.xold1 = None if sd["xold1"] is None else sd["xold1"].to(self.device)
+        self.xold2 = None if sd["xold2"] is None else sd["xold2"].to(self.device)
+
     def adapt_ready(self):
         return self.xold1 is not None and self.xold2 is not None
 
@@ -206,6 +216,16 @@ class MMA:
         self.rho = None
         self.gest = None
         self.dk = None
+
+    def state_dict(self):
+        """Iteration count, the update's state and GCMMA's rho (checkpoint)."""
+        rho = self.rho.tolist() if isinstance(self.rho, np.ndarray) else self.rho
+        return {"iter": self.iter, "core": self.core.state_dict(), "rho": rho}
+
+    def load_state_dict(self, sd):
+        self.iter = int(sd["iter"])
+        self.core.load_state_dict(sd["core"])
+        self.rho = np.asarray(sd["rho"], dtype=float) if isinstance(sd["rho"], list) else sd["rho"]
 
     # --- pyMOTO Optimizer protocol ---------------------------------------------------------------------
     def _parse_bound(self, xbnd, which="bounds"):

@@ -605,6 +605,13 @@ class LinSolve(Module):
     def lda_tol(self):
         return 5.0 * self.solver.tol if hasattr(self.solver, "tol") else 1e-7
 
+    def state_dict(self):
+        """The previous solution, the warm start of the next solve (checkpoint)."""
+        return {"u": self.u}
+
+    def load_state_dict(self, sd):
+        self.u = sd["u"]
+
     def _split(self, A, rhs):
         """(direct part on Dirichlet dofs, rhs with those dofs zeroed)."""
         direct = torch.empty_like(rhs)

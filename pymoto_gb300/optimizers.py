@@ -31,6 +31,13 @@ class OC:
         self.iter = 0
         self.history = []
 
+    def state_dict(self):
+        """Iteration count, response history and the volume target (checkpoint)."""
+        return {"iter": self.iter, "history": list(self.history), "maxvol": self.maxvol}
+
+    def load_state_dict(self, sd):
+        self.iter, self.history, self.maxvol = int(sd["iter"]), list(sd["history"]), sd["maxvol"]
+
     def _x(self):
         return _to_device(self.variable.state)
 
