@@ -714,7 +714,7 @@ class CG(LinearSolver):
         it, res = pcg(A, b, self.preconditioner.solve, x, self.tol, self.maxit, self.restart)
         _check_coarsest(self.preconditioner)
         self.iterations, self.last_residual = it, res
-        if res > self.tol:
+        if not res <= self.tol:   # also a non-finite residual (NaN / Inf in the data)
             warnings.warn(f"CG Maximum iterations ({self.maxit}) reached, with final residuals {res}")
         elif self.verbosity >= 1:
             print(f"CG Converged in {it} iterations and {np.round(time.perf_counter() - t0, 3)}s, "
@@ -1073,7 +1073,7 @@ class MixedPrecisionCG(LinearSolver):
         self.final_residual = r if trans == "N" else None
         if self.warm_start is not None and trans == "N" and math.isfinite(res):
             self.warm_start.observe(A, x)
-        if res > self.tol:
+        if not res <= self.tol:   # also a non-finite residual (NaN / Inf in the data)
             warnings.warn(f"MixedPrecisionCG did not reach tol {self.tol}: residual {res}")
         out = x.clone()
         return _from_device(out, kind)
