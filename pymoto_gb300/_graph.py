@@ -7,12 +7,19 @@ Used when pyMOTO itself is not importable.  It follows the semantics of pymoto/c
     so that calling a module with Signals connects it, creates its output Signals and appends it to every
     active Network (:481-548).  Keyword-only arguments are rejected (:408-448).
   * Network runs response() in order and sensitivity() in reverse (:750-829); `with Network() as fn:`
-    activates it; a default global network is always active (:998).
+    activates it; a default global network is always active (:998).  print_timing prints the host time of
+    each module (:790-829); PYMOTO_GB300_NVTX=1 adds an NVTX range per module response and sensitivity.
 """
 import copy
 import inspect
+import os
 import sys
 import time
+
+# PYMOTO_GB300_NVTX=1: NVTX ranges around every module's response and sensitivity (for Nsight Systems)
+_NVTX = os.environ.get("PYMOTO_GB300_NVTX", "0") == "1"
+if _NVTX:
+    import torch
 
 
 def _as_list(x):
@@ -212,6 +219,16 @@ class Network(Module):
             return ml[-1].sig_out[0] if len(ml[-1].sig_out) == 1 else ml[-1].sig_out
 
     def _run(self, fn, label):
+        if _NVTX:   # a named range per module response / sensitivity for Nsight timelines
+            torch.cuda.nvtx.range_push(label.strip("- "))
+            try:
+                self._timed(fn, label)
+            finally:
+                torch.cuda.nvtx.range_pop()
+            return
+        self._timed(fn, label)
+
+    def _timed(self, fn, label):
         if self.print_timing is False:
             fn()
             return
