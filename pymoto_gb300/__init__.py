@@ -20,7 +20,7 @@ from .solvers import (CG, Chebyshev, DampedJacobi, DenseCholesky, GeometricMulti
                       MixedPrecisionCG, Preconditioner)
 from .autograd import ComplianceObjective
 from .vti import WriteToVTI
-from .scalars import ScalarToFile
+from .scalars import DesignLog, ScalarToFile
 from .overhang import OverhangFilter
 from .checkpoint import load_checkpoint, save_checkpoint
 from .routines import finite_difference, minimize_mma, minimize_oc
@@ -33,4 +33,4 @@ __all__ = ["AssembleMass", "AssemblePoisson", "AssembleStiffness", "DensityFilte
            "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI", "Scaling",
            "MMA", "ScalarToFile", "finite_difference",
            "minimize_oc", "minimize_mma", "OverhangFilter",
-           "save_checkpoint", "load_checkpoint"]
+           "save_checkpoint", "load_checkpoint", "DesignLog"]

@@ -115,3 +115,82 @@ class ScalarToFile(Module):
         """Wait until every row queued so far is in the file."""
         self._jobs.join()
         self._raise_pending()
+
+
+class DesignLog:
+    """One JSON line per design iteration (metrics of a run): record() takes the current values of the given
+    signals (device scalars copied to pinned memory in stream order, like ScalarToFile), the solver's iteration
+    counts, residual and fallback flag, the learned warm start's predictions, the optimizer's iteration and the
+    host time since the previous record, plus any extra keyword values.  A background thread writes the lines."""
+
+    def __init__(self, path, solver=None, optimizer=None, **signals):
+        import time
+        self._time = time.perf_counter
+        self.path = path
+        Path(path).parent.mkdir(parents=True, exist_ok=True)
+        open(path, "w").close()
+        self.solver, self.optimizer, self.signals = solver, optimizer, signals
+        self._t0 = self._time()
+        self._jobs = queue.Queue()
+        self._error = None
+        threading.Thread(target=self._write_loop, daemon=True).start()
+        atexit.register(self.flush)
+
+    def _solver_fields(self):
+        s = self.solver
+        if s is None:
+            return {}
+        out = {k: getattr(s, k) for k in ("iterations", "last_residual", "inner_iterations", "fell_back")
+               if hasattr(s, k)}
+        ws = getattr(s, "warm_start", None)
+        if ws is not None:
+            out["learned_predictions"] = getattr(ws, "predictions", None)
+        return {k: (v if isinstance(v, (bool, int, float, type(None))) else float(v)) for k, v in out.items()}
+
+    def record(self, **extra):
+        if self._error is not None:
+            e, self._error = self._error, None
+            raise RuntimeError(f"DesignLog could not write {self.path}: {e}") from e
+        now = self._time()
+        row = {"time_s": now - self._t0}
+        self._t0 = now
+        if self.optimizer is not None:
+            row["iteration"] = getattr(self.optimizer, "iter", None)
+        row.update(self._solver_fields())
+        row.update(extra)
+        staged, event = {}, None
+        for name, sig in self.signals.items():
+            st = getattr(sig, "state", sig)
+            if isinstance(st, torch.Tensor) and st.is_cuda:
+                h = torch.empty(st.shape, dtype=st.dtype, pin_memory=True)
+                h.copy_(st.detach(), non_blocking=True)
+                staged[name] = h
+                event = event or torch.cuda.Event()
+            else:
+                staged[name] = st.detach().clone() if isinstance(st, torch.Tensor) else np.array(st, copy=True)
+        if event is not None:
+            event.record()
+        self._jobs.put((row, staged, event))
+
+    def _write_loop(self):
+        import json
+        while True:
+            row, staged, event = self._jobs.get()
+            try:
+                if event is not None:
+                    event.synchronize()
+                for name, v in staged.items():
+                    a = v.numpy() if isinstance(v, torch.Tensor) else v
+                    row[name] = a.reshape(-1)[0].item() if a.size == 1 else a.reshape(-1).tolist()
+                with open(self.path, "a") as f:
+                    f.write(json.dumps(row) + "\n")
+            except Exception as e:   # reported by the next record() or flush()
+                self._error = e
+            finally:
+                self._jobs.task_done()
+
+    def flush(self):
+        self._jobs.join()
+        if self._error is not None:
+            e, self._error = self._error, None
+            raise RuntimeError(f"DesignLog could not write {self.path}: {e}") from e

@@ -8,6 +8,7 @@ import torch
 
 from conftest import GOLDEN
 
+import pymoto_gb300 as pg
 from pymoto_gb300 import Network, ScalarToFile, Signal
 
 
@@ -69,3 +70,22 @@ def test_log_from_device_scalars(tmp_path):
             return torch.as_tensor(v).cuda()
         return v
     assert _run(tmp_path, fname, fmt, sep, its, conv) == _golden(fname)
+
+
+def test_design_log_writes_one_json_line_per_record(tmp_path):
+    import json
+    import types
+    solver = types.SimpleNamespace(iterations=7, last_residual=np.float64(3e-7), fell_back=False,
+                                   warm_start=types.SimpleNamespace(predictions=2))
+    opt = types.SimpleNamespace(iter=0)
+    sc, sv = Signal("c", 12.5), Signal("v", np.array([0.25, 0.5]))
+    log = pg.DesignLog(str(tmp_path / "run" / "log.jsonl"), solver=solver, optimizer=opt, compliance=sc, vol=sv)
+    for k in range(3):
+        opt.iter, sc.state = k, 12.5 - k
+        log.record(note="x" * k)
+    log.flush()
+    rows = [json.loads(line) for line in open(tmp_path / "run" / "log.jsonl")]
+    assert [r["iteration"] for r in rows] == [0, 1, 2] and [r["compliance"] for r in rows] == [12.5, 11.5, 10.5]
+    assert rows[0]["vol"] == [0.25, 0.5] and rows[2]["note"] == "xx"
+    assert rows[0]["iterations"] == 7 and rows[0]["last_residual"] == 3e-7 and rows[0]["learned_predictions"] == 2
+    assert rows[0]["fell_back"] is False and all(r["time_s"] >= 0 for r in rows)
