@@ -806,3 +806,10 @@ class Scaling(Module):
 
     def reset_scaling(self):
         self.sf = self.scaling if (self.minval is not None or self.maxval is not None) else None
+
+    def state_dict(self):
+        """The scaling factor, fixed by the first response in the objective form (checkpoint)."""
+        return {"sf": self.sf}
+
+    def load_state_dict(self, sd):
+        self.sf = sd["sf"]

@@ -94,3 +94,42 @@ def test_learned_warm_start_state_round_trip(tmp_path):
     load_checkpoint(tmp_path / "l.npz", ws=b)
     assert torch.equal(a.net.w, b.net.w) and torch.equal(a.net.w_bf, b.net.w_bf)
     assert a.rng.random() == b.rng.random()
+
+
+@pytest.mark.gpu
+def test_resumed_mma_run_reproduces_the_uninterrupted_run(tmp_path, golden):
+    """MMA keeps asymptote offsets and the two previous designs; a resumed run continues bit for bit."""
+    g = golden("mma_mbb.npz")
+
+    def build():
+        d = pg.VoxelDomain(30, 10)
+        f = torch.from_numpy(g["v2007_f"]).cuda()
+        sx = pg.Signal("x", torch.full((d.nel,), 0.5, dtype=torch.float64, device="cuda"))
+        with pg.Network() as fn:
+            xf = pg.DensityFilter(d, radius=1.5)(sx)
+            xs = pg.SIMP(xmin=1e-9, penal=3.0)(xf)
+            K = pg.AssembleStiffness(d, bc=g["v2007_bc"], plane="stress")(xs)
+            ls = pg.LinSolve(hermitian=True, symmetric=True)
+            u = ls(K, f)
+            c = pg.EinSum("i,i->")(u, f)
+            s0 = pg.Scaling(scaling=100.0)
+            g0 = s0(c)
+            g1 = pg.Scaling(scaling=5.0, maxval=0.5 * d.nel)(pg.EinSum("i->")(xf))
+        return sx, ls, s0, pg.MMA(sx, [g0, g1], fn, move=0.2, verbosity=0)
+
+    sx, ls, s0, mma = build()
+    xval = mma.x
+    for _ in range(3):
+        xval, _, _ = mma.step(x=xval)
+    mma.x = xval
+    save_checkpoint(tmp_path / "mma.npz", x=sx, mma=mma, solve=ls, scale=s0)
+    ref = []
+    for _ in range(2):
+        xval, gk, _ = mma.step(x=xval)
+        ref.append(gk.cpu().numpy())
+    sx2, ls2, s02, mma2 = build()
+    load_checkpoint(tmp_path / "mma.npz", x=sx2, mma=mma2, solve=ls2, scale=s02)
+    xval = mma2.x
+    for k in range(2):
+        xval, gk, _ = mma2.step(x=xval)
+        np.testing.assert_array_equal(gk.cpu().numpy(), ref[k])
