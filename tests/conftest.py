@@ -28,3 +28,17 @@ def clamp_face_dofs(grid):
     """Dirichlet dofs of the i = 0 face (all components), the cantilever support used in the fixtures."""
     nodes = grid.nodes_where(i=0)
     return (nodes[:, None] * grid.dim + np.arange(grid.dim)).ravel()
+
+
+# The hot path's parity files (and MMA, VTI) run first, the other next rows and the auxiliary subsystems after
+# them, so that with -x a failure in one of the later rows does not hide the hot path's results;
+# test_zz_no_alloc stays last.
+_LATER = ("test_filter_variants", "test_mass", "test_poisson", "test_overhang", "test_math_expression",
+          "test_scalars", "test_routines", "test_design_runs", "test_checkpoint", "test_faults", "test_zz_no_alloc")
+
+
+def pytest_collection_modifyitems(session, config, items):
+    def rank(item):
+        mod = item.module.__name__.rsplit(".", 1)[-1] if item.module is not None else ""
+        return _LATER.index(mod) + 1 if mod in _LATER else 0
+    items[:] = sorted(items, key=rank)     # stable: the order within a file is kept

@@ -68,3 +68,15 @@ def test_duplicate_names_are_rejected():
 def test_device_states_match_pymoto(case, golden):
     y, ds = _run(case, lambda v: torch.as_tensor(np.asarray(v, dtype=np.float64)).cuda())
     _check(case, y, ds, golden)
+
+
+@pytest.mark.parametrize("text,xmin,penal", [("1e-9 + (1-1e-9)*inp0^3", 1e-9, 3.0),
+                                             ("0.001+(1-0.001)*inp0**3.5", 1e-3, 3.5)])
+def test_simp_form_selects_the_simp_kernels(text, xmin, penal):
+    m = pg.MathExpression(text)
+    assert m._simp is not None and (m.xmin, m.penal) == (xmin, penal)
+
+
+@pytest.mark.parametrize("text", ["1e-9 + (1-1e-3)*inp0^3", "inp0^3", "1e-9 + (1-1e-9)*inp0^3 + inp1"])
+def test_other_expressions_are_not_taken_for_simp(text):
+    assert pg.MathExpression(text)._simp is None
