@@ -160,3 +160,55 @@ def test_binding_signatures_match_the_header():
         if want is not res:
             bad.append(f"{name} returns {ret} vs {getattr(res, '__name__', res)}")
     assert not bad, bad
+
+
+def test_mma_and_overhang_arguments_are_checked_before_any_launch():
+    """pmg_mma_update and pmg_overhang_* reject bad options before any launch (host buffers stand in for the
+    device arrays: every case below returns at the option checks)."""
+    import ctypes as C
+    from pymoto_gb300._lib import PMGError, call
+    from pymoto_gb300.mma import _Params
+    n, m = 8, 1
+    assert call("pmg_mma_scratch_bytes", 0, 1) == 0 and call("pmg_mma_scratch_bytes", n, 5) == 0
+    s1, s2 = call("pmg_mma_scratch_bytes", n, 1), call("pmg_mma_scratch_bytes", 2 * n, 1)
+    assert s2 - s1 == (12 + 2 * (m + 1) + m) * n * 8
+    assert call("pmg_mma_scratch_bytes", n, 2) - s1 == 3 * n * 8
+    buf = [np.zeros(64) for _ in range(14)]
+    x, x1, x2, lo, hi, mv, g, dg, off, low, upp, xn, info, scr = buf
+
+    def good():
+        p = _Params()
+        p.version, p.m, p.adapt, p.maxit, p.exact = 1, m, 0, 100, 0
+        p.epsimin = 1e-7
+        return p
+
+    def update(p, **kw):
+        args = dict(xval=x, xold1=x1, xold2=x2, xnew=xn)
+        args.update(kw)
+        return call("pmg_mma_update", n, C.byref(p), args["xval"], args["xold1"], args["xold2"], lo, hi, mv, g, dg,
+                    off, low, upp, args["xnew"], info, scr, None)
+
+    bad = []
+    for field, value in (("m", 0), ("m", 5), ("maxit", 0), ("exact", 2), ("version", 3), ("epsimin", 0.0)):
+        p = good()
+        setattr(p, field, value)
+        bad.append((p, {}))
+    p = good()
+    p.adapt = 1
+    bad.append((p, {"xold1": None}))
+    bad.append((good(), {"xnew": x}))                 # output aliases the design
+    for p, kw in bad:
+        with pytest.raises(PMGError) as e:
+            update(p, **kw)
+        assert e.value.status == 1
+    # overhang: nx ny nz lay step layer w0 w1 w2 c0 c1 c2 K kern p q shift backshift eps x y s stream
+    ok = [4, 4, 4, 1, 1, 0, 3, 1, 3, 1, 1, 1, 1]
+    for i, v in ((3, 3), (4, 2), (5, 4), (6, 2), (7, 3), (8, 5), (10, -1), (12, 0)):
+        a = list(ok)
+        a[i] = v
+        with pytest.raises(PMGError):
+            call("pmg_overhang_forward", *a, buf[0], 40.0, 1.0, 0.5, 0.5, 1e-3, buf[1], buf[2], buf[3], None)
+    with pytest.raises(PMGError):   # q must be positive
+        call("pmg_overhang_forward", *ok, buf[0], 40.0, 0.0, 0.5, 0.5, 1e-3, buf[1], buf[2], buf[3], None)
+    with pytest.raises(PMGError):   # output aliases the input
+        call("pmg_overhang_forward", *ok, buf[0], 40.0, 1.0, 0.5, 0.5, 1e-3, buf[1], buf[1], buf[3], None)
