@@ -126,11 +126,14 @@ class FilterConv(Module):
         self.pad_sizes = [s // 2 for s in self.weights.shape]
         self._maps_host = [_pad_map(n, p, bcs[2 * a], bcs[2 * a + 1]) for a, (n, p) in
                            enumerate(zip(sizes, self.pad_sizes))]
+        self._bcs, self._sizes = bcs, sizes
         self._const_host = self._constant_field(bcs, sizes)
         self._dev = None
         self._overrides = {}      # element -> fixed input value (override_values)
         self._fzero = None        # the same kernel with zero padding on every side
         self._ov_dev = None
+        self._padded = {}         # flat position in the padding ring -> fixed value (override_padded_values)
+        self._pad_dev = None
 
     def override_values(self, index, value):
         """Fixed input `value` at the elements that `index` selects in the (nelx, nely, nelz) element array
@@ -139,14 +142,126 @@ class FilterConv(Module):
         (pyMOTO zeroes the overridden positions in the adjoint)."""
         g = self.grid
         nz = max(g.nelz, 1)
-        el = np.arange(g.nel).reshape(nz, g.nely, g.nelx).transpose(2, 1, 0)
-        for e in np.atleast_1d(el[index]).ravel():
-            self._overrides[int(e)] = float(value)
+        el = np.atleast_1d(np.arange(g.nel).reshape(nz, g.nely, g.nelx).transpose(2, 1, 0)[index])
+        self._set_overrides(el.ravel(), np.broadcast_to(np.asarray(value, dtype=np.float64), el.shape).ravel())
+
+    def _set_overrides(self, elements, values):
+        for e, v in zip(elements, values):
+            self._overrides[int(e)] = float(v)
         if self._fzero is None:
-            w = self.weights if g.nelz else self.weights[:, :, 0]
+            w = self.weights if self.grid.nelz else self.weights[:, :, 0]
             zero = dict(xmin_bc=0.0, xmax_bc=0.0, ymin_bc=0.0, ymax_bc=0.0, zmin_bc=0.0, zmax_bc=0.0)
             self._fzero = FilterConv(self.domain, weights=w, **zero)
         self._ov_dev = None
+
+    @property
+    def padded_shape(self):
+        return tuple(n + 2 * p for n, p in zip(self._sizes, self.pad_sizes))
+
+    @property
+    def padded_domain(self):
+        """The element grid of the padded input (pymoto/modules/filter.py:162-167)."""
+        from .domain import VoxelDomain
+        nx, ny, nz = (n + 2 * p for n, p in zip((self.grid.nelx, self.grid.nely, self.grid.nelz), self.pad_sizes))
+        d = self.domain
+        return VoxelDomain(nx, ny, nz, unitx=d.unitx, unity=d.unity, unitz=d.unitz)
+
+    def override_padded_values(self, index, value):
+        """Fixed input `value` at the positions `index` selects in the padded array (padded_shape; pymoto's
+        filter.py:169-173); later calls win.  Positions inside the domain act as override_values.  Positions in
+        the padding ring replace what the padding put there, a constant or a copy x[src]: the constant part
+        joins the fixed field, and each copy adds -w x[src] terms to the outputs within reach, applied as a
+        gather over the (few) affected outputs with its transpose for the adjoint (pyMOTO zeroes the overridden
+        positions in the adjoint)."""
+        if all(np.asarray(i).size == 0 for i in (index if isinstance(index, tuple) else (index,))):
+            return
+        ps = self.padded_shape
+        pos = np.atleast_1d(np.arange(int(np.prod(ps))).reshape(ps)[index])
+        vals = np.broadcast_to(np.asarray(value, dtype=np.float64), pos.shape).ravel()
+        pos = pos.ravel()
+        sub = np.unravel_index(pos, ps)
+        inside = np.ones(pos.size, dtype=bool)
+        for a in range(3):
+            inside &= (sub[a] >= self.pad_sizes[a]) & (sub[a] < self.pad_sizes[a] + self._sizes[a])
+        nx, ny = self._sizes[0], self._sizes[1]
+        el = ((sub[2] - self.pad_sizes[2]) * ny + (sub[1] - self.pad_sizes[1])) * nx + (sub[0] - self.pad_sizes[0])
+        for k in range(pos.size):   # in call order: the last value given for a position wins
+            if inside[k]:
+                self._set_overrides([el[k]], [vals[k]])
+                self._padded.pop(int(pos[k]), None)
+            else:
+                self._padded[int(pos[k])] = float(vals[k])
+        self._pad_dev = None
+        self._dev = None
+
+    def get_padded_vector(self, x):
+        """The padded input array that pyMOTO's FilterConv convolves (pymoto/modules/filter.py:183-187), of shape
+        padded_shape: padding, constant sides and overrides applied.  Numpy in, numpy out; a tensor stays on its
+        device.  For inspection: the filter itself never forms this array."""
+        ps, pads = self.padded_shape, self.pad_sizes
+        nx, ny = self._sizes[0], self._sizes[1]
+        A, B, Cz = np.meshgrid(*self._maps_host, indexing="ij")
+        fixed = (A < 0) | (B < 0) | (Cz < 0)
+        src = np.where(fixed, 0, (Cz.astype(np.int64) * ny + B) * nx + A)
+        val = self._constant_padded(self._bcs, self._sizes)
+        for e, v in self._overrides.items():
+            i, j, k = e % nx, (e // nx) % ny, e // (nx * ny)
+            fixed[i + pads[0], j + pads[1], k + pads[2]] = True
+            val[i + pads[0], j + pads[1], k + pads[2]] = v
+        for f, v in self._padded.items():
+            at = np.unravel_index(f, ps)
+            fixed[at], val[at] = True, v
+        if isinstance(x, torch.Tensor):
+            out = x.reshape(-1)[torch.from_numpy(src).to(x.device)]
+            m = torch.from_numpy(fixed).to(x.device)
+            out[m] = torch.from_numpy(val).to(device=x.device, dtype=x.dtype)[m]
+            return out
+        out = np.asarray(x).reshape(-1)[src]
+        out[fixed] = val[fixed]
+        return out
+
+    def _padded_override_host(self):
+        """(fixed field, rows, row table, columns, column table) of the padding-ring overrides."""
+        ps, pads, sizes = self.padded_shape, self.pad_sizes, self._sizes
+        kx, ky, kz = self.weights.shape
+        C = self._constant_padded(self._bcs, sizes)
+        mx, my, mz = self._maps_host
+        nx, ny, nz = sizes
+        D = np.zeros(ps)
+        terms = {}   # (output element, source element) -> coefficient
+        for f, v in self._padded.items():
+            a, b, c = np.unravel_index(f, ps)
+            src = (int(mx[a]), int(my[b]), int(mz[c]))
+            if min(src) < 0:
+                D[a, b, c] = v - C[a, b, c]
+                continue
+            D[a, b, c] = v
+            j = (src[2] * ny + src[1]) * nx + src[0]
+            for oz in range(max(0, c - (kz - 1)), min(nz - 1, c) + 1):
+                for oy in range(max(0, b - (ky - 1)), min(ny - 1, b) + 1):
+                    for ox in range(max(0, a - (kx - 1)), min(nx - 1, a) + 1):
+                        wv = self.weights[ox + kx - 1 - a, oy + ky - 1 - b, oz + kz - 1 - c]
+                        if wv != 0.0:
+                            o = (oz * ny + oy) * nx + ox
+                            terms[(o, j)] = terms.get((o, j), 0.0) - wv
+        fixed = self._valid_conv(D)
+
+        def table(pairs):
+            """Unique keys and, per key, its (index, coefficient) list padded with zero coefficients."""
+            if not pairs:
+                return np.zeros(0, dtype=np.int64), np.zeros((0, 1), dtype=np.int64), np.zeros((0, 1))
+            kq = np.array(sorted(pairs), dtype=np.int64)
+            cv = np.array([pairs[(int(r), int(q))] for r, q in kq])
+            keys, start, count = np.unique(kq[:, 0], return_index=True, return_counts=True)
+            slot = np.arange(kq.shape[0]) - np.repeat(start, count)
+            row = np.repeat(np.arange(keys.size), count)
+            idx = np.zeros((keys.size, int(count.max())), dtype=np.int64)
+            coef = np.zeros((keys.size, int(count.max())))
+            idx[row, slot], coef[row, slot] = kq[:, 1], cv
+            return keys, idx, coef
+        rows = table(terms)
+        cols = table({(j, o): cv for (o, j), cv in terms.items()})
+        return fixed, rows, cols
 
     def _override_data(self, device):
         if self._ov_dev is None or self._ov_dev[0].device != device:
@@ -156,11 +271,36 @@ class FilterConv(Module):
                             torch.ones(1, dtype=torch.float64, device=device))
         return self._ov_dev
 
+    @staticmethod
+    def _padded_terms(y, v, data, transpose):
+        """Add the padding-ring overrides' terms to y (in place): y += conv(value - pad(v)) over the overridden
+        positions, or for the adjoint the removal of their copies' contributions.  Every output row is written
+        once, by a fixed-order sum over its table row."""
+        fixed, rows, idx_r, coef_r, cols, idx_c, coef_c = data
+        if transpose:
+            if cols.numel():
+                y[cols] += (coef_c * v[idx_c]).sum(1)
+        else:
+            y += fixed
+            if rows.numel():
+                y[rows] += (coef_r * v[idx_r]).sum(1)
+        return y
+
+    def _padded_data(self, device):
+        if self._pad_dev is None or self._pad_dev[0].device != device:
+            fixed, rows, cols = self._padded_override_host()
+            self._pad_dev = tuple(torch.from_numpy(np.ascontiguousarray(t)).to(device) for t in (fixed, *rows, *cols))
+        return self._pad_dev
+
     def _constant_field(self, bcs, sizes):
         """conv(C) on the element grid (element numbering), C the padded field that holds the constant values on
         the padded slabs of constant sides and 0 elsewhere; None when no side has a nonzero constant."""
         if not any(_is_value(b) and float(b) != 0.0 for b in bcs):
             return None
+        return self._valid_conv(self._constant_padded(bcs, sizes))
+
+    def _constant_padded(self, bcs, sizes):
+        """The padded field C of the constant sides' values, 0 elsewhere."""
         pads = self.pad_sizes
         C = np.zeros([n + 2 * p for n, p in zip(sizes, pads)])
         for a in range(3):   # x, y, z; high side before low side, later overrides win (filter.py:123-160)
@@ -170,6 +310,11 @@ class FilterConv(Module):
                     sl = [slice(None)] * 3
                     sl[a] = rng
                     C[tuple(sl)] = float(bc)
+        return C
+
+    def _valid_conv(self, C):
+        """'valid' convolution of a padded field with the kernel, in element numbering (host, setup)."""
+        sizes = self._sizes
         kx, ky, kz = self.weights.shape
         y3 = np.zeros(sizes)
         for a in range(kx):   # 'valid' convolution: output o reads C[o + (k-1) - m]
@@ -230,6 +375,8 @@ class FilterConv(Module):
             if const is not None:   # y += conv(C): the constant-value sides
                 field, one = const
                 call("pmg_axpy_ratio", F64, g.nel, y, field, one, one, 1.0, stream())
+        if self._padded:
+            self._padded_terms(y, vd, self._padded_data(vd.device), transpose)
         if self._overrides:
             idx, val, one = self._override_data(vd.device)
             if transpose:             # dx[S] -= (F0^T d)[S]

@@ -266,6 +266,29 @@ def filter_variants(pym):
         sy = fc(pym.Signal("x", x))
         out.update({f"{tag}_shape": np.array(shp), f"{tag}_r": np.array(r), f"{tag}_x": x, f"{tag}_dy": dy,
                     f"{tag}_y": sy.state, f"{tag}_dx": fc._sensitivity(dy)})
+    # fixed values in the padded array (override_padded_values): constant sides (the padding-filter example's
+    # use), copies made by symmetric / edge / wrap padding, positions inside the domain, array values; later
+    # calls win
+    ring = [("po3", (8, 6, 5), 2.5, dict(xmin_bc=0, xmax_bc="symmetric", ymin_bc=0, ymax_bc=0, zmin_bc=0, zmax_bc=0),
+             [(tuple(np.meshgrid(np.arange(2), 2 + np.arange(2, 4), 2 + np.arange(1, 4))), 1.0),
+              ((slice(10, 12), slice(3, 6), slice(2, 5)), 0.3),
+              ((np.array([3, 4]), np.array([4, 4]), np.array([3, 3])), 0.9),
+              ((slice(0, 1), slice(4, 5), slice(3, 4)), 0.2)]),
+            ("po2", (9, 7), 2.0, dict(xmin_bc="wrap", xmax_bc="wrap", ymin_bc="edge", ymax_bc=0.25),
+             [((slice(0, 2), slice(0, 2), 0), 0.6),
+              ((slice(None), 8, 0), 1.0),
+              ((np.array([10, 5]), np.array([3, 0]), np.array([0, 0])), np.array([0.4, 0.7]))])]
+    for tag, shp, r, bcs, povs in ring:
+        d = pym.VoxelDomain(*shp)
+        rng = np.random.default_rng(19)
+        x = rng.uniform(0.0, 1.0, d.nel)
+        dy = rng.standard_normal(d.nel)
+        fc = pym.FilterConv(d, radius=r, **bcs)
+        for idx, val in povs:
+            fc.override_padded_values(idx, val)
+        sy = fc(pym.Signal("x", x))
+        out.update({f"{tag}_shape": np.array(shp), f"{tag}_r": np.array(r), f"{tag}_x": x, f"{tag}_dy": dy,
+                    f"{tag}_y": sy.state, f"{tag}_dx": fc._sensitivity(dy), f"{tag}_xpad": fc.get_padded_vector(x)})
     for tag, shp, r in [("np2", (10, 6), 1.5), ("np3", (6, 5, 4), 2.0)]:
         d = pym.VoxelDomain(*shp)
         rng = np.random.default_rng(12)

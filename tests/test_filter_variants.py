@@ -154,3 +154,67 @@ def test_density_filter_nonpadding_on_device(tag, golden):
     np.testing.assert_allclose(df(x).cpu().numpy(), g[f"{tag}_y"], rtol=1e-13, atol=1e-15)
     dy = torch.from_numpy(g[f"{tag}_dy"]).cuda()
     np.testing.assert_allclose(df._sensitivity(dy).cpu().numpy(), g[f"{tag}_dx"], rtol=1e-13, atol=1e-15)
+
+
+PADDED = {"po3": (dict(xmin_bc=0, xmax_bc="symmetric", ymin_bc=0, ymax_bc=0, zmin_bc=0, zmax_bc=0),
+                  [(tuple(np.meshgrid(np.arange(2), 2 + np.arange(2, 4), 2 + np.arange(1, 4))), 1.0),
+                   ((slice(10, 12), slice(3, 6), slice(2, 5)), 0.3),
+                   ((np.array([3, 4]), np.array([4, 4]), np.array([3, 3])), 0.9),
+                   ((slice(0, 1), slice(4, 5), slice(3, 4)), 0.2)]),
+          "po2": (dict(xmin_bc="wrap", xmax_bc="wrap", ymin_bc="edge", ymax_bc=0.25),
+                  [((slice(0, 2), slice(0, 2), 0), 0.6),
+                   ((slice(None), 8, 0), 1.0),
+                   ((np.array([10, 5]), np.array([3, 0]), np.array([0, 0])), np.array([0.4, 0.7]))])}
+
+
+def _padded_filter(tag, golden):
+    import pymoto_gb300 as pg
+    g = golden("filter_variants.npz")
+    d = pg.VoxelDomain(*[int(v) for v in g[f"{tag}_shape"]])
+    bcs, povs = PADDED[tag]
+    fc = pg.FilterConv(d, radius=float(g[f"{tag}_r"]), **bcs)
+    for idx, val in povs:
+        fc.override_padded_values(idx, val)
+    return fc, g
+
+
+@pytest.mark.parametrize("tag", list(PADDED))
+def test_padded_overrides_host_side_matches_pymoto(tag, golden):
+    """Kernel emulation + the ring terms (the module's own torch helper on CPU tensors) + the in-domain
+    overrides reproduce pyMOTO's FilterConv with override_padded_values, forward and adjoint."""
+    fc, g = _padded_filter(tag, golden)
+    assert fc._padded and fc._overrides      # both kinds of position are exercised
+    x, dy = g[f"{tag}_x"], g[f"{tag}_dy"]
+    y, dx = _emulate(fc, x, dy)
+    data = fc._padded_data(torch.device("cpu"))
+    y = fc._padded_terms(torch.from_numpy(y), torch.from_numpy(x), data, False).numpy()
+    dx = fc._padded_terms(torch.from_numpy(dx), torch.from_numpy(dy), data, True).numpy()
+    S = np.array(sorted(fc._overrides))
+    v = np.array([fc._overrides[i] for i in S])
+    d = np.zeros_like(x)
+    d[S] = v - x[S]
+    y0, t0 = _emulate(fc._fzero, d, dy)
+    dx[S] -= t0[S]
+    np.testing.assert_allclose(y + y0, g[f"{tag}_y"], rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(dx, g[f"{tag}_dx"], rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("tag", list(PADDED))
+def test_padded_vector_and_domain_match_pymoto(tag, golden):
+    fc, g = _padded_filter(tag, golden)
+    np.testing.assert_array_equal(fc.get_padded_vector(g[f"{tag}_x"]), g[f"{tag}_xpad"])
+    t = fc.get_padded_vector(torch.from_numpy(g[f"{tag}_x"]))
+    np.testing.assert_array_equal(t.numpy(), g[f"{tag}_xpad"])
+    pd = fc.padded_domain
+    shape = g[f"{tag}_xpad"].shape
+    assert (pd.nelx, pd.nely, max(pd.nelz, 1)) == shape
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", list(PADDED))
+def test_padded_overrides_on_device(tag, golden):
+    fc, g = _padded_filter(tag, golden)
+    y = fc(torch.from_numpy(g[f"{tag}_x"]).cuda())
+    np.testing.assert_allclose(y.cpu().numpy(), g[f"{tag}_y"], rtol=1e-13, atol=1e-15)
+    dx = fc._sensitivity(torch.from_numpy(g[f"{tag}_dy"]).cuda())
+    np.testing.assert_allclose(dx.cpu().numpy(), g[f"{tag}_dx"], rtol=1e-13, atol=1e-15)
