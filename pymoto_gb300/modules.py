@@ -861,18 +861,63 @@ class LinSolve(Module):
 
 # --------------------------------------------------------------------------------------------- EinSum
 class EinSum(Module):
-    """The contractions of pyMOTO's EinSum (pymoto/modules/generic.py:143-226) used on the compliance path:
-    'i,i->' (c = f.u) and 'i->' (sum, e.g. the volume), FP64 on the device."""
+    """pyMOTO's EinSum (pymoto/modules/generic.py:143-226).  The contractions of the compliance path, 'i,i->'
+    (c = f.u) and 'i->' (sum, e.g. the volume), run in the FP64 dot kernel; any other expression is evaluated
+    by torch.einsum for tensor states (on their device) or numpy.einsum for numpy states, with pyMOTO's adjoint
+    expressions for the sensitivities (repeated indices only in the one-input scalar form, as pyMOTO)."""
 
-    _SUPPORTED = {"i,i->", "i->"}
+    _KERNEL = {"i,i->", "i->"}
 
     def __init__(self, expression):
+        self.expression = expression
         expr = expression.replace(" ", "")
-        if expr not in self._SUPPORTED:
-            raise NotImplementedError(f"EinSum({expression!r}) is not supported on the GPU path")
         self.expr = expr
+        cmd = expr.split("->")
+        self.indices_in = cmd[0].split(",")
+        self.indices_out = cmd[1] if "->" in expr else ""
+        self._general = expr not in self._KERNEL
+
+    def _einsum(self, spec, *ops):
+        if self._torch:
+            return torch.einsum(spec, *ops)
+        return np.einsum(spec, *ops, optimize=True)
+
+    def _general_call(self, *args):
+        self._torch = any(isinstance(a, torch.Tensor) for a in args)
+        if self._torch:
+            dev = next(a.device for a in args if isinstance(a, torch.Tensor))
+            args = [a if isinstance(a, torch.Tensor) else torch.as_tensor(np.asarray(a), device=dev) for a in args]
+        self._args = args
+        return self._einsum(self.expr, *args)
+
+    def _general_sensitivity(self, df):
+        inps = self._args
+        if self._torch and not isinstance(df, torch.Tensor):
+            df = torch.as_tensor(np.asarray(df), device=inps[0].device, dtype=inps[0].dtype)
+        if self.indices_out == "" and len(inps) == 1:
+            ind = self.indices_in[0]
+            if len(set(ind)) < len(ind):    # repeated indices (trace)
+                if inps[0].ndim > 2:
+                    raise NotImplementedError(f"Sensitivities for repeated incides in '{self.expr}' not supported.")
+                mat = (torch.eye(*inps[0].shape, dtype=inps[0].dtype, device=inps[0].device) if self._torch
+                       else np.eye(*inps[0].shape, dtype=inps[0].dtype))
+            else:
+                mat = torch.ones_like(inps[0]) if self._torch else np.ones_like(inps[0])
+            return df * mat
+        for ind in self.indices_in:
+            if len(set(ind)) < len(ind):
+                raise NotImplementedError(f"Sensitivities for repeated incides in '{self.expr}' not supported.")
+        out = []
+        for k in range(len(inps)):
+            spec = ",".join([self.indices_out] + [s for i, s in enumerate(self.indices_in) if i != k])
+            d = self._einsum(spec + "->" + self.indices_in[k], df, *[v for i, v in enumerate(inps) if i != k])
+            complex_in = inps[k].is_complex() if self._torch else np.iscomplexobj(inps[k])
+            out.append(d.real if not complex_in and (d.is_complex() if self._torch else np.iscomplexobj(d)) else d)
+        return out
 
     def __call__(self, *args):
+        if self._general:
+            return self._general_call(*args)
         devs = [_to_device(a) for a in args]
         self._in = devs
         ws = Workspace.get(devs[0][0].device)
@@ -885,6 +930,8 @@ class EinSum(Module):
         return np.float64(out.item())
 
     def _sensitivity(self, df):
+        if self._general:
+            return self._general_sensitivity(df)
         df = float(df)
         if self.expr == "i->":
             (a, kind), = self._in

@@ -14,6 +14,7 @@ at module level for plotting only.  The fixtures are small .npz files; the tests
     python tests/golden/make_golden.py math     # the MathExpression cases only
     python tests/golden/make_golden.py overhang # the OverhangFilter cases only
     python tests/golden/make_golden.py poisson  # the AssemblePoisson cases only
+    python tests/golden/make_golden.py einsum   # the EinSum expressions only
 """
 import os
 import sys
@@ -230,6 +231,30 @@ def mma_mbb(pym):
             out[f"{tag}_{k}"] = np.array(v)
         out[f"{tag}_bc"], out[f"{tag}_f"] = bc, f
     save("mma_mbb.npz", **out)
+
+
+EINSUM_CASES = [("i,i->i", [(6,), (6,)]), ("i,j->ij", [(4,), (3,)]), ("ii->", [(5, 5)]), ("ij,j->i", [(4, 3), (3,)]),
+                ("i,ij,j->", [(4,), (4, 3), (3,)]), ("ij,ij->ij", [(3, 4), (3, 4)]), ("ji,ij->ij", [(4, 3), (3, 4)]),
+                ("ji,jk,kl->il", [(4, 2), (4, 3), (3, 2)]), ("ij->", [(3, 4)]), ("ijk,k->ij", [(2, 3, 4), (4,)])]
+
+
+def einsums(pym):
+    """pyMOTO's EinSum: responses and sensitivities (for a random output sensitivity) of the expressions in its
+    docstring table and a few more."""
+    out = {}
+    rng = np.random.default_rng(23)
+    for n, (expr, shapes) in enumerate(EINSUM_CASES):
+        args = [rng.standard_normal(sh) for sh in shapes]
+        m = pym.EinSum(expr)
+        sig = [pym.Signal(f"a{i}", a) for i, a in enumerate(args)]
+        y = m(*sig).state
+        dy = rng.standard_normal(np.shape(y)) if np.ndim(y) else rng.standard_normal()
+        ds = m._sensitivity(dy)
+        ds = ds if isinstance(ds, list) else [ds]
+        out[f"e{n}_y"], out[f"e{n}_dy"] = np.asarray(y), np.asarray(dy)
+        for i, (a, d) in enumerate(zip(args, ds)):
+            out[f"e{n}_a{i}"], out[f"e{n}_d{i}"] = a, np.asarray(d)
+    save("einsum.npz", **out)
 
 
 def filter_variants(pym):
@@ -508,3 +533,5 @@ if __name__ == "__main__":
         overhang(pym)
     if "all" in which or "poisson" in which:
         poisson(pym)
+    if "all" in which or "einsum" in which:
+        einsums(pym)
