@@ -193,10 +193,16 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the sampler is live before the timed region starts (nvidia-smi takes a moment to print its first
+            # line); the wait is bounded, a sampler that never prints leaves "samples": 0
+            t0 = time.time()
+            while not self.lines and self.proc.poll() is None and time.time() - t0 < 10.0:
+                time.sleep(0.02)
+            self.lines.clear()
         except OSError:
             self.proc = None
         return self
