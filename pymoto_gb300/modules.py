@@ -35,6 +35,39 @@ class DensityFilter(Module):
         self.nonpadding = None if nonpadding is None else np.asarray(nonpadding, dtype=np.int64).ravel()
         self._s = None
 
+    @property
+    def H(self):
+        """The filter matrix as pyMOTO builds it (scipy CSC, host; pymoto/modules/filter.py:307-378), for code
+        that reads it.  The device path never forms it: the kernels evaluate the weights on the fly."""
+        if getattr(self, "_H", None) is None:
+            import scipy.sparse as sps
+            g = self.grid
+            nx, ny, nz = g.nelx, g.nely, max(g.nelz, 1)
+            dl = int(self.radius)
+            el = np.arange(g.nel)
+            ix, iy, iz = el % nx, (el // nx) % ny, el // (nx * ny)
+            rows, cols, vals = [], [], []
+            for dz in range(-dl, dl + 1) if g.nelz else [0]:
+                for dy in range(-dl, dl + 1):
+                    for dx in range(-dl, dl + 1):
+                        jx, jy, jz = ix + dx, iy + dy, iz + dz
+                        ok = (jx >= 0) & (jx < nx) & (jy >= 0) & (jy < ny) & (jz >= 0) & (jz < nz)
+                        rows.append(el[ok])
+                        cols.append((jz[ok] * ny + jy[ok]) * nx + jx[ok])
+                        h = max(0.0, self.radius - np.sqrt(dx * dx + dy * dy + dz * dz))
+                        vals.append(np.full(int(ok.sum()), h))
+            self._H = sps.coo_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                                     shape=(g.nel, g.nel)).tocsc()
+        return self._H
+
+    @property
+    def Hs(self):
+        """Row sums of H (an (nel, 1) matrix, as pyMOTO's), the rows outside `nonpadding` set to their maximum."""
+        hs = self.H.sum(1)
+        if self.nonpadding is not None:
+            hs[~np.isin(np.arange(hs.shape[0]), self.nonpadding)] = np.max(hs)
+        return hs
+
     def _rowsum(self, device):
         """Row sums s of H on the device; with `nonpadding`, every row outside it takes max(s), which mimics
         zero densities outside the domain (pymoto/modules/filter.py:241-255).  Setup only."""

@@ -34,7 +34,8 @@ def clamp_face_dofs(grid):
 # them, so that with -x a failure in one of the later rows does not hide the hot path's results;
 # test_zz_no_alloc stays last.
 _LATER = ("test_filter_variants", "test_mass", "test_poisson", "test_overhang", "test_math_expression",
-          "test_scalars", "test_einsum", "test_routines", "test_design_runs", "test_checkpoint", "test_faults", "test_zz_no_alloc")
+          "test_scalars", "test_einsum", "test_routines", "test_design_runs", "test_checkpoint", "test_faults",
+          "test_zz_no_alloc")
 
 
 def pytest_collection_modifyitems(session, config, items):

@@ -218,3 +218,18 @@ def test_padded_overrides_on_device(tag, golden):
     np.testing.assert_allclose(y.cpu().numpy(), g[f"{tag}_y"], rtol=1e-13, atol=1e-15)
     dx = fc._sensitivity(torch.from_numpy(g[f"{tag}_dy"]).cuda())
     np.testing.assert_allclose(dx.cpu().numpy(), g[f"{tag}_dx"], rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("shape,r,nonpad", [((7, 5), 1.5, None), ((6, 5, 4), 2.0, None), ((10, 6), 2.5, "third")])
+def test_density_filter_matrix_matches_the_oracle(shape, r, nonpad):
+    """DensityFilter.H / .Hs (host, for code that reads them) equal the oracle's pyMOTO restatement."""
+    import oracle as O
+    import pymoto_gb300 as pg
+    d = pg.VoxelDomain(*shape)
+    npd = None if nonpad is None else np.arange(0, d.nel, 3)
+    df = pg.DensityFilter(d, radius=r, nonpadding=npd)
+    H, s = O.density_filter_matrix(O.Grid(*shape), r)
+    if npd is not None:
+        s = O.density_filter_nonpadding(s, npd)
+    np.testing.assert_allclose(df.H.toarray(), H.toarray(), rtol=0, atol=1e-15)
+    np.testing.assert_allclose(np.asarray(df.Hs).ravel(), np.asarray(s).ravel(), rtol=1e-15)
