@@ -368,7 +368,20 @@ class FilterConv(Module):
         X, Y, Z = np.meshgrid(np.arange(-ex, ex + 1) * dx, np.arange(-ey, ey + 1) * dy, np.arange(-ez, ez + 1) * dz,
                               indexing="ij")
         w = np.maximum(0.0, radius - np.sqrt(X * X + Y * Y + Z * Z))
-        self.weights = w / np.sum(w)
+        w = w / np.sum(w)
+        if getattr(self, "_maps_host", None) is not None:
+            # a new radius after construction: the padding was laid out for the kernel size given then
+            if w.shape != self.weights.shape:
+                raise ValueError(f"the new kernel {w.shape} does not fit the padding of {self.weights.shape}")
+            self.weights = w
+            self._const_host = self._constant_field(self._bcs, self._sizes)
+            self._dev = None
+            self._pad_dev = None
+            if self._fzero is not None:
+                self._fzero.weights = w.copy()
+                self._fzero._dev = None
+            return
+        self.weights = w
 
     @staticmethod
     def _inverse_map(m, n):

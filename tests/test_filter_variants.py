@@ -233,3 +233,20 @@ def test_density_filter_matrix_matches_the_oracle(shape, r, nonpad):
         s = O.density_filter_nonpadding(s, npd)
     np.testing.assert_allclose(df.H.toarray(), H.toarray(), rtol=0, atol=1e-15)
     np.testing.assert_allclose(np.asarray(df.Hs).ravel(), np.asarray(s).ravel(), rtol=1e-15)
+
+
+def test_new_radius_refreshes_the_derived_data():
+    """set_filter_radius after construction (same kernel size) gives the state a fresh filter would have."""
+    import pymoto_gb300 as pg
+    d = pg.VoxelDomain(7, 5, 4)
+    bcs = dict(xmin_bc=0.5, ymax_bc=1.0)
+    a = pg.FilterConv(d, radius=2.5, **bcs)
+    a.override_values((slice(0, 2), 1, 1), 0.3)
+    a.set_filter_radius(2.8)
+    b = pg.FilterConv(d, radius=2.8, **bcs)
+    np.testing.assert_array_equal(a.weights, b.weights)
+    np.testing.assert_array_equal(a._const_host, b._const_host)
+    np.testing.assert_array_equal(a._fzero.weights, b.weights)
+    assert a._dev is None and a._pad_dev is None
+    with pytest.raises(ValueError):
+        a.set_filter_radius(3.5)
