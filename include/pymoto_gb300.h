@@ -143,6 +143,11 @@ int pmg_stencil_cheb_step(int dtype, int nelx, int nely, int nelz, const void* S
 int pmg_ebe_cheb_step(int nelx, int nely, int nelz, const float* xe, const double* K0_host, const uint8_t* bcmask,
                       double bcdiag, const float* u, const float* b, const float* dl1, float* d, const double* coef,
                       int step, float* y, void* stream);
+/* Status of the tensor-core operator kernels (pmg_ebe_apply / pmg_ebe_cheb_step on FP32 3D grids) since the
+ * last reset (host-synchronous read): PMG_OK, or PMG_TIMEOUT if a bounded wait of a kernel gave up (its
+ * output is then undefined).  reset != 0 clears the flag.  No counterpart in the reference: pyMOTO's
+ * assembly has no device waits. */
+int pmg_operator_status(int reset);
 /* Step `step`: d = a d + c r / diag, x = x + d; init != 0 starts from x = 0 (d = x = c r / diag). */
 int pmg_cheb_step(int dtype, int64_t n, const void* r, const void* diag, void* d, void* x, const double* coef, int step,
                   int init, void* stream);
@@ -192,7 +197,9 @@ int pmg_dot2(int dtype, int64_t n, const void* a, const void* b, const void* c, 
  * counterpart in the reference.  Its scratch is a static device array of about 32 KB held by every GPU that
  * loads the library; n is limited to 4,194,304 elements (larger n: PMG_BAD_ARG).  All calls on a device
  * share that array, so calls that overlap on the GPU race; calls ordered on one stream are safe.  The first
- * call on each device looks up the array's device address; make it before any stream capture. */
+ * call in each CUDA context looks up the array's device address in that context; make it before any stream
+ * capture.  Accumulation as pmg_dot (FP32 data: compensated FP32), over a different per-CTA split, so the
+ * two agree to rounding, not bit for bit. */
 int pmg_dot_noalloc(int dtype, int64_t n, const void* a, const void* b, double* out, void* stream);
 /* In the *_ratio updates below a zero denominator gives a zero ratio (no update) instead of inf/nan. */
 /* alpha = num[0]/den[0];  x += alpha p;  r -= alpha q;  rr_out[0] = r.r   (FP64 CG step). */

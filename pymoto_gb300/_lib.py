@@ -46,6 +46,7 @@ SIGNATURES = {
     "pmg_cheb_step": (I, [I, L, P, P, P, P, P, I, I, P]),
     "pmg_stencil_cheb_step": (I, [I, I, I, I, P, P, P, P, P, P, I, P, P]),
     "pmg_ebe_cheb_step": (I, [I, I, I, P, P, P, D, P, P, P, P, P, I, P, P]),
+    "pmg_operator_status": (I, [I]),
     "pmg_cholesky_factor": (I, [I, P, I, P, P]),
     "pmg_cholesky_solve": (I, [I, I, P, I, P, P, P]),
     "pmg_cholesky_inverse": (I, [I, P, I, P, P]),
@@ -158,7 +159,7 @@ def _arg(a):
 _HOST_ONLY = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_element_stiffness", "pmg_galerkin_table",
               "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth",
               "pmg_cholesky_inverse_f32_scratch_bytes", "pmg_nn_wgrad_scratch_bytes", "pmg_oc_status",
-              "pmg_coarse_ordering", "pmg_oc_status_async", "pmg_mma_scratch_bytes"}
+              "pmg_coarse_ordering", "pmg_oc_status_async", "pmg_mma_scratch_bytes", "pmg_operator_status"}
 
 
 def _launches(name, args):

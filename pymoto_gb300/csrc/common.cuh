@@ -120,7 +120,41 @@ struct ChebArgs {
 };
 constexpr int PMG_APPLY_CHEB = 3;
 
-// 3D FP32 operator apply on the tensor cores (ebe_mma.cu).
+// Dot-product accumulators.  FP64 data: one FP64 FMA per element.  FP32 data: no FP64 arithmetic per element
+// (GB300 runs FP64 at 1/64 of the FP32 rate); the product is split exactly into p + e with an FMA and added
+// to an unevaluated sum s + c by Knuth's TwoSum (Ogita, Rump, Oishi, "Accurate sum and dot product", SIAM J.
+// Sci. Comput. 26 (2005), Dot2), which is as accurate as FP64 accumulation of the exact products.  The
+// explicitly rounded intrinsics keep the compiler from contracting the error terms into FMAs.
+template <typename T>
+struct DotAcc;
+
+template <>
+struct DotAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+template <>
+struct DotAcc<float> {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = fmaf(a, b, -p);                  // a b - p, exact
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));   // s + p - t, exact
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, e));
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// 3D FP32 operator apply on the tensor cores (ebe_tc.cu: tcgen05, accumulators in tensor memory).
+int ebe_apply_tc_f32(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
+                     const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
+                     cudaStream_t st);
+// 3D FP32 operator apply with mma.sync tiles (ebe_mma.cu).
 int ebe_apply_mma_f32(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
                       const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
                       cudaStream_t st);

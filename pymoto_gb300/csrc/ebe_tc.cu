@@ -1,0 +1,453 @@
+// Matrix-free hex8 operator (FP32) on the 5th-generation tensor cores (tcgen05, TMEM accumulators).
+//
+// K(x) u = sum_e x_e K0 u_e (pymoto/modules/assembly.py:245-296 assembles the same sum as a CSR matrix).
+//
+// Work split.  A CTA (8 warps) owns a tile of 32 x 8 elements in x, y and walks up a chunk of z layers.
+// Thread (lane l, warp r) is element (ie0 + l, je0 + r) of every layer; the CTA owns the nodes strictly
+// inside its element tile (31 x 7 per layer), so every contribution to an owned node is computed inside
+// the CTA and the node sums need no atomics (deterministic results).  Neighbouring tiles overlap by one
+// element in x and y.
+//
+// Element products.  Per layer the 256 element vectors u_e (24 values) form two 128-row GEMM tiles, one
+// per warpgroup: each thread writes its row into tensor memory (tcgen05.st), and one thread per
+// warpgroup issues D = A B with A = [U_hi | U_lo] (128 x 48, TF32, in TMEM) and
+// B = [[K0_hi, K0_lo], [K0_hi, 0]] (48 x 48, TF32, in shared memory), so that
+// D[:, 0:24] + D[:, 24:48] = U_hi K0_hi + U_lo K0_hi + U_hi K0_lo: three TF32 products in six
+// tcgen05.mma (M = 128, N = 48, K = 8), FP32 accumulation in TMEM.  U is taken relative to the element's
+// first node (K0 annihilates a common translation of the 8 nodes), so the rounding error scales with the
+// variation of u over one element, not with |u|.
+//
+// Node sums.  The thread reads its row of D back (tcgen05.ld), scales by x_e and keeps the forces on its
+// upper 4 nodes in registers for the next layer (z sum in registers); the pair of elements on either side
+// of a node in x is summed with a warp shuffle, and the pair in y through a small shared-memory exchange.
+// One CTA barrier, one warpgroup barrier and one mbarrier wait per layer.
+//
+// Staging: node layers of u (masked at constrained dofs), their constraint-mask words, the element layer
+// of x and the operands of each thread's owned node (b, diag, the Chebyshev increment) are copied with
+// cp.async two layers ahead into a 5-slot ring.
+//
+// Every wait is bounded: an mbarrier wait that gives up sets the library's operator error word
+// (pmg_operator_status) and the kernel carries on to its end, where it frees its tensor memory.
+#include "common.cuh"
+
+namespace pmg {
+
+// Error word of the tensor-core operator kernels (non-zero: a bounded wait gave up).
+__device__ int g_operator_error = 0;
+
+namespace {
+
+constexpr int TX = 32, TY = 8;               // element tile: lanes x warps
+constexpr int NODX = TX + 1, NODY = TY + 1;  // staged node tile 33 x 9
+constexpr int PLANE = NODX * NODY;           // 297 nodes per staged layer
+constexpr int OWNX = TX - 1, OWNY = TY - 1;  // owned nodes per tile: 31 x 7
+constexpr int NTHREADS = TX * TY;            // 256
+constexpr int RING = 5;       // node layers t, t + 1 in use, t + 2 and t + 3 in flight, t - 1 read by the node phase
+constexpr int PFN = (PLANE + NTHREADS - 1) / NTHREADS;  // staged nodes per thread: 2
+constexpr int TMEM_COLS = 256;               // 2 warpgroups x (A 48 + D 48) = 192, rounded to a power of 2
+constexpr int COLS_PER_WG = 96;
+constexpr uint32_t WAIT_LIMIT = 1u << 22;
+
+struct TcSmem {
+  float B[48 * 48];               // K-major, no swizzle: core matrix (n/8, k/4) at (n/8)*1536 + (k/4)*128 bytes
+  float u[RING][3][PLANE];        // node layers of u: [slot][component][node of the staged tile]
+  uint32_t m[RING][PLANE];        // aligned bcmask word holding each staged node's mask byte
+  float x[RING][TX * TY];         // element layer of x
+  float xb[2][TY][3][TX];         // y-pair exchange: [parity][row][component][lane]
+  float ob[RING][3][NTHREADS];    // b of each thread's owned node (own copies, read only by the thread)
+  float od[RING][3][NTHREADS];    // diag (Jacobi, Chebyshev)
+  float oc[RING][3][NTHREADS];    // the previous Chebyshev increment
+  unsigned long long mbar[2];     // MMA completion, one per warpgroup
+  uint32_t tbase;                 // TMEM base address from tcgen05.alloc
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(smem)), "l"(gmem), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+__device__ __forceinline__ float tf32_rna(float v) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float* v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
+      "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]), "=f"(v[8]),
+        "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15])
+      : "r"(taddr)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: no swizzle, K-major; LBO = stride between core matrices along K,
+// SBO = stride between 8-row groups along M/N; bits 46-47 = 1 (descriptor version of sm_100 and later).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+         (1ull << 46);
+}
+
+// Instruction descriptor of kind::tf32: D F32, A and B TF32, both K-major, N = 48, M = 128.
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((48u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b_desc), "r"(IDESC), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(const unsigned long long* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// Bounded wait for the mbarrier phase with the given parity; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(const unsigned long long* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (uint32_t it = 0; it < WAIT_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void balanced_part(int n, int parts, int p, int& start, int& len) {
+  const int base = n / parts, rem = n - base * parts;
+  start = p * base + min(p, rem);
+  len = base + (p < rem ? 1 : 0);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(NTHREADS, 2)
+    ebe_apply_tc_kernel(Grid g, const float* __restrict__ xe, ElemMat<float, 24> K0,
+                        const uint8_t* __restrict__ bcmask, float bcdiag, const float* __restrict__ u,
+                        const float* __restrict__ b, const float* __restrict__ diag, float w, float* __restrict__ y,
+                        ChebArgs<float> ch) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcSmem& S = *reinterpret_cast<TcSmem*>(smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wg = warp >> 2;
+  const int nnx = g.nx + 1, nny = g.ny + 1, nnz = g.nz + 1;
+  const int ie0 = (int)blockIdx.x * OWNX - 1, je0 = (int)blockIdx.y * OWNY - 1;
+  int kz0, nlay;
+  balanced_part(nnz, gridDim.z, blockIdx.z, kz0, nlay);
+  const int64_t nlayer = (int64_t)nnx * nny;
+  const int64_t nn_total = nlayer * nnz;
+  float ca = 0.f, cc = 0.f;
+  if (MODE == 3) {
+    ca = (float)ch.coef[2 * ch.step];
+    cc = (float)ch.coef[2 * ch.step + 1];
+  }
+
+  // B = [[K0_hi, K0_lo], [K0_hi, 0]] (48 x 48, row k, column n) in the canonical K-major layout
+  for (int q = tid; q < 48 * 48; q += NTHREADS) {
+    const int k = q / 48, n = q - (q / 48) * 48;
+    const float kv = K0.v[(k % 24) * 24 + (n % 24)];
+    const float hi = tf32_rna(kv);
+    const float v = n < 24 ? hi : (k < 24 ? tf32_rna(kv - hi) : 0.f);
+    S.B[(n >> 3) * 384 + (k >> 2) * 32 + (n & 7) * 4 + (k & 3)] = v;
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.mbar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.mbar[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tbase)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+
+  // staging slots of this thread (layer independent)
+  int gnode[PFN], spos[PFN];
+#pragma unroll
+  for (int s = 0; s < PFN; ++s) {
+    const int v = tid + s * NTHREADS;
+    const int row = v / NODX, cx = v - row * NODX;
+    const int gi = ie0 + cx, gj = je0 + row;
+    spos[s] = v < PLANE ? v : -1;
+    gnode[s] = (v < PLANE && gi >= 0 && gi < nnx && gj >= 0 && gj < nny) ? gj * nnx + gi : -1;
+  }
+  // node owned by this thread in every layer: (ie0 + lane, je0 + warp), lane >= 1, warp >= 1
+  const int Xn = ie0 + lane, Yn = je0 + warp;
+  const bool owner = lane >= 1 && warp >= 1 && Xn < nnx && Yn < nny;
+  const int64_t node_xy = owner ? (int64_t)Yn * nnx + Xn : 0;
+  const int gie = ie0 + lane, gje = je0 + warp;
+  const int gelem = (gie >= 0 && gie < g.nx && gje >= 0 && gje < g.ny) ? gje * g.nx + gie : -1;
+
+  // copies of node layer kz0 - 1 + s (u and mask words) and element layer kz0 - 1 + s (x) into slot s % RING
+  auto issue = [&](int s) {
+    const int ku = kz0 - 1 + s, kx = ku;
+    const bool uok = ku >= 0 && ku < nnz, xok = kx >= 0 && kx < g.nz;
+    const int slot = s % RING;
+#pragma unroll
+    for (int q = 0; q < PFN; ++q) {
+      if (spos[q] < 0) continue;
+      const bool live = uok && gnode[q] >= 0;
+      const int64_t m = live ? ku * nlayer + gnode[q] : 0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) cp_async4(&S.u[slot][c][spos[q]], u + m * 3 + c, live ? 4 : 0);
+      if (bcmask) {
+        const int64_t wd = m & ~int64_t(3);
+        const int64_t left = nn_total - wd;
+        cp_async4(&S.m[slot][spos[q]], bcmask + wd, live ? (left < 4 ? (int)left : 4) : 0);
+      }
+    }
+    const bool xlive = xok && gelem >= 0;
+    cp_async4(&S.x[slot][tid], xe + (xlive ? (int64_t)kx * g.nx * g.ny + gelem : 0), xlive ? 4 : 0);
+    if (MODE >= 1 && owner && s >= 1 && s <= nlay) {          // operands of the owned node of node layer ku
+      const int64_t q0 = ((int64_t)ku * nlayer + node_xy) * 3;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        cp_async4(&S.ob[slot][c][tid], b + q0 + c, 4);
+        if (MODE >= 2) cp_async4(&S.od[slot][c][tid], diag + q0 + c, 4);
+        if (MODE == 3 && ch.step > 0) cp_async4(&S.oc[slot][c][tid], ch.d + q0 + c, 4);
+      }
+    }
+    cp_async_commit();
+  };
+  // zero the constrained dofs of this thread's staged nodes of slot s (after its copies landed)
+  auto fixup = [&](int s) {
+    if (!bcmask) return;
+    const int ku = kz0 - 1 + s;
+    if (ku < 0 || ku >= nnz) return;
+    const int slot = s % RING;
+#pragma unroll
+    for (int q = 0; q < PFN; ++q) {
+      if (spos[q] < 0 || gnode[q] < 0) continue;
+      const int64_t m = ku * nlayer + gnode[q];
+      const unsigned fixed = (S.m[slot][spos[q]] >> (8 * (int)(m & 3))) & 7u;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        if ((fixed >> c) & 1u) S.u[slot][c][spos[q]] = 0.f;
+    }
+  };
+
+  issue(0);
+  issue(1);
+  issue(2);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // B and the mbarrier inits -> async proxy
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = S.tbase;
+  const uint32_t lane_sel = (uint32_t)(32 * (warp & 3)) << 16;
+  const uint32_t colA = tbase + COLS_PER_WG * wg, colD = colA + 48;
+  const uint32_t bbase = smem_u32(S.B);
+
+
+  float carry[12];   // forces of the previous element layer on its upper nodes (local nodes 4..7)
+#pragma unroll
+  for (int q = 0; q < 12; ++q) carry[q] = 0.f;
+  float p0[3] = {0.f, 0.f, 0.f};   // x-paired forces on node (Xn, Yn) from this element row (previous layer)
+  bool timed_out = false;
+
+  // node layer kz0 - 1 + t: the owned node's output (its operands and mask byte were staged in slot t)
+  auto node_phase = [&](int t, int xpar) {
+    if (!owner || t < 1 || t > nlay) return;
+    const int slot = t % RING;
+    const int64_t n = (int64_t)(kz0 - 1 + t) * nlayer + node_xy;
+    const unsigned om = bcmask ? (S.m[slot][warp * NODX + lane] >> (8 * (int)(n & 3))) & 7u : 0u;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float acc = p0[d] + S.xb[xpar][warp - 1][d][lane];
+      const int64_t q = n * 3 + d;
+      const bool fixed = (om >> d) & 1u;
+      const float uq = (MODE >= 2 || fixed) ? u[q] : 0.f;
+      const float Au = fixed ? bcdiag * uq : acc;
+      if (MODE == 0) {
+        y[q] = Au;
+      } else if (MODE == 1) {
+        y[q] = S.ob[slot][d][tid] - Au;
+      } else if (MODE == 2) {
+        y[q] = uq + w * __fdividef(S.ob[slot][d][tid] - Au, S.od[slot][d][tid]);
+      } else {
+        const float dprev = ch.step == 0 ? 0.f : S.oc[slot][d][tid];
+        const float dn = ca * dprev + cc * __fdividef(S.ob[slot][d][tid] - Au, S.od[slot][d][tid]);
+        ch.d[q] = dn;
+        y[q] = uq + dn;
+      }
+    }
+  };
+
+  for (int t = 0; t <= nlay; ++t) {
+    // element layer kz0 - 1 + t: node layers in slots t and t + 1 (t + 1 has just landed), x in slot t
+    cp_async_wait1();
+    if (t == 0) fixup(0);
+    fixup(t + 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (t + 3 <= nlay + 1) issue(t + 3);
+    else cp_async_commit();      // empty group: keeps the wait counts uniform
+
+    // A row of this element: u_e relative to its first node, split into TF32 hi and lo parts
+    {
+      const int s0 = t % RING, s1 = (t + 1) % RING;
+      float a[48];
+#pragma unroll
+      for (int loc = 0; loc < 8; ++loc) {
+        const int dx = loc & 1, dy = (loc >> 1) & 1, dz = loc >> 2;
+        const int p = (warp + dy) * NODX + lane + dx;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) a[loc * 3 + d] = S.u[dz ? s1 : s0][d][p];
+      }
+#pragma unroll
+      for (int q = 23; q >= 0; --q) {
+        const float v = a[q] - a[q % 3];
+        const float hi = tf32_rna(v);
+        a[q] = hi;
+        a[24 + q] = tf32_rna(v - hi);
+      }
+      tmem_st16(colA + lane_sel, a);
+      tmem_st16(colA + lane_sel + 16, a + 16);
+      tmem_st16(colA + lane_sel + 32, a + 32);
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    if (wg == 0)
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+    else
+      asm volatile("bar.sync 2, 128;" ::: "memory");
+    if ((tid & 127) == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int s = 0; s < 6; ++s) mma_tf32(colD, colA + 8 * s, smem_desc(bbase + 256u * s, 128u, 1536u), s > 0);
+      mma_commit(&S.mbar[wg]);
+    }
+
+    // while the MMA runs: the output of node layer kz0 - 2 + t (completed in the previous iteration)
+    node_phase(t - 1, (t - 1) & 1);
+
+    if (!mbar_wait(&S.mbar[wg], (uint32_t)(t & 1))) timed_out = true;
+    tc_fence_after();
+    float dv[48];
+    tmem_ld16(colD + lane_sel, dv);
+    tmem_ld16(colD + lane_sel + 16, dv + 16);
+    tmem_ld16(colD + lane_sel + 32, dv + 32);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    const float xv = S.x[t % RING][tid];
+    float z[12];
+#pragma unroll
+    for (int q = 0; q < 12; ++q) {
+      z[q] = carry[q] + xv * (dv[q] + dv[24 + q]);        // local nodes 0..3: this node layer
+      carry[q] = xv * (dv[12 + q] + dv[36 + q]);          // local nodes 4..7: the next node layer
+    }
+    // x pairs: node (ie0 + lane, je0 + warp + ly) gets local node 2 ly of this element and local node 2 ly + 1
+    // of the element to its left (lane - 1)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float l0 = __shfl_up_sync(0xffffffffu, z[3 + d], 1);
+      const float l1 = __shfl_up_sync(0xffffffffu, z[9 + d], 1);
+      p0[d] = z[d] + l0;
+      S.xb[t & 1][warp][d][lane] = z[6 + d] + l1;
+    }
+    tc_fence_before();
+  }
+  __syncthreads();
+  node_phase(nlay, nlay & 1);
+
+  cp_async_wait_all();
+  if (timed_out) atomicExch(&g_operator_error, 1);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+}  // namespace
+
+// 3D FP32 operator apply on the tensor cores (modes as pmg_ebe_apply, 3 = fused Chebyshev step).
+int ebe_apply_tc_f32(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
+                     const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
+                     cudaStream_t st) {
+  static bool attr_set[64][4] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return check_launch();
+  if (bcmask && (reinterpret_cast<uintptr_t>(bcmask) & 3u)) {   // the mask is copied in aligned 4-byte words
+    set_error("ebe_apply_tc_f32: bcmask must be 4-byte aligned");
+    return PMG_BAD_ARG;
+  }
+  // at most two CTAs per SM (2 x 256 TMEM columns): the shared memory request keeps a third one out
+  const size_t smem = sizeof(TcSmem) + 1024 > 80 * 1024 ? sizeof(TcSmem) + 1024 : 80 * 1024;
+  const int tx = (g.nx + 1 + OWNX - 1) / OWNX, ty = (g.ny + 1 + OWNY - 1) / OWNY;
+  const int nnz = g.nz + 1, slots = 2 * sm_count();
+  int nzc = 1;
+  int64_t best = -1;
+  for (int c = 1; c <= nnz; ++c) {
+    const int64_t waves = ((int64_t)tx * ty * c + slots - 1) / slots;
+    const int64_t cost = waves * ((nnz + c - 1) / c + 1);
+    if (best < 0 || cost < best) {
+      best = cost;
+      nzc = c;
+    }
+  }
+  const dim3 grid(tx, ty, nzc);
+  auto K = make_elem_mat<float, 24>(K0);
+  const int m = mode == PMG_APPLY_MATVEC ? 0 : (mode == PMG_APPLY_RESIDUAL ? 1 : (mode == PMG_APPLY_JACOBI ? 2 : 3));
+  if (!attr_set[dev][m]) {
+    const void* fn = m == 0   ? (const void*)ebe_apply_tc_kernel<0>
+                     : m == 1 ? (const void*)ebe_apply_tc_kernel<1>
+                     : m == 2 ? (const void*)ebe_apply_tc_kernel<2>
+                              : (const void*)ebe_apply_tc_kernel<3>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      set_error(cudaGetErrorString(e));
+      return PMG_CUDA_ERR;
+    }
+    attr_set[dev][m] = true;
+  }
+  const float bd = (float)bcdiag, wf = (float)w;
+  if (m == 0)
+    ebe_apply_tc_kernel<0><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
+  else if (m == 1)
+    ebe_apply_tc_kernel<1><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
+  else if (m == 2)
+    ebe_apply_tc_kernel<2><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
+  else
+    ebe_apply_tc_kernel<3><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
+  return check_launch();
+}
+
+}  // namespace pmg
+
+extern "C" int pmg_operator_status(int reset) {
+  int v = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&v, pmg::g_operator_error, sizeof(int));
+  if (e == cudaSuccess && reset && v) {
+    const int zero = 0;
+    e = cudaMemcpyToSymbol(pmg::g_operator_error, &zero, sizeof(int));
+  }
+  if (e != cudaSuccess) {
+    pmg::set_error(cudaGetErrorString(e));
+    return PMG_CUDA_ERR;
+  }
+  return v ? PMG_TIMEOUT : PMG_OK;
+}

@@ -85,36 +85,6 @@ inline unsigned red_blocks(int64_t n) {
   return (unsigned)b;
 }
 
-// Dot-product accumulators.  FP64 data: one FP64 FMA per element.  FP32 data: no FP64 arithmetic per element
-// (GB300 runs FP64 at 1/64 of the FP32 rate); the product is split exactly into p + e with an FMA and added
-// to an unevaluated sum s + c by Knuth's TwoSum (Ogita, Rump, Oishi, "Accurate sum and dot product", SIAM J.
-// Sci. Comput. 26 (2005), Dot2), which is as accurate as FP64 accumulation of the exact products.  The
-// explicitly rounded intrinsics keep the compiler from contracting the error terms into FMAs.
-template <typename T>
-struct DotAcc;
-
-template <>
-struct DotAcc<double> {
-  double s = 0.0;
-  __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
-  __device__ __forceinline__ double value() const { return s; }
-};
-
-template <>
-struct DotAcc<float> {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float a, float b) {
-    const float p = __fmul_rn(a, b);
-    const float e = fmaf(a, b, -p);                  // a b - p, exact
-    const float t = __fadd_rn(s, p);
-    const float z = __fsub_rn(t, s);
-    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));   // s + p - t, exact
-    s = t;
-    c = __fadd_rn(c, __fadd_rn(err, e));
-  }
-  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
-};
-
 // Scalar num/den (times scale) computed once per CTA: an FP64 division per thread is expensive on GB300.
 // A zero denominator gives a zero ratio (no update) instead of inf/nan.
 __device__ __forceinline__ double cta_ratio(const double* num, const double* den, double scale) {

@@ -27,7 +27,7 @@ constexpr int NOALLOC_THREADS = 256;
 constexpr int NOALLOC_CHUNK = NOALLOC_THREADS * 4;
 constexpr int NOALLOC_MAX_CTAS = 4096;
 constexpr int64_t NOALLOC_MAX_N = (int64_t)NOALLOC_MAX_CTAS * NOALLOC_CHUNK;
-constexpr int NOALLOC_MAX_DEVICES = 64;
+constexpr int NOALLOC_MAX_CONTEXTS = 64;
 
 struct NoAllocScratch {
   double partial[NOALLOC_MAX_CTAS];
@@ -37,8 +37,14 @@ struct NoAllocScratch {
 // The scratch: zero-initialised when the module loads, shared by every call on a device.
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
+// cached (context, address) pairs; the driver's cuCtxGetCurrent is reached through the runtime's entry-point
+// query, so the library needs no link against libcuda
 std::mutex g_noalloc_mutex;
-NoAllocScratch* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+void* g_noalloc_ctx[NOALLOC_MAX_CONTEXTS] = {};
+NoAllocScratch* g_noalloc_addr[NOALLOC_MAX_CONTEXTS] = {};
+int g_noalloc_count = 0;
+typedef int (*CtxGetCurrentFn)(void**);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
 
 __device__ __forceinline__ double na_warp_sum(double v) {
 #pragma unroll
@@ -63,14 +69,14 @@ template <typename T>
 __global__ void __launch_bounds__(NOALLOC_THREADS) dot_noalloc_kernel(int64_t n, const T* __restrict__ a,
                                                                       const T* __restrict__ b, double* out,
                                                                       NoAllocScratch* scr) {
-  double v = 0.0;
+  DotAcc<T> acc;
   const int64_t base = (int64_t)blockIdx.x * NOALLOC_CHUNK + threadIdx.x;
 #pragma unroll
   for (int k = 0; k < NOALLOC_CHUNK / NOALLOC_THREADS; ++k) {
     const int64_t i = base + (int64_t)k * NOALLOC_THREADS;
-    if (i < n) v = fma((double)a[i], (double)b[i], v);
+    if (i < n) acc.add(a[i], b[i]);
   }
-  v = na_block_sum(v);
+  double v = na_block_sum(acc.value());
   __shared__ bool last;
   if (threadIdx.x == 0) {
     scr->partial[blockIdx.x] = v;
@@ -80,38 +86,58 @@ __global__ void __launch_bounds__(NOALLOC_THREADS) dot_noalloc_kernel(int64_t n,
   __syncthreads();
   if (!last) return;
   __threadfence();
-  double acc = 0.0;
-  for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) acc += ((volatile double*)scr->partial)[c];
-  acc = na_block_sum(acc);
+  double tot = 0.0;
+  for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) tot += ((volatile double*)scr->partial)[c];
+  tot = na_block_sum(tot);
   if (threadIdx.x == 0) {
-    out[0] = acc;
+    out[0] = tot;
     scr->ticket = 0u;
   }
 }
 
-// Device address of the static scratch on the current device, looked up once per device.
+// Device address of the static scratch in the current context, looked up once per context.
 int scratch_address(NoAllocScratch** addr) {
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  cudaError_t e = cudaGetDevice(&dev);     // also makes the runtime bind its context to this thread
   if (e != cudaSuccess) {
     set_error(cudaGetErrorString(e));
     return PMG_CUDA_ERR;
   }
-  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
-    set_error("pmg_dot_noalloc: device index beyond the supported 64 devices");
-    return PMG_BAD_ARG;
-  }
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (g_noalloc_addr[dev] == nullptr) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      set_error(e != cudaSuccess ? cudaGetErrorString(e) : "pmg_dot_noalloc: null scratch address");
+  if (g_ctx_get_current == nullptr) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || fn == nullptr) {
+      set_error("pmg_dot_noalloc: the driver's cuCtxGetCurrent is not available");
       return PMG_CUDA_ERR;
     }
-    g_noalloc_addr[dev] = static_cast<NoAllocScratch*>(p);
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
   }
-  *addr = g_noalloc_addr[dev];
+  void* ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != 0 || ctx == nullptr) {
+    set_error("pmg_dot_noalloc: no current CUDA context");
+    return PMG_CUDA_ERR;
+  }
+  for (int i = 0; i < g_noalloc_count; ++i)
+    if (g_noalloc_ctx[i] == ctx) {
+      *addr = g_noalloc_addr[i];
+      return PMG_OK;
+    }
+  if (g_noalloc_count >= NOALLOC_MAX_CONTEXTS) {
+    set_error("pmg_dot_noalloc: more than 64 CUDA contexts");
+    return PMG_BAD_ARG;
+  }
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || p == nullptr) {
+    set_error(e != cudaSuccess ? cudaGetErrorString(e) : "pmg_dot_noalloc: null scratch address");
+    return PMG_CUDA_ERR;
+  }
+  g_noalloc_ctx[g_noalloc_count] = ctx;
+  g_noalloc_addr[g_noalloc_count] = static_cast<NoAllocScratch*>(p);
+  ++g_noalloc_count;
+  *addr = g_noalloc_addr[g_noalloc_count - 1];
   return PMG_OK;
 }
 

@@ -954,8 +954,8 @@ template <typename T, int DIM>
 int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
                 const void* u, const void* b, const void* diag, double w, void* y, cudaStream_t st) {
   if constexpr (DIM == 3 && sizeof(T) == 4)
-    return ebe_apply_mma_f32(mode, g, (const float*)xe, K0, bcmask, bcdiag, (const float*)u, (const float*)b,
-                             (const float*)diag, w, (float*)y, ChebArgs<float>{nullptr, nullptr, 0}, st);
+    return ebe_apply_tc_f32(mode, g, (const float*)xe, K0, bcmask, bcdiag, (const float*)u, (const float*)b,
+                            (const float*)diag, w, (float*)y, ChebArgs<float>{nullptr, nullptr, 0}, st);
   auto K = make_elem_mat<T, Traits<DIM>::NDE>(K0);
   if constexpr (DIM == 3) {
     const dim3 block(TBX, TBY, TBZ);
@@ -1150,8 +1150,8 @@ int pmg_ebe_cheb_step(int nelx, int nely, int nelz, const float* xe, const doubl
   if (!grid_ok(nelx, nely, nelz) || nelz == 0 || !xe || !K0_host || !u || !b || !dl1 || !d || !coef || !y || y == u ||
       step < 0 || step >= 64)
     return PMG_BAD_ARG;
-  return ebe_apply_mma_f32(PMG_APPLY_CHEB, Grid{nelx, nely, nelz}, xe, K0_host, bcmask, bcdiag, u, b, dl1, 0.0, y,
-                           ChebArgs<float>{d, coef, step}, as_stream(stream));
+  return ebe_apply_tc_f32(PMG_APPLY_CHEB, Grid{nelx, nely, nelz}, xe, K0_host, bcmask, bcdiag, u, b, dl1, 0.0, y,
+                          ChebArgs<float>{d, coef, step}, as_stream(stream));
 }
 
 int pmg_stencil_diagonal(int dtype, int nelx, int nely, int nelz, const void* S, void* diag, void* stream) {

@@ -225,6 +225,8 @@ class MMA:
     def load_state_dict(self, sd):
         self.iter = int(sd["iter"])
         self.core.load_state_dict(sd["core"])
+        # the design signals are restored beside this state: responses computed before the restore are stale
+        self.response_is_uptodate = False
         self.rho = np.asarray(sd["rho"], dtype=float) if isinstance(sd["rho"], list) else sd["rho"]
 
     # --- pyMOTO Optimizer protocol ---------------------------------------------------------------------

@@ -937,29 +937,40 @@ class EinSum(Module):
         return self._einsum(self.expr, *args)
 
     def _general_sensitivity(self, df):
-        inps = self._args
-        if self._torch and not isinstance(df, torch.Tensor):
-            df = torch.as_tensor(np.asarray(df), device=inps[0].device, dtype=inps[0].dtype)
-        if self.indices_out == "" and len(inps) == 1:
-            ind = self.indices_in[0]
-            if len(set(ind)) < len(ind):    # repeated indices (trace)
-                if inps[0].ndim > 2:
-                    raise NotImplementedError(f"Sensitivities for repeated incides in '{self.expr}' not supported.")
-                mat = (torch.eye(*inps[0].shape, dtype=inps[0].dtype, device=inps[0].device) if self._torch
-                       else np.eye(*inps[0].shape, dtype=inps[0].dtype))
+        """d(out)/d(operand k) contracted with df: the einsum of df and the other operands onto operand k's
+        indices.  A single operand reduced to a scalar is the one case with repeated indices handled (a matrix
+        trace: the identity pattern)."""
+        ops = self._args
+        torch_mode = self._torch
+        if torch_mode and not isinstance(df, torch.Tensor):
+            df = torch.as_tensor(np.asarray(df), device=ops[0].device, dtype=ops[0].dtype)
+        repeated = [len(set(ix)) != len(ix) for ix in self.indices_in]
+        if len(ops) == 1 and self.indices_out == "":
+            a = ops[0]
+            if not repeated[0]:
+                pattern = torch.ones_like(a) if torch_mode else np.ones_like(a)
+            elif a.ndim <= 2:
+                pattern = (torch.eye(*a.shape, dtype=a.dtype, device=a.device) if torch_mode
+                           else np.eye(*a.shape, dtype=a.dtype))
             else:
-                mat = torch.ones_like(inps[0]) if self._torch else np.ones_like(inps[0])
-            return df * mat
-        for ind in self.indices_in:
-            if len(set(ind)) < len(ind):
-                raise NotImplementedError(f"Sensitivities for repeated incides in '{self.expr}' not supported.")
-        out = []
-        for k in range(len(inps)):
-            spec = ",".join([self.indices_out] + [s for i, s in enumerate(self.indices_in) if i != k])
-            d = self._einsum(spec + "->" + self.indices_in[k], df, *[v for i, v in enumerate(inps) if i != k])
-            complex_in = inps[k].is_complex() if self._torch else np.iscomplexobj(inps[k])
-            out.append(d.real if not complex_in and (d.is_complex() if self._torch else np.iscomplexobj(d)) else d)
-        return out
+                raise NotImplementedError(f"EinSum '{self.expr}': a trace over more than two dimensions has "
+                                          "no sensitivity here")
+            return df * pattern
+        if any(repeated):
+            raise NotImplementedError(f"EinSum '{self.expr}': an operand with a repeated index has no "
+                                      "sensitivity here")
+
+        def is_complex(v):
+            return v.is_complex() if torch_mode else np.iscomplexobj(v)
+
+        grads = []
+        for k, target in enumerate(self.indices_in):
+            others = [(ix, v) for i, (ix, v) in enumerate(zip(self.indices_in, ops)) if i != k]
+            spec = ",".join([self.indices_out] + [ix for ix, _ in others]) + "->" + target
+            g = self._einsum(spec, df, *[v for _, v in others])
+            # a real operand gets a real sensitivity
+            grads.append(g.real if is_complex(g) and not is_complex(ops[k]) else g)
+        return grads
 
     def __call__(self, *args):
         if self._general:
@@ -999,53 +1010,69 @@ def _norm(v):
 
 
 class Scaling(Module):
-    """pyMOTO's Scaling of a scalar response (pymoto/modules/scaling.py:5-83): objective y = s x / |x0|, upper
-    limit s (x - max) / |max|, lower limit s (min - x) / |min|, or the smoothed two-sided form.  A device
-    scalar (0-d CUDA tensor, e.g. EinSum's output) stays on the device; the factor of the objective form is
-    taken from the first input, as in pyMOTO."""
+    """Scaling of a scalar response for the optimizers (pyMOTO's pymoto/modules/scaling.py:5-83).
+
+    Four forms, chosen by which limits are given (s = `scaling`, a = `minmax_smooth`):
+      * no limit (objective):   g = s x / |x_0|, with x_0 the value of the first response;
+      * `maxval` only:          g = s (x - maxval) / |maxval|;
+      * `minval` only:          g = s (minval - x) / |minval|;
+      * both (smooth interval): g = s (sqrt(d^2 + a h^2) - h sqrt(1 + a)), d = x - (minval + maxval) / 2,
+        h = (maxval - minval) / 2, which is <= 0 inside the interval and > 0 outside it.
+    A limit of zero divides by one instead.  A device scalar (0-d CUDA tensor, e.g. EinSum's output) stays on
+    the device."""
 
     def __init__(self, scaling: float = 100.0, minval: float = None, maxval: float = None, minmax_smooth: float = 1.0):
-        self.minval = minval
-        self.maxval = maxval
-        self.scaling = scaling
-        self.minmax_smooth = minmax_smooth
+        self.minval, self.maxval = minval, maxval
+        self.scaling, self.minmax_smooth = scaling, minmax_smooth
+        if minval is not None and maxval is not None:
+            self._form = "interval"
+        elif maxval is not None:
+            self._form = "upper"
+        elif minval is not None:
+            self._form = "lower"
+        else:
+            self._form = "objective"
         self.sf = None
         self.reset_scaling()
 
+    @staticmethod
+    def _unit(limit):
+        return abs(limit) if limit != 0 else 1.0
+
+    def _interval(self):
+        return 0.5 * (self.minval + self.maxval), 0.5 * (self.maxval - self.minval)
+
     def __call__(self, x):
-        if self.sf is None:
+        if self.sf is None:                       # objective form: the factor is fixed by the first response
             self.sf = self.scaling / _norm(x)
-        if self.minval is not None and self.maxval is not None:
-            midp = (self.minval + self.maxval) / 2
-            diff = (self.maxval - self.minval) / 2
-            g = _sqrt((x - midp) ** 2 + self.minmax_smooth * diff ** 2) - np.sqrt((1 + self.minmax_smooth) * diff ** 2)
-        elif self.minval is not None:
-            nrm = 1 if self.minval == 0 else abs(self.minval)
-            g = (self.minval - x) / nrm
-        elif self.maxval is not None:
-            nrm = 1 if self.maxval == 0 else abs(self.maxval)
-            g = (x - self.maxval) / nrm
-        else:
-            g = x
-        return g * self.sf
+        form = self._form
+        if form == "objective":
+            return self.sf * x
+        if form == "upper":
+            return self.sf * (x - self.maxval) / self._unit(self.maxval)
+        if form == "lower":
+            return self.sf * (self.minval - x) / self._unit(self.minval)
+        mid, half = self._interval()
+        a = self.minmax_smooth
+        return self.sf * (_sqrt((x - mid) ** 2 + a * half ** 2) - abs(half) * np.sqrt(1.0 + a))
 
     def _sensitivity(self, dy):
-        dg = dy * self.sf
-        if self.minval is not None and self.maxval is not None:
-            midp = (self.minval + self.maxval) / 2
-            diff = (self.maxval - self.minval) / 2
-            x = self.get_input_states()
-            return dg * (x - midp) / _sqrt((x - midp) ** 2 + self.minmax_smooth * diff ** 2)
-        if self.minval is not None:
-            nrm = 1 if self.minval == 0 else abs(self.minval)
-            return -dg / nrm
-        if self.maxval is not None:
-            nrm = 1 if self.maxval == 0 else abs(self.maxval)
-            return dg / nrm
-        return dg
+        form = self._form
+        if form == "objective":
+            slope = self.sf
+        elif form == "upper":
+            slope = self.sf / self._unit(self.maxval)
+        elif form == "lower":
+            slope = -self.sf / self._unit(self.minval)
+        else:
+            mid, half = self._interval()
+            d = self.get_input_states() - mid
+            slope = self.sf * d / _sqrt(d ** 2 + self.minmax_smooth * half ** 2)
+        return dy * slope
 
     def reset_scaling(self):
-        self.sf = self.scaling if (self.minval is not None or self.maxval is not None) else None
+        """Forget the objective's factor (taken again from the next response); the limit forms use s itself."""
+        self.sf = None if self._form == "objective" else self.scaling
 
     def state_dict(self):
         """The scaling factor, fixed by the first response in the objective form (checkpoint)."""

@@ -1,10 +1,10 @@
 """Write the golden fixtures of tests/golden/ by running pyMOTO itself (v2.0.1).
 
-Run in a container where the pyMOTO sources are available (default: /root/reference, or the path in
-$PYMOTO_REFERENCE).  matplotlib is not needed: a module stub stands in for it, because pyMOTO imports it
+Run where the pyMOTO sources are available: give their path with --reference PATH or in
+$PYMOTO_REFERENCE; without either, a pyMOTO checkout named "reference" beside this repository is used.  matplotlib is not needed: a module stub stands in for it, because pyMOTO imports it
 at module level for plotting only.  The fixtures are small .npz files; the tests never import pyMOTO.
 
-    python tests/golden/make_golden.py          # every fixture
+    python tests/golden/make_golden.py --reference PATH          # every fixture
     python tests/golden/make_golden.py vti      # the VTI files only
     python tests/golden/make_golden.py mma      # the MMA steps only
     python tests/golden/make_golden.py scalars  # the ScalarToFile logs only
@@ -23,7 +23,17 @@ import warnings
 
 import numpy as np
 
-REF = os.environ.get("PYMOTO_REFERENCE", "/root/reference")
+def _default_reference():
+    """$PYMOTO_REFERENCE, else a pyMOTO checkout named "reference" beside this repository (None if absent)."""
+    env = os.environ.get("PYMOTO_REFERENCE")
+    if env:
+        return env
+    sibling = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.dirname(
+        os.path.abspath(__file__))))), "reference")
+    return sibling if os.path.isdir(os.path.join(sibling, "pymoto")) else None
+
+
+REF = _default_reference()
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -37,6 +47,8 @@ def import_reference():
         setattr(mpl, sub, m)
     sys.modules["matplotlib.patches"].PathPatch = object
     sys.modules["matplotlib.path"].Path = object
+    if not REF or not os.path.isdir(os.path.join(REF, "pymoto")):
+        raise SystemExit("make_golden: give the pyMOTO sources with --reference PATH or $PYMOTO_REFERENCE")
     sys.path.insert(0, REF)
     import pymoto
     return pymoto
@@ -504,8 +516,13 @@ def vti_files(pym):
 
 if __name__ == "__main__":
     warnings.filterwarnings("ignore")
+    argv = sys.argv[1:]
+    if "--reference" in argv:
+        i = argv.index("--reference")
+        REF = argv[i + 1]
+        del argv[i:i + 2]
     pym = import_reference()
-    which = sys.argv[1:] or ["all"]
+    which = argv or ["all"]
     if "all" in which:
         maps_and_k0(pym)
         assembly(pym)

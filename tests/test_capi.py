@@ -108,6 +108,19 @@ def test_invalid_arguments_fail_before_any_launch():
     assert call("pmg_stencil_bandwidth", 2, 1, 1) == (1 + 3 + 3 * 2) * 3 + 2
 
 
+def test_noalloc_dot_rejects_bad_arguments_without_a_gpu():
+    """pmg_dot_noalloc checks its arguments before it touches the device: null pointers, an unknown dtype,
+    a negative or too large n are PMG_BAD_ARG."""
+    from pymoto_gb300._lib import PMGError, call
+    buf = np.zeros(4)
+    bad = [(0, 4, None, buf, buf), (0, 4, buf, None, buf), (0, 4, buf, buf, None), (7, 4, buf, buf, buf),
+           (0, -1, buf, buf, buf), (0, 4_194_305, buf, buf, buf)]
+    for dtype, n, a, b, out in bad:
+        with pytest.raises(PMGError) as e:
+            call("pmg_dot_noalloc", dtype, n, a, b, out, None)
+        assert e.value.status == 1, (dtype, n)
+
+
 def test_product_package_never_imports_the_oracle():
     pkg = os.path.join(ROOT, "pymoto_gb300")
     for path in glob.glob(os.path.join(pkg, "**", "*.py"), recursive=True):

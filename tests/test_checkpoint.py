@@ -87,8 +87,8 @@ def test_resumed_fp64_run_reproduces_the_uninterrupted_run(tmp_path):
 @pytest.mark.gpu
 def test_learned_warm_start_state_round_trip(tmp_path):
     from pymoto_gb300.learned import LearnedWarmStart
-    a = LearnedWarmStart((16, 8, 8), seed=1)
-    b = LearnedWarmStart((16, 8, 8), seed=2)
+    a = LearnedWarmStart((32, 16, 16), seed=1)      # stride 4: voxel grid (8, 4, 4)
+    b = LearnedWarmStart((32, 16, 16), seed=2)
     a.rng.random()
     save_checkpoint(tmp_path / "l.npz", ws=a)
     load_checkpoint(tmp_path / "l.npz", ws=b)

@@ -14,7 +14,7 @@ from conftest import GOLDEN, ROOT
 sys.path.insert(0, GOLDEN)
 import make_golden  # noqa: E402
 
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(make_golden.REF, "pymoto")),
+pytestmark = pytest.mark.skipif(not make_golden.REF or not os.path.isdir(os.path.join(make_golden.REF, "pymoto")),
                                 reason="pyMOTO's sources are not available here")
 
 SCRIPT = textwrap.dedent('''
