@@ -14,16 +14,22 @@ pyMOTO's own path (oracle) on the host cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
-import argparse
-import json
 import os
-import statistics
-import subprocess
-import sys
-import threading
-import time
 
-import numpy as np
+# the CPU baseline and the reference arm use every host core (numpy/scipy BLAS and OpenMP pools are sized at
+# import, so this precedes the numpy import)
+for _v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+    os.environ.setdefault(_v, str(os.cpu_count() or 1))
+
+import argparse  # noqa: E402
+import json  # noqa: E402
+import statistics  # noqa: E402
+import subprocess  # noqa: E402
+import sys  # noqa: E402
+import threading  # noqa: E402
+import time  # noqa: E402
+
+import numpy as np  # noqa: E402
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -63,9 +69,11 @@ def parse():
     ap.add_argument("--mma-iters", type=int, default=100, help="MMA iterations of --case mma_run")
     ap.add_argument("--pretrain", type=int, default=256,
                     help="smoothed-noise fields the learned warm start sees before --case mma_run")
-    ap.add_argument("--arms", default="plain_fp64,mixed,mixed_learned",
-                    help="plain_fp64 (the reference's method), mixed, mixed_learned (headline: with the learned "
-                         "warm start), ablations: mixed_jacobi, plain_fp64_cheb")
+    ap.add_argument("--arms", default="plain_fp64,plain_fp64_cheb,mixed,mixed_learned",
+                    help="plain_fp64 (the reference's method), plain_fp64_cheb (its smoother ablation: FP64 with "
+                         "the mixed arm's Chebyshev smoother), mixed, mixed_learned (headline: with the learned "
+                         "warm start), ablation mixed_jacobi")
+    ap.add_argument("--cpu-steps", type=int, default=5, help="warm design iterations of the CPU baseline (median)")
     return ap.parse_args()
 
 
@@ -176,6 +184,48 @@ class DesignRun:
     def step(self):
         self.oc.step()
         self.iters.append(self.solver.iterations)
+
+
+def design_solution(arm, shape, x, tol, torch, pg):
+    """c, u, dc/dx (host arrays) of one design x on the GPU: arm 'fp64' (CG + FP64 GMG, damped Jacobi 0.6, 2 sweeps,
+    the plain arm's solver) or 'mixed' (the mixed arm's solver); the true FP64 relative residual."""
+    o = DesignRun.opts
+    d = pg.VoxelDomain(*shape)
+    bc, f = cantilever(shape)
+    fd = torch.from_numpy(f).cuda()
+    sx = pg.Signal("x", torch.from_numpy(np.ascontiguousarray(x)).cuda())
+    mixed = arm == "mixed"
+    with pg.Network() as fn:
+        xf = pg.FilterConv(d, radius=RADIUS)(sx)
+        xs = pg.SIMP(xmin=XMIN, penal=PENAL)(xf)
+        K = pg.AssembleStiffness(d, bc=bc, sensitivity_precision="mixed" if mixed else "fp64")(xs)
+        if mixed:
+            mgs = pg.GeometricMultigrid.hierarchy(d, levels=o["levels"], smooth_steps=o["cheb_degree"], precision="fp32",
+                                                  coarse_smooth_steps=o["cheb_coarse_degree"], smoother="chebyshev",
+                                                  cheb_ratio=o["cheb_ratio"])
+            solver = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=tol, m=o["m"], inner_iters=o["inner_iters"],
+                                         inner_tol=o["inner_tol"])
+        else:
+            mgs = pg.GeometricMultigrid.hierarchy(d, levels=o["levels"], smoother_w=OMEGA, smooth_steps=o["sweeps"])
+            solver = pg.CG(preconditioner=mgs[0], tol=tol, maxit=10000)
+        lin = pg.LinSolve(hermitian=True, symmetric=True, solver=solver)
+        u = lin(K, fd)
+        c = pg.EinSum("i,i->")(u, fd)
+    fn.reset()
+    c.sensitivity = 1.0
+    fn.sensitivity()
+    res = pg.LinearSolver.residual(lin.A, lin._u_dev, fd)
+    return {"c": float(c.state), "u": u.state.cpu().numpy(), "dc": sx.sensitivity.cpu().numpy(), "residual": res,
+            "tol": tol}
+
+
+def parity_errors(sol, ref):
+    """Relative errors of a GPU solution against the oracle's: |c - c*| / |c*|, ||u - u*|| / ||u*||,
+    max |dc - dc*| / max |dc*|."""
+    return {"c": abs(sol["c"] - ref["c"]) / abs(ref["c"]),
+            "u": float(np.linalg.norm(sol["u"] - ref["u"]) / np.linalg.norm(ref["u"])),
+            "dc": float(np.abs(sol["dc"] - ref["dc"]).max() / np.abs(ref["dc"]).max()),
+            "gpu_true_rel_residual": sol["residual"], "gpu_tol": sol["tol"]}
 
 
 class ClockSampler:
@@ -383,12 +433,19 @@ def measure_gb300(args, rank, world, local_rank):
     c_m = float(torch.dot(mask, u_m).item())
     c_t = float(torch.dot(mask, u_t).item())
 
-    # end-to-end through the public API with host buffers (headline arm)
-    run = results[headline_arm(results)]["run"]
+    # end-to-end through the public API with host buffers, on the same designs as the timed region: a second run
+    # of the headline arm from the same seed replays the warm-up designs (every kernel and reduction is
+    # deterministic), then each timed step copies the step's design from pinned host memory to the device, runs
+    # the design iteration and copies the compliance and the new design back
+    H = headline_arm(results)
+    run = DesignRun(H, shape, seed=replica_seed(rank), torch=torch, pg=pg)
+    for _ in range(args.warmup):
+        run.step()
     nel = run.nel
     x_host = torch.empty(nel, dtype=torch.float64).pin_memory()
     x_host.copy_(run.sx.state.cpu())
     c_host = torch.empty(1, dtype=torch.float64).pin_memory()
+    run.iters.clear()
     barrier()
     torch.cuda.synchronize()
     e2e_durs = []
@@ -397,17 +454,26 @@ def measure_gb300(args, rank, world, local_rank):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         run.sx.state = x_host.to("cuda", non_blocking=True)          # H2D of the step's design
-        run.oc.step()
-        c_host.copy_(torch.tensor([float(run.c.state)]))               # compliance (already read on the host)
+        run.step()
+        c_host.copy_(run.c.state.reshape(1) if isinstance(run.c.state, torch.Tensor)
+                     else torch.tensor([float(run.c.state)]), non_blocking=True)   # D2H of the compliance
         x_host.copy_(run.sx.state, non_blocking=True)                  # D2H of the new design
         torch.cuda.synchronize()
         e2e_durs.append(time.perf_counter() - t0)
     e2e_total = slowest(sum(e2e_durs))
+    e2e_same = run.iters == results[H]["iters"]
 
+    # the first design of the timed runs (same seed) solved by both GPU solvers, for the oracle comparison of the
+    # CPU-baseline leg
+    design1 = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        x1 = np.random.default_rng(replica_seed(0)).uniform(1e-3, 1.0, int(np.prod(shape)))
+        design1 = {"x": x1, "fp64": design_solution("fp64", shape, x1, 1e-10, torch, pg),
+                   "mixed": design_solution("mixed", shape, x1, TOL, torch, pg)}
     kernels = kernel_rooflines(results[headline_arm(results)]["run"], flush, torch) if rank == 0 else None
     out = {"results": results, "shape": shape, "hbm_peak": hbm_peak, "peak_src": peak_src, "c_mixed": c_m,
-           "c_tight": c_t, "e2e_total_s": e2e_total, "nel": nel, "res_mixed_same_design": ms.last_residual,
-           "kernels": kernels, "peaks": peaks}
+           "c_tight": c_t, "e2e_total_s": e2e_total, "e2e_same_designs": e2e_same, "e2e_iters": list(run.iters), "nel": nel, "res_mixed_same_design": ms.last_residual,
+           "kernels": kernels, "peaks": peaks, "design1": design1}
     if args.profile_breakdown and rank == 0:
         run = DesignRun("mixed", shape, seed=99, torch=torch, pg=pg)
         for _ in range(2):
@@ -421,19 +487,19 @@ def measure_gb300(args, rank, world, local_rank):
     return out
 
 
-def cpu_reference_sample(shape, warm_steps=1, budget_s=None):
-    """Time warm design iterations of the CPU restatement (one cold iteration first, untimed)."""
+def cpu_reference_sample(shape, warm_steps=1, warmup=1, seed=1234):
+    """Time `warm_steps` design iterations of the CPU restatement after `warmup` untimed ones (the first is the
+    cold solve), from the GPU arms' initial design (same seed)."""
     import oracle
     L = oracle.ReferenceDesignLoop(shape, radius=RADIUS, levels=REF_LEVELS, w=OMEGA, smooth_steps=SWEEPS, tol=TOL,
-                                   move=MOVE)
-    L.step()                       # cold solve, untimed
+                                   move=MOVE, seed=seed)
+    for _ in range(max(1, warmup)):
+        L.step()                   # cold solve and warm-up, untimed
     times = []
     for _ in range(warm_steps):
         t0 = time.perf_counter()
         L.step()
         times.append(time.perf_counter() - t0)
-        if budget_s is not None and sum(times) > budget_s:
-            break
     return times, L
 
 
@@ -616,17 +682,21 @@ def main():
         if rank != 0:
             return
         shape = SHAPE if args.shape is None else tuple(int(v) for v in args.shape.split("x"))
-        times, L = cpu_reference_sample(shape, warm_steps=max(1, args.steps), budget_s=150.0)
+        times, L = cpu_reference_sample(shape, warm_steps=max(1, args.steps), warmup=args.warmup,
+                                        seed=replica_seed(0))
         per = statistics.mean(times)
         line = {"metric": METRIC, "value": 1.0 / per, "unit": "design it/s", "impl": "reference", "n_gpus": args.gpus,
-                "steps": len(times), "warmup": 1, "ms_per_step": per * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded U(1e-3,1) density)",
+                "steps": len(times), "warmup": max(1, args.warmup), "ms_per_step": per * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded U(1e-3,1) density, the GPU arms' seed)",
                 "config": {"workload": f"3D cantilever hex8 {shape[0]}x{shape[1]}x{shape[2]}, FilterConv r=2.5, "
                                        f"SIMP p=3, CG+GMG {REF_LEVELS} levels (SuperLU coarsest), tol 1e-6, OC"},
                 "cpu_baseline": {"value": 1.0 / per, "unit": "design it/s", "cores": threads, "kind": "port",
-                                 "sample": f"{len(times)} warm design iteration(s) after 1 cold one; numpy/scipy "
-                                           f"restatement of pyMOTO's path (assembly by add.at, SpGEMM Galerkin, "
-                                           f"SuperLU coarsest, CG)"},
+                                 "sample": f"design iterations {max(1, args.warmup) + 1}..{max(1, args.warmup) + len(times)} "
+                                           f"of the run (the same designs the GPU arms time), after "
+                                           f"{max(1, args.warmup)} untimed; numpy/scipy restatement of pyMOTO's path "
+                                           f"(assembly by add.at, SpGEMM Galerkin, SuperLU coarsest, CG), "
+                                           f"OMP/OPENBLAS threads = {os.environ.get('OMP_NUM_THREADS')}"},
                 "e2e": {"value": 1.0 / per, "unit": "design it/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "cg_iterations": L.solver.cg_iterations}
         print(json.dumps(line))
@@ -669,11 +739,27 @@ def main():
                          "hbm_gbs": ks["bytes"] / ks["s"] / 1e9, "peak_source": "nominal 2 FP64 FMA/clk/SM x SMs x "
                                                                                 "max SM clock"}
         cpu = None
+        parity_oracle = None
         if not args.no_cpu_baseline and world == 1:
-            times, L = cpu_reference_sample(shape, warm_steps=1)
-            cpu = {"value": 1.0 / statistics.mean(times), "unit": "design it/s", "cores": os.cpu_count(),
-                   "kind": "port", "sample": "1 warm design iteration of the same workload (after 1 cold one) with "
-                                             "the numpy/scipy restatement of pyMOTO's path, 4-level CG+GMG"}
+            times, L = cpu_reference_sample(shape, warm_steps=args.cpu_steps, warmup=1, seed=replica_seed(0))
+            cpu = {"value": 1.0 / statistics.median(times), "unit": "design it/s", "cores": os.cpu_count(),
+                   "kind": "port", "median_s": statistics.median(times), "times_s": times,
+                   "sample": f"median of {len(times)} warm design iterations (iterations 2..{len(times) + 1} of the "
+                             f"same seeded workload, after 1 cold one) with the numpy/scipy restatement of pyMOTO's "
+                             f"path, 4-level CG+GMG, OMP/OPENBLAS threads = {os.environ.get('OMP_NUM_THREADS')}"}
+            if m["design1"] is not None:
+                # the oracle as the checker: pyMOTO's FP64 CG + GMG to a relative residual of 1e-12 on the first
+                # design, against both GPU solvers' solutions of it
+                import oracle
+                t0 = time.perf_counter()
+                ref = oracle.fp64_cg_reference(shape, m["design1"]["x"], radius=RADIUS, levels=REF_LEVELS, w=OMEGA,
+                                               smooth_steps=SWEEPS, tol=1e-12)
+                parity_oracle = {"design": "the first design of the timed runs (seeded U(1e-3, 1))",
+                                 "oracle": f"FP64 CG + GMG ({REF_LEVELS} levels) to recursive relative residual 1e-12, "
+                                           f"{ref['iterations']} iterations, true relative residual "
+                                           f"{ref['residual']:.3e}, {time.perf_counter() - t0:.1f} s on the host",
+                                 "fp64": parity_errors(m["design1"]["fp64"], ref),
+                                 "mixed": parity_errors(m["design1"]["mixed"], ref)}
         e2e_val = aggregate_rate(world, steps, m["e2e_total_s"])
         launches = R[H]["probe"].launches
         line = {"metric": METRIC, "value": val_head, "unit": "design it/s", "n_gpus": world, "steps": steps,
@@ -706,9 +792,14 @@ def main():
                 "parity": {"same_design_compliance_mixed": m["c_mixed"], "same_design_compliance_fp64_tol1e-11":
                            m["c_tight"], "rel_diff": abs(m["c_mixed"] - m["c_tight"]) / abs(m["c_tight"]),
                            "mixed_true_rel_residual": m["res_mixed_same_design"]},
+                "parity_vs_oracle": parity_oracle,
                 "roofline": roofline, "roofline_fp64_stencil": roofline_fp64, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": "design it/s", "h2d_bytes_per_step": 8 * m["nel"],
-                        "d2h_bytes_per_step": 8 * m["nel"] + 8},
+                        "d2h_bytes_per_step": 8 * m["nel"] + 8, "arm": H,
+                        "same_designs_as_value": m["e2e_same_designs"],
+                        "note": "a second run of the headline arm from the same seed, the same warm-up, then the "
+                                "same designs with the design vector copied host->device and the compliance and "
+                                "new design device->host every step (pinned buffers), wall clock per step"},
                 "gpu_launches": launches, "clocks": R[H]["clocks"]}
         if "breakdown" in m:
             print(json.dumps({"breakdown": {"|".join(map(str, k)): v for k, v in sorted(

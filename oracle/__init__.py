@@ -19,4 +19,5 @@ Parity pin: the oracle is checked against golden vectors written by running pyMO
 tension, prolongation row sums, filter stencil placement).
 """
 from .pymoto_oracle import *  # noqa: F401,F403
-from .design_loop import CachedHierarchy, ReferenceDesignLoop, StructuredCSR  # noqa: F401,E402
+from .design_loop import (CachedHierarchy, ReferenceDesignLoop, StructuredCSR, cantilever_loads,  # noqa: F401,E402
+                          fp64_cg_reference)

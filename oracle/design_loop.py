@@ -14,12 +14,12 @@ Restates how pyMOTO runs one design iteration of the multigrid compliance exampl
 import numpy as np
 import scipy.sparse as sps
 
-from .pymoto_oracle import (Grid, LinSolveOracle, MGLevel, conv_filter, conv_filter_T, conv_filter_weights,
-                            default_bcdiagval, element_stiffness, oc_step, prolongation, sensitivity_contract, simp,
-                            simp_derivative)
+from .pymoto_oracle import (Grid, LinSolveOracle, MGLevel, cg_solve, conv_filter, conv_filter_T,
+                            conv_filter_weights, default_bcdiagval, element_stiffness, oc_step, prolongation,
+                            relative_residual, sensitivity_contract, simp, simp_derivative, vcycle)
 from scipy.sparse.linalg import splu
 
-__all__ = ["StructuredCSR", "CachedHierarchy", "ReferenceDesignLoop"]
+__all__ = ["StructuredCSR", "CachedHierarchy", "ReferenceDesignLoop", "cantilever_loads", "fp64_cg_reference"]
 
 
 class StructuredCSR:
@@ -190,3 +190,36 @@ class ReferenceDesignLoop:
         dx = conv_filter_T(g, self.W, dxs * simp_derivative(xf))
         self.x = oc_step(x, dx, self.volfrac, move=self.move)
         return c
+
+
+def cantilever_loads(grid):
+    """The cantilever of the examples: face i = 0 clamped (all components), unit -y load at the middle node of
+    the face i = nelx (examples/topology_optimization/ex_compliance_multigrid.py:81-100)."""
+    g = grid
+    nodes = g.nodes_where(i=0)
+    bc = (nodes[:, None] * g.dim + np.arange(g.dim)).ravel()
+    f = np.zeros(g.ndof)
+    tip = g.node_number(g.nelx, g.nely // 2, g.nelz // 2)
+    f[g.dim * tip + 1] = -1.0
+    return bc, f
+
+
+def fp64_cg_reference(shape, x, radius=2.5, levels=4, w=0.6, smooth_steps=2, tol=1e-12, maxit=5000):
+    """pyMOTO's FP64 path for one design of the cantilever: FilterConv (filter.py:8-220), SIMP, assembly
+    (assembly.py:245-296), CG (iterative.py:295-403) preconditioned by the geometric multigrid V-cycle
+    (iterative.py:124-256, damped Jacobi, SuperLU on the coarsest level) until the recursive relative residual
+    is below `tol`, the compliance f.u and its adjoint sensitivity dc/dx (assembly.py:298-315, the filter's
+    transpose).  Returns a dict with c, u, dc, the true relative residual and the CG iteration count."""
+    g = Grid(*shape)
+    bc, f = cantilever_loads(g)
+    K0 = element_stiffness(g)
+    W = conv_filter_weights(g, radius)
+    xf = conv_filter(g, W, x)
+    xs = simp(xf)
+    K = StructuredCSR(g, K0, bc).assemble(xs)
+    hier = CachedHierarchy(g, levels, w, smooth_steps).update(K)
+    u, it, _ = cg_solve(K, f, lambda r: vcycle(hier[0], r), None, tol, maxit, 50)
+    res = relative_residual(K, u, f)
+    dxs = sensitivity_contract(g, K0, [-u], [u], bc)
+    dc = conv_filter_T(g, W, dxs * simp_derivative(xf))
+    return {"c": float(f @ u), "u": u, "dc": dc, "residual": float(res), "iterations": int(it) + 1, "bc": bc, "f": f}

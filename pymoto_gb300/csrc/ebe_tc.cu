@@ -46,7 +46,8 @@ constexpr int RING = 5;       // node layers t, t + 1 in use, t + 2 and t + 3 in
 constexpr int PFN = (PLANE + NTHREADS - 1) / NTHREADS;  // staged nodes per thread: 2
 constexpr int TMEM_COLS = 256;               // 2 warpgroups x (A 48 + D 48) = 192, rounded to a power of 2
 constexpr int COLS_PER_WG = 96;
-constexpr uint32_t WAIT_LIMIT = 1u << 22;
+constexpr uint32_t WAIT_LIMIT = 1u << 14;   // polls of at most WAIT_HINT_NS each: about a second in all
+constexpr uint32_t WAIT_HINT_NS = 65536;
 
 struct TcSmem {
   float B[48 * 48];               // K-major, no swizzle: core matrix (n/8, k/4) at (n/8)*1536 + (k/4)*128 bytes
@@ -125,10 +126,11 @@ __device__ __forceinline__ bool mbar_wait(const unsigned long long* bar, uint32_
   const uint32_t a = smem_u32(bar);
   for (uint32_t it = 0; it < WAIT_LIMIT; ++it) {
     uint32_t done;
+    // the thread sleeps in the hardware until the phase completes or the hint expires: no busy polling
     asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}"
         : "=r"(done)
-        : "r"(a), "r"(parity)
+        : "r"(a), "r"(parity), "r"(WAIT_HINT_NS)
         : "memory");
     if (done) return true;
   }
@@ -183,7 +185,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
 
-  // staging slots of this thread (layer independent)
+  // staging slots of this thread (layer independent): position in the staged tile and node index in its layer
   int gnode[PFN], spos[PFN];
 #pragma unroll
   for (int s = 0; s < PFN; ++s) {
@@ -205,13 +207,17 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     const int ku = kz0 - 1 + s, kx = ku;
     const bool uok = ku >= 0 && ku < nnz, xok = kx >= 0 && kx < g.nz;
     const int slot = s % RING;
+    const int64_t lbase = uok ? (int64_t)ku * nlayer : 0;
 #pragma unroll
     for (int q = 0; q < PFN; ++q) {
       if (spos[q] < 0) continue;
       const bool live = uok && gnode[q] >= 0;
-      const int64_t m = live ? ku * nlayer + gnode[q] : 0;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) cp_async4(&S.u[slot][c][spos[q]], u + m * 3 + c, live ? 4 : 0);
+      const int64_t m = live ? lbase + gnode[q] : 0;
+      const float* src = u + 3 * m;
+      const int nb = live ? 4 : 0;
+      cp_async4(&S.u[slot][0][spos[q]], src, nb);
+      cp_async4(&S.u[slot][1][spos[q]], src + 1, nb);
+      cp_async4(&S.u[slot][2][spos[q]], src + 2, nb);
       if (bcmask) {
         const int64_t wd = m & ~int64_t(3);
         const int64_t left = nn_total - wd;
@@ -322,7 +328,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
         const float v = a[q] - a[q % 3];
         const float hi = tf32_rna(v);
         a[q] = hi;
-        a[24 + q] = tf32_rna(v - hi);
+        a[24 + q] = v - hi;          // exact in FP32; the tensor core reads its leading TF32 bits
       }
       tmem_st16(colA + lane_sel, a);
       tmem_st16(colA + lane_sel + 16, a + 16);

@@ -3,8 +3,9 @@
 //
 // Layout: channels-last, act[v][c] with v = (k*ny + j)*nx + i.  Activations and weights are stored as
 // BF16, gradients and accumulators are FP32, master weights FP32 (Adam).  3x3x3 convolutions with zero
-// padding; weights w[tap][cin][cout], tap = (dz+1)*9 + (dy+1)*3 + (dx+1).  Weight gradients are summed
-// over fixed voxel chunks and then over the chunks in order, so every result is deterministic.
+// padding; weights w[tap][cin][cout], tap = (dz+1)*9 + (dy+1)*3 + (dx+1).  The convolutions run on the
+// tensor cores (BF16 mma.sync, FP32 accumulation).  Weight gradients are summed over fixed voxel chunks and
+// then over the chunks in order, so every result is deterministic.
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -27,80 +28,240 @@ __device__ __forceinline__ void vox_ijk(const VGrid& g, int v, int& i, int& j, i
 __device__ __forceinline__ float ld(const __nv_bfloat16* p) { return __bfloat162float(*p); }
 __device__ __forceinline__ float ld(const float* p) { return *p; }
 
-// out[v][co] = bias[co] + sum_{tap, ci} w[tap][ci][co] in[v + tap][ci]  (+ ReLU).  One thread per (v, co),
-// co fastest: the input values of a voxel are broadcast across the warp, the weights coalesced.
-template <typename TIN>
-__global__ void conv3d_fwd_kernel(VGrid g, int cin, int cout, const TIN* __restrict__ in,
-                                  const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias, int relu,
-                                  __nv_bfloat16* __restrict__ out_bf, float* __restrict__ out_f) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= g.nvox() * cout) return;
-  const int co = (int)(t % cout);
-  const int v = (int)(t / cout);
-  int i, j, k;
-  vox_ijk(g, v, i, j, k);
-  float acc = bias ? bias[co] : 0.f;
-  for (int tap = 0; tap < 27; ++tap) {
-    const int ii = i + tap % 3 - 1, jj = j + (tap / 3) % 3 - 1, kk = k + tap / 9 - 1;
-    if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || kk < 0 || kk >= g.nz) continue;
-    const TIN* src = in + ((int64_t)(kk * g.ny + jj) * g.nx + ii) * cin;
-    const __nv_bfloat16* wt = w + (int64_t)tap * cin * cout + co;
-    for (int ci = 0; ci < cin; ++ci) acc = fmaf(ld(src + ci), __bfloat162float(wt[(int64_t)ci * cout]), acc);
-  }
-  if (relu) acc = fmaxf(acc, 0.f);
-  if (out_bf) out_bf[t] = __float2bfloat16(acc);
-  if (out_f) out_f[t] = acc;
+// The three convolution products are implicit GEMMs on the tensor cores (mma.sync m16n8k16, BF16 operands,
+// FP32 accumulation); each warp owns a 16-row tile of the output and all of its columns:
+//   forward: out[v][co]  = bias[co] + sum_k A[v][k] W[k][co],  A[v][k] = in[v + off(tap)][ci],  k = tap*cin + ci
+//   data:    din[v][ci]  = sum_k' D[v][k'] W'[k'][ci],  D[v][k'] = dout[v - off(tap)][co],  k' = tap*cout + co,
+//                          W'[k'][ci] = w[tap][ci][co]
+//   weights: dW[k][co]   = sum_v A[v][k] dout[v][co] over a chunk of voxels (the bias gradient is the extra row
+//                          k = 27*cin with A = 1); chunks summed in order afterwards (deterministic).
+// FP32 operands (FP32 network input, the FP32 gradients) are rounded to BF16 when the fragments are built.
+constexpr int CONV_WARPS = 4;
+
+__device__ __forceinline__ float ldf(const __nv_bfloat16* p, int64_t i) { return __bfloat162float(p[i]); }
+__device__ __forceinline__ float ldf(const float* p, int64_t i) { return p[i]; }
+
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);     // .x (lower 16 bits) = lo
+  return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// din[v][ci] = sum_{tap, co} w[tap][ci][co] dout[v - tap][co]  (dout already masked by the ReLU).
-__global__ void conv3d_dgrad_kernel(VGrid g, int cin, int cout, const float* __restrict__ dout,
-                                    const __nv_bfloat16* __restrict__ w, float* __restrict__ din) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= g.nvox() * cin) return;
-  const int ci = (int)(t % cin);
-  const int v = (int)(t / cin);
-  int i, j, k;
-  vox_ijk(g, v, i, j, k);
-  float acc = 0.f;
-  for (int tap = 0; tap < 27; ++tap) {
-    const int ii = i - (tap % 3 - 1), jj = j - ((tap / 3) % 3 - 1), kk = k - (tap / 9 - 1);
-    if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || kk < 0 || kk >= g.nz) continue;
-    const float* src = dout + ((int64_t)(kk * g.ny + jj) * g.nx + ii) * cout;
-    const __nv_bfloat16* wt = w + ((int64_t)tap * cin + ci) * cout;
-    for (int co = 0; co < cout; ++co) acc = fmaf(src[co], __bfloat162float(wt[co]), acc);
-  }
-  din[t] = acc;
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// Partial weight gradients over a chunk of voxels: part[chunk][tap*cin*cout + ci*cout + co] (and the
-// bias gradient in the last cout entries).  Deterministic: the chunks are summed in order afterwards.
+// value of the voxel (i, j, k) + (dx, dy, dz) or -1 outside the grid
+__device__ __forceinline__ int neighbour(const VGrid& g, int i, int j, int k, int dx, int dy, int dz) {
+  const int ii = i + dx, jj = j + dy, kk = k + dz;
+  if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || kk < 0 || kk >= g.nz) return -1;
+  return (kk * g.ny + jj) * g.nx + ii;
+}
+
+// im2col element: x[nb(v, tap) * c + ch] for column q = tap * c + ch of voxel (i, j, k); sign -1 mirrors the tap
+template <typename T>
+__device__ __forceinline__ float im2col(const VGrid& g, const T* __restrict__ x, int c, int q, int qmax, bool ok,
+                                        int i, int j, int k, int sign) {
+  if (!ok || q >= qmax) return 0.f;
+  const int tap = q / c, ch = q - tap * c;
+  const int nb = neighbour(g, i, j, k, sign * (tap % 3 - 1), sign * ((tap / 3) % 3 - 1), sign * (tap / 9 - 1));
+  return nb < 0 ? 0.f : ldf(x, (int64_t)nb * c + ch);
+}
+
+template <typename TIN, int NT>
+__global__ void __launch_bounds__(32 * CONV_WARPS)
+    conv3d_fwd_kernel(VGrid g, int cin, int cout, const TIN* __restrict__ in, const __nv_bfloat16* __restrict__ w,
+                      const float* __restrict__ bias, int relu, __nv_bfloat16* __restrict__ out_bf,
+                      float* __restrict__ out_f) {
+  const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
+  const int64_t v0 = ((int64_t)blockIdx.x * CONV_WARPS + (threadIdx.x >> 5)) * 16;
+  const int64_t nv = g.nvox();
+  if (v0 >= nv) return;
+  int r[2], ci[2], cj[2], ck[2];
+  bool ok[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    r[h] = (int)(v0 + gid + 8 * h);
+    ok[h] = r[h] < nv;
+    vox_ijk(g, ok[h] ? r[h] : 0, ci[h], cj[h], ck[h]);
+  }
+  const int K = 27 * cin;
+  float c[NT][4];
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    uint32_t a[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {        // a0: row gid, cols 2tig..; a1: row gid+8; a2, a3: cols + 8
+      const int h = q & 1, col = k0 + 2 * tig + 8 * (q >> 1);
+      a[q] = pack2(im2col(g, in, cin, col, K, ok[h], ci[h], cj[h], ck[h], 1),
+                   im2col(g, in, cin, col + 1, K, ok[h], ci[h], cj[h], ck[h], 1));
+    }
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+      const int n = nt * 8 + gid;
+      float bw[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int kk = k0 + 2 * tig + (q & 1) + 8 * (q >> 1);
+        bw[q] = (kk < K && n < cout) ? __bfloat162float(w[(int64_t)kk * cout + n]) : 0.f;
+      }
+      mma_bf16(c[nt], a, pack2(bw[0], bw[1]), pack2(bw[2], bw[3]));
+    }
+  }
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int h = q >> 1, n = nt * 8 + 2 * tig + (q & 1);
+      if (!ok[h] || n >= cout) continue;
+      float v = c[nt][q] + (bias ? bias[n] : 0.f);
+      if (relu) v = fmaxf(v, 0.f);
+      const int64_t o = (int64_t)r[h] * cout + n;
+      if (out_bf) out_bf[o] = __float2bfloat16(v);
+      if (out_f) out_f[o] = v;
+    }
+}
+
+// din[v][ci] = sum_{tap, co} w[tap][ci][co] dout[v - off(tap)][co]  (dout already masked by the ReLU)
+template <int NT>
+__global__ void __launch_bounds__(32 * CONV_WARPS)
+    conv3d_dgrad_kernel(VGrid g, int cin, int cout, const float* __restrict__ dout, const __nv_bfloat16* __restrict__ w,
+                        float* __restrict__ din) {
+  const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
+  const int64_t v0 = ((int64_t)blockIdx.x * CONV_WARPS + (threadIdx.x >> 5)) * 16;
+  const int64_t nv = g.nvox();
+  if (v0 >= nv) return;
+  int r[2], ci[2], cj[2], ck[2];
+  bool ok[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    r[h] = (int)(v0 + gid + 8 * h);
+    ok[h] = r[h] < nv;
+    vox_ijk(g, ok[h] ? r[h] : 0, ci[h], cj[h], ck[h]);
+  }
+  const int K = 27 * cout;
+  float c[NT][4];
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    uint32_t a[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int h = q & 1, col = k0 + 2 * tig + 8 * (q >> 1);
+      a[q] = pack2(im2col(g, dout, cout, col, K, ok[h], ci[h], cj[h], ck[h], -1),
+                   im2col(g, dout, cout, col + 1, K, ok[h], ci[h], cj[h], ck[h], -1));
+    }
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+      const int n = nt * 8 + gid;                 // input channel
+      float bw[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int kk = k0 + 2 * tig + (q & 1) + 8 * (q >> 1);    // tap * cout + co
+        float v = 0.f;
+        if (kk < K && n < cin) {
+          const int tap = kk / cout, co = kk - tap * cout;
+          v = __bfloat162float(w[((int64_t)tap * cin + n) * cout + co]);
+        }
+        bw[q] = v;
+      }
+      mma_bf16(c[nt], a, pack2(bw[0], bw[1]), pack2(bw[2], bw[3]));
+    }
+  }
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int h = q >> 1, n = nt * 8 + 2 * tig + (q & 1);
+      if (ok[h] && n < cin) din[(int64_t)r[h] * cin + n] = c[nt][q];
+    }
+}
+
+// Partial weight and bias gradients over a chunk of voxels: part[chunk][k * cout + co] for k < 27 cin (k =
+// tap * cin + ci) and part[chunk][27 cin cout + co] for the bias.  Warp: 16 rows k, all cout columns.
 constexpr int WG_CHUNK = 2048;
 
-template <typename TIN>
-__global__ void conv3d_wgrad_partial_kernel(VGrid g, int cin, int cout, const TIN* __restrict__ in,
-                                            const float* __restrict__ dout, float* __restrict__ part) {
-  const int nw = 27 * cin * cout + cout;
-  const int widx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (widx >= nw) return;
+template <typename TIN, int NT>
+__global__ void __launch_bounds__(32 * CONV_WARPS)
+    conv3d_wgrad_partial_kernel(VGrid g, int cin, int cout, const TIN* __restrict__ in, const float* __restrict__ dout,
+                                float* __restrict__ part) {
+  const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
+  const int rows = 27 * cin + 1;
+  const int m0 = (blockIdx.x * CONV_WARPS + (threadIdx.x >> 5)) * 16;
+  if (m0 >= rows) return;
   const int chunk = blockIdx.y;
-  const int64_t v0 = (int64_t)chunk * WG_CHUNK;
-  const int64_t v1 = min((int64_t)g.nvox(), v0 + WG_CHUNK);
-  float acc = 0.f;
-  if (widx < 27 * cin * cout) {
-    const int co = widx % cout, ci = (widx / cout) % cin, tap = widx / (cin * cout);
-    const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
-    for (int64_t v = v0; v < v1; ++v) {
-      int i, j, k;
-      vox_ijk(g, (int)v, i, j, k);
-      const int ii = i + dx, jj = j + dy, kk = k + dz;
-      if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || kk < 0 || kk >= g.nz) continue;
-      acc = fmaf(ld(in + ((int64_t)(kk * g.ny + jj) * g.nx + ii) * cin + ci), dout[v * cout + co], acc);
-    }
-  } else {
-    const int co = widx - 27 * cin * cout;
-    for (int64_t v = v0; v < v1; ++v) acc += dout[v * cout + co];
+  const int64_t nv = g.nvox();
+  const int64_t vbeg = (int64_t)chunk * WG_CHUNK;
+  const int64_t vend = min(nv, vbeg + WG_CHUNK);
+  // the two rows k of this thread: tap offsets and channel (bias row: always 1; beyond: 0)
+  int kind[2], ch[2], odx[2], ody[2], odz[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int kr = m0 + gid + 8 * h;
+    kind[h] = kr < 27 * cin ? 0 : (kr == 27 * cin ? 1 : 2);
+    const int tap = kind[h] == 0 ? kr / cin : 0;
+    ch[h] = kind[h] == 0 ? kr - tap * cin : 0;
+    odx[h] = tap % 3 - 1;
+    ody[h] = (tap / 3) % 3 - 1;
+    odz[h] = tap / 9 - 1;
   }
-  part[(int64_t)chunk * nw + widx] = acc;
+  float c[NT][4];
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.f;
+  for (int64_t vb = vbeg; vb < vend; vb += 16) {
+    // voxels of this thread's 4 K columns: 2tig, 2tig+1, 2tig+8, 2tig+9
+    int vi[4], vj[4], vk[4];
+    bool vok[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int64_t v = vb + 2 * tig + (q & 1) + 8 * (q >> 1);
+      vok[q] = v < vend;
+      vox_ijk(g, vok[q] ? (int)v : 0, vi[q], vj[q], vk[q]);
+    }
+    uint32_t a[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {          // a[q]: row gid + 8 (q & 1), columns 2tig + 8 (q >> 1) + {0, 1}
+      const int h = q & 1;
+      float e[2];
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        const int col = 2 * (q >> 1) + s;   // index into the 4 voxels of this thread
+        float val = 0.f;
+        if (vok[col]) {
+          if (kind[h] == 1) {
+            val = 1.f;
+          } else if (kind[h] == 0) {
+            const int nb = neighbour(g, vi[col], vj[col], vk[col], odx[h], ody[h], odz[h]);
+            val = nb < 0 ? 0.f : ldf(in, (int64_t)nb * cin + ch[h]);
+          }
+        }
+        e[s] = val;
+      }
+      a[q] = pack2(e[0], e[1]);
+    }
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+      const int n = nt * 8 + gid;
+      float bv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int64_t v = vb + 2 * tig + (q & 1) + 8 * (q >> 1);
+        bv[q] = (q < 4 && v < vend && n < cout) ? dout[v * cout + n] : 0.f;
+      }
+      mma_bf16(c[nt], a, pack2(bv[0], bv[1]), pack2(bv[2], bv[3]));
+    }
+  }
+  const int nw = 27 * cin * cout + cout;
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int kr = m0 + gid + 8 * (q >> 1), n = nt * 8 + 2 * tig + (q & 1);
+      if (kr < rows && n < cout) part[(int64_t)chunk * nw + (int64_t)kr * cout + n] = c[nt][q];
+    }
 }
 
 __global__ void sum_chunks_kernel(int nw, int nchunk, const float* __restrict__ part, float* __restrict__ out,
@@ -327,6 +488,30 @@ __global__ void inject_kernel(Grid gf, int stride, const double* __restrict__ uf
 using namespace pmg;
 using namespace pmg::nn;
 
+// output columns of the convolution kernels in tiles of 8, templated on the tile count (1, 2, 4, 8 or 12:
+// up to 96 channels)
+constexpr int CONV_MAX_NT = 12;
+#define CONV_NT_DISPATCH(c, ...)                      \
+  do {                                                \
+    const int nt_ = ((c) + 7) / 8;                    \
+    if (nt_ <= 1) {                                   \
+      constexpr int NT = 1;                           \
+      __VA_ARGS__;                                    \
+    } else if (nt_ <= 2) {                            \
+      constexpr int NT = 2;                           \
+      __VA_ARGS__;                                    \
+    } else if (nt_ <= 4) {                            \
+      constexpr int NT = 4;                           \
+      __VA_ARGS__;                                    \
+    } else if (nt_ <= 8) {                            \
+      constexpr int NT = 8;                           \
+      __VA_ARGS__;                                    \
+    } else {                                          \
+      constexpr int NT = 12;                          \
+      __VA_ARGS__;                                    \
+    }                                                 \
+  } while (0)
+
 static bool vgrid_ok(int nx, int ny, int nz) {
   return nx > 0 && ny > 0 && nz > 0 && (int64_t)nx * ny * nz < (int64_t(1) << 30);
 }
@@ -335,27 +520,35 @@ extern "C" {
 
 int pmg_nn_conv3d_forward(int nx, int ny, int nz, int cin, int cout, int in_is_f32, const void* in, const void* w,
                           const float* bias, int relu, void* out_bf16, float* out_f32, void* stream) {
-  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || !in || !w || (!out_bf16 && !out_f32)) return PMG_BAD_ARG;
+  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || cout > 8 * CONV_MAX_NT || !in || !w ||
+      (!out_bf16 && !out_f32))
+    return PMG_BAD_ARG;
   VGrid g{nx, ny, nz};
-  const int64_t work = g.nvox() * cout;
-  const unsigned blocks = blocks_for(work, 256);
+  const unsigned blocks = (unsigned)((g.nvox() + 16 * CONV_WARPS - 1) / (16 * CONV_WARPS));
   cudaStream_t st = as_stream(stream);
-  if (in_is_f32)
-    conv3d_fwd_kernel<float><<<blocks, 256, 0, st>>>(g, cin, cout, (const float*)in, (const __nv_bfloat16*)w, bias, relu,
-                                                     (__nv_bfloat16*)out_bf16, out_f32);
-  else
-    conv3d_fwd_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(g, cin, cout, (const __nv_bfloat16*)in,
-                                                             (const __nv_bfloat16*)w, bias, relu,
-                                                             (__nv_bfloat16*)out_bf16, out_f32);
+  const auto* wb = (const __nv_bfloat16*)w;
+  auto* ob = (__nv_bfloat16*)out_bf16;
+  CONV_NT_DISPATCH(cout, {
+    if (in_is_f32)
+      conv3d_fwd_kernel<float, NT><<<blocks, 32 * CONV_WARPS, 0, st>>>(g, cin, cout, (const float*)in, wb, bias, relu,
+                                                                       ob, out_f32);
+    else
+      conv3d_fwd_kernel<__nv_bfloat16, NT><<<blocks, 32 * CONV_WARPS, 0, st>>>(g, cin, cout, (const __nv_bfloat16*)in,
+                                                                               wb, bias, relu, ob, out_f32);
+  });
   return check_launch();
 }
 
 int pmg_nn_conv3d_backward_data(int nx, int ny, int nz, int cin, int cout, const float* dout, const void* w, float* din,
                                 void* stream) {
-  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || !dout || !w || !din) return PMG_BAD_ARG;
+  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || cin > 8 * CONV_MAX_NT || !dout || !w || !din)
+    return PMG_BAD_ARG;
   VGrid g{nx, ny, nz};
-  conv3d_dgrad_kernel<<<blocks_for(g.nvox() * cin, 256), 256, 0, as_stream(stream)>>>(g, cin, cout, dout,
-                                                                                    (const __nv_bfloat16*)w, din);
+  const unsigned blocks = (unsigned)((g.nvox() + 16 * CONV_WARPS - 1) / (16 * CONV_WARPS));
+  CONV_NT_DISPATCH(cin, {
+    conv3d_dgrad_kernel<NT><<<blocks, 32 * CONV_WARPS, 0, as_stream(stream)>>>(g, cin, cout, dout,
+                                                                              (const __nv_bfloat16*)w, din);
+  });
   return check_launch();
 }
 
@@ -367,17 +560,22 @@ size_t pmg_nn_wgrad_scratch_bytes(int nx, int ny, int nz, int cin, int cout) {
 
 int pmg_nn_conv3d_backward_weights(int nx, int ny, int nz, int cin, int cout, int in_is_f32, const void* in,
                                    const float* dout, float* dw_db, int accumulate, void* scratch, void* stream) {
-  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || !in || !dout || !dw_db || !scratch) return PMG_BAD_ARG;
+  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || cout > 8 * CONV_MAX_NT || !in || !dout || !dw_db || !scratch)
+    return PMG_BAD_ARG;
   VGrid g{nx, ny, nz};
   const int nw = 27 * cin * cout + cout;
   const int nchunk = (int)((g.nvox() + WG_CHUNK - 1) / WG_CHUNK);
+  const int mtiles = (27 * cin + 1 + 15) / 16;
   cudaStream_t st = as_stream(stream);
-  dim3 grid((nw + 127) / 128, nchunk);
-  if (in_is_f32)
-    conv3d_wgrad_partial_kernel<float><<<grid, 128, 0, st>>>(g, cin, cout, (const float*)in, dout, (float*)scratch);
-  else
-    conv3d_wgrad_partial_kernel<__nv_bfloat16><<<grid, 128, 0, st>>>(g, cin, cout, (const __nv_bfloat16*)in, dout,
-                                                                     (float*)scratch);
+  dim3 grid((mtiles + CONV_WARPS - 1) / CONV_WARPS, nchunk);
+  CONV_NT_DISPATCH(cout, {
+    if (in_is_f32)
+      conv3d_wgrad_partial_kernel<float, NT><<<grid, 32 * CONV_WARPS, 0, st>>>(g, cin, cout, (const float*)in, dout,
+                                                                               (float*)scratch);
+    else
+      conv3d_wgrad_partial_kernel<__nv_bfloat16, NT><<<grid, 32 * CONV_WARPS, 0, st>>>(
+          g, cin, cout, (const __nv_bfloat16*)in, dout, (float*)scratch);
+  });
   sum_chunks_kernel<<<(nw + 255) / 256, 256, 0, st>>>(nw, nchunk, (const float*)scratch, dw_db, accumulate);
   return check_launch();
 }

@@ -11,8 +11,9 @@ the previous solution alone; every solve is still driven to the same FP64 residu
 
 The network is trained on the device, online, on (stiffness field, displacement) pairs of the solves of
 earlier design iterations (and optionally of seeded random density fields), by the forward and backward
-kernels of libpymoto_gb300 (csrc/learned.cu) and an Adam update.  Targets are normalised to unit 2-norm:
-the Rayleigh-Ritz step picks the scale.
+kernels of libpymoto_gb300 (csrc/learned.cu: BF16 tensor-core convolutions) and an Adam update.  Targets are
+normalised to unit 2-norm: the Rayleigh-Ritz step picks the scale.  The training steps run on a side stream
+of their own, off the solver's critical path; the next prediction waits for them.
 """
 from __future__ import annotations
 
@@ -254,14 +255,26 @@ class LearnedWarmStart:
             g = (nx // s, ny // s, nz // s)
             self._levels.append((g, torch.zeros((g[0] + 1) * (g[1] + 1) * (g[2] + 1) * 3, **f64)))
         self.last_loss = None
+        # training runs on a side stream (lower priority than the solver's) after the pair it learns from is
+        # stored; the next forward pass waits for it
+        self.side_stream = torch.cuda.Stream(device=device, priority=0) if str(device).startswith("cuda") else None
+        self._trained = None
+
+    def sync_training(self):
+        """Order the current stream after the training steps issued so far."""
+        if self._trained is not None:
+            torch.cuda.current_stream().wait_event(self._trained)
+            self._trained = None
 
     def state_dict(self):
         """Network, training buffer, sample count, random state, gate and history (checkpoint)."""
+        self.sync_training()
         return {"net": self.net.state_dict(), "feats": self.feats, "targets": self.targets, "count": self.count,
                 "rng": self.rng.bit_generator.state, "skip": self._skip, "predictions": self.predictions,
                 "hist": list(self._hist)}
 
     def load_state_dict(self, sd):
+        self.sync_training()
         self.net.load_state_dict(sd["net"])
         self.feats.copy_(sd["feats"].to(self.feats.device))
         self.targets.copy_(sd["targets"].to(self.targets.device))
@@ -279,6 +292,7 @@ class LearnedWarmStart:
 
     def predict(self, A):
         """FP64 prediction of the fine nodal displacement for the operator A (not masked, arbitrary scale)."""
+        self.sync_training()
         self._features(A._xe64 if A._xe64 is not None else A.xe, self.net.feat)
         self.net.forward()
         call("pmg_nn_vox_to_node", 0, *self.vgrid, self.net.out, self._pred, stream())
@@ -312,7 +326,8 @@ class LearnedWarmStart:
             self._skip = self.gate_skip
 
     def observe(self, A, u):
-        """Store the pair (stiffness field of A, solution u) and train on the stored pairs."""
+        """Store the pair (stiffness field of A, solution u) and train on the stored pairs (side stream)."""
+        self.sync_training()          # the training buffer is written below; earlier steps may still read it
         if self.history > 0:
             keep = self._hist[:self.history + 1]
             buf = keep.pop() if len(keep) == self.history + 1 else torch.empty_like(u)
@@ -329,9 +344,22 @@ class LearnedWarmStart:
         call("pmg_dot", F64, self.ncn, t, t, self._sc[0:1], ws.reduce, stream())
         call("pmg_scale_rsqrt", F64, self.ncn, t, t, self._sc[0:1], stream())   # unit 2-norm
         self.count += 1
-        if (self.count - 1) % self.train_every == 0:
-            for _ in range(self.train_steps):
-                self.train_step(int(self.rng.integers(min(self.count, self.capacity))))
+        if (self.count - 1) % self.train_every == 0 and self.train_steps > 0:
+            slots = [int(self.rng.integers(min(self.count, self.capacity))) for _ in range(self.train_steps)]
+            if self.side_stream is None:
+                for sl in slots:
+                    self.train_step(sl)
+                return
+            stored = torch.cuda.Event()
+            stored.record()                             # the new pair is in the buffer
+            if self._trained is not None:               # previous training steps (same network buffers)
+                self.side_stream.wait_event(self._trained)
+            self.side_stream.wait_event(stored)
+            with torch.cuda.stream(self.side_stream):
+                for sl in slots:
+                    self.train_step(sl)
+                self._trained = torch.cuda.Event()
+                self._trained.record()
 
     def train_step(self, slot):
         net = self.net
@@ -345,6 +373,7 @@ class LearnedWarmStart:
 
     def loss(self):
         """Sum of the squared errors of the last training step (host synchronisation)."""
+        self.sync_training()
         return float(self._loss.sum().item())
 
 

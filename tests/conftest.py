@@ -30,12 +30,13 @@ def clamp_face_dofs(grid):
     return (nodes[:, None] * grid.dim + np.arange(grid.dim)).ravel()
 
 
-# The hot path's parity files (and MMA, VTI) run first, the other next rows and the auxiliary subsystems after
-# them, so that with -x a failure in one of the later rows does not hide the hot path's results;
+# The hot path's kernel and pipeline parity files (and MMA, VTI) run first, the other next rows and the
+# auxiliary subsystems after them, then the parity at the benchmark sizes (the slowest file: its oracle solves
+# a 1.6M-dof system on the host), so that with -x a failure in a later file does not hide the earlier results;
 # test_zz_no_alloc stays last.
 _LATER = ("test_filter_variants", "test_mass", "test_poisson", "test_overhang", "test_math_expression",
           "test_scalars", "test_einsum", "test_routines", "test_design_runs", "test_checkpoint", "test_faults",
-          "test_zz_no_alloc")
+          "test_config_parity", "test_zz_no_alloc")
 
 
 def pytest_collection_modifyitems(session, config, items):
