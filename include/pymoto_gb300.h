@@ -65,13 +65,15 @@ int pmg_dof_connectivity(int nelx, int nely, int nelz, int64_t* dofconn, void* s
 /* ---- matrix-free stiffness operator K(x) = sum_e x_e K0 (Dirichlet rows/cols -> bcdiag) --------
  * Replaces AssembleGeneral.__call__ (pymoto/modules/assembly.py:245-296) followed by the CSR products
  * of CG and GeometricMultigrid (pymoto/solvers/iterative.py:236-255, :375) and the damped-Jacobi
- * smoother (pymoto/solvers/iterative.py:41-47).  u, b, diag, y: ndof; xe: nel. */
+ * smoother (pymoto/solvers/iterative.py:41-47).  u, b, diag, y: ndof; xe: nel.  cdiag (ndof, or NULL): a
+ * constant diagonal added to the operator after the Dirichlet rows are set, the diagonal add_constant of
+ * AssembleGeneral (pymoto/modules/assembly.py:294-295): a Dirichlet row holds bcdiag + cdiag. */
 int pmg_ebe_apply(int mode, int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
                   const uint8_t* bcmask, double bcdiag, const void* u, const void* b, const void* diag,
-                  double omega, void* y, void* stream);
-/* diag(K(x)), replaces A.diagonal() of DampedJacobi.update (pymoto/solvers/iterative.py:38-39). */
+                  double omega, void* y, const void* cdiag, void* stream);
+/* diag(K(x)) (+ cdiag), replaces A.diagonal() of DampedJacobi.update (pymoto/solvers/iterative.py:38-39). */
 int pmg_ebe_diagonal(int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
-                     const uint8_t* bcmask, double bcdiag, void* diag, void* stream);
+                     const uint8_t* bcmask, double bcdiag, void* diag, const void* cdiag, void* stream);
 
 /* ---- assembled node-stencil operator of the coarse multigrid levels ---------------------------
  * The operators are symmetric, so S holds per node only the centre block and the blocks of the forward
@@ -84,6 +86,9 @@ int pmg_ebe_diagonal(int dtype, int nelx, int nely, int nelz, const void* xe, co
 int pmg_stencil_apply(int mode, int dtype, int nelx, int nely, int nelz, const void* S, const void* u,
                       const void* b, const void* diag, double omega, void* y, void* stream);
 int pmg_stencil_diagonal(int dtype, int nelx, int nely, int nelz, const void* S, void* diag, void* stream);
+/* Centre-block diagonal of S += c (ndof): a constant diagonal (add_constant, pymoto/modules/assembly.py:294-295)
+ * on the level-0 stencils, and its restriction R^T c (a lumped Galerkin term) on the coarse levels. */
+int pmg_stencil_add_diagonal(int dtype, int nelx, int nely, int nelz, void* S, const void* c, void* stream);
 
 /* ---- grid transfers (trilinear / bilinear prolongation R of pymoto/solvers/iterative.py:178-220) --
  * Grid arguments are the FINE grid.  rc = R^T rf (iterative.py:244);  uf += R uc (iterative.py:250). */
@@ -142,7 +147,7 @@ int pmg_stencil_cheb_step(int dtype, int nelx, int nely, int nelz, const void* S
 /* The same on the matrix-free FP32 3D level-0 operator (tensor-core kernel of pmg_ebe_apply). */
 int pmg_ebe_cheb_step(int nelx, int nely, int nelz, const float* xe, const double* K0_host, const uint8_t* bcmask,
                       double bcdiag, const float* u, const float* b, const float* dl1, float* d, const double* coef,
-                      int step, float* y, void* stream);
+                      int step, float* y, const float* cdiag, void* stream);
 /* Status of the tensor-core operator kernels (pmg_ebe_apply / pmg_ebe_cheb_step on FP32 3D grids) since the
  * last reset (host-synchronous read): PMG_OK, or PMG_TIMEOUT if a bounded wait of a kernel gave up (its
  * output is then undefined).  reset != 0 clears the flag.  No counterpart in the reference: pyMOTO's
@@ -218,10 +223,11 @@ int pmg_scale(int dtype, int64_t n, void* y, const void* x, double a, void* stre
 /* y = x with the Dirichlet dofs zeroed (or only the Dirichlet dofs kept when keep_bc != 0). */
 int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int keep_bc, const void* x, void* y,
                 void* stream);
-/* One pass: direct = rhs / bcdiag on the Dirichlet dofs (0 elsewhere), free_part = rhs on the free dofs (0 on
- * the Dirichlet dofs) -- the split of LDAWrapper.solve (pymoto/solvers/solvers.py:174-176). */
+/* One pass: direct = rhs / (bcdiag + cdiag) on the Dirichlet dofs (0 elsewhere; cdiag may be NULL), free_part =
+ * rhs on the free dofs (0 on the Dirichlet dofs) -- the split of LDAWrapper.solve
+ * (pymoto/solvers/solvers.py:174-176). */
 int pmg_split_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, double bcdiag, const void* rhs,
-                 void* direct, void* free_part, void* stream);
+                 void* direct, void* free_part, const void* cdiag, void* stream);
 /* Precision conversion y(dst_dtype) = a * x(src_dtype) (product formed in FP64); and x64 += a * d32. */
 int pmg_convert(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, double a, void* stream);
 int pmg_add_f32_to_f64(int64_t n, double* x, const float* d, double a, void* stream);

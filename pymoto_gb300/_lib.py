@@ -26,10 +26,11 @@ SIGNATURES = {
     "pmg_last_error": (c_char_p, []),
     "pmg_element_stiffness": (I, [I, D, D, I, D, D, D, P]),
     "pmg_dof_connectivity": (I, [I, I, I, P, P]),
-    "pmg_ebe_apply": (I, [I, I, I, I, I, P, P, P, D, P, P, P, D, P, P]),
-    "pmg_ebe_diagonal": (I, [I, I, I, I, P, P, P, D, P, P]),
+    "pmg_ebe_apply": (I, [I, I, I, I, I, P, P, P, D, P, P, P, D, P, P, P]),
+    "pmg_ebe_diagonal": (I, [I, I, I, I, P, P, P, D, P, P, P]),
     "pmg_stencil_apply": (I, [I, I, I, I, I, P, P, P, P, D, P, P]),
     "pmg_stencil_diagonal": (I, [I, I, I, I, P, P, P]),
+    "pmg_stencil_add_diagonal": (I, [I, I, I, I, P, P, P]),
     "pmg_restrict": (I, [I, I, I, I, P, P, P]),
     "pmg_prolong_add": (I, [I, I, I, I, P, P, P]),
     "pmg_galerkin_table": (I, [I, P, P]),
@@ -45,7 +46,7 @@ SIGNATURES = {
     "pmg_cheb_coeffs": (I, [P, D, D, I, P, P]),
     "pmg_cheb_step": (I, [I, L, P, P, P, P, P, I, I, P]),
     "pmg_stencil_cheb_step": (I, [I, I, I, I, P, P, P, P, P, P, I, P, P]),
-    "pmg_ebe_cheb_step": (I, [I, I, I, P, P, P, D, P, P, P, P, P, I, P, P]),
+    "pmg_ebe_cheb_step": (I, [I, I, I, P, P, P, D, P, P, P, P, P, I, P, P, P]),
     "pmg_operator_status": (I, [I]),
     "pmg_cholesky_factor": (I, [I, P, I, P, P]),
     "pmg_cholesky_solve": (I, [I, I, P, I, P, P, P]),
@@ -66,7 +67,7 @@ SIGNATURES = {
     "pmg_scale_rsqrt": (I, [I, L, P, P, P, P]),
     "pmg_scale": (I, [I, L, P, P, D, P]),
     "pmg_mask_bc": (I, [I, I, L, P, I, P, P, P]),
-    "pmg_split_bc": (I, [I, I, L, P, D, P, P, P, P]),
+    "pmg_split_bc": (I, [I, I, L, P, D, P, P, P, P, P]),
     "pmg_convert": (I, [I, I, L, P, P, D, P]),
     "pmg_add_f32_to_f64": (I, [L, P, P, D, P]),
     "pmg_convert_dscale": (I, [I, I, L, P, P, P, I, P]),

@@ -153,10 +153,7 @@ struct DotAcc<float> {
 // 3D FP32 operator apply on the tensor cores (ebe_tc.cu: tcgen05, accumulators in tensor memory).
 int ebe_apply_tc_f32(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
                      const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
-                     cudaStream_t st);
-// 3D FP32 operator apply with mma.sync tiles (ebe_mma.cu).
-int ebe_apply_mma_f32(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
-                      const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
-                      cudaStream_t st);
+                     const float* cdiag, cudaStream_t st);
+
 
 }  // namespace pmg

@@ -10,21 +10,22 @@
 //
 // Element products.  Per layer the 256 element vectors u_e (24 values) form two 128-row GEMM tiles, one
 // per warpgroup: each thread writes its row into tensor memory (tcgen05.st), and one thread per
-// warpgroup issues D = A B with A = [U_hi | U_lo] (128 x 48, TF32, in TMEM) and
-// B = [[K0_hi, K0_lo], [K0_hi, 0]] (48 x 48, TF32, in shared memory), so that
-// D[:, 0:24] + D[:, 24:48] = U_hi K0_hi + U_lo K0_hi + U_hi K0_lo: three TF32 products in six
-// tcgen05.mma (M = 128, N = 48, K = 8), FP32 accumulation in TMEM.  U is taken relative to the element's
-// first node (K0 annihilates a common translation of the 8 nodes), so the rounding error scales with the
-// variation of u over one element, not with |u|.
+// warpgroup issues D = A B with A = [U_hi | U_lo | U_hi] (128 x 72, TF32, in TMEM) and
+// B = [K0_hi; K0_hi; K0_lo] (72 x 32, TF32, in shared memory, columns 24..31 zero), so that
+// D = U_hi K0_hi + U_lo K0_hi + U_hi K0_lo: three TF32 products in nine tcgen05.mma (M = 128, N = 32,
+// K = 8), FP32 accumulation in TMEM.  The staged displacements are taken relative to one displacement of
+// the tile (K0 annihilates a common translation of the 8 nodes of an element), so the rounding error scales
+// with the variation of u over the tile, not with |u|; the hi/lo split is done once per staged node.
 //
 // Node sums.  The thread reads its row of D back (tcgen05.ld), scales by x_e and keeps the forces on its
 // upper 4 nodes in registers for the next layer (z sum in registers); the pair of elements on either side
 // of a node in x is summed with a warp shuffle, and the pair in y through a small shared-memory exchange.
 // One CTA barrier, one warpgroup barrier and one mbarrier wait per layer.
 //
-// Staging: node layers of u (masked at constrained dofs), their constraint-mask words, the element layer
-// of x and the operands of each thread's owned node (b, diag, the Chebyshev increment) are copied with
-// cp.async two layers ahead into a 5-slot ring.
+// Staging: node layers of u, their constraint-mask words, the element layer of x and the operands of each
+// thread's owned node (b, diag, the Chebyshev increment) are copied with cp.async two layers ahead into a
+// 5-slot ring; the thread that copied a node then zeroes its constrained dofs, shifts it and splits it into
+// its TF32 hi and lo parts.
 //
 // Every wait is bounded: an mbarrier wait that gives up sets the library's operator error word
 // (pmg_operator_status) and the kernel carries on to its end, where it frees its tensor memory.
@@ -44,14 +45,16 @@ constexpr int OWNX = TX - 1, OWNY = TY - 1;  // owned nodes per tile: 31 x 7
 constexpr int NTHREADS = TX * TY;            // 256
 constexpr int RING = 5;       // node layers t, t + 1 in use, t + 2 and t + 3 in flight, t - 1 read by the node phase
 constexpr int PFN = (PLANE + NTHREADS - 1) / NTHREADS;  // staged nodes per thread: 2
-constexpr int TMEM_COLS = 256;               // 2 warpgroups x (A 48 + D 48) = 192, rounded to a power of 2
-constexpr int COLS_PER_WG = 96;
+constexpr int KA = 72, ND = 32;              // GEMM K (A columns) and N (D columns)
+constexpr int TMEM_COLS = 256;               // 2 warpgroups x (A 72 + D 32) = 208, rounded to a power of 2
+constexpr int COLS_PER_WG = KA + ND;
 constexpr uint32_t WAIT_LIMIT = 1u << 14;   // polls of at most WAIT_HINT_NS each: about a second in all
 constexpr uint32_t WAIT_HINT_NS = 65536;
 
 struct TcSmem {
-  float B[48 * 48];               // K-major, no swizzle: core matrix (n/8, k/4) at (n/8)*1536 + (k/4)*128 bytes
-  float u[RING][3][PLANE];        // node layers of u: [slot][component][node of the staged tile]
+  float B[ND * KA];               // K-major, no swizzle: core matrix (n/8, k/4) at (n/8)*2304 + (k/4)*128 bytes
+  float u[RING][3][PLANE];        // node layers of u as copied, then its TF32 hi part: [slot][component][node]
+  float ulo[RING][3][PLANE];      // the lo part
   uint32_t m[RING][PLANE];        // aligned bcmask word holding each staged node's mask byte
   float x[RING][TX * TY];         // element layer of x
   float xb[2][TY][3][TX];         // y-pair exchange: [parity][row][component][lane]
@@ -98,6 +101,18 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
       : "memory");
 }
 
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "f"(v[0]),
+               "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+               : "r"(taddr)
+               : "memory");
+}
+
 // Shared-memory matrix descriptor: no swizzle, K-major; LBO = stride between core matrices along K,
 // SBO = stride between 8-row groups along M/N; bits 46-47 = 1 (descriptor version of sm_100 and later).
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
@@ -105,8 +120,9 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
          (1ull << 46);
 }
 
-// Instruction descriptor of kind::tf32: D F32, A and B TF32, both K-major, N = 48, M = 128.
-constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((48u >> 3) << 17) | ((128u >> 4) << 24);
+// Instruction descriptor of kind::tf32: D F32, A and B TF32, both K-major, N = 32, M = 128.
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t(ND) >> 3) << 17) | ((128u >> 4) << 24);
+constexpr uint32_t B_SBO = (KA / 4) * 128;   // bytes between 8-row groups of B
 
 __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t accumulate) {
   asm volatile(
@@ -148,7 +164,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     ebe_apply_tc_kernel(Grid g, const float* __restrict__ xe, ElemMat<float, 24> K0,
                         const uint8_t* __restrict__ bcmask, float bcdiag, const float* __restrict__ u,
                         const float* __restrict__ b, const float* __restrict__ diag, float w, float* __restrict__ y,
-                        ChebArgs<float> ch) {
+                        ChebArgs<float> ch, const float* __restrict__ cdiag) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   TcSmem& S = *reinterpret_cast<TcSmem*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -165,13 +181,16 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     cc = (float)ch.coef[2 * ch.step + 1];
   }
 
-  // B = [[K0_hi, K0_lo], [K0_hi, 0]] (48 x 48, row k, column n) in the canonical K-major layout
-  for (int q = tid; q < 48 * 48; q += NTHREADS) {
-    const int k = q / 48, n = q - (q / 48) * 48;
-    const float kv = K0.v[(k % 24) * 24 + (n % 24)];
-    const float hi = tf32_rna(kv);
-    const float v = n < 24 ? hi : (k < 24 ? tf32_rna(kv - hi) : 0.f);
-    S.B[(n >> 3) * 384 + (k >> 2) * 32 + (n & 7) * 4 + (k & 3)] = v;
+  // B = [K0_hi; K0_hi; K0_lo] (72 x 32, row k, column n) in the canonical K-major layout
+  for (int q = tid; q < ND * KA; q += NTHREADS) {
+    const int k = q / ND, n = q - (q / ND) * ND;
+    float v = 0.f;
+    if (n < 24) {
+      const float kv = K0.v[(k % 24) * 24 + n];
+      const float hi = tf32_rna(kv);
+      v = k < 48 ? hi : tf32_rna(kv - hi);
+    }
+    S.B[(n >> 3) * (B_SBO / 4) + (k >> 2) * 32 + (n & 7) * 4 + (k & 3)] = v;
   }
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.mbar[0])) : "memory");
@@ -237,20 +256,34 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     }
     cp_async_commit();
   };
-  // zero the constrained dofs of this thread's staged nodes of slot s (after its copies landed)
+  // common shift of the staged displacements: u at the first owned node of the tile (clamped into the grid)
+  float cref[3];
+  {
+    const int64_t n0 = ((int64_t)min(kz0, nnz - 1) * nny + min(je0 + 1, nny - 1)) * nnx + min(ie0 + 1, nnx - 1);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) cref[d] = u[n0 * 3 + d];
+  }
+  // this thread's staged nodes of slot s (after its copies landed): constrained dofs zeroed, shifted by cref,
+  // split into the TF32 hi part (in place) and the lo part
   auto fixup = [&](int s) {
-    if (!bcmask) return;
     const int ku = kz0 - 1 + s;
-    if (ku < 0 || ku >= nnz) return;
     const int slot = s % RING;
 #pragma unroll
     for (int q = 0; q < PFN; ++q) {
-      if (spos[q] < 0 || gnode[q] < 0) continue;
-      const int64_t m = ku * nlayer + gnode[q];
-      const unsigned fixed = (S.m[slot][spos[q]] >> (8 * (int)(m & 3))) & 7u;
+      if (spos[q] < 0) continue;
+      unsigned fixed = 0u;
+      if (bcmask && gnode[q] >= 0 && ku >= 0 && ku < nnz) {
+        const int64_t m = (int64_t)ku * nlayer + gnode[q];
+        fixed = (S.m[slot][spos[q]] >> (8 * (int)(m & 3))) & 7u;
+      }
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-        if ((fixed >> c) & 1u) S.u[slot][c][spos[q]] = 0.f;
+      for (int c = 0; c < 3; ++c) {
+        float* p = &S.u[slot][c][spos[q]];
+        const float v = (((fixed >> c) & 1u) ? 0.f : *p) - cref[c];
+        const float hi = tf32_rna(v);
+        *p = hi;
+        S.ulo[slot][c][spos[q]] = v - hi;       // exact; the tensor core reads its leading TF32 bits
+      }
     }
   };
 
@@ -263,7 +296,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
   tc_fence_after();
   const uint32_t tbase = S.tbase;
   const uint32_t lane_sel = (uint32_t)(32 * (warp & 3)) << 16;
-  const uint32_t colA = tbase + COLS_PER_WG * wg, colD = colA + 48;
+  const uint32_t colA = tbase + COLS_PER_WG * wg, colD = colA + KA;
   const uint32_t bbase = smem_u32(S.B);
 
 
@@ -284,8 +317,9 @@ __global__ void __launch_bounds__(NTHREADS, 2)
       const float acc = p0[d] + S.xb[xpar][warp - 1][d][lane];
       const int64_t q = n * 3 + d;
       const bool fixed = (om >> d) & 1u;
-      const float uq = (MODE >= 2 || fixed) ? u[q] : 0.f;
-      const float Au = fixed ? bcdiag * uq : acc;
+      const float uq = (MODE >= 2 || fixed || cdiag) ? u[q] : 0.f;
+      float Au = fixed ? bcdiag * uq : acc;
+      if (cdiag) Au += cdiag[q] * uq;        // constant diagonal term (AssembleStiffness add_constant)
       if (MODE == 0) {
         y[q] = Au;
       } else if (MODE == 1) {
@@ -312,27 +346,28 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     if (t + 3 <= nlay + 1) issue(t + 3);
     else cp_async_commit();      // empty group: keeps the wait counts uniform
 
-    // A row of this element: u_e relative to its first node, split into TF32 hi and lo parts
+    // A row of this element: [u_hi | u_lo | u_hi] of its 8 nodes (staged, shifted and split)
     {
       const int s0 = t % RING, s1 = (t + 1) % RING;
-      float a[48];
+      float a[KA];
 #pragma unroll
       for (int loc = 0; loc < 8; ++loc) {
         const int dx = loc & 1, dy = (loc >> 1) & 1, dz = loc >> 2;
         const int p = (warp + dy) * NODX + lane + dx;
+        const int sl = dz ? s1 : s0;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) a[loc * 3 + d] = S.u[dz ? s1 : s0][d][p];
-      }
-#pragma unroll
-      for (int q = 23; q >= 0; --q) {
-        const float v = a[q] - a[q % 3];
-        const float hi = tf32_rna(v);
-        a[q] = hi;
-        a[24 + q] = v - hi;          // exact in FP32; the tensor core reads its leading TF32 bits
+        for (int d = 0; d < 3; ++d) {
+          const float hi = S.u[sl][d][p];
+          a[loc * 3 + d] = hi;
+          a[24 + loc * 3 + d] = S.ulo[sl][d][p];
+          a[48 + loc * 3 + d] = hi;
+        }
       }
       tmem_st16(colA + lane_sel, a);
       tmem_st16(colA + lane_sel + 16, a + 16);
       tmem_st16(colA + lane_sel + 32, a + 32);
+      tmem_st16(colA + lane_sel + 48, a + 48);
+      tmem_st8(colA + lane_sel + 64, a + 64);
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
     }
     tc_fence_before();
@@ -343,7 +378,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     if ((tid & 127) == 0) {
       tc_fence_after();
 #pragma unroll
-      for (int s = 0; s < 6; ++s) mma_tf32(colD, colA + 8 * s, smem_desc(bbase + 256u * s, 128u, 1536u), s > 0);
+      for (int s = 0; s < KA / 8; ++s) mma_tf32(colD, colA + 8 * s, smem_desc(bbase + 256u * s, 128u, B_SBO), s > 0);
       mma_commit(&S.mbar[wg]);
     }
 
@@ -352,17 +387,16 @@ __global__ void __launch_bounds__(NTHREADS, 2)
 
     if (!mbar_wait(&S.mbar[wg], (uint32_t)(t & 1))) timed_out = true;
     tc_fence_after();
-    float dv[48];
+    float dv[24];
     tmem_ld16(colD + lane_sel, dv);
-    tmem_ld16(colD + lane_sel + 16, dv + 16);
-    tmem_ld16(colD + lane_sel + 32, dv + 32);
+    tmem_ld8(colD + lane_sel + 16, dv + 16);
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     const float xv = S.x[t % RING][tid];
     float z[12];
 #pragma unroll
     for (int q = 0; q < 12; ++q) {
-      z[q] = carry[q] + xv * (dv[q] + dv[24 + q]);        // local nodes 0..3: this node layer
-      carry[q] = xv * (dv[12 + q] + dv[36 + q]);          // local nodes 4..7: the next node layer
+      z[q] = carry[q] + xv * dv[q];        // local nodes 0..3: this node layer
+      carry[q] = xv * dv[12 + q];          // local nodes 4..7: the next node layer
     }
     // x pairs: node (ie0 + lane, je0 + warp + ly) gets local node 2 ly of this element and local node 2 ly + 1
     // of the element to its left (lane - 1)
@@ -393,7 +427,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
 // 3D FP32 operator apply on the tensor cores (modes as pmg_ebe_apply, 3 = fused Chebyshev step).
 int ebe_apply_tc_f32(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
                      const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
-                     cudaStream_t st) {
+                     const float* cdiag, cudaStream_t st) {
   static bool attr_set[64][4] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return check_launch();
@@ -432,13 +466,13 @@ int ebe_apply_tc_f32(int mode, Grid g, const float* xe, const double* K0, const 
   }
   const float bd = (float)bcdiag, wf = (float)w;
   if (m == 0)
-    ebe_apply_tc_kernel<0><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
+    ebe_apply_tc_kernel<0><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch, cdiag);
   else if (m == 1)
-    ebe_apply_tc_kernel<1><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
+    ebe_apply_tc_kernel<1><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch, cdiag);
   else if (m == 2)
-    ebe_apply_tc_kernel<2><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
+    ebe_apply_tc_kernel<2><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch, cdiag);
   else
-    ebe_apply_tc_kernel<3><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch);
+    ebe_apply_tc_kernel<3><<<grid, NTHREADS, smem, st>>>(g, xe, K, bcmask, bd, u, b, diag, wf, y, ch, cdiag);
   return check_launch();
 }
 

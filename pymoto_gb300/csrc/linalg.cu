@@ -189,15 +189,16 @@ __global__ void mask_bc_kernel(int64_t nnodes, const uint8_t* __restrict__ m, in
 // Dirichlet split of a right-hand side in one pass: direct = rhs / bcdiag on constrained dofs (0 elsewhere),
 // free = rhs on free dofs (0 on constrained ones).
 template <typename T, int DIM>
-__global__ void split_bc_kernel(int64_t nnodes, const uint8_t* __restrict__ m, T inv_bcdiag, const T* __restrict__ rhs,
-                                T* __restrict__ direct, T* __restrict__ free_part) {
+__global__ void split_bc_kernel(int64_t nnodes, const uint8_t* __restrict__ m, T bcdiag, const T* __restrict__ rhs,
+                                T* __restrict__ direct, T* __restrict__ free_part, const T* __restrict__ cdiag) {
   for (int64_t nd = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; nd < nnodes; nd += (int64_t)gridDim.x * blockDim.x) {
     const unsigned mm = m[nd];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       const T v = rhs[nd * DIM + d];
       const bool bc = (mm >> d) & 1u;
-      direct[nd * DIM + d] = bc ? v * inv_bcdiag : T(0);
+      // a Dirichlet row holds bcdiag (+ the constant diagonal term) only
+      direct[nd * DIM + d] = bc ? v / (bcdiag + (cdiag ? cdiag[nd * DIM + d] : T(0))) : T(0);
       free_part[nd * DIM + d] = bc ? T(0) : v;
     }
   }
@@ -888,24 +889,24 @@ int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int k
 }
 
 int pmg_split_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, double bcdiag, const void* rhs,
-                 void* direct, void* free_part, void* stream) {
+                 void* direct, void* free_part, const void* cdiag, void* stream) {
   if (nnodes < 0 || (dim != 2 && dim != 3) || !bcmask || !rhs || !direct || !free_part || !(bcdiag != 0.0))
     return PMG_BAD_ARG;
   if (nnodes == 0) return PMG_OK;
   cudaStream_t st = as_stream(stream);
   const unsigned g = blocks_for(nnodes, 256);
   if (dtype == PMG_F64 && dim == 3)
-    split_bc_kernel<double, 3><<<g, 256, 0, st>>>(nnodes, bcmask, 1.0 / bcdiag, (const double*)rhs, (double*)direct,
-                                                 (double*)free_part);
+    split_bc_kernel<double, 3><<<g, 256, 0, st>>>(nnodes, bcmask, bcdiag, (const double*)rhs, (double*)direct,
+                                                 (double*)free_part, (const double*)cdiag);
   else if (dtype == PMG_F64)
-    split_bc_kernel<double, 2><<<g, 256, 0, st>>>(nnodes, bcmask, 1.0 / bcdiag, (const double*)rhs, (double*)direct,
-                                                 (double*)free_part);
+    split_bc_kernel<double, 2><<<g, 256, 0, st>>>(nnodes, bcmask, bcdiag, (const double*)rhs, (double*)direct,
+                                                 (double*)free_part, (const double*)cdiag);
   else if (dtype == PMG_F32 && dim == 3)
-    split_bc_kernel<float, 3><<<g, 256, 0, st>>>(nnodes, bcmask, (float)(1.0 / bcdiag), (const float*)rhs,
-                                                (float*)direct, (float*)free_part);
+    split_bc_kernel<float, 3><<<g, 256, 0, st>>>(nnodes, bcmask, (float)(bcdiag), (const float*)rhs,
+                                                (float*)direct, (float*)free_part, (const float*)cdiag);
   else if (dtype == PMG_F32)
-    split_bc_kernel<float, 2><<<g, 256, 0, st>>>(nnodes, bcmask, (float)(1.0 / bcdiag), (const float*)rhs,
-                                                (float*)direct, (float*)free_part);
+    split_bc_kernel<float, 2><<<g, 256, 0, st>>>(nnodes, bcmask, (float)(bcdiag), (const float*)rhs,
+                                                (float*)direct, (float*)free_part, (const float*)cdiag);
   else
     return PMG_BAD_ARG;
   return check_launch();

@@ -20,7 +20,8 @@ template <typename T, int DIM, int MODE>
 __global__ void __launch_bounds__(128) ebe_apply_kernel(Grid g, const T* __restrict__ xe, ElemMat<T, Traits<DIM>::NDE> K0,
                                                         const uint8_t* __restrict__ bcmask, T bcdiag,
                                                         const T* __restrict__ u, const T* __restrict__ b,
-                                                        const T* __restrict__ diag, T w, T* __restrict__ y) {
+                                                        const T* __restrict__ diag, T w, T* __restrict__ y,
+                                                        const T* __restrict__ cdiag) {
   constexpr int NN = Traits<DIM>::NN;
   constexpr int NDE = Traits<DIM>::NDE;
   constexpr int KZ = DIM == 3 ? 3 : 1;
@@ -90,6 +91,7 @@ __global__ void __launch_bounds__(128) ebe_apply_kernel(Grid g, const T* __restr
   for (int d = 0; d < DIM; ++d) {
     const int64_t q = n * DIM + d;
     T Au = ((mymask >> d) & 1) ? bcdiag * u[q] : acc[d];
+    if (cdiag) Au += cdiag[q] * u[q];        // constant diagonal term (AssembleStiffness add_constant)
     if (MODE == 0) {
       y[q] = Au;
     } else if (MODE == 1) {
@@ -125,7 +127,8 @@ __global__ void __launch_bounds__(TBX * TBY * TBZ) ebe_apply_tiled_kernel(Grid g
                                                                          const uint8_t* __restrict__ bcmask, T bcdiag,
                                                                          const T* __restrict__ u, const T* __restrict__ b,
                                                                          const T* __restrict__ diag, T w,
-                                                                         T* __restrict__ y) {
+                                                                         T* __restrict__ y,
+                                                                         const T* __restrict__ cdiag) {
   constexpr int UX = TBX + 2, UY = TBY + 2, UZ = TBZ + 2;   // node tile with halo
   constexpr int EX = TBX + 1, EY = TBY + 1, EZ = TBZ + 1;   // element tile
   constexpr int NT = TBX * TBY * TBZ;
@@ -193,7 +196,8 @@ __global__ void __launch_bounds__(TBX * TBY * TBZ) ebe_apply_tiled_kernel(Grid g
   for (int d = 0; d < 3; ++d) {
     const int64_t q = n * 3 + d;
     const T uq = u[q];
-    const T Au = ((mymask >> d) & 1) ? bcdiag * uq : acc[d];
+    T Au = ((mymask >> d) & 1) ? bcdiag * uq : acc[d];
+    if (cdiag) Au += cdiag[q] * uq;
     if (MODE == 0) {
       y[q] = Au;
     } else if (MODE == 1) {
@@ -206,7 +210,8 @@ __global__ void __launch_bounds__(TBX * TBY * TBZ) ebe_apply_tiled_kernel(Grid g
 
 template <typename T, int DIM>
 __global__ void ebe_diag_kernel(Grid g, const T* __restrict__ xe, ElemMat<T, Traits<DIM>::NDE> K0,
-                                const uint8_t* __restrict__ bcmask, T bcdiag, T* __restrict__ diag) {
+                                const uint8_t* __restrict__ bcmask, T bcdiag, T* __restrict__ diag,
+                                const T* __restrict__ cdiag) {
   constexpr int NDE = Traits<DIM>::NDE;
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= g.nnodes()) return;
@@ -230,7 +235,8 @@ __global__ void ebe_diag_kernel(Grid g, const T* __restrict__ xe, ElemMat<T, Tra
       }
   const uint8_t m = bcmask ? bcmask[n] : 0;
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) diag[n * DIM + d] = ((m >> d) & 1) ? bcdiag : acc[d];
+  for (int d = 0; d < DIM; ++d)
+    diag[n * DIM + d] = (((m >> d) & 1) ? bcdiag : acc[d]) + (cdiag ? cdiag[n * DIM + d] : T(0));
 }
 
 // ------------------------------------------------------------------------------------------ stencils
@@ -393,6 +399,16 @@ __global__ void stencil_diag_kernel(Grid g, const T* __restrict__ S, T* __restri
   if (n >= nn) return;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) diag[n * DIM + d] = S[((int64_t)d * DIM + d) * nn + n];   // centre block, h = 0
+}
+
+// centre block diagonal of the stencils += c (a constant diagonal added to the operator)
+template <typename T, int DIM>
+__global__ void stencil_add_diag_kernel(Grid g, T* __restrict__ S, const T* __restrict__ c) {
+  const int64_t nn = g.nnodes();
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nn) return;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) S[((int64_t)d * DIM + d) * nn + n] += c[n * DIM + d];
 }
 
 // Row sums of |A| of a stencil operator, per dof (the l1-Jacobi diagonal: with it the spectrum of
@@ -952,10 +968,12 @@ __global__ void dofconn_kernel(Grid g, int64_t* __restrict__ dc) {
 // ------------------------------------------------------------------------------------------ dispatch
 template <typename T, int DIM>
 int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
-                const void* u, const void* b, const void* diag, double w, void* y, cudaStream_t st) {
+                const void* u, const void* b, const void* diag, double w, void* y, const void* cdiag, cudaStream_t st) {
   if constexpr (DIM == 3 && sizeof(T) == 4)
     return ebe_apply_tc_f32(mode, g, (const float*)xe, K0, bcmask, bcdiag, (const float*)u, (const float*)b,
-                            (const float*)diag, w, (float*)y, ChebArgs<float>{nullptr, nullptr, 0}, st);
+                            (const float*)diag, w, (float*)y, ChebArgs<float>{nullptr, nullptr, 0}, (const float*)cdiag,
+                            st);
+  const T* c_ = (const T*)cdiag;
   auto K = make_elem_mat<T, Traits<DIM>::NDE>(K0);
   if constexpr (DIM == 3) {
     const dim3 block(TBX, TBY, TBZ);
@@ -966,11 +984,11 @@ int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_
     const T* d_ = (const T*)diag;
     T* y_ = (T*)y;
     if (mode == PMG_APPLY_MATVEC)
-      ebe_apply_tiled_kernel<T, 0><<<grid, block, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_);
+      ebe_apply_tiled_kernel<T, 0><<<grid, block, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_, c_);
     else if (mode == PMG_APPLY_RESIDUAL)
-      ebe_apply_tiled_kernel<T, 1><<<grid, block, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_);
+      ebe_apply_tiled_kernel<T, 1><<<grid, block, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_, c_);
     else
-      ebe_apply_tiled_kernel<T, 2><<<grid, block, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_);
+      ebe_apply_tiled_kernel<T, 2><<<grid, block, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_, c_);
     return check_launch();
   }
   const int threads = 128;
@@ -981,11 +999,11 @@ int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_
   const T* d_ = (const T*)diag;
   T* y_ = (T*)y;
   if (mode == PMG_APPLY_MATVEC)
-    ebe_apply_kernel<T, DIM, 0><<<blocks, threads, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_);
+    ebe_apply_kernel<T, DIM, 0><<<blocks, threads, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_, c_);
   else if (mode == PMG_APPLY_RESIDUAL)
-    ebe_apply_kernel<T, DIM, 1><<<blocks, threads, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_);
+    ebe_apply_kernel<T, DIM, 1><<<blocks, threads, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_, c_);
   else
-    ebe_apply_kernel<T, DIM, 2><<<blocks, threads, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_);
+    ebe_apply_kernel<T, DIM, 2><<<blocks, threads, 0, st>>>(g, xe_, K, bcmask, (T)bcdiag, u_, b_, d_, (T)w, y_, c_);
   return check_launch();
 }
 
@@ -1103,7 +1121,7 @@ int pmg_dof_connectivity(int nelx, int nely, int nelz, int64_t* dofconn, void* s
 
 int pmg_ebe_apply(int mode, int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
                   const uint8_t* bcmask, double bcdiag, const void* u, const void* b, const void* diag,
-                  double omega, void* y, void* stream) {
+                  double omega, void* y, const void* cdiag, void* stream) {
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !xe || !K0_host || !u || !y) return PMG_BAD_ARG;
   if (mode < 0 || mode > 2) return PMG_BAD_ARG;
   if (mode >= PMG_APPLY_RESIDUAL && !b) return PMG_BAD_ARG;
@@ -1111,16 +1129,18 @@ int pmg_ebe_apply(int mode, int dtype, int nelx, int nely, int nelz, const void*
   if (y == u) return PMG_BAD_ARG;  // the gather reads the neighbourhood of u
   Grid g{nelx, nely, nelz};
   PMG_DISPATCH(dtype, g.dim(),
-               (ebe_apply_t<T, DIM>(mode, g, xe, K0_host, bcmask, bcdiag, u, b, diag, omega, y, as_stream(stream))));
+               (ebe_apply_t<T, DIM>(mode, g, xe, K0_host, bcmask, bcdiag, u, b, diag, omega, y, cdiag,
+                                    as_stream(stream))));
 }
 
 int pmg_ebe_diagonal(int dtype, int nelx, int nely, int nelz, const void* xe, const double* K0_host,
-                     const uint8_t* bcmask, double bcdiag, void* diag, void* stream) {
+                     const uint8_t* bcmask, double bcdiag, void* diag, const void* cdiag, void* stream) {
   if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !xe || !K0_host || !diag) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
   PMG_DISPATCH(dtype, g.dim(),
                (launch_simple<T, DIM>(ebe_diag_kernel<T, DIM>, g.nnodes(), as_stream(stream), g, (const T*)xe,
-                                      make_elem_mat<T, Traits<DIM>::NDE>(K0_host), bcmask, (T)bcdiag, (T*)diag)));
+                                      make_elem_mat<T, Traits<DIM>::NDE>(K0_host), bcmask, (T)bcdiag, (T*)diag,
+                                      (const T*)cdiag)));
 }
 
 int pmg_stencil_apply(int mode, int dtype, int nelx, int nely, int nelz, const void* S, const void* u,
@@ -1146,12 +1166,20 @@ int pmg_stencil_cheb_step(int dtype, int nelx, int nely, int nelz, const void* S
 
 int pmg_ebe_cheb_step(int nelx, int nely, int nelz, const float* xe, const double* K0_host, const uint8_t* bcmask,
                       double bcdiag, const float* u, const float* b, const float* dl1, float* d, const double* coef,
-                      int step, float* y, void* stream) {
+                      int step, float* y, const float* cdiag, void* stream) {
   if (!grid_ok(nelx, nely, nelz) || nelz == 0 || !xe || !K0_host || !u || !b || !dl1 || !d || !coef || !y || y == u ||
       step < 0 || step >= 64)
     return PMG_BAD_ARG;
   return ebe_apply_tc_f32(PMG_APPLY_CHEB, Grid{nelx, nely, nelz}, xe, K0_host, bcmask, bcdiag, u, b, dl1, 0.0, y,
-                          ChebArgs<float>{d, coef, step}, as_stream(stream));
+                          ChebArgs<float>{d, coef, step}, cdiag, as_stream(stream));
+}
+
+int pmg_stencil_add_diagonal(int dtype, int nelx, int nely, int nelz, void* S, const void* c, void* stream) {
+  if (!grid_ok(nelx, nely, nelz) || !dtype_ok(dtype) || !S || !c) return PMG_BAD_ARG;
+  Grid g{nelx, nely, nelz};
+  PMG_DISPATCH(dtype, g.dim(),
+               (launch_simple<T, DIM>(stencil_add_diag_kernel<T, DIM>, g.nnodes(), as_stream(stream), g, (T*)S,
+                                      (const T*)c)));
 }
 
 int pmg_stencil_diagonal(int dtype, int nelx, int nely, int nelz, const void* S, void* diag, void* stream) {

@@ -633,6 +633,37 @@ class DeviceDyad:
 
 
 # --------------------------------------------------------------------------------------------- assembly
+def _diagonal_constant(add_constant, n):
+    """The diagonal (host FP64 vector of n) of AssembleGeneral's add_constant (pymoto/modules/assembly.py:294-295):
+    a sparse or dense n x n matrix, or its diagonal as a vector; None for None.  The matrix-free operators add a
+    constant diagonal (springs to ground, soft supports); other constant matrices are not supported."""
+    if add_constant is None:
+        return None
+    import scipy.sparse as sps
+    if sps.issparse(add_constant):
+        A = sps.coo_matrix(add_constant)
+        if A.shape != (n, n):
+            raise ValueError(f"add_constant has shape {A.shape}, the operator {(n, n)}")
+        on = A.row == A.col
+        if np.any(A.data[~on] != 0):
+            raise NotImplementedError("add_constant: the matrix-free operator adds a diagonal constant only")
+        c = np.zeros(n, dtype=np.result_type(A.data, np.float64))
+        np.add.at(c, A.row[on], A.data[on])
+    else:
+        a = add_constant.detach().cpu().numpy() if isinstance(add_constant, torch.Tensor) else np.asarray(add_constant)
+        if a.ndim == 1 and a.size == n:
+            c = a
+        elif a.shape == (n, n):
+            if np.any(a - np.diag(np.diagonal(a)) != 0):
+                raise NotImplementedError("add_constant: the matrix-free operator adds a diagonal constant only")
+            c = np.diagonal(a)
+        else:
+            raise ValueError(f"add_constant has shape {a.shape}, the operator {(n, n)}")
+    if np.iscomplexobj(c):
+        raise NotImplementedError("add_constant: complex constants are not supported")
+    return np.ascontiguousarray(c, dtype=np.float64)
+
+
 class AssembleStiffness(Module):
     """K(x) = sum_e x_e K0 with Dirichlet rows/columns (pymoto/modules/assembly.py:407-463 over
     AssembleGeneral :18-315).  The output is a matrix-free StiffnessOperator on the device, not a CSR
@@ -641,9 +672,8 @@ class AssembleStiffness(Module):
     def __init__(self, domain, bc=None, bcdiagval=None, matrix_type=None, add_constant=None, reuse_sparsity=True,
                  e_modulus=1.0, poisson_ratio=0.3, plane="strain", sensitivity_precision="fp64"):
         """sensitivity_precision: "fp64" (the reference's contraction) or "mixed" (element vectors shifted
-        in FP64 by their first-node value, quadratic form in FP32: for the mixed-precision solver path)."""
-        if add_constant is not None:
-            raise NotImplementedError("add_constant is not supported by the matrix-free operator")
+        in FP64 by their first-node value, quadratic form in FP32: for the mixed-precision solver path).
+        add_constant: a constant diagonal (sparse or dense matrix, or vector) added after the Dirichlet rows."""
         if sensitivity_precision not in ("fp64", "mixed"):
             raise ValueError("sensitivity_precision must be 'fp64' or 'mixed'")
         self.sensitivity_precision = sensitivity_precision
@@ -657,6 +687,26 @@ class AssembleStiffness(Module):
         self.bcdiagval = float(np.max(self.stiffness_element)) if bcdiagval is None else float(bcdiagval)
         self._mask_host = bc_node_mask(g.nnodes, g.dim, self.bc)
         self._mask = None
+        self._set_constant(add_constant, scalar=False)
+
+    def _set_constant(self, add_constant, scalar):
+        """Host diagonal of add_constant over the operator's dofs; scalar operators (one entry per node, carried
+        as component 0) take it per node."""
+        g = self.grid
+        c = _diagonal_constant(add_constant, g.nnodes if scalar else g.ndof)
+        if c is not None and scalar:
+            w = np.zeros(g.ndof)
+            w[0::g.dim] = c
+            c = w
+        self._cdiag_host = c
+        self._cdiag = None
+
+    def cdiag(self, device):
+        if self._cdiag_host is None:
+            return None
+        if self._cdiag is None or self._cdiag.device != device:
+            self._cdiag = torch.from_numpy(self._cdiag_host).to(device)
+        return self._cdiag
 
     def bcmask(self, device):
         if self._mask is None or self._mask.device != device:
@@ -668,7 +718,8 @@ class AssembleStiffness(Module):
         if xd.numel() != self.grid.nel:
             raise ValueError(f"Input vector wrong size ({xd.numel()}), must be equal to #nel ({self.grid.nel})")
         self._kind = kind
-        return StiffnessOperator(self.grid, xd, self.stiffness_element, self.bcmask(xd.device), self.bcdiagval)
+        return StiffnessOperator(self.grid, xd, self.stiffness_element, self.bcmask(xd.device), self.bcdiagval,
+                                 cdiag=self.cdiag(xd.device))
 
     def _sensitivity(self, dgdmat):
         if dgdmat is None or getattr(dgdmat, "size", 1) <= 0:
@@ -702,8 +753,6 @@ class AssembleMass(AssembleStiffness):
         self.domain = domain
         self.grid = Grid(*grid_of(domain))
         g = self.grid
-        if add_constant is not None:
-            raise NotImplementedError("add_constant is not supported by the matrix-free operator")
         if ndof not in (1, g.dim):
             raise NotImplementedError(f"AssembleMass on the device takes ndof=1 or ndof={g.dim} (got {ndof})")
         self.ndof = ndof
@@ -722,6 +771,7 @@ class AssembleMass(AssembleStiffness):
             scalar = np.zeros(0, dtype=np.int64) if self.bc is None else self.bc * g.dim
             self._mask_host = bc_node_mask(g.nnodes, g.dim, np.concatenate([scalar, extra]))
         self._mask = None
+        self._set_constant(add_constant, scalar=ndof == 1)
 
     def __call__(self, x):
         op = super().__call__(x)
@@ -740,8 +790,6 @@ class AssemblePoisson(AssembleStiffness):
 
     def __init__(self, domain, bc=None, bcdiagval=None, matrix_type=None, add_constant=None, reuse_sparsity=True,
                  material_property=1.0, sensitivity_precision="fp64"):
-        if add_constant is not None:
-            raise NotImplementedError("add_constant is not supported by the matrix-free operator")
         if sensitivity_precision not in ("fp64", "mixed"):
             raise ValueError("sensitivity_precision must be 'fp64' or 'mixed'")
         self.sensitivity_precision = sensitivity_precision   # P0 annihilates constants, as the mixed form needs
@@ -758,6 +806,7 @@ class AssemblePoisson(AssembleStiffness):
         scalar = np.zeros(0, dtype=np.int64) if self.bc is None else self.bc * g.dim
         self._mask_host = bc_node_mask(g.nnodes, g.dim, np.concatenate([scalar, extra]))
         self._mask = None
+        self._set_constant(add_constant, scalar=True)
 
     def __call__(self, x):
         op = super().__call__(x)
@@ -809,7 +858,8 @@ class LinSolve(Module):
         """(direct part on Dirichlet dofs, rhs with those dofs zeroed)."""
         direct = torch.empty_like(rhs)
         rl = torch.empty_like(rhs)
-        call("pmg_split_bc", F64, A.grid.dim, A.grid.nnodes, A.bcmask, A.bcdiag, rhs, direct, rl, stream())
+        call("pmg_split_bc", F64, A.grid.dim, A.grid.nnodes, A.bcmask, A.bcdiag, rhs, direct, rl,
+             A.cdiag() if hasattr(A, "cdiag") else None, stream())
         return direct, rl
 
     def _mask(self, A, v):

@@ -177,12 +177,15 @@ class StiffnessOperator:
 
     fp64_stencil = True
 
-    def __init__(self, grid, xe, K0, bcmask, bcdiag, dtype=F64, _xe64=None):
+    def __init__(self, grid, xe, K0, bcmask, bcdiag, dtype=F64, _xe64=None, cdiag=None):
         self.grid = grid
         self.xe = xe                      # element scaling in the operator dtype
         self.K0 = np.ascontiguousarray(K0, dtype=np.float64)
         self.bcmask = bcmask              # uint8 per node (device)
         self.bcdiag = float(bcdiag)
+        # constant diagonal (ndof, FP64 device vector) added after the Dirichlet rows, or None
+        self.cdiag64 = cdiag
+        self._cdiag = None
         self.code = dtype
         self._xe64 = xe if _xe64 is None and dtype == F64 else _xe64
         self._diag = None
@@ -196,9 +199,17 @@ class StiffnessOperator:
         meant to be refreshed in place with assign() every design iteration (stable device addresses, so
         CUDA graphs that read it stay valid)."""
         xe = torch.empty(other.xe.shape, dtype=TORCH_DTYPE[code], device=other.device)
-        op = cls(other.grid, xe, other.K0, other.bcmask, other.bcdiag, code)
+        op = cls(other.grid, xe, other.K0, other.bcmask, other.bcdiag, code, cdiag=other.cdiag64)
         op.persistent = True
         return op
+
+    def cdiag(self):
+        """The constant diagonal in the operator's precision (None without one)."""
+        if self.cdiag64 is None:
+            return None
+        if self._cdiag is None or self._cdiag.dtype != self.torch_dtype:
+            self._cdiag = self.cdiag64 if self.code == F64 else self.cdiag64.to(self.torch_dtype)
+        return self._cdiag
 
     def assign(self, other, derived=True):
         """Copy the element scaling of `other` (any precision) into this operator's buffer and (derived=True)
@@ -210,6 +221,8 @@ class StiffnessOperator:
         src = other._xe64 if other._xe64 is not None else other.xe
         call("pmg_convert", _lib.dtype_code(src), self.code, src.numel(), src, self.xe, 1.0, stream())
         self.bcmask, self.bcdiag = other.bcmask, other.bcdiag
+        if other.cdiag64 is not self.cdiag64:
+            self.cdiag64, self._cdiag = other.cdiag64, None
         if derived:
             self.refresh_derived()
         return self
@@ -253,7 +266,8 @@ class StiffnessOperator:
             return self._variants[code]
         xe = torch.empty(self.xe.shape, dtype=TORCH_DTYPE[code], device=self.xe.device)
         call("pmg_convert", self.code, code, self.xe.numel(), self.xe, xe, 1.0, stream())
-        op = StiffnessOperator(self.grid, xe, self.K0, self.bcmask, self.bcdiag, code, _xe64=self._xe64)
+        op = StiffnessOperator(self.grid, xe, self.K0, self.bcmask, self.bcdiag, code, _xe64=self._xe64,
+                               cdiag=self.cdiag64)
         op._variants = self._variants
         self._variants[code] = op
         return op
@@ -262,6 +276,9 @@ class StiffnessOperator:
         g = self.grid
         call("pmg_ebe_stencil", self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag, S,
              stream())
+        c = self.cdiag()
+        if c is not None:
+            call("pmg_stencil_add_diagonal", self.code, g.nelx, g.nely, g.nelz, S, c, stream())
 
     def stencil(self):
         """Node stencils of this operator (assembled on first use, same precision)."""
@@ -277,7 +294,7 @@ class StiffnessOperator:
         g = self.grid
         if self.code == F32 and g.dim == 3:
             call("pmg_ebe_cheb_step", g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag, u, b, dl1, d,
-                 coef, step, out, stream())
+                 coef, step, out, self.cdiag(), stream())
             return out
         if self.code == F64 and self.fp64_stencil:
             call("pmg_stencil_cheb_step", self.code, g.nelx, g.nely, g.nelz, self.stencil(), u, b, dl1, d, coef, step,
@@ -293,7 +310,7 @@ class StiffnessOperator:
                  out, stream())
         else:
             call("pmg_ebe_apply", mode, self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask,
-                 self.bcdiag, u, b, diag, float(w), out, stream())
+                 self.bcdiag, u, b, diag, float(w), out, self.cdiag(), stream())
         return out
 
     def matvec(self, u, out=None):
@@ -314,7 +331,7 @@ class StiffnessOperator:
     def _diagonal_into(self, d):
         g = self.grid
         call("pmg_ebe_diagonal", self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0, self.bcmask, self.bcdiag, d,
-             stream())
+             self.cdiag(), stream())
 
     def diagonal(self):
         if self._diag is None:
@@ -332,9 +349,11 @@ class StiffnessOperator:
         bl = self._constrained_coarse_elements()
         call("pmg_galerkin_from_ebe", self.code, g.nelx, g.nely, g.nelz, self.xe, self.K0,
              self.bcmask, self.bcdiag, table, bl if bl.numel() else None, int(bl.numel()), E, stream())
+        cc = _restricted_diagonal(g, self.cdiag(), out)
         if out is not None:
+            out.cdiag = cc
             return out.recompute()
-        return StencilOperator(gc, E, self.code)
+        return StencilOperator(gc, E, self.code, cdiag=cc)
 
     def _constrained_coarse_elements(self):
         """Indices (int32, device) of the coarse elements with a constrained fine node; cached per BC mask."""
@@ -363,13 +382,27 @@ class StiffnessOperator:
         return f"StiffnessOperator({self.grid}, {self.dtype})"
 
 
+def _restricted_diagonal(grid, c, out=None):
+    """R^T c on the coarse grid of `grid` (the lumped Galerkin term of a constant diagonal c: R^T diag(c) R 1 =
+    R^T c because the prolongation of a constant is that constant), into out.cdiag when it exists; None for
+    c = None."""
+    if c is None:
+        return None
+    gc = grid.coarse()
+    buf = out.cdiag if out is not None and getattr(out, "cdiag", None) is not None else \
+        torch.empty(gc.ndof, dtype=c.dtype, device=c.device)
+    call("pmg_restrict", _lib.dtype_code(c), grid.nelx, grid.nely, grid.nelz, c, buf, stream())
+    return buf
+
+
 class StencilOperator:
     """Galerkin operator of a coarse grid: element matrices E and node stencils S (same dtype)."""
 
-    def __init__(self, grid, E, code):
+    def __init__(self, grid, E, code, cdiag=None):
         self.grid = grid
         self.E = E
         self.code = code
+        self.cdiag = cdiag        # lumped constant diagonal R^T c of the level above (add_constant), or None
         g = grid
         self.S = torch.empty((stencil_values_per_node(g.dim), g.nnodes), dtype=TORCH_DTYPE[code], device=E.device)
         self._diag = None
@@ -379,6 +412,8 @@ class StencilOperator:
         """Refresh the node stencils (and the diagonal, if it was requested) from E in place."""
         g = self.grid
         call("pmg_stencil_from_elements", self.code, g.nelx, g.nely, g.nelz, self.E, self.S, stream())
+        if self.cdiag is not None:
+            call("pmg_stencil_add_diagonal", self.code, g.nelx, g.nely, g.nelz, self.S, self.cdiag, stream())
         if self._diag is not None:
             call("pmg_stencil_diagonal", self.code, g.nelx, g.nely, g.nelz, self.S, self._diag, stream())
         return self
@@ -439,9 +474,11 @@ class StencilOperator:
         nde = (2 ** g.dim) * g.dim
         E = out.E if out is not None else torch.empty((gc.nel, nde * nde), dtype=self.torch_dtype, device=self.device)
         call("pmg_galerkin_from_elements", self.code, g.nelx, g.nely, g.nelz, self.E, E, stream())
+        cc = _restricted_diagonal(g, self.cdiag, out)
         if out is not None:
+            out.cdiag = cc
             return out.recompute()
-        return StencilOperator(gc, E, self.code)
+        return StencilOperator(gc, E, self.code, cdiag=cc)
 
     def to_dense(self, out=None):
         g = self.grid

@@ -141,8 +141,9 @@ class Chebyshev(Preconditioner):
         if isinstance(A, StencilOperator):
             call("pmg_stencil_rowabs", A.code, g.nelx, g.nely, g.nelz, A.S, self.D, stream())
         else:
+            # the constant diagonal (add_constant, nonnegative springs) enters the l1 row sums as it is
             call("pmg_ebe_diagonal", A.code, g.nelx, g.nely, g.nelz, A.xe, self.l1_element_matrix(A.K0), A.bcmask,
-                 A.bcdiag, self.D, stream())
+                 A.bcdiag, self.D, A.cdiag(), stream())
 
     def smooth(self, A, b, x, d, r, zero_start):
         """`degree` steps from x; d and r are work vectors of the size of b.  Each step is one fused

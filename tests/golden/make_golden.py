@@ -15,6 +15,7 @@ at module level for plotting only.  The fixtures are small .npz files; the tests
     python tests/golden/make_golden.py overhang # the OverhangFilter cases only
     python tests/golden/make_golden.py poisson  # the AssemblePoisson cases only
     python tests/golden/make_golden.py einsum   # the EinSum expressions only
+    python tests/golden/make_golden.py springs  # AssembleStiffness add_constant (springs to ground) only
 """
 import os
 import sys
@@ -460,6 +461,57 @@ def poisson(pym):
     save("poisson.npz", **out)
 
 
+def springs(pym):
+    """Springs to ground through AssembleStiffness(add_constant=...) (pymoto/modules/assembly.py:294-295, the
+    compliant-mechanism example's use): 2D (mechanism-like supports, springs at an input and an output dof) and
+    3D (cantilever with springs on the loaded face, one on a Dirichlet dof); K u, the solution, compliance and
+    its sensitivities.  A 3D case without any Dirichlet dof (soft supports only, as the self-weight example)."""
+    import scipy.sparse as sps
+    out = {}
+    cases = [("q4", (12, 6), (12, 6, 0)), ("h8", (8, 4, 4), (8, 4, 4)), ("soft", (6, 4, 4), (6, 4, 4))]
+    for tag, shp, shp3 in cases:
+        d = pym.VoxelDomain(*shp)
+        dim = 2 if len(shp) == 2 else 3
+        rng = np.random.default_rng({"q4": 31, "h8": 32, "soft": 33}[tag])
+        x = rng.uniform(0.1, 1.0, d.nel)
+        f = np.zeros(d.nnodes * dim)
+        if tag == "q4":
+            left = d.get_nodenumber(0, np.arange(shp[1] + 1))
+            right = d.get_nodenumber(shp[0], np.arange(shp[1] + 1))
+            bc = np.union1d(left * 2, (right[:, None] * 2 + np.arange(2)).ravel())
+            din, dout = 2 * left[0] + 1, 2 * left[-1] + 1
+            f[din] = 1.0
+            idx, val = np.array([din, dout]), np.array([10.0, 10.0])
+        elif tag == "h8":
+            left = d.nodes[0, :, :].flatten()
+            bc = (left[:, None] * 3 + np.arange(3)).ravel()
+            tip = d.get_nodenumber(shp[0], shp[1] // 2, shp[2] // 2)
+            f[3 * tip + 1] = -1.0
+            idx = np.array([3 * tip + 1, 3 * tip, bc[4]])
+            val = np.array([0.5, 2.0, 3.0])
+        else:
+            bc = None
+            corners = [d.get_nodenumber(0, j, k) for j in (0, shp[1]) for k in (0, shp[2])]
+            idx = np.array([3 * n + c for n in corners for c in range(3)])
+            val = np.full(idx.size, 5.0)
+            f[3 * d.get_nodenumber(shp[0], shp[1] // 2, shp[2] // 2) + 1] = -1.0
+        K_const = sps.csc_matrix((val, (idx, idx)), shape=(d.nnodes * dim, d.nnodes * dim))
+        sx = pym.Signal("x", x)
+        with pym.Network() as fn:
+            sK = pym.AssembleStiffness(d, bc=bc, add_constant=K_const)(sx)
+            su = pym.LinSolve(hermitian=True, symmetric=True)(sK, f)
+            sc = pym.EinSum("i,i->")(su, f)
+        fn.reset()
+        sc.sensitivity = 1.0
+        fn.sensitivity()
+        u_rand = rng.standard_normal(d.nnodes * dim)
+        out.update({f"{tag}_shape": np.array(shp3), f"{tag}_bc": np.zeros(0, np.int64) if bc is None else bc,
+                    f"{tag}_x": x, f"{tag}_f": f, f"{tag}_idx": idx, f"{tag}_val": val,
+                    f"{tag}_urand": u_rand, f"{tag}_Ku": sK.state @ u_rand, f"{tag}_u": su.state,
+                    f"{tag}_c": np.array(float(sc.state)), f"{tag}_dx": sx.sensitivity.copy()})
+    save("springs.npz", **out)
+
+
 def vti_cases():
     """The VTI output cases: (name, (nelx, nely, nelz), element size, origin, scale, vectors).  Pure numpy, so
     the tests rebuild the same inputs without pyMOTO."""
@@ -532,6 +584,8 @@ if __name__ == "__main__":
         pipeline(pym, "q4_mg", (16, 8), "density", 2.0, 3, 1e-8, plane="stress")
         pipeline(pym, "h8_direct", (6, 4, 2), "density", 1.5, 0, 1e-8)
         oc_mbb(pym)
+    if "all" in which or "springs" in which:
+        springs(pym)
     if "all" in which or "vti" in which:
         vti_files(pym)
     if "all" in which or "mma" in which:
