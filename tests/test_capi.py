@@ -97,7 +97,7 @@ def test_coarse_ordering_is_a_band_reducing_permutation(shape):
 def test_invalid_arguments_fail_before_any_launch():
     from pymoto_gb300._lib import PMGError, call
     with pytest.raises(PMGError) as e:
-        call("pmg_ebe_apply", 0, 0, 0, 4, 4, None, None, None, 1.0, None, None, None, 0.0, None, None)
+        call("pmg_ebe_apply", 0, 0, 0, 4, 4, None, None, None, 1.0, None, None, None, 0.0, None, None, None)
     assert e.value.status == 1
     with pytest.raises(PMGError):
         call("pmg_restrict", 0, 5, 4, 0, None, None, None)      # odd grid

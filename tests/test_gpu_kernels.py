@@ -527,4 +527,4 @@ def test_bad_arguments_are_rejected(pg):
     with pytest.raises(PMGError):
         call("pmg_restrict", 0, 5, 4, 0, None, None, stream())
     with pytest.raises(PMGError):
-        call("pmg_ebe_apply", 7, 0, 4, 4, 0, None, None, None, 1.0, None, None, None, 0.0, None, stream())
+        call("pmg_ebe_apply", 7, 0, 4, 4, 0, None, None, None, 1.0, None, None, None, 0.0, None, None, stream())
