@@ -222,10 +222,9 @@ __global__ void __launch_bounds__(NTHREADS, 2)
   const int gelem = (gie >= 0 && gie < g.nx && gje >= 0 && gje < g.ny) ? gje * g.nx + gie : -1;
 
   // copies of node layer kz0 - 1 + s (u and mask words) and element layer kz0 - 1 + s (x) into slot s % RING
-  auto issue = [&](int s) {
+  auto issue = [&](int s, int slot) {
     const int ku = kz0 - 1 + s, kx = ku;
     const bool uok = ku >= 0 && ku < nnz, xok = kx >= 0 && kx < g.nz;
-    const int slot = s % RING;
     const int64_t lbase = uok ? (int64_t)ku * nlayer : 0;
 #pragma unroll
     for (int q = 0; q < PFN; ++q) {
@@ -265,9 +264,8 @@ __global__ void __launch_bounds__(NTHREADS, 2)
   }
   // this thread's staged nodes of slot s (after its copies landed): constrained dofs zeroed, shifted by cref,
   // split into the TF32 hi part (in place) and the lo part
-  auto fixup = [&](int s) {
+  auto fixup = [&](int s, int slot) {
     const int ku = kz0 - 1 + s;
-    const int slot = s % RING;
 #pragma unroll
     for (int q = 0; q < PFN; ++q) {
       if (spos[q] < 0) continue;
@@ -287,9 +285,9 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     }
   };
 
-  issue(0);
-  issue(1);
-  issue(2);
+  issue(0, 0);
+  issue(1, 1);
+  issue(2, 2);
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // B and the mbarrier inits -> async proxy
   tc_fence_before();
   __syncthreads();
@@ -307,9 +305,8 @@ __global__ void __launch_bounds__(NTHREADS, 2)
   bool timed_out = false;
 
   // node layer kz0 - 1 + t: the owned node's output (its operands and mask byte were staged in slot t)
-  auto node_phase = [&](int t, int xpar) {
+  auto node_phase = [&](int t, int xpar, int slot) {
     if (!owner || t < 1 || t > nlay) return;
-    const int slot = t % RING;
     const int64_t n = (int64_t)(kz0 - 1 + t) * nlayer + node_xy;
     const unsigned om = bcmask ? (S.m[slot][warp * NODX + lane] >> (8 * (int)(n & 3))) & 7u : 0u;
 #pragma unroll
@@ -335,20 +332,23 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     }
   };
 
-  for (int t = 0; t <= nlay; ++t) {
+  // ring slots of layers t - 1, t, t + 1 and t + 3 (advanced without divisions)
+  int spm1 = RING - 1, sp0 = 0, sp1 = 1, sp3 = 3;
+  auto next_slot = [](int v) { return v + 1 == RING ? 0 : v + 1; };
+  for (int t = 0; t <= nlay; ++t, spm1 = sp0, sp0 = sp1, sp1 = next_slot(sp1), sp3 = next_slot(sp3)) {
     // element layer kz0 - 1 + t: node layers in slots t and t + 1 (t + 1 has just landed), x in slot t
     cp_async_wait1();
-    if (t == 0) fixup(0);
-    fixup(t + 1);
+    if (t == 0) fixup(0, 0);
+    fixup(t + 1, sp1);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (t + 3 <= nlay + 1) issue(t + 3);
+    if (t + 3 <= nlay + 1) issue(t + 3, sp3);
     else cp_async_commit();      // empty group: keeps the wait counts uniform
 
     // A row of this element: [u_hi | u_lo | u_hi] of its 8 nodes (staged, shifted and split)
     {
-      const int s0 = t % RING, s1 = (t + 1) % RING;
+      const int s0 = sp0, s1 = sp1;
       float a[KA];
 #pragma unroll
       for (int loc = 0; loc < 8; ++loc) {
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     }
 
     // while the MMA runs: the output of node layer kz0 - 2 + t (completed in the previous iteration)
-    node_phase(t - 1, (t - 1) & 1);
+    node_phase(t - 1, (t - 1) & 1, spm1);
 
     if (!mbar_wait(&S.mbar[wg], (uint32_t)(t & 1))) timed_out = true;
     tc_fence_after();
@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     tmem_ld16(colD + lane_sel, dv);
     tmem_ld8(colD + lane_sel + 16, dv + 16);
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    const float xv = S.x[t % RING][tid];
+    const float xv = S.x[sp0][tid];
     float z[12];
 #pragma unroll
     for (int q = 0; q < 12; ++q) {
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     tc_fence_before();
   }
   __syncthreads();
-  node_phase(nlay, nlay & 1);
+  node_phase(nlay, nlay & 1, nlay % RING);
 
   cp_async_wait_all();
   if (timed_out) atomicExch(&g_operator_error, 1);

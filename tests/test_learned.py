@@ -272,3 +272,68 @@ def test_learned_warm_start_gain(pg):
     # the one-dimensional learned coarse space (deflation) was in use and the solves still reach the FP64
     # tolerance without more than a few extra iterations
     assert any(active) and sum(lcc[4:]) <= sum(base[4:]) + 4
+
+
+def test_pretrained_network_gains_on_cold_solves(pg):
+    """What the trained network gains where the solver has no previous solution to start from (the first
+    design of a run): trained on the solutions of 48 seeded smoothed-noise density fields, its prediction
+    (scaled by the Rayleigh-Ritz step) starts the FP64 flexible CG of 6 unseen fields.  Against the same solver
+    started from zero, it must take strictly fewer iterations and less time in all, both reaching the same FP64
+    relative residual."""
+    from scipy.ndimage import gaussian_filter
+    import oracle as O
+    from conftest import clamp_face_dofs
+    from pymoto_gb300.learned import LearnedWarmStart
+    from pymoto_gb300.operators import bc_node_mask
+    shape = (32, 16, 16)
+    g = O.Grid(*shape)
+    d = pg.VoxelDomain(*shape)
+    K0 = O.element_stiffness(g)
+    mask = torch.from_numpy(bc_node_mask(g.nnodes, g.dim, clamp_face_dofs(g))).to("cuda", torch.uint8)
+    f = np.zeros(g.ndof)
+    f[3 * g.node_number(shape[0], shape[1] // 2, shape[2] // 2) + 1] = -1.0
+    b = torch.from_numpy(f).cuda()
+
+    def operator(seed):
+        a = gaussian_filter(np.random.default_rng(seed).uniform(0.0, 1.0, shape[::-1]), sigma=2.0)
+        a = 1e-3 + (1.0 - 1e-3) * (a - a.min()) / (a.max() - a.min())
+        x = 1e-9 + (1 - 1e-9) * a.ravel() ** 3
+        return pg.StiffnessOperator(pg.Grid(*shape), torch.from_numpy(x).cuda(), K0, mask,
+                                    O.default_bcdiagval(K0))
+
+    ws = LearnedWarmStart(shape, stride=4, capacity=48, train_steps=6, lr=2e-3, history=0, seed=0)
+    mgs = pg.GeometricMultigrid.hierarchy(d, levels=3, smooth_steps=2, coarse_smooth_steps=3, precision="fp32",
+                                          smoother="chebyshev")
+    trainer = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=1e-8, m=1)
+    for seed in range(48):
+        A = operator(1000 + seed)
+        trainer.update(A)
+        ws.observe(A, trainer.solve(b))
+    for _ in range(200):                             # a few passes over the stored pairs
+        ws.train_step(int(ws.rng.integers(48)))
+    ws.sync_training()
+    ws.train_steps = 0                               # evaluation: the test fields' solutions are not learned
+
+    its, times = {False: [], True: []}, {False: 0.0, True: 0.0}
+    for seed in range(6):
+        A = operator(5000 + seed)
+        for learned in (False, True):
+            mg = pg.GeometricMultigrid.hierarchy(d, levels=3, smooth_steps=2, coarse_smooth_steps=3,
+                                                 precision="fp32", smoother="chebyshev")
+            solver = pg.MixedPrecisionCG(preconditioner=mg[0], tol=1e-6, m=1, warm_start=ws if learned else None)
+            solver.update(A)
+            solver.solve(b)                          # warm-up (graph capture, kernel loading)
+            solver.update(A)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            solver.solve(b)
+            e1.record()
+            torch.cuda.synchronize()
+            assert solver.last_residual <= 1e-6
+            its[learned].append(solver.iterations)
+            times[learned] += e0.elapsed_time(e1)
+    print(f"cold solves, FCG iterations without / with the pretrained network: {its[False]} / {its[True]}; "
+          f"time {times[False]:.2f} / {times[True]:.2f} ms")
+    assert sum(its[True]) < sum(its[False])
+    assert times[True] < times[False]
