@@ -41,8 +41,8 @@ GPU_LEVELS = 5          # 128x64x64 -> 8x4x4 coarsest (675 dofs, dense FP64 Chol
 REF_LEVELS = 4          # the reference example's hierarchy: coarsest 16x8x8 (SuperLU)
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) per launch of the roofline kernel at the bench workload, from the ncu capture
-# summarised in profiles/ebe_apply_mma_residual_hex8_128x64x64.md
-NCU_TRAFFIC_PER_LAUNCH = {"ebe_apply_mma_residual_f32": 15.756e6}
+# summarised in profiles/ebe_apply_tc_residual_hex8_128x64x64.md
+NCU_TRAFFIC_PER_LAUNCH = {"ebe_apply_tc_residual_f32": 15.756e6}
 
 
 def parse():
@@ -322,7 +322,7 @@ def headline_arm(results):
 def kernel_rooflines(run, flush, torch, reps=20):
     """Live CUDA-event times of the two level-0 operator kernels on the headline arm's final operators, one
     launch at a time on the current stream with the L2 flushed (256 MB write) before each launch:
-      * the FP32 tensor-core operator (ebe_apply_mma, residual mode): the most launched kernel of a design
+      * the FP32 tensor-core operator (ebe_apply_tc, residual mode): the most launched kernel of a design
         iteration (one matvec, one residual and one Chebyshev step per inner iteration);
       * the FP64 node-stencil product (the outer FCG operator), whose bound is the FP64 pipe.
     Returns per kernel: seconds per launch, algorithmic bytes and flops per launch."""
@@ -353,7 +353,7 @@ def kernel_rooflines(run, flush, torch, reps=20):
     out = {}
     t = timed(lambda: A32.apply(RESIDUAL, u32, b32, out=y32))
     # u, b read and y written once (FP32), element scaling (FP32) and the node constraint mask (bytes)
-    out["ebe_apply_mma_residual_f32"] = {"s": t, "bytes": 3 * 4 * ndof + 4 * nel + nn,
+    out["ebe_apply_tc_residual_f32"] = {"s": t, "bytes": 3 * 4 * ndof + 4 * nel + nn,
                                          "flops": 3 * 2 * 24 * 24 * nel}     # three TF32 products per element
     t = timed(lambda: A64.apply(MATVEC, u64, out=y64))
     # 27 blocks of 3 x 3 per row of 3 dofs: 81 FP64 FMA per dof; stored stencils (14 blocks) + u + y once
@@ -522,7 +522,7 @@ def operator_case(args):
     u1 = torch.randn(A1.grid.ndof, device="cuda")
     b1 = torch.randn_like(u1)
     out = {}
-    for name, fn in [("ebe_apply_mma_f32_residual", lambda: K32.apply(RESIDUAL, u32, b32)),
+    for name, fn in [("ebe_apply_tc_f32_residual", lambda: K32.apply(RESIDUAL, u32, b32)),
                      ("stencil_apply_f64_matvec", lambda: K.apply(MATVEC, u)),
                      ("stencil_apply_f32_level1_residual", lambda: A1.apply(RESIDUAL, u1, b1))]:
         for _ in range(2):
@@ -718,13 +718,13 @@ def main():
         val_plain = aggregate_rate(world, steps, R["plain_fp64"]["total_ms"] / 1e3) if "plain_fp64" in R else None
         # rooflines of the level-0 operator kernels, timed live after the timed region (kernel_rooflines)
         K = m["kernels"]
-        km = K["ebe_apply_mma_residual_f32"]
+        km = K["ebe_apply_tc_residual_f32"]
         achieved = km["bytes"] / km["s"] / 1e9
         tf32_peak = m["peaks"].get("bf16_tflops", 1900.0) / 2.0       # dense TF32 runs at half the BF16 rate
-        roofline = {"bound": "hbm", "kernel": "ebe_apply_mma_kernel<residual> (FP32 operator, 3xTF32 mma.sync, "
+        roofline = {"bound": "hbm", "kernel": "ebe_apply_tc_kernel<residual> (FP32 operator, 3xTF32 tcgen05.mma, "
                                                "grid %s)" % "x".join(map(str, shape)),
                     "achieved": achieved, "peak": m["hbm_peak"], "unit": "GB/s", "frac": achieved / m["hbm_peak"],
-                    "traffic": NCU_TRAFFIC_PER_LAUNCH.get("ebe_apply_mma_residual_f32"),
+                    "traffic": NCU_TRAFFIC_PER_LAUNCH.get("ebe_apply_tc_residual_f32"),
                     "bytes_per_launch": km["bytes"], "avg_launch_us": km["s"] * 1e6,
                     "tensor_tflops": km["flops"] / km["s"] / 1e12, "tensor_frac_of_tf32": km["flops"] / km["s"] / 1e12
                     / tf32_peak, "peak_source": m["peak_src"],

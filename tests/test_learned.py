@@ -301,7 +301,7 @@ def test_pretrained_network_gains_on_cold_solves(pg):
         return pg.StiffnessOperator(pg.Grid(*shape), torch.from_numpy(x).cuda(), K0, mask,
                                     O.default_bcdiagval(K0))
 
-    ws = LearnedWarmStart(shape, stride=4, capacity=48, train_steps=6, lr=2e-3, history=0, seed=0)
+    ws = LearnedWarmStart(shape, stride=2, capacity=48, train_steps=6, lr=2e-3, history=0, seed=0)
     mgs = pg.GeometricMultigrid.hierarchy(d, levels=3, smooth_steps=2, coarse_smooth_steps=3, precision="fp32",
                                           smoother="chebyshev")
     trainer = pg.MixedPrecisionCG(preconditioner=mgs[0], tol=1e-8, m=1)
@@ -312,6 +312,7 @@ def test_pretrained_network_gains_on_cold_solves(pg):
     for _ in range(200):                             # a few passes over the stored pairs
         ws.train_step(int(ws.rng.integers(48)))
     ws.sync_training()
+    print(f"training loss (squared error of a unit-norm target) after pretraining: {ws.loss():.3e}")
     ws.train_steps = 0                               # evaluation: the test fields' solutions are not learned
 
     its, times = {False: [], True: []}, {False: 0.0, True: 0.0}
@@ -333,6 +334,10 @@ def test_pretrained_network_gains_on_cold_solves(pg):
             assert solver.last_residual <= 1e-6
             its[learned].append(solver.iterations)
             times[learned] += e0.elapsed_time(e1)
+            if learned:
+                from pymoto_gb300.learned import rayleigh_ritz
+                print(f"field {seed}: Rayleigh-Ritz coefficient {solver.warm_start_coefficients}, energy shares "
+                      f"{getattr(rayleigh_ritz, 'last_shares', None)}")
     print(f"cold solves, FCG iterations without / with the pretrained network: {its[False]} / {its[True]}; "
           f"time {times[False]:.2f} / {times[True]:.2f} ms")
     assert sum(its[True]) < sum(its[False])

@@ -63,7 +63,7 @@ def _network(pg, g, tag, precision):
     f = torch.from_numpy(g[f"{tag}_f"]).cuda()
     with pg.Network() as fn:
         sK = pg.AssembleStiffness(d, bc=bc if bc.size else None, add_constant=C)(sx)
-        levels = 3 if d.nelz else 2
+        levels = 2 if tag != "h8" else 3      # 12x6 and 6x4x4 halve once, 8x4x4 twice
         if precision == "mixed":
             mgs = pg.GeometricMultigrid.hierarchy(d, levels=levels, smooth_steps=1, precision="fp32",
                                                   coarse_smooth_steps=[2] * (levels - 1), smoother="chebyshev")
