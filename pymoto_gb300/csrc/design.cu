@@ -244,6 +244,92 @@ __global__ void sens_mixed_kernel(Grid g, ElemMat<float, Traits<DIM>::NDE> K0, c
   dx[e] = accumulate ? dx[e] + val : val;
 }
 
+// Tiled form of the mixed-precision contraction (3D): a CTA owns 32 x 8 elements per layer and walks a chunk
+// of z layers.  Each staged node is shifted once by a reference displacement of the tile in FP64 and split
+// into an FP32 pair hi + lo (5 FP64 operations per value and node, instead of 2 per value and element); the
+// element differences (hi_a - hi_0) + (lo_a - lo_0) are then formed in FP32 with the accuracy of the FP64
+// shift, and the quadratic form runs in FP32 as above.
+constexpr int SENS_TX = 32, SENS_TY = 8, SENS_NX = SENS_TX + 1, SENS_NY = SENS_TY + 1;
+constexpr int SENS_PLANE = SENS_NX * SENS_NY;
+
+__global__ void __launch_bounds__(SENS_TX * SENS_TY)
+    sens_mixed_tiled_kernel(Grid g, ElemMat<float, 24> K0, const uint8_t* __restrict__ bcmask,
+                            const double* __restrict__ u, const double* __restrict__ v, double alpha, int accumulate,
+                            int zchunk, double* __restrict__ dx) {
+  __shared__ float sh[2][4][3][SENS_PLANE];     // [layer parity][u_hi, u_lo, v_hi, v_lo][component][node]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int i0 = blockIdx.x * SENS_TX, j0 = blockIdx.y * SENS_TY;
+  const int kb = blockIdx.z * zchunk, ke = min(g.nz, kb + zchunk);
+  if (kb >= ke) return;
+  const int nnx = g.nx + 1, nny = g.ny + 1;
+  double cu[3], cv[3];
+  {
+    const int64_t n0 = node_id(g, i0, j0, kb);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      cu[d] = u[n0 * 3 + d];
+      cv[d] = v[n0 * 3 + d];
+    }
+  }
+  auto stage = [&](int k, int buf) {
+    for (int q = tid; q < SENS_PLANE; q += SENS_TX * SENS_TY) {
+      const int cy = q / SENS_NX, cx = q - cy * SENS_NX;
+      const int gi = i0 + cx, gj = j0 + cy;
+      if (gi < nnx && gj < nny) {
+        const int64_t nd = node_id(g, gi, gj, k);
+        const unsigned m = bcmask ? bcmask[nd] : 0u;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const bool bc = (m >> d) & 1u;
+          const double du = (bc ? 0.0 : u[nd * 3 + d]) - cu[d];
+          const double dv = (bc ? 0.0 : v[nd * 3 + d]) - cv[d];
+          const float hu = (float)du, hv = (float)dv;
+          sh[buf][0][d][q] = hu;
+          sh[buf][1][d][q] = (float)(du - (double)hu);
+          sh[buf][2][d][q] = hv;
+          sh[buf][3][d][q] = (float)(dv - (double)hv);
+        }
+      } else {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) sh[buf][0][d][q] = sh[buf][1][d][q] = sh[buf][2][d][q] = sh[buf][3][d][q] = 0.f;
+      }
+    }
+  };
+  const int ei = i0 + lane, ej = j0 + warp;
+  const bool inside = ei < g.nx && ej < g.ny;
+  stage(kb, kb & 1);
+  for (int k = kb; k < ke; ++k) {
+    stage(k + 1, (k + 1) & 1);
+    __syncthreads();
+    if (inside) {
+      float uf[24], vf[24];
+      const int p00 = warp * SENS_NX + lane;
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        const int buf = (k + ((a >> 2) & 1)) & 1;
+        const int p = p00 + ((a >> 1) & 1) * SENS_NX + (a & 1);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          uf[a * 3 + d] = (sh[buf][0][d][p] - sh[k & 1][0][d][p00]) + (sh[buf][1][d][p] - sh[k & 1][1][d][p00]);
+          vf[a * 3 + d] = (sh[buf][2][d][p] - sh[k & 1][2][d][p00]) + (sh[buf][3][d][p] - sh[k & 1][3][d][p00]);
+        }
+      }
+      float s = 0.f;
+#pragma unroll
+      for (int r = 0; r < 24; ++r) {
+        float t = 0.f;
+#pragma unroll
+        for (int c = 0; c < 24; ++c) t = fmaf(K0.v[r * 24 + c], vf[c], t);
+        s = fmaf(uf[r], t, s);
+      }
+      const int64_t e = elem_id(g, ei, ej, k);
+      const double val = alpha * (double)s;
+      dx[e] = accumulate ? dx[e] + val : val;
+    }
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------------------------------------ OC update
 // State in scratch: sum partials and the bisection interval, all on the device.
 // x sqrt(-dg/lmid) is evaluated as (x sqrt(-dg)) / sqrt(lmid): the per-element square root is taken once and
@@ -664,10 +750,15 @@ int pmg_sens_contract_mixed(int nelx, int nely, int nelz, const double* K0_host,
   if (!grid_ok(nelx, nely, nelz) || !K0_host || !u || !v || !dx) return PMG_BAD_ARG;
   Grid g{nelx, nely, nelz};
   const unsigned b = blocks_for(g.nel(), 128);
-  if (g.dim() == 3)
-    sens_mixed_kernel<3><<<b, 128, 0, as_stream(stream)>>>(g, make_elem_mat<float, 24>(K0_host), bcmask, u, v, alpha,
-                                                           accumulate, dx);
-  else
+  if (g.dim() == 3) {
+    // z chunks: about two CTAs per SM in one wave, at least 4 layers per chunk
+    const int tx = (g.nx + SENS_TX - 1) / SENS_TX, ty = (g.ny + SENS_TY - 1) / SENS_TY;
+    int nzc = std::max(1, std::min(g.nz / 4, (2 * sm_count() + tx * ty - 1) / (tx * ty)));
+    const int zchunk = (g.nz + nzc - 1) / nzc;
+    nzc = (g.nz + zchunk - 1) / zchunk;
+    sens_mixed_tiled_kernel<<<dim3(tx, ty, nzc), SENS_TX * SENS_TY, 0, as_stream(stream)>>>(
+        g, make_elem_mat<float, 24>(K0_host), bcmask, u, v, alpha, accumulate, zchunk, dx);
+  } else
     sens_mixed_kernel<2><<<b, 128, 0, as_stream(stream)>>>(g, make_elem_mat<float, 8>(K0_host), bcmask, u, v, alpha,
                                                            accumulate, dx);
   return check_launch();

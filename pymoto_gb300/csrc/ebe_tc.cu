@@ -22,10 +22,10 @@
 // of a node in x is summed with a warp shuffle, and the pair in y through a small shared-memory exchange.
 // One CTA barrier, one warpgroup barrier and one mbarrier wait per layer.
 //
-// Staging: node layers of u, their constraint-mask words, the element layer of x and the operands of each
-// thread's owned node (b, diag, the Chebyshev increment) are copied with cp.async two layers ahead into a
-// 5-slot ring; the thread that copied a node then zeroes its constrained dofs, shifts it and splits it into
-// its TF32 hi and lo parts.
+// Staging: node layers of u, their constraint-mask words and the element layer of x are copied with cp.async
+// two layers ahead into a 5-slot ring; the thread that copied a node then zeroes its constrained dofs, shifts
+// it and splits it into its TF32 hi and lo parts.  The operands of each thread's owned node (b, diag, u, the
+// Chebyshev increment) are loaded into registers one layer before its output.
 //
 // Every wait is bounded: an mbarrier wait that gives up sets the library's operator error word
 // (pmg_operator_status) and the kernel carries on to its end, where it frees its tensor memory.
@@ -58,9 +58,6 @@ struct TcSmem {
   uint32_t m[RING][PLANE];        // aligned bcmask word holding each staged node's mask byte
   float x[RING][TX * TY];         // element layer of x
   float xb[2][TY][3][TX];         // y-pair exchange: [parity][row][component][lane]
-  float ob[RING][3][NTHREADS];    // b of each thread's owned node (own copies, read only by the thread)
-  float od[RING][3][NTHREADS];    // diag (Jacobi, Chebyshev)
-  float oc[RING][3][NTHREADS];    // the previous Chebyshev increment
   unsigned long long mbar[2];     // MMA completion, one per warpgroup
   uint32_t tbase;                 // TMEM base address from tcgen05.alloc
 };
@@ -244,15 +241,6 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     }
     const bool xlive = xok && gelem >= 0;
     cp_async4(&S.x[slot][tid], xe + (xlive ? (int64_t)kx * g.nx * g.ny + gelem : 0), xlive ? 4 : 0);
-    if (MODE >= 1 && owner && s >= 1 && s <= nlay) {          // operands of the owned node of node layer ku
-      const int64_t q0 = ((int64_t)ku * nlayer + node_xy) * 3;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        cp_async4(&S.ob[slot][c][tid], b + q0 + c, 4);
-        if (MODE >= 2) cp_async4(&S.od[slot][c][tid], diag + q0 + c, 4);
-        if (MODE == 3 && ch.step > 0) cp_async4(&S.oc[slot][c][tid], ch.d + q0 + c, 4);
-      }
-    }
     cp_async_commit();
   };
   // common shift of the staged displacements: u at the first owned node of the tile (clamped into the grid)
@@ -302,9 +290,26 @@ __global__ void __launch_bounds__(NTHREADS, 2)
 #pragma unroll
   for (int q = 0; q < 12; ++q) carry[q] = 0.f;
   float p0[3] = {0.f, 0.f, 0.f};   // x-paired forces on node (Xn, Yn) from this element row (previous layer)
+  float ob[3] = {0.f, 0.f, 0.f}, od[3] = {1.f, 1.f, 1.f}, ou[3] = {0.f, 0.f, 0.f}, oc[3] = {0.f, 0.f, 0.f};
+  float ok[3] = {0.f, 0.f, 0.f};
   bool timed_out = false;
 
-  // node layer kz0 - 1 + t: the owned node's output (its operands and mask byte were staged in slot t)
+  // operands of the owned node of node layer kz0 - 1 + t, loaded into registers one layer before its output
+  auto load_operands = [&](int t) {
+    if (!owner || t < 1 || t > nlay) return;
+    const int64_t q0 = ((int64_t)(kz0 - 1 + t) * nlayer + node_xy) * 3;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (MODE >= 1) ob[d] = b[q0 + d];
+      if (MODE >= 2 || cdiag) ou[d] = u[q0 + d];
+      if (MODE >= 2) od[d] = diag[q0 + d];
+      if (MODE == 3) oc[d] = ch.step == 0 ? 0.f : ch.d[q0 + d];
+      if (cdiag) ok[d] = cdiag[q0 + d];
+    }
+  };
+
+  // node layer kz0 - 1 + t: the owned node's output (its mask byte was staged in slot t, its operands are in
+  // registers)
   auto node_phase = [&](int t, int xpar, int slot) {
     if (!owner || t < 1 || t > nlay) return;
     const int64_t n = (int64_t)(kz0 - 1 + t) * nlayer + node_xy;
@@ -314,18 +319,18 @@ __global__ void __launch_bounds__(NTHREADS, 2)
       const float acc = p0[d] + S.xb[xpar][warp - 1][d][lane];
       const int64_t q = n * 3 + d;
       const bool fixed = (om >> d) & 1u;
-      const float uq = (MODE >= 2 || fixed || cdiag) ? u[q] : 0.f;
+      float uq = ou[d];
+      if (MODE < 2 && !cdiag && fixed) uq = u[q];
       float Au = fixed ? bcdiag * uq : acc;
-      if (cdiag) Au += cdiag[q] * uq;        // constant diagonal term (AssembleStiffness add_constant)
+      if (cdiag) Au += ok[d] * uq;            // constant diagonal term (AssembleStiffness add_constant)
       if (MODE == 0) {
         y[q] = Au;
       } else if (MODE == 1) {
-        y[q] = S.ob[slot][d][tid] - Au;
+        y[q] = ob[d] - Au;
       } else if (MODE == 2) {
-        y[q] = uq + w * __fdividef(S.ob[slot][d][tid] - Au, S.od[slot][d][tid]);
+        y[q] = uq + w * __fdividef(ob[d] - Au, od[d]);
       } else {
-        const float dprev = ch.step == 0 ? 0.f : S.oc[slot][d][tid];
-        const float dn = ca * dprev + cc * __fdividef(S.ob[slot][d][tid] - Au, S.od[slot][d][tid]);
+        const float dn = ca * oc[d] + cc * __fdividef(ob[d] - Au, od[d]);
         ch.d[q] = dn;
         y[q] = uq + dn;
       }
@@ -384,6 +389,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
 
     // while the MMA runs: the output of node layer kz0 - 2 + t (completed in the previous iteration)
     node_phase(t - 1, (t - 1) & 1, spm1);
+    load_operands(t);
 
     if (!mbar_wait(&S.mbar[wg], (uint32_t)(t & 1))) timed_out = true;
     tc_fence_after();

@@ -29,14 +29,15 @@ __device__ __forceinline__ float ld(const __nv_bfloat16* p) { return __bfloat162
 __device__ __forceinline__ float ld(const float* p) { return *p; }
 
 // The three convolution products are implicit GEMMs on the tensor cores (mma.sync m16n8k16, BF16 operands,
-// FP32 accumulation); each warp owns a 16-row tile of the output and all of its columns:
+// FP32 accumulation).  A CTA owns one 16 x 8 tile of the output; its 8 warps take interleaved 16-wide steps of
+// the reduction dimension and their fragments are summed in shared memory in warp order (deterministic):
 //   forward: out[v][co]  = bias[co] + sum_k A[v][k] W[k][co],  A[v][k] = in[v + off(tap)][ci],  k = tap*cin + ci
 //   data:    din[v][ci]  = sum_k' D[v][k'] W'[k'][ci],  D[v][k'] = dout[v - off(tap)][co],  k' = tap*cout + co,
 //                          W'[k'][ci] = w[tap][ci][co]
 //   weights: dW[k][co]   = sum_v A[v][k] dout[v][co] over a chunk of voxels (the bias gradient is the extra row
 //                          k = 27*cin with A = 1); chunks summed in order afterwards (deterministic).
 // FP32 operands (FP32 network input, the FP32 gradients) are rounded to BF16 when the fragments are built.
-constexpr int CONV_WARPS = 4;
+constexpr int CONV_WARPS = 8;
 
 __device__ __forceinline__ float ldf(const __nv_bfloat16* p, int64_t i) { return __bfloat162float(p[i]); }
 __device__ __forceinline__ float ldf(const float* p, int64_t i) { return p[i]; }
@@ -53,146 +54,172 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// value of the voxel (i, j, k) + (dx, dy, dz) or -1 outside the grid
+// index of the voxel (i, j, k) + (dx, dy, dz), or -1 outside the grid
 __device__ __forceinline__ int neighbour(const VGrid& g, int i, int j, int k, int dx, int dy, int dz) {
   const int ii = i + dx, jj = j + dy, kk = k + dz;
   if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || kk < 0 || kk >= g.nz) return -1;
   return (kk * g.ny + jj) * g.nx + ii;
 }
 
-// im2col element: x[nb(v, tap) * c + ch] for column q = tap * c + ch of voxel (i, j, k); sign -1 mirrors the tap
+// A fragment of an im2col matrix: rows (voxels) r[0] = gid, r[1] = gid + 8 of the tile, columns q = tap * c + ch
+// of the 16-wide step k0 (this thread's columns 2 tig + {0, 1} and 2 tig + 8 + {0, 1}); sign -1 mirrors the
+// taps.  With c a multiple of 16 the step lies in one tap: one division and one neighbour per row.
 template <typename T>
-__device__ __forceinline__ float im2col(const VGrid& g, const T* __restrict__ x, int c, int q, int qmax, bool ok,
-                                        int i, int j, int k, int sign) {
-  if (!ok || q >= qmax) return 0.f;
-  const int tap = q / c, ch = q - tap * c;
-  const int nb = neighbour(g, i, j, k, sign * (tap % 3 - 1), sign * ((tap / 3) % 3 - 1), sign * (tap / 9 - 1));
-  return nb < 0 ? 0.f : ldf(x, (int64_t)nb * c + ch);
+__device__ __forceinline__ void im2col_fragment(uint32_t (&a)[4], const VGrid& g, const T* __restrict__ x, int c,
+                                                int k0, int K, const bool (&ok)[2], const int (&vi)[2],
+                                                const int (&vj)[2], const int (&vk)[2], int sign, int tig) {
+  if ((c & 15) == 0) {
+    const int tap = k0 / c, ch0 = k0 - tap * c + 2 * tig;
+    const int dx = sign * (tap % 3 - 1), dy = sign * ((tap / 3) % 3 - 1), dz = sign * (tap / 9 - 1);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int nb = ok[h] ? neighbour(g, vi[h], vj[h], vk[h], dx, dy, dz) : -1;
+      const T* p = x + (int64_t)(nb < 0 ? 0 : nb) * c + ch0;
+      a[h] = nb < 0 ? 0u : pack2(ldf(p, 0), ldf(p, 1));
+      a[2 + h] = nb < 0 ? 0u : pack2(ldf(p, 8), ldf(p, 9));
+    }
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int h = q & 1, col = k0 + 2 * tig + 8 * (q >> 1);
+    float e[2];
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const int cq = col + s2;
+      float v = 0.f;
+      if (ok[h] && cq < K) {
+        const int tap = cq / c, ch = cq - tap * c;
+        const int nb = neighbour(g, vi[h], vj[h], vk[h], sign * (tap % 3 - 1), sign * ((tap / 3) % 3 - 1),
+                                 sign * (tap / 9 - 1));
+        if (nb >= 0) v = ldf(x, (int64_t)nb * c + ch);
+      }
+      e[s2] = v;
+    }
+    a[q] = pack2(e[0], e[1]);
+  }
 }
 
-template <typename TIN, int NT>
+// Fragments of the CTA's warps summed in warp order; warp 0 holds the result.
+__device__ __forceinline__ bool reduce_warps(float (&c)[4], float (*red)[32][4]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) red[warp][lane][q] = c[q];
+  __syncthreads();
+  if (warp != 0) return false;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float v = red[0][lane][q];
+    for (int w = 1; w < CONV_WARPS; ++w) v += red[w][lane][q];
+    c[q] = v;
+  }
+  return true;
+}
+
+// grid (voxel tiles of 16, output-channel tiles of 8)
+template <typename TIN>
 __global__ void __launch_bounds__(32 * CONV_WARPS)
     conv3d_fwd_kernel(VGrid g, int cin, int cout, const TIN* __restrict__ in, const __nv_bfloat16* __restrict__ w,
                       const float* __restrict__ bias, int relu, __nv_bfloat16* __restrict__ out_bf,
                       float* __restrict__ out_f) {
-  const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
-  const int64_t v0 = ((int64_t)blockIdx.x * CONV_WARPS + (threadIdx.x >> 5)) * 16;
+  __shared__ float red[CONV_WARPS][32][4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, gid = lane >> 2, tig = lane & 3;
+  const int64_t v0 = (int64_t)blockIdx.x * 16;
+  const int n = blockIdx.y * 8 + gid;
   const int64_t nv = g.nvox();
-  if (v0 >= nv) return;
-  int r[2], ci[2], cj[2], ck[2];
+  int r[2], vi[2], vj[2], vk[2];
   bool ok[2];
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     r[h] = (int)(v0 + gid + 8 * h);
     ok[h] = r[h] < nv;
-    vox_ijk(g, ok[h] ? r[h] : 0, ci[h], cj[h], ck[h]);
+    vox_ijk(g, ok[h] ? r[h] : 0, vi[h], vj[h], vk[h]);
   }
   const int K = 27 * cin;
-  float c[NT][4];
-#pragma unroll
-  for (int nt = 0; nt < NT; ++nt) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.f;
-  for (int k0 = 0; k0 < K; k0 += 16) {
+  float c[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int k0 = 16 * warp; k0 < K; k0 += 16 * CONV_WARPS) {
     uint32_t a[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {        // a0: row gid, cols 2tig..; a1: row gid+8; a2, a3: cols + 8
-      const int h = q & 1, col = k0 + 2 * tig + 8 * (q >> 1);
-      a[q] = pack2(im2col(g, in, cin, col, K, ok[h], ci[h], cj[h], ck[h], 1),
-                   im2col(g, in, cin, col + 1, K, ok[h], ci[h], cj[h], ck[h], 1));
-    }
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-      const int n = nt * 8 + gid;
-      float bw[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int kk = k0 + 2 * tig + (q & 1) + 8 * (q >> 1);
-        bw[q] = (kk < K && n < cout) ? __bfloat162float(w[(int64_t)kk * cout + n]) : 0.f;
-      }
-      mma_bf16(c[nt], a, pack2(bw[0], bw[1]), pack2(bw[2], bw[3]));
-    }
-  }
-#pragma unroll
-  for (int nt = 0; nt < NT; ++nt)
+    im2col_fragment(a, g, in, cin, k0, K, ok, vi, vj, vk, 1, tig);
+    float bw[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const int h = q >> 1, n = nt * 8 + 2 * tig + (q & 1);
-      if (!ok[h] || n >= cout) continue;
-      float v = c[nt][q] + (bias ? bias[n] : 0.f);
-      if (relu) v = fmaxf(v, 0.f);
-      const int64_t o = (int64_t)r[h] * cout + n;
-      if (out_bf) out_bf[o] = __float2bfloat16(v);
-      if (out_f) out_f[o] = v;
+      const int kk = k0 + 2 * tig + (q & 1) + 8 * (q >> 1);
+      bw[q] = (kk < K && n < cout) ? __bfloat162float(w[(int64_t)kk * cout + n]) : 0.f;
     }
+    mma_bf16(c, a, pack2(bw[0], bw[1]), pack2(bw[2], bw[3]));
+  }
+  if (!reduce_warps(c, red)) return;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int h = q >> 1, nc = blockIdx.y * 8 + 2 * tig + (q & 1);
+    if (!ok[h] || nc >= cout) continue;
+    float v = c[q] + (bias ? bias[nc] : 0.f);
+    if (relu) v = fmaxf(v, 0.f);
+    const int64_t o = (int64_t)r[h] * cout + nc;
+    if (out_bf) out_bf[o] = __float2bfloat16(v);
+    if (out_f) out_f[o] = v;
+  }
 }
 
-// din[v][ci] = sum_{tap, co} w[tap][ci][co] dout[v - off(tap)][co]  (dout already masked by the ReLU)
-template <int NT>
+// din[v][ci] = sum_{tap, co} w[tap][ci][co] dout[v - off(tap)][co]  (dout already masked by the ReLU);
+// grid (voxel tiles of 16, input-channel tiles of 8)
 __global__ void __launch_bounds__(32 * CONV_WARPS)
     conv3d_dgrad_kernel(VGrid g, int cin, int cout, const float* __restrict__ dout, const __nv_bfloat16* __restrict__ w,
                         float* __restrict__ din) {
-  const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
-  const int64_t v0 = ((int64_t)blockIdx.x * CONV_WARPS + (threadIdx.x >> 5)) * 16;
+  __shared__ float red[CONV_WARPS][32][4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, gid = lane >> 2, tig = lane & 3;
+  const int64_t v0 = (int64_t)blockIdx.x * 16;
+  const int n = blockIdx.y * 8 + gid;                 // input channel
   const int64_t nv = g.nvox();
-  if (v0 >= nv) return;
-  int r[2], ci[2], cj[2], ck[2];
+  int r[2], vi[2], vj[2], vk[2];
   bool ok[2];
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     r[h] = (int)(v0 + gid + 8 * h);
     ok[h] = r[h] < nv;
-    vox_ijk(g, ok[h] ? r[h] : 0, ci[h], cj[h], ck[h]);
+    vox_ijk(g, ok[h] ? r[h] : 0, vi[h], vj[h], vk[h]);
   }
   const int K = 27 * cout;
-  float c[NT][4];
-#pragma unroll
-  for (int nt = 0; nt < NT; ++nt) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.f;
-  for (int k0 = 0; k0 < K; k0 += 16) {
+  float c[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int k0 = 16 * warp; k0 < K; k0 += 16 * CONV_WARPS) {
     uint32_t a[4];
+    im2col_fragment(a, g, dout, cout, k0, K, ok, vi, vj, vk, -1, tig);
+    float bw[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const int h = q & 1, col = k0 + 2 * tig + 8 * (q >> 1);
-      a[q] = pack2(im2col(g, dout, cout, col, K, ok[h], ci[h], cj[h], ck[h], -1),
-                   im2col(g, dout, cout, col + 1, K, ok[h], ci[h], cj[h], ck[h], -1));
-    }
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-      const int n = nt * 8 + gid;                 // input channel
-      float bw[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int kk = k0 + 2 * tig + (q & 1) + 8 * (q >> 1);    // tap * cout + co
-        float v = 0.f;
-        if (kk < K && n < cin) {
-          const int tap = kk / cout, co = kk - tap * cout;
-          v = __bfloat162float(w[((int64_t)tap * cin + n) * cout + co]);
-        }
-        bw[q] = v;
+      const int kk = k0 + 2 * tig + (q & 1) + 8 * (q >> 1);    // tap * cout + co
+      float v = 0.f;
+      if (kk < K && n < cin) {
+        const int tap = kk / cout, co = kk - tap * cout;
+        v = __bfloat162float(w[((int64_t)tap * cin + n) * cout + co]);
       }
-      mma_bf16(c[nt], a, pack2(bw[0], bw[1]), pack2(bw[2], bw[3]));
+      bw[q] = v;
     }
+    mma_bf16(c, a, pack2(bw[0], bw[1]), pack2(bw[2], bw[3]));
   }
+  if (!reduce_warps(c, red)) return;
 #pragma unroll
-  for (int nt = 0; nt < NT; ++nt)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int h = q >> 1, n = nt * 8 + 2 * tig + (q & 1);
-      if (ok[h] && n < cin) din[(int64_t)r[h] * cin + n] = c[nt][q];
-    }
+  for (int q = 0; q < 4; ++q) {
+    const int h = q >> 1, nc = blockIdx.y * 8 + 2 * tig + (q & 1);
+    if (ok[h] && nc < cin) din[(int64_t)r[h] * cin + nc] = c[q];
+  }
 }
 
 // Partial weight and bias gradients over a chunk of voxels: part[chunk][k * cout + co] for k < 27 cin (k =
-// tap * cin + ci) and part[chunk][27 cin cout + co] for the bias.  Warp: 16 rows k, all cout columns.
+// tap * cin + ci) and part[chunk][27 cin cout + co] for the bias; grid (row tiles of 16, column tiles of 8,
+// voxel chunks of WG_CHUNK)
 constexpr int WG_CHUNK = 2048;
 
-template <typename TIN, int NT>
+template <typename TIN>
 __global__ void __launch_bounds__(32 * CONV_WARPS)
     conv3d_wgrad_partial_kernel(VGrid g, int cin, int cout, const TIN* __restrict__ in, const float* __restrict__ dout,
                                 float* __restrict__ part) {
-  const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
+  __shared__ float red[CONV_WARPS][32][4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, gid = lane >> 2, tig = lane & 3;
   const int rows = 27 * cin + 1;
-  const int m0 = (blockIdx.x * CONV_WARPS + (threadIdx.x >> 5)) * 16;
-  if (m0 >= rows) return;
-  const int chunk = blockIdx.y;
+  const int m0 = blockIdx.x * 16;
+  const int n = blockIdx.y * 8 + gid;
+  const int chunk = blockIdx.z;
   const int64_t nv = g.nvox();
   const int64_t vbeg = (int64_t)chunk * WG_CHUNK;
   const int64_t vend = min(nv, vbeg + WG_CHUNK);
@@ -208,10 +235,8 @@ __global__ void __launch_bounds__(32 * CONV_WARPS)
     ody[h] = (tap / 3) % 3 - 1;
     odz[h] = tap / 9 - 1;
   }
-  float c[NT][4];
-#pragma unroll
-  for (int nt = 0; nt < NT; ++nt) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.f;
-  for (int64_t vb = vbeg; vb < vend; vb += 16) {
+  float c[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int64_t vb = vbeg + 16 * warp; vb < vend; vb += 16 * CONV_WARPS) {
     // voxels of this thread's 4 K columns: 2tig, 2tig+1, 2tig+8, 2tig+9
     int vi[4], vj[4], vk[4];
     bool vok[4];
@@ -227,8 +252,8 @@ __global__ void __launch_bounds__(32 * CONV_WARPS)
       const int h = q & 1;
       float e[2];
 #pragma unroll
-      for (int s = 0; s < 2; ++s) {
-        const int col = 2 * (q >> 1) + s;   // index into the 4 voxels of this thread
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int col = 2 * (q >> 1) + s2;
         float val = 0.f;
         if (vok[col]) {
           if (kind[h] == 1) {
@@ -238,30 +263,25 @@ __global__ void __launch_bounds__(32 * CONV_WARPS)
             val = nb < 0 ? 0.f : ldf(in, (int64_t)nb * cin + ch[h]);
           }
         }
-        e[s] = val;
+        e[s2] = val;
       }
       a[q] = pack2(e[0], e[1]);
     }
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-      const int n = nt * 8 + gid;
-      float bv[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int64_t v = vb + 2 * tig + (q & 1) + 8 * (q >> 1);
-        bv[q] = (q < 4 && v < vend && n < cout) ? dout[v * cout + n] : 0.f;
-      }
-      mma_bf16(c[nt], a, pack2(bv[0], bv[1]), pack2(bv[2], bv[3]));
-    }
-  }
-  const int nw = 27 * cin * cout + cout;
-#pragma unroll
-  for (int nt = 0; nt < NT; ++nt)
+    float bv[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const int kr = m0 + gid + 8 * (q >> 1), n = nt * 8 + 2 * tig + (q & 1);
-      if (kr < rows && n < cout) part[(int64_t)chunk * nw + (int64_t)kr * cout + n] = c[nt][q];
+      const int64_t v = vb + 2 * tig + (q & 1) + 8 * (q >> 1);
+      bv[q] = (v < vend && n < cout) ? dout[v * cout + n] : 0.f;
     }
+    mma_bf16(c, a, pack2(bv[0], bv[1]), pack2(bv[2], bv[3]));
+  }
+  if (!reduce_warps(c, red)) return;
+  const int nw = 27 * cin * cout + cout;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int kr = m0 + gid + 8 * (q >> 1), nc = blockIdx.y * 8 + 2 * tig + (q & 1);
+    if (kr < rows && nc < cout) part[(int64_t)chunk * nw + (int64_t)kr * cout + nc] = c[q];
+  }
 }
 
 __global__ void sum_chunks_kernel(int nw, int nchunk, const float* __restrict__ part, float* __restrict__ out,
@@ -488,30 +508,6 @@ __global__ void inject_kernel(Grid gf, int stride, const double* __restrict__ uf
 using namespace pmg;
 using namespace pmg::nn;
 
-// output columns of the convolution kernels in tiles of 8, templated on the tile count (1, 2, 4, 8 or 12:
-// up to 96 channels)
-constexpr int CONV_MAX_NT = 12;
-#define CONV_NT_DISPATCH(c, ...)                      \
-  do {                                                \
-    const int nt_ = ((c) + 7) / 8;                    \
-    if (nt_ <= 1) {                                   \
-      constexpr int NT = 1;                           \
-      __VA_ARGS__;                                    \
-    } else if (nt_ <= 2) {                            \
-      constexpr int NT = 2;                           \
-      __VA_ARGS__;                                    \
-    } else if (nt_ <= 4) {                            \
-      constexpr int NT = 4;                           \
-      __VA_ARGS__;                                    \
-    } else if (nt_ <= 8) {                            \
-      constexpr int NT = 8;                           \
-      __VA_ARGS__;                                    \
-    } else {                                          \
-      constexpr int NT = 12;                          \
-      __VA_ARGS__;                                    \
-    }                                                 \
-  } while (0)
-
 static bool vgrid_ok(int nx, int ny, int nz) {
   return nx > 0 && ny > 0 && nz > 0 && (int64_t)nx * ny * nz < (int64_t(1) << 30);
 }
@@ -520,35 +516,28 @@ extern "C" {
 
 int pmg_nn_conv3d_forward(int nx, int ny, int nz, int cin, int cout, int in_is_f32, const void* in, const void* w,
                           const float* bias, int relu, void* out_bf16, float* out_f32, void* stream) {
-  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || cout > 8 * CONV_MAX_NT || !in || !w ||
-      (!out_bf16 && !out_f32))
-    return PMG_BAD_ARG;
+  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || !in || !w || (!out_bf16 && !out_f32)) return PMG_BAD_ARG;
   VGrid g{nx, ny, nz};
-  const unsigned blocks = (unsigned)((g.nvox() + 16 * CONV_WARPS - 1) / (16 * CONV_WARPS));
+  const dim3 grid((unsigned)((g.nvox() + 15) / 16), (unsigned)((cout + 7) / 8));
   cudaStream_t st = as_stream(stream);
   const auto* wb = (const __nv_bfloat16*)w;
   auto* ob = (__nv_bfloat16*)out_bf16;
-  CONV_NT_DISPATCH(cout, {
-    if (in_is_f32)
-      conv3d_fwd_kernel<float, NT><<<blocks, 32 * CONV_WARPS, 0, st>>>(g, cin, cout, (const float*)in, wb, bias, relu,
-                                                                       ob, out_f32);
-    else
-      conv3d_fwd_kernel<__nv_bfloat16, NT><<<blocks, 32 * CONV_WARPS, 0, st>>>(g, cin, cout, (const __nv_bfloat16*)in,
-                                                                               wb, bias, relu, ob, out_f32);
-  });
+  if (in_is_f32)
+    conv3d_fwd_kernel<float><<<grid, 32 * CONV_WARPS, 0, st>>>(g, cin, cout, (const float*)in, wb, bias, relu, ob,
+                                                               out_f32);
+  else
+    conv3d_fwd_kernel<__nv_bfloat16><<<grid, 32 * CONV_WARPS, 0, st>>>(g, cin, cout, (const __nv_bfloat16*)in, wb,
+                                                                       bias, relu, ob, out_f32);
   return check_launch();
 }
 
 int pmg_nn_conv3d_backward_data(int nx, int ny, int nz, int cin, int cout, const float* dout, const void* w, float* din,
                                 void* stream) {
-  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || cin > 8 * CONV_MAX_NT || !dout || !w || !din)
-    return PMG_BAD_ARG;
+  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || !dout || !w || !din) return PMG_BAD_ARG;
   VGrid g{nx, ny, nz};
-  const unsigned blocks = (unsigned)((g.nvox() + 16 * CONV_WARPS - 1) / (16 * CONV_WARPS));
-  CONV_NT_DISPATCH(cin, {
-    conv3d_dgrad_kernel<NT><<<blocks, 32 * CONV_WARPS, 0, as_stream(stream)>>>(g, cin, cout, dout,
-                                                                              (const __nv_bfloat16*)w, din);
-  });
+  const dim3 grid((unsigned)((g.nvox() + 15) / 16), (unsigned)((cin + 7) / 8));
+  conv3d_dgrad_kernel<<<grid, 32 * CONV_WARPS, 0, as_stream(stream)>>>(g, cin, cout, dout, (const __nv_bfloat16*)w,
+                                                                      din);
   return check_launch();
 }
 
@@ -560,22 +549,19 @@ size_t pmg_nn_wgrad_scratch_bytes(int nx, int ny, int nz, int cin, int cout) {
 
 int pmg_nn_conv3d_backward_weights(int nx, int ny, int nz, int cin, int cout, int in_is_f32, const void* in,
                                    const float* dout, float* dw_db, int accumulate, void* scratch, void* stream) {
-  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || cout > 8 * CONV_MAX_NT || !in || !dout || !dw_db || !scratch)
-    return PMG_BAD_ARG;
+  if (!vgrid_ok(nx, ny, nz) || cin <= 0 || cout <= 0 || !in || !dout || !dw_db || !scratch) return PMG_BAD_ARG;
   VGrid g{nx, ny, nz};
   const int nw = 27 * cin * cout + cout;
   const int nchunk = (int)((g.nvox() + WG_CHUNK - 1) / WG_CHUNK);
-  const int mtiles = (27 * cin + 1 + 15) / 16;
   cudaStream_t st = as_stream(stream);
-  dim3 grid((mtiles + CONV_WARPS - 1) / CONV_WARPS, nchunk);
-  CONV_NT_DISPATCH(cout, {
-    if (in_is_f32)
-      conv3d_wgrad_partial_kernel<float, NT><<<grid, 32 * CONV_WARPS, 0, st>>>(g, cin, cout, (const float*)in, dout,
-                                                                               (float*)scratch);
-    else
-      conv3d_wgrad_partial_kernel<__nv_bfloat16, NT><<<grid, 32 * CONV_WARPS, 0, st>>>(
-          g, cin, cout, (const __nv_bfloat16*)in, dout, (float*)scratch);
-  });
+  const dim3 grid((unsigned)((27 * cin + 1 + 15) / 16), (unsigned)((cout + 7) / 8), (unsigned)nchunk);
+  if (in_is_f32)
+    conv3d_wgrad_partial_kernel<float><<<grid, 32 * CONV_WARPS, 0, st>>>(g, cin, cout, (const float*)in, dout,
+                                                                         (float*)scratch);
+  else
+    conv3d_wgrad_partial_kernel<__nv_bfloat16><<<grid, 32 * CONV_WARPS, 0, st>>>(g, cin, cout,
+                                                                                 (const __nv_bfloat16*)in, dout,
+                                                                                 (float*)scratch);
   sum_chunks_kernel<<<(nw + 255) / 256, 256, 0, st>>>(nw, nchunk, (const float*)scratch, dw_db, accumulate);
   return check_launch();
 }
