@@ -390,7 +390,8 @@ __global__ void input_features_kernel(Grid ge, int s, VGrid gv, const double* __
   if (v >= gv.nvox()) return;
   int i, j, k;
   vox_ijk(gv, (int)v, i, j, k);
-  double acc = 0.0;
+  // the feature is stored in BF16: the cube root and the mean in FP32 (no FP64 arithmetic per element)
+  float acc = 0.f;
   int cnt = 0;
   const int ez = ge.nz == 0 ? 1 : ge.nz;
   for (int c = 0; c < s; ++c)
@@ -398,11 +399,11 @@ __global__ void input_features_kernel(Grid ge, int s, VGrid gv, const double* __
       for (int a = 0; a < s; ++a) {
         const int ei = i * s + a, ej = j * s + b, ek = k * s + c;
         if (ei < ge.nx && ej < ge.ny && ek < ez) {
-          acc += cbrt(xe[((int64_t)ek * ge.ny + ej) * ge.nx + ei]);
+          acc += cbrtf((float)xe[((int64_t)ek * ge.ny + ej) * ge.nx + ei]);
           ++cnt;
         }
       }
-  const float m = cnt ? (float)(acc / cnt) : 0.f;
+  const float m = cnt ? acc / (float)cnt : 0.f;
   feat[v * 4 + 0] = __float2bfloat16(2.f * m - 1.f);
   feat[v * 4 + 1] = __float2bfloat16(2.f * (i + 0.5f) / gv.nx - 1.f);
   feat[v * 4 + 2] = __float2bfloat16(2.f * (j + 0.5f) / gv.ny - 1.f);

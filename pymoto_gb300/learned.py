@@ -215,7 +215,9 @@ class LearnedWarmStart:
                  use_net=True, history=1, train_every=1, gate=0.0, gate_skip=3, coarse_correction=False):
         """train_every: train on every k-th observed solution (the pairs are stored every time).
         gate, gate_skip: when the network's prediction carried less than `gate` of the energy norm of the
-        Rayleigh-Ritz initial guess, skip the next `gate_skip` predictions (then predict again); 0 disables.
+        Rayleigh-Ritz initial guess, skip the next `gate_skip` predictions (then predict again); each further
+        prediction below the gate in a row doubles the skip (at most 32) and the training interval (at most
+        8 x train_every), a prediction above it resets both; gate 0 disables.
         coarse_correction: MixedPrecisionCG also uses the prediction w of a solve as a one-dimensional coarse
         space in every flexible-CG iteration, deflated (A-DEF2, Tang, Nabben, Vuik, Erlangga, J. Sci. Comput.
         39 (2009)): z = M(r - (w.r / w.Kw) Kw) + (w.r / w.Kw) w."""
@@ -224,6 +226,7 @@ class LearnedWarmStart:
         self.coarse_correction = bool(coarse_correction)
         self.train_every, self.gate, self.gate_skip = max(1, int(train_every)), float(gate), int(gate_skip)
         self._skip = 0
+        self._fail = 0              # predictions below the gate in a row
         self._predicted = False
         self.predictions = 0
         self.history = int(history)
@@ -270,7 +273,8 @@ class LearnedWarmStart:
         """Network, training buffer, sample count, random state, gate and history (checkpoint)."""
         self.sync_training()
         return {"net": self.net.state_dict(), "feats": self.feats, "targets": self.targets, "count": self.count,
-                "rng": self.rng.bit_generator.state, "skip": self._skip, "predictions": self.predictions,
+                "rng": self.rng.bit_generator.state, "skip": self._skip, "fail": self._fail,
+                "predictions": self.predictions,
                 "hist": list(self._hist)}
 
     def load_state_dict(self, sd):
@@ -279,6 +283,7 @@ class LearnedWarmStart:
         self.feats.copy_(sd["feats"].to(self.feats.device))
         self.targets.copy_(sd["targets"].to(self.targets.device))
         self.count, self._skip, self.predictions = int(sd["count"]), int(sd["skip"]), int(sd["predictions"])
+        self._fail = int(sd.get("fail", 0))
         self.rng.bit_generator.state = sd["rng"]
         self._hist = [h.to(self.targets.device) for h in sd["hist"]]
 
@@ -321,9 +326,15 @@ class LearnedWarmStart:
 
     def report(self, shares):
         """Energy shares of the Rayleigh-Ritz directions of the last solve (the prediction is the last one when
-        it was used): a prediction below the gate suspends the next `gate_skip` predictions."""
-        if self._predicted and self.gate > 0.0 and len(shares) and float(shares[-1]) < self.gate:
-            self._skip = self.gate_skip
+        it was used): a prediction below the gate suspends the next predictions (gate_skip, doubled for each
+        further one below the gate in a row, at most 32)."""
+        if not self._predicted or self.gate <= 0.0 or not len(shares):
+            return
+        if float(shares[-1]) < self.gate:
+            self._fail += 1
+            self._skip = min(32, self.gate_skip << min(self._fail - 1, 5))
+        else:
+            self._fail = 0
 
     def observe(self, A, u):
         """Store the pair (stiffness field of A, solution u) and train on the stored pairs (side stream)."""
@@ -344,7 +355,8 @@ class LearnedWarmStart:
         call("pmg_dot", F64, self.ncn, t, t, self._sc[0:1], ws.reduce, stream())
         call("pmg_scale_rsqrt", F64, self.ncn, t, t, self._sc[0:1], stream())   # unit 2-norm
         self.count += 1
-        if (self.count - 1) % self.train_every == 0 and self.train_steps > 0:
+        every = self.train_every << min(self._fail, 3)      # backs off while the predictions do not help
+        if (self.count - 1) % every == 0 and self.train_steps > 0:
             slots = [int(self.rng.integers(min(self.count, self.capacity))) for _ in range(self.train_steps)]
             if self.side_stream is None:
                 for sl in slots:
