@@ -283,6 +283,12 @@ int pmg_oc_update(int64_t n, const double* x, const double* dg, double* xnew, do
 /* Status of the last pmg_oc_update on `scratch` (host-synchronous read): PMG_OK, or PMG_TIMEOUT if a
  * bounded wait of the single-launch bisection expired (its CTAs were not all resident). */
 int pmg_oc_status(const void* scratch);
+/* Test control of the bounded device waits of the OC update (host-synchronous): every wait gives up after
+ * `polls` polls (0: the built-in limit of a few seconds), and with withhold_arrival != 0 the last CTA of the
+ * grid-wide barrier withholds its arrival, so that the waits run out; the update then ends with PMG_TIMEOUT in
+ * pmg_oc_status.  For tests of the failure path; no counterpart in the reference (pyMOTO's OC has no device
+ * waits). */
+int pmg_set_wait_test(unsigned polls, int withhold_arrival);
 /* The same status word copied into host memory (`status`, pinned for an asynchronous copy) in stream order:
  * nonzero once the copy has completed means the bisection's bounded wait expired.  Lets a host loop read
  * the status at its next synchronisation instead of adding one. */

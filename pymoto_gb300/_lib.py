@@ -48,6 +48,7 @@ SIGNATURES = {
     "pmg_stencil_cheb_step": (I, [I, I, I, I, P, P, P, P, P, P, I, P, P]),
     "pmg_ebe_cheb_step": (I, [I, I, I, P, P, P, D, P, P, P, P, P, I, P, P, P]),
     "pmg_operator_status": (I, [I]),
+    "pmg_set_wait_test": (I, [ctypes.c_uint, I]),
     "pmg_cholesky_factor": (I, [I, P, I, P, P]),
     "pmg_cholesky_solve": (I, [I, I, P, I, P, P, P]),
     "pmg_cholesky_inverse": (I, [I, P, I, P, P]),
@@ -160,7 +161,8 @@ def _arg(a):
 _HOST_ONLY = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_element_stiffness", "pmg_galerkin_table",
               "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth",
               "pmg_cholesky_inverse_f32_scratch_bytes", "pmg_nn_wgrad_scratch_bytes", "pmg_oc_status",
-              "pmg_coarse_ordering", "pmg_oc_status_async", "pmg_mma_scratch_bytes", "pmg_operator_status"}
+              "pmg_coarse_ordering", "pmg_oc_status_async", "pmg_mma_scratch_bytes", "pmg_operator_status",
+              "pmg_set_wait_test"}
 
 
 def _launches(name, args):

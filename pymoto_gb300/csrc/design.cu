@@ -448,6 +448,14 @@ __global__ void __launch_bounds__(OC_THREADS) oc_step_kernel(int64_t n, const do
 constexpr int OCP_PER_THREAD = 8;
 constexpr unsigned OC_SPIN_LIMIT = 1u << 24;   // polls of about 0.1-0.5 us each: a few seconds at most
 
+// Test control of the bounded waits (pmg_set_wait_test): a poll limit replacing OC_SPIN_LIMIT (0: the default)
+// and a switch that makes the last CTA withhold its arrival at the grid barrier, a flag nothing else sets.
+struct WaitTest {
+  unsigned limit;
+  unsigned withhold;
+};
+__device__ WaitTest g_wait_test = {0u, 0u};
+
 __device__ __forceinline__ double oc_exact_value(double xi, double gi, double sc, double move, double xmin,
                                                  double xmax) {
   const double g = gi < 0.0 ? gi : 0.0;
@@ -479,6 +487,8 @@ __global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, co
   __shared__ int s_abort, s_mode, s_depth;
   __shared__ double s_lmid;
   volatile OCScratch* vs = (volatile OCScratch*)s;
+  const WaitTest wt = g_wait_test;
+  const unsigned spin_limit = wt.limit ? wt.limit : OC_SPIN_LIMIT;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -566,13 +576,13 @@ __global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, co
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
-      vs->arrived[blockIdx.x] = gen;
+      if (!(wt.withhold && blockIdx.x == gridDim.x - 1)) vs->arrived[blockIdx.x] = gen;
     }
     if (blockIdx.x == 0) {
       for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
         unsigned polls = 0;
         while (vs->arrived[b] < gen) {
-          if (++polls > OC_SPIN_LIMIT) {
+          if (++polls > spin_limit) {
             atomicExch(&s->error, 1u);
             s_abort = 1;
             break;
@@ -638,7 +648,7 @@ __global__ void __launch_bounds__(OC_THREADS) oc_persistent_kernel(int64_t n, co
     } else if (threadIdx.x == 0) {
       unsigned polls = 0;
       while (vs->generation < gen) {
-        if (++polls > OC_SPIN_LIMIT) {
+        if (++polls > spin_limit) {
           atomicExch(&s->error, 1u);
           s_abort = 1;
           break;
@@ -765,6 +775,16 @@ int pmg_sens_contract_mixed(int nelx, int nely, int nelz, const double* K0_host,
 }
 
 size_t pmg_oc_scratch_bytes(void) { return sizeof(OCScratch); }
+
+int pmg_set_wait_test(unsigned polls, int withhold_arrival) {
+  const WaitTest wt = {polls, withhold_arrival ? 1u : 0u};
+  cudaError_t e = cudaMemcpyToSymbol(g_wait_test, &wt, sizeof(wt));
+  if (e != cudaSuccess) {
+    set_error(cudaGetErrorString(e));
+    return PMG_CUDA_ERR;
+  }
+  return PMG_OK;
+}
 
 int pmg_oc_status(const void* scratch) {
   if (!scratch) return PMG_BAD_ARG;

@@ -76,3 +76,33 @@ def test_wrongly_sized_design_is_rejected():
     d = pg.VoxelDomain(*SHAPE)
     with pytest.raises(ValueError):
         pg.AssembleStiffness(d, bc=bc)(torch.ones(d.nel + 1, dtype=torch.float64, device="cuda"))
+
+
+def test_a_bounded_device_wait_that_runs_out_reports_a_timeout():
+    """The OC update's grid-wide barrier waits a bounded number of polls.  With the test control, the last CTA
+    withholds its arrival (a flag nothing else sets) and the waits give up after 1,000 polls: the update ends
+    with PMG_TIMEOUT in its status word, the context stays usable, and with the control reset the same update
+    succeeds and matches the oracle's bisection."""
+    import pymoto_gb300 as pg
+    from pymoto_gb300 import _lib
+    lib = _lib.load()
+    n = 200_000
+    rng = np.random.default_rng(5)
+    x = rng.uniform(0.2, 0.8, n)
+    dg = -rng.uniform(0.1, 1.0, n)
+    xd, dgd = torch.from_numpy(x).cuda(), torch.from_numpy(dg).cuda()
+    xnew = torch.empty_like(xd)
+    scratch = torch.zeros(lib.pmg_oc_scratch_bytes() // 8 + 1, dtype=torch.float64, device="cuda")
+    st = _lib.stream()
+    try:
+        _lib.call("pmg_set_wait_test", 1000, 1)
+        _lib.call("pmg_oc_update", n, xd, dgd, xnew, 0.5, 0.2, 0.0, 1.0, 0.0, 1e5, 1e-4, scratch, st)
+        torch.cuda.synchronize()
+        assert lib.pmg_oc_status(scratch.data_ptr()) == 3           # PMG_TIMEOUT
+    finally:
+        _lib.call("pmg_set_wait_test", 0, 0)
+    _lib.call("pmg_oc_update", n, xd, dgd, xnew, 0.5, 0.2, 0.0, 1.0, 0.0, 1e5, 1e-4, scratch, st)
+    torch.cuda.synchronize()
+    assert lib.pmg_oc_status(scratch.data_ptr()) == 0
+    ref = O.oc_step(x, dg, 0.5, move=0.2)
+    np.testing.assert_allclose(xnew.cpu().numpy(), ref, rtol=0, atol=1e-12)
