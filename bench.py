@@ -42,7 +42,7 @@ REF_LEVELS = 4          # the reference example's hierarchy: coarsest 16x8x8 (Su
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) per launch of the roofline kernel at the bench workload, from the ncu capture
 # summarised in profiles/ebe_apply_tc_residual_hex8_128x64x64.md
-NCU_TRAFFIC_PER_LAUNCH = {"ebe_apply_tc_residual_f32": 15.756e6}
+NCU_TRAFFIC_PER_LAUNCH = {"ebe_apply_tc_residual_f32": 15.756e6, "ebe_apply_fma_residual_f32": 15.772e6}
 
 
 def parse():
@@ -320,12 +320,14 @@ def headline_arm(results):
 
 
 def kernel_rooflines(run, flush, torch, reps=20):
-    """Live CUDA-event times of the two level-0 operator kernels on the headline arm's final operators, one
-    launch at a time on the current stream with the L2 flushed (256 MB write) before each launch:
-      * the FP32 tensor-core operator (ebe_apply_tc, residual mode): the most launched kernel of a design
-        iteration (one matvec, one residual and one Chebyshev step per inner iteration);
+    """Live CUDA-event times of the level-0 operator kernels on the headline arm's final operators, one launch at
+    a time on the current stream with the L2 flushed (256 MB write) before each launch:
+      * the FP32 matrix-free operator in residual mode, the most launched kernel of a design iteration (one
+        matvec, one residual and one Chebyshev step per inner iteration), in both implementations: FP32 FMAs on
+        the CUDA cores ("fma") and 3xTF32 tcgen05.mma products ("tcgen05");
       * the FP64 node-stencil product (the outer FCG operator), whose bound is the FP64 pipe.
     Returns per kernel: seconds per launch, algorithmic bytes and flops per launch."""
+    import pymoto_gb300 as pg
     from pymoto_gb300._lib import MATVEC, RESIDUAL
     sol = run.solver
     A32, A64 = sol.A32, sol.A64
@@ -350,11 +352,15 @@ def kernel_rooflines(run, flush, torch, reps=20):
             tot += e0.elapsed_time(e1)
         return tot / reps * 1e-3
 
-    out = {}
-    t = timed(lambda: A32.apply(RESIDUAL, u32, b32, out=y32))
-    # u, b read and y written once (FP32), element scaling (FP32) and the node constraint mask (bytes)
-    out["ebe_apply_tc_residual_f32"] = {"s": t, "bytes": 3 * 4 * ndof + 4 * nel + nn,
-                                         "flops": 3 * 2 * 24 * 24 * nel}     # three TF32 products per element
+    out = {"selected": pg.operator_kernel()}
+    for kind in ("fma", "tcgen05"):
+        prev = pg.set_operator_kernel(kind)
+        t = timed(lambda: A32.apply(RESIDUAL, u32, b32, out=y32))
+        pg.set_operator_kernel(prev)
+        # u, b read and y written once (FP32), element scaling (FP32) and the node constraint mask (bytes);
+        # 24 x 24 FMAs per element (the tensor-core form runs three TF32 products of that size)
+        out[f"ebe_apply_{kind}_residual_f32"] = {"s": t, "bytes": 3 * 4 * ndof + 4 * nel + nn,
+                                                 "flops": 2 * 24 * 24 * nel}
     t = timed(lambda: A64.apply(MATVEC, u64, out=y64))
     # 27 blocks of 3 x 3 per row of 3 dofs: 81 FP64 FMA per dof; stored stencils (14 blocks) + u + y once
     out["stencil_apply_f64_matvec"] = {"s": t, "bytes": 8 * (126 * nn + 2 * ndof), "flops": 2 * 81 * ndof}
@@ -504,9 +510,9 @@ def cpu_reference_sample(shape, warm_steps=1, warmup=1, seed=1234):
 
 
 def operator_case(args):
-    """Operator products of the workload alone: FP32 tensor-core operator (residual mode), FP64 stencil
-    product, FP32 level-1 stencil residual; 3 launches each after 2 warm-up launches, CUDA-event times
-    printed as JSON (a small case for ncu)."""
+    """Operator products of the workload alone: the FP32 level-0 operator in residual mode (CUDA-core and
+    tensor-core implementations), FP64 stencil product, FP32 level-1 stencil residual; 3 launches each after 2
+    warm-up launches, CUDA-event times printed as JSON (a small case for ncu)."""
     import torch
     import pymoto_gb300 as pg
     from pymoto_gb300._lib import F32, RESIDUAL, MATVEC
@@ -522,7 +528,16 @@ def operator_case(args):
     u1 = torch.randn(A1.grid.ndof, device="cuda")
     b1 = torch.randn_like(u1)
     out = {}
-    for name, fn in [("ebe_apply_tc_f32_residual", lambda: K32.apply(RESIDUAL, u32, b32)),
+
+    def with_kernel(kind, fn):
+        def run():
+            prev = pg.set_operator_kernel(kind)
+            fn()
+            pg.set_operator_kernel(prev)
+        return run
+
+    for name, fn in [("ebe_apply_fma_f32_residual", with_kernel("fma", lambda: K32.apply(RESIDUAL, u32, b32))),
+                     ("ebe_apply_tc_f32_residual", with_kernel("tcgen05", lambda: K32.apply(RESIDUAL, u32, b32))),
                      ("stencil_apply_f64_matvec", lambda: K.apply(MATVEC, u)),
                      ("stencil_apply_f32_level1_residual", lambda: A1.apply(RESIDUAL, u1, b1))]:
         for _ in range(2):
@@ -535,6 +550,12 @@ def operator_case(args):
         e1.record()
         torch.cuda.synchronize()
         out[name + "_us"] = e0.elapsed_time(e1) / 3 * 1e3
+    prev = pg.set_operator_kernel("fma")
+    ya = K32.apply(RESIDUAL, u32, b32)
+    pg.set_operator_kernel("tcgen05")
+    yb = K32.apply(RESIDUAL, u32, b32)
+    pg.set_operator_kernel(prev)
+    out["fma_vs_tc_max_rel_diff"] = float((ya - yb).abs().max() / yb.abs().max())
     print(json.dumps({"case": "operator", "shape": list(shape), **out}))
 
 
@@ -718,18 +739,33 @@ def main():
         val_plain = aggregate_rate(world, steps, R["plain_fp64"]["total_ms"] / 1e3) if "plain_fp64" in R else None
         # rooflines of the level-0 operator kernels, timed live after the timed region (kernel_rooflines)
         K = m["kernels"]
-        km = K["ebe_apply_tc_residual_f32"]
-        achieved = km["bytes"] / km["s"] / 1e9
+        sel = K["selected"]
+        kdesc = {"fma": "ebe_apply_fma_kernel<residual> (FP32 operator, FP32 FMAs on the CUDA cores, one thread per "
+                        "node column)",
+                 "tcgen05": "ebe_apply_tc_kernel<residual> (FP32 operator, 3xTF32 tcgen05.mma, accumulators in TMEM)"}
+        fp32_peak = 2 * 128 * torch.cuda.get_device_properties(0).multi_processor_count * \
+            m["peaks"].get("sm_max_mhz", 2070.0) * 1e6 / 1e12            # 128 FP32 FMA/clk/SM nominal
         tf32_peak = m["peaks"].get("bf16_tflops", 1900.0) / 2.0       # dense TF32 runs at half the BF16 rate
-        roofline = {"bound": "hbm", "kernel": "ebe_apply_tc_kernel<residual> (FP32 operator, 3xTF32 tcgen05.mma, "
-                                               "grid %s)" % "x".join(map(str, shape)),
-                    "achieved": achieved, "peak": m["hbm_peak"], "unit": "GB/s", "frac": achieved / m["hbm_peak"],
-                    "traffic": NCU_TRAFFIC_PER_LAUNCH.get("ebe_apply_tc_residual_f32"),
-                    "bytes_per_launch": km["bytes"], "avg_launch_us": km["s"] * 1e6,
-                    "tensor_tflops": km["flops"] / km["s"] / 1e12, "tensor_frac_of_tf32": km["flops"] / km["s"] / 1e12
-                    / tf32_peak, "peak_source": m["peak_src"],
-                    "launches_per_step": "3 per inner FP32 PCG iteration (matvec, V-cycle residual, Chebyshev step)",
-                    "note": "one launch at a time after a 256 MB L2 flush, CUDA events on the launching stream"}
+
+        def op_roofline(kind):
+            km = K[f"ebe_apply_{kind}_residual_f32"]
+            achieved = km["bytes"] / km["s"] / 1e9
+            r = {"bound": "hbm", "kernel": kdesc[kind] + ", grid %s" % "x".join(map(str, shape)),
+                 "achieved": achieved, "peak": m["hbm_peak"], "unit": "GB/s", "frac": achieved / m["hbm_peak"],
+                 "traffic": NCU_TRAFFIC_PER_LAUNCH.get(f"ebe_apply_{kind}_residual_f32"),
+                 "bytes_per_launch": km["bytes"], "avg_launch_us": km["s"] * 1e6, "peak_source": m["peak_src"],
+                 "fp32_tflops": km["flops"] / km["s"] / 1e12,
+                 "fp32_frac_of_nominal": km["flops"] / km["s"] / 1e12 / fp32_peak}
+            if kind == "tcgen05":
+                r["tensor_tflops"] = 3 * km["flops"] / km["s"] / 1e12
+                r["tensor_frac_of_tf32"] = r["tensor_tflops"] / tf32_peak
+            return r
+
+        roofline = op_roofline(sel)
+        roofline.update({"launches_per_step": "3 per inner FP32 PCG iteration (matvec, V-cycle residual, Chebyshev "
+                                              "step)",
+                         "note": "one launch at a time after a 256 MB L2 flush, CUDA events on the launching stream"})
+        roofline_alt = op_roofline("tcgen05" if sel == "fma" else "fma")
         ks = K["stencil_apply_f64_matvec"]
         sms = torch.cuda.get_device_properties(0).multi_processor_count
         fp64_peak = 2 * 2 * sms * m["peaks"].get("sm_max_mhz", 2070.0) * 1e6 / 1e12   # 2 DFMA/clk/SM nominal
@@ -793,7 +829,8 @@ def main():
                            m["c_tight"], "rel_diff": abs(m["c_mixed"] - m["c_tight"]) / abs(m["c_tight"]),
                            "mixed_true_rel_residual": m["res_mixed_same_design"]},
                 "parity_vs_oracle": parity_oracle,
-                "roofline": roofline, "roofline_fp64_stencil": roofline_fp64, "cpu_baseline": cpu,
+                "roofline": roofline, "roofline_other_operator_kernel": roofline_alt,
+                "roofline_fp64_stencil": roofline_fp64, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": "design it/s", "h2d_bytes_per_step": 8 * m["nel"],
                         "d2h_bytes_per_step": 8 * m["nel"] + 8, "arm": H,
                         "same_designs_as_value": m["e2e_same_designs"],

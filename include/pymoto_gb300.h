@@ -144,7 +144,7 @@ int pmg_cheb_coeffs(const double* lmax_dev, double lmax_host, double ratio, int 
  * (d not read at step 0), y = u + d (y != u). */
 int pmg_stencil_cheb_step(int dtype, int nelx, int nely, int nelz, const void* S, const void* u, const void* b,
                           const void* dl1, void* d, const double* coef, int step, void* y, void* stream);
-/* The same on the matrix-free FP32 3D level-0 operator (tensor-core kernel of pmg_ebe_apply). */
+/* The same on the matrix-free FP32 3D level-0 operator (the kernel of pmg_ebe_apply). */
 int pmg_ebe_cheb_step(int nelx, int nely, int nelz, const float* xe, const double* K0_host, const uint8_t* bcmask,
                       double bcdiag, const float* u, const float* b, const float* dl1, float* d, const double* coef,
                       int step, float* y, const float* cdiag, void* stream);
@@ -153,6 +153,13 @@ int pmg_ebe_cheb_step(int nelx, int nely, int nelz, const float* xe, const doubl
  * output is then undefined).  reset != 0 clears the flag.  No counterpart in the reference: pyMOTO's
  * assembly has no device waits. */
 int pmg_operator_status(int reset);
+/* Implementation of the FP32 3D level-0 operator (pmg_ebe_apply, pmg_ebe_cheb_step): PMG_OPERATOR_FMA (default)
+ * runs the element products as FP32 FMAs on the CUDA cores, one thread per node column; PMG_OPERATOR_TCGEN05 as
+ * 3xTF32 products on the tensor cores (tcgen05.mma, accumulators in tensor memory).  Both give FP32-accurate
+ * K(x) u.  Host only; returns the previous selection (kind = -1: the current one, unchanged), or -1 for an
+ * unknown kind.  Process-wide: select before launching, not while another thread launches operator products. */
+enum { PMG_OPERATOR_FMA = 0, PMG_OPERATOR_TCGEN05 = 1 };
+int pmg_set_operator_kernel(int kind);
 /* Step `step`: d = a d + c r / diag, x = x + d; init != 0 starts from x = 0 (d = x = c r / diag). */
 int pmg_cheb_step(int dtype, int64_t n, const void* r, const void* diag, void* d, void* x, const double* coef, int step,
                   int init, void* stream);

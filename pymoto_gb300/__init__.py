@@ -13,7 +13,8 @@ from .core import HOST_RUNTIME, Module, Network, Signal
 from .domain import VoxelDomain
 from .modules import (AssembleMass, AssemblePoisson, AssembleStiffness, DensityFilter, DeviceDyad, EinSum, FilterConv, LinSolve, MathExpression,
                       SIMP, Scaling)
-from .operators import Grid, StencilOperator, StiffnessOperator, element_stiffness
+from .operators import (Grid, StencilOperator, StiffnessOperator, element_stiffness, operator_kernel,
+                        set_operator_kernel)
 from .optimizers import OC
 from .mma import MMA
 from .solvers import (CG, Chebyshev, DampedJacobi, DenseCholesky, GeometricMultigrid, LinearSolver,
@@ -33,4 +34,4 @@ __all__ = ["AssembleMass", "AssemblePoisson", "AssembleStiffness", "DensityFilte
            "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI", "Scaling",
            "MMA", "ScalarToFile", "finite_difference",
            "minimize_oc", "minimize_mma", "OverhangFilter",
-           "save_checkpoint", "load_checkpoint", "DesignLog"]
+           "save_checkpoint", "load_checkpoint", "DesignLog", "set_operator_kernel", "operator_kernel"]

@@ -48,6 +48,7 @@ SIGNATURES = {
     "pmg_stencil_cheb_step": (I, [I, I, I, I, P, P, P, P, P, P, I, P, P]),
     "pmg_ebe_cheb_step": (I, [I, I, I, P, P, P, D, P, P, P, P, P, I, P, P, P]),
     "pmg_operator_status": (I, [I]),
+    "pmg_set_operator_kernel": (I, [I]),
     "pmg_set_wait_test": (I, [ctypes.c_uint, I]),
     "pmg_cholesky_factor": (I, [I, P, I, P, P]),
     "pmg_cholesky_solve": (I, [I, I, P, I, P, P, P]),
@@ -107,7 +108,8 @@ SIGNATURES = {
 
 # Returns that are values, not statuses
 _VALUE_RETURNING = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_reduce_scratch_bytes",
-                    "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth", "pmg_mma_scratch_bytes"}
+                    "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth", "pmg_mma_scratch_bytes",
+                    "pmg_set_operator_kernel"}
 
 F64, F32 = 0, 1
 MATVEC, RESIDUAL, JACOBI = 0, 1, 2
@@ -162,7 +164,7 @@ _HOST_ONLY = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_element
               "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth",
               "pmg_cholesky_inverse_f32_scratch_bytes", "pmg_nn_wgrad_scratch_bytes", "pmg_oc_status",
               "pmg_coarse_ordering", "pmg_oc_status_async", "pmg_mma_scratch_bytes", "pmg_operator_status",
-              "pmg_set_wait_test"}
+              "pmg_set_wait_test", "pmg_set_operator_kernel"}
 
 
 def _launches(name, args):

@@ -154,6 +154,14 @@ struct DotAcc<float> {
 int ebe_apply_tc_f32(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
                      const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
                      const float* cdiag, cudaStream_t st);
+// The same on the CUDA cores (ebe_fma.cu: one thread per node column, FP32 FMAs).
+int ebe_apply_fma_f32(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
+                      const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
+                      const float* cdiag, cudaStream_t st);
+// The implementation selected by pmg_set_operator_kernel.
+int ebe_apply_f32_3d(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
+                     const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
+                     const float* cdiag, cudaStream_t st);
 
 
 }  // namespace pmg

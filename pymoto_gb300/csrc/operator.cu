@@ -9,6 +9,7 @@
 #include <cstdio>
 
 #include <algorithm>
+#include <atomic>
 
 #include "common.cuh"
 
@@ -966,11 +967,22 @@ __global__ void dofconn_kernel(Grid g, int64_t* __restrict__ dc) {
 }
 
 // ------------------------------------------------------------------------------------------ dispatch
+// Implementation of the FP32 3D operator (pmg_set_operator_kernel): CUDA-core FMAs by default.
+static std::atomic<int> g_f32_operator{PMG_OPERATOR_FMA};
+
+int ebe_apply_f32_3d(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
+                     const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
+                     const float* cdiag, cudaStream_t st) {
+  if (g_f32_operator.load(std::memory_order_relaxed) == PMG_OPERATOR_TCGEN05)
+    return ebe_apply_tc_f32(mode, g, xe, K0, bcmask, bcdiag, u, b, diag, w, y, ch, cdiag, st);
+  return ebe_apply_fma_f32(mode, g, xe, K0, bcmask, bcdiag, u, b, diag, w, y, ch, cdiag, st);
+}
+
 template <typename T, int DIM>
 int ebe_apply_t(int mode, Grid g, const void* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
                 const void* u, const void* b, const void* diag, double w, void* y, const void* cdiag, cudaStream_t st) {
   if constexpr (DIM == 3 && sizeof(T) == 4)
-    return ebe_apply_tc_f32(mode, g, (const float*)xe, K0, bcmask, bcdiag, (const float*)u, (const float*)b,
+    return ebe_apply_f32_3d(mode, g, (const float*)xe, K0, bcmask, bcdiag, (const float*)u, (const float*)b,
                             (const float*)diag, w, (float*)y, ChebArgs<float>{nullptr, nullptr, 0}, (const float*)cdiag,
                             st);
   const T* c_ = (const T*)cdiag;
@@ -1170,8 +1182,14 @@ int pmg_ebe_cheb_step(int nelx, int nely, int nelz, const float* xe, const doubl
   if (!grid_ok(nelx, nely, nelz) || nelz == 0 || !xe || !K0_host || !u || !b || !dl1 || !d || !coef || !y || y == u ||
       step < 0 || step >= 64)
     return PMG_BAD_ARG;
-  return ebe_apply_tc_f32(PMG_APPLY_CHEB, Grid{nelx, nely, nelz}, xe, K0_host, bcmask, bcdiag, u, b, dl1, 0.0, y,
+  return ebe_apply_f32_3d(PMG_APPLY_CHEB, Grid{nelx, nely, nelz}, xe, K0_host, bcmask, bcdiag, u, b, dl1, 0.0, y,
                           ChebArgs<float>{d, coef, step}, cdiag, as_stream(stream));
+}
+
+int pmg_set_operator_kernel(int kind) {
+  if (kind == -1) return pmg::g_f32_operator.load();
+  if (kind != PMG_OPERATOR_FMA && kind != PMG_OPERATOR_TCGEN05) return -1;
+  return pmg::g_f32_operator.exchange(kind);
 }
 
 int pmg_stencil_add_diagonal(int dtype, int nelx, int nely, int nelz, void* S, const void* c, void* stream) {

@@ -15,6 +15,23 @@ from ._lib import F32, F64, MATVEC, call, stream
 TORCH_DTYPE = {F64: torch.float64, F32: torch.float32}
 
 
+OPERATOR_KERNELS = {"fma": 0, "tcgen05": 1}
+
+
+def set_operator_kernel(kind):
+    """Select the implementation of the FP32 3D level-0 operator: "fma" (FP32 FMAs on the CUDA cores, the
+    default) or "tcgen05" (3xTF32 products on the tensor cores).  Returns the previous selection."""
+    if kind not in OPERATOR_KERNELS:
+        raise ValueError(f"operator kernel must be one of {sorted(OPERATOR_KERNELS)}")
+    prev = call("pmg_set_operator_kernel", OPERATOR_KERNELS[kind])
+    return {v: k for k, v in OPERATOR_KERNELS.items()}[prev]
+
+
+def operator_kernel():
+    """The selected implementation of the FP32 3D level-0 operator ("fma" or "tcgen05")."""
+    return {v: k for k, v in OPERATOR_KERNELS.items()}[call("pmg_set_operator_kernel", -1)]
+
+
 def stencil_values_per_node(dim):
     """Stored node-stencil values per node: the centre block and the forward-offset blocks of a symmetric
     operator (14 of the 27 blocks in 3D, 5 of 9 in 2D; the others are their neighbours' transposes)."""

@@ -1,7 +1,7 @@
 """Springs to ground: AssembleStiffness(add_constant=...) (pymoto/modules/assembly.py:294-295).
 
 The constant is added after the Dirichlet rows are set, so a constrained dof holds bcdiagval + its spring.  The
-matrix-free operators take a constant diagonal: the FP64 stencils and the FP32 tensor-core product of level 0
+matrix-free operators take a constant diagonal: the FP64 stencils and the FP32 matrix-free product of level 0
 add it exactly, the coarse multigrid levels its restriction R^T c (lumped), which keeps them nonsingular when the
 springs are the only supports.  Fixtures written by pyMOTO (tests/golden/make_golden.py springs): a 2D
 mechanism-like case, a 3D cantilever with springs (one on a Dirichlet dof) and a 3D case supported by springs
