@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--timed-only", action="store_true",
                     help="stop after the timed design iterations (no parity, e2e or kernel timing): for launch lists")
     ap.add_argument("--profile-breakdown", action="store_true", help="print a per-kernel time table")
-    ap.add_argument("--inner-iters", type=int, default=4, help="FP32 PCG iterations per FCG preconditioning")
+    ap.add_argument("--inner-iters", type=int, default=6, help="FP32 PCG iterations per FCG preconditioning")
     ap.add_argument("--inner-tol", type=float, default=0.1)
     ap.add_argument("--fcg-m", type=int, default=1)
     ap.add_argument("--levels", type=int, default=GPU_LEVELS)
@@ -119,8 +119,8 @@ def cantilever(shape):
 class DesignRun:
     """The network of the workload on the device, for one solver arm."""
 
-    opts = {"inner_iters": 4, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None,
-            "smoother": "chebyshev", "cheb_degree": 1, "cheb_coarse_degree": [2, 3, 6], "cheb_ratio": 15.0,
+    opts = {"inner_iters": 6, "inner_tol": 0.1, "m": 1, "levels": GPU_LEVELS, "sweeps": SWEEPS, "coarse_sweeps": None,
+            "smoother": "chebyshev", "cheb_degree": 1, "cheb_coarse_degree": [2, 3, 4], "cheb_ratio": 15.0,
             "learned_train_steps": 1, "learned_stride": 4, "learned_lr": 2e-3, "learned_net": True,
             "learned_history": 0, "learned_train_every": 4, "learned_gate": 0.02, "learned_gate_skip": 3,
             "learned_cc": False,
