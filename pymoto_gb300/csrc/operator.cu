@@ -973,7 +973,8 @@ static std::atomic<int> g_f32_operator{PMG_OPERATOR_FMA};
 int ebe_apply_f32_3d(int mode, Grid g, const float* xe, const double* K0, const uint8_t* bcmask, double bcdiag,
                      const float* u, const float* b, const float* diag, double w, float* y, ChebArgs<float> ch,
                      const float* cdiag, cudaStream_t st) {
-  if (g_f32_operator.load(std::memory_order_relaxed) == PMG_OPERATOR_TCGEN05)
+  const int kind = g_f32_operator.load(std::memory_order_relaxed);
+  if (kind == PMG_OPERATOR_TCGEN05)
     return ebe_apply_tc_f32(mode, g, xe, K0, bcmask, bcdiag, u, b, diag, w, y, ch, cdiag, st);
   return ebe_apply_fma_f32(mode, g, xe, K0, bcmask, bcdiag, u, b, diag, w, y, ch, cdiag, st);
 }

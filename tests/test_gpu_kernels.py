@@ -157,8 +157,8 @@ def operator_kernel(request, pg):
     pg.set_operator_kernel(prev)
 
 
-# tiles of both kernels: several in x, y and z, ragged edges; the last four only on the CUDA-core kernel
-# (its tile widths follow the node counts: 129 -> 5 x 26, 101 -> 4 x 26, 17 x 71 -> 17 x 15)
+# tiles of both kernels: several in x, y and z, ragged edges (the CUDA-core kernel's tile widths follow the node
+# counts: 129 -> 5 x 26, 101 -> 4 x 26, 17 x 71 -> 17 x 15; the tensor-core kernel's tiles are 31 x 8 elements)
 FP32_3D_SHAPES = [(40, 12, 10), (33, 9, 17), (64, 16, 8), (2, 2, 2),
                   (128, 8, 4), (100, 40, 6), (16, 70, 3), (1, 1, 1)]
 
@@ -166,12 +166,10 @@ FP32_3D_SHAPES = [(40, 12, 10), (33, 9, 17), (64, 16, 8), (2, 2, 2),
 @pytest.mark.parametrize("shape", FP32_3D_SHAPES)
 @pytest.mark.parametrize("field", ["random", "smooth"])
 def test_matvec_fp32_3d_tiles(pg, operator_kernel, shape, field):
-    """FP32 3D operator, both implementations: all modes and the fused Chebyshev step against FP64 numpy.
+    """FP32 3D operator, every implementation: all modes and the fused Chebyshev step against FP64 numpy.
     The smooth field sits on a large constant offset: K annihilates the offset, and the result must keep
     its accuracy relative to |K u|, not to |K| |u|.  Two applications give bitwise equal results."""
     from pymoto_gb300._lib import F32, JACOBI, RESIDUAL
-    if operator_kernel == "tcgen05" and shape in FP32_3D_SHAPES[4:]:
-        pytest.skip("tile shapes of the CUDA-core kernel")
     g, K, op, rng = _setup(pg, shape, seed=3)
     if field == "random":
         u = rng.standard_normal(g.ndof)
