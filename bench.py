@@ -668,6 +668,12 @@ def mma_run_case(args):
             fn.response()
         mma = pg.MMA(sx, [g0, g1], fn, move=0.2, verbosity=0)
         xval = mma.x
+        # one untimed sensitivity pass: first uses of library kernels (module loading) stay out of the timing
+        fn.reset()
+        g0.sensitivity = 1.0
+        fn.sensitivity()
+        fn.reset()
+        torch.cuda.synchronize()
         hist, solves = [], []
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

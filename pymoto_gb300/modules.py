@@ -5,6 +5,7 @@ counterpart and runs on the device through libpymoto_gb300.  Signal states may b
 answer is then numpy, so the modules mix with pyMOTO's own modules and optimizers) or CUDA tensors
 (everything stays on the device).
 """
+import math
 import re
 
 import numpy as np
@@ -885,7 +886,7 @@ class LinSolve(Module):
             # projected right-hand side rl (no operator product needed).  Without stored pairs the solver's own
             # initial residual test decides.
             call("pmg_dot2", F64, n, rl, rl, rhs, rhs, sc[2:3], ws.reduce, st)
-            rn, bn = sc[2:4].sqrt().tolist()
+            rn, bn = (math.sqrt(max(v, 0.0)) for v in sc[2:4].tolist())
             rtol = rn / (bn if bn != 0 else 1.0)
             self.last_rtol = rtol
             if rtol <= self.lda_tol:
@@ -948,7 +949,16 @@ class LinSolve(Module):
         dd, kind = _to_device(dfdv, device=self._u_dev.device)
         if self._dim_embed:
             dd = _widen(dd, self._dim_embed)
-        lam = self._lda_solve(dd)
+        # an adjoint solve: a solver's learned warm start (trained on the responses to the design's load) stays
+        # out of it
+        active = getattr(self.solver, "warm_start_active", None)
+        if active is not None:
+            self.solver.warm_start_active = False
+        try:
+            lam = self._lda_solve(dd)
+        finally:
+            if active is not None:
+                self.solver.warm_start_active = active
         dmat = DeviceDyad([-lam], [self._u_dev])
         if self._dim_embed:
             lam = lam[0::self._dim_embed].contiguous()

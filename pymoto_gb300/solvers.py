@@ -68,7 +68,7 @@ class LinearSolver:
         ws = Workspace.get(xd.device)
         out = torch.empty(2, dtype=torch.float64, device=xd.device)
         call("pmg_dot2", F64, r.numel(), r, r, bd, bd, out, ws.reduce, stream())
-        rn, bn = out.sqrt().tolist()
+        rn, bn = (math.sqrt(max(v, 0.0)) for v in out.tolist())
         return rn / (bn if bn != 0 else 1.0)
 
 
@@ -763,6 +763,7 @@ class MixedPrecisionCG(LinearSolver):
         self.restart = restart
         self.verbosity = verbosity
         self.warm_start = warm_start
+        self.warm_start_active = True      # False during adjoint solves (set by LinSolve)
         self.coarse_correction = coarse_correction
         self.iterations = 0
         self.inner_iterations = 0
@@ -985,7 +986,10 @@ class MixedPrecisionCG(LinearSolver):
         ws = Workspace.get(dev)
         st = stream()
         s = B["s"]
-        extra = self.warm_start.basis(A, x0) if self.warm_start is not None and trans == "N" else []
+        # the learned warm start predicts the response to the load of the design, not to other right-hand sides:
+        # LinSolve switches it off (warm_start_active) for the adjoint solves of the sensitivities
+        learn = self.warm_start is not None and trans == "N" and getattr(self, "warm_start_active", True)
+        extra = self.warm_start.basis(A, x0) if learn else []
         if extra:
             # initial guess: energy-optimal combination of the given guess, older solutions and the network's
             # prediction (all with their constrained dofs zeroed)
@@ -1018,7 +1022,7 @@ class MixedPrecisionCG(LinearSolver):
             else:
                 x.zero_()
             A.apply(RESIDUAL, x, b, out=r)
-        if trans == "N":
+        if learn:
             self._set_learned_correction(A, B, vecs, n, dev)
         call("pmg_dot2", F64, n, b, b, r, r, s[0:1], ws.reduce, st)
         bb, rr = s[0:2].tolist()
@@ -1072,7 +1076,7 @@ class MixedPrecisionCG(LinearSolver):
         self.iterations, self.last_residual = it, res
         # the explicit FP64 residual b - A x of the returned solution (LinSolve derives A x from it)
         self.final_residual = r if trans == "N" else None
-        if self.warm_start is not None and trans == "N" and math.isfinite(res):
+        if learn and math.isfinite(res):
             self.warm_start.observe(A, x)
         if not res <= self.tol:   # also a non-finite residual (NaN / Inf in the data)
             warnings.warn(f"MixedPrecisionCG did not reach tol {self.tol}: residual {res}")
