@@ -94,12 +94,9 @@ __global__ void conv_filter_kernel(Grid g, const double* __restrict__ w, int kx,
       if (jj < 0) continue;
       const double* wr = w + ((int64_t)0 * ky + b) * kz + c;
       for (int a = 0; a < kx; ++a) {
-        // taps outside the filter radius have zero weight (a quarter to a third of the box): skipping them skips
-        // an exact zero term, so the sum is unchanged
-        const double wv = wr[(int64_t)a * ky * kz];
         const int ii = px[i + (kx - 1) - a];
-        if (ii < 0 || wv == 0.0) continue;
-        acc = fma(wv, x[elem_id(g, ii, jj, kk)], acc);
+        if (ii < 0) continue;
+        acc = fma(wr[(int64_t)a * ky * kz], x[elem_id(g, ii, jj, kk)], acc);
       }
     }
   }
@@ -134,9 +131,8 @@ __global__ void conv_filter_adjoint_kernel(Grid g, const double* __restrict__ w,
             if (oy < 0 || oy >= g.ny) continue;
             for (int a = 0; a < kx; ++a) {
               const int ox = Px - (kx - 1) + a;
-              const double wv = w[((int64_t)a * ky + b) * kz + c];
-              if (ox < 0 || ox >= g.nx || wv == 0.0) continue;   // zero-weight taps add an exact zero
-              acc = fma(wv, d[elem_id(g, ox, oy, oz)], acc);
+              if (ox < 0 || ox >= g.nx) continue;
+              acc = fma(w[((int64_t)a * ky + b) * kz + c], d[elem_id(g, ox, oy, oz)], acc);
             }
           }
         }
