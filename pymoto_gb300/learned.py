@@ -399,7 +399,7 @@ def rayleigh_ritz(A, b, vectors, out_x, out_r, work, A32=None, work32=None):
     G_ij = v_i^T A v_j, h_i = v_i^T b), and r = b - A x.  `work` holds one FP64 vector per basis vector.
     Returns the coefficients.  Linearly dependent directions are dropped.
     With A32 (the FP32 operator of the same matrix) and work32 (two FP32 vectors) the Gram products use the
-    FP32 tensor-core operator, and r = b - A x is one FP64 product: the coefficients carry the FP32 rounding
+    FP32 level-0 operator, and r = b - A x is one FP64 product: the coefficients carry the FP32 rounding
     of the products, the residual is the exact FP64 residual of the returned x."""
     n = b.numel()
     st = stream()

@@ -187,7 +187,8 @@ class _GalerkinTables:
 class StiffnessOperator:
     """K(x) = sum_e x_e K0 with Dirichlet rows/columns (level 0 of the hierarchy).
 
-    FP32 products are matrix-free on the tensor cores (3D) or the CUDA cores (2D).  FP64 products use
+    FP32 products are matrix-free: in 3D by the kernel set_operator_kernel selects (FP32 FMAs on the CUDA cores
+    by default, or 3xTF32 products on the tensor cores), in 2D on the CUDA cores.  FP64 products use
     half-symmetric node stencils assembled once per operator on the first FP64 product (81 FMA per dof; the
     FP64 pipe of GB300 runs at 1/64 of the FP32 rate, so fewer FMAs win over the 549 MB of stencils at
     128x64x64) unless `fp64_stencil` is False."""
