@@ -227,7 +227,8 @@ int pmg_xpby_ratio(int dtype, int64_t n, void* p, const void* z, const double* n
 int pmg_scale_rsqrt(int dtype, int64_t n, void* y, const void* x, const double* nrm2, void* stream);
 /* y = a * x   (y, x of dtype), scalar a on the host. */
 int pmg_scale(int dtype, int64_t n, void* y, const void* x, double a, void* stream);
-/* y = x with the Dirichlet dofs zeroed (or only the Dirichlet dofs kept when keep_bc != 0). */
+/* y = x with the Dirichlet dofs zeroed (or only the Dirichlet dofs kept when keep_bc != 0).  dim: dofs per node
+ * (1, 2 or 3; bit d of a node's mask byte marks its dof d), here and in pmg_split_bc. */
 int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int keep_bc, const void* x, void* y,
                 void* stream);
 /* One pass: direct = rhs / (bcdiag + cdiag) on the Dirichlet dofs (0 elsewhere; cdiag may be NULL), free_part =
@@ -390,6 +391,36 @@ int pmg_nn_mse(int64_t n, const double* pred, const double* target, double weigh
 /* uc = scale * u_f at every stride-th node of the fine grid (3 components). */
 int pmg_nn_inject(int nelx, int nely, int nelz, int stride, const double* uf, double scale, double* uc,
                   void* stream);
+
+/* ---- One-component operators (one dof per node): AssemblePoisson and AssembleMass with ndof = 1
+ * (pymoto/modules/assembly.py:466-560; the CSR matrix of AssembleGeneral, assembly.py:245-296, and the
+ * multigrid of pymoto/solvers/iterative.py:124-256 for it).  Node stencils are stored in full: S[o * nnodes + n]
+ * (dtype) is the coefficient of node n towards its neighbour at offset o = (dz+1)*9 + (dy+1)*3 + (dx+1)
+ * (27 offsets in 3D, 9 in 2D), zero for neighbours outside the grid.
+ * Level 0: S = sum_e xe_e P0 (xe FP64 per element, P0 the host FP64 element matrix of 2^dim nodes in the local
+ * order of pymoto/common/domain.py:132-142), accumulated in FP64; a node with bit 0 of bcmask set has bcdiag on
+ * its diagonal and nothing else in its row and column; cdiag (FP64 per node, or NULL) is added to the diagonal. */
+int pmg_scalar_stencil(int dtype, int nelx, int nely, int nelz, const double* xe, const double* P0_host,
+                       const uint8_t* bcmask, double bcdiag, const double* cdiag, void* S, void* stream);
+/* y = S u (mode PMG_APPLY_MATVEC), b - S u (PMG_APPLY_RESIDUAL) or u + omega (b - S u) / diag
+ * (PMG_APPLY_JACOBI); y != u. */
+int pmg_scalar_apply(int mode, int dtype, int nelx, int nely, int nelz, const void* S, const void* u, const void* b,
+                     const void* diag, double omega, void* y, void* stream);
+/* rc = R^T rf and uf += R uc with the (bi/tri)linear prolongation R of the grid of nelx x nely x nelz elements
+ * (even counts) onto its coarse grid: weights 1, 1/2, 1/4, 1/8 (pymoto/solvers/iterative.py:182-189). */
+int pmg_scalar_restrict(int dtype, int nelx, int nely, int nelz, const void* rf, void* rc, void* stream);
+int pmg_scalar_prolong_add(int dtype, int nelx, int nely, int nelz, const void* uc, void* uf, void* stream);
+/* Galerkin coarse operator Sc = R^T Sf R (pymoto/solvers/iterative.py:173), stencil to stencil, FP64
+ * accumulation; the grid is the fine one. */
+int pmg_scalar_galerkin(int dtype, int nelx, int nely, int nelz, const void* Sf, void* Sc, void* stream);
+/* Dense FP64 matrix (nnodes x nnodes, row-major, nnodes <= 65536) of a one-component operator. */
+int pmg_scalar_to_dense(int dtype, int nelx, int nely, int nelz, const void* S, double* A, void* stream);
+/* d = sum_o |S(n, o)|: the l1-Jacobi diagonal of the Chebyshev smoother. */
+int pmg_scalar_rowabs(int dtype, int nelx, int nely, int nelz, const void* S, void* d, void* stream);
+/* dx_e (+= when accumulate) alpha u_e^T P0 v_e (FP64) with the Dirichlet nodes of u and v taken as zero: the
+ * design sensitivity of the assembled matrix contracted with the dyad (u, v) (assembly.py:298-315). */
+int pmg_scalar_sens(int nelx, int nely, int nelz, const double* P0_host, const uint8_t* bcmask, const double* u,
+                    const double* v, double alpha, int accumulate, double* dx, void* stream);
 
 #ifdef __cplusplus
 }

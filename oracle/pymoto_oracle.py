@@ -159,18 +159,19 @@ def default_bcdiagval(K0):
 
 
 # --------------------------------------------------------------------------- assembly
-def assemble(grid, K0, x, bc=None, bcdiagval=None):
+def assemble(grid, K0, x, bc=None, bcdiagval=None, ndof=None):
     """K = sum_e x_e K0 with Dirichlet rows/cols zeroed and bcdiagval on their diagonal.
 
     Same matrix as pymoto/modules/assembly.py:245-296 (BC data redirected at :210-230, diagonal set at
-    :272); built here through COO summation instead of the precomputed datamap.
+    :272); built here through COO summation instead of the precomputed datamap.  ndof: dofs per node (default
+    the grid's dimension; 1 for AssemblePoisson and AssembleMass(ndof=1), assembly.py:466-560).
     """
-    dc = grid.dofconn()
+    dc = grid.dofconn(ndof)
     nd = dc.shape[1]
     rows = np.repeat(dc, nd, axis=1).ravel()
     cols = np.tile(dc, (1, nd)).ravel()
     vals = (x.reshape(-1, 1) * K0.reshape(1, -1)).ravel()
-    n = grid.ndof
+    n = grid.nnodes * (grid.dim if ndof is None else ndof)
     if bc is not None and len(bc) > 0:
         bc = np.asarray(bc).ravel()
         isbc = np.zeros(n, dtype=bool)
@@ -186,13 +187,13 @@ def assemble(grid, K0, x, bc=None, bcdiagval=None):
     return K
 
 
-def sensitivity_contract(grid, K0, u_list, v_list, bc=None):
+def sensitivity_contract(grid, K0, u_list, v_list, bc=None, ndof=None):
     """dx_e = sum_k u_k[dofs_e]^T K0 v_k[dofs_e] with constrained rows/cols of the dyad zeroed.
 
     pymoto/modules/assembly.py:298-315 with DyadicMatrix.contract (pymoto/common/dyadcarrier.py:366-414)
-    and the row/column zeroing of dyadcarrier.py:179-189.
+    and the row/column zeroing of dyadcarrier.py:179-189.  ndof: dofs per node (default the grid's dimension).
     """
-    dc = grid.dofconn()
+    dc = grid.dofconn(ndof)
     out = np.zeros(grid.nel)
     for u, v in zip(u_list, v_list):
         u = np.array(u, dtype=np.float64, copy=True)
@@ -320,13 +321,14 @@ def simp_derivative(x, xmin=1e-9, penal=3.0):
 
 
 # --------------------------------------------------------------------------- multigrid
-def prolongation(grid):
+def prolongation(grid, ndof=None):
     """Trilinear prolongation R (fine dofs x coarse dofs), pymoto/solvers/iterative.py:178-220.
 
-    Fine node (2I+a, 2J+b, 2K+c) receives weight prod(1 if offset 0 else 1/2) from coarse node (I,J,K).
+    Fine node (2I+a, 2J+b, 2K+c) receives weight prod(1 if offset 0 else 1/2) from coarse node (I,J,K), for each
+    of the ndof dofs of the node (default the grid's dimension).
     """
     cg = grid.coarse()
-    nd = grid.dim
+    nd = grid.dim if ndof is None else ndof
     rows, cols, vals = [], [], []
     offs_k = [-1, 0, 1] if grid.dim == 3 else [0]
     for a in (-1, 0, 1):
@@ -344,7 +346,7 @@ def prolongation(grid):
                     cols.append(nc * nd + d)
                     vals.append(np.full(nf.size, w))
     R = sps.coo_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
-                       shape=(grid.ndof, cg.ndof)).tocsr()
+                       shape=(grid.nnodes * nd, cg.nnodes * nd)).tocsr()
     return R
 
 

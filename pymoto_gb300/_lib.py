@@ -104,6 +104,14 @@ SIGNATURES = {
     "pmg_nn_adam": (I, [I, P, P, P, P, P, F, F, F, F, I, F, P]),
     "pmg_nn_mse": (I, [L, P, P, D, P, P, P]),
     "pmg_nn_inject": (I, [I, I, I, I, P, D, P, P]),
+    "pmg_scalar_stencil": (I, [I, I, I, I, P, P, P, D, P, P, P]),
+    "pmg_scalar_apply": (I, [I, I, I, I, I, P, P, P, P, D, P, P]),
+    "pmg_scalar_restrict": (I, [I, I, I, I, P, P, P]),
+    "pmg_scalar_prolong_add": (I, [I, I, I, I, P, P, P]),
+    "pmg_scalar_galerkin": (I, [I, I, I, I, P, P, P]),
+    "pmg_scalar_to_dense": (I, [I, I, I, I, P, P, P]),
+    "pmg_scalar_rowabs": (I, [I, I, I, I, P, P, P]),
+    "pmg_scalar_sens": (I, [I, I, I, P, P, P, P, D, I, P, P]),
 }
 
 # Returns that are values, not statuses

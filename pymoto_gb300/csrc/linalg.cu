@@ -871,11 +871,15 @@ int pmg_scale(int dtype, int64_t n, void* y, const void* x, double a, void* stre
 
 int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int keep_bc, const void* x, void* y,
                 void* stream) {
-  if (nnodes < 0 || (dim != 2 && dim != 3) || !bcmask || !x || !y) return PMG_BAD_ARG;
+  if (nnodes < 0 || dim < 1 || dim > 3 || !bcmask || !x || !y) return PMG_BAD_ARG;
   cudaStream_t st = as_stream(stream);
   if (nnodes == 0) return PMG_OK;
   const unsigned g = blocks_for(nnodes, 256);
-  if (dtype == PMG_F64 && dim == 3)
+  if (dtype == PMG_F64 && dim == 1)
+    mask_bc_kernel<double, 1><<<g, 256, 0, st>>>(nnodes, bcmask, keep_bc, (const double*)x, (double*)y);
+  else if (dtype == PMG_F32 && dim == 1)
+    mask_bc_kernel<float, 1><<<g, 256, 0, st>>>(nnodes, bcmask, keep_bc, (const float*)x, (float*)y);
+  else if (dtype == PMG_F64 && dim == 3)
     mask_bc_kernel<double, 3><<<g, 256, 0, st>>>(nnodes, bcmask, keep_bc, (const double*)x, (double*)y);
   else if (dtype == PMG_F64)
     mask_bc_kernel<double, 2><<<g, 256, 0, st>>>(nnodes, bcmask, keep_bc, (const double*)x, (double*)y);
@@ -890,11 +894,21 @@ int pmg_mask_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, int k
 
 int pmg_split_bc(int dtype, int dim, int64_t nnodes, const uint8_t* bcmask, double bcdiag, const void* rhs,
                  void* direct, void* free_part, const void* cdiag, void* stream) {
-  if (nnodes < 0 || (dim != 2 && dim != 3) || !bcmask || !rhs || !direct || !free_part || !(bcdiag != 0.0))
+  if (nnodes < 0 || dim < 1 || dim > 3 || !bcmask || !rhs || !direct || !free_part || !(bcdiag != 0.0))
     return PMG_BAD_ARG;
   if (nnodes == 0) return PMG_OK;
   cudaStream_t st = as_stream(stream);
   const unsigned g = blocks_for(nnodes, 256);
+  if (dtype == PMG_F64 && dim == 1) {
+    split_bc_kernel<double, 1><<<g, 256, 0, st>>>(nnodes, bcmask, bcdiag, (const double*)rhs, (double*)direct,
+                                                 (double*)free_part, (const double*)cdiag);
+    return check_launch();
+  }
+  if (dtype == PMG_F32 && dim == 1) {
+    split_bc_kernel<float, 1><<<g, 256, 0, st>>>(nnodes, bcmask, (float)(bcdiag), (const float*)rhs,
+                                                (float*)direct, (float*)free_part, (const float*)cdiag);
+    return check_launch();
+  }
   if (dtype == PMG_F64 && dim == 3)
     split_bc_kernel<double, 3><<<g, 256, 0, st>>>(nnodes, bcmask, bcdiag, (const double*)rhs, (double*)direct,
                                                  (double*)free_part, (const double*)cdiag);

@@ -14,8 +14,8 @@ import torch
 from ._lib import F64, call, stream
 from .core import Module
 from .domain import grid_of
-from .operators import (Grid, StiffnessOperator, Workspace, bc_node_mask, element_mass, element_poisson,
-                        element_stiffness, embed_scalar_element)
+from .operators import (Grid, ScalarOperator, StiffnessOperator, Workspace, bc_node_mask, element_mass,
+                        element_poisson, element_stiffness)
 from .solvers import _from_device, _to_device, default_solver
 
 
@@ -691,15 +691,9 @@ class AssembleStiffness(Module):
         self._set_constant(add_constant, scalar=False)
 
     def _set_constant(self, add_constant, scalar):
-        """Host diagonal of add_constant over the operator's dofs; scalar operators (one entry per node, carried
-        as component 0) take it per node."""
+        """Host diagonal of add_constant over the operator's dofs (one per node for one-component operators)."""
         g = self.grid
-        c = _diagonal_constant(add_constant, g.nnodes if scalar else g.ndof)
-        if c is not None and scalar:
-            w = np.zeros(g.ndof)
-            w[0::g.dim] = c
-            c = w
-        self._cdiag_host = c
+        self._cdiag_host = _diagonal_constant(add_constant, g.nnodes if scalar else g.ndof)
         self._cdiag = None
 
     def cdiag(self, device):
@@ -741,85 +735,95 @@ class AssembleStiffness(Module):
         return _from_device(dx, self._kind)
 
 
-class AssembleMass(AssembleStiffness):
-    """M(x) = sum_e x_e M0 with the consistent element mass matrix (pymoto/modules/assembly.py:466-520), as the
-    same matrix-free device operator as the stiffness.  ndof = dim: the element matrix over dim dofs per node;
-    ndof = 1 (pyMOTO's default): the scalar matrix carried as component 0 of that operator with the other
-    components Dirichlet, as AssemblePoisson does (products and LinSolve take one entry per node).  Dirichlet
-    rows and columns hold bcdiagval (default 0, as in pyMOTO).  The sensitivity is the FP64 contraction
-    u_e^T M0 v_e (the mixed contraction relies on the element matrix annihilating translations, M0 does not)."""
+class _AssembleScalar(AssembleStiffness):
+    """Assembly of a one-component matrix (one dof per node) as a ScalarOperator: products, multigrid and solvers
+    on one value per node.  The element matrix is self.scalar_element; bc lists constrained nodes."""
 
-    def __init__(self, domain, bc=None, bcdiagval=0.0, matrix_type=None, add_constant=None, reuse_sparsity=True,
-                 material_property=1.0, ndof=1):
+    def _scalar_setup(self, domain, bc, bcdiagval, add_constant, element):
         self.domain = domain
         self.grid = Grid(*grid_of(domain))
-        g = self.grid
-        if ndof not in (1, g.dim):
-            raise NotImplementedError(f"AssembleMass on the device takes ndof=1 or ndof={g.dim} (got {ndof})")
-        self.ndof = ndof
-        self.sensitivity_precision = "fp64"
-        self.material_property = material_property
-        self.el_mat = element_mass(domain, ndof, material_property)
+        self.scalar_element = element
         self.bc = None if bc is None else np.asarray(bc, dtype=np.int64).ravel()
         self.bcdiagval = float(bcdiagval)
-        if ndof == g.dim:
-            self.stiffness_element = self.el_mat      # the operator's element matrix
-            self._mask_host = bc_node_mask(g.nnodes, g.dim, self.bc)
-        else:
-            self.stiffness_element = embed_scalar_element(self.el_mat, g.dim)
-            nodes = np.arange(g.nnodes)
-            extra = (nodes[:, None] * g.dim + np.arange(1, g.dim)).ravel()
-            scalar = np.zeros(0, dtype=np.int64) if self.bc is None else self.bc * g.dim
-            self._mask_host = bc_node_mask(g.nnodes, g.dim, np.concatenate([scalar, extra]))
-        self._mask = None
-        self._set_constant(add_constant, scalar=ndof == 1)
-
-    def __call__(self, x):
-        op = super().__call__(x)
-        if self.ndof == 1:
-            op.embedded_scalar = True
-        return op
-
-
-class AssemblePoisson(AssembleStiffness):
-    """P(x) = sum_e x_e P0 of one scalar per node (thermal conductivity, permittivity; pyMOTO's AssemblePoisson,
-    pymoto/modules/assembly.py:523-560).  On the device the scalar field is the first component of the
-    dim-component matrix-free operator: element matrix P0 on those dofs, the other components Dirichlet
-    everywhere (rows bcdiag I, solution 0), so the stiffness operator's kernels, multigrid and solvers run it
-    unchanged, at dim times the work of a one-component operator.  LinSolve widens the right-hand side and
-    narrows the solution: user vectors have one entry per node.  bc: constrained nodes (scalar dofs)."""
-
-    def __init__(self, domain, bc=None, bcdiagval=None, matrix_type=None, add_constant=None, reuse_sparsity=True,
-                 material_property=1.0, sensitivity_precision="fp64"):
-        if sensitivity_precision not in ("fp64", "mixed"):
-            raise ValueError("sensitivity_precision must be 'fp64' or 'mixed'")
-        self.sensitivity_precision = sensitivity_precision   # P0 annihilates constants, as the mixed form needs
-        self.domain = domain
-        self.grid = Grid(*grid_of(domain))
-        g = self.grid
-        self.material_property = material_property
-        self.poisson_element = element_poisson(domain, material_property)
-        self.stiffness_element = embed_scalar_element(self.poisson_element, g.dim)
-        self.bc = None if bc is None else np.asarray(bc, dtype=np.int64).ravel()
-        self.bcdiagval = float(np.max(self.poisson_element)) if bcdiagval is None else float(bcdiagval)
-        nodes = np.arange(g.nnodes)
-        extra = (nodes[:, None] * g.dim + np.arange(1, g.dim)).ravel()
-        scalar = np.zeros(0, dtype=np.int64) if self.bc is None else self.bc * g.dim
-        self._mask_host = bc_node_mask(g.nnodes, g.dim, np.concatenate([scalar, extra]))
+        self._mask_host = bc_node_mask(self.grid.nnodes, 1, self.bc)
         self._mask = None
         self._set_constant(add_constant, scalar=True)
 
     def __call__(self, x):
-        op = super().__call__(x)
-        op.embedded_scalar = True
-        return op
+        xd, kind = _to_device(x)
+        if xd.numel() != self.grid.nel:
+            raise ValueError(f"Input vector wrong size ({xd.numel()}), must be equal to #nel ({self.grid.nel})")
+        self._kind = kind
+        return ScalarOperator.assemble(self.grid, xd, self.scalar_element, self.bcmask(xd.device), self.bcdiagval,
+                                       cdiag=self.cdiag(xd.device))
+
+    def _sensitivity(self, dgdmat):
+        if dgdmat is None or getattr(dgdmat, "size", 1) <= 0:
+            return [None]
+        g = self.grid
+        device = self._mask.device
+        dx = torch.zeros(g.nel, dtype=torch.float64, device=device)
+        if not (isinstance(dgdmat, DeviceDyad) or (hasattr(dgdmat, "u") and hasattr(dgdmat, "v"))):
+            raise TypeError(f"unsupported sensitivity type {type(dgdmat).__name__} (a dyad is expected)")
+        for k, (u, v) in enumerate(zip(dgdmat.u, dgdmat.v)):
+            ud = _to_device(u, device=device)[0]
+            vd = _to_device(v, device=device)[0]
+            call("pmg_scalar_sens", g.nelx, g.nely, g.nelz, self.scalar_element, self._mask, ud, vd, 1.0, int(k > 0),
+                 dx, stream())
+        return _from_device(dx, self._kind)
 
 
-def _widen(v, dim):
-    """Scalar nodal vector -> dim-component vector with the scalar in component 0."""
-    w = torch.zeros(v.numel() * dim, dtype=v.dtype, device=v.device)
-    w[0::dim] = v
-    return w
+class AssembleMass(_AssembleScalar):
+    """M(x) = sum_e x_e M0 with the consistent element mass matrix (pymoto/modules/assembly.py:466-520).
+    ndof = 1 (pyMOTO's default): a one-component ScalarOperator (bc: constrained nodes).  ndof = dim: the
+    element matrix over dim dofs per node, as the matrix-free operator of the stiffness (bc: constrained dofs).
+    Dirichlet rows and columns hold bcdiagval (default 0, as in pyMOTO).  The sensitivity is the FP64
+    contraction u_e^T M0 v_e."""
+
+    def __init__(self, domain, bc=None, bcdiagval=0.0, matrix_type=None, add_constant=None, reuse_sparsity=True,
+                 material_property=1.0, ndof=1):
+        g = Grid(*grid_of(domain))
+        if ndof not in (1, g.dim):
+            raise NotImplementedError(f"AssembleMass on the device takes ndof=1 or ndof={g.dim} (got {ndof})")
+        self.ndof = ndof
+        self.sensitivity_precision = "fp64"     # the mixed contraction needs an element matrix that
+        self.material_property = material_property   # annihilates translations; M0 does not
+        self.el_mat = element_mass(domain, ndof, material_property)
+        if ndof == 1:
+            self._scalar_setup(domain, bc, bcdiagval, add_constant, self.el_mat)
+            return
+        self.domain = domain
+        self.grid = g
+        self.stiffness_element = self.el_mat      # the operator's element matrix
+        self.bc = None if bc is None else np.asarray(bc, dtype=np.int64).ravel()
+        self.bcdiagval = float(bcdiagval)
+        self._mask_host = bc_node_mask(g.nnodes, g.dim, self.bc)
+        self._mask = None
+        self._set_constant(add_constant, scalar=False)
+
+    def __call__(self, x):
+        if self.ndof == 1:
+            return super().__call__(x)
+        return AssembleStiffness.__call__(self, x)
+
+    def _sensitivity(self, dgdmat):
+        if self.ndof == 1:
+            return super()._sensitivity(dgdmat)
+        return AssembleStiffness._sensitivity(self, dgdmat)
+
+
+class AssemblePoisson(_AssembleScalar):
+    """P(x) = sum_e x_e P0 of one scalar per node (thermal conductivity, permittivity; pyMOTO's AssemblePoisson,
+    pymoto/modules/assembly.py:523-560), as a one-component ScalarOperator: node stencils of 27 (3D) or 9 (2D)
+    values, the same multigrid and solvers as the stiffness.  bc: constrained nodes; Dirichlet rows and columns
+    hold bcdiagval (default: the largest entry of P0, as pyMOTO)."""
+
+    def __init__(self, domain, bc=None, bcdiagval=None, matrix_type=None, add_constant=None, reuse_sparsity=True,
+                 material_property=1.0):
+        self.material_property = material_property
+        self.poisson_element = element_poisson(domain, material_property)
+        diag = float(np.max(self.poisson_element)) if bcdiagval is None else float(bcdiagval)
+        self._scalar_setup(domain, bc, diag, add_constant, self.poisson_element)
 
 
 # --------------------------------------------------------------------------------------------- LinSolve
@@ -859,13 +863,13 @@ class LinSolve(Module):
         """(direct part on Dirichlet dofs, rhs with those dofs zeroed)."""
         direct = torch.empty_like(rhs)
         rl = torch.empty_like(rhs)
-        call("pmg_split_bc", F64, A.grid.dim, A.grid.nnodes, A.bcmask, A.bcdiag, rhs, direct, rl,
+        call("pmg_split_bc", F64, getattr(A, "ncomp", A.grid.dim), A.grid.nnodes, A.bcmask, A.bcdiag, rhs, direct, rl,
              A.cdiag() if hasattr(A, "cdiag") else None, stream())
         return direct, rl
 
     def _mask(self, A, v):
         out = torch.empty_like(v)
-        call("pmg_mask_bc", F64, A.grid.dim, A.grid.nnodes, A.bcmask, 0, v, out, stream())
+        call("pmg_mask_bc", F64, getattr(A, "ncomp", A.grid.dim), A.grid.nnodes, A.bcmask, 0, v, out, stream())
         return out
 
     def _lda_solve(self, rhs, x0=None):
@@ -921,34 +925,26 @@ class LinSolve(Module):
         return sol
 
     def __call__(self, mat, rhs):
-        if not isinstance(mat, StiffnessOperator):
-            raise TypeError("LinSolve on the GPU path expects the StiffnessOperator of AssembleStiffness")
+        if not isinstance(mat, (StiffnessOperator, ScalarOperator)):
+            raise TypeError("LinSolve on the GPU path expects the operator of AssembleStiffness, AssemblePoisson "
+                            "or AssembleMass")
         fd, kind = _to_device(rhs, device=mat.device)
         self._kind = kind
-        self._dim_embed = mat.grid.dim if getattr(mat, "embedded_scalar", False) else 0
-        if self._dim_embed:
-            fd = _widen(fd, self._dim_embed)
         if self.solver is None:
             self.solver = default_solver(mat)
         self.solver.update(mat)
         # FP64 products of the LDA bookkeeping use the solver's (persistent, already assembled) operator
         sa = getattr(self.solver, "A64", None) or getattr(self.solver, "A", None)
-        self.A = sa if isinstance(sa, StiffnessOperator) and sa.code == F64 else mat.astype(F64)
+        self.A = sa if type(sa) is type(mat) and sa.code == F64 else mat.astype(F64)
         self._pairs = []
         x0 = None if self.u is None else _to_device(self.u, device=mat.device)[0]
-        if self._dim_embed and x0 is not None:
-            x0 = _widen(x0, self._dim_embed)
         u = self._lda_solve(fd, x0)
         self._u_dev = u
-        if self._dim_embed:
-            u = u[0::self._dim_embed].contiguous()
         self.u = _from_device(u, kind)
         return self.u
 
     def _sensitivity(self, dfdv):
         dd, kind = _to_device(dfdv, device=self._u_dev.device)
-        if self._dim_embed:
-            dd = _widen(dd, self._dim_embed)
         # an adjoint solve: a solver's learned warm start (trained on the responses to the design's load) stays
         # out of it
         active = getattr(self.solver, "warm_start_active", None)
@@ -960,8 +956,6 @@ class LinSolve(Module):
             if active is not None:
                 self.solver.warm_start_active = active
         dmat = DeviceDyad([-lam], [self._u_dev])
-        if self._dim_embed:
-            lam = lam[0::self._dim_embed].contiguous()
         return dmat, _from_device(lam, kind)
 
 

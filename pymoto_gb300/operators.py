@@ -141,15 +141,6 @@ def element_poisson(domain, material_property=1.0):
     return P
 
 
-def embed_scalar_element(P, dim):
-    """The element matrix of `dim` components per node whose first component carries the scalar matrix P and
-    the others nothing: P on the dofs node * dim."""
-    nn = P.shape[0]
-    K = np.zeros((nn * dim, nn * dim))
-    K[0::dim, 0::dim] = P
-    return K
-
-
 def bc_node_mask(nnodes, dim, bc):
     """One byte per node, bit d set for Dirichlet dof node*dim + d (host array)."""
     m = np.zeros(nnodes, dtype=np.uint8)
@@ -338,12 +329,6 @@ class StiffnessOperator:
         if isinstance(u, np.ndarray):
             ud = torch.from_numpy(np.ascontiguousarray(u, dtype=self.dtype)).to(self.device)
             return self.__matmul__(ud).cpu().numpy()
-        d = self.grid.dim
-        if getattr(self, "embedded_scalar", False) and u.numel() == self.grid.nnodes:
-            # a scalar operator carried as component 0: one entry per node in and out
-            w = torch.zeros(self.grid.ndof, dtype=u.dtype, device=u.device)
-            w[0::d] = u
-            return self.matvec(w)[0::d].contiguous()
         return self.matvec(u.contiguous())
 
     def _diagonal_into(self, d):
@@ -510,3 +495,177 @@ class StencilOperator:
 
     def __repr__(self):
         return f"StencilOperator({self.grid}, {self.dtype})"
+
+
+def scalar_stencil_offsets(dim):
+    """Stored node-stencil values per node of a one-component operator: all 27 (3D) or 9 (2D) neighbours."""
+    return 27 if dim == 3 else 9
+
+
+class ScalarOperator:
+    """One dof per node: pyMOTO's AssemblePoisson and AssembleMass(ndof=1) matrices
+    (pymoto/modules/assembly.py:466-560), and their Galerkin coarse operators.
+
+    The full node stencil S[o, n] (27 offsets in 3D, 9 in 2D, offset o = (dz+1)*9 + (dy+1)*3 + (dx+1)) in the
+    operator precision.  Level 0 assembles it from the element scaling: S = sum_e x_e P0 in FP64, Dirichlet nodes
+    (bit 0 of bcmask) with bcdiag on the diagonal only, and the constant diagonal of add_constant (cdiag, FP64
+    per node) added after them (assembly.py:245-296).  Coarse levels hold R^T S R (pymoto/solvers/iterative.py:
+    173), exact also for the constant diagonal.  Products read the 27 coefficients and neighbours of a node: one
+    FMA per coefficient, a ninth of the FMAs of the embedded form (the scalar as the first component of a
+    3-component operator)."""
+
+    ncomp = 1
+
+    def __init__(self, grid, S, code, bcmask=None, bcdiag=0.0, cdiag=None, xe=None, P0=None):
+        self.grid = grid
+        self.S = S
+        self.code = code
+        self.bcmask = bcmask
+        self.bcdiag = float(bcdiag)
+        self.cdiag64 = cdiag       # FP64 device vector per node (level 0), or None
+        self.xe = xe               # FP64 element scaling of a level-0 operator (None on coarse levels)
+        self.P0 = None if P0 is None else np.ascontiguousarray(P0, dtype=np.float64)
+        self._variants = {code: self}
+        self._cdiag = None
+        self.persistent = False
+
+    @classmethod
+    def assemble(cls, grid, xe, P0, bcmask, bcdiag, cdiag=None, code=F64):
+        """Level-0 operator of element scaling xe (FP64 device vector)."""
+        S = torch.empty((scalar_stencil_offsets(grid.dim), grid.nnodes), dtype=TORCH_DTYPE[code], device=xe.device)
+        op = cls(grid, S, code, bcmask, bcdiag, cdiag, xe, P0)
+        return op.recompute()
+
+    def recompute(self):
+        """Reassemble the level-0 stencil from the element scaling, in place."""
+        g = self.grid
+        call("pmg_scalar_stencil", self.code, g.nelx, g.nely, g.nelz, self.xe, self.P0, self.bcmask, self.bcdiag,
+             self.cdiag64, self.S, stream())
+        return self
+
+    @classmethod
+    def like(cls, other, code):
+        """An operator with its own stencil buffer (precision `code`) for the grid and BCs of `other`, refreshed in
+        place with assign() (stable device addresses for captured CUDA graphs)."""
+        S = torch.empty(other.S.shape, dtype=TORCH_DTYPE[code], device=other.device)
+        op = cls(other.grid, S, code, other.bcmask, other.bcdiag, other.cdiag64, other.xe, other.P0)
+        op.persistent = True
+        return op
+
+    def assign(self, other, derived=True):
+        """Copy the stencil of `other` (any precision) into this operator's buffer."""
+        if other is self:
+            return self
+        if other.grid.dims != self.grid.dims:
+            raise ValueError("assign: grid mismatch")
+        call("pmg_convert", other.code, self.code, other.S.numel(), other.S, self.S, 1.0, stream())
+        self.bcmask, self.bcdiag, self.xe, self.P0 = other.bcmask, other.bcdiag, other.xe, other.P0
+        if other.cdiag64 is not self.cdiag64:
+            self.cdiag64, self._cdiag = other.cdiag64, None
+        return self
+
+    def refresh_derived(self):
+        return self
+
+    def cdiag(self):
+        """The constant diagonal in the operator's precision (None without one)."""
+        if self.cdiag64 is None:
+            return None
+        if self._cdiag is None or self._cdiag.dtype != self.torch_dtype:
+            self._cdiag = self.cdiag64 if self.code == F64 else self.cdiag64.to(self.torch_dtype)
+        return self._cdiag
+
+    @property
+    def shape(self):
+        return (self.grid.nnodes, self.grid.nnodes)
+
+    @property
+    def ndim(self):
+        return 2
+
+    @property
+    def dtype(self):
+        return np.dtype(np.float64 if self.code == F64 else np.float32)
+
+    @property
+    def torch_dtype(self):
+        return TORCH_DTYPE[self.code]
+
+    @property
+    def device(self):
+        return self.S.device
+
+    @property
+    def T(self):
+        return self
+
+    def astype(self, code):
+        """The operator with its stencil in `code` precision (cached)."""
+        if code in self._variants:
+            return self._variants[code]
+        op = ScalarOperator.like(self, code).assign(self)
+        op.persistent = False
+        op._variants = self._variants
+        self._variants[code] = op
+        return op
+
+    def apply(self, mode, u, b=None, diag=None, w=0.0, out=None):
+        out = torch.empty_like(u) if out is None else out
+        g = self.grid
+        call("pmg_scalar_apply", mode, self.code, g.nelx, g.nely, g.nelz, self.S, u, b, diag, float(w), out, stream())
+        return out
+
+    def cheb_step(self, u, b, dl1, d, coef, step, out):
+        return None
+
+    def matvec(self, u, out=None):
+        return self.apply(MATVEC, u, out=out)
+
+    def __matmul__(self, u):
+        if isinstance(u, np.ndarray):
+            ud = torch.from_numpy(np.ascontiguousarray(u, dtype=self.dtype)).to(self.device)
+            return self.matvec(ud).cpu().numpy()
+        return self.matvec(u.contiguous())
+
+    def diagonal(self):
+        """The diagonal: the centre row of the stencil (a view, current after every reassembly)."""
+        return self.S[scalar_stencil_offsets(self.grid.dim) // 2]
+
+    def l1_diagonal(self, out):
+        """sum_j |A_ij| per row into out: the l1-Jacobi diagonal of the Chebyshev smoother."""
+        g = self.grid
+        call("pmg_scalar_rowabs", self.code, g.nelx, g.nely, g.nelz, self.S, out, stream())
+        return out
+
+    def restrict(self, rf, rc):
+        g = self.grid
+        call("pmg_scalar_restrict", self.code, g.nelx, g.nely, g.nelz, rf, rc, stream())
+
+    def prolong_add(self, uc, uf):
+        g = self.grid
+        call("pmg_scalar_prolong_add", self.code, g.nelx, g.nely, g.nelz, uc, uf, stream())
+
+    def galerkin(self, out=None):
+        """Coarse operator R^T A R (same precision); recomputed in place into `out`."""
+        g = self.grid
+        gc = g.coarse()
+        if out is None:
+            S = torch.empty((scalar_stencil_offsets(gc.dim), gc.nnodes), dtype=self.torch_dtype, device=self.device)
+            out = ScalarOperator(gc, S, self.code)
+            out.persistent = True
+        call("pmg_scalar_galerkin", self.code, g.nelx, g.nely, g.nelz, self.S, out.S, stream())
+        return out
+
+    def to_dense(self, out=None):
+        g = self.grid
+        A = torch.empty((g.nnodes, g.nnodes), dtype=torch.float64, device=self.device) if out is None else out
+        call("pmg_scalar_to_dense", self.code, g.nelx, g.nely, g.nelz, self.S, A, stream())
+        return A
+
+    def bandwidth(self):
+        """Half bandwidth in the natural node numbering (the farthest neighbour is at offset (1, 1, 1))."""
+        g = self.grid
+        return 1 + (g.nelx + 1) + ((g.nelx + 1) * (g.nely + 1) if g.dim == 3 else 0)
+
+    def __repr__(self):
+        return f"ScalarOperator({self.grid}, {self.dtype})"

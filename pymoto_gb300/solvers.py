@@ -21,7 +21,7 @@ import torch
 from . import _lib
 from ._lib import F32, F64, JACOBI, MATVEC, RESIDUAL, call, stream
 from .domain import grid_of
-from .operators import Grid, StencilOperator, StiffnessOperator, Workspace
+from .operators import Grid, ScalarOperator, StencilOperator, StiffnessOperator, Workspace
 
 PRECISIONS = {None: None, "fp64": F64, "float64": F64, "fp32": F32, "float32": F32}
 
@@ -132,13 +132,15 @@ class Chebyshev(Preconditioner):
         return np.diag(np.abs(K0).sum(axis=1))
 
     def update(self, A):
-        n = A.grid.ndof
+        n = A.shape[0]
         if self.D is None or self.D.numel() != n or self.D.dtype != A.torch_dtype or self.D.device != A.device:
             self.D = torch.empty(n, dtype=A.torch_dtype, device=A.device)
             self.coef = torch.zeros(2 * self.degree, dtype=torch.float64, device=A.device)
             call("pmg_cheb_coeffs", None, 1.0, self.ratio, self.degree, self.coef, stream())
         g = A.grid
-        if isinstance(A, StencilOperator):
+        if isinstance(A, ScalarOperator):
+            A.l1_diagonal(self.D)
+        elif isinstance(A, StencilOperator):
             call("pmg_stencil_rowabs", A.code, g.nelx, g.nely, g.nelz, A.S, self.D, stream())
         else:
             # the constant diagonal (add_constant, nonnegative springs) enters the l1 row sums as it is
@@ -201,7 +203,12 @@ class DenseCholesky(LinearSolver):
         g = A.grid
         if self.n > self.INVERSE_MAX_DOFS:
             return None, A.bandwidth()
-        key = (g.dims, A.device)
+        key = (g.dims, A.device, type(A))
+        if getattr(self, "_order_key", None) != key and isinstance(A, ScalarOperator):
+            # one dof per node: the natural numbering (its band is already that of the grid's fastest axes)
+            self._pos = torch.arange(self.n, dtype=torch.int32, device=A.device)
+            self._order_bw = A.bandwidth()
+            self._order_key = key
         if getattr(self, "_order_key", None) != key:
             pos = np.empty(self.n, dtype=np.int32)
             bw = np.zeros(1, dtype=np.int32)
@@ -212,9 +219,9 @@ class DenseCholesky(LinearSolver):
         return self._pos, self._order_bw
 
     def update(self, A):
-        if not isinstance(A, StencilOperator):
-            raise TypeError("DenseCholesky expects a coarse StencilOperator")
-        n = A.grid.ndof
+        if not isinstance(A, (StencilOperator, ScalarOperator)):
+            raise TypeError("DenseCholesky expects a coarse StencilOperator or ScalarOperator")
+        n = A.shape[0]
         if n > self.MAX_DOFS:
             raise ValueError(f"coarsest level has {n} dofs (> {self.MAX_DOFS}); add multigrid levels")
         self.n = n
@@ -245,7 +252,10 @@ class DenseCholesky(LinearSolver):
             self.ready_event.record()
         L = self.L
         g = A.grid
-        call("pmg_stencil_to_dense_perm", A.code, g.nelx, g.nely, g.nelz, A.S, pos, L, stream())
+        if isinstance(A, ScalarOperator):
+            A.to_dense(out=L)         # natural numbering: pos is the identity
+        else:
+            call("pmg_stencil_to_dense_perm", A.code, g.nelx, g.nely, g.nelz, A.S, pos, L, stream())
         call("pmg_cholesky_factor", n, L, self.bw, self._info, stream())
         # the pivot check is read back without blocking the host (check() raises once it has arrived), so
         # that the host can queue the next work while the factorisation runs
@@ -343,6 +353,25 @@ class DenseCholesky(LinearSolver):
         return out
 
 
+def _restrict(A, rf, rc):
+    """rc = R^T rf for the operator A of the fine level (per node for one-component operators, per dof
+    component otherwise)."""
+    if isinstance(A, ScalarOperator):
+        A.restrict(rf, rc)
+    else:
+        g = A.grid
+        call("pmg_restrict", A.code, g.nelx, g.nely, g.nelz, rf, rc, stream())
+
+
+def _prolong_add(A, uc, uf):
+    """uf += R uc for the operator A of the fine level."""
+    if isinstance(A, ScalarOperator):
+        A.prolong_add(uc, uf)
+    else:
+        g = A.grid
+        call("pmg_prolong_add", A.code, g.nelx, g.nely, g.nelz, uc, uf, stream())
+
+
 class GeometricMultigrid(Preconditioner):
     """Geometric multigrid preconditioner (pymoto/solvers/iterative.py:124-256).
 
@@ -381,12 +410,13 @@ class GeometricMultigrid(Preconditioner):
         """Refresh the level for a new operator.  Device buffers (level-0 copy of the operator, Galerkin
         operators, diagonals, coarsest factor) are reused in place, so a captured V-cycle stays valid."""
         code = self.precision if self.precision is not None else A.code
-        if isinstance(A, StiffnessOperator):
+        if isinstance(A, (StiffnessOperator, ScalarOperator)):
             if A.persistent and A.code == code:
                 op = A
             else:
-                if getattr(self, "_A0", None) is None or self._A0.code != code or self._A0.grid.dims != A.grid.dims:
-                    self._A0 = StiffnessOperator.like(A, code)
+                a0 = getattr(self, "_A0", None)
+                if a0 is None or type(a0) is not type(A) or a0.code != code or a0.grid.dims != A.grid.dims:
+                    self._A0 = type(A).like(A, code)
                     self._graph = None
                 op = self._A0.assign(A)
         else:
@@ -413,10 +443,11 @@ class GeometricMultigrid(Preconditioner):
         if isinstance(self.inner_level, GeometricMultigrid) and self.inner_level.precision is None:
             self.inner_level.precision = code
         self.inner_level.update(Ac)
-        n = self.grid.ndof
-        if self._buf is None or self._buf[0].dtype != op.torch_dtype or self._buf[0].device != op.device:
+        n = op.shape[0]
+        if self._buf is None or self._buf[0].dtype != op.torch_dtype or self._buf[0].device != op.device or \
+                self._buf[0].numel() != n:
             self._buf = [torch.empty(n, dtype=op.torch_dtype, device=op.device) for _ in range(3)]
-            self._rc = torch.empty(self.grid.coarse().ndof, dtype=op.torch_dtype, device=op.device)
+            self._rc = torch.empty(Ac.shape[0], dtype=op.torch_dtype, device=op.device)
 
     @property
     def code(self):
@@ -471,9 +502,9 @@ class GeometricMultigrid(Preconditioner):
         g = self.grid
         inner = self.inner_level
         rc = self._rc
-        call("pmg_restrict", A.code, g.nelx, g.nely, g.nelz, r, rc, stream())
+        _restrict(A, r, rc)
         uc = inner._vcycle(rc) if isinstance(inner, GeometricMultigrid) else inner.solve(rc)
-        call("pmg_prolong_add", A.code, g.nelx, g.nely, g.nelz, uc, u, stream())
+        _prolong_add(A, uc, u)
         for _ in range(steps):
             if fused:
                 A.apply(JACOBI, u, b, D, w, out=t)
@@ -498,9 +529,9 @@ class GeometricMultigrid(Preconditioner):
         g = self.grid
         inner = self.inner_level
         rc = self._rc
-        call("pmg_restrict", A.code, g.nelx, g.nely, g.nelz, other, rc, stream())
+        _restrict(A, other, rc)
         uc = inner._vcycle(rc) if isinstance(inner, GeometricMultigrid) else inner.solve(rc)
-        call("pmg_prolong_add", A.code, g.nelx, g.nely, g.nelz, uc, u, stream())
+        _prolong_add(A, uc, u)
         return sm.smooth(A, b, u, d, other, zero_start=False)
 
     @classmethod
@@ -771,8 +802,10 @@ class MixedPrecisionCG(LinearSolver):
         super().__init__(A)
 
     def update(self, A):
-        if getattr(self, "_A64", None) is None or self._A64.grid.dims != A.grid.dims:
-            self._A64 = StiffnessOperator.like(A, F64)
+        if self.warm_start is not None and isinstance(A, ScalarOperator):
+            raise NotImplementedError("the learned warm start predicts displacement fields (3 components per node)")
+        if getattr(self, "_A64", None) is None or type(self._A64) is not type(A) or self._A64.grid.dims != A.grid.dims:
+            self._A64 = type(A).like(A, F64)
         # the FP32 hierarchy is built from the element scaling of A alone: on a side stream, overlapping the
         # FP64 stencil assembly of the outer operator on the main stream
         main, side = torch.cuda.current_stream(), _side_stream(self)
@@ -783,7 +816,7 @@ class MixedPrecisionCG(LinearSolver):
             if self.preconditioner is not None:
                 self.preconditioner.update(A)
                 lv0 = getattr(self.preconditioner, "A", None)
-                self.A32 = lv0 if isinstance(lv0, StiffnessOperator) and lv0.code == F32 else A.astype(F32)
+                self.A32 = lv0 if type(lv0) is type(A) and lv0.code == F32 else A.astype(F32)
             else:
                 self.A32 = A.astype(F32)
         # joined just before the first preconditioner application of the next solve, so the FP64 work that
@@ -796,7 +829,7 @@ class MixedPrecisionCG(LinearSolver):
         self._side_pending = ev if ev is not None else side
         self._lagged_coarse = lv if ev is not None else None
         self._fallback_ready = False
-        n, dev = self.A64.grid.ndof, self.A64.device
+        n, dev = self.A64.shape[0], self.A64.device
         if getattr(self, "_r32", None) is None or self._r32.numel() != n or self._r32.device != dev:
             f32 = dict(dtype=torch.float32, device=dev)
             self._r32 = torch.empty(n, **f32)
@@ -1001,13 +1034,13 @@ class MixedPrecisionCG(LinearSolver):
                 B["wsq"] = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(k)]
             vecs = [] if x0 is None else [_to_device(x0, torch.float64)[0].contiguous()]
             for v, buf in zip(extra, B["wsv"]):
-                call("pmg_mask_bc", F64, A.grid.dim, A.grid.nnodes, A.bcmask, 0, v, buf, st)
+                call("pmg_mask_bc", F64, getattr(A, "ncomp", A.grid.dim), A.grid.nnodes, A.bcmask, 0, v, buf, st)
                 vecs.append(buf)
             # Gram products on the FP32 level-0 operator of the hierarchy once the set-up stream has it
             pc = self.preconditioner
             ev = getattr(pc, "level0_ready", None)
             a32 = getattr(self, "A32", None)
-            if ev is not None and a32 is not None and a32 is getattr(pc, "A", None) and a32.grid.ndof == n:
+            if ev is not None and a32 is not None and a32 is getattr(pc, "A", None) and a32.shape[0] == n:
                 torch.cuda.current_stream().wait_event(ev)
                 self.warm_start_coefficients = rayleigh_ritz(A, b, vecs, x, r, B["wsq"], A32=a32,
                                                              work32=(self._r32, self._z32))

@@ -30,21 +30,20 @@ def test_oracle_assembly_of_the_mass_matrix(golden):
     np.testing.assert_allclose(M @ g["asm_u"], g["asm_Mu"], rtol=1e-13, atol=1e-15)
 
 
-def test_scalar_mass_is_carried_as_component_zero():
-    """ndof=1: the embedded element matrix assembles to the scalar mass matrix plus decoupled Dirichlet rows."""
+def test_one_component_oracle_assembles_the_scalar_mass_matrix():
+    """ndof=1: the oracle's one-component assembly is the element loop over the node connectivity."""
     d = pg.VoxelDomain(3, 2, 2, 0.5, 1.0, 2.0)
     m = pg.AssembleMass(d, material_property=3.0)
     grid = O.Grid(3, 2, 2)
     rng = np.random.default_rng(1)
     x = rng.uniform(0.1, 1.0, grid.nel)
-    bc_dofs = np.array([n * 3 + c for n in range(grid.nnodes) for c in range(3) if (m._mask_host[n] >> c) & 1])
-    A = O.assemble(grid, m.stiffness_element, x, bc=bc_dofs, bcdiagval=0.0).tocsr()
+    A = O.assemble(grid, m.el_mat, x, ndof=1).toarray()
     Ms = np.zeros((grid.nnodes, grid.nnodes))
-    conn = grid.dofconn()[:, 0::3] // 3            # element nodes in the local order
+    conn = grid.conn()                             # element nodes in the local order
     for e in range(grid.nel):
         Ms[np.ix_(conn[e], conn[e])] += x[e] * m.el_mat
-    np.testing.assert_allclose(A[0::3, 0::3].toarray(), Ms, rtol=1e-14, atol=1e-16)
-    assert abs(A[1::3, :]).max() == 0 and abs(A[:, 2::3]).max() == 0
+    np.testing.assert_allclose(A, Ms, rtol=1e-14, atol=1e-16)
+    assert not m._mask_host.any()
     with pytest.raises(NotImplementedError):
         pg.AssembleMass(pg.VoxelDomain(4, 3, 2), ndof=2)
 
@@ -68,7 +67,7 @@ def test_scalar_mass_product_on_device():
     m = pg.AssembleMass(d, material_property=3.0)
     M = m(torch.from_numpy(x).cuda())
     Ms = np.zeros((grid.nnodes, grid.nnodes))
-    conn = grid.dofconn()[:, 0::3] // 3
+    conn = grid.conn()
     for e in range(grid.nel):
         Ms[np.ix_(conn[e], conn[e])] += x[e] * m.el_mat
     y = M @ torch.from_numpy(u).cuda()

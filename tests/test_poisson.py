@@ -1,5 +1,5 @@
-"""AssemblePoisson: the scalar element matrix, and the embedding of the scalar problem as the first component of
-the vector operator, against pyMOTO's AssemblePoisson and a thermal compliance network."""
+"""AssemblePoisson: the scalar element matrix and the one-component assembly, against pyMOTO's AssemblePoisson and a
+thermal compliance network."""
 import numpy as np
 import pytest
 import scipy.sparse.linalg as spla
@@ -18,33 +18,28 @@ def test_element_matrix_matches_pymoto(tag, shp, size, k, golden):
     np.testing.assert_allclose(P0.sum(axis=1), 0.0, atol=1e-13)     # constants are in the null space
 
 
-def _embedded(golden):
+def _scalar_system(golden):
     g = golden("poisson.npz")
     d = pg.VoxelDomain(6, 4, 4, 1.0, 0.5, 0.8)
     m = pg.AssemblePoisson(d, bc=g["net_bc"], material_property=2.0)
     grid = O.Grid(6, 4, 4)
-    bc_dofs = np.array([n * 3 + c for n in range(grid.nnodes) for c in range(3) if (m._mask_host[n] >> c) & 1])
-    A = O.assemble(grid, m.stiffness_element, g["net_x"], bc=bc_dofs, bcdiagval=m.bcdiagval).tocsr()
-    return g, m, grid, bc_dofs, A
+    A = O.assemble(grid, m.poisson_element, g["net_x"], bc=g["net_bc"], bcdiagval=m.bcdiagval, ndof=1).tocsr()
+    return g, m, grid, A
 
 
-def test_embedded_operator_is_pymotos_matrix_plus_decoupled_identity(golden):
-    g, m, grid, bc_dofs, A = _embedded(golden)
-    np.testing.assert_allclose(A[0::3, 0::3] @ g["net_urand"], g["net_Pu"], rtol=1e-13, atol=1e-15)
-    for c in (1, 2):
-        np.testing.assert_allclose(A[c::3, c::3].toarray(), m.bcdiagval * np.eye(grid.nnodes))
-        assert abs(A[0::3, c::3]).max() == 0 and abs(A[c::3, 0::3]).max() == 0
+def test_one_component_oracle_is_pymotos_matrix(golden):
+    g, m, grid, A = _scalar_system(golden)
+    assert A.shape == (grid.nnodes, grid.nnodes)
+    np.testing.assert_allclose(A @ g["net_urand"], g["net_Pu"], rtol=1e-13, atol=1e-15)
+    assert m._mask_host.max() <= 1 and np.flatnonzero(m._mask_host).tolist() == sorted(set(g["net_bc"].tolist()))
 
 
-def test_embedded_solve_and_sensitivity_reproduce_the_thermal_network(golden):
-    g, m, grid, bc_dofs, A = _embedded(golden)
-    f = np.zeros(grid.ndof)
-    f[0::3] = g["net_f"]   # the Dirichlet rows are bcdiag I: their solution is load / bcdiag, as in pyMOTO
-    u = spla.spsolve(A.tocsc(), f)
-    np.testing.assert_allclose(u[0::3], g["net_u"], rtol=1e-10, atol=1e-14)
-    np.testing.assert_allclose(u[1::3], 0.0, atol=0)
-    assert float(u[0::3] @ g["net_f"]) == pytest.approx(float(g["net_c"]), rel=1e-10)
-    dx = O.sensitivity_contract(grid, m.stiffness_element, [-u], [u], bc=bc_dofs)
+def test_one_component_solve_and_sensitivity_reproduce_the_thermal_network(golden):
+    g, m, grid, A = _scalar_system(golden)
+    u = spla.spsolve(A.tocsc(), g["net_f"])   # Dirichlet rows are bcdiag I: their solution is load / bcdiag
+    np.testing.assert_allclose(u, g["net_u"], rtol=1e-10, atol=1e-14)
+    assert float(u @ g["net_f"]) == pytest.approx(float(g["net_c"]), rel=1e-10)
+    dx = O.sensitivity_contract(grid, m.poisson_element, [-u], [u], bc=g["net_bc"], ndof=1)
     np.testing.assert_allclose(dx, g["net_dx"], rtol=1e-9, atol=1e-14)
 
 
