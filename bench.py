@@ -62,10 +62,11 @@ def parse():
     ap.add_argument("--levels", type=int, default=GPU_LEVELS)
     ap.add_argument("--sweeps", type=int, default=SWEEPS)
     ap.add_argument("--coarse-sweeps", type=int, default=None)
-    ap.add_argument("--case", default=None, choices=["operator", "mma", "mma_run"],
+    ap.add_argument("--case", default=None, choices=["operator", "mma", "mma_run", "poisson"],
                     help="instead of the bench: time the level-0 operator kernels alone (a small case for ncu), "
-                         "the device MMA update of the 96x48x48 design against the numpy MMA, or the 96x48x48 "
-                         "MMA workload (mma_run)")
+                         "the device MMA update of the 96x48x48 design against the numpy MMA, the 96x48x48 "
+                         "MMA workload (mma_run), or thermal design evaluations on the one-component operator "
+                         "(poisson)")
     ap.add_argument("--mma-iters", type=int, default=100, help="MMA iterations of --case mma_run")
     ap.add_argument("--pretrain", type=int, default=256,
                     help="smoothed-noise fields the learned warm start sees before --case mma_run")
@@ -559,6 +560,143 @@ def operator_case(args):
     print(json.dumps({"case": "operator", "shape": list(shape), **out}))
 
 
+def heat_sink(shape):
+    """Thermal load case: the middle half of the x = 0 face held at zero temperature, a uniform heat load."""
+    nx, ny, nz = shape
+    jj = np.arange(ny // 4, 3 * ny // 4 + 1)
+    kk = np.arange(nz // 4, 3 * nz // 4 + 1)
+    J, K = np.meshgrid(jj, kk, indexing="ij")
+    nodes = ((K * (ny + 1) + J) * (nx + 1)).ravel()
+    nn = (nx + 1) * (ny + 1) * (nz + 1)
+    return nodes, np.full(nn, 1.0 / nn)
+
+
+def poisson_case(args):
+    """Thermal compliance evaluations on the one-component operator (AssemblePoisson, pymoto/modules/assembly.py:
+    523-560): per step, P(x) assembled from a new design, LinSolve with CG and a 5-level FP64 multigrid (pyMOTO's
+    method: damped Jacobi w = 0.6, 2 sweeps) to 1e-8, c = f.u and dc/dx.  Also: the one-component kernels timed
+    alone (CUDA events, L2 flushed before each launch) against the measured HBM bandwidth, parity of the solve with
+    the oracle on the last evaluation's design, whose run on the host cores is the CPU baseline."""
+    import torch
+    import pymoto_gb300 as pg
+    import oracle as O
+    from pymoto_gb300._lib import F32, F64, MATVEC, RESIDUAL
+    from pymoto_gb300.operators import ScalarOperator, element_poisson
+    shape = SHAPE if args.shape is None else tuple(int(v) for v in args.shape.split("x"))
+    peaks = {}
+    pth = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pth):
+        with open(pth) as fh:
+            peaks = json.load(fh)
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tol = 1e-8
+
+    def network(shp, x0):
+        d = pg.VoxelDomain(*shp)
+        nodes, f = heat_sink(shp)
+        mgs = pg.GeometricMultigrid.hierarchy(d, levels=GPU_LEVELS, smoother_w=OMEGA,
+                                              smooth_steps=SWEEPS)
+        solver = pg.CG(preconditioner=mgs[0], tol=tol, maxit=500)
+        fd = torch.from_numpy(f).cuda()
+        sx = pg.Signal("x", torch.from_numpy(x0).cuda())
+        with pg.Network() as fn:
+            sK = pg.AssemblePoisson(d, bc=nodes)(sx)
+            su = pg.LinSolve(hermitian=True, symmetric=True, solver=solver)(sK, fd)
+            sc = pg.EinSum("i,i->")(su, fd)
+        return fn, sx, sK, su, sc, solver
+
+    rng = np.random.default_rng(0)
+    nel = shape[0] * shape[1] * shape[2]
+    x0 = rng.uniform(1e-3, 1.0, nel)
+    fn, sx, sK, su, sc, solver = network(shape, x0)
+
+    def step(k):
+        sx.state = torch.from_numpy(np.clip(x0 * (1.0 + 0.02 * k), 1e-3, 1.0)).cuda()
+        fn.response()
+        fn.reset()
+        sc.sensitivity = 1.0
+        fn.sensitivity()
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    its = []
+    with ClockSampler(0) as clk:
+        e0.record()
+        for k in range(args.steps):
+            step(args.warmup + k)
+            its.append(solver.iterations)
+        e1.record()
+        torch.cuda.synchronize()
+    per = e0.elapsed_time(e1) / 1e3 / args.steps
+
+    # kernels alone
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    K = sK.state
+    K32 = K.astype(F32)
+    nn = K.grid.nnodes
+
+    def timed(fn_, reps=20):
+        for _ in range(3):
+            fn_()
+        ts = []
+        for _ in range(reps):
+            flush.fill_(1)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn_()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        return statistics.median(ts)
+
+    u64 = torch.randn(nn, dtype=torch.float64, device="cuda")
+    u32, b32 = u64.float(), torch.randn(nn, dtype=torch.float32, device="cuda")
+    y64, y32 = torch.empty_like(u64), torch.empty_like(u32)
+    Kc = K.galerkin()
+    kern = {}
+    for name, fn_, nbytes in [
+            ("scalar_apply_f64_matvec", lambda: K.apply(MATVEC, u64, out=y64), (27 + 2) * 8 * nn),
+            ("scalar_apply_f32_residual", lambda: K32.apply(RESIDUAL, u32, b32, out=y32), (27 + 3) * 4 * nn),
+            ("scalar_galerkin_f64", lambda: K.galerkin(out=Kc), 27 * 8 * (nn + Kc.grid.nnodes)),
+            ("scalar_stencil_f64", lambda: K.recompute(), 27 * 8 * nn + 8 * nel + nn)]:
+        t = timed(fn_)
+        kern[name] = {"us": t * 1e6, "algorithmic_bytes": nbytes, "gbs": nbytes / t / 1e9,
+                      "frac_of_measured_hbm": nbytes / t / 1e9 / hbm}
+
+    # parity of the last timed evaluation with the oracle (same design, same grid), whose run is the CPU baseline
+    x_last = np.clip(x0 * (1.0 + 0.02 * (args.warmup + args.steps - 1)), 1e-3, 1.0)
+    u_gpu, dx_gpu, c_gpu = su.state.cpu().numpy(), sx.sensitivity.cpu().numpy(), float(sc.state)
+    del flush, Kc, K32
+    og = O.Grid(*shape)
+    nodes, f = heat_sink(shape)
+    P0 = element_poisson(pg.VoxelDomain(*shape), 1.0)
+    t0 = time.perf_counter()
+    A = O.assemble(og, P0, x_last, bc=nodes, bcdiagval=float(P0.max()), ndof=1).tocsr()
+    lv = O.build_hierarchy(og, A, REF_LEVELS, w=OMEGA, smooth_steps=SWEEPS, ndof=1)
+    u_ref, cpu_its, _ = O.cg_solve(A, f, precond=lambda r: O.vcycle(lv[0], r), tol=tol)
+    dx_ref = O.sensitivity_contract(og, P0, [-u_ref], [u_ref], bc=nodes, ndof=1)
+    t_cpu = time.perf_counter() - t0
+    line = {"case": "poisson", "metric": "thermal design evaluations/s (assembly + CG/GMG solve to 1e-8 + c + dc/dx)",
+            "value": 1.0 / per, "unit": "evaluations/s", "ms_per_step": per * 1e3, "steps": args.steps,
+            "warmup": args.warmup, "dtype": "f64", "data": "synthetic (seeded U(1e-3,1) conductivities)",
+            "config": {"workload": f"heat sink, one-component hex8 {shape[0]}x{shape[1]}x{shape[2]} "
+                                   f"({nn} dofs), CG + FP64 GMG {GPU_LEVELS} levels, w={OMEGA}, {SWEEPS} sweeps",
+                       "l2": "kernels: L2 flushed before each launch"},
+            "cg_iterations": its, "kernels": kern, "clocks": clk.summary(),
+            "parity": {"u_max_rel_diff": float(np.abs(u_gpu - u_ref).max() / np.abs(u_ref).max()),
+                       "dx_max_rel_diff": float(np.abs(dx_gpu - dx_ref).max() / np.abs(dx_ref).max()),
+                       "compliance_rel_diff": float(abs(c_gpu - f @ u_ref) / abs(f @ u_ref)),
+                       "oracle_relative_residual_of_gpu_u": float(O.relative_residual(A, u_gpu, f))},
+            "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "evaluations/s", "cores": os.cpu_count() or 1,
+                             "kind": "port", "sample": f"the last timed evaluation's design through the oracle "
+                                                       f"(scipy assembly, SpGEMM Galerkin, {REF_LEVELS}-level GMG, "
+                                                       f"SuperLU coarsest, CG {cpu_its} iterations, sensitivity) "
+                                                       f"on the same grid: {t_cpu:.2f} s"}}
+    print(json.dumps(line))
+
+
 def mma_case(args):
     """The MMA update of a 96x48x48 design (221,184 variables, one volume constraint) on the device, fast and exact
     variants: 2 warm-up and 5 timed updates chained on their own output (CUDA events around each), then the numpy
@@ -702,6 +840,9 @@ def main():
         return
     if args.case == "mma_run":
         mma_run_case(args)
+        return
+    if args.case == "poisson":
+        poisson_case(args)
         return
     rank, world, local_rank = dist_info()
     threads = os.cpu_count() or 1

@@ -354,22 +354,23 @@ class MGLevel:
     """One geometric-multigrid level (pymoto/solvers/iterative.py:124-256) with a damped-Jacobi smoother
     (iterative.py:21-47).  ``inner`` is the next MGLevel or None for the direct coarsest solve."""
 
-    def __init__(self, grid, A, w=0.5, smooth_steps=5):
+    def __init__(self, grid, A, w=0.5, smooth_steps=5, ndof=None):
         self.grid, self.A, self.w, self.smooth_steps = grid, A, w, smooth_steps
         self.D = A.diagonal()
-        self.R = prolongation(grid)
+        self.R = prolongation(grid, ndof)
         self.Ac = (self.R.T @ A @ self.R).tocsr()
         self.inner = None
         self.lu = None
 
 
-def build_hierarchy(grid, A, levels, w=0.5, smooth_steps=5):
+def build_hierarchy(grid, A, levels, w=0.5, smooth_steps=5, ndof=None):
     """Chain of GeometricMultigrid levels; the last Galerkin operator gets a direct LU factorisation
-    (SuperLU, pymoto/solvers/sparse.py:515-555, chosen by auto_determine.py:109-122)."""
+    (SuperLU, pymoto/solvers/sparse.py:515-555, chosen by auto_determine.py:109-122).  ndof: dofs per node
+    (default the grid's dimension)."""
     lvls = []
     g, M = grid, A
     for _ in range(levels - 1):
-        lv = MGLevel(g, M, w, smooth_steps)
+        lv = MGLevel(g, M, w, smooth_steps, ndof)
         if lvls:
             lvls[-1].inner = lv
         lvls.append(lv)

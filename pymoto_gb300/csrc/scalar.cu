@@ -131,10 +131,18 @@ __global__ void scalar_prolong_add_kernel(Grid gf, const T* __restrict__ uc, T* 
   uf[n] += acc;
 }
 
-// Sc = R^T Sf R: per coarse node N, the fine nodes n = 2N + a of its prolongation column (weight wn), each of
-// their stencil entries (n, m), and the coarse nodes M whose column holds m (weight wm): Sc(N, M) += wn Sf(n, m) wm
+// Coarse offsets q (per axis, from -1 to 1) whose prolongation column holds the fine offset e = a + d (-2 .. 2)
+// from 2N: e / 2 with weight 1 for even e, (e - 1) / 2 and (e + 1) / 2 with weight 1/2 each for odd e.
+__host__ __device__ constexpr int sc_lo(int e) { return (e & 1) ? (e - 1) / 2 : e / 2; }
+__host__ __device__ constexpr int sc_cnt(int e) { return (e & 1) ? 2 : 1; }
+__host__ __device__ constexpr double sc_wt(int e) { return (e & 1) ? 0.5 : 1.0; }
+
+// Sc = R^T Sf R: per coarse node N, the fine nodes n = 2N + a of its prolongation column (weight w(a)), each of
+// their stencil entries (n, n + d), and the coarse nodes N + q whose column holds n + d: Sc(N, q) += w(a) Sf(n, d)
+// w'(a + d, q).  Both loops are unrolled, so every accumulator index is a compile-time constant (the 27 sums stay
+// in registers).  FP64 operators accumulate in FP64, FP32 operators in FP32 (their hierarchy is a preconditioner).
 template <typename T, int DIM>
-__global__ void scalar_galerkin_kernel(Grid gf, const T* __restrict__ Sf, T* __restrict__ Sc) {
+__global__ void __launch_bounds__(128) scalar_galerkin_kernel(Grid gf, const T* __restrict__ Sf, T* __restrict__ Sc) {
   constexpr int NOFF = SC<DIM>::NOFF;
   const Grid gc = gf.coarse();
   const int64_t nnf = gf.nnodes(), nnc = gc.nnodes();
@@ -142,58 +150,39 @@ __global__ void scalar_galerkin_kernel(Grid gf, const T* __restrict__ Sf, T* __r
   if (N >= nnc) return;
   int I, J, K;
   node_ijk(gc, N, I, J, K);
-  double acc[NOFF];
+  T acc[NOFF];
 #pragma unroll
-  for (int q = 0; q < NOFF; ++q) acc[q] = 0.0;
-  for (int c = (DIM == 3 ? -1 : 0); c <= (DIM == 3 ? 1 : 0); ++c)
-    for (int bb = -1; bb <= 1; ++bb)
-      for (int a = -1; a <= 1; ++a) {
-        const int i = 2 * I + a, j = 2 * J + bb, k = 2 * K + c;
-        if (i < 0 || i > gf.nx || j < 0 || j > gf.ny || k < 0 || k > gf.nz) continue;
-        const double wn = sc_tw(a) * sc_tw(bb) * sc_tw(c);
-        const int64_t n = node_id(gf, i, j, k);
-        for (int o = 0; o < NOFF; ++o) {
-          const double s = (double)Sf[(int64_t)o * nnf + n];
-          if (s == 0.0) continue;
-          int dx, dy, dz;
-          stencil_offset<DIM>(o, dx, dy, dz);
-          const int m[3] = {i + dx, j + dy, k + dz};
-          // per axis the coarse nodes whose prolongation column holds m: m / 2 (weight 1) for even m,
-          // (m - 1) / 2 and (m + 1) / 2 (weight 1/2 each) for odd m; offsets from N in -1 .. 1
-          int lo[3], cnt[3];
-          double wt[3];
-          const int nd = DIM == 3 ? 3 : 2;
-          const int base[3] = {I, J, K};
-          for (int ax = 0; ax < 3; ++ax) {
-            if (ax >= nd) {
-              lo[ax] = 0;
-              cnt[ax] = 1;
-              wt[ax] = 1.0;
-              continue;
-            }
-            const int mm = m[ax];
-            if (mm & 1) {
-              lo[ax] = (mm - 1) / 2 - base[ax];
-              cnt[ax] = 2;
-              wt[ax] = 0.5;
-            } else {
-              lo[ax] = mm / 2 - base[ax];
-              cnt[ax] = 1;
-              wt[ax] = 1.0;
-            }
+  for (int q = 0; q < NOFF; ++q) acc[q] = T(0);
+#pragma unroll
+  for (int ia = 0; ia < NOFF; ++ia) {
+    int ax, ay, az;
+    stencil_offset<DIM>(ia, ax, ay, az);
+    const int i = 2 * I + ax, j = 2 * J + ay, k = 2 * K + az;
+    const bool in = i >= 0 && i <= gf.nx && j >= 0 && j <= gf.ny && k >= 0 && k <= gf.nz;
+    const int64_t n = in ? node_id(gf, i, j, k) : 0;
+    const T wn = (T)(sc_tw(ax) * sc_tw(ay) * sc_tw(az));
+#pragma unroll
+    for (int o = 0; o < NOFF; ++o) {
+      int dx, dy, dz;
+      stencil_offset<DIM>(o, dx, dy, dz);
+      // coefficients towards fine nodes outside the grid are zero, so only n itself needs the bounds test
+      const T s = in ? wn * Sf[(int64_t)o * nnf + n] : T(0);
+      const int ex = ax + dx, ey = ay + dy, ez = az + dz;
+#pragma unroll
+      for (int qz = 0; qz < sc_cnt(ez); ++qz)
+#pragma unroll
+        for (int qy = 0; qy < sc_cnt(ey); ++qy)
+#pragma unroll
+          for (int qx = 0; qx < sc_cnt(ex); ++qx) {
+            const int Ox = sc_lo(ex) + qx, Oy = sc_lo(ey) + qy, Oz = sc_lo(ez) + qz;
+            const int q = DIM == 3 ? (Oz + 1) * 9 + (Oy + 1) * 3 + (Ox + 1) : (Oy + 1) * 3 + (Ox + 1);
+            acc[q] = fma((T)(sc_wt(ex) * sc_wt(ey) * sc_wt(ez)), s, acc[q]);
           }
-          for (int qz = 0; qz < cnt[2]; ++qz)
-            for (int qy = 0; qy < cnt[1]; ++qy)
-              for (int qx = 0; qx < cnt[0]; ++qx) {
-                const int Ox = lo[0] + qx, Oy = lo[1] + qy, Oz = lo[2] + qz;
-                const int q = DIM == 3 ? (Oz + 1) * 9 + (Oy + 1) * 3 + (Ox + 1) : (Oy + 1) * 3 + (Ox + 1);
-                acc[q] += wn * s * (wt[0] * wt[1] * wt[2]);
-              }
-        }
-      }
+    }
+  }
   // coefficients towards coarse nodes outside the grid are zero by construction (no fine node there)
 #pragma unroll
-  for (int q = 0; q < NOFF; ++q) Sc[(int64_t)q * nnc + N] = (T)acc[q];
+  for (int q = 0; q < NOFF; ++q) Sc[(int64_t)q * nnc + N] = acc[q];
 }
 
 // A (n x n FP64, zero-filled before) gets the stencil entries

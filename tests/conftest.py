@@ -34,7 +34,8 @@ def clamp_face_dofs(grid):
 # auxiliary subsystems after them, then the parity at the benchmark sizes (the slowest file: its oracle solves
 # a 1.6M-dof system on the host), so that with -x a failure in a later file does not hide the earlier results;
 # test_zz_no_alloc stays last.
-_LATER = ("test_filter_variants", "test_mass", "test_poisson", "test_overhang", "test_math_expression",
+_LATER = ("test_filter_variants", "test_mass", "test_poisson", "test_scalar_operator", "test_overhang",
+          "test_math_expression",
           "test_scalars", "test_einsum", "test_routines", "test_design_runs", "test_checkpoint", "test_faults",
           "test_config_parity", "test_zz_no_alloc")
 

@@ -205,3 +205,22 @@ def test_scalar_operator_properties_at_128x64x64():
     Ac = op.galerkin()
     onec = torch.ones(g.coarse().nnodes, dtype=torch.float64, device="cuda")
     assert float(Ac.matvec(onec).abs().max()) < 1e-11 * float(Ac.diagonal().abs().max())
+
+
+@pytest.mark.gpu
+def test_poisson_with_a_constant_diagonal_solves_the_shifted_system():
+    """add_constant (a diagonal, e.g. convection to ambient) is added after the Dirichlet rows, as pyMOTO adds its
+    constant matrix to the assembled one (assembly.py:294-295)."""
+    og, x, nodes, f = _thermal_case((8, 6, 4))
+    d = pg.VoxelDomain(8, 6, 4)
+    P0 = element_poisson(d, 1.0)
+    c = np.random.default_rng(9).uniform(0.0, 0.5, og.nnodes)
+    A = (O.assemble(og, P0, x, bc=nodes, bcdiagval=float(P0.max()), ndof=1) + sps.diags(c)).tocsc()
+    ref = spla.spsolve(A, f)
+    sx = pg.Signal("x", torch.from_numpy(x).cuda())
+    fd = torch.from_numpy(f).cuda()
+    with pg.Network() as fn:
+        sK = pg.AssemblePoisson(d, bc=nodes, add_constant=sps.diags(c))(sx)
+        su = pg.LinSolve(hermitian=True, symmetric=True)(sK, fd)
+    np.testing.assert_allclose(su.state.cpu().numpy(), ref, rtol=0, atol=1e-9 * np.abs(ref).max())
+    np.testing.assert_allclose(sK.state.to_dense().cpu().numpy(), A.toarray(), rtol=0, atol=1e-13 * abs(A).max())
