@@ -512,8 +512,9 @@ def cpu_reference_sample(shape, warm_steps=1, warmup=1, seed=1234):
 
 def operator_case(args):
     """Operator products of the workload alone: the FP32 level-0 operator in residual mode (CUDA-core and
-    tensor-core implementations), FP64 stencil product, FP32 level-1 stencil residual; 3 launches each after 2
-    warm-up launches, CUDA-event times printed as JSON (a small case for ncu)."""
+    tensor-core implementations), FP64 stencil product, FP32 level-1 stencil residual, and the one-component
+    (Poisson) operator's FP64 product, FP32 residual and FP64 Galerkin product on the same grid; 3 launches each
+    after 2 warm-up launches, CUDA-event times printed as JSON (a small case for ncu)."""
     import torch
     import pymoto_gb300 as pg
     from pymoto_gb300._lib import F32, RESIDUAL, MATVEC
@@ -528,6 +529,15 @@ def operator_case(args):
     A1 = K32.galerkin()            # level 1 (FP32 Galerkin stencils, half-symmetric)
     u1 = torch.randn(A1.grid.ndof, device="cuda")
     b1 = torch.randn_like(u1)
+    # the one-component (Poisson) operator on the same grid and element scaling
+    from pymoto_gb300.operators import ScalarOperator, element_poisson
+    nn = K.grid.nnodes
+    P = ScalarOperator.assemble(K.grid, x, element_poisson(d, 1.0), torch.zeros(nn, dtype=torch.uint8, device="cuda"),
+                                1.0)
+    P32 = P.astype(F32)
+    Pc = P.galerkin()
+    v64, v32, c32 = torch.randn(nn, dtype=torch.float64, device="cuda"), torch.randn(nn, device="cuda"), \
+        torch.randn(nn, device="cuda")
     out = {}
 
     def with_kernel(kind, fn):
@@ -540,7 +550,10 @@ def operator_case(args):
     for name, fn in [("ebe_apply_fma_f32_residual", with_kernel("fma", lambda: K32.apply(RESIDUAL, u32, b32))),
                      ("ebe_apply_tc_f32_residual", with_kernel("tcgen05", lambda: K32.apply(RESIDUAL, u32, b32))),
                      ("stencil_apply_f64_matvec", lambda: K.apply(MATVEC, u)),
-                     ("stencil_apply_f32_level1_residual", lambda: A1.apply(RESIDUAL, u1, b1))]:
+                     ("stencil_apply_f32_level1_residual", lambda: A1.apply(RESIDUAL, u1, b1)),
+                     ("scalar_apply_f64_matvec", lambda: P.apply(MATVEC, v64)),
+                     ("scalar_apply_f32_residual", lambda: P32.apply(RESIDUAL, v32, c32)),
+                     ("scalar_galerkin_f64", lambda: P.galerkin(out=Pc))]:
         for _ in range(2):
             fn()
         torch.cuda.synchronize()
