@@ -310,15 +310,38 @@ __global__ void __launch_bounds__(FT, 2)
 
 }  // namespace
 
-// Tile of node columns for the grid: OX <= 32 covering the x node count in equal parts, then OY <= 32 with
-// OX OY <= 256 covering the y node count in equal parts.
-static void fma_tile(const Grid& g, int& OX, int& OY, int& tx, int& ty) {
-  const int nnx = g.nx + 1, nny = g.ny + 1;
-  tx = (nnx + 31) / 32;
-  OX = (nnx + tx - 1) / tx;
-  const int oymax = min(32, FT / OX);
-  ty = (nny + oymax - 1) / oymax;
-  OY = (nny + ty - 1) / ty;
+// Tile of node columns and z chunks for the grid.  Every tile width OX <= 32 that splits the x node count into
+// equal parts is a candidate, with the tallest OY that fits the thread and staging limits (again split into equal
+// parts); per candidate, the number of z chunks that minimises waves of CTAs x (layers per chunk + 1, the element
+// layer a chunk shares with the next).  The cheapest plan wins; ties go to fewer CTAs, then to wider tiles.  At
+// 128 x 64 x 64 this picks 19 x 13 columns in 8 chunks (10 layer steps per CTA) over 26 x 9 in 7 chunks (11).
+static void fma_plan(const Grid& g, int slots, int& OX, int& OY, int& tx, int& ty, int& nzc) {
+  const int nnx = g.nx + 1, nny = g.ny + 1, nnz = g.nz + 1;
+  int64_t best = -1, best_ctas = 0;
+  int best_ox = 0;
+  for (int ox = 1; ox <= 32; ++ox) {
+    const int cx = (nnx + ox - 1) / ox;
+    if ((nnx + cx - 1) / cx != ox) continue;          // each equal-part width is visited once
+    int oymax = std::min(32, FT / ox);
+    while (oymax > 1 && ((ox + 2) * (oymax + 2) > FPLANE_MAX || (ox + 1) * (oymax + 1) > FEPLANE_MAX)) --oymax;
+    const int cy = (nny + oymax - 1) / oymax;
+    const int oy = (nny + cy - 1) / cy;
+    if (cy > 65535) continue;                           // grid.y limit
+    for (int c = 1; c <= nnz && c <= 65535; ++c) {      // grid.z limit
+      const int64_t ctas = (int64_t)cx * cy * c;
+      const int64_t cost = (ctas + slots - 1) / slots * ((nnz + c - 1) / c + 1);
+      if (best < 0 || cost < best || (cost == best && (ctas < best_ctas || (ctas == best_ctas && ox > best_ox)))) {
+        best = cost;
+        best_ctas = ctas;
+        best_ox = ox;
+        OX = ox;
+        OY = oy;
+        tx = cx;
+        ty = cy;
+        nzc = c;
+      }
+    }
+  }
 }
 
 // Class values of a cube-element K0 (true when every entry is sign x value of its class to 1e-12).
@@ -378,20 +401,8 @@ int ebe_apply_fma_f32(int mode, Grid g, const float* xe, const double* K0, const
     }
     resident[dev][key] = r > 0 ? r : 1;
   }
-  int OX, OY, tx, ty;
-  fma_tile(g, OX, OY, tx, ty);
-  // z chunks: fewest waves of CTAs times the layers of a chunk (plus the one shared element layer)
-  const int nnz = g.nz + 1, slots = resident[dev][key] * sm_count();
-  int nzc = 1;
-  int64_t best = -1;
-  for (int c = 1; c <= nnz; ++c) {
-    const int64_t waves = ((int64_t)tx * ty * c + slots - 1) / slots;
-    const int64_t cost = waves * ((nnz + c - 1) / c + 1);
-    if (best < 0 || cost < best) {
-      best = cost;
-      nzc = c;
-    }
-  }
+  int OX = 1, OY = 1, tx = 1, ty = 1, nzc = 1;
+  fma_plan(g, resident[dev][key] * sm_count(), OX, OY, tx, ty, nzc);
   const dim3 grid(tx, ty, nzc);
   auto K = make_elem_mat<float, 24>(K0);
   const float bd = (float)bcdiag, wf = (float)w;
