@@ -14,6 +14,7 @@ at module level for plotting only.  The fixtures are small .npz files; the tests
     python tests/golden/make_golden.py math     # the MathExpression cases only
     python tests/golden/make_golden.py overhang # the OverhangFilter cases only
     python tests/golden/make_golden.py poisson  # the AssemblePoisson cases only
+    python tests/golden/make_golden.py poisson_mg  # multigrid on one-component (AssemblePoisson) matrices only
     python tests/golden/make_golden.py einsum   # the EinSum expressions only
     python tests/golden/make_golden.py springs  # AssembleStiffness add_constant (springs to ground) only
 """
@@ -461,6 +462,34 @@ def poisson(pym):
     save("poisson.npz", **out)
 
 
+def poisson_multigrid(pym):
+    """GeometricMultigrid on one-component (AssemblePoisson) matrices, 3D and 2D: pyMOTO sizes the interpolation
+    by the dofs per node of the matrix (one here).  Two levels with damped Jacobi (w = 0.6, 2 sweeps) over the
+    automatically chosen direct coarsest solve: R, R^T P R and one V-cycle of a random residual."""
+    out = {}
+    for tag, shp in [("s3", (8, 4, 4)), ("s2", (8, 8))]:
+        d = pym.VoxelDomain(*shp)
+        rng = np.random.default_rng(19)
+        x = rng.uniform(1e-3, 1.0, d.nel)
+        bc = d.nodes[0, ...].flatten()
+        P = pym.AssemblePoisson(d, bc=bc)(x)
+        mg1 = pym.solvers.GeometricMultigrid(d, smoother=pym.solvers.DampedJacobi(w=0.6), smooth_steps=2)
+        mg2 = pym.solvers.GeometricMultigrid(mg1.sub_domain, smoother=pym.solvers.DampedJacobi(w=0.6), smooth_steps=2)
+        mg1.inner_level = mg2
+        mg1.update(P)
+        R = mg1.R.tocoo()
+        Ac = mg2.A.tocsr()
+        Ac.eliminate_zeros()
+        r = rng.standard_normal(P.shape[0])
+        r[bc] = 0.0
+        z = mg1.solve(r)
+        out.update({f"{tag}_shape": np.array(shp), f"{tag}_x": x, f"{tag}_bc": bc,
+                    f"{tag}_R_row": R.row, f"{tag}_R_col": R.col, f"{tag}_R_val": R.data,
+                    f"{tag}_Ac_data": Ac.data, f"{tag}_Ac_indices": Ac.indices, f"{tag}_Ac_indptr": Ac.indptr,
+                    f"{tag}_r": r, f"{tag}_z": z})
+    save("poisson_mg.npz", **out)
+
+
 def springs(pym):
     """Springs to ground through AssembleStiffness(add_constant=...) (pymoto/modules/assembly.py:294-295, the
     compliant-mechanism example's use): 2D (mechanism-like supports, springs at an input and an output dof) and
@@ -604,5 +633,7 @@ if __name__ == "__main__":
         overhang(pym)
     if "all" in which or "poisson" in which:
         poisson(pym)
+    if "all" in which or "poisson_mg" in which:
+        poisson_multigrid(pym)
     if "all" in which or "einsum" in which:
         einsums(pym)

@@ -2,6 +2,7 @@
 thermal compliance network."""
 import numpy as np
 import pytest
+import scipy.sparse as sps
 import scipy.sparse.linalg as spla
 import torch
 
@@ -59,3 +60,31 @@ def test_thermal_compliance_network_on_device(golden):
     sc.sensitivity = 1.0
     fn.sensitivity()
     np.testing.assert_allclose(sx.sensitivity.cpu().numpy(), g["net_dx"], rtol=1e-7, atol=1e-12)
+
+
+def _golden_mg(golden, tag):
+    g = golden("poisson_mg.npz")
+    shp = tuple(int(v) for v in g[f"{tag}_shape"])
+    og = O.Grid(*shp) if len(shp) == 3 else O.Grid(*shp, 0)
+    nn = og.nnodes
+    R = sps.coo_matrix((g[f"{tag}_R_val"], (g[f"{tag}_R_row"], g[f"{tag}_R_col"])),
+                       shape=(nn, og.coarse().nnodes)).tocsr()
+    nc = og.coarse().nnodes
+    Ac = sps.csr_matrix((g[f"{tag}_Ac_data"], g[f"{tag}_Ac_indices"], g[f"{tag}_Ac_indptr"]), shape=(nc, nc))
+    return g, shp, og, R, Ac
+
+
+@pytest.mark.parametrize("tag", ["s3", "s2"])
+def test_one_component_multigrid_oracle_matches_pymoto(tag, golden):
+    """pyMOTO's GeometricMultigrid on AssemblePoisson matrices (one dof per node): the oracle's prolongation,
+    Galerkin operator and V-cycle (iterative.py:124-256) reproduce it."""
+    g, shp, og, R, Ac = _golden_mg(golden, tag)
+    P0 = element_poisson(pg.VoxelDomain(*shp), 1.0)
+    A = O.assemble(og, P0, g[f"{tag}_x"], bc=g[f"{tag}_bc"], bcdiagval=float(P0.max()), ndof=1).tocsr()
+    Ro = O.prolongation(og, ndof=1)
+    assert abs(Ro - R).max() == 0
+    Aco = (Ro.T @ A @ Ro).tocsr()
+    np.testing.assert_allclose(Aco.toarray(), Ac.toarray(), rtol=0, atol=1e-13 * abs(Ac).max())
+    lv = O.build_hierarchy(og, A, 3, w=0.6, smooth_steps=2, ndof=1)
+    z = O.vcycle(lv[0], g[f"{tag}_r"])
+    np.testing.assert_allclose(z, g[f"{tag}_z"], rtol=0, atol=1e-11 * np.abs(g[f"{tag}_z"]).max())

@@ -224,3 +224,23 @@ def test_poisson_with_a_constant_diagonal_solves_the_shifted_system():
         su = pg.LinSolve(hermitian=True, symmetric=True)(sK, fd)
     np.testing.assert_allclose(su.state.cpu().numpy(), ref, rtol=0, atol=1e-9 * np.abs(ref).max())
     np.testing.assert_allclose(sK.state.to_dense().cpu().numpy(), A.toarray(), rtol=0, atol=1e-13 * abs(A).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", ["s3", "s2"])
+def test_galerkin_and_vcycle_match_pymotos_multigrid(tag, golden):
+    """The device hierarchy of an AssemblePoisson operator against pyMOTO's GeometricMultigrid on the same matrix
+    (two levels, damped Jacobi w = 0.6, 2 sweeps, direct coarsest solve): R^T P R and one V-cycle."""
+    g = golden("poisson_mg.npz")
+    shp = tuple(int(v) for v in g[f"{tag}_shape"])
+    d = pg.VoxelDomain(*shp)
+    og = O.Grid(*shp) if len(shp) == 3 else O.Grid(*shp, 0)
+    nc = og.coarse().nnodes
+    Ac = sps.csr_matrix((g[f"{tag}_Ac_data"], g[f"{tag}_Ac_indices"], g[f"{tag}_Ac_indptr"]), shape=(nc, nc))
+    P = pg.AssemblePoisson(d, bc=g[f"{tag}_bc"])(torch.from_numpy(g[f"{tag}_x"]).cuda())
+    np.testing.assert_allclose(P.galerkin().to_dense().cpu().numpy(), Ac.toarray(), rtol=0,
+                               atol=1e-13 * abs(Ac).max())
+    mgs = pg.GeometricMultigrid.hierarchy(d, levels=3, smoother_w=0.6, smooth_steps=2)
+    mgs[0].update(P)
+    z = mgs[0].solve(torch.from_numpy(g[f"{tag}_r"]).cuda()).cpu().numpy()
+    np.testing.assert_allclose(z, g[f"{tag}_z"], rtol=0, atol=1e-11 * np.abs(g[f"{tag}_z"]).max())
