@@ -411,7 +411,7 @@ int pmg_scalar_apply(int mode, int dtype, int nelx, int nely, int nelz, const vo
 int pmg_scalar_restrict(int dtype, int nelx, int nely, int nelz, const void* rf, void* rc, void* stream);
 int pmg_scalar_prolong_add(int dtype, int nelx, int nely, int nelz, const void* uc, void* uf, void* stream);
 /* Galerkin coarse operator Sc = R^T Sf R (pymoto/solvers/iterative.py:173), stencil to stencil, FP64
- * accumulation; the grid is the fine one. */
+ * accumulation for FP64 operators, FP32 for FP32 ones; the grid is the fine one. */
 int pmg_scalar_galerkin(int dtype, int nelx, int nely, int nelz, const void* Sf, void* Sc, void* stream);
 /* Dense FP64 matrix (nnodes x nnodes, row-major, nnodes <= 65536) of a one-component operator. */
 int pmg_scalar_to_dense(int dtype, int nelx, int nely, int nelz, const void* S, double* A, void* stream);
