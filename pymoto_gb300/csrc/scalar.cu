@@ -139,11 +139,14 @@ __host__ __device__ constexpr double sc_wt(int e) { return (e & 1) ? 0.5 : 1.0; 
 
 // Sc = R^T Sf R: per coarse node N, the fine nodes n = 2N + a of its prolongation column (weight w(a)), each of
 // their stencil entries (n, n + d), and the coarse nodes N + q whose column holds n + d: Sc(N, q) += w(a) Sf(n, d)
-// w'(a + d, q).  Both loops are unrolled, so every accumulator index is a compile-time constant (the 27 sums stay
-// in registers).  FP64 operators accumulate in FP64, FP32 operators in FP32 (their hierarchy is a preconditioner).
+// w'(a + d, q).  Both loops are unrolled, so every accumulator index is a compile-time constant (the sums stay in
+// registers).  R^T S R is symmetric, so only the centre and the forward offsets q >= CENTER are summed here (half
+// the FMAs, and no load of an entry that reaches only backward offsets); scalar_mirror_kernel copies the backward
+// ones from the neighbours.  FP64 operators accumulate in FP64, FP32 operators in FP32 (their hierarchy is a
+// preconditioner).
 template <typename T, int DIM>
 __global__ void __launch_bounds__(128) scalar_galerkin_kernel(Grid gf, const T* __restrict__ Sf, T* __restrict__ Sc) {
-  constexpr int NOFF = SC<DIM>::NOFF;
+  constexpr int NOFF = SC<DIM>::NOFF, CENTER = SC<DIM>::CENTER;
   const Grid gc = gf.coarse();
   const int64_t nnf = gf.nnodes(), nnc = gc.nnodes();
   const int64_t N = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -165,9 +168,13 @@ __global__ void __launch_bounds__(128) scalar_galerkin_kernel(Grid gf, const T* 
     for (int o = 0; o < NOFF; ++o) {
       int dx, dy, dz;
       stencil_offset<DIM>(o, dx, dy, dz);
+      const int ex = ax + dx, ey = ay + dy, ez = az + dz;
+      // the largest target offset of this entry; an entry that reaches only backward offsets is not loaded
+      const int qmax = DIM == 3 ? (sc_lo(ez) + sc_cnt(ez)) * 9 + (sc_lo(ey) + sc_cnt(ey)) * 3 + (sc_lo(ex) + sc_cnt(ex))
+                                : (sc_lo(ey) + sc_cnt(ey)) * 3 + (sc_lo(ex) + sc_cnt(ex));
+      if (qmax < CENTER) continue;
       // coefficients towards fine nodes outside the grid are zero, so only n itself needs the bounds test
       const T s = in ? wn * Sf[(int64_t)o * nnf + n] : T(0);
-      const int ex = ax + dx, ey = ay + dy, ez = az + dz;
 #pragma unroll
       for (int qz = 0; qz < sc_cnt(ez); ++qz)
 #pragma unroll
@@ -176,13 +183,33 @@ __global__ void __launch_bounds__(128) scalar_galerkin_kernel(Grid gf, const T* 
           for (int qx = 0; qx < sc_cnt(ex); ++qx) {
             const int Ox = sc_lo(ex) + qx, Oy = sc_lo(ey) + qy, Oz = sc_lo(ez) + qz;
             const int q = DIM == 3 ? (Oz + 1) * 9 + (Oy + 1) * 3 + (Ox + 1) : (Oy + 1) * 3 + (Ox + 1);
-            acc[q] = fma((T)(sc_wt(ex) * sc_wt(ey) * sc_wt(ez)), s, acc[q]);
+            if (q >= CENTER) acc[q] = fma((T)(sc_wt(ex) * sc_wt(ey) * sc_wt(ez)), s, acc[q]);
           }
     }
   }
   // coefficients towards coarse nodes outside the grid are zero by construction (no fine node there)
 #pragma unroll
-  for (int q = 0; q < NOFF; ++q) Sc[(int64_t)q * nnc + N] = acc[q];
+  for (int q = CENTER; q < NOFF; ++q) Sc[(int64_t)q * nnc + N] = acc[q];
+}
+
+// Backward offsets of a symmetric stencil from its forward ones: S(N, q) = S(N + off(q), NOFF - 1 - q) for
+// q < CENTER, zero towards nodes outside the grid.
+template <typename T, int DIM>
+__global__ void scalar_mirror_kernel(Grid g, T* __restrict__ S) {
+  constexpr int NOFF = SC<DIM>::NOFF, CENTER = SC<DIM>::CENTER;
+  const int64_t nn = g.nnodes();
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nn) return;
+  int i, j, k;
+  node_ijk(g, n, i, j, k);
+#pragma unroll
+  for (int q = 0; q < CENTER; ++q) {
+    int dx, dy, dz;
+    stencil_offset<DIM>(q, dx, dy, dz);
+    const int mi = i + dx, mj = j + dy, mk = k + dz;
+    const bool in = mi >= 0 && mi <= g.nx && mj >= 0 && mj <= g.ny && mk >= 0 && mk <= g.nz;
+    S[(int64_t)q * nn + n] = in ? S[(int64_t)(NOFF - 1 - q) * nn + node_id(g, mi, mj, mk)] : T(0);
+  }
 }
 
 // A (n x n FP64, zero-filled before) gets the stencil entries
@@ -349,6 +376,7 @@ int pmg_scalar_galerkin(int dtype, int nelx, int nely, int nelz, const void* Sf,
   return scalar_dispatch(dtype, nelz, [&](auto t_, auto dim_) {
     PMG_SCALAR_TYPES;
     scalar_galerkin_kernel<T, DIM><<<blocks, 128, 0, st>>>(g, (const T*)Sf, (T*)Sc);
+    scalar_mirror_kernel<T, DIM><<<blocks_for(g.coarse().nnodes(), 256), 256, 0, st>>>(g.coarse(), (T*)Sc);
   });
 }
 
