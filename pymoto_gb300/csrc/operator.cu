@@ -11,6 +11,8 @@
 #include <algorithm>
 #include <atomic>
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace pmg {
@@ -267,10 +269,10 @@ __device__ __forceinline__ T stencil_coef(const T* __restrict__ S, int nn, int o
   return (o >= Traits<DIM>::CENTER || in) ? v : T(0);
 }
 
-// One thread per (component d, node n), d slowest so that the stencil loads of a warp are coalesced.  The
-// bound of 4 CTAs per SM caps the registers at 64: enough to keep most of a row's 162 loads in flight (without
-// it the compiler settles at 32 registers and the level-1 product waits on each load: 10.2 vs 8.8 us at
-// 64x32x32; with 2 CTAs per SM the FP64 level-0 product loses occupancy: 265 vs 225 us).
+// One thread per (component d, node n), d slowest so that the stencil loads of a warp are coalesced: the FP64
+// products.  The bound of 4 CTAs per SM caps the registers at 64: enough to keep most of a row's 162 loads in
+// flight (without it the compiler settles at 32 registers and each load is waited for; with 2 CTAs per SM the
+// FP64 level-0 product loses occupancy: 265 vs 225 us).
 template <typename T, int DIM, int MODE>
 __global__ void __launch_bounds__(256, 4) stencil_apply_kernel(Grid g, const T* __restrict__ S, const T* __restrict__ u,
                                                             const T* __restrict__ b, const T* __restrict__ diag, T w,
@@ -311,6 +313,62 @@ __global__ void __launch_bounds__(256, 4) stencil_apply_kernel(Grid g, const T* 
     const T dn = (ch.step == 0 ? T(0) : a * ch.d[q]) + c * ((b[q] - acc) / diag[q]);
     ch.d[q] = dn;
     y[q] = u[q] + dn;
+  }
+}
+
+// One thread per node: the DIM rows of the node together, so that each neighbour's DIM values are loaded once
+// (a third of the value loads and of the index arithmetic of one thread per row).  Every row is summed in the
+// same order as by stencil_apply_kernel (offsets, then components): the results are identical.
+template <typename T, int DIM, int MODE>
+__global__ void __launch_bounds__(256, 3) stencil_apply_node_kernel(Grid g, const T* __restrict__ S,
+                                                                 const T* __restrict__ u, const T* __restrict__ b,
+                                                                 const T* __restrict__ diag, T w, T* __restrict__ y,
+                                                                 ChebArgs<T> ch) {
+  constexpr int NOFF = Traits<DIM>::NOFF;
+  const int nn = (int)g.nnodes();
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nn) return;
+  int i, j, k;
+  node_ijk(g, n, i, j, k);
+  T acc[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) acc[d] = T(0);
+#pragma unroll
+  for (int o = 0; o < NOFF; ++o) {
+    int dx, dy, dz;
+    stencil_offset<DIM>(o, dx, dy, dz);
+    const bool in = i + dx >= 0 && i + dx <= g.nx && j + dy >= 0 && j + dy <= g.ny && k + dz >= 0 && k + dz <= g.nz;
+    const int ii = min(max(i + dx, 0), g.nx), jj = min(max(j + dy, 0), g.ny), kk = min(max(k + dz, 0), g.nz);
+    const int m = (kk * (g.ny + 1) + jj) * (g.nx + 1) + ii;
+    const bool live = o >= Traits<DIM>::CENTER || in;
+    T um[DIM];
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) um[c] = u[(int64_t)m * DIM + c];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const StencilRow<T> row = stencil_row<T, DIM>(S, nn, o, d, n, m);
+#pragma unroll
+      for (int c = 0; c < DIM; ++c) {
+        const T a = row.p[(int64_t)c * row.stride];
+        acc[d] = fma(live ? a : T(0), um[c], acc[d]);
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    const int64_t q = (int64_t)n * DIM + d;
+    if (MODE == 0) {
+      y[q] = acc[d];
+    } else if (MODE == 1) {
+      y[q] = b[q] - acc[d];
+    } else if (MODE == 2) {
+      y[q] = u[q] + w * ((b[q] - acc[d]) / diag[q]);
+    } else {
+      const T a = (T)ch.coef[2 * ch.step], c = (T)ch.coef[2 * ch.step + 1];
+      const T dn = (ch.step == 0 ? T(0) : a * ch.d[q]) + c * ((b[q] - acc[d]) / diag[q]);
+      ch.d[q] = dn;
+      y[q] = u[q] + dn;
+    }
   }
 }
 
@@ -1054,15 +1112,31 @@ int stencil_apply_t(int mode, Grid g, const void* S, const void* u, const void* 
   const T* d_ = (const T*)diag;
   T* y_ = (T*)y;
   if (rows <= SPLIT_MAX_ROWS) return split_apply<T, DIM, 1>(mode, g, rows, S_, u_, b_, d_, (T)w, y_, ch, st);
-  if (mode == PMG_APPLY_MATVEC)
-    stencil_apply_kernel<T, DIM, 0><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
-  else if (mode == PMG_APPLY_RESIDUAL)
-    stencil_apply_kernel<T, DIM, 1><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
-  else if (mode == PMG_APPLY_JACOBI)
-    stencil_apply_kernel<T, DIM, 2><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
-  else
-    stencil_apply_kernel<T, DIM, 3><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
-  return check_launch();
+  if constexpr (std::is_same<T, double>::value) {
+    // FP64 (the outer level-0 product): bound by the FP64 pipe, where a thread per row keeps more warps resident
+    // (232 us against 236 us with a thread per node at 128 x 64 x 64)
+    if (mode == PMG_APPLY_MATVEC)
+      stencil_apply_kernel<T, DIM, 0><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    else if (mode == PMG_APPLY_RESIDUAL)
+      stencil_apply_kernel<T, DIM, 1><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    else if (mode == PMG_APPLY_JACOBI)
+      stencil_apply_kernel<T, DIM, 2><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    else
+      stencil_apply_kernel<T, DIM, 3><<<blocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    return check_launch();
+  } else {
+    // FP32 (level 1 of the mixed hierarchy): a thread per node, 17.0 us against 21.1 us at 64 x 32 x 32
+    const unsigned nblocks = blocks_for(g.nnodes(), threads);
+    if (mode == PMG_APPLY_MATVEC)
+      stencil_apply_node_kernel<T, DIM, 0><<<nblocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    else if (mode == PMG_APPLY_RESIDUAL)
+      stencil_apply_node_kernel<T, DIM, 1><<<nblocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    else if (mode == PMG_APPLY_JACOBI)
+      stencil_apply_node_kernel<T, DIM, 2><<<nblocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    else
+      stencil_apply_node_kernel<T, DIM, 3><<<nblocks, threads, 0, st>>>(g, S_, u_, b_, d_, (T)w, y_, ch);
+    return check_launch();
+  }
 }
 
 #define PMG_DISPATCH(dtype, dim, CALL)                  \
