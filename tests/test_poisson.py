@@ -88,3 +88,24 @@ def test_one_component_multigrid_oracle_matches_pymoto(tag, golden):
     lv = O.build_hierarchy(og, A, 3, w=0.6, smooth_steps=2, ndof=1)
     z = O.vcycle(lv[0], g[f"{tag}_r"])
     np.testing.assert_allclose(z, g[f"{tag}_z"], rtol=0, atol=1e-11 * np.abs(g[f"{tag}_z"]).max())
+
+
+@pytest.mark.parametrize("shp", [(6, 4, 4), (5, 3, 2), (7, 5, 0)])
+def test_one_component_host_layout(shp):
+    """Host side of the one-component operator: the natural-numbering half bandwidth the coarsest direct solve
+    uses is that of the oracle's assembled matrix, and the Dirichlet mask marks bit 0 of the constrained nodes."""
+    from pymoto_gb300.operators import Grid, ScalarOperator, bc_node_mask, scalar_stencil_offsets
+    og = O.Grid(*shp)
+    rng = np.random.default_rng(3)
+    P0 = element_poisson(pg.VoxelDomain(*shp), 1.0)
+    A = O.assemble(og, P0, rng.uniform(0.1, 1.0, og.nel), ndof=1).tocoo()
+    g = Grid(*shp)
+    op = ScalarOperator(g, None, 0)
+    assert op.bandwidth() == int(np.abs(A.row - A.col).max())
+    assert op.shape == (og.nnodes, og.nnodes) and op.ncomp == 1
+    assert scalar_stencil_offsets(g.dim) == (27 if g.dim == 3 else 9)
+    nodes = np.array([0, 3, og.nnodes - 1])
+    m = bc_node_mask(og.nnodes, 1, nodes)
+    assert np.flatnonzero(m).tolist() == nodes.tolist() and m.max() == 1
+    with pytest.raises(IndexError):
+        bc_node_mask(og.nnodes, 1, [og.nnodes])
