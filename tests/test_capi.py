@@ -225,3 +225,27 @@ def test_mma_and_overhang_arguments_are_checked_before_any_launch():
         call("pmg_overhang_forward", *ok, buf[0], 40.0, 0.0, 0.5, 0.5, 1e-3, buf[1], buf[2], buf[3], None)
     with pytest.raises(PMGError):   # output aliases the input
         call("pmg_overhang_forward", *ok, buf[0], 40.0, 1.0, 0.5, 0.5, 1e-3, buf[1], buf[1], buf[3], None)
+
+
+def test_c_caller_without_python(tmp_path):
+    """The header compiles as C99 and a C program linked against the library gets the element matrix and the
+    argument checks from it (host-only calls: no GPU)."""
+    import shutil
+    import subprocess
+    from pymoto_gb300 import _lib, element_stiffness
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    _lib.load()
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    exe = str(tmp_path / "capi_host_check")
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "capi_host_check.c"), "-o", exe, "-L", libdir, "-lpymoto_gb300",
+                    "-Wl,-rpath," + libdir], check=True, capture_output=True, text=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.splitlines()
+    fields = dict(line.split(" ", 1) for line in out)
+    assert int(fields["version"]) == _lib.call("pmg_version")
+    assert fields["status"] == "invalid argument"
+    K0 = np.array([float(v) for v in fields["K0"].split()]).reshape(24, 24)
+    np.testing.assert_array_equal(K0, element_stiffness(3))
+    assert int(fields["bad_mode"]) == 1 and int(fields["bad_grid"]) == 1
