@@ -634,6 +634,49 @@ class DeviceDyad:
 
 
 # --------------------------------------------------------------------------------------------- assembly
+def _stencil_constant(add_constant, grid):
+    """add_constant of a one-component operator as (its diagonal, the node-stencil layout of its other entries or
+    None): host FP64 arrays of nnodes and (27 or 9, nnodes), entry (o, n) coupling node n with its neighbour at
+    offset o = (dz+1)*9 + (dy+1)*3 + (dx+1).  The full stencils of the one-component operators hold any constant
+    whose entries couple neighbouring nodes (convection terms on boundary faces, for instance); a constant coupling
+    nodes further apart, or a non-symmetric one, raises NotImplementedError."""
+    n = grid.nnodes
+    if add_constant is None:
+        return None, None
+    import scipy.sparse as sps
+    if sps.issparse(add_constant) or (not isinstance(add_constant, torch.Tensor) and np.ndim(add_constant) == 2):
+        A = sps.coo_matrix(add_constant)
+    elif isinstance(add_constant, torch.Tensor) and add_constant.ndim == 2:
+        A = sps.coo_matrix(add_constant.detach().cpu().numpy())
+    else:
+        return _diagonal_constant(add_constant, n), None
+    if A.shape != (n, n):
+        raise ValueError(f"add_constant has shape {A.shape}, the operator {(n, n)}")
+    if np.iscomplexobj(A.data):
+        raise NotImplementedError("add_constant: complex constants are not supported")
+    A = A.tocsr()
+    A.sum_duplicates()
+    A = A.tocoo()
+    off = A.row != A.col
+    if not np.any(A.data[off] != 0):
+        return _diagonal_constant(A, n), None
+    scale = np.abs(A.data).max()
+    if abs(A - A.T).max() > 1e-12 * scale:
+        raise NotImplementedError("add_constant: the one-component operators take a symmetric constant")
+    nnx, nny = grid.nelx + 1, grid.nely + 1
+    r, c, v = A.row[off], A.col[off], A.data[off]
+    d = [c % nnx - r % nnx, (c // nnx) % nny - (r // nnx) % nny, c // (nnx * nny) - r // (nnx * nny)]
+    if any(np.abs(x).max() > 1 for x in d):
+        raise NotImplementedError("add_constant: an entry couples nodes that are not neighbours")
+    o = (d[2] + 1) * 9 + (d[1] + 1) * 3 + (d[0] + 1) if grid.dim == 3 else (d[1] + 1) * 3 + (d[0] + 1)
+    st = np.zeros((27 if grid.dim == 3 else 9, n))
+    np.add.at(st, (o, r), v)
+    on = ~off
+    diag = np.zeros(n)
+    np.add.at(diag, A.row[on], A.data[on])
+    return diag, st
+
+
 def _diagonal_constant(add_constant, n):
     """The diagonal (host FP64 vector of n) of AssembleGeneral's add_constant (pymoto/modules/assembly.py:294-295):
     a sparse or dense n x n matrix, or its diagonal as a vector; None for None.  The matrix-free operators add a
@@ -747,7 +790,19 @@ class _AssembleScalar(AssembleStiffness):
         self.bcdiagval = float(bcdiagval)
         self._mask_host = bc_node_mask(self.grid.nnodes, 1, self.bc)
         self._mask = None
-        self._set_constant(add_constant, scalar=True)
+        self._cdiag_host, self._cstencil_host = _stencil_constant(add_constant, self.grid)
+        self._cdiag = self._cstencil = None
+        if self._cstencil_host is not None and np.any(self._cstencil_host[:, self._mask_host != 0] != 0):
+            # LinSolve solves Dirichlet rows directly, which needs them (and, by symmetry, their columns) free of
+            # couplings
+            raise NotImplementedError("add_constant: off-diagonal entries on constrained nodes are not supported")
+
+    def cstencil(self, device):
+        if self._cstencil_host is None:
+            return None
+        if self._cstencil is None or self._cstencil.device != device:
+            self._cstencil = torch.from_numpy(self._cstencil_host).to(device)
+        return self._cstencil
 
     def __call__(self, x):
         xd, kind = _to_device(x)
@@ -755,7 +810,7 @@ class _AssembleScalar(AssembleStiffness):
             raise ValueError(f"Input vector wrong size ({xd.numel()}), must be equal to #nel ({self.grid.nel})")
         self._kind = kind
         return ScalarOperator.assemble(self.grid, xd, self.scalar_element, self.bcmask(xd.device), self.bcdiagval,
-                                       cdiag=self.cdiag(xd.device))
+                                       cdiag=self.cdiag(xd.device), cstencil=self.cstencil(xd.device))
 
     def _sensitivity(self, dgdmat):
         if dgdmat is None or getattr(dgdmat, "size", 1) <= 0:

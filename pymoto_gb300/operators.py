@@ -516,13 +516,14 @@ class ScalarOperator:
 
     ncomp = 1
 
-    def __init__(self, grid, S, code, bcmask=None, bcdiag=0.0, cdiag=None, xe=None, P0=None):
+    def __init__(self, grid, S, code, bcmask=None, bcdiag=0.0, cdiag=None, xe=None, P0=None, cstencil=None):
         self.grid = grid
         self.S = S
         self.code = code
         self.bcmask = bcmask
         self.bcdiag = float(bcdiag)
         self.cdiag64 = cdiag       # FP64 device vector per node (level 0), or None
+        self.cstencil = cstencil   # FP64 device stencil (offsets x nodes) of a constant's off-diagonal entries
         self.xe = xe               # FP64 element scaling of a level-0 operator (None on coarse levels)
         self.P0 = None if P0 is None else np.ascontiguousarray(P0, dtype=np.float64)
         self._variants = {code: self}
@@ -530,10 +531,11 @@ class ScalarOperator:
         self.persistent = False
 
     @classmethod
-    def assemble(cls, grid, xe, P0, bcmask, bcdiag, cdiag=None, code=F64):
-        """Level-0 operator of element scaling xe (FP64 device vector)."""
+    def assemble(cls, grid, xe, P0, bcmask, bcdiag, cdiag=None, code=F64, cstencil=None):
+        """Level-0 operator of element scaling xe (FP64 device vector); cdiag / cstencil: the diagonal and the
+        neighbour couplings (FP64 stencil layout) of a constant added after the Dirichlet rows."""
         S = torch.empty((scalar_stencil_offsets(grid.dim), grid.nnodes), dtype=TORCH_DTYPE[code], device=xe.device)
-        op = cls(grid, S, code, bcmask, bcdiag, cdiag, xe, P0)
+        op = cls(grid, S, code, bcmask, bcdiag, cdiag, xe, P0, cstencil)
         return op.recompute()
 
     def recompute(self):
@@ -541,6 +543,11 @@ class ScalarOperator:
         g = self.grid
         call("pmg_scalar_stencil", self.code, g.nelx, g.nely, g.nelz, self.xe, self.P0, self.bcmask, self.bcdiag,
              self.cdiag64, self.S, stream())
+        if self.cstencil is not None:
+            c = self.cstencil if self.code == F64 else self.cstencil.to(self.torch_dtype)
+            if getattr(self, "_one", None) is None or self._one.device != self.S.device:
+                self._one = torch.ones(1, dtype=torch.float64, device=self.S.device)
+            call("pmg_axpy_ratio", self.code, self.S.numel(), self.S, c, self._one, self._one, 1.0, stream())
         return self
 
     @classmethod
@@ -548,7 +555,7 @@ class ScalarOperator:
         """An operator with its own stencil buffer (precision `code`) for the grid and BCs of `other`, refreshed in
         place with assign() (stable device addresses for captured CUDA graphs)."""
         S = torch.empty(other.S.shape, dtype=TORCH_DTYPE[code], device=other.device)
-        op = cls(other.grid, S, code, other.bcmask, other.bcdiag, other.cdiag64, other.xe, other.P0)
+        op = cls(other.grid, S, code, other.bcmask, other.bcdiag, other.cdiag64, other.xe, other.P0, other.cstencil)
         op.persistent = True
         return op
 
@@ -560,6 +567,7 @@ class ScalarOperator:
             raise ValueError("assign: grid mismatch")
         call("pmg_convert", other.code, self.code, other.S.numel(), other.S, self.S, 1.0, stream())
         self.bcmask, self.bcdiag, self.xe, self.P0 = other.bcmask, other.bcdiag, other.xe, other.P0
+        self.cstencil = other.cstencil
         if other.cdiag64 is not self.cdiag64:
             self.cdiag64, self._cdiag = other.cdiag64, None
         return self

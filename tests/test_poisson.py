@@ -109,3 +109,47 @@ def test_one_component_host_layout(shp):
     assert np.flatnonzero(m).tolist() == nodes.tolist() and m.max() == 1
     with pytest.raises(IndexError):
         bc_node_mask(og.nnodes, 1, [og.nnodes])
+
+
+def _neighbour_constant(og, a=0.3):
+    """A symmetric constant coupling x-neighbours in the right half of the grid (a convection-like term)."""
+    rows, cols, vals = [], [], []
+    for k in range(og.nelz + 1):
+        for j in range(og.nely + 1):
+            for i in range(og.nelx // 2, og.nelx):
+                n = int(og.node_number(i, j, k))
+                rows += [n, n + 1, n, n + 1]
+                cols += [n, n + 1, n + 1, n]
+                vals += [a, a, -a, -a]
+    return sps.coo_matrix((vals, (rows, cols)), shape=(og.nnodes, og.nnodes)).tocsr()
+
+
+@pytest.mark.parametrize("shp", [(8, 6, 4), (8, 6, 0)])
+def test_neighbour_coupling_constant_in_stencil_layout(shp):
+    """add_constant of a one-component operator: its diagonal and its neighbour couplings in the node-stencil
+    layout reproduce the matrix; couplings beyond the neighbours, non-symmetric constants and couplings of
+    constrained nodes are refused."""
+    from pymoto_gb300.modules import _stencil_constant
+    from pymoto_gb300.operators import Grid
+    og = O.Grid(*shp)
+    g = Grid(*shp)
+    C = _neighbour_constant(og)
+    diag, st = _stencil_constant(C, g)
+    dense = np.diag(diag)
+    for o in range(st.shape[0]):
+        dx, dy, dz = o % 3 - 1, (o // 3) % 3 - 1, (o // 9 - 1 if g.dim == 3 else 0)
+        for n in np.flatnonzero(st[o]):
+            dense[n, n + dx + dy * (og.nelx + 1) + dz * (og.nelx + 1) * (og.nely + 1)] += st[o, n]
+    np.testing.assert_array_equal(dense, C.toarray())
+    diag2, st2 = _stencil_constant(sps.diags(np.arange(og.nnodes, dtype=float)), g)
+    assert st2 is None and np.array_equal(diag2, np.arange(og.nnodes))
+    far = sps.coo_matrix(([1.0, 1.0], ([0, 2], [2, 0])), shape=(og.nnodes, og.nnodes))
+    with pytest.raises(NotImplementedError):
+        _stencil_constant(far, g)
+    skew = sps.coo_matrix(([1.0], ([0], [1])), shape=(og.nnodes, og.nnodes))
+    with pytest.raises(NotImplementedError):
+        _stencil_constant(skew, g)
+    d = pg.VoxelDomain(*shp)
+    pg.AssemblePoisson(d, bc=og.nodes_where(i=0), add_constant=C)
+    with pytest.raises(NotImplementedError):
+        pg.AssemblePoisson(d, bc=og.nodes_where(i=og.nelx), add_constant=C)

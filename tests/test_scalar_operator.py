@@ -244,3 +244,32 @@ def test_galerkin_and_vcycle_match_pymotos_multigrid(tag, golden):
     mgs[0].update(P)
     z = mgs[0].solve(torch.from_numpy(g[f"{tag}_r"]).cuda()).cpu().numpy()
     np.testing.assert_allclose(z, g[f"{tag}_z"], rtol=0, atol=1e-11 * np.abs(g[f"{tag}_z"]).max())
+
+
+@pytest.mark.gpu
+def test_poisson_with_a_neighbour_coupling_constant():
+    """A constant with off-diagonal entries between neighbouring nodes (add_constant, assembly.py:294-295) enters
+    the one-component stencils exactly: the operator, the multigrid solve and the sensitivities against the
+    oracle's P(x) + C."""
+    from test_poisson import _neighbour_constant
+    og, x, nodes, f = _thermal_case((8, 6, 4))
+    d = pg.VoxelDomain(8, 6, 4)
+    P0 = element_poisson(d, 1.0)
+    C = _neighbour_constant(og)
+    A = (O.assemble(og, P0, x, bc=nodes, bcdiagval=float(P0.max()), ndof=1) + C).tocsc()
+    ref = spla.spsolve(A, f)
+    sx = pg.Signal("x", torch.from_numpy(x).cuda())
+    fd = torch.from_numpy(f).cuda()
+    with pg.Network() as fn:
+        sK = pg.AssemblePoisson(d, bc=nodes, add_constant=C)(sx)
+        su = pg.LinSolve(hermitian=True, symmetric=True)(sK, fd)
+        sc = pg.EinSum("i,i->")(su, fd)
+    np.testing.assert_allclose(sK.state.to_dense().cpu().numpy(), A.toarray(), rtol=0, atol=1e-13 * abs(A).max())
+    np.testing.assert_allclose(su.state.cpu().numpy(), ref, rtol=0, atol=1e-9 * np.abs(ref).max())
+    fn.reset()
+    sc.sensitivity = 1.0
+    fn.sensitivity()
+    dref = O.sensitivity_contract(og, P0, [-ref], [ref], bc=nodes, ndof=1)
+    np.testing.assert_allclose(sx.sensitivity.cpu().numpy(), dref, rtol=0, atol=1e-8 * np.abs(dref).max())
+    K32 = sK.state.astype(F32)
+    np.testing.assert_allclose(K32.to_dense().cpu().numpy(), A.toarray(), rtol=0, atol=2e-6 * abs(A).max())
