@@ -153,3 +153,21 @@ def test_neighbour_coupling_constant_in_stencil_layout(shp):
     pg.AssemblePoisson(d, bc=og.nodes_where(i=0), add_constant=C)
     with pytest.raises(NotImplementedError):
         pg.AssemblePoisson(d, bc=og.nodes_where(i=og.nelx), add_constant=C)
+
+
+def test_constant_inputs_of_one_component_operators():
+    """add_constant as a sparse matrix, a dense matrix or a diagonal vector gives the same stencil layout."""
+    from pymoto_gb300.modules import _stencil_constant
+    from pymoto_gb300.operators import Grid
+    og, g = O.Grid(6, 4, 2), Grid(6, 4, 2)
+    C = _neighbour_constant(og) + sps.diags(np.linspace(0.1, 1.0, og.nnodes))
+    d1, s1 = _stencil_constant(C, g)
+    d2, s2 = _stencil_constant(C.toarray(), g)
+    np.testing.assert_array_equal(d1, d2)
+    np.testing.assert_array_equal(s1, s2)
+    d3, s3 = _stencil_constant(np.linspace(0.1, 1.0, og.nnodes), g)
+    assert s3 is None
+    np.testing.assert_array_equal(d3, np.linspace(0.1, 1.0, og.nnodes))
+    assert _stencil_constant(None, g) == (None, None)
+    with pytest.raises(ValueError):
+        _stencil_constant(sps.eye(og.nnodes + 1), g)
