@@ -171,3 +171,12 @@ def test_constant_inputs_of_one_component_operators():
     assert _stencil_constant(None, g) == (None, None)
     with pytest.raises(ValueError):
         _stencil_constant(sps.eye(og.nnodes + 1), g)
+
+
+def test_learned_warm_start_refuses_one_component_operators():
+    """The learned warm start predicts displacement fields: a mixed solver with one refuses a one-component
+    operator before touching the device."""
+    from pymoto_gb300.operators import Grid, ScalarOperator
+    solver = pg.MixedPrecisionCG(warm_start=object())
+    with pytest.raises(NotImplementedError):
+        solver.update(ScalarOperator(Grid(4, 4, 4), None, 0))
