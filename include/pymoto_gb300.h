@@ -160,6 +160,9 @@ int pmg_operator_status(int reset);
  * unknown kind.  Process-wide: select before launching, not while another thread launches operator products. */
 enum { PMG_OPERATOR_FMA = 0, PMG_OPERATOR_TCGEN05 = 1 };
 int pmg_set_operator_kernel(int kind);
+/* Host only: the launch plan of the CUDA-core FP32 3D operator for a grid and a number of resident CTA slots
+ * (CTAs per SM x SMs): plan_host[0..4] = tile width OX and height OY in node columns, tiles in x and y, z chunks. */
+int pmg_operator_plan(int nelx, int nely, int nelz, int slots, int* plan_host);
 /* Step `step`: d = a d + c r / diag, x = x + d; init != 0 starts from x = 0 (d = x = c r / diag). */
 int pmg_cheb_step(int dtype, int64_t n, const void* r, const void* diag, void* d, void* x, const double* coef, int step,
                   int init, void* stream);

@@ -112,6 +112,7 @@ SIGNATURES = {
     "pmg_scalar_to_dense": (I, [I, I, I, I, P, P, P]),
     "pmg_scalar_rowabs": (I, [I, I, I, I, P, P, P]),
     "pmg_scalar_sens": (I, [I, I, I, P, P, P, P, D, I, P, P]),
+    "pmg_operator_plan": (I, [I, I, I, I, P]),
 }
 
 # Returns that are values, not statuses
@@ -172,7 +173,7 @@ _HOST_ONLY = {"pmg_version", "pmg_status_string", "pmg_last_error", "pmg_element
               "pmg_reduce_scratch_bytes", "pmg_oc_scratch_bytes", "pmg_stencil_bandwidth",
               "pmg_cholesky_inverse_f32_scratch_bytes", "pmg_nn_wgrad_scratch_bytes", "pmg_oc_status",
               "pmg_coarse_ordering", "pmg_oc_status_async", "pmg_mma_scratch_bytes", "pmg_operator_status",
-              "pmg_set_wait_test", "pmg_set_operator_kernel"}
+              "pmg_set_wait_test", "pmg_set_operator_kernel", "pmg_operator_plan"}
 
 
 def _launches(name, args):
@@ -184,8 +185,8 @@ def _launches(name, args):
         return 4
     if name == "pmg_galerkin_from_ebe":
         return 2 if args[9] is not None and int(args[10]) > 0 else 1
-    if name == "pmg_nn_conv3d_backward_weights":
-        return 2
+    if name in ("pmg_nn_conv3d_backward_weights", "pmg_scalar_galerkin"):
+        return 2          # weight partials + their sum; forward offsets + the mirrored backward ones
     if name == "pmg_mma_update":
         return 3          # reset, the cooperative solve, status
     if name == "pmg_oc_update":

@@ -420,3 +420,15 @@ int ebe_apply_fma_f32(int mode, Grid g, const float* xe, const double* K0, const
 }
 
 }  // namespace pmg
+
+extern "C" int pmg_operator_plan(int nelx, int nely, int nelz, int slots, int* plan_host) {
+  if (!pmg::grid_ok(nelx, nely, nelz) || nelz < 1 || slots < 1 || !plan_host) return PMG_BAD_ARG;
+  int OX = 1, OY = 1, tx = 1, ty = 1, nzc = 1;
+  pmg::fma_plan(pmg::Grid{nelx, nely, nelz}, slots, OX, OY, tx, ty, nzc);
+  plan_host[0] = OX;
+  plan_host[1] = OY;
+  plan_host[2] = tx;
+  plan_host[3] = ty;
+  plan_host[4] = nzc;
+  return PMG_OK;
+}

@@ -249,3 +249,26 @@ def test_c_caller_without_python(tmp_path):
     K0 = np.array([float(v) for v in fields["K0"].split()]).reshape(24, 24)
     np.testing.assert_array_equal(K0, element_stiffness(3))
     assert int(fields["bad_mode"]) == 1 and int(fields["bad_grid"]) == 1
+
+
+def test_operator_launch_plan_fits_the_kernel_limits():
+    """The CUDA-core operator's launch plan (tile, tiles, z chunks) respects the kernel's thread, staging and grid
+    limits and covers the node counts, for the bench grids and many others, without a GPU."""
+    from pymoto_gb300 import _lib
+    plan = np.zeros(5, dtype=np.int32)
+    _lib.call("pmg_operator_plan", 128, 64, 64, 304, plan)
+    assert plan.tolist() == [19, 13, 7, 5, 8]
+    rng = np.random.default_rng(5)
+    shapes = [(1, 1, 1), (2, 1, 1), (31, 1, 1), (32, 32, 32), (255, 3, 7), (256, 128, 128), (96, 48, 48),
+              (4000, 2, 3), (3, 4000, 2)] + [tuple(int(v) for v in rng.integers(1, 300, 3)) for _ in range(300)]
+    for nx, ny, nz in shapes:
+        for slots in (1, 152, 304, 456):
+            _lib.call("pmg_operator_plan", nx, ny, nz, slots, plan)
+            ox, oy, tx, ty, nzc = plan.tolist()
+            assert 1 <= ox <= 32 and 1 <= oy <= 32 and ox * oy <= 256, (nx, ny, nz, plan)
+            assert (ox + 2) * (oy + 2) <= 340 and (ox + 1) * (oy + 1) <= 297, (nx, ny, nz, plan)
+            assert tx * ox >= nx + 1 and (tx - 1) * ox < nx + 1, (nx, ny, nz, plan)
+            assert ty * oy >= ny + 1 and (ty - 1) * oy < ny + 1, (nx, ny, nz, plan)
+            assert 1 <= nzc <= min(nz + 1, 65535) and ty <= 65535, (nx, ny, nz, plan)
+    with pytest.raises(_lib.PMGError):
+        _lib.call("pmg_operator_plan", 8, 8, 0, 304, plan)
