@@ -13,8 +13,8 @@ from .core import HOST_RUNTIME, Module, Network, Signal
 from .domain import VoxelDomain
 from .modules import (AssembleMass, AssemblePoisson, AssembleStiffness, DensityFilter, DeviceDyad, EinSum, FilterConv, LinSolve, MathExpression,
                       SIMP, Scaling)
-from .operators import (Grid, StencilOperator, StiffnessOperator, element_stiffness, operator_kernel,
-                        set_operator_kernel)
+from .operators import (Grid, ScalarOperator, StencilOperator, StiffnessOperator, element_stiffness,
+                        operator_kernel, set_operator_kernel)
 from .optimizers import OC
 from .mma import MMA
 from .solvers import (CG, Chebyshev, DampedJacobi, DenseCholesky, GeometricMultigrid, LinearSolver,
@@ -29,7 +29,7 @@ from .routines import finite_difference, minimize_mma, minimize_oc
 __version__ = "0.1.0"
 
 __all__ = ["AssembleMass", "AssemblePoisson", "AssembleStiffness", "DensityFilter", "DeviceDyad", "EinSum", "FilterConv", "LinSolve", "MathExpression",
-           "SIMP", "Grid", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "Chebyshev", "DampedJacobi",
+           "SIMP", "Grid", "ScalarOperator", "StencilOperator", "StiffnessOperator", "element_stiffness", "OC", "CG", "Chebyshev", "DampedJacobi",
            "DenseCholesky", "GeometricMultigrid", "LinearSolver", "MixedPrecisionCG", "Preconditioner",
            "VoxelDomain", "Module", "Network", "Signal", "HOST_RUNTIME", "ComplianceObjective", "WriteToVTI", "Scaling",
            "MMA", "ScalarToFile", "finite_difference",

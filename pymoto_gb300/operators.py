@@ -3,8 +3,10 @@
 StiffnessOperator is what AssembleStiffness outputs in place of pyMOTO's CSR matrix
 (pymoto/modules/assembly.py:245-296): the matrix-free K(x) = sum_e x_e K0 with Dirichlet rows/columns
 replaced by `bcdiag` on the diagonal.  StencilOperator holds a Galerkin coarse operator R^T A R
-(pymoto/solvers/iterative.py:173) as element matrices plus assembled node stencils.  Both provide the
-matrix protocol the solvers use: shape, dtype, `@`, diagonal(), T, apply().
+(pymoto/solvers/iterative.py:173) as element matrices plus assembled node stencils.  ScalarOperator is the
+one-component operator of AssemblePoisson and AssembleMass(ndof=1) (pymoto/modules/assembly.py:466-560) on
+every level, as full node stencils.  All provide the matrix protocol the solvers use: shape, dtype, `@`,
+diagonal(), T, apply().
 """
 import numpy as np
 import torch
