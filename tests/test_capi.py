@@ -272,3 +272,16 @@ def test_operator_launch_plan_fits_the_kernel_limits():
             assert 1 <= nzc <= min(nz + 1, 65535) and ty <= 65535, (nx, ny, nz, plan)
     with pytest.raises(_lib.PMGError):
         _lib.call("pmg_operator_plan", 8, 8, 0, 304, plan)
+
+
+def test_every_called_entry_point_is_bound():
+    """Every C-ABI name the package, the bench and the entry points call through the binding is declared and
+    bound (a misspelt name would only fail on a GPU)."""
+    from pymoto_gb300 import _lib
+    files = glob.glob(os.path.join(ROOT, "pymoto_gb300", "*.py")) + [os.path.join(ROOT, "bench.py"),
+                                                                      os.path.join(ROOT, "__graft_entry__.py")]
+    called = set()
+    for path in files:
+        called |= set(re.findall(r"""call\(\s*["'](pmg_\w+)["']""", open(path).read()))
+    assert len(called) > 50
+    assert called <= set(_lib.SIGNATURES), sorted(called - set(_lib.SIGNATURES))
