@@ -88,3 +88,24 @@ def test_hierarchy_per_level_coarse_smoothing():
                                           smoother="chebyshev")
     assert [m.smooth_steps for m in mgs] == [1, 2, 3, 3]
     assert [m.smoother.degree for m in mgs] == [1, 2, 3, 3]
+
+
+def test_hierarchy_construction_without_a_gpu():
+    """Level count (given, or automatic down to max_coarse_dofs), sub-domains with doubled element sizes, the
+    lagged coarsest solve, and the errors for grids that do not halve."""
+    import pymoto_gb300 as pg
+    d = pg.VoxelDomain(128, 64, 64, 0.5, 0.5, 0.5)
+    mgs = pg.GeometricMultigrid.hierarchy(d, levels=5, smoother_w=0.6, smooth_steps=2, coarse_lag=True)
+    assert [m.grid.dims for m in mgs] == [(128, 64, 64), (64, 32, 32), (32, 16, 16), (16, 8, 8)]
+    assert all(m.inner_level is n for m, n in zip(mgs, mgs[1:]))
+    assert isinstance(mgs[-1].inner_level, pg.DenseCholesky) and mgs[-1].inner_level.lag
+    assert mgs[1].domain.unitx == 1.0 and mgs[3].sub_domain.unitx == 8.0
+    auto = pg.GeometricMultigrid.hierarchy(d, smoother_w=0.6, smooth_steps=2, max_coarse_dofs=3000)
+    coarsest = auto[-1].grid.coarse()
+    assert coarsest.ndof <= 3000 < auto[-1].grid.ndof
+    with pytest.raises(ValueError):
+        pg.GeometricMultigrid(pg.VoxelDomain(9, 4, 4))
+    with pytest.raises(ValueError):
+        pg.GeometricMultigrid.hierarchy(pg.VoxelDomain(12, 6, 6), levels=4)
+    with pytest.raises(ValueError):
+        pg.GeometricMultigrid.hierarchy(d, smoother="sor")
